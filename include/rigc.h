@@ -1,0 +1,209 @@
+/*
+ * rigc.h -- C ABI of the GB300 (sm_103a) Rigid IPC narrow phase.
+ *
+ * Every entry point is plain C: pointers, sizes and an int status.  Device
+ * pointers are CUDA global-memory addresses on the context's device; "host"
+ * in a name means host memory.  All work is ordered on the context's stream
+ * (rigc_set_stream); an entry point synchronises only when it returns a value
+ * in host memory.  No exception crosses this boundary.
+ *
+ * Paths below are relative to the rigid-ipc source tree (ipc-sim/rigid-ipc).
+ * Each entry point names the reference interface it replaces.
+ */
+#ifndef RIGC_H
+#define RIGC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes (the reference returns bool / infinity / throws; see
+ * src/opt/distance_barrier_constraint.cpp:263-264, src/ccd/ccd.cpp:217) */
+#define RIGC_OK 0
+#define RIGC_ERR_ARG 1            /* invalid argument                         */
+#define RIGC_ERR_CUDA 2           /* CUDA runtime error                       */
+#define RIGC_ERR_OOM 3            /* device allocation failed                 */
+#define RIGC_ERR_QUEUE_OVERFLOW 4 /* CCD box stack overflowed (result kept
+                                     conservative)                            */
+#define RIGC_ERR_ITER_LIMIT 5     /* CCD box budget exhausted (result kept
+                                     conservative)                            */
+#define RIGC_ERR_NAN 6            /* non-finite pose input                    */
+
+/* body types (src/physics/rigid_body.hpp RigidBodyType) */
+#define RIGC_BODY_STATIC 0
+#define RIGC_BODY_KINEMATIC 1
+#define RIGC_BODY_DYNAMIC 2
+
+/* rigc_barrier_term flags (compute_grad / compute_hess of
+ * DistanceBarrierRBProblem::compute_barrier_term) */
+#define RIGC_GRAD 1
+#define RIGC_HESS 2
+#define RIGC_PROJECT_PSD 4 /* project each 12x12 pair Hessian to PSD       */
+
+/* rigc_earliest_toi flags */
+#define RIGC_TOI_NO_PRUNE 1 /* search every candidate in full (per-candidate
+                               times of impact become exact, slower)         */
+
+typedef struct rigc_ctx rigc_ctx;
+
+/* Flattened rigid bodies, as RigidBodyAssembler::init builds them
+ * (src/physics/rigid_body_assembler.cpp:19-118).  Host pointers; copied. */
+typedef struct rigc_scene_desc {
+    int32_t num_bodies;
+    int32_t num_vertices;
+    int32_t num_edges;
+    int32_t num_faces;
+    const double* rest_vertices;     /* num_vertices x 3, body frame         */
+    const int32_t* edges;            /* num_edges x 2, global vertex ids     */
+    const int32_t* faces;            /* num_faces x 3, global vertex ids     */
+    const int32_t* faces_to_edges;   /* num_faces x 3, edge (j, j+1 mod 3)   */
+    const int32_t* body_vertex_start;/* num_bodies + 1                       */
+    const int32_t* body_edge_start;  /* num_bodies + 1                       */
+    const int32_t* body_face_start;  /* num_bodies + 1                       */
+    const int32_t* group_ids;        /* num_bodies                           */
+    const int32_t* body_types;       /* num_bodies, RIGC_BODY_*              */
+    const double* r_max;             /* num_bodies, max rest vertex norm     */
+    double average_edge_length;
+} rigc_scene_desc;
+
+/* Candidate pairs (ipc-toolkit Candidates as filled by
+ * src/ccd/rigid/broad_phase.cpp:166-204).  Device pointers owned by the
+ * context, valid until the next call that writes candidates.  Pairs are
+ * sorted and unique: ee = (edge0 < edge1), fv = (face, vertex). */
+typedef struct rigc_candidates {
+    int64_t num_ee;
+    int64_t num_fv;
+    const int32_t* ee; /* num_ee x 2 */
+    const int32_t* fv; /* num_fv x 2 */
+} rigc_candidates;
+
+/* Constraint set (ipc-toolkit Constraints: vv | ev | ee | fv, built by
+ * DistanceBarrierConstraint::construct_constraint_set,
+ * src/opt/distance_barrier_constraint.cpp:267-306).  Device pointers owned by
+ * the context. type: 0 VV, 1 EV, 2 EE, 3 FV; verts in ipc-toolkit
+ * vertex_indices order (-1 unused); prims = VV (v0, v1), EV (edge, vertex),
+ * EE (edge0, edge1), FV (face, vertex); bodies = (local body 0, 1). */
+typedef struct rigc_constraints {
+    int64_t num;
+    int64_t num_vv, num_ev, num_ee, num_fv;
+    const int32_t* type;   /* num          */
+    const int32_t* verts;  /* num x 4      */
+    const int32_t* prims;  /* num x 2      */
+    const int32_t* bodies; /* num x 2      */
+    const double* weight;  /* num, multiplicity */
+    const double* eps_x;   /* num, EE mollifier threshold */
+} rigc_constraints;
+
+/* Barrier term: energy (host), gradient (device, 6 per body) and the Hessian
+ * as block-sparse rows of 6x6 row-major blocks (device). */
+typedef struct rigc_barrier_out {
+    double energy;
+    int64_t nnzb;
+    const double* grad;      /* 6 * num_bodies         */
+    const int32_t* row_ptr;  /* num_bodies + 1         */
+    const int32_t* col;      /* nnzb, sorted per row   */
+    const double* val;       /* nnzb x 36              */
+} rigc_barrier_out;
+
+/* Counters of the last calls (for measurement). */
+typedef struct rigc_stats {
+    int64_t ccd_boxes;        /* boxes evaluated by the last earliest-toi    */
+    int64_t ccd_candidates;   /* candidates of the last earliest-toi         */
+    int64_t ccd_collisions;   /* candidates with an impact                   */
+    int64_t grid_items;       /* hash-grid (cell, element) items             */
+    int64_t large_elements;   /* elements tested outside the grid            */
+    int64_t cand_ee;          /* current candidates (last broad phase)       */
+    int64_t cand_fv;
+    int32_t last_status;
+} rigc_stats;
+
+/* ---- context (replaces the RigidBodyAssembler set-up,
+ *      src/physics/rigid_body_assembler.cpp:19-118) ---- */
+int rigc_ctx_create(const rigc_scene_desc* desc, rigc_ctx** out);
+int rigc_ctx_destroy(rigc_ctx* ctx);
+int rigc_set_stream(rigc_ctx* ctx, void* cuda_stream);
+const char* rigc_status_string(int status);
+int rigc_get_stats(const rigc_ctx* ctx, rigc_stats* out);
+
+/* Copy bytes between any two addresses the device can see (host, pinned or
+ * device; cudaMemcpyDefault) on the context's stream, then synchronise.  For
+ * FFI callers without CUDA bindings. */
+int rigc_copy(rigc_ctx* ctx, void* dst, const void* src, size_t bytes);
+
+/* World vertices V = R(theta) v + p for all vertices (device in/out).
+ * Replaces RigidBodyAssembler::world_vertices
+ * (src/physics/rigid_body_assembler.cpp:191-202). */
+int rigc_world_vertices(rigc_ctx* ctx, const double* x, double* V);
+
+/* ---- broad phase: detect_collision_candidates_rigid with
+ * DetectionMethod::HASH_GRID (src/ccd/rigid/broad_phase.hpp:52-59,
+ * broad_phase.cpp:19-91 discrete, :127-204 continuous).  x0, x1: device,
+ * 6 * num_bodies doubles [p, theta] per body.  continuous = 0 ignores x1. */
+int rigc_detect_candidates(rigc_ctx* ctx, const double* x0, const double* x1,
+                           int continuous, double inflation_radius,
+                           rigc_candidates* out);
+
+/* ---- narrow phase CCD: compute_earliest_toi_narrow_phase
+ * (src/opt/distance_barrier_constraint.cpp:151-265) over the candidates of
+ * the last rigc_detect_candidates call, trajectory RIGID
+ * (src/ccd/rigid/time_of_impact.cpp:158-310).  Every candidate searches
+ * t in [0, 1]; *toi_host = INFINITY when nothing collides.  per_candidate
+ * (device, optional, num_ee + num_fv doubles, ee first). */
+int rigc_earliest_toi(rigc_ctx* ctx, const double* x0, const double* x1,
+                      double toi_tolerance, int flags, double* toi_host,
+                      double* per_candidate);
+
+/* DistanceBarrierConstraint::compute_earliest_toi
+ * (src/opt/distance_barrier_constraint.cpp:130-149): continuous broad phase
+ * with inflation dmin / 2, then the narrow phase. */
+int rigc_compute_earliest_toi(rigc_ctx* ctx, const double* x0,
+                              const double* x1, double dmin,
+                              double* toi_host);
+
+/* ---- constraint set: DistanceBarrierConstraint::construct_constraint_set
+ * (src/opt/distance_barrier_constraint.cpp:267-306): discrete broad phase
+ * with inflation (dhat + dmin) / 2, then ipc::construct_constraint_set. */
+int rigc_construct_constraint_set(rigc_ctx* ctx, const double* x, double dhat,
+                                  double dmin, rigc_constraints* out);
+
+/* Replace the context's constraint set with host arrays (same layout as
+ * rigc_constraints). */
+int rigc_set_constraints(rigc_ctx* ctx, int64_t num, const int32_t* type,
+                         const int32_t* verts, const int32_t* prims,
+                         const int32_t* bodies, const double* weight,
+                         const double* eps_x);
+
+/* ---- barrier term: DistanceBarrierRBProblem::compute_barrier_term
+ * (src/problems/distance_barrier_rb_problem.hpp:267-273, .cpp:1299-1399)
+ * over the context's constraint set. */
+int rigc_barrier_term(rigc_ctx* ctx, const double* x, double dhat, double dmin,
+                      int flags, rigc_barrier_out* out);
+
+/* Per-constraint energy, body-space gradient (12) and 12x12 Hessian before
+ * assembly (apply_chain_rule, distance_barrier_rb_problem.cpp:1182-1248).
+ * Device outputs; any may be NULL. */
+int rigc_barrier_local_terms(rigc_ctx* ctx, const double* x, double dhat,
+                             double dmin, int flags, double* energy,
+                             double* grad, double* hess);
+
+/* ---- one narrow-phase pass from host memory (the call a host Newton loop
+ * makes per iteration): copies x0/x1 in, runs compute_earliest_toi(x0, x1)
+ * and construct_constraint_set + compute_barrier_term at x0, copies the
+ * gradient and the block-sparse Hessian out.  Host buffers: grad_host
+ * (6 * num_bodies), row_ptr_host (num_bodies + 1), col_host / val_host of
+ * capacity nnzb_cap blocks (nnzb always written). */
+int rigc_narrow_phase_host(rigc_ctx* ctx, const double* x0_host,
+                           const double* x1_host, double dhat, double dmin,
+                           double* toi_host, double* energy_host,
+                           double* grad_host, int32_t* row_ptr_host,
+                           int32_t* col_host, double* val_host,
+                           int64_t nnzb_cap, int64_t* nnzb_host);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RIGC_H */

@@ -1,0 +1,343 @@
+// C entry points of the oracle for the Python test harness (test
+// infrastructure only; never linked into the product library).
+#include "interval.hpp"
+#include "oracle.hpp"
+
+#include <cstring>
+#include <memory>
+
+using namespace orc;
+
+namespace orc {
+I isinc(const I& x);
+void irotation(const I r[3], I R[9]);
+}
+
+namespace {
+struct OwnedScene {
+    Scene s;
+    std::vector<double> rest, rmax;
+    std::vector<int> edges, faces, f2e, bvs, bes, bfs, group, type;
+};
+
+std::vector<Constraint> unpack_constraints(
+    long long n, const int* types, const int* verts, const int* prims,
+    const int* bodies, const double* weight, const double* eps)
+{
+    std::vector<Constraint> cs(n);
+    for (long long i = 0; i < n; i++) {
+        Constraint& c = cs[i];
+        c.type = types[i];
+        for (int k = 0; k < 4; k++) c.v[k] = verts[4 * i + k];
+        c.prim[0] = prims[2 * i];
+        c.prim[1] = prims[2 * i + 1];
+        c.body[0] = bodies[2 * i];
+        c.body[1] = bodies[2 * i + 1];
+        c.weight = weight[i];
+        c.eps_x = eps[i];
+    }
+    return cs;
+}
+
+Candidates pack_candidates(const int* ee, long long nee, const int* fv, long long nfv)
+{
+    Candidates c;
+    c.ee.resize(nee);
+    c.fv.resize(nfv);
+    for (long long i = 0; i < nee; i++) c.ee[i] = { ee[2 * i], ee[2 * i + 1] };
+    for (long long i = 0; i < nfv; i++) c.fv[i] = { fv[2 * i], fv[2 * i + 1] };
+    return c;
+}
+} // namespace
+
+extern "C" {
+
+void* orc_scene_new(
+    int nb, int nv, int ne, int nf, const double* rest, const int* edges,
+    const int* faces, const int* f2e, const int* bvs, const int* bes,
+    const int* bfs, const int* group, const int* type, const double* rmax,
+    double avg_edge_len)
+{
+    auto* o = new OwnedScene;
+    o->rest.assign(rest, rest + 3 * nv);
+    o->edges.assign(edges, edges + 2 * ne);
+    o->faces.assign(faces, faces + 3 * nf);
+    o->f2e.assign(f2e, f2e + 3 * nf);
+    o->bvs.assign(bvs, bvs + nb + 1);
+    o->bes.assign(bes, bes + nb + 1);
+    o->bfs.assign(bfs, bfs + nb + 1);
+    o->group.assign(group, group + nb);
+    o->type.assign(type, type + nb);
+    o->rmax.assign(rmax, rmax + nb);
+    Scene& s = o->s;
+    s.nb = nb;
+    s.nv = nv;
+    s.ne = ne;
+    s.nf = nf;
+    s.rest = o->rest.data();
+    s.edges = o->edges.data();
+    s.faces = o->faces.data();
+    s.f2e = o->f2e.data();
+    s.bvs = o->bvs.data();
+    s.bes = o->bes.data();
+    s.bfs = o->bfs.data();
+    s.group = o->group.data();
+    s.type = o->type.data();
+    s.rmax = o->rmax.data();
+    s.avg_edge_len = avg_edge_len;
+    s.finalize();
+    return o;
+}
+
+void orc_scene_free(void* p) { delete static_cast<OwnedScene*>(p); }
+
+void orc_rotation_matrix(const double* theta, double* R) { rotation_matrix(theta, R); }
+
+void orc_world_vertices(void* p, const double* x, double* V)
+{
+    std::vector<double> v;
+    world_vertices(static_cast<OwnedScene*>(p)->s, x, v);
+    std::memcpy(V, v.data(), v.size() * sizeof(double));
+}
+
+void orc_world_vertices_diff(void* p, const double* x, double* V, double* dV, double* d2V)
+{
+    std::vector<double> v, d, dd;
+    world_vertices_diff(static_cast<OwnedScene*>(p)->s, x, v, d, dd);
+    std::memcpy(V, v.data(), v.size() * sizeof(double));
+    std::memcpy(dV, d.data(), d.size() * sizeof(double));
+    std::memcpy(d2V, dd.data(), dd.size() * sizeof(double));
+}
+
+int orc_point_triangle_distance_type(const double* p, const double* t0, const double* t1, const double* t2)
+{
+    return point_triangle_distance_type(p, t0, t1, t2);
+}
+
+int orc_edge_edge_distance_type(const double* a0, const double* a1, const double* b0, const double* b1)
+{
+    return edge_edge_distance_type(a0, a1, b0, b1);
+}
+
+double orc_barrier(double d, double s) { return barrier(d, s); }
+
+void orc_project_to_psd(int n, const double* A, double* out) { project_to_psd(n, A, out); }
+
+// candidates: returns 0 and fills when capacities suffice, else 1 (counts set)
+int orc_detect_candidates(
+    void* p, const double* x0, const double* x1, int continuous,
+    double inflation, int brute, int* ee, long long ee_cap, int* fv,
+    long long fv_cap, long long* n_ee, long long* n_fv)
+{
+    Candidates c;
+    detect_candidates(static_cast<OwnedScene*>(p)->s, x0, x1, continuous != 0,
+                      inflation, brute != 0, c);
+    *n_ee = (long long)c.ee.size();
+    *n_fv = (long long)c.fv.size();
+    if (*n_ee > ee_cap || *n_fv > fv_cap) return 1;
+    for (size_t i = 0; i < c.ee.size(); i++) {
+        ee[2 * i] = c.ee[i][0];
+        ee[2 * i + 1] = c.ee[i][1];
+    }
+    for (size_t i = 0; i < c.fv.size(); i++) {
+        fv[2 * i] = c.fv[i][0];
+        fv[2 * i + 1] = c.fv[i][1];
+    }
+    return 0;
+}
+
+long long orc_close_bodies(void* p, const double* x0, const double* x1,
+                           double inflation, int* out, long long cap)
+{
+    auto pairs = close_bodies(static_cast<OwnedScene*>(p)->s, x0, x1, inflation);
+    for (size_t i = 0; i < pairs.size() && (long long)i < cap; i++) {
+        out[2 * i] = pairs[i][0];
+        out[2 * i + 1] = pairs[i][1];
+    }
+    return (long long)pairs.size();
+}
+
+// element boxes (lo, hi per element; included flags)
+void orc_element_aabbs(
+    void* p, const double* x0, const double* x1, int continuous,
+    double inflation, double* vbox, double* ebox, double* fbox, char* vin,
+    char* ein, char* fin)
+{
+    const Scene& s = static_cast<OwnedScene*>(p)->s;
+    auto pairs = close_bodies(s, x0, continuous ? x1 : x0, inflation);
+    std::vector<AABB> vb, eb, fb;
+    std::vector<char> vi, ei, fi;
+    element_aabbs(s, x0, x1, continuous != 0, inflation, pairs, vb, eb, fb, vi, ei, fi);
+    for (int i = 0; i < s.nv; i++) {
+        std::memcpy(vbox + 6 * i, vb[i].lo, 3 * sizeof(double));
+        std::memcpy(vbox + 6 * i + 3, vb[i].hi, 3 * sizeof(double));
+        vin[i] = vi[i];
+    }
+    for (int i = 0; i < s.ne; i++) {
+        std::memcpy(ebox + 6 * i, eb[i].lo, 3 * sizeof(double));
+        std::memcpy(ebox + 6 * i + 3, eb[i].hi, 3 * sizeof(double));
+        ein[i] = ei[i];
+    }
+    for (int i = 0; i < s.nf; i++) {
+        std::memcpy(fbox + 6 * i, fb[i].lo, 3 * sizeof(double));
+        std::memcpy(fbox + 6 * i + 3, fb[i].hi, 3 * sizeof(double));
+        fin[i] = fi[i];
+    }
+}
+
+int orc_constraint_set(
+    void* p, const double* x, const int* ee, long long nee, const int* fv,
+    long long nfv, double dhat, double dmin, int* types, int* verts,
+    int* prims, int* bodies, double* weight, double* eps, long long cap,
+    long long* n_out)
+{
+    const Scene& s = static_cast<OwnedScene*>(p)->s;
+    std::vector<double> V;
+    world_vertices(s, x, V);
+    std::vector<Constraint> cs;
+    construct_constraint_set(s, pack_candidates(ee, nee, fv, nfv), V, dhat, dmin, cs);
+    *n_out = (long long)cs.size();
+    if (*n_out > cap) return 1;
+    for (size_t i = 0; i < cs.size(); i++) {
+        types[i] = cs[i].type;
+        for (int k = 0; k < 4; k++) verts[4 * i + k] = cs[i].v[k];
+        prims[2 * i] = cs[i].prim[0];
+        prims[2 * i + 1] = cs[i].prim[1];
+        bodies[2 * i] = cs[i].body[0];
+        bodies[2 * i + 1] = cs[i].body[1];
+        weight[i] = cs[i].weight;
+        eps[i] = cs[i].eps_x;
+    }
+    return 0;
+}
+
+void orc_local_terms(
+    void* p, const double* x, long long n, const int* types, const int* verts,
+    const int* prims, const int* bodies, const double* weight,
+    const double* eps, double dhat, double dmin, int project, double* energy,
+    double* grad, double* hess)
+{
+    const Scene& s = static_cast<OwnedScene*>(p)->s;
+    auto cs = unpack_constraints(n, types, verts, prims, bodies, weight, eps);
+    std::vector<double> V, dV, d2V;
+    world_vertices_diff(s, x, V, dV, d2V);
+    for (long long i = 0; i < n; i++) {
+        LocalTerm t;
+        constraint_local_term(s, cs[i], V, dV, d2V, dhat, dmin, project != 0, t);
+        energy[i] = t.energy;
+        std::memcpy(grad + 12 * i, t.grad, 12 * sizeof(double));
+        std::memcpy(hess + 144 * i, t.hess, 144 * sizeof(double));
+    }
+}
+
+// assembled barrier term; returns 1 when the block capacity is too small
+int orc_barrier_term(
+    void* p, const double* x, long long n, const int* types, const int* verts,
+    const int* prims, const int* bodies, const double* weight,
+    const double* eps, double dhat, double dmin, int project, double* energy,
+    double* grad, int* row_ptr, int* col, double* val, long long cap,
+    long long* nnzb)
+{
+    const Scene& s = static_cast<OwnedScene*>(p)->s;
+    auto cs = unpack_constraints(n, types, verts, prims, bodies, weight, eps);
+    std::vector<double> g;
+    BSR h;
+    *energy = barrier_term(s, x, cs, dhat, dmin, g, h, project != 0);
+    std::memcpy(grad, g.data(), g.size() * sizeof(double));
+    *nnzb = (long long)h.col.size();
+    if (*nnzb > cap) return 1;
+    std::memcpy(row_ptr, h.row_ptr.data(), h.row_ptr.size() * sizeof(int));
+    std::memcpy(col, h.col.data(), h.col.size() * sizeof(int));
+    std::memcpy(val, h.val.data(), h.val.size() * sizeof(double));
+    return 0;
+}
+
+double orc_body_energy(
+    double mass, const double* moment, const double* pose_t0,
+    const double* vel_t0, const double* Qdot, const int* fixed, int type,
+    const double* x6, const double* gravity, double h, double* grad,
+    double* hess)
+{
+    BodyState b;
+    b.mass = mass;
+    for (int i = 0; i < 3; i++) b.moment[i] = moment[i];
+    for (int i = 0; i < 6; i++) {
+        b.pose_t0[i] = pose_t0[i];
+        b.vel_t0[i] = vel_t0[i];
+        b.fixed[i] = fixed[i] != 0;
+    }
+    for (int i = 0; i < 9; i++) b.Qdot[i] = Qdot[i];
+    b.type = type;
+    return body_energy(b, x6, gravity, h, grad, hess);
+}
+
+int orc_edge_edge_toi(void* p, const double* x0, const double* x1, int ea,
+                      int eb, double bound, double tol, double* toi,
+                      long long* boxes)
+{
+    CCDStats st;
+    bool hit = edge_edge_toi(static_cast<OwnedScene*>(p)->s, x0, x1, ea, eb, bound, tol, *toi, &st);
+    *boxes = st.boxes;
+    return hit ? 1 : 0;
+}
+
+int orc_face_vertex_toi(void* p, const double* x0, const double* x1, int f,
+                        int v, double bound, double tol, double* toi,
+                        long long* boxes)
+{
+    CCDStats st;
+    bool hit = face_vertex_toi(static_cast<OwnedScene*>(p)->s, x0, x1, f, v, bound, tol, *toi, &st);
+    *boxes = st.boxes;
+    return hit ? 1 : 0;
+}
+
+double orc_earliest_toi(
+    void* p, const double* x0, const double* x1, const int* ee, long long nee,
+    const int* fv, long long nfv, double tol, int nthreads, double* per,
+    long long* boxes)
+{
+    std::vector<double> tois;
+    CCDStats st;
+    double t = earliest_toi(static_cast<OwnedScene*>(p)->s, x0, x1,
+                            pack_candidates(ee, nee, fv, nfv), tol, nthreads,
+                            per ? &tois : nullptr, &st);
+    if (per) std::memcpy(per, tois.data(), tois.size() * sizeof(double));
+    if (boxes) *boxes = st.boxes;
+    return t;
+}
+
+// interval primitives: op 0 add, 1 sub, 2 mul, 3 div, 4 sqrt, 5 cos, 6 sin,
+// 7 sinc, 8 abs
+void orc_interval_op(int op, double al, double ah, double bl, double bh, double* out)
+{
+    I a(al, ah), b(bl, bh), r;
+    switch (op) {
+    case 0: r = a + b; break;
+    case 1: r = a - b; break;
+    case 2: r = a * b; break;
+    case 3: r = a / b; break;
+    case 4: r = isqrt(a); break;
+    case 5: r = icos(a); break;
+    case 6: r = isin(a); break;
+    case 7: r = isinc(a); break;
+    default: r = iabs(a); break;
+    }
+    out[0] = r.lo;
+    out[1] = r.hi;
+}
+
+void orc_interval_rotation(const double* rlo, const double* rhi, double* Rlo, double* Rhi)
+{
+    I r[3] = { I(rlo[0], rhi[0]), I(rlo[1], rhi[1]), I(rlo[2], rhi[2]) };
+    I R[9];
+    irotation(r, R);
+    for (int i = 0; i < 9; i++) {
+        Rlo[i] = R[i].lo;
+        Rhi[i] = R[i].hi;
+    }
+}
+
+double orc_det_sin(double x) { return det_sin(x); }
+double orc_det_cos(double x) { return det_cos(x); }
+
+} // extern "C"

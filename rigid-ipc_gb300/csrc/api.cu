@@ -1,0 +1,418 @@
+// C ABI of the rigc library (declared in include/rigc.h).
+#include <cmath>
+#include <cstring>
+#include <mutex>
+
+#include "common.cuh"
+
+namespace rigc {
+
+int detect_candidates(Ctx& c, const double* x0, const double* x1, bool continuous, double infl);
+int construct_constraints(Ctx& c, const double* x, double dhat, double dmin);
+int launch_barrier_local(Ctx& c, const double* x, double dhat, double dmin, int flags,
+                         double* energy, double* grad, double* blocks, double* hess);
+int assemble_barrier(Ctx& c, bool with_hess);
+int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flags,
+            double* toi_host, double* per);
+int compute_world_vertices_rn(Ctx& c, const double* x, double* V, DevBuf& rotbuf);
+int sum_f64(const double* in, int64_t n, double* out_dev, DevBuf& tmp, cudaStream_t stream);
+
+static thread_local std::string g_last_error;
+
+// broad phase, then record the candidate counts (also on an early exit)
+static int detect_and_count(Ctx& c, const double* x0, const double* x1, bool continuous,
+                            double infl)
+{
+    int st = detect_candidates(c, x0, x1, continuous, infl);
+    c.stats.cand_ee = c.cand.num_ee;
+    c.stats.cand_fv = c.cand.num_fv;
+    return st;
+}
+
+void set_error(int code, const char* what, const char* file, int line)
+{
+    char buf[512];
+    snprintf(buf, sizeof(buf), "rigc error %d: %s (%s:%d)", code, what, file, line);
+    g_last_error = buf;
+}
+
+Ctx* ctx_of(rigc_ctx* c) { return reinterpret_cast<Ctx*>(c); }
+
+template <class T> static int upload(T*& dst, const T* src, size_t n)
+{
+    if (n == 0) {
+        dst = nullptr;
+        return RIGC_OK;
+    }
+    RIGC_CUDA(cudaMalloc(&dst, n * sizeof(T)));
+    RIGC_CUDA(cudaMemcpy(dst, src, n * sizeof(T), cudaMemcpyHostToDevice));
+    return RIGC_OK;
+}
+
+static void free_scene(Scene& s)
+{
+    void* ptrs[] = { s.rest, s.edges, s.faces, s.f2e, s.bvs, s.bes, s.bfs, s.group,
+                     s.type, s.rmax, s.vbody, s.ebody, s.fbody, s.edge_len };
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+}
+
+static void release_all(Ctx* c)
+{
+    DevBuf* bufs[] = { &c->cand.ee, &c->cand.fv, &c->cons.type, &c->cons.verts, &c->cons.prims,
+                       &c->cons.bodies, &c->cons.weight, &c->cons.eps, &c->frames, &c->c_energy,
+                       &c->c_grad, &c->c_blocks, &c->grad, &c->row_ptr, &c->col, &c->val,
+                       &c->d_scalars, &c->body_box, &c->body_in, &c->vbox, &c->ebox, &c->fbox,
+                       &c->vin, &c->ein, &c->fin, &c->items_key, &c->items_val, &c->items_key2,
+                       &c->items_val2, &c->seg, &c->pair_out, &c->pair_key, &c->large_list,
+                       &c->x0_dev, &c->x1_dev };
+    for (DevBuf* b : bufs) b->release();
+    for (auto& b : c->scratch) b.release();
+    if (c->h_scalars) cudaFreeHost(c->h_scalars);
+    c->h_scalars = nullptr;
+    free_scene(c->s);
+}
+
+} // namespace rigc
+
+using namespace rigc;
+
+extern "C" {
+
+const char* rigc_status_string(int status)
+{
+    switch (status) {
+    case RIGC_OK: return "ok";
+    case RIGC_ERR_ARG: return "invalid argument";
+    case RIGC_ERR_CUDA: return g_last_error.empty() ? "CUDA error" : g_last_error.c_str();
+    case RIGC_ERR_OOM: return "device out of memory";
+    case RIGC_ERR_QUEUE_OVERFLOW: return "CCD box stack overflow (conservative result)";
+    case RIGC_ERR_ITER_LIMIT: return "CCD box budget exhausted (conservative result)";
+    case RIGC_ERR_NAN: return "non-finite input";
+    default: return "unknown status";
+    }
+}
+
+int rigc_ctx_create(const rigc_scene_desc* d, rigc_ctx** out)
+{
+    if (!d || !out) return RIGC_ERR_ARG;
+    *out = nullptr;
+    if (d->num_bodies < 0 || d->num_vertices < 0 || d->num_edges < 0 || d->num_faces < 0)
+        return RIGC_ERR_ARG;
+    if (d->num_bodies > 0 && (!d->body_vertex_start || !d->body_edge_start || !d->body_face_start
+                              || !d->group_ids || !d->body_types || !d->r_max))
+        return RIGC_ERR_ARG;
+    if (d->num_vertices > 0 && !d->rest_vertices) return RIGC_ERR_ARG;
+    if (d->num_edges > 0 && !d->edges) return RIGC_ERR_ARG;
+    if (d->num_faces > 0 && (!d->faces || !d->faces_to_edges)) return RIGC_ERR_ARG;
+    if ((int64_t)d->num_vertices >= (1ll << 30) || (int64_t)d->num_edges >= (1ll << 30)
+        || (int64_t)d->num_faces >= (1ll << 30))
+        return RIGC_ERR_ARG;
+    const int nb = d->num_bodies, nv = d->num_vertices, ne = d->num_edges, nf = d->num_faces;
+    // validate prefix arrays and indices on the host
+    if (nb > 0) {
+        if (d->body_vertex_start[0] != 0 || d->body_vertex_start[nb] != nv) return RIGC_ERR_ARG;
+        if (d->body_edge_start[0] != 0 || d->body_edge_start[nb] != ne) return RIGC_ERR_ARG;
+        if (d->body_face_start[0] != 0 || d->body_face_start[nb] != nf) return RIGC_ERR_ARG;
+        for (int b = 0; b < nb; b++)
+            if (d->body_vertex_start[b + 1] < d->body_vertex_start[b]
+                || d->body_edge_start[b + 1] < d->body_edge_start[b]
+                || d->body_face_start[b + 1] < d->body_face_start[b])
+                return RIGC_ERR_ARG;
+    }
+    for (int i = 0; i < 2 * ne; i++)
+        if (d->edges[i] < 0 || d->edges[i] >= nv) return RIGC_ERR_ARG;
+    for (int i = 0; i < 3 * nf; i++) {
+        if (d->faces[i] < 0 || d->faces[i] >= nv) return RIGC_ERR_ARG;
+        if (d->faces_to_edges[i] < 0 || d->faces_to_edges[i] >= ne) return RIGC_ERR_ARG;
+    }
+    Ctx* c = new Ctx;
+    Scene& s = c->s;
+    s.nb = nb;
+    s.nv = nv;
+    s.ne = ne;
+    s.nf = nf;
+    s.avg_edge_len = d->average_edge_length;
+    std::vector<int> vbody(nv), ebody(ne), fbody(nf);
+    std::vector<double> elen(ne);
+    for (int b = 0; b < nb; b++) {
+        for (int i = d->body_vertex_start[b]; i < d->body_vertex_start[b + 1]; i++) vbody[i] = b;
+        for (int i = d->body_edge_start[b]; i < d->body_edge_start[b + 1]; i++) ebody[i] = b;
+        for (int i = d->body_face_start[b]; i < d->body_face_start[b + 1]; i++) fbody[i] = b;
+        s.max_body_vertices = std::max(s.max_body_vertices,
+                                       d->body_vertex_start[b + 1] - d->body_vertex_start[b]);
+    }
+    for (int e = 0; e < ne; e++) {
+        const double* a = d->rest_vertices + 3 * d->edges[2 * e];
+        const double* b = d->rest_vertices + 3 * d->edges[2 * e + 1];
+        double d0 = a[0] - b[0], d1 = a[1] - b[1], d2 = a[2] - b[2];
+        elen[e] = std::sqrt((d0 * d0 + d1 * d1) + d2 * d2);
+    }
+    s.h_bvs.assign(d->body_vertex_start, d->body_vertex_start + nb + 1);
+    s.h_type.assign(d->body_types, d->body_types + nb);
+    int st = RIGC_OK;
+    auto chk = [&](int r) {
+        if (st == RIGC_OK) st = r;
+    };
+    chk(upload(s.rest, d->rest_vertices, (size_t)3 * nv));
+    chk(upload(s.edges, d->edges, (size_t)2 * ne));
+    chk(upload(s.faces, d->faces, (size_t)3 * nf));
+    chk(upload(s.f2e, d->faces_to_edges, (size_t)3 * nf));
+    chk(upload(s.bvs, d->body_vertex_start, (size_t)nb + 1));
+    chk(upload(s.bes, d->body_edge_start, (size_t)nb + 1));
+    chk(upload(s.bfs, d->body_face_start, (size_t)nb + 1));
+    chk(upload(s.group, d->group_ids, (size_t)nb));
+    chk(upload(s.type, d->body_types, (size_t)nb));
+    chk(upload(s.rmax, d->r_max, (size_t)nb));
+    chk(upload(s.vbody, vbody.data(), (size_t)nv));
+    chk(upload(s.ebody, ebody.data(), (size_t)ne));
+    chk(upload(s.fbody, fbody.data(), (size_t)nf));
+    chk(upload(s.edge_len, elen.data(), (size_t)ne));
+    chk(c->d_scalars.reserve(4096));
+    if (st == RIGC_OK) {
+        cudaError_t e = cudaMallocHost(&c->h_scalars, 4096);
+        if (e != cudaSuccess) st = RIGC_ERR_OOM;
+    }
+    if (st != RIGC_OK) {
+        release_all(c);
+        delete c;
+        return st;
+    }
+    *out = reinterpret_cast<rigc_ctx*>(c);
+    return RIGC_OK;
+}
+
+int rigc_ctx_destroy(rigc_ctx* ctx)
+{
+    if (!ctx) return RIGC_ERR_ARG;
+    Ctx* c = ctx_of(ctx);
+    cudaStreamSynchronize(c->stream);
+    release_all(c);
+    delete c;
+    return RIGC_OK;
+}
+
+int rigc_set_stream(rigc_ctx* ctx, void* stream)
+{
+    if (!ctx) return RIGC_ERR_ARG;
+    ctx_of(ctx)->stream = static_cast<cudaStream_t>(stream);
+    return RIGC_OK;
+}
+
+int rigc_get_stats(const rigc_ctx* ctx, rigc_stats* out)
+{
+    if (!ctx || !out) return RIGC_ERR_ARG;
+    *out = reinterpret_cast<const Ctx*>(ctx)->stats;
+    return RIGC_OK;
+}
+
+int rigc_copy(rigc_ctx* ctx, void* dst, const void* src, size_t bytes)
+{
+    if (!ctx || (bytes && (!dst || !src))) return RIGC_ERR_ARG;
+    if (bytes == 0) return RIGC_OK;
+    Ctx& c = *ctx_of(ctx);
+    RIGC_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, c.stream));
+    RIGC_CUDA(cudaStreamSynchronize(c.stream));
+    return RIGC_OK;
+}
+
+int rigc_world_vertices(rigc_ctx* ctx, const double* x, double* V)
+{
+    if (!ctx || !x || !V) return RIGC_ERR_ARG;
+    Ctx& c = *ctx_of(ctx);
+    return compute_world_vertices_rn(c, x, V, c.scratch[5]);
+}
+
+int rigc_detect_candidates(rigc_ctx* ctx, const double* x0, const double* x1, int continuous,
+                           double inflation, rigc_candidates* out)
+{
+    if (!ctx || !x0 || (continuous && !x1) || !(inflation >= 0)) return RIGC_ERR_ARG;
+    Ctx& c = *ctx_of(ctx);
+    RIGC_TRY(detect_and_count(c, x0, x1, continuous != 0, inflation));
+    if (out) {
+        out->num_ee = c.cand.num_ee;
+        out->num_fv = c.cand.num_fv;
+        out->ee = c.cand.ee.as<int32_t>();
+        out->fv = c.cand.fv.as<int32_t>();
+    }
+    return RIGC_OK;
+}
+
+int rigc_earliest_toi(rigc_ctx* ctx, const double* x0, const double* x1, double toi_tol,
+                      int flags, double* toi_host, double* per_candidate)
+{
+    if (!ctx || !x0 || !x1 || !toi_host || !(toi_tol > 0)) return RIGC_ERR_ARG;
+    Ctx& c = *ctx_of(ctx);
+    return run_ccd(c, x0, x1, toi_tol, flags, toi_host, per_candidate);
+}
+
+int rigc_compute_earliest_toi(rigc_ctx* ctx, const double* x0, const double* x1, double dmin,
+                              double* toi_host)
+{
+    if (!ctx || !x0 || !x1 || !toi_host || !(dmin >= 0)) return RIGC_ERR_ARG;
+    Ctx& c = *ctx_of(ctx);
+    RIGC_TRY(detect_and_count(c, x0, x1, true, dmin / 2.0));
+    return run_ccd(c, x0, x1, 1e-4, 0, toi_host, nullptr);
+}
+
+int rigc_construct_constraint_set(rigc_ctx* ctx, const double* x, double dhat, double dmin,
+                                  rigc_constraints* out)
+{
+    if (!ctx || !x || !(dhat > 0) || !(dmin >= 0)) return RIGC_ERR_ARG;
+    Ctx& c = *ctx_of(ctx);
+    if (c.s.nb <= 1) {
+        c.cons.num = c.cons.num_vv = c.cons.num_ev = c.cons.num_ee = c.cons.num_fv = 0;
+    } else {
+        RIGC_TRY(detect_and_count(c, x, x, false, (dhat + dmin) / 2.0));
+        RIGC_TRY(construct_constraints(c, x, dhat, dmin));
+    }
+    if (out) {
+        Constraints& C = c.cons;
+        out->num = C.num;
+        out->num_vv = C.num_vv;
+        out->num_ev = C.num_ev;
+        out->num_ee = C.num_ee;
+        out->num_fv = C.num_fv;
+        out->type = C.type.as<int32_t>();
+        out->verts = C.verts.as<int32_t>();
+        out->prims = C.prims.as<int32_t>();
+        out->bodies = C.bodies.as<int32_t>();
+        out->weight = C.weight.as<double>();
+        out->eps_x = C.eps.as<double>();
+    }
+    return RIGC_OK;
+}
+
+int rigc_set_constraints(rigc_ctx* ctx, int64_t num, const int32_t* type, const int32_t* verts,
+                         const int32_t* prims, const int32_t* bodies, const double* weight,
+                         const double* eps_x)
+{
+    if (!ctx || num < 0) return RIGC_ERR_ARG;
+    if (num > 0 && (!type || !verts || !prims || !bodies || !weight || !eps_x)) return RIGC_ERR_ARG;
+    Ctx& c = *ctx_of(ctx);
+    Constraints& C = c.cons;
+    int64_t k[4] = { 0, 0, 0, 0 };
+    for (int64_t i = 0; i < num; i++) {
+        if (type[i] < 0 || type[i] > 3) return RIGC_ERR_ARG;
+        int nvc = type[i] == 0 ? 2 : (type[i] == 1 ? 3 : 4);
+        for (int j = 0; j < nvc; j++)
+            if (verts[4 * i + j] < 0 || verts[4 * i + j] >= c.s.nv) return RIGC_ERR_ARG;
+        for (int j = 0; j < 2; j++)
+            if (bodies[2 * i + j] < 0 || bodies[2 * i + j] >= c.s.nb) return RIGC_ERR_ARG;
+        k[type[i]]++;
+    }
+    RIGC_TRY(C.type.reserve((size_t)num * 4 + 8));
+    RIGC_TRY(C.verts.reserve((size_t)num * 16 + 8));
+    RIGC_TRY(C.prims.reserve((size_t)num * 8 + 8));
+    RIGC_TRY(C.bodies.reserve((size_t)num * 8 + 8));
+    RIGC_TRY(C.weight.reserve((size_t)num * 8 + 8));
+    RIGC_TRY(C.eps.reserve((size_t)num * 8 + 8));
+    cudaStream_t st = c.stream;
+    if (num > 0) {
+        RIGC_CUDA(cudaMemcpyAsync(C.type.ptr, type, num * 4, cudaMemcpyHostToDevice, st));
+        RIGC_CUDA(cudaMemcpyAsync(C.verts.ptr, verts, num * 16, cudaMemcpyHostToDevice, st));
+        RIGC_CUDA(cudaMemcpyAsync(C.prims.ptr, prims, num * 8, cudaMemcpyHostToDevice, st));
+        RIGC_CUDA(cudaMemcpyAsync(C.bodies.ptr, bodies, num * 8, cudaMemcpyHostToDevice, st));
+        RIGC_CUDA(cudaMemcpyAsync(C.weight.ptr, weight, num * 8, cudaMemcpyHostToDevice, st));
+        RIGC_CUDA(cudaMemcpyAsync(C.eps.ptr, eps_x, num * 8, cudaMemcpyHostToDevice, st));
+        RIGC_CUDA(cudaStreamSynchronize(st));
+    }
+    C.num = num;
+    C.num_vv = k[0];
+    C.num_ev = k[1];
+    C.num_ee = k[2];
+    C.num_fv = k[3];
+    return RIGC_OK;
+}
+
+static int barrier_term_impl(Ctx& c, const double* x, double dhat, double dmin, int flags,
+                             rigc_barrier_out* out)
+{
+    const int64_t n = c.cons.num;
+    const bool g = (flags & (RIGC_GRAD | RIGC_HESS)) != 0, h = (flags & RIGC_HESS) != 0;
+    RIGC_TRY(c.c_energy.reserve((size_t)n * 8 + 8));
+    if (g) RIGC_TRY(c.c_grad.reserve((size_t)n * 96 + 8));
+    if (h) RIGC_TRY(c.c_blocks.reserve((size_t)n * 144 * 8 + 8));
+    RIGC_TRY(launch_barrier_local(c, x, dhat, dmin, flags, c.c_energy.as<double>(),
+                                  g ? c.c_grad.as<double>() : nullptr,
+                                  h ? c.c_blocks.as<double>() : nullptr, nullptr));
+    double* e_dev = reinterpret_cast<double*>(c.d_scalars.as<char>() + 2048);
+    if (n > 0) {
+        RIGC_TRY(sum_f64(c.c_energy.as<double>(), n, e_dev, c.scratch[6], c.stream));
+    } else {
+        RIGC_CUDA(cudaMemsetAsync(e_dev, 0, sizeof(double), c.stream));
+    }
+    if (g) {
+        RIGC_TRY(assemble_barrier(c, h));
+    }
+    RIGC_CUDA(cudaMemcpyAsync(c.h_scalars, e_dev, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    RIGC_CUDA(cudaStreamSynchronize(c.stream));
+    if (out) {
+        out->energy = c.h_scalars[0];
+        out->nnzb = h ? c.nnzb : 0;
+        out->grad = g ? c.grad.as<double>() : nullptr;
+        out->row_ptr = h ? c.row_ptr.as<int32_t>() : nullptr;
+        out->col = h ? c.col.as<int32_t>() : nullptr;
+        out->val = h ? c.val.as<double>() : nullptr;
+    }
+    return RIGC_OK;
+}
+
+int rigc_barrier_term(rigc_ctx* ctx, const double* x, double dhat, double dmin, int flags,
+                      rigc_barrier_out* out)
+{
+    if (!ctx || !x || !(dhat > 0) || !(dmin >= 0)) return RIGC_ERR_ARG;
+    return barrier_term_impl(*ctx_of(ctx), x, dhat, dmin, flags, out);
+}
+
+int rigc_barrier_local_terms(rigc_ctx* ctx, const double* x, double dhat, double dmin, int flags,
+                             double* energy, double* grad, double* hess)
+{
+    if (!ctx || !x || !(dhat > 0) || !(dmin >= 0)) return RIGC_ERR_ARG;
+    Ctx& c = *ctx_of(ctx);
+    RIGC_TRY(launch_barrier_local(c, x, dhat, dmin, flags, energy, grad, nullptr, hess));
+    RIGC_CUDA(cudaStreamSynchronize(c.stream));
+    return RIGC_OK;
+}
+
+int rigc_narrow_phase_host(rigc_ctx* ctx, const double* x0_host, const double* x1_host,
+                           double dhat, double dmin, double* toi_host, double* energy_host,
+                           double* grad_host, int32_t* row_ptr_host, int32_t* col_host,
+                           double* val_host, int64_t nnzb_cap, int64_t* nnzb_host)
+{
+    if (!ctx || !x0_host || !x1_host || !toi_host || !energy_host || !grad_host || !row_ptr_host
+        || !nnzb_host || !(dhat > 0) || !(dmin >= 0) || nnzb_cap < 0)
+        return RIGC_ERR_ARG;
+    Ctx& c = *ctx_of(ctx);
+    const size_t xb = (size_t)6 * c.s.nb * sizeof(double);
+    for (size_t i = 0; i < 6 * (size_t)c.s.nb; i++)
+        if (!std::isfinite(x0_host[i]) || !std::isfinite(x1_host[i])) return RIGC_ERR_NAN;
+    RIGC_TRY(c.x0_dev.reserve(xb + 8));
+    RIGC_TRY(c.x1_dev.reserve(xb + 8));
+    cudaStream_t st = c.stream;
+    RIGC_CUDA(cudaMemcpyAsync(c.x0_dev.ptr, x0_host, xb, cudaMemcpyHostToDevice, st));
+    RIGC_CUDA(cudaMemcpyAsync(c.x1_dev.ptr, x1_host, xb, cudaMemcpyHostToDevice, st));
+    const double* x0 = c.x0_dev.as<double>();
+    const double* x1 = c.x1_dev.as<double>();
+    int st_toi = rigc_compute_earliest_toi(ctx, x0, x1, dmin, toi_host);
+    if (st_toi != RIGC_OK && st_toi != RIGC_ERR_QUEUE_OVERFLOW && st_toi != RIGC_ERR_ITER_LIMIT)
+        return st_toi;
+    RIGC_TRY(rigc_construct_constraint_set(ctx, x0, dhat, dmin, nullptr));
+    rigc_barrier_out bo;
+    RIGC_TRY(barrier_term_impl(c, x0, dhat, dmin, RIGC_GRAD | RIGC_HESS | RIGC_PROJECT_PSD, &bo));
+    *energy_host = bo.energy;
+    *nnzb_host = bo.nnzb;
+    RIGC_CUDA(cudaMemcpyAsync(grad_host, bo.grad, xb, cudaMemcpyDeviceToHost, st));
+    RIGC_CUDA(cudaMemcpyAsync(row_ptr_host, bo.row_ptr, (size_t)(c.s.nb + 1) * sizeof(int32_t),
+                              cudaMemcpyDeviceToHost, st));
+    if (bo.nnzb > 0 && bo.nnzb <= nnzb_cap && col_host && val_host) {
+        RIGC_CUDA(cudaMemcpyAsync(col_host, bo.col, (size_t)bo.nnzb * sizeof(int32_t),
+                                  cudaMemcpyDeviceToHost, st));
+        RIGC_CUDA(cudaMemcpyAsync(val_host, bo.val, (size_t)bo.nnzb * 36 * sizeof(double),
+                                  cudaMemcpyDeviceToHost, st));
+    }
+    RIGC_CUDA(cudaStreamSynchronize(st));
+    return st_toi;
+}
+
+} // extern "C"

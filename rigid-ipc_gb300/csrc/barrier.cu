@@ -1,0 +1,768 @@
+// Barrier energy, body-space gradient and 12x12 pair Hessian per constraint,
+// with the rigid-pose chain rule folded in, and their deterministic assembly
+// into a per-body gradient and a 6x6 block-sparse Hessian.
+//
+// Replaces DistanceBarrierRBProblem::compute_barrier_term
+// (src/problems/distance_barrier_rb_problem.cpp:1299-1399): the ipc-toolkit
+// constraint potentials (log barrier of the squared distance shifted by
+// dmin^2, src/opt/distance_barrier_constraint.tpp:11-17; EE mollifier),
+// apply_chain_rule (:1182-1248, including project_to_psd of the 12x12),
+// local_hessian_to_global_triplets (:1157-1179) and merge_derivative_storage
+// (:1260-1297).
+//
+// Derivation used by k_barrier_local.  With X the constraint's vertex
+// positions and x the two bodies' 6-dof poses, X_i = R_b v_i + p_b and
+// J_i = dX_i/dx_b = [I | D_i], D_i[:, k] = (dR/dtheta_k) v_i.
+//  * PT / EE: d = u^2 / D with u = (A x B).w and D = |A x B|^2, where
+//    A, B, w are signed sums of the vertices (coefficients alpha, beta,
+//    gamma).  grad u = {alpha_i (B x w) + beta_i (w x A) + gamma_i n},
+//    grad D = {2 alpha_i (B x n) + 2 beta_i (n x A)}; the Hessians are
+//    Gram(dn) terms and skew bilinear blocks [s_ij]x between vertices i != j.
+//  * PE: d = |a x b|^2 / |e|^2, the same pieces with a Gram(de) term.
+//  * PP: d = |w|^2.
+// f = weight * m(D) * b(d - dmin^2) (m = 1 except mollified EE), so the body
+// Hessian is  sum of outer products of the body-space gradients of the basic
+// scalars + Gram terms + skew pair blocks + the curvature term
+// sum_i grad_Xi f . d2X_i/dtheta2.  It is then projected to the PSD cone: a
+// Cholesky attempt first (a positive definite matrix is returned unchanged,
+// as project_to_psd does), else cyclic Jacobi and V max(L, 0) V^T.
+#include "common.cuh"
+#include "rotation.cuh"
+#include "sort.cuh"
+
+namespace rigc {
+
+// ---------------------------------------------------------------------------
+// per-body frames (R, dR, d2R) and positions
+
+__global__ void k_body_frames(const double* __restrict__ x, int nb, double* __restrict__ frames)
+{
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    double t[3] = { x[6 * b + 3], x[6 * b + 4], x[6 * b + 5] };
+    double F[kFrameDoubles];
+    body_frame(t, F);
+    double* out = frames + (size_t)b * 96;
+#pragma unroll
+    for (int i = 0; i < kFrameDoubles; i++) out[i] = F[i];
+    out[90] = x[6 * b];
+    out[91] = x[6 * b + 1];
+    out[92] = x[6 * b + 2];
+}
+
+// ---------------------------------------------------------------------------
+
+constexpr int kBarrierTPB = 32;
+
+struct Vtx {
+    double X[3];     // world position
+    double D[3][3];  // dX/dtheta  [coord][k]
+};
+
+__device__ __forceinline__ void cross(const double* a, const double* b, double* r)
+{
+    r[0] = a[1] * b[2] - a[2] * b[1];
+    r[1] = a[2] * b[0] - a[0] * b[2];
+    r[2] = a[0] * b[1] - a[1] * b[0];
+}
+__device__ __forceinline__ double dot(const double* a, const double* b)
+{
+    return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+}
+
+// shared-memory 12x12 accumulator, entry-major / thread-minor
+struct SMat {
+    double* base;
+    __device__ __forceinline__ double& at(int r, int c) const
+    {
+        return base[(r * 12 + c) * kBarrierTPB];
+    }
+};
+
+// H += coef * (a b^T + b a^T) on the upper triangle (a, b in body space)
+__device__ __forceinline__ void add_sym_outer(SMat H, double coef, const double* a, const double* b)
+{
+    for (int r = 0; r < 12; r++) {
+        double ar = coef * a[r], br = coef * b[r];
+        for (int c = r; c < 12; c++) H.at(r, c) += ar * b[c] + br * a[c];
+    }
+}
+__device__ __forceinline__ void add_outer(SMat H, double coef, const double* a)
+{
+    for (int r = 0; r < 12; r++) {
+        double ar = coef * a[r];
+        for (int c = r; c < 12; c++) H.at(r, c) += ar * a[c];
+    }
+}
+
+// body-space image of a per-vertex vector field: out[6 lb + 0..2] += g_i,
+// out[6 lb + 3 + k] += D_i[:, k] . g_i
+__device__ __forceinline__ void to_body(const Vtx* V, const int* lbody, int nvc,
+                                        const double (*g)[3], double* out)
+{
+    for (int k = 0; k < 12; k++) out[k] = 0;
+    for (int i = 0; i < nvc; i++) {
+        int o = 6 * lbody[i];
+        for (int j = 0; j < 3; j++) out[o + j] += g[i][j];
+        for (int k = 0; k < 3; k++)
+            out[o + 3 + k] += V[i].D[0][k] * g[i][0] + V[i].D[1][k] * g[i][1] + V[i].D[2][k] * g[i][2];
+    }
+}
+
+// Gram term H += coef * JM^T JM where JM (3 x 12) = sum_i M_i J_i and
+// M_i = m_i * I + (skew parts): here M_i given as full 3x3 per vertex.
+__device__ __forceinline__ void add_gram(SMat H, double coef, const Vtx* V, const int* lbody,
+                                         int nvc, const double (*M)[9])
+{
+    double JM[3][12];
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 12; c++) JM[r][c] = 0;
+    for (int i = 0; i < nvc; i++) {
+        int o = 6 * lbody[i];
+        for (int r = 0; r < 3; r++) {
+            for (int j = 0; j < 3; j++) JM[r][o + j] += M[i][3 * r + j];
+            for (int k = 0; k < 3; k++)
+                JM[r][o + 3 + k] += M[i][3 * r] * V[i].D[0][k] + M[i][3 * r + 1] * V[i].D[1][k]
+                    + M[i][3 * r + 2] * V[i].D[2][k];
+        }
+    }
+    for (int r = 0; r < 12; r++) {
+        double a0 = coef * JM[0][r], a1 = coef * JM[1][r], a2 = coef * JM[2][r];
+        for (int c = r; c < 12; c++) H.at(r, c) += a0 * JM[0][c] + a1 * JM[1][c] + a2 * JM[2][c];
+    }
+}
+
+// skew pair block: H(i-part, j-part) += J_i^T [s]x J_j, and its transpose
+__device__ __forceinline__ void add_skew_pair(SMat H, const Vtx& Vi, int oi, const Vtx& Vj,
+                                              int oj, const double* s)
+{
+    // K = [s]x
+    const double K[3][3] = { { 0, -s[2], s[1] }, { s[2], 0, -s[0] }, { -s[1], s[0], 0 } };
+    // blocks: [K, K Dj ; Di^T K, Di^T K Dj]
+    double KD[3][3], DK[3][3], DKD[3][3];
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) {
+            KD[r][c] = K[r][0] * Vj.D[0][c] + K[r][1] * Vj.D[1][c] + K[r][2] * Vj.D[2][c];
+            DK[r][c] = Vi.D[0][r] * K[0][c] + Vi.D[1][r] * K[1][c] + Vi.D[2][r] * K[2][c];
+        }
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++)
+            DKD[r][c] = Vi.D[0][r] * KD[0][c] + Vi.D[1][r] * KD[1][c] + Vi.D[2][r] * KD[2][c];
+    // B (6x6) = [[K, KD], [DK, DKD]] goes to rows oi.., cols oj..; its
+    // transpose to rows oj.., cols oi..; accumulate into the upper triangle.
+    for (int r = 0; r < 6; r++)
+        for (int c = 0; c < 6; c++) {
+            double v = r < 3 ? (c < 3 ? K[r][c] : KD[r][c - 3])
+                             : (c < 3 ? DK[r - 3][c] : DKD[r - 3][c - 3]);
+            int R = oi + r, C = oj + c;
+            // entry (R, C) of B and entry (C, R) of B^T are both v
+            if (R <= C) H.at(R, C) += v;
+            if (C <= R) H.at(C, R) += v;
+        }
+}
+
+// curvature term: H(rot lb, rot lb) += sum_j g_j (d2R_kl v)_j
+__device__ __forceinline__ void add_curvature(SMat H, const double* frame, int lb,
+                                              const double* v, const double* g)
+{
+    const double* d2 = frame + 36;
+    int o = 6 * lb + 3;
+    for (int k = 0; k < 3; k++)
+        for (int l = k; l < 3; l++) {
+            const double* M = d2 + 9 * sym_index(k, l);
+            double acc = 0;
+            for (int j = 0; j < 3; j++)
+                acc += g[j] * (M[3 * j] * v[0] + M[3 * j + 1] * v[1] + M[3 * j + 2] * v[2]);
+            H.at(o + k, o + l) += acc;
+        }
+}
+
+// ---------------------------------------------------------------------------
+// PSD projection of the (upper-triangle filled) 12x12 in shared memory.
+// Returns with the full symmetric projected matrix in H.
+
+__device__ bool cholesky_pd(SMat H, double* L)
+{
+    // L in registers-by-unrolling is too large; factor into scratch L (smem)
+    // L holds the lower factor in the same entry-major layout.
+    SMat Lm { L };
+    for (int j = 0; j < 12; j++) {
+        double d = H.at(j, j);
+        for (int k = 0; k < j; k++) d -= Lm.at(j, k) * Lm.at(j, k);
+        if (!(d > 0.0)) return false;
+        double ljj = sqrt(d);
+        Lm.at(j, j) = ljj;
+        double inv = 1.0 / ljj;
+        for (int i = j + 1; i < 12; i++) {
+            double s = H.at(j, i);  // upper triangle holds (j, i) = (i, j)
+            for (int k = 0; k < j; k++) s -= Lm.at(i, k) * Lm.at(j, k);
+            Lm.at(i, j) = s * inv;
+        }
+    }
+    return true;
+}
+
+__device__ void jacobi_project(SMat A, SMat Vm)
+{
+    // full symmetric A from the upper triangle
+    for (int r = 0; r < 12; r++)
+        for (int c = 0; c < r; c++) A.at(r, c) = A.at(c, r);
+    for (int r = 0; r < 12; r++)
+        for (int c = 0; c < 12; c++) Vm.at(r, c) = r == c ? 1.0 : 0.0;
+    for (int sweep = 0; sweep < 30; sweep++) {
+        double off = 0, diag = 0;
+        for (int i = 0; i < 12; i++) {
+            diag += A.at(i, i) * A.at(i, i);
+            for (int j = i + 1; j < 12; j++) off += A.at(i, j) * A.at(i, j);
+        }
+        if (off <= 1e-32 * diag || off == 0.0) break;
+        for (int p = 0; p < 12; p++)
+            for (int q = p + 1; q < 12; q++) {
+                double apq = A.at(p, q);
+                if (apq == 0.0) continue;
+                double app = A.at(p, p), aqq = A.at(q, q);
+                double theta = (aqq - app) / (2 * apq);
+                double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1));
+                double c = 1.0 / sqrt(t * t + 1);
+                double s = t * c;
+                for (int k = 0; k < 12; k++) {
+                    double akp = A.at(k, p), akq = A.at(k, q);
+                    A.at(k, p) = c * akp - s * akq;
+                    A.at(k, q) = s * akp + c * akq;
+                }
+                for (int k = 0; k < 12; k++) {
+                    double apk = A.at(p, k), aqk = A.at(q, k);
+                    A.at(p, k) = c * apk - s * aqk;
+                    A.at(q, k) = s * apk + c * aqk;
+                }
+                for (int k = 0; k < 12; k++) {
+                    double vkp = Vm.at(k, p), vkq = Vm.at(k, q);
+                    Vm.at(k, p) = c * vkp - s * vkq;
+                    Vm.at(k, q) = s * vkp + c * vkq;
+                }
+            }
+    }
+    double w[12];
+    for (int i = 0; i < 12; i++) w[i] = A.at(i, i);
+    // rebuild: A = V max(w, 0) V^T
+    for (int r = 0; r < 12; r++)
+        for (int c = r; c < 12; c++) {
+            double acc = 0;
+            for (int k = 0; k < 12; k++)
+                if (w[k] > 0) acc += Vm.at(r, k) * w[k] * Vm.at(c, k);
+            A.at(r, c) = acc;
+        }
+}
+
+// ---------------------------------------------------------------------------
+
+struct BarrierArgs {
+    const double* rest;
+    const double* frames;
+    const int* ctype;
+    const int* cverts;
+    const int* cbodies;
+    const double* cweight;
+    const double* ceps;
+    int64_t n;
+    double dhat, dmin;
+    int flags;
+    double* energy;   // n
+    double* grad;     // n x 12
+    double* blocks;   // n x 4 x 36 (blocks (0,0) (0,1) (1,0) (1,1))
+    double* hess;     // optional n x 144 (full local Hessian)
+};
+
+__device__ __forceinline__ int local_body_of(int type, int i)
+{
+    if (type == 2) return i < 2 ? 0 : 1;
+    return i == 0 ? 0 : 1;
+}
+
+__global__ void __launch_bounds__(kBarrierTPB)
+k_barrier_local(BarrierArgs a)
+{
+    extern __shared__ double smem[];
+    const int tid = threadIdx.x;
+    const int64_t ci = (int64_t)blockIdx.x * kBarrierTPB + tid;
+    if (ci >= a.n) return;
+    SMat H { smem + tid };
+    SMat V2 { smem + 144 * kBarrierTPB + tid };
+
+    const int type = a.ctype[ci];
+    const int nvc = type == 0 ? 2 : (type == 1 ? 3 : 4);
+    const double weight = a.cweight[ci];
+    int lbody[4];
+    const double* fr[2];
+    int bod[2] = { a.cbodies[2 * ci], a.cbodies[2 * ci + 1] };
+    fr[0] = a.frames + (size_t)bod[0] * 96;
+    fr[1] = a.frames + (size_t)bod[1] * 96;
+    Vtx V[4];
+    double vrest[4][3];
+    for (int i = 0; i < nvc; i++) {
+        lbody[i] = local_body_of(type, i);
+        int vi = a.cverts[4 * ci + i];
+        const double* f = fr[lbody[i]];
+        for (int j = 0; j < 3; j++) vrest[i][j] = a.rest[3 * (size_t)vi + j];
+        const double* v = vrest[i];
+        for (int j = 0; j < 3; j++) {
+            V[i].X[j] = f[3 * j] * v[0] + f[3 * j + 1] * v[1] + f[3 * j + 2] * v[2] + f[90 + j];
+            for (int k = 0; k < 3; k++) {
+                const double* dR = f + 9 + 9 * k;
+                V[i].D[j][k] = dR[3 * j] * v[0] + dR[3 * j + 1] * v[1] + dR[3 * j + 2] * v[2];
+            }
+        }
+    }
+
+    // coefficient patterns: A = sum alpha_i X_i, B = sum beta_i X_i, w = sum gamma_i X_i
+    double al[4] = { 0, 0, 0, 0 }, be[4] = { 0, 0, 0, 0 }, ga[4] = { 0, 0, 0, 0 };
+    double A[3], B[3], W[3], n[3];
+    double d, u = 0, Dn = 0;
+    if (type == 2) {        // EE: A = X1 - X0, B = X3 - X2, w = X2 - X0
+        al[0] = -1; al[1] = 1; be[2] = -1; be[3] = 1; ga[0] = -1; ga[2] = 1;
+    } else if (type == 3) { // FV: A = X2 - X1, B = X3 - X1, w = X0 - X1
+        al[1] = -1; al[2] = 1; be[1] = -1; be[3] = 1; ga[0] = 1; ga[1] = -1;
+    } else if (type == 1) { // EV: a = X1 - X0, b = X2 - X0 ; e = X2 - X1 (gamma)
+        al[0] = -1; al[1] = 1; be[0] = -1; be[2] = 1; ga[1] = -1; ga[2] = 1;
+    } else {                // VV: w = X0 - X1
+        ga[0] = 1; ga[1] = -1;
+    }
+    for (int j = 0; j < 3; j++) {
+        A[j] = 0; B[j] = 0; W[j] = 0;
+        for (int i = 0; i < nvc; i++) {
+            A[j] += al[i] * V[i].X[j];
+            B[j] += be[i] * V[i].X[j];
+            W[j] += ga[i] * V[i].X[j];
+        }
+    }
+    double De = 0;
+    if (type >= 2) {
+        cross(A, B, n);
+        u = dot(n, W);
+        Dn = dot(n, n);
+        d = u * u / Dn;
+    } else if (type == 1) {
+        cross(A, B, n);  // c = a x b
+        Dn = dot(n, n);  // N = |c|^2
+        De = dot(W, W);  // |e|^2
+        d = Dn / De;
+    } else {
+        d = dot(W, W);
+        n[0] = n[1] = n[2] = 0;
+    }
+
+    // barrier of the shifted squared distance
+    const double s = 2 * a.dmin * a.dhat + a.dhat * a.dhat;
+    const double dd = d - a.dmin * a.dmin;
+    double bv = 0, b1 = 0, b2 = 0;
+    bool active = dd < s;
+    if (dd <= 0.0) {
+        bv = INFINITY;
+        active = false;
+    } else if (active) {
+        double lg = log(dd / s);
+        double dm = dd - s;
+        bv = -dm * dm * lg;
+        b1 = (s - dd) * (2 * lg - s / dd + 1);
+        double sd = s / dd;
+        b2 = (sd + 2) * sd - 2 * lg - 3;
+    }
+    // EE mollifier m(D), D = |A x B|^2
+    double m = 1, m1 = 0, m2 = 0;
+    if (type == 2 && Dn < a.ceps[ci]) {
+        double ie = 1.0 / a.ceps[ci];
+        double xe = Dn * ie;
+        m = (2 - xe) * xe;
+        m1 = (2 - 2 * xe) * ie;
+        m2 = -2 * ie * ie;
+    }
+    if (a.energy) a.energy[ci] = weight * m * bv;
+    const bool want_g = (a.flags & (RIGC_GRAD | RIGC_HESS)) != 0;
+    const bool want_h = (a.flags & RIGC_HESS) != 0;
+    if (!active) {
+        if (a.grad)
+            for (int k = 0; k < 12; k++) a.grad[ci * 12 + k] = 0;
+        if (a.blocks && want_h)
+            for (int k = 0; k < 144; k++) a.blocks[ci * 144 + k] = 0;
+        if (a.hess && want_h)
+            for (int k = 0; k < 144; k++) a.hess[ci * 144 + k] = 0;
+        return;
+    }
+    if (!want_g) return;
+
+    // ---- basic scalars and their vertex-space gradients
+    // g1: gradient of the first scalar (u, N or d), g2: of the second (D, |e|^2)
+    double g1v[4][3], g2v[4][3];
+    double c1, c2;  // grad d = c1 g1 + c2 g2
+    if (type >= 2) {
+        double Bw[3], wA[3], Bn[3], nA[3];
+        cross(B, W, Bw);
+        cross(W, A, wA);
+        cross(B, n, Bn);
+        cross(n, A, nA);
+        for (int i = 0; i < 4; i++)
+            for (int j = 0; j < 3; j++) {
+                g1v[i][j] = al[i] * Bw[j] + be[i] * wA[j] + ga[i] * n[j];
+                g2v[i][j] = 2 * (al[i] * Bn[j] + be[i] * nA[j]);
+            }
+        c1 = 2 * u / Dn;
+        c2 = -u * u / (Dn * Dn);
+    } else if (type == 1) {
+        double bc[3], ca[3];
+        cross(B, n, bc);
+        cross(n, A, ca);
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) {
+                g1v[i][j] = 2 * (al[i] * bc[j] + be[i] * ca[j]);
+                g2v[i][j] = 2 * ga[i] * W[j];
+            }
+        c1 = 1 / De;
+        c2 = -Dn / (De * De);
+    } else {
+        for (int j = 0; j < 3; j++) {
+            g1v[0][j] = 2 * W[j];
+            g1v[1][j] = -2 * W[j];
+            g2v[0][j] = g2v[1][j] = 0;
+        }
+        c1 = 1;
+        c2 = 0;
+    }
+    // f = weight * m * b(d):  grad f = P_g1 g1 + P_g2 g2
+    const double wm = weight * m;
+    // (the mollifier's gradient lies along grad D = g2, EE only)
+    const double Pg1 = wm * b1 * c1;
+    const double Pg2 = wm * b1 * c2 + (type == 2 ? weight * bv * m1 : 0.0);
+    double gv[4][3];
+    for (int i = 0; i < nvc; i++)
+        for (int j = 0; j < 3; j++) gv[i][j] = Pg1 * g1v[i][j] + Pg2 * g2v[i][j];
+    double G[12];
+    to_body(V, lbody, nvc, gv, G);
+    if (a.grad)
+        for (int k = 0; k < 12; k++) a.grad[ci * 12 + k] = G[k];
+    if (!want_h) return;
+
+    // ---- Hessian
+    for (int r = 0; r < 12; r++)
+        for (int c = r; c < 12; c++) H.at(r, c) = 0;
+    double G1[12], G2[12];
+    to_body(V, lbody, nvc, g1v, G1);
+    to_body(V, lbody, nvc, g2v, G2);
+    // second-derivative coefficients of d in terms of (g1, g2) and the
+    // Hessians of the basic scalars:
+    //  PT/EE: hess d = (2/D) g1g1 + c1 H_u - (2u/D^2)(g1g2 + g2g1) + (2u^2/D^3) g2g2 + c2 H_D
+    //  PE:    hess d = (1/De) H_N - (1/De^2)(g1g2 + g2g1) + (2N/De^3) g2g2 + c2 H_e
+    //  PP:    hess d = H_w (Gram of dw)
+    double duu, duD, dDD;
+    if (type >= 2) {
+        duu = 2 / Dn;
+        duD = -2 * u / (Dn * Dn);
+        dDD = 2 * u * u / (Dn * Dn * Dn);
+    } else if (type == 1) {
+        duu = 0;
+        duD = -1 / (De * De);
+        dDD = 2 * Dn / (De * De * De);
+    } else {
+        duu = duD = dDD = 0;
+    }
+    // f Hessian = P1 gd gd^T + P2 hess d + [EE] P3 g2g2 + P4 H_D + P5 (g2 gd^T + gd g2^T)
+    const double P1 = wm * b2, P2 = wm * b1;
+    const double P3 = type == 2 ? weight * bv * m2 : 0.0;
+    const double P4 = type == 2 ? weight * bv * m1 : 0.0;
+    const double P5 = type == 2 ? weight * m1 * b1 : 0.0;
+    const double a11 = P1 * c1 * c1 + P2 * duu;
+    const double a12 = P1 * c1 * c2 + P2 * duD + P5 * c1;
+    const double a22 = P1 * c2 * c2 + P2 * dDD + P3 + 2 * P5 * c2;
+    add_outer(H, a11, G1);
+    add_sym_outer(H, a12, G1, G2);
+    add_outer(H, a22, G2);
+
+    // coefficients of the scalar Hessians
+    const double bu = P2 * c1;            // on H_u (PT/EE) or H_N (PE)
+    const double bD = P2 * c2 + P4;       // on H_D (PT/EE) or H_e (PE)
+    double M[4][9];
+    if (type >= 2) {
+        // H_D Gram part: 2 (dn)^T(dn), dn/dX_i = alpha_i(-[B]x) + beta_i [A]x
+        for (int i = 0; i < 4; i++) {
+            double* Mi = M[i];
+            double sa = al[i], sb = be[i];
+            // -[B]x * sa + [A]x * sb
+            double v0 = -sa * B[0] + sb * A[0], v1 = -sa * B[1] + sb * A[1], v2 = -sa * B[2] + sb * A[2];
+            Mi[0] = 0; Mi[1] = -v2; Mi[2] = v1;
+            Mi[3] = v2; Mi[4] = 0; Mi[5] = -v0;
+            Mi[6] = -v1; Mi[7] = v0; Mi[8] = 0;
+        }
+        add_gram(H, 2 * bD, V, lbody, 4, M);
+        // skew pair blocks: s_ij = bu * s_ij(u) + bD * s_ij(D)
+        for (int i = 0; i < 4; i++)
+            for (int j = i + 1; j < 4; j++) {
+                double sv[3];
+                for (int k = 0; k < 3; k++) {
+                    double su = -al[i] * be[j] * W[k] + al[j] * be[i] * W[k]
+                        + al[i] * ga[j] * B[k] - al[j] * ga[i] * B[k]
+                        - be[i] * ga[j] * A[k] + be[j] * ga[i] * A[k];
+                    double sD = 2 * (-al[i] * be[j] * n[k] + al[j] * be[i] * n[k]);
+                    sv[k] = bu * su + bD * sD;
+                }
+                if (sv[0] == 0 && sv[1] == 0 && sv[2] == 0) continue;
+                add_skew_pair(H, V[i], 6 * lbody[i], V[j], 6 * lbody[j], sv);
+            }
+    } else if (type == 1) {
+        // H_N = 2 (dc)^T(dc) + skew(c); H_e = 2 (de)^T(de)
+        for (int i = 0; i < 3; i++) {
+            double* Mi = M[i];
+            double sa = al[i], sb = be[i];
+            double v0 = -sa * B[0] + sb * A[0], v1 = -sa * B[1] + sb * A[1], v2 = -sa * B[2] + sb * A[2];
+            Mi[0] = 0; Mi[1] = -v2; Mi[2] = v1;
+            Mi[3] = v2; Mi[4] = 0; Mi[5] = -v0;
+            Mi[6] = -v1; Mi[7] = v0; Mi[8] = 0;
+        }
+        add_gram(H, 2 * bu, V, lbody, 3, M);
+        for (int i = 0; i < 3; i++) {
+            double* Mi = M[i];
+            for (int k = 0; k < 9; k++) Mi[k] = 0;
+            Mi[0] = Mi[4] = Mi[8] = ga[i];
+        }
+        add_gram(H, 2 * bD, V, lbody, 3, M);
+        for (int i = 0; i < 3; i++)
+            for (int j = i + 1; j < 3; j++) {
+                double sv[3];
+                for (int k = 0; k < 3; k++)
+                    sv[k] = bu * 2 * (-al[i] * be[j] * n[k] + al[j] * be[i] * n[k]);
+                if (sv[0] == 0 && sv[1] == 0 && sv[2] == 0) continue;
+                add_skew_pair(H, V[i], 6 * lbody[i], V[j], 6 * lbody[j], sv);
+            }
+    } else {
+        // d = |w|^2: hess = 2 (dw)^T (dw), coefficient P2 (c1 = 1)
+        for (int i = 0; i < 2; i++) {
+            double* Mi = M[i];
+            for (int k = 0; k < 9; k++) Mi[k] = 0;
+            Mi[0] = Mi[4] = Mi[8] = ga[i];
+        }
+        add_gram(H, 2 * P2, V, lbody, 2, M);
+    }
+    // curvature of the rigid maps
+    for (int i = 0; i < nvc; i++) add_curvature(H, fr[lbody[i]], lbody[i], vrest[i], gv[i]);
+
+    if (a.flags & RIGC_PROJECT_PSD) {
+        if (!cholesky_pd(H, V2.base)) jacobi_project(H, V2);
+    }
+    // write outputs (symmetric)
+    for (int r = 0; r < 12; r++)
+        for (int c = 0; c < 12; c++) {
+            double v = r <= c ? H.at(r, c) : H.at(c, r);
+            if (a.hess) a.hess[ci * 144 + 12 * r + c] = v;
+            if (a.blocks) {
+                int blk = (r / 6) * 2 + (c / 6);
+                a.blocks[ci * 144 + blk * 36 + (r % 6) * 6 + (c % 6)] = v;
+            }
+        }
+}
+
+size_t barrier_smem_bytes() { return (size_t)2 * 144 * kBarrierTPB * sizeof(double); }
+
+int launch_body_frames(Ctx& c, const double* x)
+{
+    RIGC_TRY(c.frames.reserve((size_t)c.s.nb * 96 * sizeof(double)));
+    k_body_frames<<<grid_for(c.s.nb, 128), 128, 0, c.stream>>>(x, c.s.nb, c.frames.as<double>());
+    RIGC_CUDA(cudaGetLastError());
+    return RIGC_OK;
+}
+
+int launch_barrier_local(Ctx& c, const double* x, double dhat, double dmin, int flags,
+                         double* energy, double* grad, double* blocks, double* hess)
+{
+    RIGC_TRY(launch_body_frames(c, x));
+    if (c.cons.num == 0) return RIGC_OK;
+    static bool attr = false;
+    if (!attr) {
+        RIGC_CUDA(cudaFuncSetAttribute(k_barrier_local, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)barrier_smem_bytes()));
+        attr = true;
+    }
+    BarrierArgs a;
+    a.rest = c.s.rest;
+    a.frames = c.frames.as<double>();
+    a.ctype = c.cons.type.as<int>();
+    a.cverts = c.cons.verts.as<int>();
+    a.cbodies = c.cons.bodies.as<int>();
+    a.cweight = c.cons.weight.as<double>();
+    a.ceps = c.cons.eps.as<double>();
+    a.n = c.cons.num;
+    a.dhat = dhat;
+    a.dmin = dmin;
+    a.flags = flags;
+    a.energy = energy;
+    a.grad = grad;
+    a.blocks = blocks;
+    a.hess = hess;
+    k_barrier_local<<<grid_for(c.cons.num, kBarrierTPB), kBarrierTPB, barrier_smem_bytes(),
+                      c.stream>>>(a);
+    RIGC_CUDA(cudaGetLastError());
+    return RIGC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// deterministic assembly: sort block keys, sum equal keys in constraint order
+
+__global__ void k_block_keys(const int* __restrict__ bodies, int64_t n, int nb,
+                             uint64_t* __restrict__ keys, uint32_t* __restrict__ vals)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 4 * n) return;
+    int64_t c = i >> 2;
+    int blk = (int)(i & 3);
+    int bi = bodies[2 * c + (blk >> 1)], bj = bodies[2 * c + (blk & 1)];
+    keys[i] = (uint64_t)bi * (uint64_t)nb + (uint64_t)bj;
+    vals[i] = (uint32_t)i;
+}
+
+__global__ void k_grad_keys(const int* __restrict__ bodies, int64_t n,
+                            uint32_t* __restrict__ keys, uint32_t* __restrict__ vals)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 2 * n) return;
+    keys[i] = (uint32_t)bodies[i];
+    vals[i] = (uint32_t)i;
+}
+
+template <class Key>
+__global__ void k_heads(const Key* __restrict__ keys, int64_t m, int32_t* __restrict__ head)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    head[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1 : 0;
+}
+
+// segment starts: seg_start[segid] = i for heads
+__global__ void k_seg_starts(const int32_t* __restrict__ head, const int32_t* __restrict__ segid,
+                             int64_t m, int32_t* __restrict__ seg_start)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    if (head[i]) seg_start[segid[i]] = (int32_t)i;
+}
+
+// one thread per (unique block, entry): sequential sum in slot order
+__global__ void k_block_sums(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ slots,
+                             const int32_t* __restrict__ seg_start, int32_t nseg, int64_t m,
+                             const double* __restrict__ blocks, int nb,
+                             int32_t* __restrict__ col, double* __restrict__ val,
+                             int32_t* __restrict__ row_count)
+{
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)nseg * 36) return;
+    int32_t sgi = (int32_t)(t / 36);
+    int e = (int)(t % 36);
+    int64_t s0 = seg_start[sgi];
+    int64_t s1 = sgi + 1 < nseg ? seg_start[sgi + 1] : m;
+    double acc = 0;
+    for (int64_t i = s0; i < s1; i++) acc += blocks[(size_t)slots[i] * 36 + e];
+    val[(size_t)sgi * 36 + e] = acc;
+    if (e == 0) {
+        uint64_t k = keys[s0];
+        int32_t r = (int32_t)(k / (uint64_t)nb);
+        col[sgi] = (int32_t)(k % (uint64_t)nb);
+        atomicAdd(&row_count[r], 1);
+    }
+}
+
+__global__ void k_grad_sums(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ slots,
+                            const int32_t* __restrict__ seg_start, int32_t nseg, int64_t m,
+                            const double* __restrict__ cgrad, double* __restrict__ grad)
+{
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)nseg * 6) return;
+    int32_t sgi = (int32_t)(t / 6);
+    int e = (int)(t % 6);
+    int64_t s0 = seg_start[sgi];
+    int64_t s1 = sgi + 1 < nseg ? seg_start[sgi + 1] : m;
+    double acc = 0;
+    for (int64_t i = s0; i < s1; i++) {
+        uint32_t slot = slots[i];  // = 2 c + side
+        acc += cgrad[(size_t)(slot >> 1) * 12 + 6 * (slot & 1) + e];
+    }
+    grad[(size_t)keys[s0] * 6 + e] = acc;
+}
+
+int assemble_barrier(Ctx& c, bool with_hess)
+{
+    const int64_t n = c.cons.num;
+    const int nb = c.s.nb;
+    cudaStream_t st = c.stream;
+    RIGC_TRY(c.grad.reserve((size_t)6 * nb * sizeof(double)));
+    RIGC_TRY(c.row_ptr.reserve((size_t)(nb + 1) * sizeof(int32_t)));
+    RIGC_CUDA(cudaMemsetAsync(c.grad.ptr, 0, (size_t)6 * nb * sizeof(double), st));
+    RIGC_CUDA(cudaMemsetAsync(c.row_ptr.ptr, 0, (size_t)(nb + 1) * sizeof(int32_t), st));
+    c.nnzb = 0;
+    if (n == 0) return RIGC_OK;
+    // scratch usage: 0 keys_in, 1 vals_in, 2 keys_out, 3 vals_out, 4/5 sort tmp,
+    // 6 hist/scan tmp, 7 head/segid/seg_start
+    DevBuf* S = c.scratch;
+    // ---- gradient
+    {
+        int64_t m = 2 * n;
+        RIGC_TRY(S[0].reserve(m * 4));
+        RIGC_TRY(S[1].reserve(m * 4));
+        RIGC_TRY(S[2].reserve(m * 4));
+        RIGC_TRY(S[3].reserve(m * 4));
+        RIGC_TRY(S[7].reserve(m * 12 + 16));
+        k_grad_keys<<<grid_for(m, 256), 256, 0, st>>>(c.cons.bodies.as<int>(), n, S[0].as<uint32_t>(),
+                                                     S[1].as<uint32_t>());
+        RIGC_TRY(radix_sort_pairs<uint32_t>(S[0].as<uint32_t>(), S[1].as<uint32_t>(),
+                                            S[2].as<uint32_t>(), S[3].as<uint32_t>(), m,
+                                            bits_for((uint64_t)nb), S[4], S[5], S[6], st));
+        int32_t* head = S[7].as<int32_t>();
+        int32_t* segid = head + m;
+        int32_t* segst = segid + m;
+        k_heads<uint32_t><<<grid_for(m, 256), 256, 0, st>>>(S[2].as<uint32_t>(), m, head);
+        int32_t* nseg_dev = c.d_scalars.as<int32_t>();
+        RIGC_TRY(exclusive_scan_i32(head, segid, m, nseg_dev, S[6], st));
+        k_seg_starts<<<grid_for(m, 256), 256, 0, st>>>(head, segid, m, segst);
+        int32_t nseg;
+        RIGC_CUDA(cudaMemcpyAsync(&nseg, nseg_dev, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+        RIGC_CUDA(cudaStreamSynchronize(st));
+        k_grad_sums<<<grid_for((int64_t)nseg * 6, 256), 256, 0, st>>>(
+            S[2].as<uint32_t>(), S[3].as<uint32_t>(), segst, nseg, m, c.c_grad.as<double>(),
+            c.grad.as<double>());
+    }
+    if (!with_hess) return RIGC_OK;
+    // ---- Hessian blocks
+    {
+        int64_t m = 4 * n;
+        RIGC_TRY(S[0].reserve(m * 8));
+        RIGC_TRY(S[1].reserve(m * 4));
+        RIGC_TRY(S[2].reserve(m * 8));
+        RIGC_TRY(S[3].reserve(m * 4));
+        RIGC_TRY(S[7].reserve(m * 12 + 16));
+        k_block_keys<<<grid_for(m, 256), 256, 0, st>>>(c.cons.bodies.as<int>(), n, nb,
+                                                      S[0].as<uint64_t>(), S[1].as<uint32_t>());
+        RIGC_TRY(radix_sort_pairs<uint64_t>(S[0].as<uint64_t>(), S[1].as<uint32_t>(),
+                                            S[2].as<uint64_t>(), S[3].as<uint32_t>(), m,
+                                            bits_for((uint64_t)nb * nb), S[4], S[5], S[6], st));
+        int32_t* head = S[7].as<int32_t>();
+        int32_t* segid = head + m;
+        int32_t* segst = segid + m;
+        k_heads<uint64_t><<<grid_for(m, 256), 256, 0, st>>>(S[2].as<uint64_t>(), m, head);
+        int32_t* nseg_dev = c.d_scalars.as<int32_t>();
+        RIGC_TRY(exclusive_scan_i32(head, segid, m, nseg_dev, S[6], st));
+        k_seg_starts<<<grid_for(m, 256), 256, 0, st>>>(head, segid, m, segst);
+        int32_t nseg;
+        RIGC_CUDA(cudaMemcpyAsync(&nseg, nseg_dev, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+        RIGC_CUDA(cudaStreamSynchronize(st));
+        RIGC_TRY(c.col.reserve((size_t)nseg * sizeof(int32_t)));
+        RIGC_TRY(c.val.reserve((size_t)nseg * 36 * sizeof(double)));
+        k_block_sums<<<grid_for((int64_t)nseg * 36, 256), 256, 0, st>>>(
+            S[2].as<uint64_t>(), S[3].as<uint32_t>(), segst, nseg, m, c.c_blocks.as<double>(), nb,
+            c.col.as<int32_t>(), c.val.as<double>(), c.row_ptr.as<int32_t>() + 1);
+        // row counts -> row_ptr (exclusive scan of counts shifted by one)
+        int32_t* rp = c.row_ptr.as<int32_t>();
+        RIGC_TRY(S[4].reserve((size_t)(nb + 1) * sizeof(int32_t)));
+        RIGC_CUDA(cudaMemcpyAsync(S[4].ptr, rp + 1, (size_t)nb * sizeof(int32_t),
+                                  cudaMemcpyDeviceToDevice, st));
+        RIGC_TRY(exclusive_scan_i32(S[4].as<int32_t>(), rp, nb, rp + nb, S[6], st));
+        c.nnzb = nseg;
+    }
+    return RIGC_OK;
+}
+
+} // namespace rigc

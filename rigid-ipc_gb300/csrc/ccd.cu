@@ -1,0 +1,330 @@
+// Conservative rigid-trajectory interval CCD over EE and FV candidates.
+//
+// Replaces compute_earliest_toi_narrow_phase
+// (src/opt/distance_barrier_constraint.cpp:151-265) with trajectory RIGID:
+// compute_edge_edge_time_of_impact / compute_face_vertex_time_of_impact
+// (src/ccd/rigid/time_of_impact.cpp:158-310) over the interval point
+// functions of src/ccd/rigid/rigid_trajectory_aabb.cpp:7-103, searched by the
+// branch and bound of src/interval/interval_root_finder.cpp:97-203:
+//  * boxes (t, alpha, beta) / (t, u, v) start at [0, 1]^3;
+//  * if f([0, tol]) contains zero the time tolerance shrinks 100x;
+//  * a box is skipped when its t.lo is not before the earliest root found,
+//    when (FV) u + v misses [0, 1], or when f(box) excludes zero;
+//  * a box within tolerance (and with t.lo > 0 or all widths <= 1e-10)
+//    becomes the new earliest root; otherwise it is split at the midpoint of
+//    the dimension with the largest width / tolerance, second half pushed
+//    first.
+// The time of impact of a candidate (the t.lo of its earliest root box) does
+// not depend on the order boxes are visited, so boxes whose t.lo is not below
+// the running minimum over all candidates can be skipped too: that never
+// changes the minimum.  One thread per candidate, a depth-first stack in
+// local memory, the interval vertex positions cached per time interval.  Every
+// stack and every search is bounded: on overflow or budget exhaustion the
+// candidate reports the smallest t.lo still unexplored (a conservative time
+// of impact) and an error status.
+#include "common.cuh"
+#include "interval.cuh"
+
+namespace rigc {
+
+constexpr int kCCDStack = 128;
+constexpr int kCCDThreads = 128;
+
+struct CCDArgs {
+    const double* rest;
+    const int* edges;
+    const int* faces;
+    const int* f2e;
+    const int* vbody;
+    const int* ebody;
+    const int* fbody;
+    const double* edge_len;
+    const double* x0;
+    const double* x1;
+    const int2* ee;
+    const int2* fv;
+    int64_t nee, nfv;
+    double toi_tol;
+    int prune;
+    long long max_boxes;
+    unsigned long long* gmin;   // running minimum time of impact (double bits)
+    double* per;                // optional per-candidate result
+    int* status;                // worst status
+    unsigned long long* boxes;  // total boxes evaluated
+    unsigned long long* hits;   // candidates with an impact
+};
+
+struct Box {
+    double t0, t1, a0, a1, b0, b1;
+};
+
+struct BodyTraj {
+    double x0[6];
+    Itv dx[6];  // I(x1) - I(x0)
+};
+
+__device__ __forceinline__ void load_traj(const double* x0, const double* x1, int b, BodyTraj& T)
+{
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        double a = x0[6 * b + k], c = x1[6 * b + k];
+        T.x0[k] = a;
+        T.dx[k] = Itv { sub_dn(c, a), sub_up(c, a) };
+    }
+}
+
+// R(t), p(t) of a body over the time interval t
+__device__ __forceinline__ void body_at(const BodyTraj& T, const Itv& t, Itv R[9], Itv p[3])
+{
+    Itv r[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        p[k] = iadd(imul(T.dx[k], t), pt(T.x0[k]));
+        r[k] = iadd(imul(T.dx[3 + k], t), pt(T.x0[3 + k]));
+    }
+    irotation(r, R);
+}
+
+struct Query {
+    bool fv;            // face-vertex (else edge-edge)
+    double v[4][3];     // rest vertices: EE (a0, a1, b0, b1); FV (v, f0, f1, f2)
+    BodyTraj A, B;      // EE: edge a / edge b bodies; FV: vertex / face bodies
+    // cached vertex intervals for one time interval
+    double ct0, ct1;
+    Itv P[4][3];
+};
+
+__device__ __noinline__ void eval_vertices(Query& q, const Itv& t)
+{
+    Itv R[9], p[3];
+    body_at(q.A, t, R, p);
+    if (q.fv) {
+        iworld_vertex(R, p, q.v[0], q.P[0]);
+        body_at(q.B, t, R, p);
+        iworld_vertex(R, p, q.v[1], q.P[1]);
+        iworld_vertex(R, p, q.v[2], q.P[2]);
+        iworld_vertex(R, p, q.v[3], q.P[3]);
+    } else {
+        iworld_vertex(R, p, q.v[0], q.P[0]);
+        iworld_vertex(R, p, q.v[1], q.P[1]);
+        body_at(q.B, t, R, p);
+        iworld_vertex(R, p, q.v[2], q.P[2]);
+        iworld_vertex(R, p, q.v[3], q.P[3]);
+    }
+    q.ct0 = t.lo;
+    q.ct1 = t.hi;
+}
+
+// zero in f(box)?
+__device__ __forceinline__ bool f_contains_zero(Query& q, const Box& x)
+{
+    Itv t { x.t0, x.t1 };
+    if (!(x.t0 == q.ct0 && x.t1 == q.ct1)) eval_vertices(q, t);
+    Itv a { x.a0, x.a1 }, b { x.b0, x.b1 };
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        Itv y;
+        if (q.fv) {
+            Itv fp = iadd(iadd(imul(isub(q.P[2][j], q.P[1][j]), a), imul(isub(q.P[3][j], q.P[1][j]), b)),
+                          q.P[1][j]);
+            y = isub(q.P[0][j], fp);
+        } else {
+            Itv ea = iadd(imul(isub(q.P[1][j], q.P[0][j]), a), q.P[0][j]);
+            Itv eb = iadd(imul(isub(q.P[3][j], q.P[2][j]), b), q.P[2][j]);
+            y = isub(ea, eb);
+        }
+        if (!zero_in(y)) return false;
+    }
+    return true;
+}
+
+__global__ void __launch_bounds__(kCCDThreads)
+k_ccd(CCDArgs a)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t n = a.nee + a.nfv;
+    bool active = i < n;
+    double toi = INFINITY;
+    bool found = false;
+    unsigned long long nboxes = 0;
+    int status = RIGC_OK;
+    if (active) {
+        Query q;
+        double tol[3];
+        q.ct0 = q.ct1 = __longlong_as_double(0x7ff8000000000000ll);
+        if (i < a.nee) {
+            q.fv = false;
+            int ea = a.ee[i].x, eb = a.ee[i].y;
+            int va[2] = { a.edges[2 * ea], a.edges[2 * ea + 1] };
+            int vb[2] = { a.edges[2 * eb], a.edges[2 * eb + 1] };
+            for (int j = 0; j < 3; j++) {
+                q.v[0][j] = a.rest[3 * (size_t)va[0] + j];
+                q.v[1][j] = a.rest[3 * (size_t)va[1] + j];
+                q.v[2][j] = a.rest[3 * (size_t)vb[0] + j];
+                q.v[3][j] = a.rest[3 * (size_t)vb[1] + j];
+            }
+            load_traj(a.x0, a.x1, a.ebody[ea], q.A);
+            load_traj(a.x0, a.x1, a.ebody[eb], q.B);
+            tol[1] = RDIV(1e-4, a.edge_len[ea]);
+            tol[2] = RDIV(1e-4, a.edge_len[eb]);
+        } else {
+            q.fv = true;
+            int64_t k = i - a.nee;
+            int f = a.fv[k].x, v = a.fv[k].y;
+            int fvx[3] = { a.faces[3 * f], a.faces[3 * f + 1], a.faces[3 * f + 2] };
+            for (int j = 0; j < 3; j++) {
+                q.v[0][j] = a.rest[3 * (size_t)v + j];
+                q.v[1][j] = a.rest[3 * (size_t)fvx[0] + j];
+                q.v[2][j] = a.rest[3 * (size_t)fvx[1] + j];
+                q.v[3][j] = a.rest[3 * (size_t)fvx[2] + j];
+            }
+            load_traj(a.x0, a.x1, a.vbody[v], q.A);
+            load_traj(a.x0, a.x1, a.fbody[f], q.B);
+            tol[1] = RDIV(1e-4, a.edge_len[a.f2e[3 * f]]);
+            tol[2] = RDIV(1e-4, a.edge_len[a.f2e[3 * f + 1]]);
+        }
+        tol[0] = a.toi_tol;
+        {
+            Box xt { 0.0, tol[0], 0.0, tol[1], 0.0, tol[2] };
+            if (f_contains_zero(q, xt)) tol[0] = RDIV(tol[0], 1e2);
+        }
+        Box stack[kCCDStack];
+        int sp = 0;
+        stack[sp++] = Box { 0.0, 1.0, 0.0, 1.0, 0.0, 1.0 };
+        double earliest = INFINITY;
+        double gbound = INFINITY;
+        while (sp > 0) {
+            Box x = stack[--sp];
+            if (x.t0 >= earliest) continue;
+            if (a.prune) {
+                if ((nboxes & 7) == 0) gbound = __longlong_as_double(
+                    (long long)*(volatile unsigned long long*)a.gmin);
+                if (x.t0 >= gbound) continue;
+            }
+            if (q.fv) {
+                double sl = add_dn(x.a0, x.b0), sh = add_up(x.a1, x.b1);
+                if (!(sl <= 1.0 && 0.0 <= sh)) continue;
+            }
+            if (nboxes >= (unsigned long long)a.max_boxes) {
+                // budget exhausted: earliest unexplored t.lo is conservative
+                double m = x.t0;
+                for (int s = 0; s < sp; s++) m = smin(m, stack[s].t0);
+                earliest = smin(earliest, m);
+                found = true;
+                status = RIGC_ERR_ITER_LIMIT;
+                break;
+            }
+            nboxes++;
+            if (!f_contains_zero(q, x)) continue;
+            double w[3] = { sub_up(x.t1, x.t0), sub_up(x.a1, x.a0), sub_up(x.b1, x.b0) };
+            bool all_tol = w[0] <= tol[0] && w[1] <= tol[1] && w[2] <= tol[2];
+            bool all_zero = w[0] <= 1e-10 && w[1] <= 1e-10 && w[2] <= 1e-10;
+            if ((x.t0 > 0 || all_zero) && all_tol) {
+                earliest = x.t0;
+                found = true;
+                if (a.prune) {
+                    atomicMin(a.gmin, (unsigned long long)__double_as_longlong(earliest));
+                    gbound = smin(gbound, earliest);
+                }
+                continue;
+            }
+            int split = -1;
+#pragma unroll
+            for (int d = 0; d < 3; d++)
+                if ((all_tol || w[d] > tol[d])
+                    && (split == -1 || RMUL(w[d], tol[split]) > RMUL(w[split], tol[d])))
+                    split = d;
+            Box lo = x, hi = x;
+            if (split == 0) {
+                double m = RMUL(0.5, RADD(x.t0, x.t1));
+                lo.t1 = m;
+                hi.t0 = m;
+            } else if (split == 1) {
+                double m = RMUL(0.5, RADD(x.a0, x.a1));
+                lo.a1 = m;
+                hi.a0 = m;
+            } else {
+                double m = RMUL(0.5, RADD(x.b0, x.b1));
+                lo.b1 = m;
+                hi.b0 = m;
+            }
+            if (sp + 2 > kCCDStack) {
+                // cannot descend: keep the box's start as a conservative root
+                earliest = smin(earliest, x.t0);
+                found = true;
+                status = RIGC_ERR_QUEUE_OVERFLOW;
+                continue;
+            }
+            stack[sp++] = hi;
+            stack[sp++] = lo;
+        }
+        toi = found ? earliest : INFINITY;
+        if (found && a.prune)
+            atomicMin(a.gmin, (unsigned long long)__double_as_longlong(toi));
+        if (a.per) a.per[i] = toi;
+        if (status != RIGC_OK) atomicMax(a.status, status);
+    }
+    // block-wide counters
+    unsigned long long b = nboxes, h = found ? 1ull : 0ull;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        b += __shfl_down_sync(0xffffffffu, b, o);
+        h += __shfl_down_sync(0xffffffffu, h, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (b) atomicAdd(a.boxes, b);
+        if (h) atomicAdd(a.hits, h);
+    }
+}
+
+// counters layout in the context's device scalars (after 16 ints):
+// [0] gmin bits, [1] boxes, [2] hits, [3] status
+int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flags,
+            double* toi_host, double* per)
+{
+    cudaStream_t st = c.stream;
+    const int64_t n = c.cand.num_ee + c.cand.num_fv;
+    unsigned long long* cnt = reinterpret_cast<unsigned long long*>(c.d_scalars.as<char>() + 256);
+    unsigned long long init[4] = { (unsigned long long)0x7ff0000000000000ull, 0, 0, 0 };
+    RIGC_CUDA(cudaMemcpyAsync(cnt, init, sizeof(init), cudaMemcpyHostToDevice, st));
+    if (n > 0) {
+        CCDArgs a;
+        a.rest = c.s.rest;
+        a.edges = c.s.edges;
+        a.faces = c.s.faces;
+        a.f2e = c.s.f2e;
+        a.vbody = c.s.vbody;
+        a.ebody = c.s.ebody;
+        a.fbody = c.s.fbody;
+        a.edge_len = c.s.edge_len;
+        a.x0 = x0;
+        a.x1 = x1;
+        a.ee = c.cand.ee.as<int2>();
+        a.fv = c.cand.fv.as<int2>();
+        a.nee = c.cand.num_ee;
+        a.nfv = c.cand.num_fv;
+        a.toi_tol = toi_tol;
+        a.prune = (flags & RIGC_TOI_NO_PRUNE) ? 0 : 1;
+        a.max_boxes = 1ll << 22;
+        a.gmin = cnt;
+        a.per = per;
+        a.status = reinterpret_cast<int*>(cnt + 3);
+        a.boxes = cnt + 1;
+        a.hits = cnt + 2;
+        k_ccd<<<grid_for(n, kCCDThreads), kCCDThreads, 0, st>>>(a);
+        RIGC_CUDA(cudaGetLastError());
+    }
+    unsigned long long out[4];
+    RIGC_CUDA(cudaMemcpyAsync(out, cnt, sizeof(out), cudaMemcpyDeviceToHost, st));
+    RIGC_CUDA(cudaStreamSynchronize(st));
+    double g = __builtin_bit_cast(double, out[0]);
+    *toi_host = out[2] ? g : INFINITY;
+    c.stats.ccd_boxes = (int64_t)out[1];
+    c.stats.ccd_candidates = n;
+    c.stats.ccd_collisions = (int64_t)out[2];
+    int status = (int)(out[3] & 0xffffffffu);
+    c.stats.last_status = status;
+    return status;
+}
+
+} // namespace rigc

@@ -1,0 +1,148 @@
+// Shared definitions of the rigc CUDA library: context, device buffers,
+// error handling and small device helpers.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/rigc.h"
+
+namespace rigc {
+
+constexpr int kNumSMs = 152;  // GB300: 2 dies x 76 SMs
+
+// ---------------------------------------------------------------------------
+// error handling: every host function returns an int status; CUDA failures
+// are recorded in the context and surface as RIGC_ERR_CUDA / RIGC_ERR_OOM.
+
+struct Status {
+    int code = RIGC_OK;
+    std::string msg;
+};
+
+#define RIGC_CUDA(expr)                                                       \
+    do {                                                                      \
+        cudaError_t _e = (expr);                                              \
+        if (_e != cudaSuccess) {                                              \
+            ::rigc::set_error(_e == cudaErrorMemoryAllocation ? RIGC_ERR_OOM  \
+                                                             : RIGC_ERR_CUDA, \
+                              cudaGetErrorString(_e), __FILE__, __LINE__);    \
+            return _e == cudaErrorMemoryAllocation ? RIGC_ERR_OOM             \
+                                                   : RIGC_ERR_CUDA;           \
+        }                                                                     \
+    } while (0)
+
+#define RIGC_TRY(expr)                                                        \
+    do {                                                                      \
+        int _s = (expr);                                                      \
+        if (_s != RIGC_OK) return _s;                                         \
+    } while (0)
+
+void set_error(int code, const char* what, const char* file, int line);
+
+// grow-only device buffer
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    int reserve(size_t n)
+    {
+        if (n <= bytes) return RIGC_OK;
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+        size_t want = n + n / 4 + 256;
+        cudaError_t e = cudaMalloc(&ptr, want);
+        if (e != cudaSuccess) {
+            set_error(RIGC_ERR_OOM, cudaGetErrorString(e), __FILE__, __LINE__);
+            return RIGC_ERR_OOM;
+        }
+        bytes = want;
+        return RIGC_OK;
+    }
+    template <class T> T* as() const { return static_cast<T*>(ptr); }
+    void release()
+    {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// context
+
+struct Scene {
+    int nb = 0, nv = 0, ne = 0, nf = 0;
+    double avg_edge_len = 0;
+    // device arrays
+    double* rest = nullptr;        // nv x 3
+    int* edges = nullptr;          // ne x 2
+    int* faces = nullptr;          // nf x 3
+    int* f2e = nullptr;            // nf x 3
+    int* bvs = nullptr;            // nb + 1
+    int* bes = nullptr;
+    int* bfs = nullptr;
+    int* group = nullptr;          // nb
+    int* type = nullptr;           // nb
+    double* rmax = nullptr;        // nb
+    int* vbody = nullptr;          // nv
+    int* ebody = nullptr;          // ne
+    int* fbody = nullptr;          // nf
+    double* edge_len = nullptr;    // ne
+    // host copies of the prefix arrays
+    std::vector<int> h_bvs, h_type;
+    int max_body_vertices = 0;
+};
+
+struct Candidates {
+    int64_t num_ee = 0, num_fv = 0;
+    DevBuf ee, fv;  // int2
+};
+
+struct Constraints {
+    int64_t num = 0, num_vv = 0, num_ev = 0, num_ee = 0, num_fv = 0;
+    DevBuf type, verts, prims, bodies, weight, eps;
+};
+
+struct Ctx {
+    Scene s;
+    cudaStream_t stream = 0;
+    Candidates cand;
+    Constraints cons;
+    rigc_stats stats {};
+    // barrier outputs
+    DevBuf frames;        // per body rotation frame (R, dR, d2R)
+    DevBuf c_energy, c_grad, c_blocks;
+    DevBuf grad, row_ptr, col, val;
+    int64_t nnzb = 0;
+    // scratch
+    DevBuf scratch[8];
+    DevBuf host_pinned_dummy;
+    DevBuf d_scalars;     // small device scalars (reductions, counters)
+    double* h_scalars = nullptr;  // pinned host mirror
+    // broad-phase buffers
+    DevBuf body_box, body_in, vbox, ebox, fbox, vin, ein, fin;
+    DevBuf items_key, items_val, items_key2, items_val2, seg, pair_out, pair_key;
+    DevBuf large_list;
+    // temporary pose buffers for host entry points
+    DevBuf x0_dev, x1_dev;
+};
+
+Ctx* ctx_of(rigc_ctx* c);
+
+// ---------------------------------------------------------------------------
+// launch helpers
+
+inline unsigned grid_for(int64_t n, int block)
+{
+    int64_t g = (n + block - 1) / block;
+    if (g < 1) g = 1;
+    if (g > 0x7fffffff) g = 0x7fffffff;
+    return (unsigned)g;
+}
+
+} // namespace rigc

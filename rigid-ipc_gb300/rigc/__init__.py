@@ -1,0 +1,237 @@
+"""rigc: the GB300 (sm_103a) Rigid IPC narrow phase, Python front end.
+
+The compute path is the CUDA library behind the C ABI of ``include/rigc.h``;
+this module only moves arrays.  Names follow the reference's interface
+(``detect_collision_candidates_rigid``, ``construct_constraint_set``,
+``compute_barrier_term``, ``compute_earliest_toi``) so the parity tests read
+like the reference's own.  Device memory comes from torch CUDA tensors.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import _lib as L
+from .scene import Scene  # noqa: F401
+
+__all__ = ["Context", "Scene", "L"]
+
+
+def _torch():
+    import torch
+
+    if not torch.cuda.is_available():
+        raise RuntimeError("rigc needs a CUDA device")
+    return torch
+
+
+class Context:
+    """One scene on one GPU (a RigidBodyAssembler plus its device buffers)."""
+
+    def __init__(self, scene: Scene, stream=None):
+        self.lib = L.load()
+        self.scene = scene
+        torch = _torch()
+        self.torch = torch
+        self._keep = [
+            np.ascontiguousarray(scene.rest_vertices, dtype=np.float64),
+            np.ascontiguousarray(scene.edges, dtype=np.int32),
+            np.ascontiguousarray(scene.faces, dtype=np.int32),
+            np.ascontiguousarray(scene.faces_to_edges, dtype=np.int32),
+            np.ascontiguousarray(scene.body_vertex_start, dtype=np.int32),
+            np.ascontiguousarray(scene.body_edge_start, dtype=np.int32),
+            np.ascontiguousarray(scene.body_face_start, dtype=np.int32),
+            np.ascontiguousarray(scene.group_ids, dtype=np.int32),
+            np.ascontiguousarray(scene.body_type, dtype=np.int32),
+            np.ascontiguousarray(scene.r_max, dtype=np.float64),
+        ]
+        k = self._keep
+        d = L.SceneDesc()
+        d.num_bodies = scene.num_bodies
+        d.num_vertices = scene.num_vertices
+        d.num_edges = len(scene.edges)
+        d.num_faces = len(scene.faces)
+        d.rest_vertices = k[0].ctypes.data_as(L._d)
+        d.edges = k[1].ctypes.data_as(L._i32)
+        d.faces = k[2].ctypes.data_as(L._i32)
+        d.faces_to_edges = k[3].ctypes.data_as(L._i32)
+        d.body_vertex_start = k[4].ctypes.data_as(L._i32)
+        d.body_edge_start = k[5].ctypes.data_as(L._i32)
+        d.body_face_start = k[6].ctypes.data_as(L._i32)
+        d.group_ids = k[7].ctypes.data_as(L._i32)
+        d.body_types = k[8].ctypes.data_as(L._i32)
+        d.r_max = k[9].ctypes.data_as(L._d)
+        d.average_edge_length = scene.average_edge_length
+        h = C.c_void_p()
+        L.check(self.lib.rigc_ctx_create(C.byref(d), C.byref(h)), "rigc_ctx_create")
+        self.h = h
+        self._last_counts = (0, 0)
+        if stream is not None:
+            self.set_stream(stream)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.rigc_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream):
+        ptr = stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
+        L.check(self.lib.rigc_set_stream(self.h, C.c_void_p(ptr)), "rigc_set_stream")
+
+    # -- helpers ----------------------------------------------------------
+    def device(self, x):
+        """float64 CUDA tensor from numpy / tensor."""
+        t = self.torch
+        if isinstance(x, t.Tensor):
+            return x.to(device="cuda", dtype=t.float64).contiguous()
+        return t.as_tensor(np.ascontiguousarray(x, dtype=np.float64), device="cuda")
+
+    def copy_out(self, ptr, shape, dtype):
+        out = np.empty(shape, dtype=dtype)
+        if out.nbytes:
+            L.check(self.lib.rigc_copy(self.h, out.ctypes.data, C.c_void_p(ptr), out.nbytes),
+                    "rigc_copy")
+        return out
+
+    def stats(self):
+        s = L.Stats()
+        L.check(self.lib.rigc_get_stats(self.h, C.byref(s)), "rigc_get_stats")
+        return {f: getattr(s, f) for f, _ in L.Stats._fields_}
+
+    # -- reference-facing operations --------------------------------------
+    def world_vertices(self, x):
+        xd = self.device(x)
+        V = self.torch.empty((self.scene.num_vertices, 3), dtype=self.torch.float64, device="cuda")
+        L.check(self.lib.rigc_world_vertices(self.h, C.c_void_p(xd.data_ptr()),
+                                             C.c_void_p(V.data_ptr())), "rigc_world_vertices")
+        return V
+
+    def detect_collision_candidates_rigid(self, x0, x1=None, continuous=True, inflation=0.0):
+        """Hash-grid candidates; returns (ee, fv) as int32 numpy arrays."""
+        x0d = self.device(x0)
+        x1d = self.device(x0 if x1 is None else x1)
+        out = L.Candidates()
+        L.check(self.lib.rigc_detect_candidates(self.h, C.c_void_p(x0d.data_ptr()),
+                                                C.c_void_p(x1d.data_ptr()), int(continuous),
+                                                inflation, C.byref(out)),
+                "rigc_detect_candidates")
+        self._last_counts = (out.num_ee, out.num_fv)
+        ee = self.copy_out(out.ee, (out.num_ee, 2), np.int32)
+        fv = self.copy_out(out.fv, (out.num_fv, 2), np.int32)
+        return ee, fv
+
+    def earliest_toi(self, x0, x1, toi_tol=1e-4, prune=True, per_candidate=False):
+        """compute_earliest_toi_narrow_phase over the last continuous candidates."""
+        x0d, x1d = self.device(x0), self.device(x1)
+        toi = C.c_double()
+        per = None
+        s = self.stats()
+        n = s["cand_ee"] + s["cand_fv"]
+        if per_candidate:
+            per = self.torch.empty(max(n, 1), dtype=self.torch.float64, device="cuda")
+        flags = 0 if prune else L.RIGC_TOI_NO_PRUNE
+        st = self.lib.rigc_earliest_toi(self.h, C.c_void_p(x0d.data_ptr()),
+                                        C.c_void_p(x1d.data_ptr()), toi_tol, flags,
+                                        C.byref(toi),
+                                        C.c_void_p(per.data_ptr()) if per is not None else None)
+        L.check(st, "rigc_earliest_toi",
+                allow=(L.RIGC_ERR_QUEUE_OVERFLOW, L.RIGC_ERR_ITER_LIMIT))
+        if per_candidate:
+            return toi.value, per[:n].cpu().numpy(), st
+        return toi.value
+
+    def compute_earliest_toi(self, x0, x1, dmin=0.0):
+        """DistanceBarrierConstraint::compute_earliest_toi (broad + narrow)."""
+        x0d, x1d = self.device(x0), self.device(x1)
+        toi = C.c_double()
+        st = self.lib.rigc_compute_earliest_toi(self.h, C.c_void_p(x0d.data_ptr()),
+                                                C.c_void_p(x1d.data_ptr()), dmin, C.byref(toi))
+        L.check(st, "rigc_compute_earliest_toi",
+                allow=(L.RIGC_ERR_QUEUE_OVERFLOW, L.RIGC_ERR_ITER_LIMIT))
+        return toi.value
+
+    def construct_constraint_set(self, x, dhat, dmin=0.0):
+        """Returns the constraint arrays (numpy): type, verts, prims, bodies, weight, eps."""
+        xd = self.device(x)
+        v = L.ConstraintsView()
+        L.check(self.lib.rigc_construct_constraint_set(self.h, C.c_void_p(xd.data_ptr()), dhat,
+                                                       dmin, C.byref(v)),
+                "rigc_construct_constraint_set")
+        n = v.num
+        return dict(
+            type=self.copy_out(v.type, (n,), np.int32),
+            verts=self.copy_out(v.verts, (n, 4), np.int32),
+            prims=self.copy_out(v.prims, (n, 2), np.int32),
+            bodies=self.copy_out(v.bodies, (n, 2), np.int32),
+            weight=self.copy_out(v.weight, (n,), np.float64),
+            eps=self.copy_out(v.eps_x, (n,), np.float64),
+            counts=(v.num_vv, v.num_ev, v.num_ee, v.num_fv),
+        )
+
+    def set_constraints(self, types, verts, prims, bodies, weight, eps):
+        arrs = [np.ascontiguousarray(types, np.int32), np.ascontiguousarray(verts, np.int32),
+                np.ascontiguousarray(prims, np.int32), np.ascontiguousarray(bodies, np.int32),
+                np.ascontiguousarray(weight, np.float64), np.ascontiguousarray(eps, np.float64)]
+        L.check(self.lib.rigc_set_constraints(self.h, len(arrs[0]),
+                                              *[a.ctypes.data for a in arrs]),
+                "rigc_set_constraints")
+
+    def compute_barrier_term(self, x, dhat, dmin=0.0, grad=True, hess=True, project=True):
+        """Energy, gradient (6 nb) and BSR Hessian (row_ptr, col, val[nnzb, 6, 6])."""
+        xd = self.device(x)
+        flags = (L.RIGC_GRAD if grad else 0) | (L.RIGC_HESS if hess else 0) | \
+                (L.RIGC_PROJECT_PSD if project else 0)
+        o = L.BarrierOut()
+        L.check(self.lib.rigc_barrier_term(self.h, C.c_void_p(xd.data_ptr()), dhat, dmin, flags,
+                                           C.byref(o)), "rigc_barrier_term")
+        nb = self.scene.num_bodies
+        g = self.copy_out(o.grad, (6 * nb,), np.float64) if grad or hess else None
+        H = None
+        if hess:
+            H = (self.copy_out(o.row_ptr, (nb + 1,), np.int32),
+                 self.copy_out(o.col, (o.nnzb,), np.int32),
+                 self.copy_out(o.val, (o.nnzb, 6, 6), np.float64))
+        return o.energy, g, H
+
+    def barrier_local_terms(self, x, n, dhat, dmin=0.0, project=True):
+        torch = self.torch
+        xd = self.device(x)
+        e = torch.empty(max(n, 1), dtype=torch.float64, device="cuda")
+        g = torch.empty((max(n, 1), 12), dtype=torch.float64, device="cuda")
+        H = torch.empty((max(n, 1), 12, 12), dtype=torch.float64, device="cuda")
+        flags = L.RIGC_GRAD | L.RIGC_HESS | (L.RIGC_PROJECT_PSD if project else 0)
+        L.check(self.lib.rigc_barrier_local_terms(self.h, C.c_void_p(xd.data_ptr()), dhat, dmin,
+                                                  flags, C.c_void_p(e.data_ptr()),
+                                                  C.c_void_p(g.data_ptr()),
+                                                  C.c_void_p(H.data_ptr())),
+                "rigc_barrier_local_terms")
+        return e[:n].cpu().numpy(), g[:n].cpu().numpy(), H[:n].cpu().numpy()
+
+    def narrow_phase_host(self, x0, x1, dhat, dmin=0.0, nnzb_cap=None):
+        """One host-facing narrow-phase pass (host buffers in and out)."""
+        nb = self.scene.num_bodies
+        x0 = np.ascontiguousarray(x0, np.float64)
+        x1 = np.ascontiguousarray(x1, np.float64)
+        cap = nnzb_cap if nnzb_cap is not None else 64 * nb
+        grad = np.empty(6 * nb)
+        rp = np.empty(nb + 1, np.int32)
+        col = np.empty(cap, np.int32)
+        val = np.empty((cap, 6, 6))
+        toi, energy = C.c_double(), C.c_double()
+        nnzb = C.c_int64()
+        st = self.lib.rigc_narrow_phase_host(self.h, x0.ctypes.data, x1.ctypes.data, dhat, dmin,
+                                             C.byref(toi), C.byref(energy), grad.ctypes.data,
+                                             rp.ctypes.data, col.ctypes.data, val.ctypes.data,
+                                             cap, C.byref(nnzb))
+        L.check(st, "rigc_narrow_phase_host",
+                allow=(L.RIGC_ERR_QUEUE_OVERFLOW, L.RIGC_ERR_ITER_LIMIT))
+        k = nnzb.value
+        return toi.value, energy.value, grad, (rp, col[:k], val[:k]), k

@@ -1,0 +1,214 @@
+"""Parity of the CUDA path (through the C ABI) with the CPU oracle.
+
+Bars: candidate sets, constraint sets, world vertices and times of impact are
+bit-exact (integer / decision work and the same round-to-nearest operation
+order); barrier energy and gradient within 1e-10 relative, Hessians within
+1e-9 relative (Frobenius, per local 12x12 or per assembled block row).
+"""
+import math
+
+import numpy as np
+import pytest
+
+from test_oracle_pins import EE_Y1, EE_Z, FV_Y, FV_Z1, ee_case, fv_case
+
+pytestmark = pytest.mark.gpu
+
+ENERGY_RTOL = 1e-10
+GRAD_RTOL = 1e-10
+HESS_RTOL = 1e-9
+
+
+@pytest.fixture(scope="module")
+def ctx_c1(cube_scene):
+    import rigc
+
+    return rigc.Context(cube_scene)
+
+
+def _canon_constraints(types, verts, prims, bodies, weight, eps):
+    """Order constraints by (type, prim0, prim1); VV by (min, max) vertex."""
+    types = np.asarray(types)
+    verts = np.array(verts)
+    prims = np.array(prims)
+    bodies = np.array(bodies)
+    vv = types == 0
+    swap = vv & (verts[:, 0] > verts[:, 1])
+    verts[swap, 0], verts[swap, 1] = verts[swap, 1].copy(), verts[swap, 0].copy()
+    bodies[swap, 0], bodies[swap, 1] = bodies[swap, 1].copy(), bodies[swap, 0].copy()
+    prims[vv, 0], prims[vv, 1] = verts[vv, 0], verts[vv, 1]
+    order = np.lexsort((prims[:, 1], prims[:, 0], types))
+    return (types[order], verts[order], prims[order], bodies[order],
+            np.asarray(weight)[order], np.asarray(eps)[order])
+
+
+def test_world_vertices_bitexact(oracle, cube_scene, ctx_c1):
+    rng = np.random.default_rng(1)
+    o = oracle.OracleScene(cube_scene)
+    for _ in range(3):
+        x = cube_scene.poses() + rng.normal(0, 0.3, 6 * cube_scene.num_bodies)
+        Vg = ctx_c1.world_vertices(x).cpu().numpy()
+        Vo = o.world_vertices(x)
+        assert np.array_equal(Vg, Vo)
+
+
+@pytest.mark.parametrize("continuous", [False, True])
+def test_candidates_bitexact(oracle, cube_scene, cube_contact, ctx_c1, continuous):
+    o = oracle.OracleScene(cube_scene)
+    x0 = cube_contact
+    x1 = cube_scene.predictor_poses(x0) if continuous else x0
+    infl = 0.0 if continuous else 5e-4
+    ee_g, fv_g = ctx_c1.detect_collision_candidates_rigid(x0, x1, continuous, infl)
+    ee_o, fv_o = o.detect_candidates(x0, x1, continuous, infl)
+    ee_b, fv_b = o.detect_candidates(x0, x1, continuous, infl, brute=True)
+    assert len(ee_o) > 0 and len(fv_o) > 0
+    assert np.array_equal(ee_o, ee_b) and np.array_equal(fv_o, fv_b)
+    assert np.array_equal(ee_g, ee_o)
+    assert np.array_equal(fv_g, fv_o)
+
+
+def test_constraint_set_bitexact(oracle, cube_scene, cube_contact, ctx_c1):
+    dhat = 1e-3
+    o = oracle.OracleScene(cube_scene)
+    ee, fv = o.detect_candidates(cube_contact, continuous=False, inflation=dhat / 2)
+    co = o.constraint_set(cube_contact, ee, fv, dhat)
+    cg = ctx_c1.construct_constraint_set(cube_contact, dhat)
+    assert len(co) > 0
+    a = _canon_constraints(co.types, co.verts, co.prims, co.bodies, co.weight, co.eps)
+    b = _canon_constraints(cg["type"], cg["verts"], cg["prims"], cg["bodies"], cg["weight"],
+                           cg["eps"])
+    for u, v in zip(a, b):
+        assert np.array_equal(u, v)
+
+
+def _rel_err(a, b):
+    scale = max(np.abs(b).max(), 1e-300)
+    return np.abs(a - b).max() / scale
+
+
+@pytest.mark.parametrize("project", [False, True])
+def test_barrier_local_terms(oracle, cube_scene, cube_contact, ctx_c1, project):
+    dhat = 1e-3
+    o = oracle.OracleScene(cube_scene)
+    ee, fv = o.detect_candidates(cube_contact, continuous=False, inflation=dhat / 2)
+    cs = o.constraint_set(cube_contact, ee, fv, dhat)
+    ctx_c1.set_constraints(cs.types, cs.verts, cs.prims, cs.bodies, cs.weight, cs.eps)
+    e_o, g_o, H_o = o.local_terms(cube_contact, cs, dhat, project=project)
+    e_g, g_g, H_g = ctx_c1.barrier_local_terms(cube_contact, len(cs), dhat, project=project)
+    for i in range(len(cs)):
+        assert abs(e_g[i] - e_o[i]) <= ENERGY_RTOL * abs(e_o[i])
+        assert _rel_err(g_g[i], g_o[i]) <= GRAD_RTOL
+        assert np.linalg.norm(H_g[i] - H_o[i]) <= HESS_RTOL * np.linalg.norm(H_o[i])
+
+
+def test_barrier_term_assembled(oracle, cube_scene, cube_contact, ctx_c1):
+    dhat = 1e-3
+    o = oracle.OracleScene(cube_scene)
+    ee, fv = o.detect_candidates(cube_contact, continuous=False, inflation=dhat / 2)
+    cs = o.constraint_set(cube_contact, ee, fv, dhat)
+    e_o, g_o, (rp_o, col_o, val_o) = o.barrier_term(cube_contact, cs, dhat)
+    # the GPU builds its own constraint set (bit-exact with the oracle's)
+    ctx_c1.construct_constraint_set(cube_contact, dhat)
+    e_g, g_g, (rp_g, col_g, val_g) = ctx_c1.compute_barrier_term(cube_contact, dhat)
+    assert abs(e_g - e_o) <= ENERGY_RTOL * abs(e_o)
+    assert _rel_err(g_g, g_o) <= GRAD_RTOL
+    assert np.array_equal(rp_g, rp_o) and np.array_equal(col_g, col_o)
+    for r in range(len(rp_o) - 1):
+        blk_o = val_o[rp_o[r]:rp_o[r + 1]]
+        blk_g = val_g[rp_o[r]:rp_o[r + 1]]
+        if blk_o.size:
+            assert np.linalg.norm(blk_g - blk_o) <= HESS_RTOL * max(np.linalg.norm(blk_o), 1e-300)
+
+
+def _gpu_toi_case(sc, x0, x1, tol=1e-6):
+    import rigc
+
+    ctx = rigc.Context(sc)
+    ctx.detect_collision_candidates_rigid(x0, x1, True, 0.0)
+    toi, per, st = ctx.earliest_toi(x0, x1, toi_tol=tol, prune=False, per_candidate=True)
+    return ctx, toi, per
+
+
+@pytest.mark.parametrize("z", EE_Z)
+@pytest.mark.parametrize("sign", [-1, 1])
+@pytest.mark.parametrize("y_t1", [1.0, 0.1, 0.0, -1e-6, -2, -1000])
+def test_gpu_edge_edge_toi_analytic(oracle, z, sign, y_t1):
+    sc, x0, x1, expected, hit = ee_case(z, sign, y_t1)
+    import rigc
+
+    ctx = rigc.Context(sc)
+    o = oracle.OracleScene(sc)
+    ee_g, fv_g = ctx.detect_collision_candidates_rigid(x0, x1, True, 0.0)
+    ee_o, fv_o = o.detect_candidates(x0, x1, True, 0.0)
+    assert np.array_equal(ee_g, ee_o) and np.array_equal(fv_g, fv_o)
+    toi_g = ctx.earliest_toi(x0, x1, toi_tol=1e-6, prune=False)
+    if len(ee_g):
+        is_hit_o, toi_o, _ = o.edge_edge_toi(x0, x1, 0, 1, bound=1.0, tol=1e-6)
+        assert is_hit_o == hit
+        assert math.isinf(toi_g) == (not is_hit_o)
+        if is_hit_o:
+            assert toi_g == toi_o
+            assert toi_g <= expected
+    else:
+        assert not hit
+
+
+@pytest.mark.parametrize("y", FV_Y)
+@pytest.mark.parametrize("z_t1", FV_Z1)
+def test_gpu_face_vertex_toi_analytic(oracle, y, z_t1):
+    sc, x0, x1, expected, hit = fv_case(y, z_t1)
+    import rigc
+
+    ctx = rigc.Context(sc)
+    o = oracle.OracleScene(sc)
+    ee_g, fv_g = ctx.detect_collision_candidates_rigid(x0, x1, True, 0.0)
+    toi_g, per, st = ctx.earliest_toi(x0, x1, toi_tol=1e-6, prune=False, per_candidate=True)
+    _, toi_min, _ = o.earliest_toi(x0, x1, ee_g, fv_g, tol=1e-6, per_candidate=True)
+    assert toi_g == toi_min
+    if hit:
+        assert toi_g <= expected
+        assert toi_g == pytest.approx(expected, abs=1e-4)
+
+
+def test_ccd_per_candidate_bitexact(oracle, cube_scene, cube_contact, ctx_c1):
+    x0 = cube_contact
+    x1 = cube_scene.predictor_poses(x0)
+    o = oracle.OracleScene(cube_scene)
+    ee, fv = ctx_c1.detect_collision_candidates_rigid(x0, x1, True, 0.0)
+    toi_o, per_o, _ = o.earliest_toi(x0, x1, ee, fv, per_candidate=True, nthreads=8)
+    toi_g, per_g, st = ctx_c1.earliest_toi(x0, x1, prune=False, per_candidate=True)
+    assert st == 0
+    assert np.array_equal(per_g, per_o)
+    assert toi_g == toi_o
+    # pruned search: same earliest time of impact
+    toi_p = ctx_c1.earliest_toi(x0, x1, prune=True)
+    assert toi_p == toi_o
+    assert ctx_c1.compute_earliest_toi(x0, x1) == toi_o
+
+
+def test_narrow_phase_host_matches_device(cube_scene, cube_contact, ctx_c1):
+    x0 = cube_contact
+    x1 = cube_scene.predictor_poses(x0)
+    dhat = 1e-3
+    toi, energy, grad, (rp, col, val), nnzb = ctx_c1.narrow_phase_host(x0, x1, dhat)
+    assert toi == ctx_c1.compute_earliest_toi(x0, x1)
+    ctx_c1.construct_constraint_set(x0, dhat)
+    e2, g2, (rp2, col2, val2) = ctx_c1.compute_barrier_term(x0, dhat)
+    assert energy == e2 and np.array_equal(grad, g2)
+    assert np.array_equal(rp, rp2) and np.array_equal(col, col2) and np.array_equal(val, val2)
+
+
+def test_error_statuses(cube_scene, ctx_c1):
+    import ctypes as C
+
+    import rigc
+    from rigc import _lib as L
+
+    lib = L.load()
+    assert lib.rigc_ctx_create(None, None) == L.RIGC_ERR_ARG
+    assert lib.rigc_barrier_term(ctx_c1.h, None, 1e-3, 0.0, 3, None) == L.RIGC_ERR_ARG
+    x = cube_scene.poses()
+    x[3] = np.nan
+    with pytest.raises(L.RigcError) as e:
+        ctx_c1.narrow_phase_host(x, x, 1e-3)
+    assert e.value.status == L.RIGC_ERR_NAN
