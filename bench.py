@@ -1,0 +1,341 @@
+"""Benchmark of the GB300 Rigid IPC narrow phase.
+
+One step = one narrow-phase pass of a Newton iteration on the large plain
+scene (1000 subdivision-3 icospheres, radii U[0.3, 0.6] m, over a static
+floor; dhat = 1e-3, dt = 0.01): continuous hash-grid broad phase between the
+current poses and the poses after one explicit step of the seeded velocities
+(v ~ N(0, 1), omega ~ N(0, 2)), rigid interval CCD over every candidate,
+discrete broad phase at the current poses, constraint set, barrier energy,
+gradient and PSD-projected 12x12 pair Hessians, and the block-sparse
+assembly.  The poses are a seeded contact-rich pile (bounding-sphere
+relaxation, 2e-4 m gaps) standing in for the settled state of that scene.
+
+value: candidate pairs per second = (continuous candidates through the CCD
++ discrete candidates through the constraint set / barrier) / step time, with
+inputs resident in HBM; e2e: the same through rigc_narrow_phase_host from
+host buffers (pose upload and gradient / Hessian download inside the timed
+region).  L2 is flushed (a 512 MiB write) before every timed step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, "rigid-ipc_gb300"), os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "candidate pairs/s (CCD+barrier grad/Hess)"
+UNIT = "pairs/s"
+CCD_BYTES_PER_PAIR = 304        # ids + 4 rest vertices + 4 poses + toi
+BARRIER_BYTES_PER_CONSTRAINT = 1456
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="rigc", choices=["rigc", "reference"])
+    ap.add_argument("--bodies", type=int, default=1000)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def make_workload(n_bodies, seed):
+    from rigc import scene as S
+
+    spec = S.spec_icospheres(seed=seed, n=n_bodies)
+    sc = S.scene_from_json(spec)
+    x0 = S.packed_pile_poses(sc, seed=seed)
+    x1 = sc.predictor_poses(x0)
+    return sc, x0, x1
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons while running."""
+
+    def __init__(self):
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
+                 f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, ValueError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([s.strip() for s in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for s in self.samples:
+            for i, n in enumerate(names):
+                if len(s) > 4 + i and s[4 + i].lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(self.samples)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_baseline(sc, x0, x1, dhat, budget_s=15.0):
+    """The oracle (a port of the reference's CPU path) on a bounded sample of
+    the same workload, on every host core."""
+    import oracle as O
+
+    O.build()
+    o = O.OracleScene(sc)
+    nthreads = os.cpu_count() or 1
+    ee, fv = o.detect_candidates(x0, x1, True, 0.0)
+    rng = np.random.default_rng(0)
+    # sample candidates until the time budget is spent (at least 256)
+    n_ee, n_fv = len(ee), len(fv)
+    take = 4096
+    t_ccd, done = 0.0, 0
+    while t_ccd < budget_s / 2 and done < n_ee + n_fv:
+        sel = rng.choice(n_ee + n_fv, size=min(take, n_ee + n_fv), replace=False)
+        e_s = ee[sel[sel < n_ee]]
+        f_s = fv[sel[sel >= n_ee] - n_ee]
+        t = time.perf_counter()
+        o.earliest_toi(x0, x1, e_s, f_s, nthreads=nthreads)
+        t_ccd += time.perf_counter() - t
+        done += len(sel)
+        take *= 2
+    ccd_rate = done / t_ccd
+    # constraint set + barrier on the discrete candidates
+    t = time.perf_counter()
+    ee_d, fv_d = o.detect_candidates(x0, continuous=False, inflation=dhat / 2)
+    t_bp = time.perf_counter() - t
+    sel = slice(0, min(len(ee_d), 20000))
+    self_fv = slice(0, min(len(fv_d), 20000))
+    t = time.perf_counter()
+    cs = o.constraint_set(x0, ee_d[sel], fv_d[self_fv], dhat)
+    o.barrier_term(x0, cs, dhat)
+    t_bar = time.perf_counter() - t
+    n_bar = len(ee_d[sel]) + len(fv_d[self_fv])
+    bar_rate = n_bar / t_bar
+    return {"ccd_pairs_per_s": ccd_rate, "barrier_pairs_per_s": bar_rate,
+            "broad_phase_s": t_bp, "cores": nthreads,
+            "sample": f"{done} CCD candidates ({nthreads} threads), {n_bar} discrete "
+                      f"candidates through constraint set + barrier (1 thread)"}
+
+
+def combined_rate(n_ccd, n_disc, ccd_rate, bar_rate):
+    t = n_ccd / ccd_rate + n_disc / bar_rate
+    return (n_ccd + n_disc) / t
+
+
+def run_reference(args):
+    """The CPU path of the reference restated (oracle) on the machine's cores."""
+    if args.gpus > 1 and int(os.environ.get("RANK", "0")) != 0:
+        return
+    sc, x0, x1 = make_workload(args.bodies, args.seed)
+    import oracle as O
+
+    O.build()
+    o = O.OracleScene(sc)
+    dhat = sc.dhat
+    ee, fv = o.detect_candidates(x0, x1, True, 0.0)
+    ee_d, fv_d = o.detect_candidates(x0, continuous=False, inflation=dhat / 2)
+    n_ccd, n_disc = len(ee) + len(fv), len(ee_d) + len(fv_d)
+    vals = []
+    for s in range(args.warmup + args.steps):
+        base = cpu_baseline(sc, x0, x1, dhat, budget_s=6.0)
+        if s >= args.warmup:
+            vals.append(combined_rate(n_ccd, n_disc, base["ccd_pairs_per_s"],
+                                      base["barrier_pairs_per_s"]))
+    v = statistics.median(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": (n_ccd + n_disc) / v * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{args.bodies} icospheres (subdivision 3) contact pile, one "
+                               "narrow-phase pass", "ccd_candidates": n_ccd,
+                   "discrete_candidates": n_disc},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": base["cores"], "kind": "port",
+                         "sample": base["sample"]},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    import torch
+
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+    import rigc
+
+    sc, x0, x1 = make_workload(args.bodies, args.seed + rank)
+    dhat = sc.dhat
+    ctx = rigc.Context(sc)
+    x0d, x1d = ctx.device(x0), ctx.device(x1)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def step():
+        toi = ctx.compute_earliest_toi(x0d, x1d)
+        ctx.construct_constraint_set(x0d, dhat)
+        e, g, H = ctx.compute_barrier_term(x0d, dhat)
+        return toi
+
+    # sizes
+    ee, fv = ctx.detect_collision_candidates_rigid(x0d, x1d, True, 0.0)
+    n_ccd = len(ee) + len(fv)
+    ee_d, fv_d = ctx.detect_collision_candidates_rigid(x0d, x0d, False, dhat / 2)
+    n_disc = len(ee_d) + len(fv_d)
+    cs = ctx.construct_constraint_set(x0d, dhat)
+    n_cons = len(cs["type"])
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    launches0 = ctx.stats()["kernel_launches"]
+    times = []
+    with ClockSampler() as clk:
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            step()
+            b.record()
+            torch.cuda.synchronize()
+            times.append(a.elapsed_time(b) / 1e3)
+        if world > 1:
+            torch.distributed.barrier()
+    launches = ctx.stats()["kernel_launches"] - launches0
+    total = sum(times)
+    if world > 1:
+        t = torch.tensor([total], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total = float(t.item())
+    ms = total / args.steps * 1e3
+    value = world * (n_ccd + n_disc) * args.steps / total
+
+    # per-phase timing (kernel-level, resident inputs, after an L2 flush)
+    def timed(fn, reps=3):
+        best = []
+        for _ in range(reps):
+            flush.fill_(1.0)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            torch.cuda.synchronize()
+            best.append(a.elapsed_time(b) / 1e3)
+        return statistics.median(best)
+
+    ctx.detect_collision_candidates_rigid(x0d, x1d, True, 0.0)
+    t_ccd = timed(lambda: ctx.earliest_toi(x0d, x1d))
+    st = ctx.stats()
+    t_bp = timed(lambda: ctx.detect_collision_candidates_rigid(x0d, x1d, True, 0.0))
+    ctx.construct_constraint_set(x0d, dhat)
+    t_bar = timed(lambda: ctx.compute_barrier_term(x0d, dhat))
+
+    # end to end from host buffers
+    e2e_times = []
+    nb = sc.num_bodies
+    for i in range(args.warmup + args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        toi, energy, grad, (rp, col, val), nnzb = ctx.narrow_phase_host(x0, x1, dhat)
+        t = time.perf_counter() - t
+        if i >= args.warmup:
+            e2e_times.append(t)
+    e2e = (n_ccd + n_disc) / statistics.median(e2e_times)
+    h2d = 2 * 6 * nb * 8
+    d2h = 6 * nb * 8 + (nb + 1) * 4 + nnzb * (4 + 36 * 8)
+
+    peak, peak_kind = measured_peaks()
+    ccd_bytes = CCD_BYTES_PER_PAIR * n_ccd
+    achieved = ccd_bytes / t_ccd / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{args.bodies} icospheres (subdivision 3) contact pile, one "
+                               "narrow-phase pass (CCD broad+narrow, constraint set, "
+                               "barrier grad + PSD Hessian, BSR assembly)",
+                   "ccd_candidates": n_ccd, "discrete_candidates": n_disc,
+                   "constraints": n_cons, "ccd_boxes": st["ccd_boxes"],
+                   "ccd_collisions": st["ccd_collisions"], "l2": "flushed (512 MiB write) "
+                   "before every timed step", "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "phases_s": {"ccd_narrow": t_ccd, "ccd_broad": t_bp, "barrier_and_assembly": t_bar},
+        "ccd_pairs_per_s": n_ccd / t_ccd, "barrier_constraints_per_s": n_cons / t_bar,
+        "roofline": {"bound": "hbm", "kernel": "k_ccd", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                     "peak_source": peak_kind,
+                     "note": "FP64-issue bound: algorithmic bytes are 304 B per candidate"},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "clocks": clk.summary(),
+        "gpu_launches": launches,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        base = cpu_baseline(sc, x0, x1, dhat)
+        v = combined_rate(n_ccd, n_disc, base["ccd_pairs_per_s"], base["barrier_pairs_per_s"])
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": base["cores"],
+                                "kind": "port", "sample": base["sample"]}
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -117,6 +117,7 @@ typedef struct rigc_stats {
     int64_t large_elements;   /* elements tested outside the grid            */
     int64_t cand_ee;          /* current candidates (last broad phase)       */
     int64_t cand_fv;
+    int64_t kernel_launches;  /* kernels launched by this library so far     */
     int32_t last_status;
 } rigc_stats;
 

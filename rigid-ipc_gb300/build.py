@@ -41,7 +41,9 @@ def nvcc() -> str:
 def _compile(unit: str, extra: list, verbose: bool) -> str:
     src = os.path.join(CSRC, unit)
     obj = os.path.join(OUT_DIR, unit.replace(".cu", ".o"))
+    # host code never contracts a*b+c into fma (aarch64 gcc does by default)
     cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+           "-Xcompiler", "-ffp-contract=off",
            "-I", os.path.join(ROOT, "include"), *extra, "-c", src, "-o", obj]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")

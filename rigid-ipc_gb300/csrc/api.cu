@@ -1,6 +1,7 @@
 // C ABI of the rigc library (declared in include/rigc.h).
 #include <cmath>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 
 #include "common.cuh"
@@ -18,6 +19,10 @@ int compute_world_vertices_rn(Ctx& c, const double* x, double* V, DevBuf& rotbuf
 int sum_f64(const double* in, int64_t n, double* out_dev, DevBuf& tmp, cudaStream_t stream);
 
 static thread_local std::string g_last_error;
+static std::atomic<int64_t> g_launches { 0 };
+
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+int64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 // broad phase, then record the candidate counts (also on an early exit)
 static int detect_and_count(Ctx& c, const double* x0, const double* x1, bool continuous,
@@ -203,6 +208,7 @@ int rigc_get_stats(const rigc_ctx* ctx, rigc_stats* out)
 {
     if (!ctx || !out) return RIGC_ERR_ARG;
     *out = reinterpret_cast<const Ctx*>(ctx)->stats;
+    out->kernel_launches = launch_count();
     return RIGC_OK;
 }
 

@@ -563,6 +563,7 @@ size_t barrier_smem_bytes() { return (size_t)2 * 144 * kBarrierTPB * sizeof(doub
 int launch_body_frames(Ctx& c, const double* x)
 {
     RIGC_TRY(c.frames.reserve((size_t)c.s.nb * 96 * sizeof(double)));
+    RIGC_COUNT_LAUNCH();
     k_body_frames<<<grid_for(c.s.nb, 128), 128, 0, c.stream>>>(x, c.s.nb, c.frames.as<double>());
     RIGC_CUDA(cudaGetLastError());
     return RIGC_OK;
@@ -595,6 +596,7 @@ int launch_barrier_local(Ctx& c, const double* x, double dhat, double dmin, int 
     a.grad = grad;
     a.blocks = blocks;
     a.hess = hess;
+    RIGC_COUNT_LAUNCH();
     k_barrier_local<<<grid_for(c.cons.num, kBarrierTPB), kBarrierTPB, barrier_smem_bytes(),
                       c.stream>>>(a);
     RIGC_CUDA(cudaGetLastError());
@@ -706,6 +708,7 @@ int assemble_barrier(Ctx& c, bool with_hess)
         RIGC_TRY(S[2].reserve(m * 4));
         RIGC_TRY(S[3].reserve(m * 4));
         RIGC_TRY(S[7].reserve(m * 12 + 16));
+        RIGC_COUNT_LAUNCH();
         k_grad_keys<<<grid_for(m, 256), 256, 0, st>>>(c.cons.bodies.as<int>(), n, S[0].as<uint32_t>(),
                                                      S[1].as<uint32_t>());
         RIGC_TRY(radix_sort_pairs<uint32_t>(S[0].as<uint32_t>(), S[1].as<uint32_t>(),
@@ -714,13 +717,16 @@ int assemble_barrier(Ctx& c, bool with_hess)
         int32_t* head = S[7].as<int32_t>();
         int32_t* segid = head + m;
         int32_t* segst = segid + m;
+        RIGC_COUNT_LAUNCH();
         k_heads<uint32_t><<<grid_for(m, 256), 256, 0, st>>>(S[2].as<uint32_t>(), m, head);
         int32_t* nseg_dev = c.d_scalars.as<int32_t>();
         RIGC_TRY(exclusive_scan_i32(head, segid, m, nseg_dev, S[6], st));
+        RIGC_COUNT_LAUNCH();
         k_seg_starts<<<grid_for(m, 256), 256, 0, st>>>(head, segid, m, segst);
         int32_t nseg;
         RIGC_CUDA(cudaMemcpyAsync(&nseg, nseg_dev, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
         RIGC_CUDA(cudaStreamSynchronize(st));
+        RIGC_COUNT_LAUNCH();
         k_grad_sums<<<grid_for((int64_t)nseg * 6, 256), 256, 0, st>>>(
             S[2].as<uint32_t>(), S[3].as<uint32_t>(), segst, nseg, m, c.c_grad.as<double>(),
             c.grad.as<double>());
@@ -734,6 +740,7 @@ int assemble_barrier(Ctx& c, bool with_hess)
         RIGC_TRY(S[2].reserve(m * 8));
         RIGC_TRY(S[3].reserve(m * 4));
         RIGC_TRY(S[7].reserve(m * 12 + 16));
+        RIGC_COUNT_LAUNCH();
         k_block_keys<<<grid_for(m, 256), 256, 0, st>>>(c.cons.bodies.as<int>(), n, nb,
                                                       S[0].as<uint64_t>(), S[1].as<uint32_t>());
         RIGC_TRY(radix_sort_pairs<uint64_t>(S[0].as<uint64_t>(), S[1].as<uint32_t>(),
@@ -742,15 +749,18 @@ int assemble_barrier(Ctx& c, bool with_hess)
         int32_t* head = S[7].as<int32_t>();
         int32_t* segid = head + m;
         int32_t* segst = segid + m;
+        RIGC_COUNT_LAUNCH();
         k_heads<uint64_t><<<grid_for(m, 256), 256, 0, st>>>(S[2].as<uint64_t>(), m, head);
         int32_t* nseg_dev = c.d_scalars.as<int32_t>();
         RIGC_TRY(exclusive_scan_i32(head, segid, m, nseg_dev, S[6], st));
+        RIGC_COUNT_LAUNCH();
         k_seg_starts<<<grid_for(m, 256), 256, 0, st>>>(head, segid, m, segst);
         int32_t nseg;
         RIGC_CUDA(cudaMemcpyAsync(&nseg, nseg_dev, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
         RIGC_CUDA(cudaStreamSynchronize(st));
         RIGC_TRY(c.col.reserve((size_t)nseg * sizeof(int32_t)));
         RIGC_TRY(c.val.reserve((size_t)nseg * 36 * sizeof(double)));
+        RIGC_COUNT_LAUNCH();
         k_block_sums<<<grid_for((int64_t)nseg * 36, 256), 256, 0, st>>>(
             S[2].as<uint64_t>(), S[3].as<uint32_t>(), segst, nseg, m, c.c_blocks.as<double>(), nb,
             c.col.as<int32_t>(), c.val.as<double>(), c.row_ptr.as<int32_t>() + 1);

@@ -575,9 +575,11 @@ int detect_candidates(Ctx& c, const double* x0, const double* x1, bool continuou
     // ---- 1. bodies
     RIGC_TRY(c.body_box.reserve((size_t)6 * s.nb * sizeof(double)));
     RIGC_TRY(c.body_in.reserve((size_t)(s.nb + 1) * sizeof(int)));
+    RIGC_COUNT_LAUNCH();
     k_body_boxes<<<grid_for((int64_t)s.nb * 32, 128), 128, 0, st>>>(
         x0, x1, s.rest, s.bvs, s.type, s.rmax, s.nb, c.body_box.as<double>());
     RIGC_CUDA(cudaMemsetAsync(c.body_in.ptr, 0, (size_t)s.nb * sizeof(int), st));
+    RIGC_COUNT_LAUNCH();
     k_close_bodies<<<grid_for((int64_t)s.nb * s.nb, 256), 256, 0, st>>>(
         c.body_box.as<double>(), s.group, s.nb, infl, c.body_in.as<int>());
     std::vector<int> h_in(s.nb);
@@ -601,8 +603,11 @@ int detect_candidates(Ctx& c, const double* x0, const double* x1, bool continuou
         double* d_domain = reinterpret_cast<double*>(S[0].as<char>() + ((blist.size() * sizeof(int) + 63) / 64) * 64);
         RIGC_CUDA(cudaMemcpyAsync(d_list, blist.data(), blist.size() * sizeof(int),
                                   cudaMemcpyHostToDevice, st));
+        RIGC_COUNT_LAUNCH();
         k_scene_box<<<1, 256, 0, st>>>(c.body_box.as<double>(), c.body_in.as<int>(), s.nb, d_domain);
+        RIGC_COUNT_LAUNCH();
         k_clear_flags<<<grid_for(s.nv, 256), 256, 0, st>>>(c.vin.as<char>(), s.nv);
+        RIGC_COUNT_LAUNCH();
         k_vertex_boxes_cont<<<(unsigned)blist.size(), kVBThreads, 0, st>>>(
             x0, x1, s.rest, s.bvs, d_list, d_domain, infl, c.vbox.as<double>(), c.vin.as<char>());
         // the host copy of blist must outlive the async copy
@@ -610,10 +615,12 @@ int detect_candidates(Ctx& c, const double* x0, const double* x1, bool continuou
     } else {
         RIGC_TRY(S[0].reserve((size_t)12 * s.nb * sizeof(double)));
         RIGC_TRY(body_rot_rn(c, x0, S[0].as<double>()));
+        RIGC_COUNT_LAUNCH();
         k_vertex_boxes_disc<<<grid_for(s.nv, 256), 256, 0, st>>>(
             S[0].as<double>(), s.rest, s.vbody, c.body_in.as<int>(), s.nv, infl, c.vbox.as<double>(),
             c.vin.as<char>());
     }
+    RIGC_COUNT_LAUNCH();
     k_edge_face_boxes<<<grid_for((int64_t)s.ne + s.nf, 256), 256, 0, st>>>(
         s.edges, s.ne, s.faces, s.nf, c.vbox.as<double>(), c.vin.as<char>(), c.ebox.as<double>(),
         c.ein.as<char>(), c.fbox.as<double>(), c.fin.as<char>());
@@ -624,6 +631,7 @@ int detect_candidates(Ctx& c, const double* x0, const double* x1, bool continuou
     int32_t* flag = S[1].as<int32_t>();
     int32_t* pos = flag + ntot;
     int32_t* cnt_dev = c.d_scalars.as<int32_t>();
+    RIGC_COUNT_LAUNCH();
     k_elem_flags<<<grid_for(ntot, 256), 256, 0, st>>>(c.vin.as<char>(), c.ein.as<char>(),
                                                      c.fin.as<char>(), s.nv, s.ne, s.nf, flag);
     RIGC_TRY(exclusive_scan_i32(flag, pos, ntot, cnt_dev, S[7], st));
@@ -640,8 +648,10 @@ int detect_candidates(Ctx& c, const double* x0, const double* x1, bool continuou
     uint32_t* elems = S[2].as<uint32_t>();
     double* ext = reinterpret_cast<double*>(S[2].as<char>() + (((size_t)m * 4 + 255) / 256) * 256);
     double* part = ext + m;
+    RIGC_COUNT_LAUNCH();
     k_elem_list<<<grid_for(ntot, 256), 256, 0, st>>>(flag, pos, s.nv, s.ne, s.nf, elems);
     const int nbk = 256;
+    RIGC_COUNT_LAUNCH();
     k_elem_bounds<<<nbk, 256, 0, st>>>(elems, m, c.vbox.as<double>(), c.ebox.as<double>(),
                                        c.fbox.as<double>(), part, ext);
     double* d_sum = reinterpret_cast<double*>(c.d_scalars.as<char>() + 512);
@@ -681,6 +691,7 @@ int detect_candidates(Ctx& c, const double* x0, const double* x1, bool continuou
     int32_t* icnt = S[3].as<int32_t>();
     int32_t* ioff = icnt + m;
     int32_t* lflag = ioff + m;
+    RIGC_COUNT_LAUNCH();
     k_count_cells<<<grid_for(m, 256), 256, 0, st>>>(elems, m, c.vbox.as<double>(), c.ebox.as<double>(),
                                                    c.fbox.as<double>(), g, icnt, lflag);
     RIGC_TRY(exclusive_scan_i32(icnt, ioff, m, cnt_dev, S[7], st));
@@ -698,6 +709,7 @@ int detect_candidates(Ctx& c, const double* x0, const double* x1, bool continuou
     RIGC_TRY(c.items_val.reserve((size_t)nitems * 4 + 8));
     RIGC_TRY(c.items_key2.reserve((size_t)nitems * 8 + 8));
     RIGC_TRY(c.items_val2.reserve((size_t)nitems * 4 + 8));
+    RIGC_COUNT_LAUNCH();
     k_emit_items<<<grid_for(m, 256), 256, 0, st>>>(elems, m, c.vbox.as<double>(), c.ebox.as<double>(),
                                                   c.fbox.as<double>(), g, icnt, ioff,
                                                   c.items_key.as<uint64_t>(), c.items_val.as<uint32_t>());
@@ -705,6 +717,7 @@ int detect_candidates(Ctx& c, const double* x0, const double* x1, bool continuou
                                         c.items_key2.as<uint64_t>(), c.items_val2.as<uint32_t>(),
                                         nitems, bits_for(ncells), S[4], S[5], S[7], st));
     RIGC_TRY(c.large_list.reserve((size_t)(nlarge + 1) * sizeof(uint32_t)));
+    RIGC_COUNT_LAUNCH();
     k_large_list<<<grid_for(m, 256), 256, 0, st>>>(elems, lflag, lpos, m, c.large_list.as<uint32_t>());
     // ---- 5. pairs (retry once with exact capacity on overflow)
     PairCtx P { c.vbox.as<double>(), c.ebox.as<double>(), c.fbox.as<double>(), s.vbody, s.ebody,
@@ -717,12 +730,16 @@ int detect_candidates(Ctx& c, const double* x0, const double* x1, bool continuou
         PairOut o { c.pair_out.as<unsigned long long>(), c.pair_out.as<unsigned long long>() + cap_ee,
                     cap_ee, cap_fv, pn, pn + 1 };
         RIGC_CUDA(cudaMemsetAsync(pn, 0, 2 * sizeof(unsigned long long), st));
-        if (nitems > 0)
+        if (nitems > 0) {
+            RIGC_COUNT_LAUNCH();
             k_cell_pairs<<<grid_for(nitems, 128), 128, 0, st>>>(c.items_key2.as<uint64_t>(),
                                                               c.items_val2.as<uint32_t>(), nitems, P, g, o);
-        if (nlarge > 0)
+        }
+        if (nlarge > 0) {
+            RIGC_COUNT_LAUNCH();
             k_large_pairs<<<grid_for((int64_t)nlarge * m, 256), 256, 0, st>>>(
                 c.large_list.as<uint32_t>(), nlarge, elems, lflag, m, P, o);
+        }
         RIGC_CUDA(cudaGetLastError());
         unsigned long long hn[2];
         RIGC_CUDA(cudaMemcpyAsync(hn, pn, sizeof(hn), cudaMemcpyDeviceToHost, st));
@@ -747,18 +764,22 @@ int detect_candidates(Ctx& c, const double* x0, const double* x1, bool continuou
     RIGC_TRY(S[0].reserve((size_t)nmax * 4 + 8));
     RIGC_TRY(S[1].reserve((size_t)nmax * 4 + 8));
     if (nee > 0) {
+        RIGC_COUNT_LAUNCH();
         k_iota<<<grid_for(nee, 256), 256, 0, st>>>(S[0].as<uint32_t>(), nee);
         RIGC_TRY(radix_sort_pairs<uint64_t>(reinterpret_cast<uint64_t*>(kee), S[0].as<uint32_t>(), c.pair_key.as<uint64_t>(),
                                             S[1].as<uint32_t>(), nee,
                                             bits_for((uint64_t)s.ne * (uint64_t)s.ne), S[4], S[5], S[7], st));
+        RIGC_COUNT_LAUNCH();
         k_decode_pairs<<<grid_for(nee, 256), 256, 0, st>>>(c.pair_key.as<unsigned long long>(), nee,
                                                           (unsigned long long)s.ne, c.cand.ee.as<int2>());
     }
     if (nfv > 0) {
+        RIGC_COUNT_LAUNCH();
         k_iota<<<grid_for(nfv, 256), 256, 0, st>>>(S[0].as<uint32_t>(), nfv);
         RIGC_TRY(radix_sort_pairs<uint64_t>(reinterpret_cast<uint64_t*>(kfv), S[0].as<uint32_t>(), c.pair_key.as<uint64_t>(),
                                             S[1].as<uint32_t>(), nfv,
                                             bits_for((uint64_t)s.nf * (uint64_t)s.nv), S[4], S[5], S[7], st));
+        RIGC_COUNT_LAUNCH();
         k_decode_pairs<<<grid_for(nfv, 256), 256, 0, st>>>(c.pair_key.as<unsigned long long>(), nfv,
                                                           (unsigned long long)s.nv, c.cand.fv.as<int2>());
     }

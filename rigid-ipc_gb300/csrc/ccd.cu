@@ -259,8 +259,7 @@ k_ccd(CCDArgs a)
             stack[sp++] = lo;
         }
         toi = found ? earliest : INFINITY;
-        if (found && a.prune)
-            atomicMin(a.gmin, (unsigned long long)__double_as_longlong(toi));
+        if (found) atomicMin(a.gmin, (unsigned long long)__double_as_longlong(toi));
         if (a.per) a.per[i] = toi;
         if (status != RIGC_OK) atomicMax(a.status, status);
     }
@@ -311,6 +310,7 @@ int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flag
         a.status = reinterpret_cast<int*>(cnt + 3);
         a.boxes = cnt + 1;
         a.hits = cnt + 2;
+        RIGC_COUNT_LAUNCH();
         k_ccd<<<grid_for(n, kCCDThreads), kCCDThreads, 0, st>>>(a);
         RIGC_CUDA(cudaGetLastError());
     }

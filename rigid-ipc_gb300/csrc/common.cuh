@@ -44,6 +44,11 @@ struct Status {
 
 void set_error(int code, const char* what, const char* file, int line);
 
+// number of kernels this library has launched (for measurement)
+void count_launch();
+int64_t launch_count();
+#define RIGC_COUNT_LAUNCH() ::rigc::count_launch()
+
 // grow-only device buffer
 struct DevBuf {
     void* ptr = nullptr;

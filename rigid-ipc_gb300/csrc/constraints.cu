@@ -49,6 +49,7 @@ __global__ void k_world_vertices_rn(const double* __restrict__ rest, const int* 
 
 int body_rot_rn(Ctx& c, const double* x, double* out)
 {
+    RIGC_COUNT_LAUNCH();
     k_body_rot_rn<<<grid_for(c.s.nb, 128), 128, 0, c.stream>>>(x, c.s.nb, out);
     RIGC_CUDA(cudaGetLastError());
     return RIGC_OK;
@@ -57,7 +58,9 @@ int body_rot_rn(Ctx& c, const double* x, double* out)
 int compute_world_vertices_rn(Ctx& c, const double* x, double* V, DevBuf& rotbuf)
 {
     RIGC_TRY(rotbuf.reserve((size_t)12 * c.s.nb * sizeof(double)));
+    RIGC_COUNT_LAUNCH();
     k_body_rot_rn<<<grid_for(c.s.nb, 128), 128, 0, c.stream>>>(x, c.s.nb, rotbuf.as<double>());
+    RIGC_COUNT_LAUNCH();
     k_world_vertices_rn<<<grid_for(c.s.nv, 256), 256, 0, c.stream>>>(
         c.s.rest, c.s.vbody, c.s.nv, rotbuf.as<double>(), V);
     RIGC_CUDA(cudaGetLastError());
@@ -272,6 +275,7 @@ int construct_constraints(Ctx& c, const double* x, double dhat, double dmin)
     int32_t* flag = S[6].as<int32_t>();
     int32_t* pos = flag + n;
     int32_t* cnt_dev = c.d_scalars.as<int32_t>();
+    RIGC_COUNT_LAUNCH();
     k_classify_count<<<grid_for(n, 128), 128, 0, st>>>(
         n, nee, c.cand.ee.as<int2>(), c.cand.fv.as<int2>(), c.s.edges, c.s.faces, c.s.f2e, V, off,
         flag);
@@ -289,6 +293,7 @@ int construct_constraints(Ctx& c, const double* x, double dhat, double dmin)
     DevBuf& re = c.items_val2;
     RIGC_TRY(rv.reserve((size_t)m * sizeof(int4)));
     RIGC_TRY(re.reserve((size_t)m * sizeof(double)));
+    RIGC_COUNT_LAUNCH();
     k_classify_write<<<grid_for(n, 128), 128, 0, st>>>(
         n, nee, c.cand.ee.as<int2>(), c.cand.fv.as<int2>(), c.s.edges, c.s.faces, c.s.f2e, V, off,
         flag, pos, S[0].as<uint64_t>(), S[1].as<uint32_t>(), rv.as<int4>(), re.as<double>());
@@ -298,6 +303,7 @@ int construct_constraints(Ctx& c, const double* x, double dhat, double dmin)
     RIGC_TRY(S[6].reserve((size_t)(2 * m + 16) * sizeof(int32_t)));
     int32_t* head = S[6].as<int32_t>();
     int32_t* segid = head + m;
+    RIGC_COUNT_LAUNCH();
     k_cons_heads<<<grid_for(m, 256), 256, 0, st>>>(S[2].as<uint64_t>(), m, head);
     RIGC_TRY(exclusive_scan_i32(head, segid, m, cnt_dev, S[7], st));
     int32_t nc;
@@ -312,6 +318,7 @@ int construct_constraints(Ctx& c, const double* x, double dhat, double dmin)
     RIGC_TRY(C.eps.reserve((size_t)nc * 8));
     int32_t* kc = cnt_dev + 4;
     RIGC_CUDA(cudaMemsetAsync(kc, 0, 4 * sizeof(int32_t), st));
+    RIGC_COUNT_LAUNCH();
     k_cons_emit<<<grid_for(m, 256), 256, 0, st>>>(
         S[2].as<uint64_t>(), S[3].as<uint32_t>(), rv.as<int4>(), re.as<double>(), head, segid, m,
         c.s.vbody, c.s.ebody, c.s.fbody, C.type.as<int>(), C.verts.as<int4>(), C.prims.as<int2>(),

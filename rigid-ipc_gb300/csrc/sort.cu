@@ -135,9 +135,12 @@ int radix_sort_pairs(const Key* keys_in, const uint32_t* vals_in, Key* keys_out,
         Key* dk = to_out ? keys_out : tmp_keys.as<Key>();
         uint32_t* dv = to_out ? vals_out : tmp_vals.as<uint32_t>();
         int shift = 8 * p;
+        RIGC_COUNT_LAUNCH();
         k_digit_hist<Key><<<ntiles, kSortThreads, 0, stream>>>(src_k, n, shift, ntiles,
                                                                hist.as<uint32_t>());
+        RIGC_COUNT_LAUNCH();
         k_scan_single<<<1, 1024, 0, stream>>>(hist.as<uint32_t>(), (int64_t)256 * ntiles);
+        RIGC_COUNT_LAUNCH();
         k_scatter<Key><<<ntiles, kSortThreads, 0, stream>>>(src_k, src_v, dk, dv, n, shift,
                                                             ntiles, hist.as<uint32_t>());
         src_k = dk;
@@ -253,8 +256,11 @@ int exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, int32_t* tota
     }
     int64_t tiles = (n + kScanTile - 1) / kScanTile;
     RIGC_TRY(tmp.reserve(tiles * sizeof(int32_t)));
+    RIGC_COUNT_LAUNCH();
     k_tile_sums<<<(unsigned)tiles, kScanThreads, 0, stream>>>(in, n, tmp.as<int32_t>());
+    RIGC_COUNT_LAUNCH();
     k_scan_sums<<<1, kScanThreads, 0, stream>>>(tmp.as<int32_t>(), tiles, total_dev);
+    RIGC_COUNT_LAUNCH();
     k_tile_scan<<<(unsigned)tiles, kScanThreads, 0, stream>>>(in, out, n, tmp.as<int32_t>());
     RIGC_CUDA(cudaGetLastError());
     return RIGC_OK;
@@ -297,7 +303,9 @@ __global__ void k_sum_final(const double* __restrict__ part, int m, double* out)
 int sum_f64(const double* in, int64_t n, double* out_dev, DevBuf& tmp, cudaStream_t stream)
 {
     RIGC_TRY(tmp.reserve(kSumBlocks * sizeof(double)));
+    RIGC_COUNT_LAUNCH();
     k_sum_partials<<<kSumBlocks, 256, 0, stream>>>(in, n, tmp.as<double>());
+    RIGC_COUNT_LAUNCH();
     k_sum_final<<<1, 1024, 0, stream>>>(tmp.as<double>(), kSumBlocks, out_dev);
     RIGC_CUDA(cudaGetLastError());
     return RIGC_OK;

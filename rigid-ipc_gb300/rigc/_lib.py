@@ -71,7 +71,8 @@ class Stats(C.Structure):
     _fields_ = [("ccd_boxes", C.c_int64), ("ccd_candidates", C.c_int64),
                 ("ccd_collisions", C.c_int64), ("grid_items", C.c_int64),
                 ("large_elements", C.c_int64), ("cand_ee", C.c_int64),
-                ("cand_fv", C.c_int64), ("last_status", C.c_int32)]
+                ("cand_fv", C.c_int64), ("kernel_launches", C.c_int64),
+                ("last_status", C.c_int32)]
 
 
 _lib = None

@@ -163,8 +163,9 @@ def test_gpu_face_vertex_toi_analytic(oracle, y, z_t1):
     o = oracle.OracleScene(sc)
     ee_g, fv_g = ctx.detect_collision_candidates_rigid(x0, x1, True, 0.0)
     toi_g, per, st = ctx.earliest_toi(x0, x1, toi_tol=1e-6, prune=False, per_candidate=True)
-    _, toi_min, _ = o.earliest_toi(x0, x1, ee_g, fv_g, tol=1e-6, per_candidate=True)
+    toi_min, per_o, _ = o.earliest_toi(x0, x1, ee_g, fv_g, tol=1e-6, per_candidate=True)
     assert toi_g == toi_min
+    assert np.array_equal(per, per_o)
     if hit:
         assert toi_g <= expected
         assert toi_g == pytest.approx(expected, abs=1e-4)
