@@ -31,6 +31,8 @@ extern "C" {
 #define RIGC_ERR_ITER_LIMIT 5     /* CCD box budget exhausted (result kept
                                      conservative)                            */
 #define RIGC_ERR_NAN 6            /* non-finite pose input                    */
+#define RIGC_ERR_TOO_LARGE 7      /* input larger than a fixed-capacity entry
+                                     point accepts                            */
 
 /* body types (src/physics/rigid_body.hpp RigidBodyType) */
 #define RIGC_BODY_STATIC 0
@@ -202,6 +204,39 @@ int rigc_narrow_phase_host(rigc_ctx* ctx, const double* x0_host,
                            double* grad_host, int32_t* row_ptr_host,
                            int32_t* col_host, double* val_host,
                            int64_t nnzb_cap, int64_t* nnzb_host);
+
+/* ---- per-constraint barrier terms without any device allocation.
+ * No counterpart in the reference: the reference allocates freely on the
+ * host.  This entry point is for callers that must not allocate device
+ * memory at call time -- code that runs inside another framework's memory
+ * pool or a fixed memory budget, or latency-critical loops where a
+ * cudaMalloc / cudaFree would synchronise the device -- and that therefore
+ * cannot create a rigc_ctx.  The caller passes every input and output as
+ * device memory it already owns; the only working memory is a file-scope
+ * device array inside the library (the per-body rotation frames) that holds
+ * RIGC_NOALLOC_MAX_BODIES bodies, 3 MiB, and stays resident on every GPU that
+ * loads the library until the process exits.
+ *
+ * Same results as rigc_barrier_local_terms for the same constraints.
+ * Inputs (device): rest_vertices (num_vertices x 3, body frame), x (6 per
+ * body), the constraint arrays in rigc_constraints layout (type, verts x 4,
+ * bodies x 2, weight, eps_x).  Outputs (device, any may be NULL): energy
+ * (num_constraints), grad (x 12), hess (x 144).  flags as rigc_barrier_term.
+ * Returns RIGC_ERR_TOO_LARGE when num_bodies > RIGC_NOALLOC_MAX_BODIES.
+ *
+ * The first call on a device looks up the device address of the working
+ * array (a one-time set-up per device); make that first call before any
+ * stream capture.  Every call shares the one working array, so calls that
+ * overlap on the GPU (different streams, or different host threads) race:
+ * serialise them on one stream.  The array keeps the last call's contents;
+ * each call overwrites every frame it reads. */
+#define RIGC_NOALLOC_MAX_BODIES 4096
+int rigc_barrier_local_terms_noalloc(
+    const double* rest_vertices, int32_t num_bodies, const double* x,
+    int64_t num_constraints, const int32_t* type, const int32_t* verts,
+    const int32_t* bodies, const double* weight, const double* eps_x,
+    double dhat, double dmin, int flags, double* energy, double* grad,
+    double* hess, void* cuda_stream);
 
 #ifdef __cplusplus
 }

@@ -28,6 +28,7 @@ UNITS = {
     "constraints.cu": ["--fmad=false"],
     "broad_phase.cu": ["--fmad=false"],
     "ccd.cu": ["--fmad=false"],
+    "noalloc.cu": ["--fmad=false"],
 }
 
 

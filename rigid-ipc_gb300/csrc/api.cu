@@ -94,6 +94,7 @@ const char* rigc_status_string(int status)
     case RIGC_ERR_QUEUE_OVERFLOW: return "CCD box stack overflow (conservative result)";
     case RIGC_ERR_ITER_LIMIT: return "CCD box budget exhausted (conservative result)";
     case RIGC_ERR_NAN: return "non-finite input";
+    case RIGC_ERR_TOO_LARGE: return "input exceeds the entry point's fixed capacity";
     default: return "unknown status";
     }
 }

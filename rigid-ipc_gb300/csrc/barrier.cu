@@ -603,6 +603,43 @@ int launch_barrier_local(Ctx& c, const double* x, double dhat, double dmin, int 
     return RIGC_OK;
 }
 
+// Frames and per-constraint terms with every buffer supplied by the caller
+// (the frames array holds 96 doubles per body); used by the entry point that
+// allocates nothing.
+int launch_barrier_local_raw(const double* rest, int nb, const double* x, int64_t n,
+                             const int* ctype, const int* cverts, const int* cbodies,
+                             const double* cweight, const double* ceps, double dhat, double dmin,
+                             int flags, double* frames, double* energy, double* grad,
+                             double* hess, cudaStream_t stream)
+{
+    RIGC_COUNT_LAUNCH();
+    k_body_frames<<<grid_for(nb, 128), 128, 0, stream>>>(x, nb, frames);
+    RIGC_CUDA(cudaGetLastError());
+    if (n == 0) return RIGC_OK;
+    RIGC_CUDA(cudaFuncSetAttribute(k_barrier_local, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)barrier_smem_bytes()));
+    BarrierArgs a;
+    a.rest = rest;
+    a.frames = frames;
+    a.ctype = ctype;
+    a.cverts = cverts;
+    a.cbodies = cbodies;
+    a.cweight = cweight;
+    a.ceps = ceps;
+    a.n = n;
+    a.dhat = dhat;
+    a.dmin = dmin;
+    a.flags = flags;
+    a.energy = energy;
+    a.grad = grad;
+    a.blocks = nullptr;
+    a.hess = hess;
+    RIGC_COUNT_LAUNCH();
+    k_barrier_local<<<grid_for(n, kBarrierTPB), kBarrierTPB, barrier_smem_bytes(), stream>>>(a);
+    RIGC_CUDA(cudaGetLastError());
+    return RIGC_OK;
+}
+
 // ---------------------------------------------------------------------------
 // deterministic assembly: sort block keys, sum equal keys in constraint order
 

@@ -31,8 +31,10 @@ EXPORTS = [
     "rigc_get_stats", "rigc_copy", "rigc_world_vertices", "rigc_detect_candidates",
     "rigc_earliest_toi", "rigc_compute_earliest_toi", "rigc_construct_constraint_set",
     "rigc_set_constraints", "rigc_barrier_term", "rigc_barrier_local_terms",
-    "rigc_narrow_phase_host",
+    "rigc_narrow_phase_host", "rigc_barrier_local_terms_noalloc",
 ]
+RIGC_ERR_TOO_LARGE = 7
+RIGC_NOALLOC_MAX_BODIES = 4096
 
 _vp = C.c_void_p
 _d = C.POINTER(C.c_double)
@@ -106,6 +108,9 @@ def load():
     L.rigc_barrier_local_terms.argtypes = [_vp, _vp, C.c_double, C.c_double, C.c_int, _vp, _vp, _vp]
     L.rigc_narrow_phase_host.argtypes = [_vp, _vp, _vp, C.c_double, C.c_double, _d, _d, _vp, _vp,
                                          _vp, _vp, C.c_int64, _i64]
+    L.rigc_barrier_local_terms_noalloc.argtypes = [
+        _vp, C.c_int32, _vp, C.c_int64, _vp, _vp, _vp, _vp, _vp, C.c_double, C.c_double,
+        C.c_int, _vp, _vp, _vp, _vp]
     for f in EXPORTS:
         getattr(L, f).restype = C.c_char_p if f == "rigc_status_string" else C.c_int
     _lib = L
