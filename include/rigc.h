@@ -192,6 +192,26 @@ int rigc_barrier_local_terms(rigc_ctx* ctx, const double* x, double dhat,
                              double dmin, int flags, double* energy,
                              double* grad, double* hess);
 
+/* Per-body state at the start of the time step (device pointers). */
+typedef struct rigc_body_state {
+    const double* mass;        /* num_bodies                                 */
+    const double* moment;      /* num_bodies x 3, principal moments          */
+    const double* x_t0;        /* num_bodies x 6, pose [p, theta]            */
+    const double* v_t0;        /* num_bodies x 6, [v world, omega body]      */
+    const double* Qdot_t0;     /* num_bodies x 9, dR/dt row-major            */
+    const int32_t* dof_fixed;  /* num_bodies, bit k set when dof k is fixed  */
+} rigc_body_state;
+
+/* ---- inertial energy: DistanceBarrierRBProblem::compute_energy_term with
+ * implicit Euler (src/problems/distance_barrier_rb_problem.cpp:706-944).
+ * Per dynamic body E = 1/2 m q.q - m q.(q0 + h (v0 + h g))
+ * + 1/2 tr(Q J Q^T) - tr(Q J (Q0 + h Qdot0)^T).  Outputs: energy (host,
+ * summed), grad (device, 6 per body), hess (device, 36 per body, the
+ * body's diagonal 6x6 block, row-major); grad / hess may be NULL. */
+int rigc_body_energy(rigc_ctx* ctx, const rigc_body_state* state,
+                     const double* x, const double gravity[3], double h,
+                     double* energy_host, double* grad, double* hess);
+
 /* ---- one narrow-phase pass from host memory (the call a host Newton loop
  * makes per iteration): copies x0/x1 in, runs compute_earliest_toi(x0, x1)
  * and construct_constraint_set + compute_barrier_term at x0, copies the

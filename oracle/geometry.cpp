@@ -811,4 +811,221 @@ double body_energy(
     return e.v;
 }
 
+
+// ---------------------------------------------------------------------------
+// lagged friction (IPC paper, Li et al. 2020 sec. 5, as ipc-toolkit provides
+// it to compute_friction_term, distance_barrier_rb_problem.cpp:1410-1572):
+// per collision constraint at the start of the step, a normal force
+// magnitude lambda = -kappa w b'(d - dmin^2) 2 sqrt(d), closest-point weights
+// Gamma (3 x 3n blocks) and an orthonormal tangent basis T (3 x 2) of the
+// contact plane; D = mu lambda f0(|T^T Gamma (X - X0)|) with the mollified
+// f0 of eps_v h.
+
+namespace {
+void normalize3(double* v)
+{
+    double n = std::sqrt(dot3(v, v));
+    for (int i = 0; i < 3; i++) v[i] /= n;
+}
+// two orthonormal vectors spanning the plane orthogonal to n
+void basis_from_normal(const double* n_in, double* t1, double* t2)
+{
+    double n[3] = { n_in[0], n_in[1], n_in[2] };
+    normalize3(n);
+    double ax[3] = { 1, 0, 0 };
+    if (std::fabs(n[0]) > 0.9) { ax[0] = 0; ax[1] = 1; }
+    cross3(n, ax, t1);
+    normalize3(t1);
+    cross3(n, t1, t2);
+}
+// barrier derivative of the shifted squared distance
+double barrier_gradient_d(double d, double s)
+{
+    if (d <= 0.0 || d >= s) return 0.0;
+    return (s - d) * (2 * std::log(d / s) - s / d + 1);
+}
+} // namespace
+
+void construct_friction_constraints(
+    const Scene& s, const std::vector<Constraint>& cs, const std::vector<double>& V0,
+    double dhat, double dmin, double kappa, std::vector<FrictionConstraint>& out)
+{
+    out.clear();
+    auto P = [&](int i) { return &V0[3 * i]; };
+    const double sb = 2 * dmin * dhat + dhat * dhat;
+    for (const auto& c : cs) {
+        FrictionConstraint f;
+        f.c = c;
+        f.p0 = f.p1 = 0;
+        double d = 0, n[3], t1[3], t2[3];
+        switch (c.type) {
+        case C_VV: {
+            sub3(P(c.v[0]), P(c.v[1]), n);
+            d = dot3(n, n);
+            basis_from_normal(n, t1, t2);
+            break;
+        }
+        case C_EV: {
+            const double *p = P(c.v[0]), *e0 = P(c.v[1]), *e1 = P(c.v[2]);
+            double e[3], w[3];
+            sub3(e1, e0, e);
+            sub3(p, e0, w);
+            f.p0 = dot3(e, w) / dot3(e, e);
+            d = point_line_sqdist(p, e0, e1);
+            double c3[3];
+            for (int i = 0; i < 3; i++) n[i] = w[i] - f.p0 * e[i];
+            for (int i = 0; i < 3; i++) t1[i] = e[i];
+            normalize3(t1);
+            cross3(e, n, c3);
+            for (int i = 0; i < 3; i++) t2[i] = c3[i];
+            normalize3(t2);
+            break;
+        }
+        case C_EE: {
+            const double *a0 = P(c.v[0]), *a1 = P(c.v[1]), *b0 = P(c.v[2]), *b1 = P(c.v[3]);
+            double a[3], b[3], w[3];
+            sub3(a1, a0, a);
+            sub3(b1, b0, b);
+            sub3(b0, a0, w);
+            // minimise |a0 + alpha a - b0 - beta b|^2
+            double aa = dot3(a, a), ab = dot3(a, b), bb = dot3(b, b), aw = dot3(a, w), bw = dot3(b, w);
+            double det = aa * bb - ab * ab;
+            f.p0 = (aw * bb - ab * bw) / det;
+            f.p1 = (aw * ab - aa * bw) / det;
+            d = line_line_sqdist(a0, a1, b0, b1);
+            cross3(a, b, n);
+            for (int i = 0; i < 3; i++) t1[i] = a[i];
+            normalize3(t1);
+            double nn[3] = { n[0], n[1], n[2] };
+            normalize3(nn);
+            cross3(nn, t1, t2);
+            break;
+        }
+        default: {
+            const double *p = P(c.v[0]), *q0 = P(c.v[1]), *q1 = P(c.v[2]), *q2 = P(c.v[3]);
+            double e1[3], e2[3], w[3];
+            sub3(q1, q0, e1);
+            sub3(q2, q0, e2);
+            sub3(p, q0, w);
+            double a11 = dot3(e1, e1), a12 = dot3(e1, e2), a22 = dot3(e2, e2);
+            double r1 = dot3(e1, w), r2 = dot3(e2, w);
+            double det = a11 * a22 - a12 * a12;
+            f.p0 = (a22 * r1 - a12 * r2) / det;
+            f.p1 = (a11 * r2 - a12 * r1) / det;
+            d = point_plane_sqdist(p, q0, q1, q2);
+            cross3(e1, e2, n);
+            for (int i = 0; i < 3; i++) t1[i] = e1[i];
+            normalize3(t1);
+            double nn[3] = { n[0], n[1], n[2] };
+            normalize3(nn);
+            cross3(nn, t1, t2);
+            break;
+        }
+        }
+        f.lambda = -kappa * c.weight * barrier_gradient_d(d - dmin * dmin, sb) * 2 * std::sqrt(d);
+        for (int i = 0; i < 3; i++) {
+            f.T[i] = t1[i];
+            f.T[3 + i] = t2[i];
+        }
+        out.push_back(f);
+    }
+}
+
+// closest-point weights of the relative displacement: Delta = sum_i g_i U_i
+static void friction_weights(const FrictionConstraint& f, double g[4])
+{
+    switch (f.c.type) {
+    case C_VV: g[0] = 1; g[1] = -1; g[2] = g[3] = 0; break;
+    case C_EV: g[0] = 1; g[1] = -(1 - f.p0); g[2] = -f.p0; g[3] = 0; break;
+    case C_EE: g[0] = 1 - f.p0; g[1] = f.p0; g[2] = -(1 - f.p1); g[3] = -f.p1; break;
+    default: g[0] = 1; g[1] = -(1 - f.p0 - f.p1); g[2] = -f.p0; g[3] = -f.p1; break;
+    }
+}
+
+void friction_local_term(
+    const Scene& s, const FrictionConstraint& f, const std::vector<double>& V,
+    const std::vector<double>& V0, const std::vector<double>& dV,
+    const std::vector<double>& d2V, double mu, double epsvh, bool project, LocalTerm& out)
+{
+    const Constraint& c = f.c;
+    const int nvc = c.nverts();
+    double g[4];
+    friction_weights(f, g);
+    // A (2 x 12) = T^T Gamma
+    double A[2][12] = {};
+    for (int i = 0; i < nvc; i++)
+        for (int r = 0; r < 2; r++)
+            for (int j = 0; j < 3; j++) A[r][3 * i + j] = g[i] * f.T[3 * r + j];
+    double u[2] = { 0, 0 };
+    for (int i = 0; i < nvc; i++)
+        for (int j = 0; j < 3; j++) {
+            double Uij = V[3 * c.v[i] + j] - V0[3 * c.v[i] + j];
+            u[0] += A[0][3 * i + j] * Uij;
+            u[1] += A[1][3 * i + j] * Uij;
+        }
+    double x = std::sqrt(u[0] * u[0] + u[1] * u[1]);
+    const double ml = mu * f.lambda;
+    double f0, f1_over_x, hu[2][2];
+    if (x >= epsvh) {
+        f0 = x;
+        f1_over_x = 1 / x;
+        for (int a = 0; a < 2; a++)
+            for (int b = 0; b < 2; b++)
+                hu[a][b] = -u[a] * u[b] / (x * x * x) + (a == b ? 1 / x : 0.0);
+    } else {
+        f0 = -x * x * x / (3 * epsvh * epsvh) + x * x / epsvh + epsvh / 3;
+        f1_over_x = 2 / epsvh - x / (epsvh * epsvh);
+        for (int a = 0; a < 2; a++)
+            for (int b = 0; b < 2; b++)
+                hu[a][b] = (x > 0 ? -u[a] * u[b] / (epsvh * epsvh * x) : 0.0)
+                    + (a == b ? f1_over_x : 0.0);
+    }
+    out.energy = ml * f0;
+    double gx[12] = {};
+    for (int k = 0; k < 12; k++) gx[k] = ml * f1_over_x * (A[0][k] * u[0] + A[1][k] * u[1]);
+    double Hx[12][12];
+    for (int k = 0; k < 12; k++)
+        for (int l = 0; l < 12; l++) {
+            double acc = 0;
+            for (int a = 0; a < 2; a++)
+                for (int b = 0; b < 2; b++) acc += A[a][k] * hu[a][b] * A[b][l];
+            Hx[k][l] = ml * acc;
+        }
+    // rigid chain rule (apply_chain_rule)
+    double J[12][12] = {};
+    for (int i = 0; i < nvc; i++) {
+        int lb = local_body(c.type, i);
+        int vi = c.v[i];
+        for (int j = 0; j < 3; j++) {
+            J[3 * i + j][6 * lb + j] = 1.0;
+            for (int k = 0; k < 3; k++) J[3 * i + j][6 * lb + 3 + k] = dV[9 * vi + 3 * j + k];
+        }
+    }
+    for (int a = 0; a < 12; a++) {
+        double acc = 0;
+        for (int r = 0; r < 12; r++) acc += J[r][a] * gx[r];
+        out.grad[a] = acc;
+    }
+    double H[144];
+    for (int a = 0; a < 12; a++)
+        for (int b = 0; b < 12; b++) {
+            double acc = 0;
+            for (int r = 0; r < 12; r++) {
+                if (J[r][a] == 0.0) continue;
+                for (int q = 0; q < 12; q++) acc += J[r][a] * Hx[r][q] * J[q][b];
+            }
+            H[12 * a + b] = acc;
+        }
+    for (int i = 0; i < nvc; i++) {
+        int lb = local_body(c.type, i);
+        int vi = c.v[i];
+        for (int j = 0; j < 3; j++)
+            for (int k = 0; k < 3; k++)
+                for (int l = 0; l < 3; l++)
+                    H[12 * (6 * lb + 3 + k) + 6 * lb + 3 + l] += gx[3 * i + j] * d2V[27 * vi + 9 * j + 3 * k + l];
+    }
+    if (project) project_to_psd(12, H, out.hess);
+    else std::copy(H, H + 144, out.hess);
+}
+
 } // namespace orc

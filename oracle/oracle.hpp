@@ -259,6 +259,21 @@ double body_energy(
     const BodyState& b, const double* x6, const double gravity[3], double h,
     double grad[6], double hess[36]);
 
+// lagged friction constraints and their local terms
+struct FrictionConstraint {
+    Constraint c;
+    double lambda;   // normal force magnitude at the start of the step
+    double p0, p1;   // closest-point parameters (EV alpha; EE alpha, beta; FV b1, b2)
+    double T[6];     // tangent basis, columns t1 = T[0..2], t2 = T[3..5]
+};
+void construct_friction_constraints(
+    const Scene& s, const std::vector<Constraint>& cs, const std::vector<double>& V0,
+    double dhat, double dmin, double kappa, std::vector<FrictionConstraint>& out);
+void friction_local_term(
+    const Scene& s, const FrictionConstraint& f, const std::vector<double>& V,
+    const std::vector<double>& V0, const std::vector<double>& dV,
+    const std::vector<double>& d2V, double mu, double epsvh, bool project, LocalTerm& out);
+
 // ---------------------------------------------------------------------------
 // broad phase
 struct AABB {

@@ -29,6 +29,7 @@ UNITS = {
     "broad_phase.cu": ["--fmad=false"],
     "ccd.cu": ["--fmad=false"],
     "noalloc.cu": ["--fmad=false"],
+    "body.cu": ["--fmad=true"],
 }
 
 

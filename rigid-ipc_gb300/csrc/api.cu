@@ -17,6 +17,8 @@ int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flag
             double* toi_host, double* per);
 int compute_world_vertices_rn(Ctx& c, const double* x, double* V, DevBuf& rotbuf);
 int sum_f64(const double* in, int64_t n, double* out_dev, DevBuf& tmp, cudaStream_t stream);
+int body_energy(Ctx& c, const rigc_body_state& s, const double* x, const double gravity[3],
+                double h, double* energy_host, double* grad, double* hess);
 
 static thread_local std::string g_last_error;
 static std::atomic<int64_t> g_launches { 0 };
@@ -70,7 +72,7 @@ static void release_all(Ctx* c)
                        &c->d_scalars, &c->body_box, &c->body_in, &c->vbox, &c->ebox, &c->fbox,
                        &c->vin, &c->ein, &c->fin, &c->items_key, &c->items_val, &c->items_key2,
                        &c->items_val2, &c->seg, &c->pair_out, &c->pair_key, &c->large_list,
-                       &c->x0_dev, &c->x1_dev };
+                       &c->x0_dev, &c->x1_dev, &c->rot_table };
     for (DevBuf* b : bufs) b->release();
     for (auto& b : c->scratch) b.release();
     if (c->h_scalars) cudaFreeHost(c->h_scalars);
@@ -353,7 +355,15 @@ static int barrier_term_impl(Ctx& c, const double* x, double dhat, double dmin, 
         RIGC_TRY(assemble_barrier(c, h));
     }
     RIGC_CUDA(cudaMemcpyAsync(c.h_scalars, e_dev, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    if (h && n > 0)
+        RIGC_CUDA(cudaMemcpyAsync(c.h_scalars + 1, c.d_scalars.as<int32_t>() + 1, sizeof(int32_t),
+                                  cudaMemcpyDeviceToHost, c.stream));
     RIGC_CUDA(cudaStreamSynchronize(c.stream));
+    if (h && n > 0) {
+        int32_t nn;
+        std::memcpy(&nn, c.h_scalars + 1, sizeof(int32_t));
+        c.nnzb = nn;
+    }
     if (out) {
         out->energy = c.h_scalars[0];
         out->nnzb = h ? c.nnzb : 0;
@@ -380,6 +390,17 @@ int rigc_barrier_local_terms(rigc_ctx* ctx, const double* x, double dhat, double
     RIGC_TRY(launch_barrier_local(c, x, dhat, dmin, flags, energy, grad, nullptr, hess));
     RIGC_CUDA(cudaStreamSynchronize(c.stream));
     return RIGC_OK;
+}
+
+int rigc_body_energy(rigc_ctx* ctx, const rigc_body_state* state, const double* x,
+                     const double gravity[3], double h, double* energy_host, double* grad,
+                     double* hess)
+{
+    if (!ctx || !state || !x || !gravity || !energy_host || !(h > 0)) return RIGC_ERR_ARG;
+    if (!state->mass || !state->moment || !state->x_t0 || !state->v_t0 || !state->Qdot_t0
+        || !state->dof_fixed)
+        return RIGC_ERR_ARG;
+    return body_energy(*ctx_of(ctx), *state, x, gravity, h, energy_host, grad, hess);
 }
 
 int rigc_narrow_phase_host(rigc_ctx* ctx, const double* x0_host, const double* x1_host,

@@ -683,12 +683,14 @@ __global__ void k_seg_starts(const int32_t* __restrict__ head, const int32_t* __
 
 // one thread per (unique block, entry): sequential sum in slot order
 __global__ void k_block_sums(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ slots,
-                             const int32_t* __restrict__ seg_start, int32_t nseg, int64_t m,
+                             const int32_t* __restrict__ seg_start,
+                             const int32_t* __restrict__ nseg_ptr, int64_t m,
                              const double* __restrict__ blocks, int nb,
                              int32_t* __restrict__ col, double* __restrict__ val,
                              int32_t* __restrict__ row_count)
 {
     int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int32_t nseg = *nseg_ptr;
     if (t >= (int64_t)nseg * 36) return;
     int32_t sgi = (int32_t)(t / 36);
     int e = (int)(t % 36);
@@ -706,10 +708,12 @@ __global__ void k_block_sums(const uint64_t* __restrict__ keys, const uint32_t* 
 }
 
 __global__ void k_grad_sums(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ slots,
-                            const int32_t* __restrict__ seg_start, int32_t nseg, int64_t m,
+                            const int32_t* __restrict__ seg_start,
+                            const int32_t* __restrict__ nseg_ptr, int64_t m,
                             const double* __restrict__ cgrad, double* __restrict__ grad)
 {
     int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int32_t nseg = *nseg_ptr;
     if (t >= (int64_t)nseg * 6) return;
     int32_t sgi = (int32_t)(t / 6);
     int e = (int)(t % 6);
@@ -760,12 +764,10 @@ int assemble_barrier(Ctx& c, bool with_hess)
         RIGC_TRY(exclusive_scan_i32(head, segid, m, nseg_dev, S[6], st));
         RIGC_COUNT_LAUNCH();
         k_seg_starts<<<grid_for(m, 256), 256, 0, st>>>(head, segid, m, segst);
-        int32_t nseg;
-        RIGC_CUDA(cudaMemcpyAsync(&nseg, nseg_dev, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-        RIGC_CUDA(cudaStreamSynchronize(st));
+        // at most m segments; the kernel reads the true count on the device
         RIGC_COUNT_LAUNCH();
-        k_grad_sums<<<grid_for((int64_t)nseg * 6, 256), 256, 0, st>>>(
-            S[2].as<uint32_t>(), S[3].as<uint32_t>(), segst, nseg, m, c.c_grad.as<double>(),
+        k_grad_sums<<<grid_for(m * 6, 256), 256, 0, st>>>(
+            S[2].as<uint32_t>(), S[3].as<uint32_t>(), segst, nseg_dev, m, c.c_grad.as<double>(),
             c.grad.as<double>());
     }
     if (!with_hess) return RIGC_OK;
@@ -788,18 +790,16 @@ int assemble_barrier(Ctx& c, bool with_hess)
         int32_t* segst = segid + m;
         RIGC_COUNT_LAUNCH();
         k_heads<uint64_t><<<grid_for(m, 256), 256, 0, st>>>(S[2].as<uint64_t>(), m, head);
-        int32_t* nseg_dev = c.d_scalars.as<int32_t>();
+        int32_t* nseg_dev = c.d_scalars.as<int32_t>() + 1;  // read back by the caller
         RIGC_TRY(exclusive_scan_i32(head, segid, m, nseg_dev, S[6], st));
         RIGC_COUNT_LAUNCH();
         k_seg_starts<<<grid_for(m, 256), 256, 0, st>>>(head, segid, m, segst);
-        int32_t nseg;
-        RIGC_CUDA(cudaMemcpyAsync(&nseg, nseg_dev, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-        RIGC_CUDA(cudaStreamSynchronize(st));
-        RIGC_TRY(c.col.reserve((size_t)nseg * sizeof(int32_t)));
-        RIGC_TRY(c.val.reserve((size_t)nseg * 36 * sizeof(double)));
+        // capacity for the upper bound m blocks: no host round trip here
+        RIGC_TRY(c.col.reserve((size_t)m * sizeof(int32_t)));
+        RIGC_TRY(c.val.reserve((size_t)m * 36 * sizeof(double)));
         RIGC_COUNT_LAUNCH();
-        k_block_sums<<<grid_for((int64_t)nseg * 36, 256), 256, 0, st>>>(
-            S[2].as<uint64_t>(), S[3].as<uint32_t>(), segst, nseg, m, c.c_blocks.as<double>(), nb,
+        k_block_sums<<<grid_for(m * 36, 256), 256, 0, st>>>(
+            S[2].as<uint64_t>(), S[3].as<uint32_t>(), segst, nseg_dev, m, c.c_blocks.as<double>(), nb,
             c.col.as<int32_t>(), c.val.as<double>(), c.row_ptr.as<int32_t>() + 1);
         // row counts -> row_ptr (exclusive scan of counts shifted by one)
         int32_t* rp = c.row_ptr.as<int32_t>();
@@ -807,7 +807,7 @@ int assemble_barrier(Ctx& c, bool with_hess)
         RIGC_CUDA(cudaMemcpyAsync(S[4].ptr, rp + 1, (size_t)nb * sizeof(int32_t),
                                   cudaMemcpyDeviceToDevice, st));
         RIGC_TRY(exclusive_scan_i32(S[4].as<int32_t>(), rp, nb, rp + nb, S[6], st));
-        c.nnzb = nseg;
+        c.nnzb = -1;  // on the device (d_scalars int 1) until the caller syncs
     }
     return RIGC_OK;
 }

@@ -22,6 +22,9 @@
 // stack and every search is bounded: on overflow or budget exhaustion the
 // candidate reports the smallest t.lo still unexplored (a conservative time
 // of impact) and an error status.
+#include <algorithm>
+#include <cstring>
+
 #include "common.cuh"
 #include "interval.cuh"
 
@@ -52,6 +55,8 @@ struct CCDArgs {
     int* status;                // worst status
     unsigned long long* boxes;  // total boxes evaluated
     unsigned long long* hits;   // candidates with an impact
+    unsigned long long* next;   // next unprocessed candidate
+    const double* table;        // per-body frames over the top dyadic time intervals
 };
 
 struct Box {
@@ -85,8 +90,60 @@ __device__ __forceinline__ void body_at(const BodyTraj& T, const Itv& t, Itv R[9
     irotation(r, R);
 }
 
+// Interval rotation and position of every body over the dyadic time
+// intervals [k 2^-d, (k + 1) 2^-d] of the first kTableDepth levels of the
+// bisection tree (node (1 << d) - 1 + k), computed once per call and shared by
+// all candidates of the body.  The same operations produce the same bits as
+// evaluating them inside a box.
+constexpr int kTableDepth = 7;                          // levels 0..6
+constexpr int kTableNodes = (1 << kTableDepth) - 1;     // 127
+constexpr int kTableEntry = 24;                         // R (9 intervals) + p (3)
+
+__global__ void k_rot_table(const double* __restrict__ x0, const double* __restrict__ x1, int nb,
+                            double* __restrict__ table)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (int64_t)nb * kTableNodes) return;
+    int b = (int)(i / kTableNodes), node = (int)(i % kTableNodes);
+    int d = 31 - __clz(node + 1);
+    int k = node + 1 - (1 << d);
+    Itv t { ldexp((double)k, -d), ldexp((double)(k + 1), -d) };
+    BodyTraj T;
+    load_traj(x0, x1, b, T);
+    Itv R[9], p[3];
+    body_at(T, t, R, p);
+    double* o = table + (size_t)i * kTableEntry;
+#pragma unroll
+    for (int j = 0; j < 9; j++) {
+        o[2 * j] = R[j].lo;
+        o[2 * j + 1] = R[j].hi;
+    }
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        o[18 + 2 * j] = p[j].lo;
+        o[18 + 2 * j + 1] = p[j].hi;
+    }
+}
+
+// table node of a dyadic interval of depth < kTableDepth, else -1
+__device__ __forceinline__ int table_node(double t0, double t1)
+{
+    int e;
+    double m = frexp(t1 - t0, &e);   // exact for dyadic widths
+    if (m != 0.5) return -1;
+    int d = 1 - e;
+    if (d < 0 || d >= kTableDepth) return -1;
+    double kd = ldexp(t0, d);
+    if (kd != floor(kd) || ldexp(kd + 1.0, -d) != t1) return -1;
+    return (1 << d) - 1 + (int)kd;
+}
+
 struct Query {
     bool fv;            // face-vertex (else edge-edge)
+    bool a_fixed;       // body A does not move: its vertex intervals never change
+    bool b_fixed;
+    int body_a, body_b;
+    const double* table;
     double v[4][3];     // rest vertices: EE (a0, a1, b0, b1); FV (v, f0, f1, f2)
     BodyTraj A, B;      // EE: edge a / edge b bodies; FV: vertex / face bodies
     // cached vertex intervals for one time interval
@@ -94,22 +151,42 @@ struct Query {
     Itv P[4][3];
 };
 
-__device__ __noinline__ void eval_vertices(Query& q, const Itv& t)
+__device__ __forceinline__ bool traj_fixed(const BodyTraj& T)
+{
+    bool z = true;
+#pragma unroll
+    for (int k = 0; k < 6; k++) z = z && T.dx[k].lo == 0.0 && T.dx[k].hi == 0.0;
+    return z;
+}
+
+// vertex intervals of the bodies over t (a body that does not move has
+// t-independent intervals, computed once per query)
+__device__ __forceinline__ void frame_at(const Query& q, const BodyTraj& T, int body, int node,
+                                         const Itv& t, Itv R[9], Itv p[3])
+{
+    if (node >= 0 && q.table) {
+        const double* e = q.table + ((size_t)body * kTableNodes + node) * kTableEntry;
+#pragma unroll
+        for (int j = 0; j < 9; j++) R[j] = Itv { e[2 * j], e[2 * j + 1] };
+#pragma unroll
+        for (int j = 0; j < 3; j++) p[j] = Itv { e[18 + 2 * j], e[18 + 2 * j + 1] };
+    } else {
+        body_at(T, t, R, p);
+    }
+}
+
+static __device__ __noinline__ void eval_vertices(Query& q, const Itv& t, bool all)
 {
     Itv R[9], p[3];
-    body_at(q.A, t, R, p);
-    if (q.fv) {
-        iworld_vertex(R, p, q.v[0], q.P[0]);
-        body_at(q.B, t, R, p);
-        iworld_vertex(R, p, q.v[1], q.P[1]);
-        iworld_vertex(R, p, q.v[2], q.P[2]);
-        iworld_vertex(R, p, q.v[3], q.P[3]);
-    } else {
-        iworld_vertex(R, p, q.v[0], q.P[0]);
-        iworld_vertex(R, p, q.v[1], q.P[1]);
-        body_at(q.B, t, R, p);
-        iworld_vertex(R, p, q.v[2], q.P[2]);
-        iworld_vertex(R, p, q.v[3], q.P[3]);
+    const int na = q.fv ? 1 : 2;
+    const int node = table_node(t.lo, t.hi);
+    if (all || !q.a_fixed) {
+        frame_at(q, q.A, q.body_a, node, t, R, p);
+        for (int i = 0; i < na; i++) iworld_vertex(R, p, q.v[i], q.P[i]);
+    }
+    if (all || !q.b_fixed) {
+        frame_at(q, q.B, q.body_b, node, t, R, p);
+        for (int i = na; i < 4; i++) iworld_vertex(R, p, q.v[i], q.P[i]);
     }
     q.ct0 = t.lo;
     q.ct1 = t.hi;
@@ -119,7 +196,7 @@ __device__ __noinline__ void eval_vertices(Query& q, const Itv& t)
 __device__ __forceinline__ bool f_contains_zero(Query& q, const Box& x)
 {
     Itv t { x.t0, x.t1 };
-    if (!(x.t0 == q.ct0 && x.t1 == q.ct1)) eval_vertices(q, t);
+    if (!(x.t0 == q.ct0 && x.t1 == q.ct1)) eval_vertices(q, t, false);
     Itv a { x.a0, x.a1 }, b { x.b0, x.b1 };
 #pragma unroll
     for (int j = 0; j < 3; j++) {
@@ -138,153 +215,183 @@ __device__ __forceinline__ bool f_contains_zero(Query& q, const Box& x)
     return true;
 }
 
+// load candidate i and its tolerances; returns the time tolerance
+__device__ __forceinline__ void load_query(const CCDArgs& a, int64_t i, Query& q, double tol[3])
+{
+    q.ct0 = q.ct1 = __longlong_as_double(0x7ff8000000000000ll);
+    if (i < a.nee) {
+        q.fv = false;
+        int ea = a.ee[i].x, eb = a.ee[i].y;
+        int va[2] = { a.edges[2 * ea], a.edges[2 * ea + 1] };
+        int vb[2] = { a.edges[2 * eb], a.edges[2 * eb + 1] };
+        for (int j = 0; j < 3; j++) {
+            q.v[0][j] = a.rest[3 * (size_t)va[0] + j];
+            q.v[1][j] = a.rest[3 * (size_t)va[1] + j];
+            q.v[2][j] = a.rest[3 * (size_t)vb[0] + j];
+            q.v[3][j] = a.rest[3 * (size_t)vb[1] + j];
+        }
+        q.body_a = a.ebody[ea];
+        q.body_b = a.ebody[eb];
+        load_traj(a.x0, a.x1, q.body_a, q.A);
+        load_traj(a.x0, a.x1, q.body_b, q.B);
+        tol[1] = RDIV(1e-4, a.edge_len[ea]);
+        tol[2] = RDIV(1e-4, a.edge_len[eb]);
+    } else {
+        q.fv = true;
+        int64_t k = i - a.nee;
+        int f = a.fv[k].x, v = a.fv[k].y;
+        int fvx[3] = { a.faces[3 * f], a.faces[3 * f + 1], a.faces[3 * f + 2] };
+        for (int j = 0; j < 3; j++) {
+            q.v[0][j] = a.rest[3 * (size_t)v + j];
+            q.v[1][j] = a.rest[3 * (size_t)fvx[0] + j];
+            q.v[2][j] = a.rest[3 * (size_t)fvx[1] + j];
+            q.v[3][j] = a.rest[3 * (size_t)fvx[2] + j];
+        }
+        q.body_a = a.vbody[v];
+        q.body_b = a.fbody[f];
+        load_traj(a.x0, a.x1, q.body_a, q.A);
+        load_traj(a.x0, a.x1, q.body_b, q.B);
+        tol[1] = RDIV(1e-4, a.edge_len[a.f2e[3 * f]]);
+        tol[2] = RDIV(1e-4, a.edge_len[a.f2e[3 * f + 1]]);
+    }
+    q.table = a.table;
+    q.a_fixed = traj_fixed(q.A);
+    q.b_fixed = traj_fixed(q.B);
+    tol[0] = a.toi_tol;
+    // every interval of a fixed body is the same for any t: fill all once
+    Box xt { 0.0, tol[0], 0.0, tol[1], 0.0, tol[2] };
+    eval_vertices(q, Itv { xt.t0, xt.t1 }, true);
+    if (f_contains_zero(q, xt)) tol[0] = RDIV(tol[0], 1e2);
+}
+
+// Persistent kernel: each thread takes the next unprocessed candidate from a
+// global counter whenever its box stack runs empty, so lanes of a warp keep
+// evaluating boxes instead of waiting for the warp's longest search.
 __global__ void __launch_bounds__(kCCDThreads)
 k_ccd(CCDArgs a)
 {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t n = a.nee + a.nfv;
-    bool active = i < n;
-    double toi = INFINITY;
+    unsigned long long tot_boxes = 0, tot_hits = 0;
+    Query q;
+    double tol[3];
+    Box stack[kCCDStack];
+    int sp = 0;
+    int64_t cur = -1;
+    double earliest = INFINITY;
     bool found = false;
-    unsigned long long nboxes = 0;
     int status = RIGC_OK;
-    if (active) {
-        Query q;
-        double tol[3];
-        q.ct0 = q.ct1 = __longlong_as_double(0x7ff8000000000000ll);
-        if (i < a.nee) {
-            q.fv = false;
-            int ea = a.ee[i].x, eb = a.ee[i].y;
-            int va[2] = { a.edges[2 * ea], a.edges[2 * ea + 1] };
-            int vb[2] = { a.edges[2 * eb], a.edges[2 * eb + 1] };
-            for (int j = 0; j < 3; j++) {
-                q.v[0][j] = a.rest[3 * (size_t)va[0] + j];
-                q.v[1][j] = a.rest[3 * (size_t)va[1] + j];
-                q.v[2][j] = a.rest[3 * (size_t)vb[0] + j];
-                q.v[3][j] = a.rest[3 * (size_t)vb[1] + j];
-            }
-            load_traj(a.x0, a.x1, a.ebody[ea], q.A);
-            load_traj(a.x0, a.x1, a.ebody[eb], q.B);
-            tol[1] = RDIV(1e-4, a.edge_len[ea]);
-            tol[2] = RDIV(1e-4, a.edge_len[eb]);
-        } else {
-            q.fv = true;
-            int64_t k = i - a.nee;
-            int f = a.fv[k].x, v = a.fv[k].y;
-            int fvx[3] = { a.faces[3 * f], a.faces[3 * f + 1], a.faces[3 * f + 2] };
-            for (int j = 0; j < 3; j++) {
-                q.v[0][j] = a.rest[3 * (size_t)v + j];
-                q.v[1][j] = a.rest[3 * (size_t)fvx[0] + j];
-                q.v[2][j] = a.rest[3 * (size_t)fvx[1] + j];
-                q.v[3][j] = a.rest[3 * (size_t)fvx[2] + j];
-            }
-            load_traj(a.x0, a.x1, a.vbody[v], q.A);
-            load_traj(a.x0, a.x1, a.fbody[f], q.B);
-            tol[1] = RDIV(1e-4, a.edge_len[a.f2e[3 * f]]);
-            tol[2] = RDIV(1e-4, a.edge_len[a.f2e[3 * f + 1]]);
-        }
-        tol[0] = a.toi_tol;
-        {
-            Box xt { 0.0, tol[0], 0.0, tol[1], 0.0, tol[2] };
-            if (f_contains_zero(q, xt)) tol[0] = RDIV(tol[0], 1e2);
-        }
-        Box stack[kCCDStack];
-        int sp = 0;
-        stack[sp++] = Box { 0.0, 1.0, 0.0, 1.0, 0.0, 1.0 };
-        double earliest = INFINITY;
-        double gbound = INFINITY;
-        while (sp > 0) {
-            Box x = stack[--sp];
-            if (x.t0 >= earliest) continue;
-            if (a.prune) {
-                if ((nboxes & 7) == 0) gbound = __longlong_as_double(
-                    (long long)*(volatile unsigned long long*)a.gmin);
-                if (x.t0 >= gbound) continue;
-            }
-            if (q.fv) {
-                double sl = add_dn(x.a0, x.b0), sh = add_up(x.a1, x.b1);
-                if (!(sl <= 1.0 && 0.0 <= sh)) continue;
-            }
-            if (nboxes >= (unsigned long long)a.max_boxes) {
-                // budget exhausted: earliest unexplored t.lo is conservative
-                double m = x.t0;
-                for (int s = 0; s < sp; s++) m = smin(m, stack[s].t0);
-                earliest = smin(earliest, m);
-                found = true;
-                status = RIGC_ERR_ITER_LIMIT;
-                break;
-            }
-            nboxes++;
-            if (!f_contains_zero(q, x)) continue;
-            double w[3] = { sub_up(x.t1, x.t0), sub_up(x.a1, x.a0), sub_up(x.b1, x.b0) };
-            bool all_tol = w[0] <= tol[0] && w[1] <= tol[1] && w[2] <= tol[2];
-            bool all_zero = w[0] <= 1e-10 && w[1] <= 1e-10 && w[2] <= 1e-10;
-            if ((x.t0 > 0 || all_zero) && all_tol) {
-                earliest = x.t0;
-                found = true;
-                if (a.prune) {
-                    atomicMin(a.gmin, (unsigned long long)__double_as_longlong(earliest));
-                    gbound = smin(gbound, earliest);
+    unsigned long long cboxes = 0;
+    double gbound = INFINITY;
+    while (true) {
+        if (sp == 0) {
+            if (cur >= 0) {
+                double toi = found ? earliest : INFINITY;
+                if (found) {
+                    atomicMin(a.gmin, (unsigned long long)__double_as_longlong(toi));
+                    tot_hits++;
                 }
-                continue;
+                if (a.per) a.per[cur] = toi;
+                if (status != RIGC_OK) atomicMax(a.status, status);
             }
-            int split = -1;
-#pragma unroll
-            for (int d = 0; d < 3; d++)
-                if ((all_tol || w[d] > tol[d])
-                    && (split == -1 || RMUL(w[d], tol[split]) > RMUL(w[split], tol[d])))
-                    split = d;
-            Box lo = x, hi = x;
-            if (split == 0) {
-                double m = RMUL(0.5, RADD(x.t0, x.t1));
-                lo.t1 = m;
-                hi.t0 = m;
-            } else if (split == 1) {
-                double m = RMUL(0.5, RADD(x.a0, x.a1));
-                lo.a1 = m;
-                hi.a0 = m;
-            } else {
-                double m = RMUL(0.5, RADD(x.b0, x.b1));
-                lo.b1 = m;
-                hi.b0 = m;
-            }
-            if (sp + 2 > kCCDStack) {
-                // cannot descend: keep the box's start as a conservative root
-                earliest = smin(earliest, x.t0);
-                found = true;
-                status = RIGC_ERR_QUEUE_OVERFLOW;
-                continue;
-            }
-            stack[sp++] = hi;
-            stack[sp++] = lo;
+            cur = (int64_t)atomicAdd(a.next, 1ull);
+            if (cur >= n) break;
+            load_query(a, cur, q, tol);
+            if (a.prune)
+                gbound = __longlong_as_double((long long)*(volatile unsigned long long*)a.gmin);
+            stack[sp++] = Box { 0.0, 1.0, 0.0, 1.0, 0.0, 1.0 };
+            earliest = INFINITY;
+            found = false;
+            status = RIGC_OK;
+            cboxes = 0;
+            continue;
         }
-        toi = found ? earliest : INFINITY;
-        if (found) atomicMin(a.gmin, (unsigned long long)__double_as_longlong(toi));
-        if (a.per) a.per[i] = toi;
-        if (status != RIGC_OK) atomicMax(a.status, status);
+        Box x = stack[--sp];
+        if (x.t0 >= earliest) continue;
+        if (a.prune) {
+            if ((tot_boxes & 7) == 0)
+                gbound = __longlong_as_double((long long)*(volatile unsigned long long*)a.gmin);
+            if (x.t0 >= gbound) continue;
+        }
+        if (q.fv) {
+            double sl = add_dn(x.a0, x.b0), sh = add_up(x.a1, x.b1);
+            if (!(sl <= 1.0 && 0.0 <= sh)) continue;
+        }
+        if (cboxes >= (unsigned long long)a.max_boxes) {
+            // budget exhausted: the earliest unexplored t.lo is conservative
+            double m = x.t0;
+            for (int s = 0; s < sp; s++) m = smin(m, stack[s].t0);
+            earliest = smin(earliest, m);
+            found = true;
+            status = RIGC_ERR_ITER_LIMIT;
+            sp = 0;
+            continue;
+        }
+        cboxes++;
+        tot_boxes++;
+        if (!f_contains_zero(q, x)) continue;
+        double w[3] = { sub_up(x.t1, x.t0), sub_up(x.a1, x.a0), sub_up(x.b1, x.b0) };
+        bool all_tol = w[0] <= tol[0] && w[1] <= tol[1] && w[2] <= tol[2];
+        bool all_zero = w[0] <= 1e-10 && w[1] <= 1e-10 && w[2] <= 1e-10;
+        if ((x.t0 > 0 || all_zero) && all_tol) {
+            earliest = x.t0;
+            found = true;
+            if (a.prune) {
+                atomicMin(a.gmin, (unsigned long long)__double_as_longlong(earliest));
+                gbound = smin(gbound, earliest);
+            }
+            continue;
+        }
+        int split = -1;
+#pragma unroll
+        for (int d = 0; d < 3; d++)
+            if ((all_tol || w[d] > tol[d])
+                && (split == -1 || RMUL(w[d], tol[split]) > RMUL(w[split], tol[d])))
+                split = d;
+        Box lo = x, hi = x;
+        if (split == 0) {
+            double m = RMUL(0.5, RADD(x.t0, x.t1));
+            lo.t1 = m;
+            hi.t0 = m;
+        } else if (split == 1) {
+            double m = RMUL(0.5, RADD(x.a0, x.a1));
+            lo.a1 = m;
+            hi.a0 = m;
+        } else {
+            double m = RMUL(0.5, RADD(x.b0, x.b1));
+            lo.b1 = m;
+            hi.b0 = m;
+        }
+        if (sp + 2 > kCCDStack) {
+            // cannot descend: keep the box's start as a conservative root
+            earliest = smin(earliest, x.t0);
+            found = true;
+            status = RIGC_ERR_QUEUE_OVERFLOW;
+            continue;
+        }
+        stack[sp++] = hi;
+        stack[sp++] = lo;
     }
-    // block-wide counters
-    unsigned long long b = nboxes, h = found ? 1ull : 0ull;
+    // warp-aggregated counters
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        b += __shfl_down_sync(0xffffffffu, b, o);
-        h += __shfl_down_sync(0xffffffffu, h, o);
+        tot_boxes += __shfl_down_sync(0xffffffffu, tot_boxes, o);
+        tot_hits += __shfl_down_sync(0xffffffffu, tot_hits, o);
     }
     if ((threadIdx.x & 31) == 0) {
-        if (b) atomicAdd(a.boxes, b);
-        if (h) atomicAdd(a.hits, h);
+        if (tot_boxes) atomicAdd(a.boxes, tot_boxes);
+        if (tot_hits) atomicAdd(a.hits, tot_hits);
     }
 }
 
-// counters layout in the context's device scalars (after 16 ints):
-// [0] gmin bits, [1] boxes, [2] hits, [3] status
+// counters layout in the context's device scalars (byte offset 256):
+// [0] gmin bits, [1] boxes, [2] hits, [3] status, [4] next candidate
 int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flags,
             double* toi_host, double* per)
 {
     cudaStream_t st = c.stream;
     const int64_t n = c.cand.num_ee + c.cand.num_fv;
     unsigned long long* cnt = reinterpret_cast<unsigned long long*>(c.d_scalars.as<char>() + 256);
-    unsigned long long init[4] = { (unsigned long long)0x7ff0000000000000ull, 0, 0, 0 };
+    unsigned long long init[5] = { (unsigned long long)0x7ff0000000000000ull, 0, 0, 0, 0 };
     RIGC_CUDA(cudaMemcpyAsync(cnt, init, sizeof(init), cudaMemcpyHostToDevice, st));
     if (n > 0) {
         CCDArgs a;
@@ -310,14 +417,32 @@ int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flag
         a.status = reinterpret_cast<int*>(cnt + 3);
         a.boxes = cnt + 1;
         a.hits = cnt + 2;
+        a.next = cnt + 4;
+        RIGC_TRY(c.rot_table.reserve((size_t)c.s.nb * kTableNodes * kTableEntry * sizeof(double)));
         RIGC_COUNT_LAUNCH();
-        k_ccd<<<grid_for(n, kCCDThreads), kCCDThreads, 0, st>>>(a);
+        k_rot_table<<<grid_for((int64_t)c.s.nb * kTableNodes, 128), 128, 0, st>>>(
+            x0, x1, c.s.nb, c.rot_table.as<double>());
+        a.table = c.rot_table.as<double>();
+        static int blocks_per_sm = 0;
+        if (!blocks_per_sm) {
+            RIGC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_ccd,
+                                                                    kCCDThreads, 0));
+            if (blocks_per_sm < 1) blocks_per_sm = 1;
+        }
+        int dev = 0, sms = kNumSMs;
+        RIGC_CUDA(cudaGetDevice(&dev));
+        RIGC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        int64_t want = (n + kCCDThreads - 1) / kCCDThreads;
+        int64_t full = (int64_t)sms * blocks_per_sm;
+        RIGC_COUNT_LAUNCH();
+        k_ccd<<<(unsigned)std::min(want, full), kCCDThreads, 0, st>>>(a);
         RIGC_CUDA(cudaGetLastError());
     }
     unsigned long long out[4];
     RIGC_CUDA(cudaMemcpyAsync(out, cnt, sizeof(out), cudaMemcpyDeviceToHost, st));
     RIGC_CUDA(cudaStreamSynchronize(st));
-    double g = __builtin_bit_cast(double, out[0]);
+    double g;
+    std::memcpy(&g, &out[0], sizeof(g));
     *toi_host = out[2] ? g : INFINITY;
     c.stats.ccd_boxes = (int64_t)out[1];
     c.stats.ccd_candidates = n;

@@ -135,6 +135,8 @@ struct Ctx {
     DevBuf large_list;
     // temporary pose buffers for host entry points
     DevBuf x0_dev, x1_dev;
+    // CCD: body frames over the top dyadic time intervals
+    DevBuf rot_table;
 };
 
 Ctx* ctx_of(rigc_ctx* c);

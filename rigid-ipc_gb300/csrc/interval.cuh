@@ -187,7 +187,7 @@ __device__ __forceinline__ Itv ifmod(const Itv& x, const Itv& y)
     return isub(x, imul(n, y));
 }
 
-__device__ inline Itv icos(Itv x)
+static __device__ __noinline__ Itv icos(Itv x)
 {
     const Itv pi2 { kPiLo * 2, kPiHi * 2 };
     bool negate = false;
@@ -218,7 +218,7 @@ __device__ __forceinline__ Itv isin(const Itv& x)
 }
 
 // sinc of a point (sinc.cpp:36-47)
-__device__ __forceinline__ Itv sinc_taylor(double xd)
+static __device__ __noinline__ Itv sinc_taylor(double xd)
 {
     Itv x = pt(xd);
     if (fabs(xd) >= 1.220703125e-04) return idiv(isin(x), x);
@@ -227,7 +227,7 @@ __device__ __forceinline__ Itv sinc_taylor(double xd)
 }
 
 // sinc over a non-negative interval (sinc.cpp:49-101; the input is a norm)
-__device__ inline Itv isinc_nonneg(const Itv& x)
+static __device__ __noinline__ Itv isinc_nonneg(const Itv& x)
 {
     const double kMono = 4.4934094579;
     Itv y = iempty();
@@ -254,7 +254,7 @@ __device__ __forceinline__ Itv isinc_norm(const Itv r[3])
 }
 
 // interval rotation matrix (pose.tpp:203-218), row-major
-__device__ inline void irotation(const Itv r[3], Itv R[9])
+static __device__ __noinline__ void irotation(const Itv r[3], Itv R[9])
 {
     Itv sa = isinc_norm(r);
     Itv rh[3];

@@ -215,6 +215,41 @@ class Context:
                 "rigc_barrier_local_terms")
         return e[:n].cpu().numpy(), g[:n].cpu().numpy(), H[:n].cpu().numpy()
 
+    def body_state(self, x_t0=None):
+        """Device arrays of the bodies' state at the start of the step."""
+        sc = self.scene
+        t = self.torch
+        dev = dict(device="cuda")
+        fixed = np.array([int(sum(1 << k for k in range(6) if b.is_dof_fixed[k]))
+                          for b in sc.bodies], dtype=np.int32)
+        arrs = dict(
+            mass=t.as_tensor(sc.mass, dtype=t.float64, **dev),
+            moment=t.as_tensor(sc.moment.reshape(-1), dtype=t.float64, **dev),
+            x_t0=self.device(sc.poses() if x_t0 is None else x_t0),
+            v_t0=self.device(sc.velocities()),
+            Qdot_t0=t.as_tensor(np.concatenate([b.Qdot.reshape(-1) for b in sc.bodies]),
+                                dtype=t.float64, **dev),
+            dof_fixed=t.as_tensor(fixed, dtype=t.int32, **dev))
+        return arrs
+
+    def body_energy(self, x, state=None, h=None):
+        """compute_energy_term: (energy, grad[6 nb], hess[nb, 6, 6])."""
+        sc = self.scene
+        st = self.body_state() if state is None else state
+        s = L.BodyState(*[C.c_void_p(st[k].data_ptr()) for k in
+                          ("mass", "moment", "x_t0", "v_t0", "Qdot_t0", "dof_fixed")])
+        xd = self.device(x)
+        t = self.torch
+        g = t.empty(6 * sc.num_bodies, dtype=t.float64, device="cuda")
+        H = t.empty((sc.num_bodies, 6, 6), dtype=t.float64, device="cuda")
+        grav = (C.c_double * 3)(*sc.gravity)
+        e = C.c_double()
+        L.check(self.lib.rigc_body_energy(self.h, C.byref(s), C.c_void_p(xd.data_ptr()), grav,
+                                          sc.timestep if h is None else h, C.byref(e),
+                                          C.c_void_p(g.data_ptr()), C.c_void_p(H.data_ptr())),
+                "rigc_body_energy")
+        return e.value, g.cpu().numpy(), H.cpu().numpy()
+
     def narrow_phase_host(self, x0, x1, dhat, dmin=0.0, nnzb_cap=None):
         """One host-facing narrow-phase pass (host buffers in and out)."""
         nb = self.scene.num_bodies

@@ -31,7 +31,7 @@ EXPORTS = [
     "rigc_get_stats", "rigc_copy", "rigc_world_vertices", "rigc_detect_candidates",
     "rigc_earliest_toi", "rigc_compute_earliest_toi", "rigc_construct_constraint_set",
     "rigc_set_constraints", "rigc_barrier_term", "rigc_barrier_local_terms",
-    "rigc_narrow_phase_host", "rigc_barrier_local_terms_noalloc",
+    "rigc_narrow_phase_host", "rigc_barrier_local_terms_noalloc", "rigc_body_energy",
 ]
 RIGC_ERR_TOO_LARGE = 7
 RIGC_NOALLOC_MAX_BODIES = 4096
@@ -62,6 +62,11 @@ class ConstraintsView(C.Structure):
     _fields_ = [("num", C.c_int64), ("num_vv", C.c_int64), ("num_ev", C.c_int64),
                 ("num_ee", C.c_int64), ("num_fv", C.c_int64), ("type", _vp), ("verts", _vp),
                 ("prims", _vp), ("bodies", _vp), ("weight", _vp), ("eps_x", _vp)]
+
+
+class BodyState(C.Structure):
+    _fields_ = [("mass", _vp), ("moment", _vp), ("x_t0", _vp), ("v_t0", _vp),
+                ("Qdot_t0", _vp), ("dof_fixed", _vp)]
 
 
 class BarrierOut(C.Structure):
@@ -108,6 +113,7 @@ def load():
     L.rigc_barrier_local_terms.argtypes = [_vp, _vp, C.c_double, C.c_double, C.c_int, _vp, _vp, _vp]
     L.rigc_narrow_phase_host.argtypes = [_vp, _vp, _vp, C.c_double, C.c_double, _d, _d, _vp, _vp,
                                          _vp, _vp, C.c_int64, _i64]
+    L.rigc_body_energy.argtypes = [_vp, C.POINTER(BodyState), _vp, _d, C.c_double, _d, _vp, _vp]
     L.rigc_barrier_local_terms_noalloc.argtypes = [
         _vp, C.c_int32, _vp, C.c_int64, _vp, _vp, _vp, _vp, _vp, C.c_double, C.c_double,
         C.c_int, _vp, _vp, _vp, _vp]

@@ -199,6 +199,21 @@ def test_narrow_phase_host_matches_device(cube_scene, cube_contact, ctx_c1):
     assert np.array_equal(rp, rp2) and np.array_equal(col, col2) and np.array_equal(val, val2)
 
 
+def test_body_energy(oracle, cube_scene, cube_contact, ctx_c1):
+    """compute_energy_term per body vs the oracle's autodiff restatement."""
+    sc = cube_scene
+    rng = np.random.default_rng(3)
+    x = cube_contact + rng.normal(0, 0.05, 6 * sc.num_bodies)
+    e_g, g_g, H_g = ctx_c1.body_energy(x)
+    e_sum = 0.0
+    for b, body in enumerate(sc.bodies):
+        e_o, g_o, H_o = oracle.body_energy(body, x[6 * b:6 * b + 6], sc.gravity, sc.timestep)
+        e_sum += e_o
+        assert np.abs(g_g[6 * b:6 * b + 6] - g_o).max() <= GRAD_RTOL * max(np.abs(g_o).max(), 1.0)
+        assert np.linalg.norm(H_g[b] - H_o) <= HESS_RTOL * max(np.linalg.norm(H_o), 1.0)
+    assert abs(e_g - e_sum) <= ENERGY_RTOL * max(abs(e_sum), 1.0)
+
+
 def test_error_statuses(cube_scene, ctx_c1):
     import ctypes as C
 

@@ -205,3 +205,80 @@ def test_ipc_barrier_finite_differences(oracle, s_exp):
         assert hess == pytest.approx(hess_fd, rel=1e-5)
     assert oracle.barrier(s, s) == 0.0 and oracle.barrier(2 * s, s) == 0.0
     assert math.isinf(oracle.barrier(0.0, s))
+
+
+# ---------------------------------------------------------------------------
+# derivative checks of the oracle's own autodiff (the reference checks its
+# energy and barrier derivatives by finite differences the same way,
+# src/problems/distance_barrier_rb_problem.cpp:819-841, 1385-1396)
+
+def test_body_energy_finite_differences(oracle, cube_scene):
+    sc = cube_scene
+    body = sc.bodies[4]
+    rng = np.random.default_rng(2)
+    x = body.pose + rng.normal(0, 0.2, 6)
+    e, g, H = oracle.body_energy(body, x, sc.gravity, sc.timestep)
+    h = 1e-6
+    for i in range(6):
+        xp, xm = x.copy(), x.copy()
+        xp[i] += h
+        xm[i] -= h
+        ep, gp, _ = oracle.body_energy(body, xp, sc.gravity, sc.timestep)
+        em, gm, _ = oracle.body_energy(body, xm, sc.gravity, sc.timestep)
+        assert g[i] == pytest.approx((ep - em) / (2 * h), rel=1e-6, abs=1e-6)
+        assert np.allclose(H[:, i], (gp - gm) / (2 * h), rtol=1e-5, atol=1e-5)
+
+
+def test_barrier_local_terms_finite_differences(oracle, cube_scene):
+    from conftest import contact_poses
+
+    sc = cube_scene
+    x = contact_poses(sc)
+    o = oracle.OracleScene(sc)
+    ee, fv = o.detect_candidates(x, continuous=False, inflation=5e-4)
+    cs = o.constraint_set(x, ee, fv, 1e-3)
+    assert len(cs) > 0
+    e, g, H = o.local_terms(x, cs, 1e-3, project=False)
+    h = 1e-7
+    for ci in range(min(len(cs), 6)):
+        one = oracle.Constraints(cs.types[ci:ci + 1], cs.verts[ci:ci + 1], cs.prims[ci:ci + 1],
+                                 cs.bodies[ci:ci + 1], cs.weight[ci:ci + 1], cs.eps[ci:ci + 1])
+        b0, b1 = cs.bodies[ci]
+        for k in range(12):
+            dof = 6 * (b0 if k < 6 else b1) + k % 6
+            xp, xm = x.copy(), x.copy()
+            xp[dof] += h
+            xm[dof] -= h
+            ep, gp, _ = o.local_terms(xp, one, 1e-3, project=False)
+            em, gm, _ = o.local_terms(xm, one, 1e-3, project=False)
+            assert g[ci][k] == pytest.approx((ep[0] - em[0]) / (2 * h), rel=1e-4,
+                                             abs=1e-6 * np.abs(g[ci]).max())
+            col = (gp[0] - gm[0]) / (2 * h)
+            assert np.allclose(H[ci][:, k], col, rtol=1e-4, atol=1e-5 * np.abs(H[ci]).max())
+
+
+def test_psd_projection_matches_eigh(oracle):
+    rng = np.random.default_rng(0)
+    for _ in range(20):
+        A = rng.normal(size=(12, 12))
+        A = A + A.T
+        P = oracle.project_to_psd(A)
+        w, V = np.linalg.eigh(A)
+        ref = (V * np.maximum(w, 0)) @ V.T
+        assert np.abs(P - ref).max() <= 1e-10 * np.abs(ref).max()
+    S = rng.normal(size=(12, 12))
+    S = S @ S.T + np.eye(12)
+    assert np.array_equal(oracle.project_to_psd(S), S)   # PSD input returned unchanged
+
+
+def test_hash_grid_equals_brute_force(oracle, cube_scene):
+    from conftest import contact_poses
+
+    sc = cube_scene
+    x0 = contact_poses(sc)
+    x1 = sc.predictor_poses(x0)
+    o = oracle.OracleScene(sc)
+    for cont, infl in ((True, 0.0), (False, 5e-4), (False, 1e-2)):
+        a = o.detect_candidates(x0, x1, cont, infl)
+        b = o.detect_candidates(x0, x1, cont, infl, brute=True)
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
