@@ -72,7 +72,8 @@ static void release_all(Ctx* c)
                        &c->d_scalars, &c->body_box, &c->body_in, &c->vbox, &c->ebox, &c->fbox,
                        &c->vin, &c->ein, &c->fin, &c->items_key, &c->items_val, &c->items_key2,
                        &c->items_val2, &c->seg, &c->pair_out, &c->pair_key, &c->large_list,
-                       &c->x0_dev, &c->x1_dev, &c->rot_table };
+                       &c->x0_dev, &c->x1_dev, &c->rot_table, &c->frame_keys,
+                       &c->frame_vals };
     for (DevBuf* b : bufs) b->release();
     for (auto& b : c->scratch) b.release();
     if (c->h_scalars) cudaFreeHost(c->h_scalars);

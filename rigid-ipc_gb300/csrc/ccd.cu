@@ -18,7 +18,11 @@
 // not depend on the order boxes are visited, so boxes whose t.lo is not below
 // the running minimum over all candidates can be skipped too: that never
 // changes the minimum.  One thread per candidate, a depth-first stack in
-// local memory, the interval vertex positions cached per time interval.  Every
+// local memory, the interval vertex positions cached per time interval.  The
+// interval frames R(t), p(t) of a body depend only on the body and the time
+// interval, which is always a node of the dyadic bisection tree of [0, 1]:
+// the top levels come from a table built per call, deeper nodes from a hash
+// table filled on first use and shared by all candidates of the body.  Every
 // stack and every search is bounded: on overflow or budget exhaustion the
 // candidate reports the smallest t.lo still unexplored (a conservative time
 // of impact) and an error status.
@@ -57,6 +61,9 @@ struct CCDArgs {
     unsigned long long* hits;   // candidates with an impact
     unsigned long long* next;   // next unprocessed candidate
     const double* table;        // per-body frames over the top dyadic time intervals
+    unsigned long long* fkeys;  // frame cache: keys (0 = empty)
+    double* fvals;              // frame cache: kTableEntry doubles per slot
+    unsigned long long fmask;   // slots - 1 (a power of two)
 };
 
 struct Box {
@@ -90,6 +97,64 @@ __device__ __forceinline__ void body_at(const BodyTraj& T, const Itv& t, Itv R[9
     irotation(r, R);
 }
 
+// Bisection-tree node of a time interval: (1 << d) + k for [k 2^-d, (k + 1) 2^-d]
+// with d < kNodeDepth, else 0.  Every time interval of the search is such a
+// node (midpoints of dyadic intervals are exact), up to depth 1074.
+constexpr int kNodeDepth = 40;
+
+__device__ __forceinline__ unsigned long long time_node(double t0, double t1)
+{
+    int e;
+    double m = frexp(t1 - t0, &e);   // exact for dyadic widths
+    if (m != 0.5) return 0;
+    int d = 1 - e;
+    if (d < 0 || d >= kNodeDepth) return 0;
+    double kd = ldexp(t0, d);
+    if (kd != floor(kd) || ldexp(kd + 1.0, -d) != t1) return 0;
+    return (1ull << d) + (unsigned long long)kd;
+}
+
+// Frame cache: an open-addressing hash table of (body, time node) -> R(t),
+// p(t) intervals shared by every thread of the launch.  A slot is claimed by
+// a compare-and-swap of its key with the pending bit set, filled, and
+// published by clearing the bit after a fence; readers acquire the key and
+// read the frame through L2.  A thread that meets a pending slot, or that
+// finds no slot within kProbes, computes the frame itself: the cache only
+// skips recomputation, the bits are the same either way.
+constexpr unsigned long long kPending = 1ull << 63;
+constexpr int kProbes = 16;
+
+__device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long* p)
+{
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ unsigned long long mix64(unsigned long long x)
+{
+    x ^= x >> 33;
+    x *= 0xff51afd7ed558ccdull;
+    x ^= x >> 33;
+    x *= 0xc4ceb9fe1a85ec53ull;
+    x ^= x >> 33;
+    return x;
+}
+
+__device__ __forceinline__ void frame_store(double* o, const Itv R[9], const Itv p[3])
+{
+#pragma unroll
+    for (int j = 0; j < 9; j++) {
+        o[2 * j] = R[j].lo;
+        o[2 * j + 1] = R[j].hi;
+    }
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        o[18 + 2 * j] = p[j].lo;
+        o[18 + 2 * j + 1] = p[j].hi;
+    }
+}
+
 // Interval rotation and position of every body over the dyadic time
 // intervals [k 2^-d, (k + 1) 2^-d] of the first kTableDepth levels of the
 // bisection tree (node (1 << d) - 1 + k), computed once per call and shared by
@@ -112,31 +177,9 @@ __global__ void k_rot_table(const double* __restrict__ x0, const double* __restr
     load_traj(x0, x1, b, T);
     Itv R[9], p[3];
     body_at(T, t, R, p);
-    double* o = table + (size_t)i * kTableEntry;
-#pragma unroll
-    for (int j = 0; j < 9; j++) {
-        o[2 * j] = R[j].lo;
-        o[2 * j + 1] = R[j].hi;
-    }
-#pragma unroll
-    for (int j = 0; j < 3; j++) {
-        o[18 + 2 * j] = p[j].lo;
-        o[18 + 2 * j + 1] = p[j].hi;
-    }
+    frame_store(table + (size_t)i * kTableEntry, R, p);
 }
 
-// table node of a dyadic interval of depth < kTableDepth, else -1
-__device__ __forceinline__ int table_node(double t0, double t1)
-{
-    int e;
-    double m = frexp(t1 - t0, &e);   // exact for dyadic widths
-    if (m != 0.5) return -1;
-    int d = 1 - e;
-    if (d < 0 || d >= kTableDepth) return -1;
-    double kd = ldexp(t0, d);
-    if (kd != floor(kd) || ldexp(kd + 1.0, -d) != t1) return -1;
-    return (1 << d) - 1 + (int)kd;
-}
 
 struct Query {
     bool fv;            // face-vertex (else edge-edge)
@@ -144,6 +187,9 @@ struct Query {
     bool b_fixed;
     int body_a, body_b;
     const double* table;
+    unsigned long long* fkeys;
+    double* fvals;
+    unsigned long long fmask;
     double v[4][3];     // rest vertices: EE (a0, a1, b0, b1); FV (v, f0, f1, f2)
     BodyTraj A, B;      // EE: edge a / edge b bodies; FV: vertex / face bodies
     // cached vertex intervals for one time interval
@@ -161,15 +207,57 @@ __device__ __forceinline__ bool traj_fixed(const BodyTraj& T)
 
 // vertex intervals of the bodies over t (a body that does not move has
 // t-independent intervals, computed once per query)
-__device__ __forceinline__ void frame_at(const Query& q, const BodyTraj& T, int body, int node,
-                                         const Itv& t, Itv R[9], Itv p[3])
+__device__ __forceinline__ void frame_load(const double* e, Itv R[9], Itv p[3])
 {
-    if (node >= 0 && q.table) {
-        const double* e = q.table + ((size_t)body * kTableNodes + node) * kTableEntry;
 #pragma unroll
-        for (int j = 0; j < 9; j++) R[j] = Itv { e[2 * j], e[2 * j + 1] };
+    for (int j = 0; j < 9; j++) R[j] = Itv { e[2 * j], e[2 * j + 1] };
 #pragma unroll
-        for (int j = 0; j < 3; j++) p[j] = Itv { e[18 + 2 * j], e[18 + 2 * j + 1] };
+    for (int j = 0; j < 3; j++) p[j] = Itv { e[18 + 2 * j], e[18 + 2 * j + 1] };
+}
+
+__device__ __forceinline__ void frame_load_cg(const double* e, Itv R[9], Itv p[3])
+{
+#pragma unroll
+    for (int j = 0; j < 9; j++) R[j] = Itv { __ldcg(e + 2 * j), __ldcg(e + 2 * j + 1) };
+#pragma unroll
+    for (int j = 0; j < 3; j++) p[j] = Itv { __ldcg(e + 18 + 2 * j), __ldcg(e + 19 + 2 * j) };
+}
+
+static __device__ __noinline__ void frame_cached(const Query& q, const BodyTraj& T, int body,
+                                                 unsigned long long node, const Itv& t,
+                                                 Itv R[9], Itv p[3])
+{
+    const unsigned long long key = ((unsigned long long)(body + 1) << kNodeDepth) | node;
+    unsigned long long h = mix64(key);
+    for (int probe = 0; probe < kProbes; probe++, h++) {
+        unsigned long long* slot = q.fkeys + (h & q.fmask);
+        unsigned long long k = ld_acquire(slot);
+        if (k == 0) {
+            k = atomicCAS(slot, 0ull, key | kPending);
+            if (k == 0) {
+                body_at(T, t, R, p);
+                frame_store(q.fvals + (h & q.fmask) * kTableEntry, R, p);
+                __threadfence();
+                atomicExch(slot, key);
+                return;
+            }
+        }
+        if (k == key) {
+            frame_load_cg(q.fvals + (h & q.fmask) * kTableEntry, R, p);
+            return;
+        }
+        if (k == (key | kPending)) break;
+    }
+    body_at(T, t, R, p);
+}
+
+__device__ __forceinline__ void frame_at(const Query& q, const BodyTraj& T, int body,
+                                         unsigned long long node, const Itv& t, Itv R[9], Itv p[3])
+{
+    if (node != 0 && node < (1ull << kTableDepth) && q.table) {
+        frame_load(q.table + ((size_t)body * kTableNodes + (node - 1)) * kTableEntry, R, p);
+    } else if (node != 0 && q.fkeys) {
+        frame_cached(q, T, body, node, t, R, p);
     } else {
         body_at(T, t, R, p);
     }
@@ -179,7 +267,7 @@ static __device__ __noinline__ void eval_vertices(Query& q, const Itv& t, bool a
 {
     Itv R[9], p[3];
     const int na = q.fv ? 1 : 2;
-    const int node = table_node(t.lo, t.hi);
+    const unsigned long long node = time_node(t.lo, t.hi);
     if (all || !q.a_fixed) {
         frame_at(q, q.A, q.body_a, node, t, R, p);
         for (int i = 0; i < na; i++) iworld_vertex(R, p, q.v[i], q.P[i]);
@@ -255,6 +343,9 @@ __device__ __forceinline__ void load_query(const CCDArgs& a, int64_t i, Query& q
         tol[2] = RDIV(1e-4, a.edge_len[a.f2e[3 * f + 1]]);
     }
     q.table = a.table;
+    q.fkeys = a.fkeys;
+    q.fvals = a.fvals;
+    q.fmask = a.fmask;
     q.a_fixed = traj_fixed(q.A);
     q.b_fixed = traj_fixed(q.B);
     tol[0] = a.toi_tol;
@@ -423,6 +514,15 @@ int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flag
         k_rot_table<<<grid_for((int64_t)c.s.nb * kTableNodes, 128), 128, 0, st>>>(
             x0, x1, c.s.nb, c.rot_table.as<double>());
         a.table = c.rot_table.as<double>();
+        // frame cache: 1024 slots per body, at least 2^16, at most 2^22
+        size_t slots = 1u << 16;
+        while (slots < (size_t)c.s.nb * 1024 && slots < (1u << 22)) slots <<= 1;
+        RIGC_TRY(c.frame_keys.reserve(slots * sizeof(unsigned long long)));
+        RIGC_TRY(c.frame_vals.reserve(slots * kTableEntry * sizeof(double)));
+        RIGC_CUDA(cudaMemsetAsync(c.frame_keys.ptr, 0, slots * sizeof(unsigned long long), st));
+        a.fkeys = c.frame_keys.as<unsigned long long>();
+        a.fvals = c.frame_vals.as<double>();
+        a.fmask = slots - 1;
         static int blocks_per_sm = 0;
         if (!blocks_per_sm) {
             RIGC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_ccd,

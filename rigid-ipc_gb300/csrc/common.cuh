@@ -137,6 +137,7 @@ struct Ctx {
     DevBuf x0_dev, x1_dev;
     // CCD: body frames over the top dyadic time intervals
     DevBuf rot_table;
+    DevBuf frame_keys, frame_vals;  // CCD frame cache (hash table)
 };
 
 Ctx* ctx_of(rigc_ctx* c);
