@@ -212,6 +212,53 @@ int rigc_body_energy(rigc_ctx* ctx, const rigc_body_state* state,
                      const double* x, const double gravity[3], double h,
                      double* energy_host, double* grad, double* hess);
 
+/* ---- lagged friction.
+ * rigc_friction_setup replaces
+ * DistanceBarrierRBProblem::update_friction_constraints
+ * (src/problems/distance_barrier_rb_problem.cpp:168-188): from the context's
+ * current collision constraint set (built by rigc_construct_constraint_set
+ * at the start-of-step poses x_t0, device) it builds the friction constraints
+ * of ipc-toolkit's construct_friction_constraint_set: per constraint the
+ * normal force magnitude lambda = -kappa w b'(d) 2 sqrt(d) (dhat the barrier
+ * activation distance, w the multiplicity), the closest-point parameters and
+ * an orthonormal tangent basis at x_t0; coefficient_friction (mu) is kept
+ * with them.  The set stays fixed until the next setup, as the reference
+ * keeps it through a lagging iteration.  num_out (host, may be NULL). */
+int rigc_friction_setup(rigc_ctx* ctx, const double* x_t0, double dhat,
+                        double barrier_stiffness, double coefficient_friction,
+                        int64_t* num_out);
+
+/* Friction constraints as built (device pointers, valid until the next
+ * setup): type / verts x 4 / bodies x 2 as rigc_constraints; coef x 9 per
+ * constraint = lambda, closest-point parameters (EV alpha; EE alpha, beta;
+ * FV b1, b2; 0 otherwise), tangent basis t1 (3), t2 (3). */
+typedef struct rigc_friction_view {
+    int64_t num;
+    double mu;
+    const int32_t* type;
+    const int32_t* verts;
+    const int32_t* bodies;
+    const double* coef;
+} rigc_friction_view;
+int rigc_get_friction(rigc_ctx* ctx, rigc_friction_view* out);
+
+/* Friction potential D(x) = sum mu lambda f0(|T^T Gamma (V(x) - V(x_t0))|)
+ * with its body gradient and PSD-projected block-sparse Hessian:
+ * DistanceBarrierRBProblem::compute_friction_term
+ * (src/problems/distance_barrier_rb_problem.cpp:1469-1572) with
+ * epsv_times_h = static_friction_speed_bound * timestep (:1436).  Outputs
+ * as rigc_barrier_term (own buffers: a friction term and a barrier term can
+ * be held at the same time). */
+int rigc_friction_term(rigc_ctx* ctx, const double* x, double epsv_times_h,
+                       int flags, rigc_barrier_out* out);
+
+/* Per-constraint friction energy, body gradient (12) and 12x12 Hessian
+ * before assembly (compute_friction_potential, :1411-1467).  Device outputs;
+ * any may be NULL. */
+int rigc_friction_local_terms(rigc_ctx* ctx, const double* x,
+                              double epsv_times_h, int flags, double* energy,
+                              double* grad, double* hess);
+
 /* ---- one narrow-phase pass from host memory (the call a host Newton loop
  * makes per iteration): copies x0/x1 in, runs compute_earliest_toi(x0, x1)
  * and construct_constraint_set + compute_barrier_term at x0, copies the

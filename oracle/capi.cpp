@@ -340,4 +340,85 @@ void orc_interval_rotation(const double* rlo, const double* rhi, double* Rlo, do
 double orc_det_sin(double x) { return det_sin(x); }
 double orc_det_cos(double x) { return det_cos(x); }
 
+
+// ---------------------------------------------------------------------------
+// lagged friction
+
+static std::vector<FrictionConstraint> unpack_friction(
+    const std::vector<Constraint>& cs, const double* lambda, const double* params,
+    const double* T)
+{
+    std::vector<FrictionConstraint> fcs(cs.size());
+    for (size_t i = 0; i < cs.size(); i++) {
+        fcs[i].c = cs[i];
+        fcs[i].lambda = lambda[i];
+        fcs[i].p0 = params[2 * i];
+        fcs[i].p1 = params[2 * i + 1];
+        for (int k = 0; k < 6; k++) fcs[i].T[k] = T[6 * i + k];
+    }
+    return fcs;
+}
+
+void orc_friction_constraints(
+    void* p, const double* x0, long long n, const int* types, const int* verts,
+    const int* prims, const int* bodies, const double* weight, const double* eps,
+    double dhat, double dmin, double kappa, double* lambda, double* params, double* T)
+{
+    const Scene& s = static_cast<OwnedScene*>(p)->s;
+    auto cs = unpack_constraints(n, types, verts, prims, bodies, weight, eps);
+    std::vector<double> V0;
+    world_vertices(s, x0, V0);
+    std::vector<FrictionConstraint> fcs;
+    construct_friction_constraints(s, cs, V0, dhat, dmin, kappa, fcs);
+    for (long long i = 0; i < n; i++) {
+        lambda[i] = fcs[i].lambda;
+        params[2 * i] = fcs[i].p0;
+        params[2 * i + 1] = fcs[i].p1;
+        for (int k = 0; k < 6; k++) T[6 * i + k] = fcs[i].T[k];
+    }
+}
+
+void orc_friction_local_terms(
+    void* p, const double* x, const double* x0, long long n, const int* types,
+    const int* verts, const int* prims, const int* bodies, const double* weight,
+    const double* eps, const double* lambda, const double* params, const double* T,
+    double mu, double epsvh, int project, double* energy, double* grad, double* hess)
+{
+    const Scene& s = static_cast<OwnedScene*>(p)->s;
+    auto cs = unpack_constraints(n, types, verts, prims, bodies, weight, eps);
+    auto fcs = unpack_friction(cs, lambda, params, T);
+    std::vector<double> V, dV, d2V, V0;
+    world_vertices_diff(s, x, V, dV, d2V);
+    world_vertices(s, x0, V0);
+    for (long long i = 0; i < n; i++) {
+        LocalTerm t;
+        friction_local_term(s, fcs[i], V, V0, dV, d2V, mu, epsvh, project != 0, t);
+        energy[i] = t.energy;
+        std::memcpy(grad + 12 * i, t.grad, 12 * sizeof(double));
+        std::memcpy(hess + 144 * i, t.hess, 144 * sizeof(double));
+    }
+}
+
+int orc_friction_term(
+    void* p, const double* x, const double* x0, long long n, const int* types,
+    const int* verts, const int* prims, const int* bodies, const double* weight,
+    const double* eps, const double* lambda, const double* params, const double* T,
+    double mu, double epsvh, int project, double* energy, double* grad, int* row_ptr,
+    int* col, double* val, long long cap, long long* nnzb)
+{
+    const Scene& s = static_cast<OwnedScene*>(p)->s;
+    auto cs = unpack_constraints(n, types, verts, prims, bodies, weight, eps);
+    auto fcs = unpack_friction(cs, lambda, params, T);
+    std::vector<double> g;
+    BSR h;
+    *energy = friction_term(s, x, x0, fcs, mu, epsvh, g, h, project != 0);
+    std::memcpy(grad, g.data(), g.size() * sizeof(double));
+    *nnzb = (long long)h.col.size();
+    if (*nnzb > cap) return 1;
+    std::memcpy(row_ptr, h.row_ptr.data(), h.row_ptr.size() * sizeof(int));
+    std::memcpy(col, h.col.data(), h.col.size() * sizeof(int));
+    std::memcpy(val, h.val.data(), h.val.size() * sizeof(double));
+    return 0;
+}
+
 } // extern "C"

@@ -1028,4 +1028,47 @@ void friction_local_term(
     else std::copy(H, H + 144, out.hess);
 }
 
+// assembled friction term (compute_friction_term,
+// distance_barrier_rb_problem.cpp:1469-1572): U = V(x) - V(x_t0)
+double friction_term(
+    const Scene& s, const double* x, const double* x0, const std::vector<FrictionConstraint>& fcs,
+    double mu, double epsvh, std::vector<double>& grad, BSR& hess, bool project)
+{
+    std::vector<double> V, dV, d2V, V0;
+    world_vertices_diff(s, x, V, dV, d2V);
+    world_vertices(s, x0, V0);
+    grad.assign(6 * s.nb, 0.0);
+    std::map<std::pair<int, int>, std::array<double, 36>> blocks;
+    double energy = 0;
+    for (const auto& f : fcs) {
+        LocalTerm t;
+        friction_local_term(s, f, V, V0, dV, d2V, mu, epsvh, project, t);
+        energy += t.energy;
+        for (int lb = 0; lb < 2; lb++)
+            for (int k = 0; k < 6; k++) grad[6 * f.c.body[lb] + k] += t.grad[6 * lb + k];
+        for (int bi = 0; bi < 2; bi++)
+            for (int bj = 0; bj < 2; bj++) {
+                auto key = std::make_pair(f.c.body[bi], f.c.body[bj]);
+                auto it = blocks.find(key);
+                if (it == blocks.end()) {
+                    std::array<double, 36> z {};
+                    it = blocks.emplace(key, z).first;
+                }
+                for (int r = 0; r < 6; r++)
+                    for (int q = 0; q < 6; q++)
+                        it->second[6 * r + q] += t.hess[12 * (6 * bi + r) + 6 * bj + q];
+            }
+    }
+    hess.row_ptr.assign(s.nb + 1, 0);
+    hess.col.clear();
+    hess.val.clear();
+    for (const auto& kv : blocks) hess.row_ptr[kv.first.first + 1]++;
+    for (int i = 0; i < s.nb; i++) hess.row_ptr[i + 1] += hess.row_ptr[i];
+    for (const auto& kv : blocks) {
+        hess.col.push_back(kv.first.second);
+        hess.val.insert(hess.val.end(), kv.second.begin(), kv.second.end());
+    }
+    return energy;
+}
+
 } // namespace orc

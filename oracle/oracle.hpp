@@ -273,6 +273,9 @@ void friction_local_term(
     const Scene& s, const FrictionConstraint& f, const std::vector<double>& V,
     const std::vector<double>& V0, const std::vector<double>& dV,
     const std::vector<double>& d2V, double mu, double epsvh, bool project, LocalTerm& out);
+double friction_term(
+    const Scene& s, const double* x, const double* x0, const std::vector<FrictionConstraint>& fcs,
+    double mu, double epsvh, std::vector<double>& grad, BSR& hess, bool project);
 
 // ---------------------------------------------------------------------------
 // broad phase

@@ -56,6 +56,14 @@ def lib():
                                          C.c_longlong, _ll]
         L.orc_local_terms.argtypes = [C.c_void_p, _d, C.c_longlong, _i, _i, _i, _i, _d, _d,
                                       C.c_double, C.c_double, C.c_int, _d, _d, _d]
+        L.orc_friction_constraints.argtypes = [C.c_void_p, _d, C.c_longlong, _i, _i, _i, _i, _d,
+                                               _d, C.c_double, C.c_double, C.c_double, _d, _d, _d]
+        L.orc_friction_local_terms.argtypes = [C.c_void_p, _d, _d, C.c_longlong, _i, _i, _i, _i,
+                                               _d, _d, _d, _d, _d, C.c_double, C.c_double, C.c_int,
+                                               _d, _d, _d]
+        L.orc_friction_term.argtypes = [C.c_void_p, _d, _d, C.c_longlong, _i, _i, _i, _i, _d, _d,
+                                        _d, _d, _d, C.c_double, C.c_double, C.c_int, _d, _d, _i,
+                                        _i, _d, C.c_longlong, _ll]
         L.orc_barrier_term.argtypes = [C.c_void_p, _d, C.c_longlong, _i, _i, _i, _i, _d, _d,
                                        C.c_double, C.c_double, C.c_int, _d, _d, _i, _i, _d,
                                        C.c_longlong, _ll]
@@ -212,6 +220,59 @@ class OracleScene:
                               _p(cs.eps, _d), dhat, dmin, int(project), _p(e, _d), _p(g, _d),
                               _p(H, _d))
         return e, g, H
+
+    # ---- lagged friction
+    def friction_constraints(self, x0, cs: Constraints, dhat, kappa, dmin=0.0):
+        """(lambda[n], closest[n, 2], basis[n, 2, 3]) at the start-of-step poses x0."""
+        x0 = _dd(x0)
+        n = len(cs)
+        lam = np.zeros(max(n, 1))
+        params = np.zeros((max(n, 1), 2))
+        T = np.zeros((max(n, 1), 6))
+        lib().orc_friction_constraints(self.h, _p(x0, _d), n, _p(cs.types, _i), _p(cs.verts, _i),
+                                       _p(cs.prims, _i), _p(cs.bodies, _i), _p(cs.weight, _d),
+                                       _p(cs.eps, _d), dhat, dmin, kappa, _p(lam, _d),
+                                       _p(params, _d), _p(T, _d))
+        return lam[:n], params[:n], T[:n].reshape(n, 2, 3)
+
+    def _fric_args(self, cs, fc):
+        lam, params, T = fc
+        n = len(cs)
+        lam = _dd(lam) if n else np.zeros(1)
+        params = _dd(params).reshape(-1) if n else np.zeros(2)
+        T = _dd(T).reshape(-1) if n else np.zeros(6)
+        return (n, _p(cs.types, _i), _p(cs.verts, _i), _p(cs.prims, _i), _p(cs.bodies, _i),
+                _p(cs.weight, _d), _p(cs.eps, _d), _p(lam, _d), _p(params, _d), _p(T, _d)), \
+            (lam, params, T)
+
+    def friction_local_terms(self, x, x0, cs: Constraints, fc, mu, epsvh, project=True):
+        x, x0 = _dd(x), _dd(x0)
+        n = len(cs)
+        e = np.empty(max(n, 1))
+        g = np.empty((max(n, 1), 12))
+        H = np.empty((max(n, 1), 12, 12))
+        args, keep = self._fric_args(cs, fc)
+        lib().orc_friction_local_terms(self.h, _p(x, _d), _p(x0, _d), *args, mu, epsvh,
+                                       int(project), _p(e, _d), _p(g, _d), _p(H, _d))
+        return e[:n], g[:n], H[:n]
+
+    def friction_term(self, x, x0, cs: Constraints, fc, mu, epsvh, project=True):
+        x, x0 = _dd(x), _dd(x0)
+        nb = self.scene.num_bodies
+        grad = np.zeros(6 * nb)
+        cap = 4 * len(cs) + 1
+        row_ptr = np.zeros(nb + 1, np.int32)
+        col = np.zeros(cap, np.int32)
+        val = np.zeros((cap, 6, 6))
+        energy = C.c_double()
+        nnzb = C.c_longlong()
+        args, keep = self._fric_args(cs, fc)
+        rc = lib().orc_friction_term(self.h, _p(x, _d), _p(x0, _d), *args, mu, epsvh, int(project),
+                                     C.byref(energy), _p(grad, _d), _p(row_ptr, _i), _p(col, _i),
+                                     _p(val, _d), cap, C.byref(nnzb))
+        assert rc == 0
+        k = nnzb.value
+        return energy.value, grad, (row_ptr, col[:k], val[:k])
 
     def barrier_term(self, x, cs: Constraints, dhat, dmin=0.0, project=True):
         x = _dd(x)

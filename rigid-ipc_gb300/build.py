@@ -4,7 +4,7 @@ Each translation unit is compiled by nvcc in parallel, then linked into one
 shared library exporting the C ABI of ``include/rigc.h``.  Units whose exact
 decisions must match a round-to-nearest restatement bit for bit (broad phase,
 constraint set, CCD) are compiled without fused multiply-add contraction;
-the barrier derivatives allow it.
+the barrier, friction and body-energy derivatives allow it.
 """
 from __future__ import annotations
 
@@ -30,6 +30,7 @@ UNITS = {
     "ccd.cu": ["--fmad=false"],
     "noalloc.cu": ["--fmad=false"],
     "body.cu": ["--fmad=true"],
+    "friction.cu": ["--fmad=true"],
 }
 
 

@@ -19,6 +19,10 @@ int compute_world_vertices_rn(Ctx& c, const double* x, double* V, DevBuf& rotbuf
 int sum_f64(const double* in, int64_t n, double* out_dev, DevBuf& tmp, cudaStream_t stream);
 int body_energy(Ctx& c, const rigc_body_state& s, const double* x, const double gravity[3],
                 double h, double* energy_host, double* grad, double* hess);
+int friction_setup(Ctx& c, const double* x0, double dhat, double kappa, double mu, double dmin);
+int launch_friction_local(Ctx& c, const double* x, double epsvh, int flags, double* energy,
+                          double* grad, double* blocks, double* hess);
+int friction_term(Ctx& c, const double* x, double epsvh, int flags, rigc_barrier_out* out);
 
 static thread_local std::string g_last_error;
 static std::atomic<int64_t> g_launches { 0 };
@@ -73,7 +77,10 @@ static void release_all(Ctx* c)
                        &c->vin, &c->ein, &c->fin, &c->items_key, &c->items_val, &c->items_key2,
                        &c->items_val2, &c->seg, &c->pair_out, &c->pair_key, &c->large_list,
                        &c->x0_dev, &c->x1_dev, &c->rot_table, &c->frame_keys,
-                       &c->frame_vals };
+                       &c->frame_vals, &c->fric.type, &c->fric.verts, &c->fric.bodies,
+                       &c->fric.coef, &c->fric.v0c, &c->fric.V0, &c->fric.c_energy,
+                       &c->fric.c_grad, &c->fric.c_blocks, &c->fric.grad, &c->fric.row_ptr,
+                       &c->fric.col, &c->fric.val };
     for (DevBuf* b : bufs) b->release();
     for (auto& b : c->scratch) b.release();
     if (c->h_scalars) cudaFreeHost(c->h_scalars);
@@ -402,6 +409,47 @@ int rigc_body_energy(rigc_ctx* ctx, const rigc_body_state* state, const double* 
         || !state->dof_fixed)
         return RIGC_ERR_ARG;
     return body_energy(*ctx_of(ctx), *state, x, gravity, h, energy_host, grad, hess);
+}
+
+int rigc_friction_setup(rigc_ctx* ctx, const double* x_t0, double dhat, double barrier_stiffness,
+                        double coefficient_friction, int64_t* num_out)
+{
+    if (!ctx || !x_t0 || !(dhat > 0) || !(barrier_stiffness >= 0) || !(coefficient_friction >= 0))
+        return RIGC_ERR_ARG;
+    Ctx& c = *ctx_of(ctx);
+    RIGC_TRY(friction_setup(c, x_t0, dhat, barrier_stiffness, coefficient_friction, 0.0));
+    if (num_out) *num_out = c.fric.num;
+    return RIGC_OK;
+}
+
+int rigc_get_friction(rigc_ctx* ctx, rigc_friction_view* out)
+{
+    if (!ctx || !out) return RIGC_ERR_ARG;
+    Friction& F = ctx_of(ctx)->fric;
+    out->num = F.num;
+    out->mu = F.mu;
+    out->type = F.type.as<int32_t>();
+    out->verts = F.verts.as<int32_t>();
+    out->bodies = F.bodies.as<int32_t>();
+    out->coef = F.coef.as<double>();
+    return RIGC_OK;
+}
+
+int rigc_friction_term(rigc_ctx* ctx, const double* x, double epsv_times_h, int flags,
+                       rigc_barrier_out* out)
+{
+    if (!ctx || !x || !(epsv_times_h > 0)) return RIGC_ERR_ARG;
+    return friction_term(*ctx_of(ctx), x, epsv_times_h, flags, out);
+}
+
+int rigc_friction_local_terms(rigc_ctx* ctx, const double* x, double epsv_times_h, int flags,
+                              double* energy, double* grad, double* hess)
+{
+    if (!ctx || !x || !(epsv_times_h > 0)) return RIGC_ERR_ARG;
+    Ctx& c = *ctx_of(ctx);
+    RIGC_TRY(launch_friction_local(c, x, epsv_times_h, flags, energy, grad, nullptr, hess));
+    RIGC_CUDA(cudaStreamSynchronize(c.stream));
+    return RIGC_OK;
 }
 
 int rigc_narrow_phase_host(rigc_ctx* ctx, const double* x0_host, const double* x1_host,

@@ -23,10 +23,13 @@
 // f = weight * m(D) * b(d - dmin^2) (m = 1 except mollified EE), so the body
 // Hessian is  sum of outer products of the body-space gradients of the basic
 // scalars + Gram terms + skew pair blocks + the curvature term
-// sum_i grad_Xi f . d2X_i/dtheta2.  It is then projected to the PSD cone: a
-// Cholesky attempt first (a positive definite matrix is returned unchanged,
-// as project_to_psd does), else cyclic Jacobi and V max(L, 0) V^T.
+// sum_i grad_Xi f . d2X_i/dtheta2.  It is then projected to the PSD cone by
+// a warp-parallel Jacobi eigensolver (a matrix with no negative eigenvalue is
+// returned unchanged, as project_to_psd does), V max(L, 0) V^T otherwise.
+#include <algorithm>
+
 #include "common.cuh"
+#include "local_terms.cuh"
 #include "rotation.cuh"
 #include "sort.cuh"
 
@@ -48,210 +51,6 @@ __global__ void k_body_frames(const double* __restrict__ x, int nb, double* __re
     out[90] = x[6 * b];
     out[91] = x[6 * b + 1];
     out[92] = x[6 * b + 2];
-}
-
-// ---------------------------------------------------------------------------
-
-constexpr int kBarrierTPB = 32;
-
-struct Vtx {
-    double X[3];     // world position
-    double D[3][3];  // dX/dtheta  [coord][k]
-};
-
-__device__ __forceinline__ void cross(const double* a, const double* b, double* r)
-{
-    r[0] = a[1] * b[2] - a[2] * b[1];
-    r[1] = a[2] * b[0] - a[0] * b[2];
-    r[2] = a[0] * b[1] - a[1] * b[0];
-}
-__device__ __forceinline__ double dot(const double* a, const double* b)
-{
-    return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
-}
-
-// shared-memory 12x12 accumulator, entry-major / thread-minor
-struct SMat {
-    double* base;
-    __device__ __forceinline__ double& at(int r, int c) const
-    {
-        return base[(r * 12 + c) * kBarrierTPB];
-    }
-};
-
-// H += coef * (a b^T + b a^T) on the upper triangle (a, b in body space)
-__device__ __forceinline__ void add_sym_outer(SMat H, double coef, const double* a, const double* b)
-{
-    for (int r = 0; r < 12; r++) {
-        double ar = coef * a[r], br = coef * b[r];
-        for (int c = r; c < 12; c++) H.at(r, c) += ar * b[c] + br * a[c];
-    }
-}
-__device__ __forceinline__ void add_outer(SMat H, double coef, const double* a)
-{
-    for (int r = 0; r < 12; r++) {
-        double ar = coef * a[r];
-        for (int c = r; c < 12; c++) H.at(r, c) += ar * a[c];
-    }
-}
-
-// body-space image of a per-vertex vector field: out[6 lb + 0..2] += g_i,
-// out[6 lb + 3 + k] += D_i[:, k] . g_i
-__device__ __forceinline__ void to_body(const Vtx* V, const int* lbody, int nvc,
-                                        const double (*g)[3], double* out)
-{
-    for (int k = 0; k < 12; k++) out[k] = 0;
-    for (int i = 0; i < nvc; i++) {
-        int o = 6 * lbody[i];
-        for (int j = 0; j < 3; j++) out[o + j] += g[i][j];
-        for (int k = 0; k < 3; k++)
-            out[o + 3 + k] += V[i].D[0][k] * g[i][0] + V[i].D[1][k] * g[i][1] + V[i].D[2][k] * g[i][2];
-    }
-}
-
-// Gram term H += coef * JM^T JM where JM (3 x 12) = sum_i M_i J_i and
-// M_i = m_i * I + (skew parts): here M_i given as full 3x3 per vertex.
-__device__ __forceinline__ void add_gram(SMat H, double coef, const Vtx* V, const int* lbody,
-                                         int nvc, const double (*M)[9])
-{
-    double JM[3][12];
-    for (int r = 0; r < 3; r++)
-        for (int c = 0; c < 12; c++) JM[r][c] = 0;
-    for (int i = 0; i < nvc; i++) {
-        int o = 6 * lbody[i];
-        for (int r = 0; r < 3; r++) {
-            for (int j = 0; j < 3; j++) JM[r][o + j] += M[i][3 * r + j];
-            for (int k = 0; k < 3; k++)
-                JM[r][o + 3 + k] += M[i][3 * r] * V[i].D[0][k] + M[i][3 * r + 1] * V[i].D[1][k]
-                    + M[i][3 * r + 2] * V[i].D[2][k];
-        }
-    }
-    for (int r = 0; r < 12; r++) {
-        double a0 = coef * JM[0][r], a1 = coef * JM[1][r], a2 = coef * JM[2][r];
-        for (int c = r; c < 12; c++) H.at(r, c) += a0 * JM[0][c] + a1 * JM[1][c] + a2 * JM[2][c];
-    }
-}
-
-// skew pair block: H(i-part, j-part) += J_i^T [s]x J_j, and its transpose
-__device__ __forceinline__ void add_skew_pair(SMat H, const Vtx& Vi, int oi, const Vtx& Vj,
-                                              int oj, const double* s)
-{
-    // K = [s]x
-    const double K[3][3] = { { 0, -s[2], s[1] }, { s[2], 0, -s[0] }, { -s[1], s[0], 0 } };
-    // blocks: [K, K Dj ; Di^T K, Di^T K Dj]
-    double KD[3][3], DK[3][3], DKD[3][3];
-    for (int r = 0; r < 3; r++)
-        for (int c = 0; c < 3; c++) {
-            KD[r][c] = K[r][0] * Vj.D[0][c] + K[r][1] * Vj.D[1][c] + K[r][2] * Vj.D[2][c];
-            DK[r][c] = Vi.D[0][r] * K[0][c] + Vi.D[1][r] * K[1][c] + Vi.D[2][r] * K[2][c];
-        }
-    for (int r = 0; r < 3; r++)
-        for (int c = 0; c < 3; c++)
-            DKD[r][c] = Vi.D[0][r] * KD[0][c] + Vi.D[1][r] * KD[1][c] + Vi.D[2][r] * KD[2][c];
-    // B (6x6) = [[K, KD], [DK, DKD]] goes to rows oi.., cols oj..; its
-    // transpose to rows oj.., cols oi..; accumulate into the upper triangle.
-    for (int r = 0; r < 6; r++)
-        for (int c = 0; c < 6; c++) {
-            double v = r < 3 ? (c < 3 ? K[r][c] : KD[r][c - 3])
-                             : (c < 3 ? DK[r - 3][c] : DKD[r - 3][c - 3]);
-            int R = oi + r, C = oj + c;
-            // entry (R, C) of B and entry (C, R) of B^T are both v
-            if (R <= C) H.at(R, C) += v;
-            if (C <= R) H.at(C, R) += v;
-        }
-}
-
-// curvature term: H(rot lb, rot lb) += sum_j g_j (d2R_kl v)_j
-__device__ __forceinline__ void add_curvature(SMat H, const double* frame, int lb,
-                                              const double* v, const double* g)
-{
-    const double* d2 = frame + 36;
-    int o = 6 * lb + 3;
-    for (int k = 0; k < 3; k++)
-        for (int l = k; l < 3; l++) {
-            const double* M = d2 + 9 * sym_index(k, l);
-            double acc = 0;
-            for (int j = 0; j < 3; j++)
-                acc += g[j] * (M[3 * j] * v[0] + M[3 * j + 1] * v[1] + M[3 * j + 2] * v[2]);
-            H.at(o + k, o + l) += acc;
-        }
-}
-
-// ---------------------------------------------------------------------------
-// PSD projection of the (upper-triangle filled) 12x12 in shared memory.
-// Returns with the full symmetric projected matrix in H.
-
-__device__ bool cholesky_pd(SMat H, double* L)
-{
-    // L in registers-by-unrolling is too large; factor into scratch L (smem)
-    // L holds the lower factor in the same entry-major layout.
-    SMat Lm { L };
-    for (int j = 0; j < 12; j++) {
-        double d = H.at(j, j);
-        for (int k = 0; k < j; k++) d -= Lm.at(j, k) * Lm.at(j, k);
-        if (!(d > 0.0)) return false;
-        double ljj = sqrt(d);
-        Lm.at(j, j) = ljj;
-        double inv = 1.0 / ljj;
-        for (int i = j + 1; i < 12; i++) {
-            double s = H.at(j, i);  // upper triangle holds (j, i) = (i, j)
-            for (int k = 0; k < j; k++) s -= Lm.at(i, k) * Lm.at(j, k);
-            Lm.at(i, j) = s * inv;
-        }
-    }
-    return true;
-}
-
-__device__ void jacobi_project(SMat A, SMat Vm)
-{
-    // full symmetric A from the upper triangle
-    for (int r = 0; r < 12; r++)
-        for (int c = 0; c < r; c++) A.at(r, c) = A.at(c, r);
-    for (int r = 0; r < 12; r++)
-        for (int c = 0; c < 12; c++) Vm.at(r, c) = r == c ? 1.0 : 0.0;
-    for (int sweep = 0; sweep < 30; sweep++) {
-        double off = 0, diag = 0;
-        for (int i = 0; i < 12; i++) {
-            diag += A.at(i, i) * A.at(i, i);
-            for (int j = i + 1; j < 12; j++) off += A.at(i, j) * A.at(i, j);
-        }
-        if (off <= 1e-32 * diag || off == 0.0) break;
-        for (int p = 0; p < 12; p++)
-            for (int q = p + 1; q < 12; q++) {
-                double apq = A.at(p, q);
-                if (apq == 0.0) continue;
-                double app = A.at(p, p), aqq = A.at(q, q);
-                double theta = (aqq - app) / (2 * apq);
-                double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1));
-                double c = 1.0 / sqrt(t * t + 1);
-                double s = t * c;
-                for (int k = 0; k < 12; k++) {
-                    double akp = A.at(k, p), akq = A.at(k, q);
-                    A.at(k, p) = c * akp - s * akq;
-                    A.at(k, q) = s * akp + c * akq;
-                }
-                for (int k = 0; k < 12; k++) {
-                    double apk = A.at(p, k), aqk = A.at(q, k);
-                    A.at(p, k) = c * apk - s * aqk;
-                    A.at(q, k) = s * apk + c * aqk;
-                }
-                for (int k = 0; k < 12; k++) {
-                    double vkp = Vm.at(k, p), vkq = Vm.at(k, q);
-                    Vm.at(k, p) = c * vkp - s * vkq;
-                    Vm.at(k, q) = s * vkp + c * vkq;
-                }
-            }
-    }
-    double w[12];
-    for (int i = 0; i < 12; i++) w[i] = A.at(i, i);
-    // rebuild: A = V max(w, 0) V^T
-    for (int r = 0; r < 12; r++)
-        for (int c = r; c < 12; c++) {
-            double acc = 0;
-            for (int k = 0; k < 12; k++)
-                if (w[k] > 0) acc += Vm.at(r, k) * w[k] * Vm.at(c, k);
-            A.at(r, c) = acc;
-        }
 }
 
 // ---------------------------------------------------------------------------
@@ -279,16 +78,11 @@ __device__ __forceinline__ int local_body_of(int type, int i)
     return i == 0 ? 0 : 1;
 }
 
-__global__ void __launch_bounds__(kBarrierTPB)
-k_barrier_local(BarrierArgs a)
+// Energy, gradient and (upper triangle of the) unprojected body Hessian of
+// constraint ci into H; returns true when H holds a Hessian to project and
+// write, false when every output of the constraint is already written.
+static __device__ __noinline__ bool barrier_build(const BarrierArgs& a, int64_t ci, SMat H)
 {
-    extern __shared__ double smem[];
-    const int tid = threadIdx.x;
-    const int64_t ci = (int64_t)blockIdx.x * kBarrierTPB + tid;
-    if (ci >= a.n) return;
-    SMat H { smem + tid };
-    SMat V2 { smem + 144 * kBarrierTPB + tid };
-
     const int type = a.ctype[ci];
     const int nvc = type == 0 ? 2 : (type == 1 ? 3 : 4);
     const double weight = a.cweight[ci];
@@ -386,9 +180,9 @@ k_barrier_local(BarrierArgs a)
             for (int k = 0; k < 144; k++) a.blocks[ci * 144 + k] = 0;
         if (a.hess && want_h)
             for (int k = 0; k < 144; k++) a.hess[ci * 144 + k] = 0;
-        return;
+        return false;
     }
-    if (!want_g) return;
+    if (!want_g) return false;
 
     // ---- basic scalars and their vertex-space gradients
     // g1: gradient of the first scalar (u, N or d), g2: of the second (D, |e|^2)
@@ -439,7 +233,7 @@ k_barrier_local(BarrierArgs a)
     to_body(V, lbody, nvc, gv, G);
     if (a.grad)
         for (int k = 0; k < 12; k++) a.grad[ci * 12 + k] = G[k];
-    if (!want_h) return;
+    if (!want_h) return false;
 
     // ---- Hessian
     for (int r = 0; r < 12; r++)
@@ -542,23 +336,48 @@ k_barrier_local(BarrierArgs a)
     }
     // curvature of the rigid maps
     for (int i = 0; i < nvc; i++) add_curvature(H, fr[lbody[i]], lbody[i], vrest[i], gv[i]);
-
-    if (a.flags & RIGC_PROJECT_PSD) {
-        if (!cholesky_pd(H, V2.base)) jacobi_project(H, V2);
-    }
-    // write outputs (symmetric)
-    for (int r = 0; r < 12; r++)
-        for (int c = 0; c < 12; c++) {
-            double v = r <= c ? H.at(r, c) : H.at(c, r);
-            if (a.hess) a.hess[ci * 144 + 12 * r + c] = v;
-            if (a.blocks) {
-                int blk = (r / 6) * 2 + (c / 6);
-                a.blocks[ci * 144 + blk * 36 + (r % 6) * 6 + (c % 6)] = v;
-            }
-        }
+    return true;
 }
 
-size_t barrier_smem_bytes() { return (size_t)2 * 144 * kBarrierTPB * sizeof(double); }
+
+// One warp per block.  Lanes 0 .. per_warp-1 each build one constraint's
+// terms (a thread per constraint); then the whole warp projects the built
+// Hessians one after another.  per_warp is chosen by the host so that small
+// constraint sets still spread over the SMs.
+__global__ void __launch_bounds__(kBarrierTPB)
+k_barrier_local(BarrierArgs a, int per_warp)
+{
+    extern __shared__ double smem[];
+    const int lane = threadIdx.x;
+    const int64_t ci = (int64_t)blockIdx.x * per_warp + lane;
+    const bool mine = lane < per_warp && ci < a.n;
+    SMat H { smem + lane };
+    bool built = mine && barrier_build(a, ci, H);
+    if (!(a.flags & RIGC_HESS)) return;  // uniform over the block
+    if (a.flags & RIGC_PROJECT_PSD) {
+        double* work = smem + 144 * kBarrierTPB;
+        unsigned todo = __ballot_sync(0xffffffffu, built);
+        while (todo) {
+            int t = __ffs(todo) - 1;
+            todo &= todo - 1;
+            warp_psd_project(SMat { smem + t }, work, lane);
+        }
+    }
+    if (built) write_local_hessian(H, ci, a.hess, a.blocks);
+}
+
+size_t local_terms_smem_bytes()
+{
+    return (size_t)(144 * kBarrierTPB + kWorkDoubles) * sizeof(double);
+}
+
+// constraints per warp: a thread per constraint once there are enough of
+// them to fill the GPU, fewer (down to one) for small sets
+int local_terms_per_warp(int64_t n)
+{
+    int64_t w = (n + kNumSMs * 8 - 1) / (kNumSMs * 8);
+    return (int)std::max<int64_t>(1, std::min<int64_t>(kBarrierTPB, w));
+}
 
 int launch_body_frames(Ctx& c, const double* x)
 {
@@ -577,7 +396,7 @@ int launch_barrier_local(Ctx& c, const double* x, double dhat, double dmin, int 
     static bool attr = false;
     if (!attr) {
         RIGC_CUDA(cudaFuncSetAttribute(k_barrier_local, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)barrier_smem_bytes()));
+                                       (int)local_terms_smem_bytes()));
         attr = true;
     }
     BarrierArgs a;
@@ -596,9 +415,9 @@ int launch_barrier_local(Ctx& c, const double* x, double dhat, double dmin, int 
     a.grad = grad;
     a.blocks = blocks;
     a.hess = hess;
+    const int pw = local_terms_per_warp(c.cons.num);
     RIGC_COUNT_LAUNCH();
-    k_barrier_local<<<grid_for(c.cons.num, kBarrierTPB), kBarrierTPB, barrier_smem_bytes(),
-                      c.stream>>>(a);
+    k_barrier_local<<<grid_for(c.cons.num, pw), kBarrierTPB, local_terms_smem_bytes(), c.stream>>>(a, pw);
     RIGC_CUDA(cudaGetLastError());
     return RIGC_OK;
 }
@@ -617,7 +436,7 @@ int launch_barrier_local_raw(const double* rest, int nb, const double* x, int64_
     RIGC_CUDA(cudaGetLastError());
     if (n == 0) return RIGC_OK;
     RIGC_CUDA(cudaFuncSetAttribute(k_barrier_local, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)barrier_smem_bytes()));
+                                   (int)local_terms_smem_bytes()));
     BarrierArgs a;
     a.rest = rest;
     a.frames = frames;
@@ -634,8 +453,9 @@ int launch_barrier_local_raw(const double* rest, int nb, const double* x, int64_
     a.grad = grad;
     a.blocks = nullptr;
     a.hess = hess;
+    const int pw = local_terms_per_warp(n);
     RIGC_COUNT_LAUNCH();
-    k_barrier_local<<<grid_for(n, kBarrierTPB), kBarrierTPB, barrier_smem_bytes(), stream>>>(a);
+    k_barrier_local<<<grid_for(n, pw), kBarrierTPB, local_terms_smem_bytes(), stream>>>(a, pw);
     RIGC_CUDA(cudaGetLastError());
     return RIGC_OK;
 }
@@ -727,16 +547,16 @@ __global__ void k_grad_sums(const uint32_t* __restrict__ keys, const uint32_t* _
     grad[(size_t)keys[s0] * 6 + e] = acc;
 }
 
-int assemble_barrier(Ctx& c, bool with_hess)
+int assemble_terms(Ctx& c, const int* bodies, int64_t n, const double* cgrad,
+                   const double* cblocks, DevBuf& grad, DevBuf& row_ptr, DevBuf& col,
+                   DevBuf& val, int32_t* nseg_dev_pair, bool with_hess)
 {
-    const int64_t n = c.cons.num;
     const int nb = c.s.nb;
     cudaStream_t st = c.stream;
-    RIGC_TRY(c.grad.reserve((size_t)6 * nb * sizeof(double)));
-    RIGC_TRY(c.row_ptr.reserve((size_t)(nb + 1) * sizeof(int32_t)));
-    RIGC_CUDA(cudaMemsetAsync(c.grad.ptr, 0, (size_t)6 * nb * sizeof(double), st));
-    RIGC_CUDA(cudaMemsetAsync(c.row_ptr.ptr, 0, (size_t)(nb + 1) * sizeof(int32_t), st));
-    c.nnzb = 0;
+    RIGC_TRY(grad.reserve((size_t)6 * nb * sizeof(double)));
+    RIGC_TRY(row_ptr.reserve((size_t)(nb + 1) * sizeof(int32_t)));
+    RIGC_CUDA(cudaMemsetAsync(grad.ptr, 0, (size_t)6 * nb * sizeof(double), st));
+    RIGC_CUDA(cudaMemsetAsync(row_ptr.ptr, 0, (size_t)(nb + 1) * sizeof(int32_t), st));
     if (n == 0) return RIGC_OK;
     // scratch usage: 0 keys_in, 1 vals_in, 2 keys_out, 3 vals_out, 4/5 sort tmp,
     // 6 hist/scan tmp, 7 head/segid/seg_start
@@ -750,7 +570,7 @@ int assemble_barrier(Ctx& c, bool with_hess)
         RIGC_TRY(S[3].reserve(m * 4));
         RIGC_TRY(S[7].reserve(m * 12 + 16));
         RIGC_COUNT_LAUNCH();
-        k_grad_keys<<<grid_for(m, 256), 256, 0, st>>>(c.cons.bodies.as<int>(), n, S[0].as<uint32_t>(),
+        k_grad_keys<<<grid_for(m, 256), 256, 0, st>>>(bodies, n, S[0].as<uint32_t>(),
                                                      S[1].as<uint32_t>());
         RIGC_TRY(radix_sort_pairs<uint32_t>(S[0].as<uint32_t>(), S[1].as<uint32_t>(),
                                             S[2].as<uint32_t>(), S[3].as<uint32_t>(), m,
@@ -760,15 +580,15 @@ int assemble_barrier(Ctx& c, bool with_hess)
         int32_t* segst = segid + m;
         RIGC_COUNT_LAUNCH();
         k_heads<uint32_t><<<grid_for(m, 256), 256, 0, st>>>(S[2].as<uint32_t>(), m, head);
-        int32_t* nseg_dev = c.d_scalars.as<int32_t>();
+        int32_t* nseg_dev = nseg_dev_pair;
         RIGC_TRY(exclusive_scan_i32(head, segid, m, nseg_dev, S[6], st));
         RIGC_COUNT_LAUNCH();
         k_seg_starts<<<grid_for(m, 256), 256, 0, st>>>(head, segid, m, segst);
         // at most m segments; the kernel reads the true count on the device
         RIGC_COUNT_LAUNCH();
         k_grad_sums<<<grid_for(m * 6, 256), 256, 0, st>>>(
-            S[2].as<uint32_t>(), S[3].as<uint32_t>(), segst, nseg_dev, m, c.c_grad.as<double>(),
-            c.grad.as<double>());
+            S[2].as<uint32_t>(), S[3].as<uint32_t>(), segst, nseg_dev, m, cgrad,
+            grad.as<double>());
     }
     if (!with_hess) return RIGC_OK;
     // ---- Hessian blocks
@@ -780,7 +600,7 @@ int assemble_barrier(Ctx& c, bool with_hess)
         RIGC_TRY(S[3].reserve(m * 4));
         RIGC_TRY(S[7].reserve(m * 12 + 16));
         RIGC_COUNT_LAUNCH();
-        k_block_keys<<<grid_for(m, 256), 256, 0, st>>>(c.cons.bodies.as<int>(), n, nb,
+        k_block_keys<<<grid_for(m, 256), 256, 0, st>>>(bodies, n, nb,
                                                       S[0].as<uint64_t>(), S[1].as<uint32_t>());
         RIGC_TRY(radix_sort_pairs<uint64_t>(S[0].as<uint64_t>(), S[1].as<uint32_t>(),
                                             S[2].as<uint64_t>(), S[3].as<uint32_t>(), m,
@@ -790,26 +610,34 @@ int assemble_barrier(Ctx& c, bool with_hess)
         int32_t* segst = segid + m;
         RIGC_COUNT_LAUNCH();
         k_heads<uint64_t><<<grid_for(m, 256), 256, 0, st>>>(S[2].as<uint64_t>(), m, head);
-        int32_t* nseg_dev = c.d_scalars.as<int32_t>() + 1;  // read back by the caller
+        int32_t* nseg_dev = nseg_dev_pair + 1;  // read back by the caller
         RIGC_TRY(exclusive_scan_i32(head, segid, m, nseg_dev, S[6], st));
         RIGC_COUNT_LAUNCH();
         k_seg_starts<<<grid_for(m, 256), 256, 0, st>>>(head, segid, m, segst);
         // capacity for the upper bound m blocks: no host round trip here
-        RIGC_TRY(c.col.reserve((size_t)m * sizeof(int32_t)));
-        RIGC_TRY(c.val.reserve((size_t)m * 36 * sizeof(double)));
+        RIGC_TRY(col.reserve((size_t)m * sizeof(int32_t)));
+        RIGC_TRY(val.reserve((size_t)m * 36 * sizeof(double)));
         RIGC_COUNT_LAUNCH();
         k_block_sums<<<grid_for(m * 36, 256), 256, 0, st>>>(
-            S[2].as<uint64_t>(), S[3].as<uint32_t>(), segst, nseg_dev, m, c.c_blocks.as<double>(), nb,
-            c.col.as<int32_t>(), c.val.as<double>(), c.row_ptr.as<int32_t>() + 1);
+            S[2].as<uint64_t>(), S[3].as<uint32_t>(), segst, nseg_dev, m, cblocks, nb,
+            col.as<int32_t>(), val.as<double>(), row_ptr.as<int32_t>() + 1);
         // row counts -> row_ptr (exclusive scan of counts shifted by one)
-        int32_t* rp = c.row_ptr.as<int32_t>();
+        int32_t* rp = row_ptr.as<int32_t>();
         RIGC_TRY(S[4].reserve((size_t)(nb + 1) * sizeof(int32_t)));
         RIGC_CUDA(cudaMemcpyAsync(S[4].ptr, rp + 1, (size_t)nb * sizeof(int32_t),
                                   cudaMemcpyDeviceToDevice, st));
         RIGC_TRY(exclusive_scan_i32(S[4].as<int32_t>(), rp, nb, rp + nb, S[6], st));
-        c.nnzb = -1;  // on the device (d_scalars int 1) until the caller syncs
     }
     return RIGC_OK;
+}
+
+int assemble_barrier(Ctx& c, bool with_hess)
+{
+    // on the device (d_scalars int 1) until the caller syncs
+    c.nnzb = (with_hess && c.cons.num > 0) ? -1 : 0;
+    return assemble_terms(c, c.cons.bodies.as<int>(), c.cons.num, c.c_grad.as<double>(),
+                          c.c_blocks.as<double>(), c.grad, c.row_ptr, c.col, c.val,
+                          c.d_scalars.as<int32_t>(), with_hess);
 }
 
 } // namespace rigc

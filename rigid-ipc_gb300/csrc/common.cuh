@@ -113,6 +113,18 @@ struct Constraints {
     DevBuf type, verts, prims, bodies, weight, eps;
 };
 
+// lagged friction constraints (a copy of the collision constraints at the
+// start of the step with their normal forces, closest points and bases) and
+// the friction term's outputs
+struct Friction {
+    int64_t num = 0;
+    double mu = 0;
+    DevBuf type, verts, bodies, coef, v0c, V0;
+    DevBuf c_energy, c_grad, c_blocks;
+    DevBuf grad, row_ptr, col, val;
+    int64_t nnzb = 0;
+};
+
 struct Ctx {
     Scene s;
     cudaStream_t stream = 0;
@@ -138,6 +150,7 @@ struct Ctx {
     // CCD: body frames over the top dyadic time intervals
     DevBuf rot_table;
     DevBuf frame_keys, frame_vals;  // CCD frame cache (hash table)
+    Friction fric;
 };
 
 Ctx* ctx_of(rigc_ctx* c);

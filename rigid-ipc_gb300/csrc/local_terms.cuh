@@ -1,0 +1,284 @@
+// Device helpers shared by the per-constraint local terms (barrier and
+// friction): vertex positions with their rotation derivatives, body-space
+// images of vertex-space vectors, shared-memory 12x12 accumulators, the rigid
+// curvature term of apply_chain_rule
+// (src/problems/distance_barrier_rb_problem.cpp:1182-1248) and the
+// warp-parallel PSD projection.
+#pragma once
+
+#include "common.cuh"
+#include "rotation.cuh"
+
+namespace rigc {
+
+// ---------------------------------------------------------------------------
+
+constexpr int kBarrierTPB = 32;
+
+struct Vtx {
+    double X[3];     // world position
+    double D[3][3];  // dX/dtheta  [coord][k]
+};
+
+__device__ __forceinline__ void cross(const double* a, const double* b, double* r)
+{
+    r[0] = a[1] * b[2] - a[2] * b[1];
+    r[1] = a[2] * b[0] - a[0] * b[2];
+    r[2] = a[0] * b[1] - a[1] * b[0];
+}
+__device__ __forceinline__ double dot(const double* a, const double* b)
+{
+    return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+}
+
+// shared-memory 12x12 accumulator, entry-major / thread-minor
+struct SMat {
+    double* base;
+    __device__ __forceinline__ double& at(int r, int c) const
+    {
+        return base[(r * 12 + c) * kBarrierTPB];
+    }
+};
+
+// H += coef * (a b^T + b a^T) on the upper triangle (a, b in body space)
+__device__ __forceinline__ void add_sym_outer(SMat H, double coef, const double* a, const double* b)
+{
+    for (int r = 0; r < 12; r++) {
+        double ar = coef * a[r], br = coef * b[r];
+        for (int c = r; c < 12; c++) H.at(r, c) += ar * b[c] + br * a[c];
+    }
+}
+__device__ __forceinline__ void add_outer(SMat H, double coef, const double* a)
+{
+    for (int r = 0; r < 12; r++) {
+        double ar = coef * a[r];
+        for (int c = r; c < 12; c++) H.at(r, c) += ar * a[c];
+    }
+}
+
+// body-space image of a per-vertex vector field: out[6 lb + 0..2] += g_i,
+// out[6 lb + 3 + k] += D_i[:, k] . g_i
+__device__ __forceinline__ void to_body(const Vtx* V, const int* lbody, int nvc,
+                                        const double (*g)[3], double* out)
+{
+    for (int k = 0; k < 12; k++) out[k] = 0;
+    for (int i = 0; i < nvc; i++) {
+        int o = 6 * lbody[i];
+        for (int j = 0; j < 3; j++) out[o + j] += g[i][j];
+        for (int k = 0; k < 3; k++)
+            out[o + 3 + k] += V[i].D[0][k] * g[i][0] + V[i].D[1][k] * g[i][1] + V[i].D[2][k] * g[i][2];
+    }
+}
+
+// Gram term H += coef * JM^T JM where JM (3 x 12) = sum_i M_i J_i and
+// M_i = m_i * I + (skew parts): here M_i given as full 3x3 per vertex.
+__device__ __forceinline__ void add_gram(SMat H, double coef, const Vtx* V, const int* lbody,
+                                         int nvc, const double (*M)[9])
+{
+    double JM[3][12];
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 12; c++) JM[r][c] = 0;
+    for (int i = 0; i < nvc; i++) {
+        int o = 6 * lbody[i];
+        for (int r = 0; r < 3; r++) {
+            for (int j = 0; j < 3; j++) JM[r][o + j] += M[i][3 * r + j];
+            for (int k = 0; k < 3; k++)
+                JM[r][o + 3 + k] += M[i][3 * r] * V[i].D[0][k] + M[i][3 * r + 1] * V[i].D[1][k]
+                    + M[i][3 * r + 2] * V[i].D[2][k];
+        }
+    }
+    for (int r = 0; r < 12; r++) {
+        double a0 = coef * JM[0][r], a1 = coef * JM[1][r], a2 = coef * JM[2][r];
+        for (int c = r; c < 12; c++) H.at(r, c) += a0 * JM[0][c] + a1 * JM[1][c] + a2 * JM[2][c];
+    }
+}
+
+// skew pair block: H(i-part, j-part) += J_i^T [s]x J_j, and its transpose
+__device__ __forceinline__ void add_skew_pair(SMat H, const Vtx& Vi, int oi, const Vtx& Vj,
+                                              int oj, const double* s)
+{
+    // K = [s]x
+    const double K[3][3] = { { 0, -s[2], s[1] }, { s[2], 0, -s[0] }, { -s[1], s[0], 0 } };
+    // blocks: [K, K Dj ; Di^T K, Di^T K Dj]
+    double KD[3][3], DK[3][3], DKD[3][3];
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) {
+            KD[r][c] = K[r][0] * Vj.D[0][c] + K[r][1] * Vj.D[1][c] + K[r][2] * Vj.D[2][c];
+            DK[r][c] = Vi.D[0][r] * K[0][c] + Vi.D[1][r] * K[1][c] + Vi.D[2][r] * K[2][c];
+        }
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++)
+            DKD[r][c] = Vi.D[0][r] * KD[0][c] + Vi.D[1][r] * KD[1][c] + Vi.D[2][r] * KD[2][c];
+    // B (6x6) = [[K, KD], [DK, DKD]] goes to rows oi.., cols oj..; its
+    // transpose to rows oj.., cols oi..; accumulate into the upper triangle.
+    for (int r = 0; r < 6; r++)
+        for (int c = 0; c < 6; c++) {
+            double v = r < 3 ? (c < 3 ? K[r][c] : KD[r][c - 3])
+                             : (c < 3 ? DK[r - 3][c] : DKD[r - 3][c - 3]);
+            int R = oi + r, C = oj + c;
+            // entry (R, C) of B and entry (C, R) of B^T are both v
+            if (R <= C) H.at(R, C) += v;
+            if (C <= R) H.at(C, R) += v;
+        }
+}
+
+// curvature term: H(rot lb, rot lb) += sum_j g_j (d2R_kl v)_j
+__device__ __forceinline__ void add_curvature(SMat H, const double* frame, int lb,
+                                              const double* v, const double* g)
+{
+    const double* d2 = frame + 36;
+    int o = 6 * lb + 3;
+    for (int k = 0; k < 3; k++)
+        for (int l = k; l < 3; l++) {
+            const double* M = d2 + 9 * sym_index(k, l);
+            double acc = 0;
+            for (int j = 0; j < 3; j++)
+                acc += g[j] * (M[3 * j] * v[0] + M[3 * j + 1] * v[1] + M[3 * j + 2] * v[2]);
+            H.at(o + k, o + l) += acc;
+        }
+}
+
+// ---------------------------------------------------------------------------
+// PSD projection of one 12x12 (upper triangle filled, in the entry-major
+// layout of its owner thread) by the whole warp: parallel cyclic Jacobi in
+// round-robin order (each round rotates six disjoint (p, q) planes at once,
+// eleven rounds visit all 66 pairs), then V max(L, 0) V^T.  As
+// project_to_psd does, a matrix whose eigenvalues are all >= 0 is left as it
+// is.  Rotation (c, s) per plane follows the textbook symmetric Schur step:
+// theta = (a_qq - a_pp) / (2 a_pq), t = sign(theta) / (|theta| +
+// sqrt(theta^2 + 1)), c = 1 / sqrt(t^2 + 1), s = t c.
+
+constexpr int kLd = 13;  // padded row stride of the warp's work matrices
+constexpr int kWorkDoubles = 2 * 12 * kLd + 16;
+
+// round-robin schedule over 12 indices: round r pairs (11, pos0) and
+// (pos_k, pos_{11-k}), pos_k = (k + r) mod 11, stored with p < q
+static __constant__ unsigned char kRoundPairs[11][6][2] = {
+    { { 0, 11 }, { 1, 10 }, { 2, 9 }, { 3, 8 }, { 4, 7 }, { 5, 6 } },
+    { { 1, 11 }, { 0, 2 }, { 3, 10 }, { 4, 9 }, { 5, 8 }, { 6, 7 } },
+    { { 2, 11 }, { 1, 3 }, { 0, 4 }, { 5, 10 }, { 6, 9 }, { 7, 8 } },
+    { { 3, 11 }, { 2, 4 }, { 1, 5 }, { 0, 6 }, { 7, 10 }, { 8, 9 } },
+    { { 4, 11 }, { 3, 5 }, { 2, 6 }, { 1, 7 }, { 0, 8 }, { 9, 10 } },
+    { { 5, 11 }, { 4, 6 }, { 3, 7 }, { 2, 8 }, { 1, 9 }, { 0, 10 } },
+    { { 6, 11 }, { 5, 7 }, { 4, 8 }, { 3, 9 }, { 2, 10 }, { 0, 1 } },
+    { { 7, 11 }, { 6, 8 }, { 5, 9 }, { 4, 10 }, { 0, 3 }, { 1, 2 } },
+    { { 8, 11 }, { 7, 9 }, { 6, 10 }, { 0, 5 }, { 1, 4 }, { 2, 3 } },
+    { { 9, 11 }, { 8, 10 }, { 0, 7 }, { 1, 6 }, { 2, 5 }, { 3, 4 } },
+    { { 10, 11 }, { 0, 9 }, { 1, 8 }, { 2, 7 }, { 3, 6 }, { 4, 5 } },
+};
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+static __device__ void warp_psd_project(SMat H, double* work, int lane)
+{
+    double* A = work;
+    double* V = work + 12 * kLd;
+    double* cs = work + 24 * kLd;   // 6 x (c, s)
+    for (int e = lane; e < 144; e += 32) {
+        int r = e / 12, c = e % 12;
+        A[r * kLd + c] = r <= c ? H.at(r, c) : H.at(c, r);
+        V[r * kLd + c] = r == c ? 1.0 : 0.0;
+    }
+    __syncwarp();
+    for (int sweep = 0; sweep < 30; sweep++) {
+        double off = 0, diag = 0;
+        for (int e = lane; e < 144; e += 32) {
+            int r = e / 12, c = e % 12;
+            double v = A[r * kLd + c];
+            if (r == c) diag += v * v;
+            else if (r < c) off += v * v;
+        }
+        off = warp_sum(off);
+        diag = warp_sum(diag);
+        if (off <= 1e-30 * diag || off == 0.0) break;
+        for (int round = 0; round < 11; round++) {
+            if (lane < 6) {
+                int p = kRoundPairs[round][lane][0], q = kRoundPairs[round][lane][1];
+                double apq = A[p * kLd + q];
+                double c = 1.0, sn = 0.0;
+                if (apq != 0.0) {
+                    double app = A[p * kLd + p], aqq = A[q * kLd + q];
+                    double theta = (aqq - app) / (2 * apq);
+                    double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1));
+                    c = 1.0 / sqrt(t * t + 1);
+                    sn = t * c;
+                }
+                cs[2 * lane] = c;
+                cs[2 * lane + 1] = sn;
+            }
+            __syncwarp();
+            // columns of A and V: 2 x 6 planes x 12 rows
+            for (int it = lane; it < 144; it += 32) {
+                double* M = it < 72 ? A : V;
+                int j = it < 72 ? it : it - 72;
+                int pr = j % 6, k = j / 6;
+                int p = kRoundPairs[round][pr][0], q = kRoundPairs[round][pr][1];
+                double c = cs[2 * pr], sn = cs[2 * pr + 1];
+                double mkp = M[k * kLd + p], mkq = M[k * kLd + q];
+                M[k * kLd + p] = c * mkp - sn * mkq;
+                M[k * kLd + q] = sn * mkp + c * mkq;
+            }
+            __syncwarp();
+            // rows of A: 6 planes x 12 columns
+            for (int it = lane; it < 72; it += 32) {
+                int pr = it % 6, k = it / 6;
+                int p = kRoundPairs[round][pr][0], q = kRoundPairs[round][pr][1];
+                double c = cs[2 * pr], sn = cs[2 * pr + 1];
+                double apk = A[p * kLd + k], aqk = A[q * kLd + k];
+                A[p * kLd + k] = c * apk - sn * aqk;
+                A[q * kLd + k] = sn * apk + c * aqk;
+            }
+            __syncwarp();
+        }
+    }
+    double wmin = INFINITY;
+#pragma unroll
+    for (int i = 0; i < 12; i++) wmin = fmin(wmin, A[i * kLd + i]);
+    if (wmin >= 0.0) return;  // already PSD: keep the matrix as it is
+    // rebuild the upper triangle: sum over positive eigenvalues
+    for (int e = lane; e < 144; e += 32) {
+        int r = e / 12, c = e % 12;
+        if (r > c) continue;
+        double acc = 0;
+        for (int k = 0; k < 12; k++) {
+            double w = A[k * kLd + k];
+            if (w > 0) acc += V[r * kLd + k] * w * V[c * kLd + k];
+        }
+        H.at(r, c) = acc;
+    }
+    __syncwarp();
+}
+
+// local Hessian (symmetric from the upper triangle) to the outputs
+__device__ __forceinline__ void write_local_hessian(SMat H, int64_t ci, double* hess, double* blocks)
+{
+    for (int r = 0; r < 12; r++)
+        for (int c = 0; c < 12; c++) {
+            double v = r <= c ? H.at(r, c) : H.at(c, r);
+            if (hess) hess[ci * 144 + 12 * r + c] = v;
+            if (blocks) {
+                int blk = (r / 6) * 2 + (c / 6);
+                blocks[ci * 144 + blk * 36 + (r % 6) * 6 + (c % 6)] = v;
+            }
+        }
+}
+
+// Generic deterministic assembly of per-constraint body-space terms: cgrad
+// (n x 12, two 6-blocks per constraint) into grad (nb x 6) and cblocks
+// (n x 4 x 36) into a block-sparse matrix (row_ptr, col, val).  nseg_dev
+// points at two device ints: the gradient segment count and the number of
+// Hessian blocks (read back by the caller after a sync).
+int assemble_terms(Ctx& c, const int* bodies, int64_t n, const double* cgrad,
+                   const double* cblocks, DevBuf& grad, DevBuf& row_ptr, DevBuf& col,
+                   DevBuf& val, int32_t* nseg_dev, bool with_hess);
+
+size_t local_terms_smem_bytes();
+int local_terms_per_warp(int64_t n);
+int launch_body_frames(Ctx& c, const double* x);
+
+} // namespace rigc

@@ -1,7 +1,7 @@
 // Stable LSD radix sort, scans and deterministic sums.
 //
 // Radix sort: 8-bit digits, tiles of 2048 items (256 threads x 8 rounds).
-// Per pass: (1) per-tile digit histograms in shared memory, (2) one
+// Per pass: (1) per-tile digit histograms in shared memory, (2) a parallel
 // exclusive scan over the digit-major [digit][tile] histogram, (3) a stable
 // scatter: each round of 256 items ranks equal digits inside a warp with
 // __match_any_sync, then across the 8 warps by a per-digit prefix, on top of
@@ -35,32 +35,6 @@ __global__ void k_digit_hist(const Key* __restrict__ keys, int64_t n, int shift,
     }
     __syncthreads();
     hist[(int64_t)threadIdx.x * ntiles + blockIdx.x] = cnt[threadIdx.x];
-}
-
-// single-block exclusive scan of m uint32 (m = 256 * ntiles)
-__global__ void k_scan_single(uint32_t* __restrict__ a, int64_t m)
-{
-    __shared__ uint32_t part[1024];
-    const int T = blockDim.x;
-    int64_t chunk = (m + T - 1) / T;
-    int64_t lo = threadIdx.x * chunk, hi = min(m, lo + chunk);
-    uint32_t s = 0;
-    for (int64_t i = lo; i < hi; i++) s += a[i];
-    part[threadIdx.x] = s;
-    __syncthreads();
-    // Hillis-Steele inclusive scan over the partials
-    for (int off = 1; off < T; off <<= 1) {
-        uint32_t v = threadIdx.x >= off ? part[threadIdx.x - off] : 0;
-        __syncthreads();
-        part[threadIdx.x] += v;
-        __syncthreads();
-    }
-    uint32_t run = threadIdx.x ? part[threadIdx.x - 1] : 0;
-    for (int64_t i = lo; i < hi; i++) {
-        uint32_t v = a[i];
-        a[i] = run;
-        run += v;
-    }
 }
 
 template <class Key>
@@ -110,6 +84,9 @@ k_scatter(const Key* __restrict__ kin, const uint32_t* __restrict__ vin,
     }
 }
 
+int64_t scan_tiles(int64_t n);
+int scan_in_place(int32_t* a, int64_t n, int32_t* sums, cudaStream_t stream);
+
 } // namespace
 
 template <class Key>
@@ -124,7 +101,10 @@ int radix_sort_pairs(const Key* keys_in, const uint32_t* vals_in, Key* keys_out,
     const int ntiles = (int)((n + kSortTile - 1) / kSortTile);
     RIGC_TRY(tmp_keys.reserve(n * sizeof(Key)));
     RIGC_TRY(tmp_vals.reserve(n * sizeof(uint32_t)));
-    RIGC_TRY(hist.reserve((size_t)256 * ntiles * sizeof(uint32_t)));
+    // digit-major histogram followed by the tile sums of its scan
+    const int64_t m = (int64_t)256 * ntiles;
+    RIGC_TRY(hist.reserve((size_t)(m + scan_tiles(m)) * sizeof(uint32_t)));
+    int32_t* hist_i = reinterpret_cast<int32_t*>(hist.as<uint32_t>());
     // Pass p writes keys_out when (passes - 1 - p) is even, the temporaries
     // otherwise, so the last pass lands in keys_out and no pass writes the
     // buffer it reads (keys_in must not alias keys_out).
@@ -138,8 +118,7 @@ int radix_sort_pairs(const Key* keys_in, const uint32_t* vals_in, Key* keys_out,
         RIGC_COUNT_LAUNCH();
         k_digit_hist<Key><<<ntiles, kSortThreads, 0, stream>>>(src_k, n, shift, ntiles,
                                                                hist.as<uint32_t>());
-        RIGC_COUNT_LAUNCH();
-        k_scan_single<<<1, 1024, 0, stream>>>(hist.as<uint32_t>(), (int64_t)256 * ntiles);
+        RIGC_TRY(scan_in_place(hist_i, m, hist_i + m, stream));
         RIGC_COUNT_LAUNCH();
         k_scatter<Key><<<ntiles, kSortThreads, 0, stream>>>(src_k, src_v, dk, dv, n, shift,
                                                             ntiles, hist.as<uint32_t>());
@@ -225,7 +204,7 @@ __global__ void k_scan_sums(int32_t* __restrict__ sums, int64_t m, int32_t* tota
     if (threadIdx.x == 0 && total_dev) *total_dev = carry;
 }
 
-__global__ void k_tile_scan(const int32_t* __restrict__ in, int32_t* __restrict__ out, int64_t n,
+__global__ void k_tile_scan(const int32_t* in, int32_t* out, int64_t n,
                             const int32_t* __restrict__ sums)
 {
     int64_t base = (int64_t)blockIdx.x * kScanTile + threadIdx.x * kScanItems;
@@ -243,6 +222,22 @@ __global__ void k_tile_scan(const int32_t* __restrict__ in, int32_t* __restrict_
         if (base + k < n) out[base + k] = ex;
         ex += v[k];
     }
+}
+
+int64_t scan_tiles(int64_t n) { return (n + kScanTile - 1) / kScanTile; }
+
+// exclusive scan of a[0..n) in place (each tile is read before it is written);
+// sums holds scan_tiles(n) entries
+int scan_in_place(int32_t* a, int64_t n, int32_t* sums, cudaStream_t stream)
+{
+    const int64_t tiles = scan_tiles(n);
+    RIGC_COUNT_LAUNCH();
+    k_tile_sums<<<(unsigned)tiles, kScanThreads, 0, stream>>>(a, n, sums);
+    RIGC_COUNT_LAUNCH();
+    k_scan_sums<<<1, kScanThreads, 0, stream>>>(sums, tiles, nullptr);
+    RIGC_COUNT_LAUNCH();
+    k_tile_scan<<<(unsigned)tiles, kScanThreads, 0, stream>>>(a, a, n, sums);
+    return RIGC_OK;
 }
 
 } // namespace

@@ -215,6 +215,65 @@ class Context:
                 "rigc_barrier_local_terms")
         return e[:n].cpu().numpy(), g[:n].cpu().numpy(), H[:n].cpu().numpy()
 
+    # ---- lagged friction (DistanceBarrierRBProblem::update_friction_constraints
+    # and compute_friction_term, distance_barrier_rb_problem.cpp:168-188,1469-1572)
+
+    def friction_setup(self, x_t0, dhat, barrier_stiffness, coefficient_friction):
+        """Friction constraints from the current constraint set at x_t0; returns their count."""
+        xd = self.device(x_t0)
+        n = C.c_int64()
+        L.check(self.lib.rigc_friction_setup(self.h, C.c_void_p(xd.data_ptr()), dhat,
+                                             barrier_stiffness, coefficient_friction,
+                                             C.byref(n)), "rigc_friction_setup")
+        self._fric_x0 = xd
+        return n.value
+
+    def friction_constraints(self):
+        """dict: type, verts, bodies, lambda, closest (n x 2), basis (n x 2 x 3), mu."""
+        v = L.FrictionView()
+        L.check(self.lib.rigc_get_friction(self.h, C.byref(v)), "rigc_get_friction")
+        n = v.num
+        coef = self.copy_out(v.coef, (n, 9), np.float64) if n else np.zeros((0, 9))
+        return {
+            "type": self.copy_out(v.type, (n,), np.int32) if n else np.zeros(0, np.int32),
+            "verts": self.copy_out(v.verts, (n, 4), np.int32) if n else np.zeros((0, 4), np.int32),
+            "bodies": self.copy_out(v.bodies, (n, 2), np.int32) if n else np.zeros((0, 2), np.int32),
+            "lambda": coef[:, 0], "closest": coef[:, 1:3], "basis": coef[:, 3:9].reshape(n, 2, 3),
+            "mu": v.mu,
+        }
+
+    def compute_friction_term(self, x, epsv_times_h, grad=True, hess=True, project=True):
+        """Energy, gradient (6 nb) and BSR Hessian (row_ptr, col, val[nnzb, 6, 6])."""
+        xd = self.device(x)
+        flags = (L.RIGC_GRAD if grad else 0) | (L.RIGC_HESS if hess else 0) | \
+                (L.RIGC_PROJECT_PSD if project else 0)
+        o = L.BarrierOut()
+        L.check(self.lib.rigc_friction_term(self.h, C.c_void_p(xd.data_ptr()), epsv_times_h, flags,
+                                            C.byref(o)), "rigc_friction_term")
+        nb = self.scene.num_bodies
+        g = self.copy_out(o.grad, (6 * nb,), np.float64) if grad or hess else None
+        H = None
+        if hess:
+            H = (self.copy_out(o.row_ptr, (nb + 1,), np.int32),
+                 self.copy_out(o.col, (o.nnzb,), np.int32) if o.nnzb else np.zeros(0, np.int32),
+                 self.copy_out(o.val, (o.nnzb, 6, 6), np.float64) if o.nnzb else
+                 np.zeros((0, 6, 6)))
+        return o.energy, g, H
+
+    def friction_local_terms(self, x, n, epsv_times_h, project=True):
+        torch = self.torch
+        xd = self.device(x)
+        e = torch.empty(max(n, 1), dtype=torch.float64, device="cuda")
+        g = torch.empty((max(n, 1), 12), dtype=torch.float64, device="cuda")
+        H = torch.empty((max(n, 1), 12, 12), dtype=torch.float64, device="cuda")
+        flags = L.RIGC_GRAD | L.RIGC_HESS | (L.RIGC_PROJECT_PSD if project else 0)
+        L.check(self.lib.rigc_friction_local_terms(self.h, C.c_void_p(xd.data_ptr()), epsv_times_h,
+                                                   flags, C.c_void_p(e.data_ptr()),
+                                                   C.c_void_p(g.data_ptr()),
+                                                   C.c_void_p(H.data_ptr())),
+                "rigc_friction_local_terms")
+        return e[:n].cpu().numpy(), g[:n].cpu().numpy(), H[:n].cpu().numpy()
+
     def body_state(self, x_t0=None):
         """Device arrays of the bodies' state at the start of the step."""
         sc = self.scene

@@ -32,6 +32,7 @@ EXPORTS = [
     "rigc_earliest_toi", "rigc_compute_earliest_toi", "rigc_construct_constraint_set",
     "rigc_set_constraints", "rigc_barrier_term", "rigc_barrier_local_terms",
     "rigc_narrow_phase_host", "rigc_barrier_local_terms_noalloc", "rigc_body_energy",
+    "rigc_friction_setup", "rigc_get_friction", "rigc_friction_term", "rigc_friction_local_terms",
 ]
 RIGC_ERR_TOO_LARGE = 7
 RIGC_NOALLOC_MAX_BODIES = 4096
@@ -72,6 +73,11 @@ class BodyState(C.Structure):
 class BarrierOut(C.Structure):
     _fields_ = [("energy", C.c_double), ("nnzb", C.c_int64), ("grad", _vp),
                 ("row_ptr", _vp), ("col", _vp), ("val", _vp)]
+
+
+class FrictionView(C.Structure):
+    _fields_ = [("num", C.c_int64), ("mu", C.c_double), ("type", _vp), ("verts", _vp),
+                ("bodies", _vp), ("coef", _vp)]
 
 
 class Stats(C.Structure):
@@ -117,6 +123,10 @@ def load():
     L.rigc_barrier_local_terms_noalloc.argtypes = [
         _vp, C.c_int32, _vp, C.c_int64, _vp, _vp, _vp, _vp, _vp, C.c_double, C.c_double,
         C.c_int, _vp, _vp, _vp, _vp]
+    L.rigc_friction_setup.argtypes = [_vp, _vp, C.c_double, C.c_double, C.c_double, _i64]
+    L.rigc_get_friction.argtypes = [_vp, C.POINTER(FrictionView)]
+    L.rigc_friction_term.argtypes = [_vp, _vp, C.c_double, C.c_int, C.POINTER(BarrierOut)]
+    L.rigc_friction_local_terms.argtypes = [_vp, _vp, C.c_double, C.c_int, _vp, _vp, _vp]
     for f in EXPORTS:
         getattr(L, f).restype = C.c_char_p if f == "rigc_status_string" else C.c_int
     _lib = L
