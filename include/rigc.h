@@ -149,9 +149,23 @@ int rigc_detect_candidates(rigc_ctx* ctx, const double* x0, const double* x1,
                            int continuous, double inflation_radius,
                            rigc_candidates* out);
 
+/* Candidates given by the caller instead of the broad phase (host arrays,
+ * ee: num_ee (edge, edge) pairs, fv: num_fv (face, vertex) pairs), the
+ * Candidates argument of compute_earliest_toi_narrow_phase
+ * (src/opt/distance_barrier_constraint.cpp:151-156).  Indices are checked;
+ * RIGC_ERR_ARG when one is out of range. */
+int rigc_set_candidates(rigc_ctx* ctx, int64_t num_ee, const int32_t* ee,
+                        int64_t num_fv, const int32_t* fv);
+
+/* Per-candidate cap on the boxes one CCD search may evaluate (default
+ * 2^22; the reference has none).  A search that reaches it reports the
+ * smallest t.lo still unexplored, a conservative time of impact, and
+ * RIGC_ERR_ITER_LIMIT. */
+int rigc_set_ccd_budget(rigc_ctx* ctx, int64_t max_boxes_per_candidate);
+
 /* ---- narrow phase CCD: compute_earliest_toi_narrow_phase
  * (src/opt/distance_barrier_constraint.cpp:151-265) over the candidates of
- * the last rigc_detect_candidates call, trajectory RIGID
+ * the last rigc_detect_candidates / rigc_set_candidates call, trajectory RIGID
  * (src/ccd/rigid/time_of_impact.cpp:158-310).  Every candidate searches
  * t in [0, 1]; *toi_host = INFINITY when nothing collides.  per_candidate
  * (device, optional, num_ee + num_fv doubles, ee first). */

@@ -294,15 +294,17 @@ int orc_face_vertex_toi(void* p, const double* x0, const double* x1, int f,
 double orc_earliest_toi(
     void* p, const double* x0, const double* x1, const int* ee, long long nee,
     const int* fv, long long nfv, double tol, int nthreads, double* per,
-    long long* boxes)
+    long long* boxes, long long max_boxes, int* status)
 {
     std::vector<double> tois;
     CCDStats st;
+    st.max_boxes = max_boxes;
     double t = earliest_toi(static_cast<OwnedScene*>(p)->s, x0, x1,
                             pack_candidates(ee, nee, fv, nfv), tol, nthreads,
                             per ? &tois : nullptr, &st);
     if (per) std::memcpy(per, tois.data(), tois.size() * sizeof(double));
     if (boxes) *boxes = st.boxes;
+    if (status) *status = st.status;
     return t;
 }
 

@@ -135,11 +135,23 @@ static bool root_finder(F f, Valid valid, const Box& x0, double tol[3],
         f(xt, y);
         if (zero_in(y[0]) && zero_in(y[1]) && zero_in(y[2])) tol[0] /= 1e2;
     }
+    long long nbox = 0;
+    const long long budget = st ? st->max_boxes : 0;
     while (!stack.empty()) {
         Box x = stack.back();
         stack.pop_back();
         if (x.x[0].lo >= earliest.x[0].lo) continue;
         if (!valid(x)) continue;
+        if (budget > 0 && nbox >= budget) {
+            // budget exhausted: the earliest unexplored t.lo is conservative
+            double m = x.x[0].lo;
+            for (const Box& b : stack) m = std::min(m, b.x[0].lo);
+            earliest.x[0] = I(std::min(earliest.x[0].lo, m));
+            found = true;
+            st->status = std::max(st->status, 5);
+            break;
+        }
+        nbox++;
         I y[3];
         f(x, y);
         if (st) st->boxes++;
@@ -243,8 +255,10 @@ double earliest_toi(
     std::vector<double> tois(n, INFINITY);
     std::atomic<size_t> next(0);
     std::vector<long long> boxes(std::max(1, nthreads), 0);
+    std::vector<int> status(std::max(1, nthreads), 0);
     auto work = [&](int tid) {
         CCDStats local;
+        local.max_boxes = st ? st->max_boxes : 0;
         for (;;) {
             size_t i = next.fetch_add(64);
             if (i >= n) break;
@@ -257,6 +271,7 @@ double earliest_toi(
             }
         }
         boxes[tid] = local.boxes;
+        status[tid] = local.status;
     };
     if (nthreads <= 1) {
         work(0);
@@ -268,8 +283,10 @@ double earliest_toi(
     double m = INFINITY;
     for (double t : tois) m = std::min(m, t);
     if (per) *per = tois;
-    if (st)
+    if (st) {
         for (long long b : boxes) st->boxes += b;
+        for (int v : status) st->status = std::max(st->status, v);
+    }
     return m;
 }
 

@@ -304,8 +304,13 @@ void detect_candidates(
 
 // ---------------------------------------------------------------------------
 // rigid interval CCD
+// box counter, optional per-candidate box budget (0 = none, as the
+// reference) and the worst status (5 = budget exhausted, with the smallest
+// unexplored t.lo reported as a conservative time of impact)
 struct CCDStats {
     long long boxes = 0;
+    long long max_boxes = 0;
+    int status = 0;
 };
 bool edge_edge_toi(
     const Scene& s, const double* x0, const double* x1, int ea, int eb,

@@ -75,7 +75,7 @@ def lib():
         L.orc_face_vertex_toi.argtypes = L.orc_edge_edge_toi.argtypes
         L.orc_earliest_toi.restype = C.c_double
         L.orc_earliest_toi.argtypes = [C.c_void_p, _d, _d, _i, C.c_longlong, _i, C.c_longlong,
-                                       C.c_double, C.c_int, _d, _ll]
+                                       C.c_double, C.c_int, _d, _ll, C.c_longlong, _i]
         L.orc_interval_op.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, _d]
         L.orc_interval_rotation.argtypes = [_d, _d, _d, _d]
         L.orc_det_sin.restype = C.c_double
@@ -307,14 +307,23 @@ class OracleScene:
                                         C.byref(toi), C.byref(boxes))
         return bool(hit), toi.value, boxes.value
 
-    def earliest_toi(self, x0, x1, ee, fv, tol=1e-4, nthreads=1, per_candidate=False):
+    def earliest_toi(self, x0, x1, ee, fv, tol=1e-4, nthreads=1, per_candidate=False,
+                     max_boxes=0, with_status=False):
+        """Earliest time of impact (per candidate too with per_candidate=True).
+        max_boxes > 0 caps each candidate's search as the CUDA path does;
+        with_status=True appends the worst status (5 = budget exhausted)."""
         x0, x1, ee, fv = _dd(x0), _dd(x1), _ii(ee), _ii(fv)
         per = np.empty(len(ee) + len(fv)) if per_candidate else None
         boxes = C.c_longlong()
+        status = C.c_int()
         t = lib().orc_earliest_toi(self.h, _p(x0, _d), _p(x1, _d), _p(ee, _i), len(ee),
                                    _p(fv, _i), len(fv), tol, nthreads,
-                                   _p(per, _d) if per is not None else None, C.byref(boxes))
-        return (t, per, boxes.value) if per_candidate else t
+                                   _p(per, _d) if per is not None else None, C.byref(boxes),
+                                   int(max_boxes), C.byref(status))
+        out = (t, per, boxes.value) if per_candidate else (t,)
+        if with_status:
+            out = out + (status.value,)
+        return out if len(out) > 1 else out[0]
 
 
 def rotation_matrix(theta):

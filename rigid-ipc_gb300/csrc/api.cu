@@ -76,7 +76,7 @@ static void release_all(Ctx* c)
                        &c->d_scalars, &c->body_box, &c->body_in, &c->vbox, &c->ebox, &c->fbox,
                        &c->vin, &c->ein, &c->fin, &c->items_key, &c->items_val, &c->items_key2,
                        &c->items_val2, &c->seg, &c->pair_out, &c->pair_key, &c->large_list,
-                       &c->x0_dev, &c->x1_dev, &c->rot_table, &c->frame_keys,
+                       &c->x0_dev, &c->x1_dev, &c->rot_table, &c->cand_tol, &c->frame_keys,
                        &c->frame_vals, &c->fric.type, &c->fric.verts, &c->fric.bodies,
                        &c->fric.coef, &c->fric.v0c, &c->fric.V0, &c->fric.c_energy,
                        &c->fric.c_grad, &c->fric.c_blocks, &c->fric.grad, &c->fric.row_ptr,
@@ -252,6 +252,38 @@ int rigc_detect_candidates(rigc_ctx* ctx, const double* x0, const double* x1, in
         out->ee = c.cand.ee.as<int32_t>();
         out->fv = c.cand.fv.as<int32_t>();
     }
+    return RIGC_OK;
+}
+
+int rigc_set_candidates(rigc_ctx* ctx, int64_t num_ee, const int32_t* ee, int64_t num_fv,
+                        const int32_t* fv)
+{
+    if (!ctx || num_ee < 0 || num_fv < 0 || (num_ee && !ee) || (num_fv && !fv))
+        return RIGC_ERR_ARG;
+    Ctx& c = *ctx_of(ctx);
+    for (int64_t i = 0; i < 2 * num_ee; i++)
+        if (ee[i] < 0 || ee[i] >= c.s.ne) return RIGC_ERR_ARG;
+    for (int64_t i = 0; i < num_fv; i++)
+        if (fv[2 * i] < 0 || fv[2 * i] >= c.s.nf || fv[2 * i + 1] < 0 || fv[2 * i + 1] >= c.s.nv)
+            return RIGC_ERR_ARG;
+    RIGC_TRY(c.cand.ee.reserve((size_t)num_ee * 8 + 8));
+    RIGC_TRY(c.cand.fv.reserve((size_t)num_fv * 8 + 8));
+    if (num_ee)
+        RIGC_CUDA(cudaMemcpyAsync(c.cand.ee.ptr, ee, num_ee * 8, cudaMemcpyHostToDevice, c.stream));
+    if (num_fv)
+        RIGC_CUDA(cudaMemcpyAsync(c.cand.fv.ptr, fv, num_fv * 8, cudaMemcpyHostToDevice, c.stream));
+    RIGC_CUDA(cudaStreamSynchronize(c.stream));
+    c.cand.num_ee = num_ee;
+    c.cand.num_fv = num_fv;
+    c.stats.cand_ee = num_ee;
+    c.stats.cand_fv = num_fv;
+    return RIGC_OK;
+}
+
+int rigc_set_ccd_budget(rigc_ctx* ctx, int64_t max_boxes_per_candidate)
+{
+    if (!ctx || max_boxes_per_candidate < 1) return RIGC_ERR_ARG;
+    ctx_of(ctx)->ccd_max_boxes = max_boxes_per_candidate;
     return RIGC_OK;
 }
 

@@ -17,8 +17,12 @@
 // The time of impact of a candidate (the t.lo of its earliest root box) does
 // not depend on the order boxes are visited, so boxes whose t.lo is not below
 // the running minimum over all candidates can be skipped too: that never
-// changes the minimum.  One thread per candidate, a depth-first stack in
-// local memory, the interval vertex positions cached per time interval.  The
+// changes the minimum.  One thread per candidate at a time, a depth-first
+// stack in local memory, the interval vertex positions cached per time
+// interval; the warp advances in lock step, one box per lane per iteration
+// (a lane whose search ends takes the next candidate in the same iteration),
+// and the per-candidate set-up that needs no search (tolerances, the
+// tolerance test) runs beforehand in a kernel of its own.  The
 // interval frames R(t), p(t) of a body depend only on the body and the time
 // interval, which is always a node of the dyadic bisection tree of [0, 1]:
 // the top levels come from a table built per call, deeper nodes from a hash
@@ -64,6 +68,9 @@ struct CCDArgs {
     unsigned long long* fkeys;  // frame cache: keys (0 = empty)
     double* fvals;              // frame cache: kTableEntry doubles per slot
     unsigned long long fmask;   // slots - 1 (a power of two)
+    const double* traj;         // per body: x0 (6), I(x1) - I(x0) (6 intervals)
+    const int* bfixed;          // per body: 1 when the body does not move
+    double* ctol;               // per candidate: the three tolerances
 };
 
 struct Box {
@@ -75,6 +82,8 @@ struct BodyTraj {
     Itv dx[6];  // I(x1) - I(x0)
 };
 
+constexpr int kTrajDoubles = 18;
+
 __device__ __forceinline__ void load_traj(const double* x0, const double* x1, int b, BodyTraj& T)
 {
 #pragma unroll
@@ -85,14 +94,24 @@ __device__ __forceinline__ void load_traj(const double* x0, const double* x1, in
     }
 }
 
+__device__ __forceinline__ void traj_from_table(const double* traj, int b, BodyTraj& T)
+{
+    const double* e = traj + (size_t)b * kTrajDoubles;
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        T.x0[k] = e[k];
+        T.dx[k] = Itv { e[6 + 2 * k], e[7 + 2 * k] };
+    }
+}
+
 // R(t), p(t) of a body over the time interval t
 __device__ __forceinline__ void body_at(const BodyTraj& T, const Itv& t, Itv R[9], Itv p[3])
 {
     Itv r[3];
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-        p[k] = iadd(imul(T.dx[k], t), pt(T.x0[k]));
-        r[k] = iadd(imul(T.dx[3 + k], t), pt(T.x0[3 + k]));
+        p[k] = iadd(imul_nonneg(T.dx[k], t), pt(T.x0[k]));
+        r[k] = iadd(imul_nonneg(T.dx[3 + k], t), pt(T.x0[3 + k]));
     }
     irotation(r, R);
 }
@@ -157,27 +176,43 @@ __device__ __forceinline__ void frame_store(double* o, const Itv R[9], const Itv
 
 // Interval rotation and position of every body over the dyadic time
 // intervals [k 2^-d, (k + 1) 2^-d] of the first kTableDepth levels of the
-// bisection tree (node (1 << d) - 1 + k), computed once per call and shared by
-// all candidates of the body.  The same operations produce the same bits as
-// evaluating them inside a box.
+// bisection tree (slot (1 << d) - 1 + k), and over [0, toi_tol] (the
+// interval of the tolerance test every candidate starts with, slot
+// kTableNodes), computed once per call and shared by all candidates of the
+// body.  The same operations produce the same bits as evaluating them inside
+// a box.
 constexpr int kTableDepth = 7;                          // levels 0..6
 constexpr int kTableNodes = (1 << kTableDepth) - 1;     // 127
+constexpr int kTableSlots = kTableNodes + 1;            // + [0, toi_tol]
 constexpr int kTableEntry = 24;                         // R (9 intervals) + p (3)
 
 __global__ void k_rot_table(const double* __restrict__ x0, const double* __restrict__ x1, int nb,
-                            double* __restrict__ table)
+                            double toi_tol, double* __restrict__ table, double* __restrict__ traj,
+                            int* __restrict__ bfixed)
 {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= (int64_t)nb * kTableNodes) return;
-    int b = (int)(i / kTableNodes), node = (int)(i % kTableNodes);
+    if (i >= (int64_t)nb * kTableSlots) return;
+    int b = (int)(i / kTableSlots), node = (int)(i % kTableSlots);
     int d = 31 - __clz(node + 1);
     int k = node + 1 - (1 << d);
     Itv t { ldexp((double)k, -d), ldexp((double)(k + 1), -d) };
+    if (node == kTableNodes) t = Itv { 0.0, toi_tol };
     BodyTraj T;
     load_traj(x0, x1, b, T);
     Itv R[9], p[3];
     body_at(T, t, R, p);
     frame_store(table + (size_t)i * kTableEntry, R, p);
+    if (node == 0) {
+        double* e = traj + (size_t)b * kTrajDoubles;
+        bool fixed = true;
+        for (int k = 0; k < 6; k++) {
+            e[k] = T.x0[k];
+            e[6 + 2 * k] = T.dx[k].lo;
+            e[7 + 2 * k] = T.dx[k].hi;
+            fixed = fixed && is_zero(T.dx[k].lo) && is_zero(T.dx[k].hi);
+        }
+        bfixed[b] = fixed ? 1 : 0;
+    }
 }
 
 
@@ -185,28 +220,14 @@ struct Query {
     bool fv;            // face-vertex (else edge-edge)
     bool a_fixed;       // body A does not move: its vertex intervals never change
     bool b_fixed;
+    bool fresh;         // no vertex interval computed yet for this candidate
     int body_a, body_b;
-    const double* table;
-    unsigned long long* fkeys;
-    double* fvals;
-    unsigned long long fmask;
     double v[4][3];     // rest vertices: EE (a0, a1, b0, b1); FV (v, f0, f1, f2)
-    BodyTraj A, B;      // EE: edge a / edge b bodies; FV: vertex / face bodies
     // cached vertex intervals for one time interval
     double ct0, ct1;
     Itv P[4][3];
 };
 
-__device__ __forceinline__ bool traj_fixed(const BodyTraj& T)
-{
-    bool z = true;
-#pragma unroll
-    for (int k = 0; k < 6; k++) z = z && T.dx[k].lo == 0.0 && T.dx[k].hi == 0.0;
-    return z;
-}
-
-// vertex intervals of the bodies over t (a body that does not move has
-// t-independent intervals, computed once per query)
 __device__ __forceinline__ void frame_load(const double* e, Itv R[9], Itv p[3])
 {
 #pragma unroll
@@ -223,79 +244,90 @@ __device__ __forceinline__ void frame_load_cg(const double* e, Itv R[9], Itv p[3
     for (int j = 0; j < 3; j++) p[j] = Itv { __ldcg(e + 18 + 2 * j), __ldcg(e + 19 + 2 * j) };
 }
 
-static __device__ __noinline__ void frame_cached(const Query& q, const BodyTraj& T, int body,
+// frame of a body over a time interval computed from its trajectory
+static __device__ __noinline__ void frame_compute(const CCDArgs& a, int body, const Itv& t,
+                                                  Itv R[9], Itv p[3])
+{
+    BodyTraj T;
+    traj_from_table(a.traj, body, T);
+    body_at(T, t, R, p);
+}
+
+static __device__ __noinline__ void frame_cached(const CCDArgs& a, int body,
                                                  unsigned long long node, const Itv& t,
                                                  Itv R[9], Itv p[3])
 {
     const unsigned long long key = ((unsigned long long)(body + 1) << kNodeDepth) | node;
     unsigned long long h = mix64(key);
     for (int probe = 0; probe < kProbes; probe++, h++) {
-        unsigned long long* slot = q.fkeys + (h & q.fmask);
+        unsigned long long* slot = a.fkeys + (h & a.fmask);
         unsigned long long k = ld_acquire(slot);
         if (k == 0) {
             k = atomicCAS(slot, 0ull, key | kPending);
             if (k == 0) {
-                body_at(T, t, R, p);
-                frame_store(q.fvals + (h & q.fmask) * kTableEntry, R, p);
+                frame_compute(a, body, t, R, p);
+                frame_store(a.fvals + (h & a.fmask) * kTableEntry, R, p);
                 __threadfence();
                 atomicExch(slot, key);
                 return;
             }
         }
         if (k == key) {
-            frame_load_cg(q.fvals + (h & q.fmask) * kTableEntry, R, p);
+            frame_load_cg(a.fvals + (h & a.fmask) * kTableEntry, R, p);
             return;
         }
         if (k == (key | kPending)) break;
     }
-    body_at(T, t, R, p);
+    frame_compute(a, body, t, R, p);
 }
 
-__device__ __forceinline__ void frame_at(const Query& q, const BodyTraj& T, int body,
-                                         unsigned long long node, const Itv& t, Itv R[9], Itv p[3])
+__device__ __forceinline__ void frame_at(const CCDArgs& a, int body, unsigned long long node,
+                                         const Itv& t, Itv R[9], Itv p[3])
 {
-    if (node != 0 && node < (1ull << kTableDepth) && q.table) {
-        frame_load(q.table + ((size_t)body * kTableNodes + (node - 1)) * kTableEntry, R, p);
-    } else if (node != 0 && q.fkeys) {
-        frame_cached(q, T, body, node, t, R, p);
+    if (node != 0 && node < (1ull << kTableDepth)) {
+        frame_load(a.table + ((size_t)body * kTableSlots + (node - 1)) * kTableEntry, R, p);
+    } else if (node != 0) {
+        frame_cached(a, body, node, t, R, p);
     } else {
-        body_at(T, t, R, p);
+        frame_compute(a, body, t, R, p);
     }
 }
 
-static __device__ __noinline__ void eval_vertices(Query& q, const Itv& t, bool all)
+// vertex intervals of the bodies over t (a body that does not move has
+// t-independent intervals: computed at the candidate's first evaluation only)
+static __device__ __noinline__ void eval_vertices(const CCDArgs& a, Query& q, const Itv& t)
 {
     Itv R[9], p[3];
     const int na = q.fv ? 1 : 2;
     const unsigned long long node = time_node(t.lo, t.hi);
-    if (all || !q.a_fixed) {
-        frame_at(q, q.A, q.body_a, node, t, R, p);
+    if (q.fresh || !q.a_fixed) {
+        frame_at(a, q.body_a, node, t, R, p);
         for (int i = 0; i < na; i++) iworld_vertex(R, p, q.v[i], q.P[i]);
     }
-    if (all || !q.b_fixed) {
-        frame_at(q, q.B, q.body_b, node, t, R, p);
+    if (q.fresh || !q.b_fixed) {
+        frame_at(a, q.body_b, node, t, R, p);
         for (int i = na; i < 4; i++) iworld_vertex(R, p, q.v[i], q.P[i]);
     }
+    q.fresh = false;
     q.ct0 = t.lo;
     q.ct1 = t.hi;
 }
 
-// zero in f(box)?
-__device__ __forceinline__ bool f_contains_zero(Query& q, const Box& x)
+// zero in f(box), with the vertex intervals already at the box's t
+__device__ __forceinline__ bool f_zero(const Query& q, const Box& x)
 {
-    Itv t { x.t0, x.t1 };
-    if (!(x.t0 == q.ct0 && x.t1 == q.ct1)) eval_vertices(q, t, false);
     Itv a { x.a0, x.a1 }, b { x.b0, x.b1 };
 #pragma unroll
     for (int j = 0; j < 3; j++) {
         Itv y;
         if (q.fv) {
-            Itv fp = iadd(iadd(imul(isub(q.P[2][j], q.P[1][j]), a), imul(isub(q.P[3][j], q.P[1][j]), b)),
+            Itv fp = iadd(iadd(imul_nonneg(isub(q.P[2][j], q.P[1][j]), a),
+                               imul_nonneg(isub(q.P[3][j], q.P[1][j]), b)),
                           q.P[1][j]);
             y = isub(q.P[0][j], fp);
         } else {
-            Itv ea = iadd(imul(isub(q.P[1][j], q.P[0][j]), a), q.P[0][j]);
-            Itv eb = iadd(imul(isub(q.P[3][j], q.P[2][j]), b), q.P[2][j]);
+            Itv ea = iadd(imul_nonneg(isub(q.P[1][j], q.P[0][j]), a), q.P[0][j]);
+            Itv eb = iadd(imul_nonneg(isub(q.P[3][j], q.P[2][j]), b), q.P[2][j]);
             y = isub(ea, eb);
         }
         if (!zero_in(y)) return false;
@@ -303,68 +335,94 @@ __device__ __forceinline__ bool f_contains_zero(Query& q, const Box& x)
     return true;
 }
 
-// load candidate i and its tolerances; returns the time tolerance
-__device__ __forceinline__ void load_query(const CCDArgs& a, int64_t i, Query& q, double tol[3])
+// rest vertices and bodies of candidate i
+__device__ __forceinline__ void load_candidate(const CCDArgs& a, int64_t i, Query& q)
 {
-    q.ct0 = q.ct1 = __longlong_as_double(0x7ff8000000000000ll);
+    int vid[4];
     if (i < a.nee) {
         q.fv = false;
         int ea = a.ee[i].x, eb = a.ee[i].y;
-        int va[2] = { a.edges[2 * ea], a.edges[2 * ea + 1] };
-        int vb[2] = { a.edges[2 * eb], a.edges[2 * eb + 1] };
-        for (int j = 0; j < 3; j++) {
-            q.v[0][j] = a.rest[3 * (size_t)va[0] + j];
-            q.v[1][j] = a.rest[3 * (size_t)va[1] + j];
-            q.v[2][j] = a.rest[3 * (size_t)vb[0] + j];
-            q.v[3][j] = a.rest[3 * (size_t)vb[1] + j];
-        }
+        vid[0] = a.edges[2 * ea];
+        vid[1] = a.edges[2 * ea + 1];
+        vid[2] = a.edges[2 * eb];
+        vid[3] = a.edges[2 * eb + 1];
         q.body_a = a.ebody[ea];
         q.body_b = a.ebody[eb];
-        load_traj(a.x0, a.x1, q.body_a, q.A);
-        load_traj(a.x0, a.x1, q.body_b, q.B);
-        tol[1] = RDIV(1e-4, a.edge_len[ea]);
-        tol[2] = RDIV(1e-4, a.edge_len[eb]);
     } else {
         q.fv = true;
         int64_t k = i - a.nee;
         int f = a.fv[k].x, v = a.fv[k].y;
-        int fvx[3] = { a.faces[3 * f], a.faces[3 * f + 1], a.faces[3 * f + 2] };
-        for (int j = 0; j < 3; j++) {
-            q.v[0][j] = a.rest[3 * (size_t)v + j];
-            q.v[1][j] = a.rest[3 * (size_t)fvx[0] + j];
-            q.v[2][j] = a.rest[3 * (size_t)fvx[1] + j];
-            q.v[3][j] = a.rest[3 * (size_t)fvx[2] + j];
-        }
+        vid[0] = v;
+        vid[1] = a.faces[3 * f];
+        vid[2] = a.faces[3 * f + 1];
+        vid[3] = a.faces[3 * f + 2];
         q.body_a = a.vbody[v];
         q.body_b = a.fbody[f];
-        load_traj(a.x0, a.x1, q.body_a, q.A);
-        load_traj(a.x0, a.x1, q.body_b, q.B);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) q.v[k][j] = a.rest[3 * (size_t)vid[k] + j];
+    q.a_fixed = a.bfixed[q.body_a] != 0;
+    q.b_fixed = a.bfixed[q.body_b] != 0;
+    q.fresh = true;
+    q.ct0 = q.ct1 = __longlong_as_double(0x7ff8000000000000ll);
+}
+
+// Per-candidate set-up, one thread per candidate: the tolerances (length
+// tolerances 1e-4 / edge length; the time tolerance divided by 100 when f
+// over [0, toi_tol] x [0, tol_a] x [0, tol_b] contains zero).
+__global__ void __launch_bounds__(128) k_ccd_prepare(CCDArgs a)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.nee + a.nfv) return;
+    Query q;
+    load_candidate(a, i, q);
+    double tol[3];
+    if (i < a.nee) {
+        tol[1] = RDIV(1e-4, a.edge_len[a.ee[i].x]);
+        tol[2] = RDIV(1e-4, a.edge_len[a.ee[i].y]);
+    } else {
+        int f = a.fv[i - a.nee].x;
         tol[1] = RDIV(1e-4, a.edge_len[a.f2e[3 * f]]);
         tol[2] = RDIV(1e-4, a.edge_len[a.f2e[3 * f + 1]]);
     }
-    q.table = a.table;
-    q.fkeys = a.fkeys;
-    q.fvals = a.fvals;
-    q.fmask = a.fmask;
-    q.a_fixed = traj_fixed(q.A);
-    q.b_fixed = traj_fixed(q.B);
     tol[0] = a.toi_tol;
-    // every interval of a fixed body is the same for any t: fill all once
     Box xt { 0.0, tol[0], 0.0, tol[1], 0.0, tol[2] };
-    eval_vertices(q, Itv { xt.t0, xt.t1 }, true);
-    if (f_contains_zero(q, xt)) tol[0] = RDIV(tol[0], 1e2);
+    Itv R[9], p[3];
+    const int na = q.fv ? 1 : 2;
+    frame_load(a.table + ((size_t)q.body_a * kTableSlots + kTableNodes) * kTableEntry, R, p);
+    for (int k = 0; k < na; k++) iworld_vertex(R, p, q.v[k], q.P[k]);
+    frame_load(a.table + ((size_t)q.body_b * kTableSlots + kTableNodes) * kTableEntry, R, p);
+    for (int k = na; k < 4; k++) iworld_vertex(R, p, q.v[k], q.P[k]);
+    if (f_zero(q, xt)) tol[0] = RDIV(tol[0], 1e2);
+    a.ctol[3 * i] = tol[0];
+    a.ctol[3 * i + 1] = tol[1];
+    a.ctol[3 * i + 2] = tol[2];
 }
 
-// Persistent kernel: each thread takes the next unprocessed candidate from a
-// global counter whenever its box stack runs empty, so lanes of a warp keep
-// evaluating boxes instead of waiting for the warp's longest search.
+// a <= b for non-negative doubles (+0 and +inf included), on the bit pattern
+__device__ __forceinline__ bool le_nn(double a, double b)
+{
+    return __double_as_longlong(a) <= __double_as_longlong(b);
+}
+
+__device__ __forceinline__ double load_gmin(const CCDArgs& a)
+{
+    return __longlong_as_double((long long)*(volatile unsigned long long*)a.gmin);
+}
+
+// Persistent kernel: each lane takes the next unprocessed candidate from a
+// global counter whenever its box stack runs empty.  Every iteration each
+// lane pops boxes until one survives the cheap tests (or takes a new
+// candidate's root box), then all lanes evaluate their boxes together.
 __global__ void __launch_bounds__(kCCDThreads)
 k_ccd(CCDArgs a)
 {
     const int64_t n = a.nee + a.nfv;
-    unsigned long long tot_boxes = 0, tot_hits = 0;
+    unsigned long long tot_boxes = 0, tot_hits = 0, pops = 0;
     Query q;
-    double tol[3];
+    double tol[3] = { 0, 0, 0 };
     Box stack[kCCDStack];
     int sp = 0;
     int64_t cur = -1;
@@ -373,40 +431,56 @@ k_ccd(CCDArgs a)
     int status = RIGC_OK;
     unsigned long long cboxes = 0;
     double gbound = INFINITY;
+    bool done = false;
     while (true) {
-        if (sp == 0) {
-            if (cur >= 0) {
-                double toi = found ? earliest : INFINITY;
-                if (found) {
-                    atomicMin(a.gmin, (unsigned long long)__double_as_longlong(toi));
-                    tot_hits++;
+        bool have = false;
+        Box x;
+        if (!done) {
+            while (sp > 0) {
+                x = stack[--sp];
+                if (le_nn(earliest, x.t0)) continue;
+                if (a.prune) {
+                    if ((++pops & 7) == 0) gbound = load_gmin(a);
+                    if (le_nn(gbound, x.t0)) continue;
                 }
-                if (a.per) a.per[cur] = toi;
-                if (status != RIGC_OK) atomicMax(a.status, status);
+                if (q.fv) {
+                    double sl = add_dn(x.a0, x.b0), sh = add_up(x.a1, x.b1);
+                    if (!(le_nn(sl, 1.0) && !is_neg(sh))) continue;
+                }
+                have = true;
+                break;
             }
-            cur = (int64_t)atomicAdd(a.next, 1ull);
-            if (cur >= n) break;
-            load_query(a, cur, q, tol);
-            if (a.prune)
-                gbound = __longlong_as_double((long long)*(volatile unsigned long long*)a.gmin);
-            stack[sp++] = Box { 0.0, 1.0, 0.0, 1.0, 0.0, 1.0 };
-            earliest = INFINITY;
-            found = false;
-            status = RIGC_OK;
-            cboxes = 0;
-            continue;
+            if (!have) {
+                if (cur >= 0) {
+                    double toi = found ? earliest : INFINITY;
+                    if (found) {
+                        atomicMin(a.gmin, (unsigned long long)__double_as_longlong(toi));
+                        tot_hits++;
+                    }
+                    if (a.per) a.per[cur] = toi;
+                    if (status != RIGC_OK) atomicMax(a.status, status);
+                }
+                cur = (int64_t)atomicAdd(a.next, 1ull);
+                if (cur >= n) {
+                    done = true;
+                } else {
+                    load_candidate(a, cur, q);
+                    tol[0] = a.ctol[3 * cur];
+                    tol[1] = a.ctol[3 * cur + 1];
+                    tol[2] = a.ctol[3 * cur + 2];
+                    if (a.prune) gbound = load_gmin(a);
+                    earliest = INFINITY;
+                    found = false;
+                    status = RIGC_OK;
+                    cboxes = 0;
+                    x = Box { 0.0, 1.0, 0.0, 1.0, 0.0, 1.0 };
+                    have = !(a.prune && le_nn(gbound, x.t0));
+                }
+            }
         }
-        Box x = stack[--sp];
-        if (x.t0 >= earliest) continue;
-        if (a.prune) {
-            if ((tot_boxes & 7) == 0)
-                gbound = __longlong_as_double((long long)*(volatile unsigned long long*)a.gmin);
-            if (x.t0 >= gbound) continue;
-        }
-        if (q.fv) {
-            double sl = add_dn(x.a0, x.b0), sh = add_up(x.a1, x.b1);
-            if (!(sl <= 1.0 && 0.0 <= sh)) continue;
-        }
+        // every lane reaches this point once per iteration
+        if (__all_sync(0xffffffffu, done)) break;
+        if (!have) continue;
         if (cboxes >= (unsigned long long)a.max_boxes) {
             // budget exhausted: the earliest unexplored t.lo is conservative
             double m = x.t0;
@@ -419,11 +493,12 @@ k_ccd(CCDArgs a)
         }
         cboxes++;
         tot_boxes++;
-        if (!f_contains_zero(q, x)) continue;
+        if (!(x.t0 == q.ct0 && x.t1 == q.ct1)) eval_vertices(a, q, Itv { x.t0, x.t1 });
+        if (!f_zero(q, x)) continue;
         double w[3] = { sub_up(x.t1, x.t0), sub_up(x.a1, x.a0), sub_up(x.b1, x.b0) };
-        bool all_tol = w[0] <= tol[0] && w[1] <= tol[1] && w[2] <= tol[2];
-        bool all_zero = w[0] <= 1e-10 && w[1] <= 1e-10 && w[2] <= 1e-10;
-        if ((x.t0 > 0 || all_zero) && all_tol) {
+        bool all_tol = le_nn(w[0], tol[0]) && le_nn(w[1], tol[1]) && le_nn(w[2], tol[2]);
+        bool all_zero = le_nn(w[0], 1e-10) && le_nn(w[1], 1e-10) && le_nn(w[2], 1e-10);
+        if ((is_pos(x.t0) || all_zero) && all_tol) {
             earliest = x.t0;
             found = true;
             if (a.prune) {
@@ -435,8 +510,8 @@ k_ccd(CCDArgs a)
         int split = -1;
 #pragma unroll
         for (int d = 0; d < 3; d++)
-            if ((all_tol || w[d] > tol[d])
-                && (split == -1 || RMUL(w[d], tol[split]) > RMUL(w[split], tol[d])))
+            if ((all_tol || !le_nn(w[d], tol[d]))
+                && (split == -1 || !le_nn(RMUL(w[d], tol[split]), RMUL(w[split], tol[d]))))
                 split = d;
         Box lo = x, hi = x;
         if (split == 0) {
@@ -502,18 +577,27 @@ int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flag
         a.nfv = c.cand.num_fv;
         a.toi_tol = toi_tol;
         a.prune = (flags & RIGC_TOI_NO_PRUNE) ? 0 : 1;
-        a.max_boxes = 1ll << 22;
+        a.max_boxes = c.ccd_max_boxes;
         a.gmin = cnt;
         a.per = per;
         a.status = reinterpret_cast<int*>(cnt + 3);
         a.boxes = cnt + 1;
         a.hits = cnt + 2;
         a.next = cnt + 4;
-        RIGC_TRY(c.rot_table.reserve((size_t)c.s.nb * kTableNodes * kTableEntry * sizeof(double)));
-        RIGC_COUNT_LAUNCH();
-        k_rot_table<<<grid_for((int64_t)c.s.nb * kTableNodes, 128), 128, 0, st>>>(
-            x0, x1, c.s.nb, c.rot_table.as<double>());
+        // per-body frames over the table's time intervals, then the
+        // per-body trajectories and fixed flags, then per-candidate tolerances
+        const size_t table_bytes = (size_t)c.s.nb * kTableSlots * kTableEntry * sizeof(double);
+        const size_t traj_bytes = (size_t)c.s.nb * kTrajDoubles * sizeof(double);
+        RIGC_TRY(c.rot_table.reserve(table_bytes + traj_bytes + (size_t)c.s.nb * sizeof(int) + 64));
+        RIGC_TRY(c.cand_tol.reserve((size_t)n * 3 * sizeof(double)));
         a.table = c.rot_table.as<double>();
+        a.traj = reinterpret_cast<double*>(c.rot_table.as<char>() + table_bytes);
+        a.bfixed = reinterpret_cast<int*>(c.rot_table.as<char>() + table_bytes + traj_bytes);
+        a.ctol = c.cand_tol.as<double>();
+        RIGC_COUNT_LAUNCH();
+        k_rot_table<<<grid_for((int64_t)c.s.nb * kTableSlots, 128), 128, 0, st>>>(
+            x0, x1, c.s.nb, toi_tol, const_cast<double*>(a.table), const_cast<double*>(a.traj),
+            const_cast<int*>(a.bfixed));
         // frame cache: 1024 slots per body, at least 2^16, at most 2^22
         size_t slots = 1u << 16;
         while (slots < (size_t)c.s.nb * 1024 && slots < (1u << 22)) slots <<= 1;
@@ -523,6 +607,8 @@ int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flag
         a.fkeys = c.frame_keys.as<unsigned long long>();
         a.fvals = c.frame_vals.as<double>();
         a.fmask = slots - 1;
+        RIGC_COUNT_LAUNCH();
+        k_ccd_prepare<<<grid_for(n, 128), 128, 0, st>>>(a);
         static int blocks_per_sm = 0;
         if (!blocks_per_sm) {
             RIGC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_ccd,

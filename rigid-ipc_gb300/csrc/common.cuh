@@ -149,8 +149,10 @@ struct Ctx {
     DevBuf x0_dev, x1_dev;
     // CCD: body frames over the top dyadic time intervals
     DevBuf rot_table;
+    DevBuf cand_tol;  // CCD: per-candidate tolerances
     DevBuf frame_keys, frame_vals;  // CCD frame cache (hash table)
     Friction fric;
+    int64_t ccd_max_boxes = int64_t(1) << 22;  // per-candidate CCD box budget
 };
 
 Ctx* ctx_of(rigc_ctx* c);

@@ -44,19 +44,64 @@ __device__ __forceinline__ double dsucc(double x)
     return __longlong_as_double(b > 0 ? b + 1 : b - 1);
 }
 
-__device__ __forceinline__ double add_dn(double x, double y) { return x == -y ? 0.0 : dpred(RADD(x, y)); }
-__device__ __forceinline__ double add_up(double x, double y) { return x == -y ? 0.0 : dsucc(RADD(x, y)); }
-__device__ __forceinline__ double sub_dn(double x, double y) { return x == y ? 0.0 : dpred(RSUB(x, y)); }
-__device__ __forceinline__ double sub_up(double x, double y) { return x == y ? 0.0 : dsucc(RSUB(x, y)); }
-__device__ __forceinline__ double mul_dn(double x, double y) { return (x == 0 || y == 0) ? 0.0 : dpred(RMUL(x, y)); }
-__device__ __forceinline__ double mul_up(double x, double y) { return (x == 0 || y == 0) ? 0.0 : dsucc(RMUL(x, y)); }
-__device__ __forceinline__ double div_dn(double x, double y) { return x == 0 ? 0.0 : dpred(RDIV(x, y)); }
-__device__ __forceinline__ double div_up(double x, double y) { return x == 0 ? 0.0 : dsucc(RDIV(x, y)); }
+// Sign and order tests on the bit pattern (integer instructions; the
+// double-precision pipe is the scarce one on this GPU).  Exact for every
+// non-NaN double, +-0 and +-inf included; no NaN reaches them.
+__device__ __forceinline__ bool is_zero(double x) { return (__double_as_longlong(x) << 1) == 0; }
+// x < 0: sign bit set and not -0
+__device__ __forceinline__ bool is_neg(double x)
+{
+    return (unsigned long long)__double_as_longlong(x) > 0x8000000000000000ull;
+}
+// x > 0
+__device__ __forceinline__ bool is_pos(double x) { return __double_as_longlong(x) > 0; }
+// monotone integer key: key(x) < key(y) iff x < y, except -0 < +0
+__device__ __forceinline__ long long order_key(double x)
+{
+    long long b = __double_as_longlong(x);
+    return b ^ ((b >> 63) & 0x7fffffffffffffffll);
+}
+// x < y
+__device__ __forceinline__ bool lt(double x, double y)
+{
+    return order_key(x) < order_key(y) && !(is_zero(x) && is_zero(y));
+}
 
-__device__ __forceinline__ double smin(double a, double b) { return b < a ? b : a; }
-__device__ __forceinline__ double smax(double a, double b) { return a < b ? b : a; }
-__device__ __forceinline__ bool is_neg(double x) { return x < 0; }
-__device__ __forceinline__ bool is_pos(double x) { return x > 0; }
+// A sum or difference of finite doubles is zero only when exact (no
+// underflow to zero), so the exact-zero rule tests the rounded result.
+__device__ __forceinline__ double add_dn(double x, double y)
+{
+    double r = RADD(x, y);
+    return is_zero(r) ? 0.0 : dpred(r);
+}
+__device__ __forceinline__ double add_up(double x, double y)
+{
+    double r = RADD(x, y);
+    return is_zero(r) ? 0.0 : dsucc(r);
+}
+__device__ __forceinline__ double sub_dn(double x, double y)
+{
+    double r = RSUB(x, y);
+    return is_zero(r) ? 0.0 : dpred(r);
+}
+__device__ __forceinline__ double sub_up(double x, double y)
+{
+    double r = RSUB(x, y);
+    return is_zero(r) ? 0.0 : dsucc(r);
+}
+__device__ __forceinline__ double mul_dn(double x, double y)
+{
+    return (is_zero(x) || is_zero(y)) ? 0.0 : dpred(RMUL(x, y));
+}
+__device__ __forceinline__ double mul_up(double x, double y)
+{
+    return (is_zero(x) || is_zero(y)) ? 0.0 : dsucc(RMUL(x, y));
+}
+__device__ __forceinline__ double div_dn(double x, double y) { return is_zero(x) ? 0.0 : dpred(RDIV(x, y)); }
+__device__ __forceinline__ double div_up(double x, double y) { return is_zero(x) ? 0.0 : dsucc(RDIV(x, y)); }
+
+__device__ __forceinline__ double smin(double a, double b) { return lt(b, a) ? b : a; }
+__device__ __forceinline__ double smax(double a, double b) { return lt(a, b) ? b : a; }
 
 __device__ __forceinline__ Itv ineg(const Itv& x) { return Itv { -x.hi, -x.lo }; }
 __device__ __forceinline__ Itv iadd(const Itv& x, const Itv& y)
@@ -101,12 +146,21 @@ __device__ __forceinline__ Itv imul(const Itv& x, const Itv& y)
     return Itv { 0.0, 0.0 };
 }
 
-// scalar times interval
+// Product with an interval y whose lower bound is not negative (time and
+// barycentric intervals): the sign-case table reduces to one choice of
+// factor per bound, made without branches.
+__device__ __forceinline__ Itv imul_nonneg(const Itv& x, const Itv& y)
+{
+    const double yl = is_neg(x.lo) ? y.hi : y.lo;
+    const double yu = is_neg(x.hi) ? y.lo : y.hi;
+    return Itv { mul_dn(x.lo, yl), mul_up(x.hi, yu) };
+}
+
+// scalar times interval (a zero scalar gives [0, 0] through the zero rule)
 __device__ __forceinline__ Itv imul(double x, const Itv& y)
 {
-    if (is_neg(x)) return Itv { mul_dn(x, y.hi), mul_up(x, y.lo) };
-    if (x == 0) return Itv { 0.0, 0.0 };
-    return Itv { mul_dn(x, y.lo), mul_up(x, y.hi) };
+    const bool neg = is_neg(x);
+    return Itv { mul_dn(x, neg ? y.hi : y.lo), mul_up(x, neg ? y.lo : y.hi) };
 }
 
 // quotient by an interval that excludes zero (the only case on this path)
@@ -156,7 +210,7 @@ __device__ __forceinline__ Itv ihull(const Itv& x, const Itv& y)
     return Itv { smin(x.lo, y.lo), smax(x.hi, y.hi) };
 }
 
-__device__ __forceinline__ bool zero_in(const Itv& x) { return x.lo <= 0 && x.hi >= 0; }
+__device__ __forceinline__ bool zero_in(const Itv& x) { return !is_pos(x.lo) && !is_neg(x.hi); }
 __device__ __forceinline__ double iwidth(const Itv& x) { return sub_up(x.hi, x.lo); }
 
 // ---------------------------------------------------------------------------

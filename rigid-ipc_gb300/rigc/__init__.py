@@ -128,6 +128,18 @@ class Context:
         fv = self.copy_out(out.fv, (out.num_fv, 2), np.int32)
         return ee, fv
 
+    def set_candidates(self, ee, fv):
+        """Use the given (edge, edge) and (face, vertex) pairs as the candidate set."""
+        ee = np.ascontiguousarray(np.asarray(ee, np.int32).reshape(-1, 2))
+        fv = np.ascontiguousarray(np.asarray(fv, np.int32).reshape(-1, 2))
+        L.check(self.lib.rigc_set_candidates(self.h, len(ee), ee.ctypes.data if len(ee) else None,
+                                             len(fv), fv.ctypes.data if len(fv) else None),
+                "rigc_set_candidates")
+
+    def set_ccd_budget(self, max_boxes_per_candidate):
+        L.check(self.lib.rigc_set_ccd_budget(self.h, int(max_boxes_per_candidate)),
+                "rigc_set_ccd_budget")
+
     def earliest_toi(self, x0, x1, toi_tol=1e-4, prune=True, per_candidate=False):
         """compute_earliest_toi_narrow_phase over the last continuous candidates."""
         x0d, x1d = self.device(x0), self.device(x1)

@@ -33,6 +33,7 @@ EXPORTS = [
     "rigc_set_constraints", "rigc_barrier_term", "rigc_barrier_local_terms",
     "rigc_narrow_phase_host", "rigc_barrier_local_terms_noalloc", "rigc_body_energy",
     "rigc_friction_setup", "rigc_get_friction", "rigc_friction_term", "rigc_friction_local_terms",
+    "rigc_set_candidates", "rigc_set_ccd_budget",
 ]
 RIGC_ERR_TOO_LARGE = 7
 RIGC_NOALLOC_MAX_BODIES = 4096
@@ -127,6 +128,8 @@ def load():
     L.rigc_get_friction.argtypes = [_vp, C.POINTER(FrictionView)]
     L.rigc_friction_term.argtypes = [_vp, _vp, C.c_double, C.c_int, C.POINTER(BarrierOut)]
     L.rigc_friction_local_terms.argtypes = [_vp, _vp, C.c_double, C.c_int, _vp, _vp, _vp]
+    L.rigc_set_candidates.argtypes = [_vp, C.c_int64, _vp, C.c_int64, _vp]
+    L.rigc_set_ccd_budget.argtypes = [_vp, C.c_int64]
     for f in EXPORTS:
         getattr(L, f).restype = C.c_char_p if f == "rigc_status_string" else C.c_int
     _lib = L
