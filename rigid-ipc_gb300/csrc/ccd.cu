@@ -121,16 +121,30 @@ __device__ __forceinline__ void body_at(const BodyTraj& T, const Itv& t, Itv R[9
 // node (midpoints of dyadic intervals are exact), up to depth 1074.
 constexpr int kNodeDepth = 40;
 
+// t * 2^52 for t in [0, 1] when that is an integer, else ~0 (bit operations)
+__device__ __forceinline__ unsigned long long fixed52(double t)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(t);
+    if (b == 0) return 0;
+    const int e = (int)(b >> 52);                      // biased exponent, t > 0
+    const unsigned long long m = (b & 0xfffffffffffffull) | (1ull << 52);
+    const int sh = 1023 - e;                           // t * 2^52 = m >> sh
+    if (e == 0 || sh < 0 || sh > 52) return ~0ull;     // subnormal, > 1 or < 2^-52
+    if (m & ((1ull << sh) - 1)) return ~0ull;          // not a multiple of 2^-52
+    return m >> sh;
+}
+
 __device__ __forceinline__ unsigned long long time_node(double t0, double t1)
 {
-    int e;
-    double m = frexp(t1 - t0, &e);   // exact for dyadic widths
-    if (m != 0.5) return 0;
-    int d = 1 - e;
-    if (d < 0 || d >= kNodeDepth) return 0;
-    double kd = ldexp(t0, d);
-    if (kd != floor(kd) || ldexp(kd + 1.0, -d) != t1) return 0;
-    return (1ull << d) + (unsigned long long)kd;
+    const unsigned long long k0 = fixed52(t0), k1 = fixed52(t1);
+    if (k0 == ~0ull || k1 == ~0ull || k1 <= k0) return 0;
+    const unsigned long long w = k1 - k0;              // 2^(52 - d) for a node
+    if (w & (w - 1)) return 0;
+    const int lw = 63 - __clzll((long long)w);
+    if (k0 & (w - 1)) return 0;                        // aligned to its width
+    const int d = 52 - lw;
+    if (d >= kNodeDepth) return 0;
+    return (1ull << d) + (k0 >> lw);
 }
 
 // Frame cache: an open-addressing hash table of (body, time node) -> R(t),
@@ -493,7 +507,9 @@ k_ccd(CCDArgs a)
         }
         cboxes++;
         tot_boxes++;
-        if (!(x.t0 == q.ct0 && x.t1 == q.ct1)) eval_vertices(a, q, Itv { x.t0, x.t1 });
+        if (!(__double_as_longlong(x.t0) == __double_as_longlong(q.ct0)
+              && __double_as_longlong(x.t1) == __double_as_longlong(q.ct1)))
+            eval_vertices(a, q, Itv { x.t0, x.t1 });
         if (!f_zero(q, x)) continue;
         double w[3] = { sub_up(x.t1, x.t0), sub_up(x.a1, x.a0), sub_up(x.b1, x.b0) };
         bool all_tol = le_nn(w[0], tol[0]) && le_nn(w[1], tol[1]) && le_nn(w[2], tol[2]);
