@@ -26,7 +26,11 @@
 // interval frames R(t), p(t) of a body depend only on the body and the time
 // interval, which is always a node of the dyadic bisection tree of [0, 1]:
 // the top levels come from a table built per call, deeper nodes from a hash
-// table filled on first use and shared by all candidates of the body.  Every
+// table shared by all candidates of the body.  A lane whose box needs a frame
+// that is not there yet pushes the box back; at the top of the next
+// iteration the whole warp computes that frame together with its sibling and
+// their descendants three levels down (one converged pass instead of many
+// single-lane ones) and publishes them.  Every
 // stack and every search is bounded: on overflow or budget exhaustion the
 // candidate reports the smallest t.lo still unexplored (a conservative time
 // of impact) and an error status.
@@ -267,64 +271,163 @@ static __device__ __noinline__ void frame_compute(const CCDArgs& a, int body, co
     body_at(T, t, R, p);
 }
 
-static __device__ __noinline__ void frame_cached(const CCDArgs& a, int body,
-                                                 unsigned long long node, const Itv& t,
-                                                 Itv R[9], Itv p[3])
+// Frame cache lookup: true (and the frame) when the key is published.
+__device__ __forceinline__ bool cache_find(const CCDArgs& a, unsigned long long key, Itv R[9],
+                                          Itv p[3])
 {
-    const unsigned long long key = ((unsigned long long)(body + 1) << kNodeDepth) | node;
+    unsigned long long h = mix64(key);
+    for (int probe = 0; probe < kProbes; probe++, h++) {
+        const unsigned long long k = ld_acquire(a.fkeys + (h & a.fmask));
+        if (k == key) {
+            frame_load_cg(a.fvals + (h & a.fmask) * kTableEntry, R, p);
+            return true;
+        }
+        if (k == 0 || k == (key | kPending)) return false;
+    }
+    return false;
+}
+
+// Publish a frame unless the key is present or claimed, or no slot is free
+// within kProbes.
+__device__ __forceinline__ void cache_insert(const CCDArgs& a, unsigned long long key,
+                                             const Itv R[9], const Itv p[3])
+{
     unsigned long long h = mix64(key);
     for (int probe = 0; probe < kProbes; probe++, h++) {
         unsigned long long* slot = a.fkeys + (h & a.fmask);
         unsigned long long k = ld_acquire(slot);
+        if (k == 0) k = atomicCAS(slot, 0ull, key | kPending);
         if (k == 0) {
-            k = atomicCAS(slot, 0ull, key | kPending);
-            if (k == 0) {
-                frame_compute(a, body, t, R, p);
-                frame_store(a.fvals + (h & a.fmask) * kTableEntry, R, p);
-                __threadfence();
-                atomicExch(slot, key);
-                return;
-            }
-        }
-        if (k == key) {
-            frame_load_cg(a.fvals + (h & a.fmask) * kTableEntry, R, p);
+            frame_store(a.fvals + (h & a.fmask) * kTableEntry, R, p);
+            __threadfence();
+            atomicExch(slot, key);
             return;
         }
-        if (k == (key | kPending)) break;
+        if (k == key || k == (key | kPending)) return;
     }
-    frame_compute(a, body, t, R, p);
 }
 
-__device__ __forceinline__ void frame_at(const CCDArgs& a, int body, unsigned long long node,
-                                         const Itv& t, Itv R[9], Itv p[3])
+__device__ __forceinline__ unsigned long long frame_key(int body, unsigned long long node)
+{
+    return ((unsigned long long)(body + 1) << kNodeDepth) | node;
+}
+
+// Frames of the two sides (body A, body B) a lane received in the last
+// batched computation, so that the box that asked for them can always go on.
+struct OwnFrames {
+    unsigned long long key[2];
+    double f[2][kTableEntry];
+};
+
+// Frame of a body over t: the table, the lane's own frames, the cache; a
+// time interval that is not a tree node is computed on the spot.  False
+// when the frame still has to be computed.
+__device__ __forceinline__ bool frame_find(const CCDArgs& a, const OwnFrames& own, int side,
+                                          int body, unsigned long long node, const Itv& t,
+                                          Itv R[9], Itv p[3])
 {
     if (node != 0 && node < (1ull << kTableDepth)) {
         frame_load(a.table + ((size_t)body * kTableSlots + (node - 1)) * kTableEntry, R, p);
-    } else if (node != 0) {
-        frame_cached(a, body, node, t, R, p);
-    } else {
-        frame_compute(a, body, t, R, p);
+        return true;
     }
+    if (node == 0) {
+        frame_compute(a, body, t, R, p);
+        return true;
+    }
+    const unsigned long long key = frame_key(body, node);
+    if (own.key[side] == key) {
+        frame_load(own.f[side], R, p);
+        return true;
+    }
+    return cache_find(a, key, R, p);
 }
 
-// vertex intervals of the bodies over t (a body that does not move has
-// t-independent intervals: computed at the candidate's first evaluation only)
-static __device__ __noinline__ void eval_vertices(const CCDArgs& a, Query& q, const Itv& t)
+// Vertex intervals of the bodies over t (a body that does not move has
+// t-independent intervals: computed at the candidate's first evaluation
+// only).  Returns 0, or a mask of the sides whose frame is missing (the
+// cached intervals are then left invalid).
+static __device__ __noinline__ int eval_vertices(const CCDArgs& a, const OwnFrames& own, Query& q,
+                                                 const Itv& t)
 {
     Itv R[9], p[3];
     const int na = q.fv ? 1 : 2;
     const unsigned long long node = time_node(t.lo, t.hi);
+    const double nan = __longlong_as_double(0x7ff8000000000000ll);
+    q.ct0 = q.ct1 = nan;
+    int miss = 0;
     if (q.fresh || !q.a_fixed) {
-        frame_at(a, q.body_a, node, t, R, p);
-        for (int i = 0; i < na; i++) iworld_vertex(R, p, q.v[i], q.P[i]);
+        if (frame_find(a, own, 0, q.body_a, node, t, R, p)) {
+            for (int i = 0; i < na; i++) iworld_vertex(R, p, q.v[i], q.P[i]);
+        } else {
+            miss |= 1;
+        }
     }
     if (q.fresh || !q.b_fixed) {
-        frame_at(a, q.body_b, node, t, R, p);
-        for (int i = na; i < 4; i++) iworld_vertex(R, p, q.v[i], q.P[i]);
+        if (frame_find(a, own, 1, q.body_b, node, t, R, p)) {
+            for (int i = na; i < 4; i++) iworld_vertex(R, p, q.v[i], q.P[i]);
+        } else {
+            miss |= 2;
+        }
     }
+    if (miss) return miss;
     q.fresh = false;
     q.ct0 = t.lo;
     q.ct1 = t.hi;
+    return 0;
+}
+
+// Batched frame computation, executed by the whole warp.  For each lane
+// with a missing frame (body, node n at depth d), the 31 lanes compute the
+// frames of the five-level subtree below n's parent (n, its sibling and
+// their descendants down to depth d + 3), publish them in the cache, and the
+// requesting lane receives n's frame.  The depth-first search keeps asking
+// for those nodes, so one converged pass replaces up to 31 single-lane
+// rotation enclosures.
+static __device__ __noinline__ void warp_compute_frames(const CCDArgs& a, OwnFrames& own,
+                                                        unsigned req, int req_side,
+                                                        int req_body,
+                                                        unsigned long long req_node)
+{
+    const int lane = threadIdx.x & 31;
+    while (req) {
+        const int src = __ffs(req) - 1;
+        req &= req - 1;
+        const int side = __shfl_sync(0xffffffffu, req_side, src);
+        const int body = __shfl_sync(0xffffffffu, req_body, src);
+        const unsigned long long node = __shfl_sync(0xffffffffu, req_node, src);
+        const int d = 63 - __clzll((long long)node);           // node depth (>= kTableDepth)
+        const unsigned long long root = node >> 1;             // depth d - 1
+        // lane L < 31: subtree node L + 1 below root, level l = log2(L + 1)
+        const int l = 31 - __clz(lane + 1);
+        const unsigned long long mine = (root << l) + (unsigned long long)(lane + 1 - (1 << l));
+        const int dm = d - 1 + l;
+        Itv R[9], p[3];
+        const bool work = lane < 31 && l >= 1 && dm < kNodeDepth;
+        if (work) {
+            const unsigned long long k = mine - (1ull << dm);
+            const Itv t { ldexp((double)k, -dm), ldexp((double)(k + 1), -dm) };
+            frame_compute(a, body, t, R, p);
+            cache_insert(a, frame_key(body, mine), R, p);
+        }
+        // hand n's frame to the lane that asked for it
+        const int owner = (int)(node - (root << 1)) + 1;       // lane of n (level 1)
+        double f[kTableEntry];
+#pragma unroll
+        for (int j = 0; j < 9; j++) {
+            f[2 * j] = __shfl_sync(0xffffffffu, R[j].lo, owner);
+            f[2 * j + 1] = __shfl_sync(0xffffffffu, R[j].hi, owner);
+        }
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            f[18 + 2 * j] = __shfl_sync(0xffffffffu, p[j].lo, owner);
+            f[19 + 2 * j] = __shfl_sync(0xffffffffu, p[j].hi, owner);
+        }
+        if (lane == src) {
+            own.key[side] = frame_key(body, node);
+#pragma unroll
+            for (int j = 0; j < kTableEntry; j++) own.f[side][j] = f[j];
+        }
+    }
 }
 
 // zero in f(box), with the vertex intervals already at the box's t
@@ -446,7 +549,18 @@ k_ccd(CCDArgs a)
     unsigned long long cboxes = 0;
     double gbound = INFINITY;
     bool done = false;
+    OwnFrames own;
+    own.key[0] = own.key[1] = 0;
+    bool pend = false;
+    int req_side = 0, req_body = 0;
+    unsigned long long req_node = 0;
     while (true) {
+        // frames asked for in the last iteration, computed by the whole warp
+        const unsigned req = __ballot_sync(0xffffffffu, pend);
+        if (req) {
+            warp_compute_frames(a, own, req, req_side, req_body, req_node);
+            pend = false;
+        }
         bool have = false;
         Box x;
         if (!done) {
@@ -505,11 +619,21 @@ k_ccd(CCDArgs a)
             sp = 0;
             continue;
         }
+        if (!(__double_as_longlong(x.t0) == __double_as_longlong(q.ct0)
+              && __double_as_longlong(x.t1) == __double_as_longlong(q.ct1))) {
+            const int miss = eval_vertices(a, own, q, Itv { x.t0, x.t1 });
+            if (miss) {
+                // retry the box once the warp has computed the frame
+                stack[sp++] = x;
+                pend = true;
+                req_side = (miss & 1) ? 0 : 1;
+                req_body = req_side ? q.body_b : q.body_a;
+                req_node = time_node(x.t0, x.t1);
+                continue;
+            }
+        }
         cboxes++;
         tot_boxes++;
-        if (!(__double_as_longlong(x.t0) == __double_as_longlong(q.ct0)
-              && __double_as_longlong(x.t1) == __double_as_longlong(q.ct1)))
-            eval_vertices(a, q, Itv { x.t0, x.t1 });
         if (!f_zero(q, x)) continue;
         double w[3] = { sub_up(x.t1, x.t0), sub_up(x.a1, x.a0), sub_up(x.b1, x.b0) };
         bool all_tol = le_nn(w[0], tol[0]) && le_nn(w[1], tol[1]) && le_nn(w[2], tol[2]);
