@@ -128,7 +128,7 @@ constexpr int kNodeDepth = 40;
 // t * 2^52 for t in [0, 1] when that is an integer, else ~0 (bit operations)
 __device__ __forceinline__ unsigned long long fixed52(double t)
 {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(t);
+    const unsigned long long b = (unsigned long long)dbits(t);
     if (b == 0) return 0;
     const int e = (int)(b >> 52);                      // biased exponent, t > 0
     const unsigned long long m = (b & 0xfffffffffffffull) | (1ull << 52);
@@ -521,7 +521,7 @@ __global__ void __launch_bounds__(128) k_ccd_prepare(CCDArgs a)
 // a <= b for non-negative doubles (+0 and +inf included), on the bit pattern
 __device__ __forceinline__ bool le_nn(double a, double b)
 {
-    return __double_as_longlong(a) <= __double_as_longlong(b);
+    return dbits(a) <= dbits(b);
 }
 
 __device__ __forceinline__ double load_gmin(const CCDArgs& a)
@@ -619,8 +619,7 @@ k_ccd(CCDArgs a)
             sp = 0;
             continue;
         }
-        if (!(__double_as_longlong(x.t0) == __double_as_longlong(q.ct0)
-              && __double_as_longlong(x.t1) == __double_as_longlong(q.ct1))) {
+        if (!(dbits(x.t0) == dbits(q.ct0) && dbits(x.t1) == dbits(q.ct1))) {
             const int miss = eval_vertices(a, own, q, Itv { x.t0, x.t1 });
             if (miss) {
                 // retry the box once the warp has computed the frame

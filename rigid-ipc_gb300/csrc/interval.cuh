@@ -28,17 +28,26 @@ __device__ __forceinline__ Itv iempty()
 }
 __device__ __forceinline__ bool is_empty(const Itv& x) { return !(x.lo <= x.hi); }
 
+// Bit pattern of a double through an opaque move: the optimizer cannot turn
+// the integer tests below back into double-precision compares.
+__device__ __forceinline__ long long dbits(double x)
+{
+    long long r;
+    asm("mov.b64 %0, %1;" : "=l"(r) : "d"(x));
+    return r;
+}
+
 // next double towards -inf / +inf (nextafter semantics, finite and zero inputs)
 __device__ __forceinline__ double dpred(double x)
 {
-    long long b = __double_as_longlong(x);
+    long long b = dbits(x);
     if ((b & 0x7fffffffffffffffll) == 0) return __longlong_as_double(0x8000000000000001ll);
     if (b == (long long)0xfff0000000000000ull) return x;
     return __longlong_as_double(b > 0 ? b - 1 : b + 1);
 }
 __device__ __forceinline__ double dsucc(double x)
 {
-    long long b = __double_as_longlong(x);
+    long long b = dbits(x);
     if ((b & 0x7fffffffffffffffll) == 0) return __longlong_as_double(1ll);
     if (b == 0x7ff0000000000000ll) return x;
     return __longlong_as_double(b > 0 ? b + 1 : b - 1);
@@ -47,18 +56,18 @@ __device__ __forceinline__ double dsucc(double x)
 // Sign and order tests on the bit pattern (integer instructions; the
 // double-precision pipe is the scarce one on this GPU).  Exact for every
 // non-NaN double, +-0 and +-inf included; no NaN reaches them.
-__device__ __forceinline__ bool is_zero(double x) { return (__double_as_longlong(x) << 1) == 0; }
+__device__ __forceinline__ bool is_zero(double x) { return (dbits(x) << 1) == 0; }
 // x < 0: sign bit set and not -0
 __device__ __forceinline__ bool is_neg(double x)
 {
-    return (unsigned long long)__double_as_longlong(x) > 0x8000000000000000ull;
+    return (unsigned long long)dbits(x) > 0x8000000000000000ull;
 }
 // x > 0
-__device__ __forceinline__ bool is_pos(double x) { return __double_as_longlong(x) > 0; }
+__device__ __forceinline__ bool is_pos(double x) { return dbits(x) > 0; }
 // monotone integer key: key(x) < key(y) iff x < y, except -0 < +0
 __device__ __forceinline__ long long order_key(double x)
 {
-    long long b = __double_as_longlong(x);
+    long long b = dbits(x);
     return b ^ ((b >> 63) & 0x7fffffffffffffffll);
 }
 // x < y
