@@ -50,6 +50,10 @@ def parse():
     ap.add_argument("--bodies", type=int, default=1000)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-sim", action="store_true", help="skip the steps/s measurement")
+    ap.add_argument("--sim-steps", type=int, default=20)
+    ap.add_argument("--batch-scenes", type=int, default=256,
+                    help="scenes of the batched-vs-plain measurement (0 skips it)")
     return ap.parse_args()
 
 
@@ -167,6 +171,116 @@ def cpu_baseline(sc, x0, x1, dhat, budget_s=15.0):
 def combined_rate(n_ccd, n_disc, ccd_rate, bar_rate):
     t = n_ccd / ccd_rate + n_disc / bar_rate
     return (n_ccd + n_disc) / t
+
+
+SIM_WORKLOAD = ("27 unit cubes in a 3x3x3 lattice (spacing 1.05 m, seeded rotations and "
+                "velocities) over a static plane; dt 0.01, dhat 1e-3, g 9.81, implicit-Euler "
+                "IPC Newton solve per step, friction off")
+
+
+def sim_rate(args, torch):
+    """Simulated steps per second of the device time step on the small plain
+    scene, after 3 warm-up steps, and the oracle's restated CPU step on the
+    same scene (a bounded number of steps) as its baseline."""
+    import rigc
+    from rigc import scene as S
+
+    sc = S.scene_from_json(S.spec_cubes(args.seed))
+    ctx = rigc.Context(sc)
+    ctx.sim_init(0.01, (0.0, -9.81, 0.0), 1e-3)
+    ctx.sim_step(3)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    st = ctx.sim_step(args.sim_steps)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t
+    out = {"workload": SIM_WORKLOAD, "steps": args.sim_steps, "steps_per_s": args.sim_steps / dt,
+           "newton_iterations_per_step": st["newton_iterations"] / args.sim_steps,
+           "cg_iterations_per_newton": st["cg_iterations"] / max(st["newton_iterations"], 1)}
+    if not args.no_cpu_baseline:
+        import oracle as O
+
+        O.build()
+        sim = O.OracleSim(sc, h=0.01, gravity=(0.0, -9.81, 0.0), dhat=1e-3)
+        for _ in range(3):
+            sim.step()
+        k, t = 0, time.perf_counter()
+        while k < args.sim_steps and time.perf_counter() - t < 15.0:
+            sim.step()
+            k += 1
+        out["cpu_oracle_steps_per_s"] = k / (time.perf_counter() - t)
+    return out
+
+
+BATCH_WORKLOAD = ("{n} scenes, each a seeded count U[8, 512] of convex hulls of 32 random "
+                  "unit-sphere points (scale U[0.5, 2.0]) in a contact pile (2e-4 m gaps) on its "
+                  "own static plane; dhat 1e-3; one narrow-phase pass per scene")
+
+
+def _hull_scene(seed):
+    """One scene of the batched form with its pile poses and predictor poses."""
+    from rigc import scene as S
+
+    rng = np.random.default_rng(seed)
+    n = int(rng.integers(8, 513))
+    sc = S.scene_from_json(S.spec_hulls(seed, n))
+    x0 = S.packed_pile_poses(sc, seed=seed)
+    return sc, x0, sc.predictor_poses(x0)
+
+
+def batched_rate(args, torch):
+    """Candidate pairs per second of one narrow-phase pass over many small
+    scenes: one batched context (all scenes in the same launches) against one
+    context per scene run one after the other (the plain path)."""
+    import multiprocessing as mp
+
+    import rigc
+    from rigc import scene as S
+
+    seeds = [10_000 + args.seed * 1000 + k for k in range(args.batch_scenes)]
+    with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1)) as pool:
+        items = pool.map(_hull_scene, seeds)
+    scenes = [sc for sc, _, _ in items]
+    big, sob = S.concat_scenes(scenes)
+    X0 = np.concatenate([x for _, x, _ in items])
+    X1 = np.concatenate([x for _, _, x in items])
+    dhat = scenes[0].dhat
+
+    def run_pass(ctx, x0, x1):
+        ctx.compute_earliest_toi(x0, x1)
+        s = ctx.stats()
+        ctx.construct_constraint_set(x0, dhat)
+        ctx.compute_barrier_term(x0, dhat)
+        s2 = ctx.stats()
+        return s["cand_ee"] + s["cand_fv"] + s2["cand_ee"] + s2["cand_fv"]
+
+    cb = rigc.Context(big, scene_of_body=sob)
+    x0d, x1d = cb.device(X0), cb.device(X1)
+    for _ in range(2):
+        run_pass(cb, x0d, x1d)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    pairs_b = 0
+    reps = 3
+    for _ in range(reps):
+        pairs_b += run_pass(cb, x0d, x1d)
+    torch.cuda.synchronize()
+    tb = (time.perf_counter() - t) / reps
+    pairs_b //= reps
+    ctxs = [(rigc.Context(sc), None) for sc in scenes]
+    dev = [(c.device(x0), c.device(x1)) for (c, _), (_, x0, x1) in zip(ctxs, items)]
+    for (c, _), (a, b) in zip(ctxs, dev):
+        run_pass(c, a, b)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    pairs_p = 0
+    for (c, _), (a, b) in zip(ctxs, dev):
+        pairs_p += run_pass(c, a, b)
+    torch.cuda.synchronize()
+    tp = time.perf_counter() - t
+    return {"workload": BATCH_WORKLOAD.format(n=args.batch_scenes), "bodies": big.num_bodies,
+            "pairs_per_pass": pairs_b, "batched_pairs_per_s": pairs_b / tb,
+            "plain_pairs_per_s": pairs_p / tp, "batched_ms": tb * 1e3, "plain_ms": tp * 1e3}
 
 
 def run_reference(args):
@@ -326,6 +440,10 @@ def main():
         "clocks": clk.summary(),
         "gpu_launches": launches,
     }
+    if rank == 0 and not args.no_sim:
+        line["steps_per_s"] = sim_rate(args, torch)
+    if rank == 0 and args.batch_scenes > 0:
+        line["batched"] = batched_rate(args, torch)
     if rank == 0 and not args.no_cpu_baseline:
         base = cpu_baseline(sc, x0, x1, dhat)
         v = combined_rate(n_ccd, n_disc, base["ccd_pairs_per_s"], base["barrier_pairs_per_s"])

@@ -127,6 +127,23 @@ typedef struct rigc_stats {
  *      src/physics/rigid_body_assembler.cpp:19-118) ---- */
 int rigc_ctx_create(const rigc_scene_desc* desc, rigc_ctx** out);
 int rigc_ctx_destroy(rigc_ctx* ctx);
+
+/* ---- batched form (no counterpart in the reference, which simulates one
+ * scene per process): many independent scenes in one context, so that every
+ * call processes all of them in the same launches.  body_scene (host,
+ * num_bodies) gives each body's scene, non-decreasing, in [0, num_scenes).
+ * Element pairs are only formed within a scene (the scene is part of the
+ * hash-grid cell key); the CCD prunes each scene by its own running minimum;
+ * constraint sets, gradients and the block-sparse Hessian are those of the
+ * scenes side by side.  Per-scene results of the last call: */
+int rigc_ctx_create_batched(const rigc_scene_desc* desc, int32_t num_scenes,
+                            const int32_t* body_scene, rigc_ctx** out);
+int rigc_num_scenes(const rigc_ctx* ctx);
+/* earliest time of impact of each scene (host, num_scenes; INFINITY when a
+ * scene has no impact), after rigc_earliest_toi / rigc_compute_earliest_toi */
+int rigc_scene_tois(rigc_ctx* ctx, double* toi_host);
+/* barrier energy of each scene (host, num_scenes), after rigc_barrier_term */
+int rigc_scene_barrier_energies(rigc_ctx* ctx, double* energy_host);
 int rigc_set_stream(rigc_ctx* ctx, void* cuda_stream);
 const char* rigc_status_string(int status);
 int rigc_get_stats(const rigc_ctx* ctx, rigc_stats* out);
@@ -272,6 +289,61 @@ int rigc_friction_term(rigc_ctx* ctx, const double* x, double epsv_times_h,
 int rigc_friction_local_terms(rigc_ctx* ctx, const double* x,
                               double epsv_times_h, int flags, double* energy,
                               double* grad, double* hess);
+
+/* ---- time stepping.  DistanceBarrierRBProblem::simulation_step
+ * (src/problems/distance_barrier_rb_problem.cpp:118-143) with the IPC Newton
+ * solver (src/solvers/ipc_solver.cpp, src/solvers/newton_solver.cpp) for the
+ * default settings: implicit Euler, velocity convergence, one friction
+ * lagging iteration, no kinematic bodies.  Every term, the CCD line-search
+ * filter and the Newton linear solve (block-Jacobi preconditioned conjugate
+ * gradients on the block-sparse Hessian, relative residual 1e-12) run on the
+ * device; the solver's scalar decisions run on the host.  Field names follow
+ * the reference's JSON settings; average_mass and world_bbox_diagonal are the
+ * values the problem computes at start-up (RigidBodyAssembler::average_mass,
+ * rigid_body_assembler.cpp:104-118; the world bounding-box diagonal,
+ * rigid_body_problem.cpp:91-94). */
+typedef struct rigc_sim_params {
+    double timestep;
+    double gravity[3];
+    double dhat;                        /* barrier activation distance      */
+    double dmin;                        /* minimum separation distance      */
+    double coefficient_friction;        /* mu; 0 disables friction          */
+    double static_friction_speed_bound; /* eps_v                            */
+    int32_t max_newton_iterations;      /* 3000                             */
+    double velocity_conv_tol;           /* 1e-2                             */
+    int32_t velocity_conv_tol_abs;      /* 0: relative to the bbox diagonal */
+    double line_search_lower_bound;     /* 1e-12                            */
+    double dhat_epsilon;                /* 1e-9                             */
+    double min_barrier_stiffness_scale; /* 1e11                             */
+    double average_mass;
+    double world_bbox_diagonal;
+} rigc_sim_params;
+
+/* Bodies' state (host pointers, copied by rigc_sim_init). */
+typedef struct rigc_sim_state {
+    const double* mass;        /* num_bodies                                */
+    const double* moment;      /* num_bodies x 3, principal moments         */
+    const int32_t* dof_fixed;  /* num_bodies, bit k set when dof k is fixed */
+    const double* poses;       /* num_bodies x 6 [p, theta]                 */
+    const double* velocities;  /* num_bodies x 6 [v world, omega body]      */
+    const double* Qdot;        /* num_bodies x 9, dR/dt row-major           */
+} rigc_sim_state;
+
+typedef struct rigc_step_stats {
+    int64_t newton_iterations, newton_steps, objective_evals, ccd_calls, cg_iterations;
+    double barrier_stiffness;  /* kappa after the last step               */
+} rigc_step_stats;
+
+/* Start a simulation on the context (barrier stiffness 1, as the reference
+ * starts), advance it by num_steps steps (stats accumulated, may be NULL),
+ * and read the state back (host outputs, any may be NULL).  The linear
+ * velocities and Qdot advance; the angular velocities are left as given
+ * (the implicit-Euler energy uses Qdot). */
+int rigc_sim_init(rigc_ctx* ctx, const rigc_sim_params* params,
+                  const rigc_sim_state* state);
+int rigc_sim_step(rigc_ctx* ctx, int32_t num_steps, rigc_step_stats* stats);
+int rigc_sim_get_state(rigc_ctx* ctx, double* poses, double* velocities,
+                       double* Qdot, double* barrier_stiffness);
 
 /* ---- one narrow-phase pass from host memory (the call a host Newton loop
  * makes per iteration): copies x0/x1 in, runs compute_earliest_toi(x0, x1)

@@ -423,4 +423,62 @@ int orc_friction_term(
     return 0;
 }
 
+
+// one simulation step; per-body arrays are updated in place.  params:
+// h, gravity (3), dhat, dmin, mu, epsv, max_newton_iterations,
+// velocity_conv_tol, velocity_conv_tol_abs, line_search_lower_bound,
+// dhat_epsilon, min_barrier_stiffness_scale, bbox_diagonal, average_mass
+// (17 doubles).  stats: newton iterations, newton steps, objective
+// evaluations, CCD calls.
+void orc_simulation_step(
+    void* p, const double* mass, const double* moment, double* pose, double* vel,
+    double* Qdot, const int* fixed, const int* type, const double* params, double* kappa,
+    long long* stats)
+{
+    const Scene& s = static_cast<OwnedScene*>(p)->s;
+    std::vector<BodyState> bodies(s.nb);
+    for (int b = 0; b < s.nb; b++) {
+        BodyState& B = bodies[b];
+        B.mass = mass[b];
+        for (int i = 0; i < 3; i++) B.moment[i] = moment[3 * b + i];
+        for (int i = 0; i < 6; i++) {
+            B.pose_t0[i] = pose[6 * b + i];
+            B.vel_t0[i] = vel[6 * b + i];
+            B.fixed[i] = fixed[6 * b + i] != 0;
+        }
+        for (int i = 0; i < 9; i++) B.Qdot[i] = Qdot[9 * b + i];
+        B.type = type[b];
+    }
+    SimParams sp;
+    sp.h = params[0];
+    for (int i = 0; i < 3; i++) sp.gravity[i] = params[1 + i];
+    sp.dhat = params[4];
+    sp.dmin = params[5];
+    sp.mu = params[6];
+    sp.epsv = params[7];
+    sp.max_newton_iterations = (int)params[8];
+    sp.velocity_conv_tol = params[9];
+    sp.velocity_conv_tol_abs = (int)params[10];
+    sp.line_search_lower_bound = params[11];
+    sp.dhat_epsilon = params[12];
+    sp.min_barrier_stiffness_scale = params[13];
+    sp.bbox_diagonal = params[14];
+    sp.average_mass = params[15];
+    SimStats st;
+    simulation_step(s, bodies, sp, *kappa, &st);
+    for (int b = 0; b < s.nb; b++) {
+        for (int i = 0; i < 6; i++) {
+            pose[6 * b + i] = bodies[b].pose_t0[i];
+            vel[6 * b + i] = bodies[b].vel_t0[i];
+        }
+        for (int i = 0; i < 9; i++) Qdot[9 * b + i] = bodies[b].Qdot[i];
+    }
+    if (stats) {
+        stats[0] = st.newton_iterations;
+        stats[1] = st.newton_steps;
+        stats[2] = st.objective_evals;
+        stats[3] = st.ccd_calls;
+    }
+}
+
 } // extern "C"

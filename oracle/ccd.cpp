@@ -13,6 +13,8 @@
 // domain), so its time of impact is a function of the candidate alone; the
 // earliest time of impact is the minimum over candidates.
 #include "interval.hpp"
+#include <cstring>
+
 #include "oracle.hpp"
 
 #include <atomic>
@@ -141,6 +143,12 @@ static bool root_finder(F f, Valid valid, const Box& x0, double tol[3],
         Box x = stack.back();
         stack.pop_back();
         if (x.x[0].lo >= earliest.x[0].lo) continue;
+        if (st && st->gmin) {
+            unsigned long long gb = st->gmin->load(std::memory_order_relaxed);
+            double g;
+            std::memcpy(&g, &gb, sizeof(g));
+            if (x.x[0].lo >= g) continue;
+        }
         if (!valid(x)) continue;
         if (budget > 0 && nbox >= budget) {
             // budget exhausted: the earliest unexplored t.lo is conservative
@@ -162,6 +170,12 @@ static bool root_finder(F f, Valid valid, const Box& x0, double tol[3],
         if ((x.x[0].lo > 0 || all_zero) && all_tol) {
             earliest = x;
             found = true;
+            if (st && st->gmin) {
+                unsigned long long nb, ob = st->gmin->load();
+                std::memcpy(&nb, &x.x[0].lo, sizeof(nb));
+                while (nb < ob && !st->gmin->compare_exchange_weak(ob, nb)) {
+                }
+            }
             continue;
         }
         int split = -1;
@@ -256,9 +270,13 @@ double earliest_toi(
     std::atomic<size_t> next(0);
     std::vector<long long> boxes(std::max(1, nthreads), 0);
     std::vector<int> status(std::max(1, nthreads), 0);
+    // without per-candidate results the search skips boxes at or after the
+    // running minimum over all candidates
+    std::atomic<unsigned long long> gmin(0x7ff0000000000000ull);
     auto work = [&](int tid) {
         CCDStats local;
         local.max_boxes = st ? st->max_boxes : 0;
+        if (!per) local.gmin = &gmin;
         for (;;) {
             size_t i = next.fetch_add(64);
             if (i >= n) break;

@@ -1071,4 +1071,33 @@ double friction_term(
     return energy;
 }
 
+// barrier energy only (the value of compute_barrier_term), in doubles
+double barrier_energy(const Scene& s, const double* x, const std::vector<Constraint>& cs,
+                      double dhat, double dmin)
+{
+    std::vector<double> V;
+    world_vertices(s, x, V);
+    auto P = [&](int i) { return &V[3 * i]; };
+    double e = 0;
+    for (const auto& c : cs) {
+        double d;
+        switch (c.type) {
+        case C_VV: d = point_point_sqdist(P(c.v[0]), P(c.v[1])); break;
+        case C_EV: d = point_line_sqdist(P(c.v[0]), P(c.v[1]), P(c.v[2])); break;
+        case C_EE: d = line_line_sqdist(P(c.v[0]), P(c.v[1]), P(c.v[2]), P(c.v[3])); break;
+        default: d = point_plane_sqdist(P(c.v[0]), P(c.v[1]), P(c.v[2]), P(c.v[3])); break;
+        }
+        double f = barrier_t<double>(d - dmin * dmin, 2 * dmin * dhat + dhat * dhat);
+        if (c.type == C_EE) {
+            double x2 = ee_cross_sqnorm(P(c.v[0]), P(c.v[1]), P(c.v[2]), P(c.v[3]));
+            if (x2 < c.eps_x) {
+                double xe = x2 / c.eps_x;
+                f = ((2.0 - xe) * xe) * f;
+            }
+        }
+        e += c.weight * f;
+    }
+    return e;
+}
+
 } // namespace orc

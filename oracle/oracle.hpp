@@ -15,6 +15,7 @@
 
 #include <algorithm>
 #include <array>
+#include <atomic>
 #include <cmath>
 #include <cstdint>
 #include <vector>
@@ -245,6 +246,9 @@ double barrier_term(
     double dhat, double dmin, std::vector<double>& grad, BSR& hess,
     bool project);
 
+double barrier_energy(const Scene& s, const double* x, const std::vector<Constraint>& cs,
+                      double dhat, double dmin);
+
 // body energy (compute_body_energy, distance_barrier_rb_problem.cpp:847-944)
 struct BodyState {
     double mass;
@@ -258,6 +262,24 @@ struct BodyState {
 double body_energy(
     const BodyState& b, const double* x6, const double gravity[3], double h,
     double grad[6], double hess[36]);
+
+// one simulation time step (DistanceBarrierRBProblem::simulation_step with
+// the IPC Newton solver); bodies' pose_t0 / vel_t0 (linear) / Qdot advance,
+// kappa is the barrier stiffness carried from step to step (1 before the
+// first step)
+struct SimParams {
+    double h, gravity[3], dhat, dmin, mu, epsv;
+    int max_newton_iterations;
+    double velocity_conv_tol;
+    int velocity_conv_tol_abs;
+    double line_search_lower_bound, dhat_epsilon, min_barrier_stiffness_scale;
+    double bbox_diagonal, average_mass;
+};
+struct SimStats {
+    long long newton_iterations = 0, newton_steps = 0, objective_evals = 0, ccd_calls = 0;
+};
+void simulation_step(const Scene& s, std::vector<BodyState>& bodies, const SimParams& p,
+                     double& kappa, SimStats* st);
 
 // lagged friction constraints and their local terms
 struct FrictionConstraint {
@@ -311,6 +333,10 @@ struct CCDStats {
     long long boxes = 0;
     long long max_boxes = 0;
     int status = 0;
+    // optional running minimum over all candidates (bits of a non-negative
+    // double): boxes starting at or after it are skipped, which keeps the
+    // earliest time of impact (it does not depend on the visiting order)
+    std::atomic<unsigned long long>* gmin = nullptr;
 };
 bool edge_edge_toi(
     const Scene& s, const double* x0, const double* x1, int ea, int eb,

@@ -64,6 +64,7 @@ def lib():
         L.orc_friction_term.argtypes = [C.c_void_p, _d, _d, C.c_longlong, _i, _i, _i, _i, _d, _d,
                                         _d, _d, _d, C.c_double, C.c_double, C.c_int, _d, _d, _i,
                                         _i, _d, C.c_longlong, _ll]
+        L.orc_simulation_step.argtypes = [C.c_void_p, _d, _d, _d, _d, _d, _i, _i, _d, _d, _ll]
         L.orc_barrier_term.argtypes = [C.c_void_p, _d, C.c_longlong, _i, _i, _i, _i, _d, _d,
                                        C.c_double, C.c_double, C.c_int, _d, _d, _i, _i, _d,
                                        C.c_longlong, _ll]
@@ -377,6 +378,55 @@ def det_sin(x):
 
 def det_cos(x):
     return lib().orc_det_cos(float(x))
+
+
+SIM_DEFAULTS = dict(dmin=0.0, mu=0.0, epsv=1e-3, max_newton_iterations=3000,
+                    velocity_conv_tol=1e-2, velocity_conv_tol_abs=0,
+                    line_search_lower_bound=1e-12, dhat_epsilon=1e-9,
+                    min_barrier_stiffness_scale=1e11)
+
+
+class OracleSim:
+    """Time stepping of a scene with the oracle's restated IPC Newton solver.
+    State: poses (nb x 6), linear/angular velocities (nb x 6), Qdot (nb x 9),
+    barrier stiffness (1 before the first step, as the reference starts)."""
+
+    def __init__(self, scene, h, gravity, dhat, **kw):
+        self.scene = scene
+        self.o = OracleScene(scene)
+        self.p = dict(SIM_DEFAULTS)
+        self.p.update(kw)
+        self.h, self.gravity, self.dhat = h, _dd(gravity), dhat
+        sc = scene
+        self.mass = _dd(sc.mass)
+        self.moment = _dd(sc.moment.reshape(-1))
+        self.fixed = _ii(np.asarray(sc.is_dof_fixed, np.int32).reshape(-1))
+        self.type = _ii(sc.body_type)
+        self.pose = _dd(sc.poses()).copy()
+        self.vel = _dd(sc.velocities()).copy()
+        self.Qdot = _dd(np.concatenate([b.Qdot.reshape(-1) for b in sc.bodies])).copy()
+        V = sc.world_vertices(self.pose)
+        self.bbox_diagonal = float(np.linalg.norm(V.max(0) - V.min(0)))
+        self.kappa = C.c_double(1.0)
+        self.stats = np.zeros(4, np.int64)
+
+    def params(self):
+        p = self.p
+        return _dd([self.h, *self.gravity, self.dhat, p["dmin"], p["mu"], p["epsv"],
+                    p["max_newton_iterations"], p["velocity_conv_tol"],
+                    p["velocity_conv_tol_abs"], p["line_search_lower_bound"],
+                    p["dhat_epsilon"], p["min_barrier_stiffness_scale"], self.bbox_diagonal,
+                    self.scene.average_mass, 0.0])
+
+    def step(self):
+        prm = self.params()
+        st = np.zeros(4, np.int64)
+        lib().orc_simulation_step(self.o.h, _p(self.mass, _d), _p(self.moment, _d),
+                                  _p(self.pose, _d), _p(self.vel, _d), _p(self.Qdot, _d),
+                                  _p(self.fixed, _i), _p(self.type, _i), _p(prm, _d),
+                                  C.byref(self.kappa), st.ctypes.data_as(_ll))
+        self.stats += st
+        return st
 
 
 def body_energy(body, x6, gravity, h):

@@ -1,0 +1,360 @@
+// One simulation time step of the rigid IPC problem (test infrastructure).
+//
+// Restates DistanceBarrierRBProblem::simulation_step
+// (src/problems/distance_barrier_rb_problem.cpp:118-143) for the default
+// settings (implicit Euler, IPC solver with velocity convergence, one friction
+// lagging iteration, no kinematic bodies):
+//  * update_constraints (:145-166): constraint set at the start-of-step poses
+//    x0 and, with friction, the lagged friction constraints (normal forces
+//    with the current barrier stiffness);
+//  * IPCSolver::init_solve (src/solvers/ipc_solver.cpp:36-65): the initial
+//    barrier stiffness from the energy and barrier gradients at x0 and the
+//    initial minimum distance;
+//  * NewtonSolver::solve (src/solvers/newton_solver.cpp:158-300): objective
+//    E/m + kappa/m B + D/m (compute_objective, :633-703) over the free
+//    degrees of freedom, regularised Newton direction
+//    (compute_regularized_direction, :421-478; a dense LDL^T stands in for the
+//    sparse one), the velocity convergence test (:95-140), a line search over
+//    [0, min(toi, 1)] halving the step until the objective decreases
+//    (:302-418), the gradient fallback, and the adaptive stiffness update
+//    after each step (ipc_solver.cpp:67-89);
+//  * take_step (:488-626): implicit-Euler velocity and Qdot updates.
+// The two ipc-toolkit functions used by the solver are restated from the
+// published adaptive-stiffness scheme of Li et al. 2020 (IPC, sec. 4.3):
+// kappa0 = argmin |grad E + kappa grad B| clamped to [kappa_min, 100 kappa_min]
+// with kappa_min = scale * m / (4 d0 b''(d0)), d0 = (1e-8 bbox)^2; kappa
+// doubles while the minimum distance keeps shrinking below 1e-9 bbox.
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <thread>
+
+#include "oracle.hpp"
+
+namespace orc {
+
+namespace {
+
+double barrier_hessian_d(double d, double s)
+{
+    if (d <= 0.0 || d >= s) return 0.0;
+    double sd = s / d;
+    return (sd + 2) * sd - 2 * std::log(d / s) - 3;
+}
+
+// squared distance of one constraint (the distance its barrier uses)
+double constraint_sqdist(const Constraint& c, const std::vector<double>& V)
+{
+    auto P = [&](int i) { return &V[3 * c.v[i]]; };
+    switch (c.type) {
+    case C_VV: return point_point_sqdist(P(0), P(1));
+    case C_EV: return point_line_sqdist(P(0), P(1), P(2));
+    case C_EE: return line_line_sqdist(P(0), P(1), P(2), P(3));
+    default: return point_plane_sqdist(P(0), P(1), P(2), P(3));
+    }
+}
+
+// dense LDL^T (no pivoting) of a symmetric matrix; false on a zero pivot
+bool ldlt_solve(int n, std::vector<double> A, const std::vector<double>& b,
+                std::vector<double>& x)
+{
+    std::vector<double> D(n);
+    for (int j = 0; j < n; j++) {
+        double d = A[j * n + j];
+        for (int k = 0; k < j; k++) d -= A[j * n + k] * A[j * n + k] * D[k];
+        if (!(std::fabs(d) > 0) || !std::isfinite(d)) return false;
+        D[j] = d;
+        for (int i = j + 1; i < n; i++) {
+            double s = A[i * n + j];
+            for (int k = 0; k < j; k++) s -= A[i * n + k] * A[j * n + k] * D[k];
+            A[i * n + j] = s / d;
+        }
+    }
+    x = b;
+    for (int i = 0; i < n; i++)
+        for (int k = 0; k < i; k++) x[i] -= A[i * n + k] * x[k];
+    for (int i = 0; i < n; i++) x[i] /= D[i];
+    for (int i = n - 1; i >= 0; i--)
+        for (int k = i + 1; k < n; k++) x[i] -= A[k * n + i] * x[k];
+    for (double v : x)
+        if (!std::isfinite(v)) return false;
+    return true;
+}
+
+struct Problem {
+    const Scene& s;
+    const std::vector<BodyState>& bodies;
+    const SimParams& p;
+    double kappa, kappa_max = 0;
+    std::vector<FrictionConstraint> fric;
+    std::vector<double> x0;
+    SimStats* st;
+    double s_average_mass;
+
+    Problem(const Scene& s_, const std::vector<BodyState>& b, const SimParams& p_, double k,
+            SimStats* st_)
+        : s(s_), bodies(b), p(p_), kappa(k), st(st_), s_average_mass(p_.average_mass)
+    {
+    }
+
+    int n() const { return 6 * s.nb; }
+
+    std::vector<Constraint> constraints(const double* x) const
+    {
+        Candidates cand;
+        detect_candidates(s, x, x, false, (p.dhat + p.dmin) / 2, false, cand);
+        std::vector<double> V;
+        world_vertices(s, x, V);
+        std::vector<Constraint> cs;
+        construct_constraint_set(s, cand, V, p.dhat, p.dmin, cs);
+        return cs;
+    }
+
+    double min_distance(const double* x) const
+    {
+        std::vector<Constraint> cs = constraints(x);
+        if (cs.empty()) return -1;
+        std::vector<double> V;
+        world_vertices(s, x, V);
+        double m = INFINITY;
+        for (const auto& c : cs) m = std::min(m, constraint_sqdist(c, V));
+        return std::isfinite(m) ? std::sqrt(m) : -1;
+    }
+
+    // body energy term (not divided by the average mass)
+    double energy_term(const double* x, std::vector<double>* g, std::vector<double>* H) const
+    {
+        const int N = n();
+        if (g) g->assign(N, 0.0);
+        if (H) H->assign((size_t)N * N, 0.0);
+        double e = 0;
+        for (int b = 0; b < s.nb; b++) {
+            if (bodies[b].type != 2) continue;
+            double gb[6], hb[36];
+            e += body_energy(bodies[b], x + 6 * b, p.gravity, p.h, gb, hb);
+            // PSD projection of the position block (:765-768)
+            double P3[9], Q3[9];
+            for (int r = 0; r < 3; r++)
+                for (int c = 0; c < 3; c++) P3[3 * r + c] = hb[6 * r + c];
+            project_to_psd(3, P3, Q3);
+            for (int r = 0; r < 3; r++)
+                for (int c = 0; c < 3; c++) hb[6 * r + c] = Q3[3 * r + c];
+            if (g)
+                for (int k = 0; k < 6; k++) (*g)[6 * b + k] += gb[k];
+            if (H)
+                for (int r = 0; r < 6; r++)
+                    for (int c = 0; c < 6; c++)
+                        (*H)[(size_t)(6 * b + r) * N + 6 * b + c] += hb[6 * r + c];
+        }
+        return e;
+    }
+
+    static void add_bsr(const BSR& h, int N, double scale, std::vector<double>& H)
+    {
+        const int nb = (int)h.row_ptr.size() - 1;
+        for (int r = 0; r < nb; r++)
+            for (int k = h.row_ptr[r]; k < h.row_ptr[r + 1]; k++)
+                for (int i = 0; i < 6; i++)
+                    for (int j = 0; j < 6; j++)
+                        H[(size_t)(6 * r + i) * N + 6 * h.col[k] + j] += scale * h.val[36 * k + 6 * i + j];
+    }
+
+    // compute_objective (:633-703)
+    double objective(const double* x, std::vector<double>* g, std::vector<double>* H) const
+    {
+        const int N = n();
+        const double m = s_average_mass;
+        double f = energy_term(x, g, H) / m;
+        if (g)
+            for (double& v : *g) v /= m;
+        if (H)
+            for (double& v : *H) v /= m;
+        std::vector<Constraint> cs = constraints(x);
+        if (g || H) {
+            std::vector<double> gb;
+            BSR hb;
+            double B = barrier_term(s, x, cs, p.dhat, p.dmin, gb, hb, true);
+            f += kappa / m * B;
+            if (g)
+                for (int k = 0; k < N; k++) (*g)[k] += kappa / m * gb[k];
+            if (H) add_bsr(hb, N, kappa / m, *H);
+        } else {
+            f += kappa / m * barrier_energy(s, x, cs, p.dhat, p.dmin);
+        }
+        if (p.mu > 0 && !fric.empty()) {
+            std::vector<double> gd;
+            BSR hd;
+            double D = friction_term(s, x, x0.data(), fric, p.mu, p.epsv * p.h, gd, hd, true);
+            f += D / m;
+            if (g)
+                for (int k = 0; k < N; k++) (*g)[k] += gd[k] / m;
+            if (H) add_bsr(hd, N, 1.0 / m, *H);
+        }
+        if (st) st->objective_evals++;
+        return f;
+    }
+
+    double toi(const double* x, const double* x1) const
+    {
+        Candidates cand;
+        detect_candidates(s, x, x1, true, p.dmin / 2, false, cand);
+        const int nt = std::max(1, (int)std::thread::hardware_concurrency());
+        return earliest_toi(s, x, x1, cand, 1e-4, nt, nullptr, nullptr);
+    }
+};
+
+} // namespace
+
+void simulation_step(const Scene& s, std::vector<BodyState>& bodies, const SimParams& p,
+                     double& kappa, SimStats* st)
+{
+    const int nb = s.nb, N = 6 * nb;
+    Problem pr(s, bodies, p, kappa, st);
+    pr.x0.resize(N);
+    for (int b = 0; b < nb; b++)
+        for (int k = 0; k < 6; k++) pr.x0[6 * b + k] = bodies[b].pose_t0[k];
+    const double* x0 = pr.x0.data();
+
+    // update_constraints: lagged friction at x0 with the current stiffness
+    if (p.mu > 0) {
+        std::vector<Constraint> cs = pr.constraints(x0);
+        std::vector<double> V0;
+        world_vertices(s, x0, V0);
+        construct_friction_constraints(s, cs, V0, p.dhat, 0.0, pr.kappa, pr.fric);
+    }
+
+    // IPCSolver::init_solve
+    {
+        std::vector<double> gE, gB;
+        pr.energy_term(x0, &gE, nullptr);
+        BSR hb;
+        std::vector<Constraint> cs = pr.constraints(x0);
+        barrier_term(s, x0, cs, p.dhat, p.dmin, gB, hb, false);
+        const double dmin = p.dmin;
+        double d0 = 1e-8 * p.bbox_diagonal + dmin;
+        d0 *= d0;
+        const double sb = 2 * dmin * p.dhat + p.dhat * p.dhat;
+        if (d0 - dmin * dmin >= sb) d0 = dmin * p.dhat + 0.5 * p.dhat * p.dhat;
+        double kmin = 4 * d0 * barrier_hessian_d(d0 - dmin * dmin, sb);
+        kmin = p.min_barrier_stiffness_scale * p.average_mass / kmin;
+        pr.kappa_max = 100 * kmin;
+        double gg = 0, ge = 0;
+        for (int k = 0; k < N; k++) {
+            gg += gB[k] * gB[k];
+            ge += gB[k] * gE[k];
+        }
+        double k0 = gg > 0 ? -ge / gg : 1.0;
+        pr.kappa = std::min(pr.kappa_max, std::max(kmin, k0));
+    }
+    double prev_min_distance = pr.min_distance(x0);
+
+    // free degrees of freedom
+    std::vector<int> free_dof;
+    for (int b = 0; b < nb; b++)
+        for (int k = 0; k < 6; k++)
+            if (!bodies[b].fixed[k]) free_dof.push_back(6 * b + k);
+    const int nf = (int)free_dof.size();
+
+    std::vector<double> x = pr.x0, g, H, dir(N, 0.0), gdir(N, 0.0);
+    double coeff = 0;
+    int it = 0;
+    for (; it < p.max_newton_iterations; it++) {
+        double fx = pr.objective(x.data(), &g, &H);
+        std::vector<double> gf(nf), Hf((size_t)nf * nf), df;
+        for (int i = 0; i < nf; i++) {
+            gf[i] = g[free_dof[i]];
+            for (int j = 0; j < nf; j++) Hf[(size_t)i * nf + j] = H[(size_t)free_dof[i] * N + free_dof[j]];
+        }
+        // compute_regularized_direction
+        bool ok = false;
+        while (!ok) {
+            std::vector<double> Hr = Hf, mg(nf);
+            if (coeff > 0)
+                for (int i = 0; i < nf; i++) Hr[(size_t)i * nf + i] += coeff;
+            for (int i = 0; i < nf; i++) mg[i] = -gf[i];
+            // a failed factorisation counts as a failed solve: regularise
+            ok = ldlt_solve(nf, Hr, mg, df);
+            double gd = 0;
+            if (!ok) df = mg;
+            for (int i = 0; i < nf; i++) gd += gf[i] * df[i];
+            ok = ok && gd <= 0;
+            if (ok) {
+                coeff /= 2;
+                if (coeff < 1e-8) coeff = 0;
+            } else {
+                coeff = std::max(2 * coeff, 1e-8);
+                if (!std::isfinite(coeff)) break;
+            }
+        }
+        if (!ok) break;
+        std::fill(dir.begin(), dir.end(), 0.0);
+        std::fill(gdir.begin(), gdir.end(), 0.0);
+        for (int i = 0; i < nf; i++) {
+            dir[free_dof[i]] = df[i];
+            gdir[free_dof[i]] = gf[i];
+        }
+        // velocity convergence
+        if (it > 0) {
+            std::vector<double> V, V1, x1(N);
+            for (int k = 0; k < N; k++) x1[k] = x[k] + dir[k];
+            world_vertices(s, x.data(), V);
+            world_vertices(s, x1.data(), V1);
+            double m = 0;
+            for (size_t k = 0; k < V.size(); k++) m = std::max(m, std::fabs(V1[k] - V[k]));
+            double tol = p.velocity_conv_tol * (p.velocity_conv_tol_abs ? 1.0 : p.bbox_diagonal);
+            if (m / p.h <= tol) break;
+        }
+        auto line_search = [&](const std::vector<double>& d, double& alpha) {
+            double gd = 0;
+            for (int k = 0; k < N; k++) gd += gdir[k] * d[k];
+            double lb = std::min(p.line_search_lower_bound / std::sqrt(std::fabs(gd)), 1e-1);
+            std::vector<double> x1(N);
+            for (int k = 0; k < N; k++) x1[k] = x[k] + d[k];
+            double tmax = std::min(pr.toi(x.data(), x1.data()), 1.0);
+            if (st) st->ccd_calls++;
+            alpha = std::min(1.0, tmax);
+            while (std::isfinite(lb) && alpha >= lb) {
+                for (int k = 0; k < N; k++) x1[k] = x[k] + alpha * d[k];
+                double fxi = pr.objective(x1.data(), nullptr, nullptr);
+                if (fxi < fx) return true;
+                alpha /= 2.0;
+            }
+            return false;
+        };
+        double alpha = 1;
+        bool found = line_search(dir, alpha);
+        if (!found) {
+            for (int k = 0; k < N; k++) dir[k] = -gdir[k];
+            alpha = 1;
+            if (!line_search(dir, alpha)) break;
+        }
+        for (int k = 0; k < N; k++) x[k] += alpha * dir[k];
+        if (st) st->newton_steps++;
+        // IPCSolver::post_step_update: adaptive stiffness
+        double md = pr.min_distance(x.data());
+        double eps = p.dhat_epsilon * (p.bbox_diagonal + p.dmin);
+        if (prev_min_distance < eps && md < eps && md < prev_min_distance)
+            pr.kappa = std::min(pr.kappa_max, 2 * pr.kappa);
+        prev_min_distance = md;
+    }
+    if (st) st->newton_iterations += it;
+
+    // take_step: implicit Euler velocities
+    for (int b = 0; b < nb; b++) {
+        BodyState& B = bodies[b];
+        if (B.type != 2) {
+            continue;
+        }
+        double Q[9], Qp[9];
+        rotation_matrix(&x[6 * b + 3], Q);
+        rotation_matrix(&B.pose_t0[3], Qp);
+        for (int k = 0; k < 3; k++) B.vel_t0[k] = (x[6 * b + k] - B.pose_t0[k]) / p.h;
+        for (int k = 0; k < 9; k++) B.Qdot[k] = (Q[k] - Qp[k]) / p.h;
+        for (int k = 0; k < 3; k++)
+            if (B.fixed[k]) B.vel_t0[k] = 0;
+        for (int k = 0; k < 6; k++) B.pose_t0[k] = x[6 * b + k];
+    }
+    kappa = pr.kappa;
+}
+
+} // namespace orc

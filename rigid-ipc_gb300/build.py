@@ -31,6 +31,7 @@ UNITS = {
     "noalloc.cu": ["--fmad=false"],
     "body.cu": ["--fmad=true"],
     "friction.cu": ["--fmad=true"],
+    "step.cu": ["--fmad=false"],
 }
 
 

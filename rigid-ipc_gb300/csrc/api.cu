@@ -13,6 +13,8 @@ int construct_constraints(Ctx& c, const double* x, double dhat, double dmin);
 int launch_barrier_local(Ctx& c, const double* x, double dhat, double dmin, int flags,
                          double* energy, double* grad, double* blocks, double* hess);
 int assemble_barrier(Ctx& c, bool with_hess);
+int scene_sums(Ctx& c, const double* val, const int* bodies, int64_t n, const int64_t seg[4],
+               std::vector<double>& out);
 int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flags,
             double* toi_host, double* per);
 int compute_world_vertices_rn(Ctx& c, const double* x, double* V, DevBuf& rotbuf);
@@ -23,6 +25,10 @@ int friction_setup(Ctx& c, const double* x0, double dhat, double kappa, double m
 int launch_friction_local(Ctx& c, const double* x, double epsvh, int flags, double* energy,
                           double* grad, double* blocks, double* hess);
 int friction_term(Ctx& c, const double* x, double epsvh, int flags, rigc_barrier_out* out);
+int sim_init(Ctx& c, const rigc_sim_params& p, const rigc_sim_state& s);
+int sim_step(Ctx& c, rigc_step_stats* stats);
+int sim_get_state(Ctx& c, double* poses, double* velocities, double* Qdot, double* kappa);
+void sim_release(Ctx& c);
 
 static thread_local std::string g_last_error;
 static std::atomic<int64_t> g_launches { 0 };
@@ -31,13 +37,62 @@ void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 int64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 // broad phase, then record the candidate counts (also on an early exit)
-static int detect_and_count(Ctx& c, const double* x0, const double* x1, bool continuous,
-                            double infl)
+int detect_and_count(Ctx& c, const double* x0, const double* x1, bool continuous,
+                     double infl)
 {
     int st = detect_candidates(c, x0, x1, continuous, infl);
     c.stats.cand_ee = c.cand.num_ee;
     c.stats.cand_fv = c.cand.num_fv;
     return st;
+}
+
+int barrier_term_impl(Ctx& c, const double* x, double dhat, double dmin, int flags,
+                      rigc_barrier_out* out)
+{
+    const int64_t n = c.cons.num;
+    const bool g = (flags & (RIGC_GRAD | RIGC_HESS)) != 0, h = (flags & RIGC_HESS) != 0;
+    RIGC_TRY(c.c_energy.reserve((size_t)n * 8 + 8));
+    if (g) RIGC_TRY(c.c_grad.reserve((size_t)n * 96 + 8));
+    if (h) RIGC_TRY(c.c_blocks.reserve((size_t)n * 144 * 8 + 8));
+    RIGC_TRY(launch_barrier_local(c, x, dhat, dmin, flags, c.c_energy.as<double>(),
+                                  g ? c.c_grad.as<double>() : nullptr,
+                                  h ? c.c_blocks.as<double>() : nullptr, nullptr));
+    double* e_dev = reinterpret_cast<double*>(c.d_scalars.as<char>() + 2048);
+    if (n > 0) {
+        RIGC_TRY(sum_f64(c.c_energy.as<double>(), n, e_dev, c.scratch[6], c.stream));
+    } else {
+        RIGC_CUDA(cudaMemsetAsync(e_dev, 0, sizeof(double), c.stream));
+    }
+    if (g) {
+        RIGC_TRY(assemble_barrier(c, h));
+    }
+    RIGC_CUDA(cudaMemcpyAsync(c.h_scalars, e_dev, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    if (h && n > 0)
+        RIGC_CUDA(cudaMemcpyAsync(c.h_scalars + 1, c.d_scalars.as<int32_t>() + 1, sizeof(int32_t),
+                                  cudaMemcpyDeviceToHost, c.stream));
+    RIGC_CUDA(cudaStreamSynchronize(c.stream));
+    if (h && n > 0) {
+        int32_t nn;
+        std::memcpy(&nn, c.h_scalars + 1, sizeof(int32_t));
+        c.nnzb = nn;
+    }
+    if (c.s.nscenes > 1) {
+        const int64_t seg[4] = { 0, c.cons.num_vv, c.cons.num_vv + c.cons.num_ev,
+                                 c.cons.num_vv + c.cons.num_ev + c.cons.num_ee };
+        RIGC_TRY(scene_sums(c, c.c_energy.as<double>(), c.cons.bodies.as<int>(), n, seg,
+                            c.h_scene_energy));
+    } else {
+        c.h_scene_energy.assign(1, c.h_scalars[0]);
+    }
+    if (out) {
+        out->energy = c.h_scalars[0];
+        out->nnzb = h ? c.nnzb : 0;
+        out->grad = g ? c.grad.as<double>() : nullptr;
+        out->row_ptr = h ? c.row_ptr.as<int32_t>() : nullptr;
+        out->col = h ? c.col.as<int32_t>() : nullptr;
+        out->val = h ? c.val.as<double>() : nullptr;
+    }
+    return RIGC_OK;
 }
 
 void set_error(int code, const char* what, const char* file, int line)
@@ -63,7 +118,8 @@ template <class T> static int upload(T*& dst, const T* src, size_t n)
 static void free_scene(Scene& s)
 {
     void* ptrs[] = { s.rest, s.edges, s.faces, s.f2e, s.bvs, s.bes, s.bfs, s.group,
-                     s.type, s.rmax, s.vbody, s.ebody, s.fbody, s.edge_len };
+                     s.type, s.rmax, s.vbody, s.ebody, s.fbody, s.edge_len, s.bscene,
+                     s.scene_bstart };
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -80,9 +136,10 @@ static void release_all(Ctx* c)
                        &c->frame_vals, &c->fric.type, &c->fric.verts, &c->fric.bodies,
                        &c->fric.coef, &c->fric.v0c, &c->fric.V0, &c->fric.c_energy,
                        &c->fric.c_grad, &c->fric.c_blocks, &c->fric.grad, &c->fric.row_ptr,
-                       &c->fric.col, &c->fric.val };
+                       &c->fric.col, &c->fric.val, &c->scene_toi, &c->scene_energy };
     for (DevBuf* b : bufs) b->release();
     for (auto& b : c->scratch) b.release();
+    sim_release(*c);
     if (c->h_scalars) cudaFreeHost(c->h_scalars);
     c->h_scalars = nullptr;
     free_scene(c->s);
@@ -109,7 +166,26 @@ const char* rigc_status_string(int status)
     }
 }
 
+static int ctx_create(const rigc_scene_desc* d, int num_scenes, const int32_t* body_scene,
+                      rigc_ctx** out);
+
 int rigc_ctx_create(const rigc_scene_desc* d, rigc_ctx** out)
+{
+    return ctx_create(d, 1, nullptr, out);
+}
+
+int rigc_ctx_create_batched(const rigc_scene_desc* d, int32_t num_scenes,
+                            const int32_t* body_scene, rigc_ctx** out)
+{
+    if (!d || !out || num_scenes < 1 || (d->num_bodies > 0 && !body_scene)) return RIGC_ERR_ARG;
+    for (int b = 0; b < d->num_bodies; b++)
+        if (body_scene[b] < 0 || body_scene[b] >= num_scenes || (b && body_scene[b] < body_scene[b - 1]))
+            return RIGC_ERR_ARG;
+    return ctx_create(d, num_scenes, body_scene, out);
+}
+
+static int ctx_create(const rigc_scene_desc* d, int num_scenes, const int32_t* body_scene,
+                      rigc_ctx** out)
 {
     if (!d || !out) return RIGC_ERR_ARG;
     *out = nullptr;
@@ -184,6 +260,19 @@ int rigc_ctx_create(const rigc_scene_desc* d, rigc_ctx** out)
     chk(upload(s.ebody, ebody.data(), (size_t)ne));
     chk(upload(s.fbody, fbody.data(), (size_t)nf));
     chk(upload(s.edge_len, elen.data(), (size_t)ne));
+    // scenes (one unless batched): scene of each body and first body of each
+    std::vector<int> bscene(nb, 0), sstart(num_scenes + 1, nb);
+    for (int b = nb - 1; b >= 0; b--) {
+        bscene[b] = body_scene ? body_scene[b] : 0;
+        sstart[bscene[b]] = b;
+    }
+    for (int k = num_scenes - 1; k >= 0; k--) sstart[k] = std::min(sstart[k], sstart[k + 1]);
+    s.nscenes = num_scenes;
+    s.h_scene_bstart = sstart;
+    s.h_bes.assign(d->body_edge_start, d->body_edge_start + nb + 1);
+    s.h_bfs.assign(d->body_face_start, d->body_face_start + nb + 1);
+    chk(upload(s.bscene, bscene.data(), (size_t)nb));
+    chk(upload(s.scene_bstart, sstart.data(), (size_t)num_scenes + 1));
     chk(c->d_scalars.reserve(4096));
     if (st == RIGC_OK) {
         cudaError_t e = cudaMallocHost(&c->h_scalars, 4096);
@@ -277,6 +366,29 @@ int rigc_set_candidates(rigc_ctx* ctx, int64_t num_ee, const int32_t* ee, int64_
     c.cand.num_fv = num_fv;
     c.stats.cand_ee = num_ee;
     c.stats.cand_fv = num_fv;
+    return RIGC_OK;
+}
+
+int rigc_num_scenes(const rigc_ctx* ctx)
+{
+    return ctx ? reinterpret_cast<const Ctx*>(ctx)->s.nscenes : 0;
+}
+
+int rigc_scene_tois(rigc_ctx* ctx, double* toi_host)
+{
+    if (!ctx || !toi_host) return RIGC_ERR_ARG;
+    Ctx& c = *ctx_of(ctx);
+    for (int k = 0; k < c.s.nscenes; k++)
+        toi_host[k] = k < (int)c.h_scene_toi.size() ? c.h_scene_toi[k] : INFINITY;
+    return RIGC_OK;
+}
+
+int rigc_scene_barrier_energies(rigc_ctx* ctx, double* energy_host)
+{
+    if (!ctx || !energy_host) return RIGC_ERR_ARG;
+    Ctx& c = *ctx_of(ctx);
+    for (int k = 0; k < c.s.nscenes; k++)
+        energy_host[k] = k < (int)c.h_scene_energy.size() ? c.h_scene_energy[k] : 0.0;
     return RIGC_OK;
 }
 
@@ -374,47 +486,6 @@ int rigc_set_constraints(rigc_ctx* ctx, int64_t num, const int32_t* type, const 
     return RIGC_OK;
 }
 
-static int barrier_term_impl(Ctx& c, const double* x, double dhat, double dmin, int flags,
-                             rigc_barrier_out* out)
-{
-    const int64_t n = c.cons.num;
-    const bool g = (flags & (RIGC_GRAD | RIGC_HESS)) != 0, h = (flags & RIGC_HESS) != 0;
-    RIGC_TRY(c.c_energy.reserve((size_t)n * 8 + 8));
-    if (g) RIGC_TRY(c.c_grad.reserve((size_t)n * 96 + 8));
-    if (h) RIGC_TRY(c.c_blocks.reserve((size_t)n * 144 * 8 + 8));
-    RIGC_TRY(launch_barrier_local(c, x, dhat, dmin, flags, c.c_energy.as<double>(),
-                                  g ? c.c_grad.as<double>() : nullptr,
-                                  h ? c.c_blocks.as<double>() : nullptr, nullptr));
-    double* e_dev = reinterpret_cast<double*>(c.d_scalars.as<char>() + 2048);
-    if (n > 0) {
-        RIGC_TRY(sum_f64(c.c_energy.as<double>(), n, e_dev, c.scratch[6], c.stream));
-    } else {
-        RIGC_CUDA(cudaMemsetAsync(e_dev, 0, sizeof(double), c.stream));
-    }
-    if (g) {
-        RIGC_TRY(assemble_barrier(c, h));
-    }
-    RIGC_CUDA(cudaMemcpyAsync(c.h_scalars, e_dev, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
-    if (h && n > 0)
-        RIGC_CUDA(cudaMemcpyAsync(c.h_scalars + 1, c.d_scalars.as<int32_t>() + 1, sizeof(int32_t),
-                                  cudaMemcpyDeviceToHost, c.stream));
-    RIGC_CUDA(cudaStreamSynchronize(c.stream));
-    if (h && n > 0) {
-        int32_t nn;
-        std::memcpy(&nn, c.h_scalars + 1, sizeof(int32_t));
-        c.nnzb = nn;
-    }
-    if (out) {
-        out->energy = c.h_scalars[0];
-        out->nnzb = h ? c.nnzb : 0;
-        out->grad = g ? c.grad.as<double>() : nullptr;
-        out->row_ptr = h ? c.row_ptr.as<int32_t>() : nullptr;
-        out->col = h ? c.col.as<int32_t>() : nullptr;
-        out->val = h ? c.val.as<double>() : nullptr;
-    }
-    return RIGC_OK;
-}
-
 int rigc_barrier_term(rigc_ctx* ctx, const double* x, double dhat, double dmin, int flags,
                       rigc_barrier_out* out)
 {
@@ -482,6 +553,37 @@ int rigc_friction_local_terms(rigc_ctx* ctx, const double* x, double epsv_times_
     RIGC_TRY(launch_friction_local(c, x, epsv_times_h, flags, energy, grad, nullptr, hess));
     RIGC_CUDA(cudaStreamSynchronize(c.stream));
     return RIGC_OK;
+}
+
+int rigc_sim_init(rigc_ctx* ctx, const rigc_sim_params* params, const rigc_sim_state* state)
+{
+    if (!ctx || !params || !state || !state->mass || !state->moment || !state->dof_fixed
+        || !state->poses || !state->velocities || !state->Qdot)
+        return RIGC_ERR_ARG;
+    const rigc_sim_params& p = *params;
+    if (!(p.timestep > 0) || !(p.dhat > 0) || !(p.dmin >= 0) || !(p.average_mass > 0)
+        || !(p.world_bbox_diagonal > 0) || p.max_newton_iterations < 1)
+        return RIGC_ERR_ARG;
+    Ctx& c = *ctx_of(ctx);
+    for (int i = 0; i < 6 * c.s.nb; i++)
+        if (!std::isfinite(state->poses[i]) || !std::isfinite(state->velocities[i])) return RIGC_ERR_NAN;
+    return sim_init(c, p, *state);
+}
+
+int rigc_sim_step(rigc_ctx* ctx, int32_t num_steps, rigc_step_stats* stats)
+{
+    if (!ctx || num_steps < 0) return RIGC_ERR_ARG;
+    Ctx& c = *ctx_of(ctx);
+    if (stats) *stats = rigc_step_stats {};
+    for (int32_t k = 0; k < num_steps; k++) RIGC_TRY(sim_step(c, stats));
+    return RIGC_OK;
+}
+
+int rigc_sim_get_state(rigc_ctx* ctx, double* poses, double* velocities, double* Qdot,
+                       double* barrier_stiffness)
+{
+    if (!ctx) return RIGC_ERR_ARG;
+    return sim_get_state(*ctx_of(ctx), poses, velocities, Qdot, barrier_stiffness);
 }
 
 int rigc_narrow_phase_host(rigc_ctx* ctx, const double* x0_host, const double* x1_host,

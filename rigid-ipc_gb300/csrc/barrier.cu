@@ -631,6 +631,49 @@ int assemble_terms(Ctx& c, const int* bodies, int64_t n, const double* cgrad,
     return RIGC_OK;
 }
 
+// Per-scene sums of per-constraint values in constraint order.  Within each
+// type segment the constraints are ordered by their first primitive, hence
+// by body and by scene; each thread binary-searches its scene's range in the
+// four segments.
+__global__ void k_scene_sums(const double* __restrict__ val, const int* __restrict__ bodies,
+                             const int* __restrict__ bscene, int4 seg_start, int64_t n,
+                             int nscenes, double* __restrict__ out)
+{
+    int sc = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sc >= nscenes) return;
+    const int64_t starts[5] = { seg_start.x, seg_start.y, seg_start.z, seg_start.w, n };
+    double acc = 0;
+    for (int t = 0; t < 4; t++) {
+        int64_t lo = starts[t], hi = starts[t + 1];
+        // first constraint of the segment with scene >= sc
+        int64_t a = lo, b = hi;
+        while (a < b) {
+            int64_t m = (a + b) / 2;
+            if (bscene[bodies[2 * m]] < sc) a = m + 1;
+            else b = m;
+        }
+        for (int64_t i = a; i < hi && bscene[bodies[2 * i]] == sc; i++) acc += val[i];
+    }
+    out[sc] = acc;
+}
+
+int scene_sums(Ctx& c, const double* val, const int* bodies, int64_t n, const int64_t seg[4],
+               std::vector<double>& out)
+{
+    const int ns = c.s.nscenes;
+    out.assign(ns, 0.0);
+    if (n == 0) return RIGC_OK;
+    RIGC_TRY(c.scene_energy.reserve((size_t)ns * 8 + 8));
+    int4 st4 = make_int4((int)seg[0], (int)seg[1], (int)seg[2], (int)seg[3]);
+    RIGC_COUNT_LAUNCH();
+    k_scene_sums<<<grid_for(ns, 128), 128, 0, c.stream>>>(val, bodies, c.s.bscene, st4, n, ns,
+                                                          c.scene_energy.as<double>());
+    RIGC_CUDA(cudaMemcpyAsync(out.data(), c.scene_energy.ptr, (size_t)ns * 8, cudaMemcpyDeviceToHost,
+                              c.stream));
+    RIGC_CUDA(cudaStreamSynchronize(c.stream));
+    return RIGC_OK;
+}
+
 int assemble_barrier(Ctx& c, bool with_hess)
 {
     // on the device (d_scalars int 1) until the caller syncs

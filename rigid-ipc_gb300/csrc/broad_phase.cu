@@ -82,21 +82,29 @@ __global__ void k_body_boxes(const double* __restrict__ x0, const double* __rest
         }
 }
 
-__global__ void k_close_bodies(const double* __restrict__ box, const int* __restrict__ group, int nb,
-                               double infl, int* __restrict__ body_in)
+// body pairs of one scene whose inflated boxes overlap (different groups):
+// one thread per (body, later body of the same scene)
+__global__ void k_close_bodies(const double* __restrict__ box, const int* __restrict__ group,
+                               const int* __restrict__ bscene, const int* __restrict__ scene_bstart,
+                               int nb, int chunk, double infl, int* __restrict__ body_in)
 {
     int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    int64_t npairs = (int64_t)nb * nb;
-    if (t >= npairs) return;
-    int i = (int)(t / nb), j = (int)(t % nb);
-    if (j <= i || group[i] == group[j]) return;
-    for (int k = 0; k < 3; k++) {
-        double li = RSUB(box[6 * i + k], infl), hi_i = RADD(box[6 * i + 3 + k], infl);
-        double lj = RSUB(box[6 * j + k], infl), hj = RADD(box[6 * j + 3 + k], infl);
-        if (li > hj || lj > hi_i) return;
+    const int i = (int)(t / chunk);
+    if (i >= nb) return;
+    const int end = scene_bstart[bscene[i] + 1];
+    for (int j = i + 1 + (int)(t % chunk); j < end; j += chunk) {
+        if (group[i] == group[j]) continue;
+        bool overlap = true;
+        for (int k = 0; k < 3; k++) {
+            double li = RSUB(box[6 * i + k], infl), hi_i = RADD(box[6 * i + 3 + k], infl);
+            double lj = RSUB(box[6 * j + k], infl), hj = RADD(box[6 * j + 3 + k], infl);
+            if (li > hj || lj > hi_i) overlap = false;
+        }
+        if (overlap) {
+            body_in[i] = 1;
+            body_in[j] = 1;
+        }
     }
-    body_in[i] = 1;
-    body_in[j] = 1;
 }
 
 // scene box over included bodies (unpadded box of compute_bounding_box)
@@ -407,20 +415,37 @@ __global__ void k_count_cells(const uint32_t* __restrict__ elems, int m, const d
     large_flag[i] = large ? 1 : 0;
 }
 
+// scene of an element (tag: type << 30 | index)
+struct ElemScene {
+    const int* vbody;
+    const int* ebody;
+    const int* fbody;
+    const int* bscene;
+    __device__ __forceinline__ uint64_t of(uint32_t tag) const
+    {
+        const int t = tag >> 30, i = tag & 0x3fffffff;
+        const int b = t == 0 ? vbody[i] : (t == 1 ? ebody[i] : fbody[i]);
+        return (uint64_t)bscene[b];
+    }
+};
+
+// (scene, cell) keys: elements of different scenes never share a key
 __global__ void k_emit_items(const uint32_t* __restrict__ elems, int m, const double* __restrict__ vb,
                              const double* __restrict__ eb, const double* __restrict__ fb, Grid g,
-                             const int32_t* __restrict__ cnt, const int32_t* __restrict__ off,
-                             uint64_t* __restrict__ keys, uint32_t* __restrict__ vals)
+                             ElemScene es, uint64_t ncells, const int32_t* __restrict__ cnt,
+                             const int32_t* __restrict__ off, uint64_t* __restrict__ keys,
+                             uint32_t* __restrict__ vals)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m || cnt[i] == 0) return;
     long long c0[3], c1[3];
     cell_range(elem_box(elems[i], vb, eb, fb), g, c0, c1);
+    const uint64_t base = es.of(elems[i]) * ncells;
     int o = off[i];
     for (long long z = c0[2]; z <= c1[2]; z++)
         for (long long y = c0[1]; y <= c1[1]; y++)
             for (long long x = c0[0]; x <= c1[0]; x++) {
-                keys[o] = (uint64_t)((z * g.dims[1] + y) * g.dims[0] + x);
+                keys[o] = base + (uint64_t)((z * g.dims[1] + y) * g.dims[0] + x);
                 vals[o] = elems[i];
                 o++;
             }
@@ -489,7 +514,7 @@ __device__ __forceinline__ bool pair_filter(const PairCtx& P, uint32_t a, uint32
 // one thread per sorted item: pairs with later items of the same cell,
 // reported only in the first cell both elements cover
 __global__ void k_cell_pairs(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ vals,
-                             int64_t m, PairCtx P, Grid g, PairOut o)
+                             int64_t m, PairCtx P, Grid g, ElemScene es, uint64_t ncells, PairOut o)
 {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m) return;
@@ -511,28 +536,63 @@ __global__ void k_cell_pairs(const uint64_t* __restrict__ keys, const uint32_t* 
         long long b0[3], b1[3];
         cell_range(elem_box(b, P.vb, P.eb, P.fb), g, b0, b1);
         long long fx = max(a0[0], b0[0]), fy = max(a0[1], b0[1]), fz = max(a0[2], b0[2]);
-        uint64_t first = (uint64_t)((fz * g.dims[1] + fy) * g.dims[0] + fx);
+        uint64_t first = es.of(a) * ncells + (uint64_t)((fz * g.dims[1] + fy) * g.dims[0] + fx);
         if (first != key) continue;
         push_pair(o, is_ee, pk);
     }
 }
 
-// large elements against every included element of the matching type
-__global__ void k_large_pairs(const uint32_t* __restrict__ large, int nl,
+// large elements against every included element of the matching type in
+// their scene: grid row y = large element, its blocks stride over the range;
+// range[s * 3 + t] is the first
+// position in elems of scene s's type-t elements (vertices, edges, faces;
+// elems is ordered by type, then by element index, hence by scene)
+__global__ void k_large_pairs(const uint32_t* __restrict__ large, int nl, int row0,
                               const uint32_t* __restrict__ elems, const int32_t* __restrict__ is_large,
-                              int m, PairCtx P, PairOut o)
+                              const int32_t* __restrict__ range, int nscenes, ElemScene es, PairCtx P,
+                              PairOut o)
 {
-    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (int64_t)nl * m) return;
-    int li = (int)(t / m), ei = (int)(t % m);
-    uint32_t a = large[li], b = elems[ei];
-    int ta = a >> 30, tb = b >> 30;
-    if (!((ta == 1 && tb == 1) || (ta + tb == 2 && ta != tb))) return;
-    // a pair of two large elements is reported by the one with the smaller tag
-    if (is_large[ei] && b < a) return;
-    bool is_ee;
-    unsigned long long pk;
-    if (pair_filter(P, a, b, is_ee, pk)) push_pair(o, is_ee, pk);
+    const int li = row0 + blockIdx.y;
+    if (li >= nl) return;
+    const uint32_t a = large[li];
+    const int ta = a >> 30;
+    const int s = (int)es.of(a);
+    // edges meet edges, faces meet vertices (and vertices faces)
+    const int tb = ta == 1 ? 1 : (ta == 2 ? 0 : 2);
+    const int lo = range[3 * s + tb];
+    const int hi = range[3 * (s + 1) + tb];
+    for (int ei = lo + blockIdx.x * blockDim.x + threadIdx.x; ei < hi; ei += gridDim.x * blockDim.x) {
+        const uint32_t b = elems[ei];
+        // a pair of two large elements is reported by the one with the smaller tag
+        if (is_large[ei] && b < a) continue;
+        bool is_ee;
+        unsigned long long pk;
+        if (pair_filter(P, a, b, is_ee, pk)) push_pair(o, is_ee, pk);
+    }
+}
+
+// positions in elems of each scene's first vertex, edge and face (from the
+// exclusive scan of the inclusion flags over all elements); row nscenes
+// holds the end of each type
+__global__ void k_scene_ranges(const int32_t* __restrict__ pos, const int* __restrict__ scene_bstart,
+                               const int* __restrict__ bvs, const int* __restrict__ bes,
+                               const int* __restrict__ bfs, int nscenes, int nv, int ne, int nf,
+                               int m, int32_t* __restrict__ range)
+{
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s > nscenes) return;
+    const int ntot = nv + ne + nf;
+    auto at = [&](int idx) { return idx < ntot ? pos[idx] : m; };
+    if (s == nscenes) {
+        range[3 * s] = at(nv);
+        range[3 * s + 1] = at(nv + ne);
+        range[3 * s + 2] = m;
+        return;
+    }
+    const int b = scene_bstart[s];
+    range[3 * s] = at(bvs[b]);
+    range[3 * s + 1] = at(nv + bes[b]);
+    range[3 * s + 2] = at(nv + ne + bfs[b]);
 }
 
 __global__ void k_large_list(const uint32_t* __restrict__ elems, const int32_t* __restrict__ flag,
@@ -579,9 +639,17 @@ int detect_candidates(Ctx& c, const double* x0, const double* x1, bool continuou
     k_body_boxes<<<grid_for((int64_t)s.nb * 32, 128), 128, 0, st>>>(
         x0, x1, s.rest, s.bvs, s.type, s.rmax, s.nb, c.body_box.as<double>());
     RIGC_CUDA(cudaMemsetAsync(c.body_in.ptr, 0, (size_t)s.nb * sizeof(int), st));
-    RIGC_COUNT_LAUNCH();
-    k_close_bodies<<<grid_for((int64_t)s.nb * s.nb, 256), 256, 0, st>>>(
-        c.body_box.as<double>(), s.group, s.nb, infl, c.body_in.as<int>());
+    {
+        // threads per body: enough to cover the largest scene's pairs
+        int maxs = 1;
+        for (int k = 0; k < s.nscenes; k++)
+            maxs = std::max(maxs, s.h_scene_bstart[k + 1] - s.h_scene_bstart[k]);
+        const int chunk = std::min(256, maxs);
+        RIGC_COUNT_LAUNCH();
+        k_close_bodies<<<grid_for((int64_t)s.nb * chunk, 256), 256, 0, st>>>(
+            c.body_box.as<double>(), s.group, s.bscene, s.scene_bstart, s.nb, chunk, infl,
+            c.body_in.as<int>());
+    }
     std::vector<int> h_in(s.nb);
     RIGC_CUDA(cudaMemcpyAsync(h_in.data(), c.body_in.ptr, (size_t)s.nb * sizeof(int),
                               cudaMemcpyDeviceToHost, st));
@@ -686,6 +754,13 @@ int detect_candidates(Ctx& c, const double* x0, const double* x1, bool continuou
     g.cell = cell;
     g.grow = 1e-9 * cell;
     uint64_t ncells = (uint64_t)g.dims[0] * g.dims[1] * g.dims[2];
+    const ElemScene es { s.vbody, s.ebody, s.fbody, s.bscene };
+    // positions of each scene's elements in elems, per type
+    RIGC_TRY(c.seg.reserve((size_t)(3 * (s.nscenes + 1) + 8) * sizeof(int32_t)));
+    int32_t* srange = c.seg.as<int32_t>();
+    RIGC_COUNT_LAUNCH();
+    k_scene_ranges<<<grid_for(s.nscenes + 1, 128), 128, 0, st>>>(
+        pos, s.scene_bstart, s.bvs, s.bes, s.bfs, s.nscenes, s.nv, s.ne, s.nf, m, srange);
     // ---- 4. items
     RIGC_TRY(S[3].reserve((size_t)(3 * m + 16) * sizeof(int32_t)));
     int32_t* icnt = S[3].as<int32_t>();
@@ -711,11 +786,12 @@ int detect_candidates(Ctx& c, const double* x0, const double* x1, bool continuou
     RIGC_TRY(c.items_val2.reserve((size_t)nitems * 4 + 8));
     RIGC_COUNT_LAUNCH();
     k_emit_items<<<grid_for(m, 256), 256, 0, st>>>(elems, m, c.vbox.as<double>(), c.ebox.as<double>(),
-                                                  c.fbox.as<double>(), g, icnt, ioff,
+                                                  c.fbox.as<double>(), g, es, ncells, icnt, ioff,
                                                   c.items_key.as<uint64_t>(), c.items_val.as<uint32_t>());
     RIGC_TRY(radix_sort_pairs<uint64_t>(c.items_key.as<uint64_t>(), c.items_val.as<uint32_t>(),
                                         c.items_key2.as<uint64_t>(), c.items_val2.as<uint32_t>(),
-                                        nitems, bits_for(ncells), S[4], S[5], S[7], st));
+                                        nitems, bits_for(ncells * (uint64_t)s.nscenes - 1), S[4],
+                                        S[5], S[7], st));
     RIGC_TRY(c.large_list.reserve((size_t)(nlarge + 1) * sizeof(uint32_t)));
     RIGC_COUNT_LAUNCH();
     k_large_list<<<grid_for(m, 256), 256, 0, st>>>(elems, lflag, lpos, m, c.large_list.as<uint32_t>());
@@ -733,12 +809,19 @@ int detect_candidates(Ctx& c, const double* x0, const double* x1, bool continuou
         if (nitems > 0) {
             RIGC_COUNT_LAUNCH();
             k_cell_pairs<<<grid_for(nitems, 128), 128, 0, st>>>(c.items_key2.as<uint64_t>(),
-                                                              c.items_val2.as<uint32_t>(), nitems, P, g, o);
+                                                              c.items_val2.as<uint32_t>(), nitems, P, g,
+                                                              es, ncells, o);
         }
         if (nlarge > 0) {
-            RIGC_COUNT_LAUNCH();
-            k_large_pairs<<<grid_for((int64_t)nlarge * m, 256), 256, 0, st>>>(
-                c.large_list.as<uint32_t>(), nlarge, elems, lflag, m, P, o);
+            // enough blocks per large element to cover a whole scene's elements
+            const unsigned bx = (unsigned)std::min<int64_t>(
+                1024, std::max<int64_t>(1, ((int64_t)m / s.nscenes + 255) / 256));
+            for (int row0 = 0; row0 < nlarge; row0 += 65535) {
+                const unsigned rows = (unsigned)std::min(65535, nlarge - row0);
+                RIGC_COUNT_LAUNCH();
+                k_large_pairs<<<dim3(bx, rows), 256, 0, st>>>(c.large_list.as<uint32_t>(), nlarge, row0,
+                                                            elems, lflag, srange, s.nscenes, es, P, o);
+            }
         }
         RIGC_CUDA(cudaGetLastError());
         unsigned long long hn[2];

@@ -63,6 +63,8 @@ struct CCDArgs {
     int prune;
     long long max_boxes;
     unsigned long long* gmin;   // running minimum time of impact (double bits)
+    unsigned long long* scene_gmin;  // batched contexts: the same per scene, else null
+    const int* bscene;          // scene of each body
     double* per;                // optional per-candidate result
     int* status;                // worst status
     unsigned long long* boxes;  // total boxes evaluated
@@ -524,9 +526,22 @@ __device__ __forceinline__ bool le_nn(double a, double b)
     return dbits(a) <= dbits(b);
 }
 
-__device__ __forceinline__ double load_gmin(const CCDArgs& a)
+// running minimum of the candidate's scene (the whole context unless batched)
+__device__ __forceinline__ unsigned long long* gmin_of(const CCDArgs& a, const Query& q)
 {
-    return __longlong_as_double((long long)*(volatile unsigned long long*)a.gmin);
+    return a.scene_gmin ? a.scene_gmin + a.bscene[q.body_a] : a.gmin;
+}
+
+__device__ __forceinline__ double load_gmin(const CCDArgs& a, const Query& q)
+{
+    return __longlong_as_double((long long)*(volatile unsigned long long*)gmin_of(a, q));
+}
+
+__device__ __forceinline__ void record_min(const CCDArgs& a, const Query& q, double t)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(t);
+    if (a.scene_gmin) atomicMin(gmin_of(a, q), b);
+    atomicMin(a.gmin, b);
 }
 
 // Persistent kernel: each lane takes the next unprocessed candidate from a
@@ -540,8 +555,8 @@ k_ccd(CCDArgs a)
     unsigned long long tot_boxes = 0, tot_hits = 0, pops = 0;
     Query q;
     double tol[3] = { 0, 0, 0 };
-    Box stack[kCCDStack];
-    int sp = 0;
+    Box stack[kCCDStack];  // boxes stack[sb .. sp): pop at sp, shared from sb
+    int sp = 0, sb = 0;
     int64_t cur = -1;
     double earliest = INFINITY;
     bool found = false;
@@ -554,6 +569,7 @@ k_ccd(CCDArgs a)
     bool pend = false;
     int req_side = 0, req_body = 0;
     unsigned long long req_node = 0;
+    const int lane = threadIdx.x & 31;
     while (true) {
         // frames asked for in the last iteration, computed by the whole warp
         const unsigned req = __ballot_sync(0xffffffffu, pend);
@@ -561,14 +577,63 @@ k_ccd(CCDArgs a)
             warp_compute_frames(a, own, req, req_side, req_body, req_node);
             pend = false;
         }
+        // Once the candidate list is exhausted, a lane with nothing left takes
+        // the bottom (largest) box of the fullest stack in its warp together
+        // with its candidate.  Prune mode only: split searches find the same
+        // earliest time of impact, but a search stopped by the box budget
+        // would not report what one search reports.
+        if (a.prune) {
+            const unsigned idle = __ballot_sync(0xffffffffu, done);
+            if (idle) {
+                int best = done ? 0 : sp - sb - 1, bl = lane;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    const int ob = __shfl_xor_sync(0xffffffffu, best, o);
+                    const int ol = __shfl_xor_sync(0xffffffffu, bl, o);
+                    if (ob > best || (ob == best && ol < bl)) {
+                        best = ob;
+                        bl = ol;
+                    }
+                }
+                if (best >= 1) {
+                    const int thief = __ffs(idle) - 1;
+                    Box g = stack[sb < sp ? sb : 0];
+                    if (lane == bl) sb++;
+                    const double e = __shfl_sync(0xffffffffu, earliest, bl);
+                    const long long c = __shfl_sync(0xffffffffu, (long long)cur, bl);
+                    g.t0 = __shfl_sync(0xffffffffu, g.t0, bl);
+                    g.t1 = __shfl_sync(0xffffffffu, g.t1, bl);
+                    g.a0 = __shfl_sync(0xffffffffu, g.a0, bl);
+                    g.a1 = __shfl_sync(0xffffffffu, g.a1, bl);
+                    g.b0 = __shfl_sync(0xffffffffu, g.b0, bl);
+                    g.b1 = __shfl_sync(0xffffffffu, g.b1, bl);
+                    if (lane == thief) {
+                        cur = c;
+                        load_candidate(a, cur, q);
+                        tol[0] = a.ctol[3 * cur];
+                        tol[1] = a.ctol[3 * cur + 1];
+                        tol[2] = a.ctol[3 * cur + 2];
+                        gbound = load_gmin(a, q);
+                        earliest = e;
+                        found = false;
+                        status = RIGC_OK;
+                        cboxes = 0;
+                        sb = 0;
+                        sp = 0;
+                        stack[sp++] = g;
+                        done = false;
+                    }
+                }
+            }
+        }
         bool have = false;
         Box x;
         if (!done) {
-            while (sp > 0) {
+            while (sp > sb) {
                 x = stack[--sp];
                 if (le_nn(earliest, x.t0)) continue;
                 if (a.prune) {
-                    if ((++pops & 7) == 0) gbound = load_gmin(a);
+                    if ((++pops & 7) == 0) gbound = load_gmin(a, q);
                     if (le_nn(gbound, x.t0)) continue;
                 }
                 if (q.fv) {
@@ -582,10 +647,12 @@ k_ccd(CCDArgs a)
                 if (cur >= 0) {
                     double toi = found ? earliest : INFINITY;
                     if (found) {
-                        atomicMin(a.gmin, (unsigned long long)__double_as_longlong(toi));
+                        record_min(a, q, toi);
                         tot_hits++;
                     }
-                    if (a.per) a.per[cur] = toi;
+                    if (a.per && found)
+                        atomicMin(reinterpret_cast<unsigned long long*>(a.per) + cur,
+                                  (unsigned long long)__double_as_longlong(toi));
                     if (status != RIGC_OK) atomicMax(a.status, status);
                 }
                 cur = (int64_t)atomicAdd(a.next, 1ull);
@@ -596,11 +663,12 @@ k_ccd(CCDArgs a)
                     tol[0] = a.ctol[3 * cur];
                     tol[1] = a.ctol[3 * cur + 1];
                     tol[2] = a.ctol[3 * cur + 2];
-                    if (a.prune) gbound = load_gmin(a);
+                    if (a.prune) gbound = load_gmin(a, q);
                     earliest = INFINITY;
                     found = false;
                     status = RIGC_OK;
                     cboxes = 0;
+                    sb = sp = 0;
                     x = Box { 0.0, 1.0, 0.0, 1.0, 0.0, 1.0 };
                     have = !(a.prune && le_nn(gbound, x.t0));
                 }
@@ -612,11 +680,11 @@ k_ccd(CCDArgs a)
         if (cboxes >= (unsigned long long)a.max_boxes) {
             // budget exhausted: the earliest unexplored t.lo is conservative
             double m = x.t0;
-            for (int s = 0; s < sp; s++) m = smin(m, stack[s].t0);
+            for (int s = sb; s < sp; s++) m = smin(m, stack[s].t0);
             earliest = smin(earliest, m);
             found = true;
             status = RIGC_ERR_ITER_LIMIT;
-            sp = 0;
+            sp = sb = 0;
             continue;
         }
         if (!(dbits(x.t0) == dbits(q.ct0) && dbits(x.t1) == dbits(q.ct1))) {
@@ -641,7 +709,7 @@ k_ccd(CCDArgs a)
             earliest = x.t0;
             found = true;
             if (a.prune) {
-                atomicMin(a.gmin, (unsigned long long)__double_as_longlong(earliest));
+                record_min(a, q, earliest);
                 gbound = smin(gbound, earliest);
             }
             continue;
@@ -666,6 +734,11 @@ k_ccd(CCDArgs a)
             lo.b1 = m;
             hi.b0 = m;
         }
+        if (sp + 2 > kCCDStack && sb > 0) {
+            for (int s2 = sb; s2 < sp; s2++) stack[s2 - sb] = stack[s2];
+            sp -= sb;
+            sb = 0;
+        }
         if (sp + 2 > kCCDStack) {
             // cannot descend: keep the box's start as a conservative root
             earliest = smin(earliest, x.t0);
@@ -686,6 +759,12 @@ k_ccd(CCDArgs a)
         if (tot_boxes) atomicAdd(a.boxes, tot_boxes);
         if (tot_hits) atomicAdd(a.hits, tot_hits);
     }
+}
+
+__global__ void k_fill_inf(double* __restrict__ v, int64_t n)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) v[i] = INFINITY;
 }
 
 // counters layout in the context's device scalars (byte offset 256):
@@ -718,6 +797,16 @@ int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flag
         a.prune = (flags & RIGC_TOI_NO_PRUNE) ? 0 : 1;
         a.max_boxes = c.ccd_max_boxes;
         a.gmin = cnt;
+        a.bscene = c.s.bscene;
+        a.scene_gmin = nullptr;
+        if (c.s.nscenes > 1) {
+            RIGC_TRY(c.scene_toi.reserve((size_t)c.s.nscenes * 8 + 8));
+            std::vector<unsigned long long> inf(c.s.nscenes, 0x7ff0000000000000ull);
+            RIGC_CUDA(cudaMemcpyAsync(c.scene_toi.ptr, inf.data(), inf.size() * 8,
+                                      cudaMemcpyHostToDevice, st));
+            RIGC_CUDA(cudaStreamSynchronize(st));
+            a.scene_gmin = c.scene_toi.as<unsigned long long>();
+        }
         a.per = per;
         a.status = reinterpret_cast<int*>(cnt + 3);
         a.boxes = cnt + 1;
@@ -748,6 +837,11 @@ int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flag
         a.fmask = slots - 1;
         RIGC_COUNT_LAUNCH();
         k_ccd_prepare<<<grid_for(n, 128), 128, 0, st>>>(a);
+        if (per) {
+            // per-candidate results are minima over the lanes that share a search
+            RIGC_COUNT_LAUNCH();
+            k_fill_inf<<<grid_for(n, 256), 256, 0, st>>>(per, n);
+        }
         static int blocks_per_sm = 0;
         if (!blocks_per_sm) {
             RIGC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_ccd,
@@ -768,7 +862,15 @@ int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flag
     RIGC_CUDA(cudaStreamSynchronize(st));
     double g;
     std::memcpy(&g, &out[0], sizeof(g));
-    *toi_host = out[2] ? g : INFINITY;
+    *toi_host = g;  // +inf bits when no candidate found an impact
+    c.h_scene_toi.assign(c.s.nscenes, INFINITY);
+    if (n > 0 && c.s.nscenes > 1) {
+        RIGC_CUDA(cudaMemcpyAsync(c.h_scene_toi.data(), c.scene_toi.ptr, (size_t)c.s.nscenes * 8,
+                                  cudaMemcpyDeviceToHost, st));
+        RIGC_CUDA(cudaStreamSynchronize(st));
+    } else {
+        c.h_scene_toi.assign(c.s.nscenes, g);
+    }
     c.stats.ccd_boxes = (int64_t)out[1];
     c.stats.ccd_candidates = n;
     c.stats.ccd_collisions = (int64_t)out[2];

@@ -101,6 +101,11 @@ struct Scene {
     // host copies of the prefix arrays
     std::vector<int> h_bvs, h_type;
     int max_body_vertices = 0;
+    // batched contexts: independent scenes, bodies ordered by scene
+    int nscenes = 1;
+    int* bscene = nullptr;         // nb, scene of each body
+    int* scene_bstart = nullptr;   // nscenes + 1, first body of each scene
+    std::vector<int> h_scene_bstart, h_bes, h_bfs;
 };
 
 struct Candidates {
@@ -124,6 +129,8 @@ struct Friction {
     DevBuf grad, row_ptr, col, val;
     int64_t nnzb = 0;
 };
+
+struct Sim;  // time-stepping state (step.cu)
 
 struct Ctx {
     Scene s;
@@ -153,6 +160,10 @@ struct Ctx {
     DevBuf frame_keys, frame_vals;  // CCD frame cache (hash table)
     Friction fric;
     int64_t ccd_max_boxes = int64_t(1) << 22;  // per-candidate CCD box budget
+    Sim* sim = nullptr;
+    // batched contexts: per-scene results of the last calls
+    DevBuf scene_toi, scene_energy;
+    std::vector<double> h_scene_toi, h_scene_energy;
 };
 
 Ctx* ctx_of(rigc_ctx* c);

@@ -1,0 +1,932 @@
+// Time stepping on the device: the rigid IPC problem's simulation step with
+// the IPC Newton solver, every term, the collision filtering and the linear
+// solve on the GPU, the solver's scalar decisions on the host.
+//
+// Replaces DistanceBarrierRBProblem::simulation_step
+// (src/problems/distance_barrier_rb_problem.cpp:118-143) for the default
+// settings (implicit Euler, IPC solver with velocity convergence, one friction
+// lagging iteration, no kinematic bodies):
+//  * update_constraints (:145-166): lagged friction constraints at the
+//    start-of-step poses x0 with the current barrier stiffness;
+//  * IPCSolver::init_solve (src/solvers/ipc_solver.cpp:36-65): initial
+//    stiffness from the energy and barrier gradients at x0 (ipc-toolkit's
+//    initial_barrier_stiffness: argmin |grad E + kappa grad B| clamped to
+//    [kappa_min, 100 kappa_min], kappa_min = scale m / (4 d0 b''(d0)),
+//    d0 = (1e-8 bbox + dmin)^2) and the initial minimum distance;
+//  * NewtonSolver::solve (src/solvers/newton_solver.cpp:158-300): objective
+//    E/m + kappa/m B + D/m (compute_objective, :633-703) on the free degrees
+//    of freedom, regularised Newton direction (:421-478; H + c I with c
+//    doubling from 1e-8 while the solve fails or is not a descent direction,
+//    halving after a success), velocity convergence (:95-140), line search
+//    over [0, min(toi(x, x + d), 1)] halving until the objective decreases
+//    (:302-418), the gradient fallback, and the adaptive stiffness update
+//    (ipc_solver.cpp:67-89: kappa doubles, up to 100 kappa_min, while the
+//    minimum distance keeps shrinking below dhat_epsilon (bbox + dmin));
+//  * take_step (:488-626): implicit-Euler v and Qdot.
+// The Newton system on the free dofs is factorised densely (LDL^T without
+// pivoting, one block) when it has at most kDenseMax unknowns, else solved by
+// preconditioned conjugate gradients on the block-sparse Hessian (6x6 blocks:
+// body energy + barrier + friction) with a block-Jacobi preconditioner, to a
+// relative residual of 1e-12.  A failed solve (zero pivot, non-positive
+// curvature, no convergence) counts as a failed factorisation in the
+// reference and raises the regularisation.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+#include "geometry_rn.cuh"
+#include "rotation.cuh"
+#include "sort.cuh"
+
+namespace rigc {
+
+int construct_constraints(Ctx& c, const double* x, double dhat, double dmin);
+int detect_and_count(Ctx& c, const double* x0, const double* x1, bool continuous, double infl);
+int compute_world_vertices_rn(Ctx& c, const double* x, double* V, DevBuf& rotbuf);
+int body_energy(Ctx& c, const rigc_body_state& s, const double* x, const double gravity[3],
+                double h, double* energy_host, double* grad, double* hess);
+int friction_setup(Ctx& c, const double* x0, double dhat, double kappa, double mu, double dmin);
+int friction_term(Ctx& c, const double* x, double epsvh, int flags, rigc_barrier_out* out);
+int barrier_term_impl(Ctx& c, const double* x, double dhat, double dmin, int flags,
+                      rigc_barrier_out* out);
+int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flags,
+            double* toi_host, double* per);
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// kernels
+
+__global__ void k_axpy(int64_t n, double a, const double* __restrict__ x,
+                       const double* __restrict__ y, double* __restrict__ out)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = y[i] + a * x[i];
+}
+
+// g = gE / m + (kappa / m) gB + gD / m, zero on fixed degrees of freedom
+__global__ void k_combine_grad(int nb, const double* __restrict__ gE, const double* __restrict__ gB,
+                               const double* __restrict__ gD, double sE, double sB, double sD,
+                               const int* __restrict__ fixed, double* __restrict__ g)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 6 * nb) return;
+    double v = sE * gE[i];
+    if (gB) v += sB * gB[i];
+    if (gD) v += sD * gD[i];
+    g[i] = ((fixed[i / 6] >> (i % 6)) & 1) ? 0.0 : v;
+}
+
+struct HessView {
+    const double* body;      // nb x 36 (scale sE)
+    const int* brp;          // barrier BSR (scale sB)
+    const int* bcol;
+    const double* bval;
+    const int* frp;          // friction BSR (scale sD)
+    const int* fcol;
+    const double* fval;
+    double sE, sB, sD, reg;  // scales and the regularisation c (H + c I)
+    const int* fixed;
+    int nb;
+};
+
+// y = H x on the free degrees of freedom (fixed rows and columns removed)
+__global__ void k_hess_matvec(HessView H, const double* __restrict__ x, double* __restrict__ y)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 6 * H.nb) return;
+    const int b = i / 6, r = i % 6;
+    if ((H.fixed[b] >> r) & 1) {
+        y[i] = 0;
+        return;
+    }
+    double acc = 0;
+    const double* Bb = H.body + 36 * (size_t)b + 6 * r;
+    for (int c = 0; c < 6; c++) acc += H.sE * Bb[c] * x[6 * b + c];
+    if (H.brp)
+        for (int k = H.brp[b]; k < H.brp[b + 1]; k++) {
+            const double* V = H.bval + 36 * (size_t)k + 6 * r;
+            const int cb = H.bcol[k];
+            for (int c = 0; c < 6; c++) acc += H.sB * V[c] * x[6 * cb + c];
+        }
+    if (H.frp)
+        for (int k = H.frp[b]; k < H.frp[b + 1]; k++) {
+            const double* V = H.fval + 36 * (size_t)k + 6 * r;
+            const int cb = H.fcol[k];
+            for (int c = 0; c < 6; c++) acc += H.sD * V[c] * x[6 * cb + c];
+        }
+    y[i] = acc + H.reg * x[i];
+}
+
+// inverse of each body's diagonal 6x6 block (free part; fixed rows and
+// columns become the identity), by Cholesky; a block that is not positive
+// definite falls back to the inverse of its absolute diagonal
+__global__ void k_block_jacobi(HessView H, double* __restrict__ Minv)
+{
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= H.nb) return;
+    double A[36];
+    for (int k = 0; k < 36; k++) A[k] = H.sE * H.body[36 * (size_t)b + k];
+    if (H.brp)
+        for (int k = H.brp[b]; k < H.brp[b + 1]; k++)
+            if (H.bcol[k] == b)
+                for (int e = 0; e < 36; e++) A[e] += H.sB * H.bval[36 * (size_t)k + e];
+    if (H.frp)
+        for (int k = H.frp[b]; k < H.frp[b + 1]; k++)
+            if (H.fcol[k] == b)
+                for (int e = 0; e < 36; e++) A[e] += H.sD * H.fval[36 * (size_t)k + e];
+    const int fx = H.fixed[b];
+    for (int r = 0; r < 6; r++) {
+        A[7 * r] += H.reg;
+        for (int c = 0; c < 6; c++)
+            if (((fx >> r) & 1) || ((fx >> c) & 1)) A[6 * r + c] = r == c ? 1.0 : 0.0;
+    }
+    // Cholesky A = L L^T
+    double L[36];
+    bool pd = true;
+    for (int k = 0; k < 36; k++) L[k] = 0;
+    for (int j = 0; j < 6 && pd; j++) {
+        double d = A[7 * j];
+        for (int k = 0; k < j; k++) d -= L[6 * j + k] * L[6 * j + k];
+        if (!(d > 0)) {
+            pd = false;
+            break;
+        }
+        double ljj = sqrt(d);
+        L[7 * j] = ljj;
+        for (int i = j + 1; i < 6; i++) {
+            double s = 0.5 * (A[6 * i + j] + A[6 * j + i]);
+            for (int k = 0; k < j; k++) s -= L[6 * i + k] * L[6 * j + k];
+            L[6 * i + j] = s / ljj;
+        }
+    }
+    double* M = Minv + 36 * (size_t)b;
+    if (!pd) {
+        for (int r = 0; r < 6; r++)
+            for (int c = 0; c < 6; c++) {
+                double a = fabs(A[7 * r]);
+                M[6 * r + c] = r == c ? (a > 0 ? 1.0 / a : 1.0) : 0.0;
+            }
+        return;
+    }
+    // columns of A^-1 by two triangular solves
+    for (int c = 0; c < 6; c++) {
+        double y[6];
+        for (int i = 0; i < 6; i++) {
+            double s = i == c ? 1.0 : 0.0;
+            for (int k = 0; k < i; k++) s -= L[6 * i + k] * y[k];
+            y[i] = s / L[7 * i];
+        }
+        for (int i = 5; i >= 0; i--) {
+            double s = y[i];
+            for (int k = i + 1; k < 6; k++) s -= L[6 * k + i] * y[k];
+            y[i] = s / L[7 * i];
+        }
+        for (int i = 0; i < 6; i++) M[6 * i + c] = y[i];
+    }
+}
+
+__global__ void k_block_apply(int nb, const double* __restrict__ Minv, const double* __restrict__ r,
+                              const int* __restrict__ fixed, double* __restrict__ z)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 6 * nb) return;
+    const int b = i / 6, row = i % 6;
+    double acc = 0;
+    const double* M = Minv + 36 * (size_t)b + 6 * row;
+    for (int c = 0; c < 6; c++) acc += M[c] * r[6 * b + c];
+    z[i] = ((fixed[b] >> row) & 1) ? 0.0 : acc;
+}
+
+// deterministic dot product: 256 partial sums, then one block
+__global__ void k_dot_partial(int64_t n, const double* __restrict__ a, const double* __restrict__ b,
+                              double* __restrict__ part)
+{
+    __shared__ double sh[256];
+    double s = 0;
+    for (int64_t i = (int64_t)blockIdx.x * 256 + threadIdx.x; i < n; i += (int64_t)gridDim.x * 256)
+        s += a[i] * b[i];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+__global__ void k_dot_final(const double* __restrict__ part, int m, double* __restrict__ out)
+{
+    __shared__ double sh[256];
+    sh[threadIdx.x] = threadIdx.x < m ? part[threadIdx.x] : 0.0;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = sh[0];
+}
+
+// CG step length on the device: alpha = rz / pAp, or 0 once the residual
+// is within the tolerance (then the iteration has converged, and a zero
+// direction is not a breakdown)
+__global__ void k_cg_alpha(const double* __restrict__ rz, const double* __restrict__ pAp,
+                           const double* __restrict__ rr, double tol2,
+                           double* __restrict__ alpha, int* __restrict__ flags)
+{
+    if (flags[1] || *rr <= tol2) {
+        flags[1] = 1;  // converged
+        *alpha = 0;
+        return;
+    }
+    const double d = *pAp;
+    if (!(d > 0) || !isfinite(d)) {
+        flags[0] = 1;  // breakdown: not positive definite
+        *alpha = 0;
+    } else {
+        *alpha = *rz / d;
+    }
+}
+
+// x += alpha p; r -= alpha Ap
+__global__ void k_cg_update(int64_t n, const double* __restrict__ alpha, const double* __restrict__ p,
+                            const double* __restrict__ Ap, double* __restrict__ x,
+                            double* __restrict__ r)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double a = *alpha;
+    x[i] += a * p[i];
+    r[i] -= a * Ap[i];
+}
+
+// p = z + (rz_new / rz_old) p (unchanged once converged)
+__global__ void k_cg_direction(int64_t n, const double* __restrict__ rz_new,
+                               const double* __restrict__ rz_old, const double* __restrict__ z,
+                               const int* __restrict__ flags, double* __restrict__ p)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || flags[0] || flags[1]) return;
+    p[i] = z[i] + (*rz_new / *rz_old) * p[i];
+}
+
+// largest |V(x1) - V(x0)| coordinate over all vertices (max of non-negative
+// doubles through their bit patterns)
+__global__ void k_max_vertex_move(int nv, const double* __restrict__ V0, const double* __restrict__ V1,
+                                  unsigned long long* __restrict__ out)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double m = 0;
+    if (i < 3 * nv) m = fabs(V1[i] - V0[i]);
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
+}
+
+// smallest squared distance of the constraint set (the distance each barrier
+// uses, in the round-to-nearest order of the constraint set)
+__global__ void k_min_constraint_distance(int64_t n, const int* __restrict__ type,
+                                          const int* __restrict__ verts, const double* __restrict__ V,
+                                          unsigned long long* __restrict__ out)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double d = INFINITY;
+    if (i < n) {
+        const int t = type[i];
+        const double* P[4];
+        for (int k = 0; k < 4; k++) {
+            int v = verts[4 * i + k];
+            P[k] = V + 3 * (size_t)(v < 0 ? 0 : v);
+        }
+        if (t == 0) d = pp_sqdist_rn(P[0], P[1]);
+        else if (t == 1) d = pl_sqdist_rn(P[0], P[1], P[2]);
+        else if (t == 2) d = ll_sqdist_rn(P[0], P[1], P[2], P[3]);
+        else d = ptplane_sqdist_rn(P[0], P[1], P[2], P[3]);
+    }
+    for (int o = 16; o > 0; o >>= 1) d = fmin(d, __shfl_xor_sync(0xffffffffu, d, o));
+    if ((threadIdx.x & 31) == 0) atomicMin(out, (unsigned long long)__double_as_longlong(d));
+}
+
+// implicit-Euler update of the dynamic bodies: v = (q - q0) / h,
+// Qdot = (R(theta) - R(theta0)) / h, then the poses
+__global__ void k_take_step(int nb, const int* __restrict__ type, const int* __restrict__ fixed,
+                            const double* __restrict__ x, double* __restrict__ x0,
+                            double* __restrict__ v, double* __restrict__ Qdot, double h)
+{
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    if (type[b] == RIGC_BODY_DYNAMIC) {
+        double Q[9], Q0[9];
+        const double t[3] = { x[6 * b + 3], x[6 * b + 4], x[6 * b + 5] };
+        const double t0[3] = { x0[6 * b + 3], x0[6 * b + 4], x0[6 * b + 5] };
+        rot_rn(t, Q);
+        rot_rn(t0, Q0);
+        for (int k = 0; k < 3; k++)
+            v[6 * b + k] = ((fixed[b] >> k) & 1) ? 0.0 : (x[6 * b + k] - x0[6 * b + k]) / h;
+        for (int k = 0; k < 9; k++) Qdot[9 * b + k] = (Q[k] - Q0[k]) / h;
+    }
+    for (int k = 0; k < 6; k++) x0[6 * b + k] = x[6 * b + k];
+}
+
+// DistanceBarrierConstraint::construct_constraint_set: discrete candidates
+// with inflation (dhat + dmin) / 2, then the constraint set
+int build_constraints(Ctx& c, const double* x, double dhat, double dmin)
+{
+    if (c.s.nb <= 1) {
+        c.cons.num = c.cons.num_vv = c.cons.num_ev = c.cons.num_ee = c.cons.num_fv = 0;
+        return RIGC_OK;
+    }
+    RIGC_TRY(detect_and_count(c, x, x, false, (dhat + dmin) / 2.0));
+    return construct_constraints(c, x, dhat, dmin);
+}
+
+// dense copy of the free part of H + reg I: one thread per (body, row)
+__global__ void k_dense_fill(HessView H, const int* __restrict__ free_idx, int nfree,
+                             double* __restrict__ A)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 6 * H.nb) return;
+    const int b = i / 6, r = i % 6;
+    const int fi = free_idx[i];
+    if (fi < 0) return;
+    double* row = A + (size_t)fi * nfree;
+    for (int c = 0; c < 6; c++) {
+        const int fj = free_idx[6 * b + c];
+        if (fj >= 0) row[fj] += H.sE * H.body[36 * (size_t)b + 6 * r + c];
+    }
+    if (H.brp)
+        for (int k = H.brp[b]; k < H.brp[b + 1]; k++) {
+            const int cb = H.bcol[k];
+            for (int c = 0; c < 6; c++) {
+                const int fj = free_idx[6 * cb + c];
+                if (fj >= 0) row[fj] += H.sB * H.bval[36 * (size_t)k + 6 * r + c];
+            }
+        }
+    if (H.frp)
+        for (int k = H.frp[b]; k < H.frp[b + 1]; k++) {
+            const int cb = H.fcol[k];
+            for (int c = 0; c < 6; c++) {
+                const int fj = free_idx[6 * cb + c];
+                if (fj >= 0) row[fj] += H.sD * H.fval[36 * (size_t)k + 6 * r + c];
+            }
+        }
+    row[fi] += H.reg;
+}
+
+// Dense LDL^T (no pivoting) and solve A x = b by one block, left-looking:
+// d_j = a_jj - sum_k l_jk^2 d_k, l_ij = (a_ij - sum_k l_ik l_jk d_k) / d_j,
+// each sum in increasing k by one thread.  flags[0] = 1 on a zero or
+// non-finite pivot.  A's lower triangle is overwritten by L.
+__global__ void __launch_bounds__(256) k_dense_ldlt(double* __restrict__ A, int n,
+                                                    const double* __restrict__ b,
+                                                    double* __restrict__ x, double* __restrict__ D,
+                                                    int* __restrict__ flags)
+{
+    __shared__ double dj;
+    __shared__ int fail;
+    if (threadIdx.x == 0) fail = 0;
+    __syncthreads();
+    for (int j = 0; j < n; j++) {
+        if (threadIdx.x == 0) {
+            double d = A[(size_t)j * n + j];
+            for (int k = 0; k < j; k++) d -= A[(size_t)j * n + k] * A[(size_t)j * n + k] * D[k];
+            if (!(fabs(d) > 0) || !isfinite(d)) fail = 1;
+            D[j] = d;
+            dj = d;
+        }
+        __syncthreads();
+        if (fail) break;
+        for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x) {
+            double s = A[(size_t)i * n + j];
+            for (int k = 0; k < j; k++) s -= A[(size_t)i * n + k] * A[(size_t)j * n + k] * D[k];
+            A[(size_t)i * n + j] = s / dj;
+        }
+        __syncthreads();
+    }
+    if (fail) {
+        if (threadIdx.x == 0) flags[0] = 1;
+        return;
+    }
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < n; i++) {
+            double s = b[i];
+            for (int k = 0; k < i; k++) s -= A[(size_t)i * n + k] * x[k];
+            x[i] = s;
+        }
+        for (int i = 0; i < n; i++) x[i] /= D[i];
+        for (int i = n - 1; i >= 0; i--) {
+            double s = x[i];
+            for (int k = i + 1; k < n; k++) s -= A[(size_t)k * n + i] * x[k];
+            x[i] = s;
+        }
+        for (int i = 0; i < n; i++)
+            if (!isfinite(x[i])) flags[0] = 1;
+    }
+}
+
+// rhs of the free dofs (-g) and the scatter of the solution back
+__global__ void k_gather_neg(int n6, const int* __restrict__ free_idx, const double* __restrict__ g,
+                             double* __restrict__ out)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n6 && free_idx[i] >= 0) out[free_idx[i]] = -g[i];
+}
+__global__ void k_scatter_free(int n6, const int* __restrict__ free_idx, const double* __restrict__ xf,
+                               double* __restrict__ x)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n6) x[i] = free_idx[i] >= 0 ? xf[free_idx[i]] : 0.0;
+}
+
+double barrier_hessian_d(double d, double s)
+{
+    if (d <= 0.0 || d >= s) return 0.0;
+    double sd = s / d;
+    return (sd + 2) * sd - 2 * std::log(d / s) - 3;
+}
+
+} // namespace
+
+// ---------------------------------------------------------------------------
+
+// systems with at most this many free dofs are factorised densely
+constexpr int kDenseMax = 384;
+
+struct Sim {
+    rigc_sim_params p {};
+    int nb = 0, nv = 0, nfree = 0;
+    DevBuf free_idx, dense, dense_b, dense_x, dense_d;  // dense LDL^T path
+    DevBuf mass, moment, fixed, x0, vel, Qdot;          // body state
+    DevBuf x, xt, dir, g, gE, hE, gtmp;                 // Newton vectors
+    DevBuf r, z, pp, Ap, Minv, sol, part, scal;         // CG
+    DevBuf V0, V1;                                      // world vertices
+    double kappa = 1, kappa_max = 0;
+    std::vector<int> h_fixed;
+};
+
+namespace {
+
+struct Objective {
+    double f;
+    bool grad_hess;
+    rigc_barrier_out bo, fo;
+};
+
+rigc_body_state state_of(Sim& S)
+{
+    rigc_body_state s;
+    s.mass = S.mass.as<double>();
+    s.moment = S.moment.as<double>();
+    s.x_t0 = S.x0.as<double>();
+    s.v_t0 = S.vel.as<double>();
+    s.Qdot_t0 = S.Qdot.as<double>();
+    s.dof_fixed = S.fixed.as<int32_t>();
+    return s;
+}
+
+int dot_dev(Ctx& c, Sim& S, int64_t n, const double* a, const double* b, double* out_dev)
+{
+    RIGC_COUNT_LAUNCH();
+    k_dot_partial<<<64, 256, 0, c.stream>>>(n, a, b, S.part.as<double>());
+    RIGC_COUNT_LAUNCH();
+    k_dot_final<<<1, 256, 0, c.stream>>>(S.part.as<double>(), 64, out_dev);
+    return RIGC_OK;
+}
+
+int read_scalars(Ctx& c, const double* dev, double* host, int n)
+{
+    RIGC_CUDA(cudaMemcpyAsync(host, dev, n * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    RIGC_CUDA(cudaStreamSynchronize(c.stream));
+    return RIGC_OK;
+}
+
+// objective (and optionally its gradient in S.g and the Hessian pieces)
+int objective(Ctx& c, Sim& S, const double* x, bool grad_hess, Objective& O)
+{
+    const rigc_sim_params& p = S.p;
+    const double m = p.average_mass;
+    rigc_body_state bs = state_of(S);
+    double E;
+    RIGC_TRY(body_energy(c, bs, x, p.gravity, p.timestep, &E, grad_hess ? S.gE.as<double>() : nullptr,
+                         grad_hess ? S.hE.as<double>() : nullptr));
+    RIGC_TRY(build_constraints(c, x, p.dhat, p.dmin));
+    const int flags = grad_hess ? (RIGC_GRAD | RIGC_HESS | RIGC_PROJECT_PSD) : 0;
+    RIGC_TRY(barrier_term_impl(c, x, p.dhat, p.dmin, flags, &O.bo));
+    double D = 0;
+    O.fo = rigc_barrier_out {};
+    if (p.coefficient_friction > 0 && c.fric.num > 0) {
+        RIGC_TRY(friction_term(c, x, p.static_friction_speed_bound * p.timestep, flags, &O.fo));
+        D = O.fo.energy;
+    }
+    O.f = E / m + S.kappa / m * O.bo.energy + D / m;
+    O.grad_hess = grad_hess;
+    if (grad_hess) {
+        RIGC_COUNT_LAUNCH();
+        k_combine_grad<<<grid_for(6 * S.nb, 256), 256, 0, c.stream>>>(
+            S.nb, S.gE.as<double>(), O.bo.grad, O.fo.grad, 1.0 / m, S.kappa / m, 1.0 / m,
+            S.fixed.as<int>(), S.g.as<double>());
+        RIGC_CUDA(cudaGetLastError());
+    }
+    return RIGC_OK;
+}
+
+HessView hess_view(Sim& S, const Objective& O, double reg)
+{
+    const double m = S.p.average_mass;
+    HessView H;
+    H.body = S.hE.as<double>();
+    H.brp = O.bo.nnzb > 0 ? O.bo.row_ptr : nullptr;
+    H.bcol = O.bo.col;
+    H.bval = O.bo.val;
+    H.frp = O.fo.nnzb > 0 ? O.fo.row_ptr : nullptr;
+    H.fcol = O.fo.col;
+    H.fval = O.fo.val;
+    H.sE = 1.0 / m;
+    H.sB = S.kappa / m;
+    H.sD = 1.0 / m;
+    H.reg = reg;
+    H.fixed = S.fixed.as<int>();
+    H.nb = S.nb;
+    return H;
+}
+
+// PCG for (H + reg I) d = -g on the free dofs; false when it breaks down
+// or does not reach the tolerance
+int pcg(Ctx& c, Sim& S, const HessView& H, bool& ok, int64_t& iters)
+{
+    const int64_t n = 6 * (int64_t)S.nb;
+    cudaStream_t st = c.stream;
+    const unsigned gn = grid_for(n, 256);
+    double* d = S.sol.as<double>();
+    double* r = S.r.as<double>();
+    double* z = S.z.as<double>();
+    double* pp = S.pp.as<double>();
+    double* Ap = S.Ap.as<double>();
+    double* sc = S.scal.as<double>();  // [0] rz, [1] rz_new, [2] pAp, [3] alpha, [4] rr, [5] bb
+    int* flags = reinterpret_cast<int*>(sc + 8);  // [0] breakdown, [1] converged
+    RIGC_CUDA(cudaMemsetAsync(d, 0, n * sizeof(double), st));
+    RIGC_CUDA(cudaMemsetAsync(flags, 0, 2 * sizeof(int), st));
+    // r = -g
+    RIGC_COUNT_LAUNCH();
+    k_axpy<<<gn, 256, 0, st>>>(n, -2.0, S.g.as<double>(), S.g.as<double>(), r);
+    RIGC_COUNT_LAUNCH();
+    k_block_jacobi<<<grid_for(S.nb, 64), 64, 0, st>>>(H, S.Minv.as<double>());
+    RIGC_COUNT_LAUNCH();
+    k_block_apply<<<gn, 256, 0, st>>>(S.nb, S.Minv.as<double>(), r, H.fixed, z);
+    RIGC_CUDA(cudaMemcpyAsync(pp, z, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    RIGC_TRY(dot_dev(c, S, n, r, z, sc + 0));
+    RIGC_TRY(dot_dev(c, S, n, r, r, sc + 5));
+    RIGC_CUDA(cudaMemcpyAsync(sc + 4, sc + 5, sizeof(double), cudaMemcpyDeviceToDevice, st));
+    double h5[2];
+    RIGC_TRY(read_scalars(c, sc + 5, h5, 1));
+    const double bnorm2 = h5[0];
+    ok = true;
+    iters = 0;
+    if (bnorm2 == 0) return RIGC_OK;
+    const double tol2 = 1e-24 * bnorm2;  // relative residual 1e-12
+    const int64_t max_it = std::max<int64_t>(1000, 4 * n);
+    for (int64_t it = 0; it < max_it; it++) {
+        RIGC_COUNT_LAUNCH();
+        k_hess_matvec<<<gn, 256, 0, st>>>(H, pp, Ap);
+        RIGC_TRY(dot_dev(c, S, n, pp, Ap, sc + 2));
+        RIGC_COUNT_LAUNCH();
+        k_cg_alpha<<<1, 1, 0, st>>>(sc + 0, sc + 2, sc + 4, tol2, sc + 3, flags);
+        RIGC_COUNT_LAUNCH();
+        k_cg_update<<<gn, 256, 0, st>>>(n, sc + 3, pp, Ap, d, r);
+        RIGC_COUNT_LAUNCH();
+        k_block_apply<<<gn, 256, 0, st>>>(S.nb, S.Minv.as<double>(), r, H.fixed, z);
+        RIGC_TRY(dot_dev(c, S, n, r, z, sc + 1));
+        RIGC_TRY(dot_dev(c, S, n, r, r, sc + 4));
+        RIGC_COUNT_LAUNCH();
+        k_cg_direction<<<gn, 256, 0, st>>>(n, sc + 1, sc + 0, z, flags, pp);
+        RIGC_CUDA(cudaMemcpyAsync(sc + 0, sc + 1, sizeof(double), cudaMemcpyDeviceToDevice, st));
+        iters = it + 1;
+        if ((it & 7) == 7 || it + 1 == max_it) {
+            double rr;
+            int fl[2];
+            RIGC_CUDA(cudaMemcpyAsync(&rr, sc + 4, sizeof(double), cudaMemcpyDeviceToHost, st));
+            RIGC_CUDA(cudaMemcpyAsync(fl, flags, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
+            RIGC_CUDA(cudaStreamSynchronize(st));
+            if (fl[1] || rr <= tol2) return RIGC_OK;
+            if (fl[0] || !std::isfinite(rr)) {
+                ok = false;
+                return RIGC_OK;
+            }
+        }
+    }
+    ok = false;
+    return RIGC_OK;
+}
+
+// dense LDL^T solve of (H + reg I) d = -g on the free dofs into S.sol
+int dense_solve(Ctx& c, Sim& S, const HessView& H, bool& ok)
+{
+    const int n = S.nfree;
+    const int n6 = 6 * S.nb;
+    cudaStream_t st = c.stream;
+    int* flags = reinterpret_cast<int*>(S.scal.as<double>() + 8);
+    RIGC_CUDA(cudaMemsetAsync(flags, 0, 2 * sizeof(int), st));
+    RIGC_CUDA(cudaMemsetAsync(S.dense.ptr, 0, (size_t)n * n * sizeof(double), st));
+    RIGC_COUNT_LAUNCH();
+    k_dense_fill<<<grid_for(n6, 128), 128, 0, st>>>(H, S.free_idx.as<int>(), n, S.dense.as<double>());
+    RIGC_COUNT_LAUNCH();
+    k_gather_neg<<<grid_for(n6, 256), 256, 0, st>>>(n6, S.free_idx.as<int>(), S.g.as<double>(),
+                                                    S.dense_b.as<double>());
+    RIGC_COUNT_LAUNCH();
+    k_dense_ldlt<<<1, 256, 0, st>>>(S.dense.as<double>(), n, S.dense_b.as<double>(),
+                                    S.dense_x.as<double>(), S.dense_d.as<double>(), flags);
+    RIGC_COUNT_LAUNCH();
+    k_scatter_free<<<grid_for(n6, 256), 256, 0, st>>>(n6, S.free_idx.as<int>(), S.dense_x.as<double>(),
+                                                      S.sol.as<double>());
+    RIGC_CUDA(cudaGetLastError());
+    int fl = 0;
+    RIGC_CUDA(cudaMemcpyAsync(&fl, flags, sizeof(int), cudaMemcpyDeviceToHost, st));
+    RIGC_CUDA(cudaStreamSynchronize(st));
+    ok = fl == 0;
+    return RIGC_OK;
+}
+
+double host_dot(Ctx& c, Sim& S, const double* a, const double* b)
+{
+    double v = 0;
+    if (dot_dev(c, S, 6 * (int64_t)S.nb, a, b, S.scal.as<double>() + 6) != RIGC_OK) return NAN;
+    if (read_scalars(c, S.scal.as<double>() + 6, &v, 1) != RIGC_OK) return NAN;
+    return v;
+}
+
+int min_distance(Ctx& c, Sim& S, const double* x, double* md)
+{
+    RIGC_TRY(build_constraints(c, x, S.p.dhat, S.p.dmin));
+    const int64_t n = c.cons.num;
+    if (n == 0) {
+        *md = -1;
+        return RIGC_OK;
+    }
+    RIGC_TRY(compute_world_vertices_rn(c, x, S.V0.as<double>(), c.scratch[5]));
+    unsigned long long* out = reinterpret_cast<unsigned long long*>(S.scal.as<double>() + 12);
+    const unsigned long long inf = 0x7ff0000000000000ull;
+    RIGC_CUDA(cudaMemcpyAsync(out, &inf, sizeof(inf), cudaMemcpyHostToDevice, c.stream));
+    RIGC_COUNT_LAUNCH();
+    k_min_constraint_distance<<<grid_for(n, 256), 256, 0, c.stream>>>(
+        n, c.cons.type.as<int>(), c.cons.verts.as<int>(), S.V0.as<double>(), out);
+    double d2;
+    RIGC_TRY(read_scalars(c, reinterpret_cast<double*>(out), &d2, 1));
+    *md = std::isfinite(d2) ? std::sqrt(d2) : -1;
+    return RIGC_OK;
+}
+
+// max over vertices and coordinates of |V(x + d) - V(x)|
+int max_vertex_move(Ctx& c, Sim& S, const double* x, const double* x1, double* m)
+{
+    RIGC_TRY(compute_world_vertices_rn(c, x, S.V0.as<double>(), c.scratch[5]));
+    RIGC_TRY(compute_world_vertices_rn(c, x1, S.V1.as<double>(), c.scratch[5]));
+    unsigned long long* out = reinterpret_cast<unsigned long long*>(S.scal.as<double>() + 13);
+    RIGC_CUDA(cudaMemsetAsync(out, 0, sizeof(unsigned long long), c.stream));
+    RIGC_COUNT_LAUNCH();
+    k_max_vertex_move<<<grid_for(3 * (int64_t)S.nv, 256), 256, 0, c.stream>>>(
+        S.nv, S.V0.as<double>(), S.V1.as<double>(), out);
+    RIGC_TRY(read_scalars(c, reinterpret_cast<double*>(out), m, 1));
+    return RIGC_OK;
+}
+
+} // namespace
+
+int sim_init(Ctx& c, const rigc_sim_params& p, const rigc_sim_state& s)
+{
+    if (!c.sim) c.sim = new Sim;
+    Sim& S = *c.sim;
+    S.p = p;
+    S.nb = c.s.nb;
+    S.nv = c.s.nv;
+    const int nb = S.nb;
+    const size_t v6 = (size_t)6 * nb * sizeof(double) + 64;
+    DevBuf* vecs[] = { &S.x0, &S.vel, &S.x, &S.xt, &S.dir, &S.g, &S.gE, &S.gtmp,
+                       &S.r, &S.z, &S.pp, &S.Ap, &S.sol };
+    for (DevBuf* b : vecs) RIGC_TRY(b->reserve(v6));
+    RIGC_TRY(S.mass.reserve((size_t)nb * 8 + 8));
+    RIGC_TRY(S.moment.reserve((size_t)nb * 24 + 8));
+    RIGC_TRY(S.fixed.reserve((size_t)nb * 4 + 8));
+    RIGC_TRY(S.Qdot.reserve((size_t)nb * 72 + 8));
+    RIGC_TRY(S.hE.reserve((size_t)nb * 36 * 8 + 8));
+    RIGC_TRY(S.Minv.reserve((size_t)nb * 36 * 8 + 8));
+    RIGC_TRY(S.part.reserve(64 * 8));
+    RIGC_TRY(S.scal.reserve(32 * 8));
+    RIGC_TRY(S.V0.reserve((size_t)S.nv * 24 + 8));
+    RIGC_TRY(S.V1.reserve((size_t)S.nv * 24 + 8));
+    cudaStream_t st = c.stream;
+    RIGC_CUDA(cudaMemcpyAsync(S.mass.ptr, s.mass, (size_t)nb * 8, cudaMemcpyHostToDevice, st));
+    RIGC_CUDA(cudaMemcpyAsync(S.moment.ptr, s.moment, (size_t)nb * 24, cudaMemcpyHostToDevice, st));
+    RIGC_CUDA(cudaMemcpyAsync(S.fixed.ptr, s.dof_fixed, (size_t)nb * 4, cudaMemcpyHostToDevice, st));
+    RIGC_CUDA(cudaMemcpyAsync(S.x0.ptr, s.poses, (size_t)nb * 48, cudaMemcpyHostToDevice, st));
+    RIGC_CUDA(cudaMemcpyAsync(S.vel.ptr, s.velocities, (size_t)nb * 48, cudaMemcpyHostToDevice, st));
+    RIGC_CUDA(cudaMemcpyAsync(S.Qdot.ptr, s.Qdot, (size_t)nb * 72, cudaMemcpyHostToDevice, st));
+    RIGC_CUDA(cudaStreamSynchronize(st));
+    S.h_fixed.assign(s.dof_fixed, s.dof_fixed + nb);
+    // compact indices of the free dofs (the reference's free_dof slicing)
+    std::vector<int> fidx(6 * (size_t)nb, -1);
+    int nf = 0;
+    for (int b = 0; b < nb; b++)
+        for (int k = 0; k < 6; k++)
+            if (!((s.dof_fixed[b] >> k) & 1)) fidx[6 * b + k] = nf++;
+    S.nfree = nf;
+    RIGC_TRY(S.free_idx.reserve(fidx.size() * sizeof(int) + 8));
+    RIGC_CUDA(cudaMemcpyAsync(S.free_idx.ptr, fidx.data(), fidx.size() * sizeof(int),
+                              cudaMemcpyHostToDevice, st));
+    if (nf <= kDenseMax) {
+        RIGC_TRY(S.dense.reserve((size_t)nf * nf * sizeof(double) + 8));
+        RIGC_TRY(S.dense_b.reserve((size_t)nf * sizeof(double) + 8));
+        RIGC_TRY(S.dense_x.reserve((size_t)nf * sizeof(double) + 8));
+        RIGC_TRY(S.dense_d.reserve((size_t)nf * sizeof(double) + 8));
+    }
+    RIGC_CUDA(cudaStreamSynchronize(st));
+    S.kappa = 1;  // m_barrier_stiffness before the first solve
+    return RIGC_OK;
+}
+
+int sim_step(Ctx& c, rigc_step_stats* stats)
+{
+    if (!c.sim) return RIGC_ERR_ARG;
+    Sim& S = *c.sim;
+    const rigc_sim_params& p = S.p;
+    const int nb = S.nb;
+    const int64_t n = 6 * (int64_t)nb;
+    cudaStream_t st = c.stream;
+    double* x0 = S.x0.as<double>();
+    double* x = S.x.as<double>();
+    double* xt = S.xt.as<double>();
+    double* dir = S.dir.as<double>();
+    rigc_step_stats local {};
+
+    // update_constraints: lagged friction at x0 with the current stiffness
+    if (p.coefficient_friction > 0) {
+        RIGC_TRY(build_constraints(c, x0, p.dhat, p.dmin));
+        RIGC_TRY(friction_setup(c, x0, p.dhat, S.kappa, p.coefficient_friction, 0.0));
+    }
+
+    // IPCSolver::init_solve
+    {
+        rigc_body_state bs = state_of(S);
+        double E;
+        RIGC_TRY(body_energy(c, bs, x0, p.gravity, p.timestep, &E, S.gE.as<double>(), nullptr));
+        RIGC_TRY(build_constraints(c, x0, p.dhat, p.dmin));
+        rigc_barrier_out bo;
+        RIGC_TRY(barrier_term_impl(c, x0, p.dhat, p.dmin, RIGC_GRAD, &bo));
+        RIGC_CUDA(cudaMemcpyAsync(S.gtmp.ptr, bo.grad, n * 8, cudaMemcpyDeviceToDevice, st));
+        const double gg = host_dot(c, S, S.gtmp.as<double>(), S.gtmp.as<double>());
+        const double ge = host_dot(c, S, S.gtmp.as<double>(), S.gE.as<double>());
+        const double dmin = p.dmin;
+        double d0 = 1e-8 * p.world_bbox_diagonal + dmin;
+        d0 *= d0;
+        const double sb = 2 * dmin * p.dhat + p.dhat * p.dhat;
+        if (d0 - dmin * dmin >= sb) d0 = dmin * p.dhat + 0.5 * p.dhat * p.dhat;
+        double kmin = 4 * d0 * barrier_hessian_d(d0 - dmin * dmin, sb);
+        kmin = p.min_barrier_stiffness_scale * p.average_mass / kmin;
+        S.kappa_max = 100 * kmin;
+        const double k0 = gg > 0 ? -ge / gg : 1.0;
+        S.kappa = std::min(S.kappa_max, std::max(kmin, k0));
+    }
+    double prev_min_distance;
+    RIGC_TRY(min_distance(c, S, x0, &prev_min_distance));
+
+    RIGC_CUDA(cudaMemcpyAsync(x, x0, n * 8, cudaMemcpyDeviceToDevice, st));
+    double coeff = 0;
+    int it = 0;
+    for (; it < p.max_newton_iterations; it++) {
+        Objective O;
+        RIGC_TRY(objective(c, S, x, true, O));
+        local.objective_evals++;
+        const double fx = O.f;
+        // compute_regularized_direction
+        bool ok = false;
+        while (!ok) {
+            bool solved;
+            int64_t cgit;
+            HessView H = hess_view(S, O, coeff);
+            if (S.nfree <= kDenseMax) {
+                cgit = 0;
+                RIGC_TRY(dense_solve(c, S, H, solved));
+            } else {
+                RIGC_TRY(pcg(c, S, H, solved, cgit));
+            }
+            local.cg_iterations += cgit;
+            double gd = solved ? host_dot(c, S, S.g.as<double>(), S.sol.as<double>()) : 0;
+            ok = solved && gd <= 0;
+            if (ok) {
+                coeff /= 2;
+                if (coeff < 1e-8) coeff = 0;
+            } else {
+                coeff = std::max(2 * coeff, 1e-8);
+                if (!std::isfinite(coeff)) break;
+            }
+        }
+        if (!ok) break;
+        RIGC_CUDA(cudaMemcpyAsync(dir, S.sol.ptr, n * 8, cudaMemcpyDeviceToDevice, st));
+        // velocity convergence
+        if (it > 0) {
+            RIGC_COUNT_LAUNCH();
+            k_axpy<<<grid_for(n, 256), 256, 0, st>>>(n, 1.0, dir, x, xt);
+            double mv;
+            RIGC_TRY(max_vertex_move(c, S, x, xt, &mv));
+            const double tol = p.velocity_conv_tol * (p.velocity_conv_tol_abs ? 1.0 : p.world_bbox_diagonal);
+            if (mv / p.timestep <= tol) break;
+        }
+        // line search (the gradient on the free dofs is S.g)
+        auto line_search = [&](double& alpha, bool& found) -> int {
+            found = false;
+            const double gdv = host_dot(c, S, S.g.as<double>(), dir);
+            const double lb = std::min(p.line_search_lower_bound / std::sqrt(std::fabs(gdv)), 1e-1);
+            RIGC_COUNT_LAUNCH();
+            k_axpy<<<grid_for(n, 256), 256, 0, st>>>(n, 1.0, dir, x, xt);
+            double toi;
+            RIGC_TRY(detect_and_count(c, x, xt, true, p.dmin / 2.0));
+            int s2 = run_ccd(c, x, xt, 1e-4, 0, &toi, nullptr);
+            if (s2 != RIGC_OK && s2 != RIGC_ERR_QUEUE_OVERFLOW && s2 != RIGC_ERR_ITER_LIMIT) return s2;
+            local.ccd_calls++;
+            alpha = std::min(1.0, std::min(toi, 1.0));
+            while (std::isfinite(lb) && alpha >= lb) {
+                RIGC_COUNT_LAUNCH();
+                k_axpy<<<grid_for(n, 256), 256, 0, st>>>(n, alpha, dir, x, xt);
+                Objective Oi;
+                RIGC_TRY(objective(c, S, xt, false, Oi));
+                local.objective_evals++;
+                if (Oi.f < fx) {
+                    found = true;
+                    return RIGC_OK;
+                }
+                alpha /= 2.0;
+            }
+            return RIGC_OK;
+        };
+        double alpha = 1;
+        bool found;
+        RIGC_TRY(line_search(alpha, found));
+        if (!found) {
+            // gradient fallback: d = -g
+            RIGC_COUNT_LAUNCH();
+            k_axpy<<<grid_for(n, 256), 256, 0, st>>>(n, -2.0, S.g.as<double>(), S.g.as<double>(), dir);
+            alpha = 1;
+            RIGC_TRY(line_search(alpha, found));
+            if (!found) break;
+        }
+        RIGC_COUNT_LAUNCH();
+        k_axpy<<<grid_for(n, 256), 256, 0, st>>>(n, alpha, dir, x, x);
+        local.newton_steps++;
+        // adaptive stiffness
+        double md;
+        RIGC_TRY(min_distance(c, S, x, &md));
+        const double eps = p.dhat_epsilon * (p.world_bbox_diagonal + p.dmin);
+        if (prev_min_distance < eps && md < eps && md < prev_min_distance)
+            S.kappa = std::min(S.kappa_max, 2 * S.kappa);
+        prev_min_distance = md;
+    }
+    local.newton_iterations = it;
+
+    // take_step
+    RIGC_COUNT_LAUNCH();
+    k_take_step<<<grid_for(nb, 128), 128, 0, st>>>(nb, c.s.type, S.fixed.as<int>(), x, x0,
+                                                   S.vel.as<double>(), S.Qdot.as<double>(),
+                                                   p.timestep);
+    RIGC_CUDA(cudaGetLastError());
+    RIGC_CUDA(cudaStreamSynchronize(st));
+    local.barrier_stiffness = S.kappa;
+    if (stats) {
+        stats->newton_iterations += local.newton_iterations;
+        stats->newton_steps += local.newton_steps;
+        stats->objective_evals += local.objective_evals;
+        stats->ccd_calls += local.ccd_calls;
+        stats->cg_iterations += local.cg_iterations;
+        stats->barrier_stiffness = local.barrier_stiffness;
+    }
+    return RIGC_OK;
+}
+
+int sim_get_state(Ctx& c, double* poses, double* velocities, double* Qdot, double* kappa)
+{
+    if (!c.sim) return RIGC_ERR_ARG;
+    Sim& S = *c.sim;
+    const int nb = S.nb;
+    cudaStream_t st = c.stream;
+    if (poses) RIGC_CUDA(cudaMemcpyAsync(poses, S.x0.ptr, (size_t)nb * 48, cudaMemcpyDeviceToHost, st));
+    if (velocities)
+        RIGC_CUDA(cudaMemcpyAsync(velocities, S.vel.ptr, (size_t)nb * 48, cudaMemcpyDeviceToHost, st));
+    if (Qdot) RIGC_CUDA(cudaMemcpyAsync(Qdot, S.Qdot.ptr, (size_t)nb * 72, cudaMemcpyDeviceToHost, st));
+    RIGC_CUDA(cudaStreamSynchronize(st));
+    if (kappa) *kappa = S.kappa;
+    return RIGC_OK;
+}
+
+void sim_release(Ctx& c)
+{
+    if (!c.sim) return;
+    Sim& S = *c.sim;
+    DevBuf* bufs[] = { &S.mass, &S.moment, &S.fixed, &S.x0, &S.vel, &S.Qdot, &S.x, &S.xt,
+                       &S.dir, &S.g, &S.gE, &S.hE, &S.gtmp, &S.r, &S.z, &S.pp, &S.Ap,
+                       &S.Minv, &S.sol, &S.part, &S.scal, &S.V0, &S.V1, &S.free_idx,
+                       &S.dense, &S.dense_b, &S.dense_x, &S.dense_d };
+    for (DevBuf* b : bufs) b->release();
+    delete c.sim;
+    c.sim = nullptr;
+}
+
+} // namespace rigc

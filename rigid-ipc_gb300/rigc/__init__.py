@@ -30,7 +30,9 @@ def _torch():
 class Context:
     """One scene on one GPU (a RigidBodyAssembler plus its device buffers)."""
 
-    def __init__(self, scene: Scene, stream=None):
+    def __init__(self, scene: Scene, stream=None, scene_of_body=None):
+        """scene_of_body (num_bodies ints, non-decreasing) makes a batched
+        context of independent scenes (rigc_ctx_create_batched)."""
         self.lib = L.load()
         self.scene = scene
         torch = _torch()
@@ -65,7 +67,15 @@ class Context:
         d.r_max = k[9].ctypes.data_as(L._d)
         d.average_edge_length = scene.average_edge_length
         h = C.c_void_p()
-        L.check(self.lib.rigc_ctx_create(C.byref(d), C.byref(h)), "rigc_ctx_create")
+        if scene_of_body is None:
+            L.check(self.lib.rigc_ctx_create(C.byref(d), C.byref(h)), "rigc_ctx_create")
+            self.num_scenes = 1
+        else:
+            sob = np.ascontiguousarray(scene_of_body, dtype=np.int32)
+            self._keep.append(sob)
+            self.num_scenes = int(sob.max()) + 1 if len(sob) else 1
+            L.check(self.lib.rigc_ctx_create_batched(C.byref(d), self.num_scenes, sob.ctypes.data,
+                                                     C.byref(h)), "rigc_ctx_create_batched")
         self.h = h
         self._last_counts = (0, 0)
         if stream is not None:
@@ -127,6 +137,19 @@ class Context:
         ee = self.copy_out(out.ee, (out.num_ee, 2), np.int32)
         fv = self.copy_out(out.fv, (out.num_fv, 2), np.int32)
         return ee, fv
+
+    def scene_tois(self):
+        """Per-scene earliest time of impact of the last CCD call."""
+        out = np.empty(self.num_scenes)
+        L.check(self.lib.rigc_scene_tois(self.h, out.ctypes.data_as(L._d)), "rigc_scene_tois")
+        return out
+
+    def scene_barrier_energies(self):
+        """Per-scene barrier energy of the last barrier-term call."""
+        out = np.empty(self.num_scenes)
+        L.check(self.lib.rigc_scene_barrier_energies(self.h, out.ctypes.data_as(L._d)),
+                "rigc_scene_barrier_energies")
+        return out
 
     def set_candidates(self, ee, fv):
         """Use the given (edge, edge) and (face, vertex) pairs as the candidate set."""
@@ -285,6 +308,58 @@ class Context:
                                                    C.c_void_p(H.data_ptr())),
                 "rigc_friction_local_terms")
         return e[:n].cpu().numpy(), g[:n].cpu().numpy(), H[:n].cpu().numpy()
+
+    # ---- time stepping (DistanceBarrierRBProblem::simulation_step with the IPC solver)
+
+    def sim_init(self, timestep, gravity, dhat, dmin=0.0, coefficient_friction=0.0,
+                 static_friction_speed_bound=1e-3, max_newton_iterations=3000,
+                 velocity_conv_tol=1e-2, velocity_conv_tol_abs=False,
+                 line_search_lower_bound=1e-12, dhat_epsilon=1e-9,
+                 min_barrier_stiffness_scale=1e11):
+        """Start a simulation from the scene's poses, velocities and Qdot."""
+        sc = self.scene
+        V = sc.world_vertices(sc.poses())
+        p = L.SimParams()
+        p.timestep = timestep
+        p.gravity[:] = list(gravity)
+        p.dhat, p.dmin = dhat, dmin
+        p.coefficient_friction = coefficient_friction
+        p.static_friction_speed_bound = static_friction_speed_bound
+        p.max_newton_iterations = max_newton_iterations
+        p.velocity_conv_tol = velocity_conv_tol
+        p.velocity_conv_tol_abs = int(velocity_conv_tol_abs)
+        p.line_search_lower_bound = line_search_lower_bound
+        p.dhat_epsilon = dhat_epsilon
+        p.min_barrier_stiffness_scale = min_barrier_stiffness_scale
+        p.average_mass = sc.average_mass
+        p.world_bbox_diagonal = float(np.linalg.norm(V.max(0) - V.min(0)))
+        fixed = np.array([int(sum(1 << k for k in range(6) if b.is_dof_fixed[k]))
+                          for b in sc.bodies], dtype=np.int32)
+        keep = [np.ascontiguousarray(sc.mass, np.float64),
+                np.ascontiguousarray(sc.moment.reshape(-1), np.float64), fixed,
+                np.ascontiguousarray(sc.poses(), np.float64),
+                np.ascontiguousarray(sc.velocities(), np.float64),
+                np.ascontiguousarray(np.concatenate([b.Qdot.reshape(-1) for b in sc.bodies]),
+                                     np.float64)]
+        s = L.SimState(*[k.ctypes.data for k in keep])
+        L.check(self.lib.rigc_sim_init(self.h, C.byref(p), C.byref(s)), "rigc_sim_init")
+        self.sim_params = p
+
+    def sim_step(self, num_steps=1):
+        st = L.StepStats()
+        L.check(self.lib.rigc_sim_step(self.h, num_steps, C.byref(st)), "rigc_sim_step")
+        return {f: getattr(st, f) for f, _ in L.StepStats._fields_}
+
+    def sim_state(self):
+        """(poses[nb, 6], velocities[nb, 6], Qdot[nb, 9], barrier stiffness)."""
+        nb = self.scene.num_bodies
+        P = np.empty((nb, 6))
+        V = np.empty((nb, 6))
+        Q = np.empty((nb, 9))
+        k = C.c_double()
+        L.check(self.lib.rigc_sim_get_state(self.h, P.ctypes.data, V.ctypes.data, Q.ctypes.data,
+                                            C.byref(k)), "rigc_sim_get_state")
+        return P, V, Q, k.value
 
     def body_state(self, x_t0=None):
         """Device arrays of the bodies' state at the start of the step."""

@@ -33,7 +33,9 @@ EXPORTS = [
     "rigc_set_constraints", "rigc_barrier_term", "rigc_barrier_local_terms",
     "rigc_narrow_phase_host", "rigc_barrier_local_terms_noalloc", "rigc_body_energy",
     "rigc_friction_setup", "rigc_get_friction", "rigc_friction_term", "rigc_friction_local_terms",
-    "rigc_set_candidates", "rigc_set_ccd_budget",
+    "rigc_set_candidates", "rigc_set_ccd_budget", "rigc_sim_init", "rigc_sim_step",
+    "rigc_sim_get_state", "rigc_ctx_create_batched", "rigc_num_scenes", "rigc_scene_tois",
+    "rigc_scene_barrier_energies",
 ]
 RIGC_ERR_TOO_LARGE = 7
 RIGC_NOALLOC_MAX_BODIES = 4096
@@ -79,6 +81,27 @@ class BarrierOut(C.Structure):
 class FrictionView(C.Structure):
     _fields_ = [("num", C.c_int64), ("mu", C.c_double), ("type", _vp), ("verts", _vp),
                 ("bodies", _vp), ("coef", _vp)]
+
+
+class SimParams(C.Structure):
+    _fields_ = [("timestep", C.c_double), ("gravity", C.c_double * 3), ("dhat", C.c_double),
+                ("dmin", C.c_double), ("coefficient_friction", C.c_double),
+                ("static_friction_speed_bound", C.c_double), ("max_newton_iterations", C.c_int32),
+                ("velocity_conv_tol", C.c_double), ("velocity_conv_tol_abs", C.c_int32),
+                ("line_search_lower_bound", C.c_double), ("dhat_epsilon", C.c_double),
+                ("min_barrier_stiffness_scale", C.c_double), ("average_mass", C.c_double),
+                ("world_bbox_diagonal", C.c_double)]
+
+
+class SimState(C.Structure):
+    _fields_ = [("mass", _vp), ("moment", _vp), ("dof_fixed", _vp), ("poses", _vp),
+                ("velocities", _vp), ("Qdot", _vp)]
+
+
+class StepStats(C.Structure):
+    _fields_ = [("newton_iterations", C.c_int64), ("newton_steps", C.c_int64),
+                ("objective_evals", C.c_int64), ("ccd_calls", C.c_int64),
+                ("cg_iterations", C.c_int64), ("barrier_stiffness", C.c_double)]
 
 
 class Stats(C.Structure):
@@ -130,6 +153,13 @@ def load():
     L.rigc_friction_local_terms.argtypes = [_vp, _vp, C.c_double, C.c_int, _vp, _vp, _vp]
     L.rigc_set_candidates.argtypes = [_vp, C.c_int64, _vp, C.c_int64, _vp]
     L.rigc_set_ccd_budget.argtypes = [_vp, C.c_int64]
+    L.rigc_sim_init.argtypes = [_vp, C.POINTER(SimParams), C.POINTER(SimState)]
+    L.rigc_sim_step.argtypes = [_vp, C.c_int32, C.POINTER(StepStats)]
+    L.rigc_sim_get_state.argtypes = [_vp, _vp, _vp, _vp, _d]
+    L.rigc_ctx_create_batched.argtypes = [C.POINTER(SceneDesc), C.c_int32, _vp, C.POINTER(_vp)]
+    L.rigc_num_scenes.argtypes = [_vp]
+    L.rigc_scene_tois.argtypes = [_vp, _d]
+    L.rigc_scene_barrier_energies.argtypes = [_vp, _d]
     for f in EXPORTS:
         getattr(L, f).restype = C.c_char_p if f == "rigc_status_string" else C.c_int
     _lib = L

@@ -698,3 +698,15 @@ def packed_pile_poses(scene: Scene, seed=0, gap=2e-4, iters=400):
         P[:, 1] = np.maximum(P[:, 1], r + gap)
     x[idx, :3] = P
     return x.reshape(-1)
+
+
+def concat_scenes(scenes):
+    """Independent scenes as one batched scene: (Scene, scene of each body).
+    Bodies keep their group ids (pairs never cross scenes)."""
+    bodies, sob = [], []
+    for k, sc in enumerate(scenes):
+        bodies += list(sc.bodies)
+        sob += [k] * len(sc.bodies)
+    first = scenes[0]
+    return (Scene(bodies=bodies, timestep=first.timestep, dhat=first.dhat, dmin=first.dmin,
+                  gravity=first.gravity, name="batched"), np.array(sob, dtype=np.int32))

@@ -1,0 +1,67 @@
+"""Batched contexts (rigc_ctx_create_batched): independent scenes in one
+context give exactly the per-scene results of one context per scene --
+candidate sets (with index offsets), per-scene earliest times of impact,
+constraint sets, per-scene barrier energies (1e-12: summed in another order)
+and the gradient (bit for bit)."""
+import numpy as np
+import pytest
+
+from conftest import contact_poses
+
+pytestmark = pytest.mark.gpu
+
+DHAT = 1e-3
+
+
+def _scenes():
+    from rigc import scene as S
+
+    out = []
+    for seed in (0, 1, 2):
+        sc = S.scene_from_json(S.spec_cubes(seed))
+        out.append((sc, contact_poses(sc, seed=seed)))
+    return out
+
+
+def test_batched_matches_plain():
+    import rigc
+    from rigc import scene as S
+
+    items = _scenes()
+    big, sob = S.concat_scenes([sc for sc, _ in items])
+    x0 = np.concatenate([x for _, x in items])
+    x1 = np.concatenate([sc.predictor_poses(x) for sc, x in items])
+    cb = rigc.Context(big, scene_of_body=sob)
+    ee_b, fv_b = cb.detect_collision_candidates_rigid(x0, x1, True, 0.0)
+    toi_b = cb.compute_earliest_toi(x0, x1)
+    scene_toi = cb.scene_tois()
+    cs_b = cb.construct_constraint_set(x0, DHAT)
+    e_b, g_b, _ = cb.compute_barrier_term(x0, DHAT)
+    se_b = cb.scene_barrier_energies()
+
+    ee_p, fv_p, tois, grads, energies, ncons = [], [], [], [], [], 0
+    vo = eo = fo = 0
+    for sc, x in items:
+        cp = rigc.Context(sc)
+        x1s = sc.predictor_poses(x)
+        ee, fv = cp.detect_collision_candidates_rigid(x, x1s, True, 0.0)
+        ee_p.append(ee + eo)
+        fv_p.append(fv + np.array([fo, vo]))
+        tois.append(cp.compute_earliest_toi(x, x1s))
+        cs = cp.construct_constraint_set(x, DHAT)
+        ncons += len(cs["type"])
+        e, g, _ = cp.compute_barrier_term(x, DHAT)
+        energies.append(e)
+        grads.append(g)
+        vo += sc.num_vertices
+        eo += len(sc.edges)
+        fo += len(sc.faces)
+    assert len(ee_b) > 0 and len(fv_b) > 0
+    assert np.array_equal(ee_b, np.concatenate(ee_p))
+    assert np.array_equal(fv_b, np.concatenate(fv_p))
+    assert np.array_equal(scene_toi, np.array(tois))
+    assert toi_b == min(tois)
+    assert len(cs_b["type"]) == ncons
+    assert np.array_equal(g_b, np.concatenate(grads))
+    assert np.allclose(se_b, energies, rtol=1e-12, atol=0)
+    assert e_b == pytest.approx(sum(energies), rel=1e-12)
