@@ -33,6 +33,8 @@ extern "C" {
 #define RIGC_ERR_NAN 6            /* non-finite pose input                    */
 #define RIGC_ERR_TOO_LARGE 7      /* input larger than a fixed-capacity entry
                                      point accepts                            */
+#define RIGC_ERR_SOLVE 8          /* the Hessian of the free dofs could not be
+                                     factorised (adjoint)                     */
 
 /* body types (src/physics/rigid_body.hpp RigidBodyType) */
 #define RIGC_BODY_STATIC 0
@@ -295,9 +297,9 @@ int rigc_friction_local_terms(rigc_ctx* ctx, const double* x,
  * solver (src/solvers/ipc_solver.cpp, src/solvers/newton_solver.cpp) for the
  * default settings: implicit Euler, velocity convergence, one friction
  * lagging iteration, no kinematic bodies.  Every term, the CCD line-search
- * filter and the Newton linear solve (block-Jacobi preconditioned conjugate
- * gradients on the block-sparse Hessian, relative residual 1e-12) run on the
- * device; the solver's scalar decisions run on the host.  Field names follow
+ * filter and the Newton linear solve (a dense LDL^T for at most 384 free
+ * dofs, else block-Jacobi preconditioned conjugate gradients on the
+ * block-sparse Hessian, relative residual 1e-12) run on the device; the solver's scalar decisions run on the host.  Field names follow
  * the reference's JSON settings; average_mass and world_bbox_diagonal are the
  * values the problem computes at start-up (RigidBodyAssembler::average_mass,
  * rigid_body_assembler.cpp:104-118; the world bounding-box diagonal,
@@ -317,6 +319,19 @@ typedef struct rigc_sim_params {
     double min_barrier_stiffness_scale; /* 1e11                             */
     double average_mass;
     double world_bbox_diagonal;
+    /* Full Newton steps (unprojected Hessian) after the solver converges,
+     * while they keep contracting and the CCD admits them; 0 (the
+     * reference's solver) by default.  The line search accepts a step only
+     * when the objective decreases, which stalls at |dx| ~ sqrt(eps); the
+     * differentiable rollout needs the solution to the rounding of the
+     * gradient instead. */
+    int32_t newton_polish;
+    /* Bound of the line search's step when the CCD limits it: s * toi with
+     * s in (0, 1] (1: the reference's solver).  s < 1 keeps the first step
+     * into a contact from ending closer than (1 - s) of the gap, below the
+     * rigid CCD's spatial resolution (1e-4 m), where the CCD's conservative
+     * time of impact shrinks every following step. */
+    double ccd_rescale;
 } rigc_sim_params;
 
 /* Bodies' state (host pointers, copied by rigc_sim_init). */
@@ -344,6 +359,29 @@ int rigc_sim_init(rigc_ctx* ctx, const rigc_sim_params* params,
 int rigc_sim_step(rigc_ctx* ctx, int32_t num_steps, rigc_step_stats* stats);
 int rigc_sim_get_state(rigc_ctx* ctx, double* poses, double* velocities,
                        double* Qdot, double* barrier_stiffness);
+
+/* ---- differentiation (new: the reference has no adjoint).
+ * rigc_sim_rollout advances the simulation by num_steps steps like
+ * rigc_sim_step and keeps the state before every checkpoint_every-th step on
+ * the device.  rigc_sim_backward then takes the gradient of a loss with
+ * respect to the state after the rollout (host arrays: poses num_bodies x 6,
+ * velocities num_bodies x 6, Qdot num_bodies x 9; velocities and Qdot may be
+ * NULL for zero) and writes its gradient with respect to the state before
+ * it (host outputs of the same shapes).  Each step is differentiated
+ * implicitly at its converged solution x*: H lambda = dL/dx* on the free
+ * dofs with H the unprojected Hessian of E/m + kappa/m B assembled on the
+ * device, then dL/ds = dL/ds|direct - (1/m) (d2E/dx ds)^T lambda, including
+ * the dependence of the step's initial barrier stiffness on the state.
+ * Steps between checkpoints are recomputed (bit-identical) from the
+ * checkpoint, segment by segment from the last.  Friction is not
+ * differentiated (RIGC_ERR_ARG when coefficient_friction > 0); use
+ * newton_polish > 0 so that each step's gradient vanishes to rounding.
+ * The simulation state is left as it was after the rollout. */
+int rigc_sim_rollout(rigc_ctx* ctx, int32_t num_steps, int32_t checkpoint_every,
+                     rigc_step_stats* stats);
+int rigc_sim_backward(rigc_ctx* ctx, const double* d_poses, const double* d_velocities,
+                      const double* d_Qdot, double* g_poses, double* g_velocities,
+                      double* g_Qdot);
 
 /* ---- one narrow-phase pass from host memory (the call a host Newton loop
  * makes per iteration): copies x0/x1 in, runs compute_earliest_toi(x0, x1)

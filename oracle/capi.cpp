@@ -427,17 +427,15 @@ int orc_friction_term(
 // one simulation step; per-body arrays are updated in place.  params:
 // h, gravity (3), dhat, dmin, mu, epsv, max_newton_iterations,
 // velocity_conv_tol, velocity_conv_tol_abs, line_search_lower_bound,
-// dhat_epsilon, min_barrier_stiffness_scale, bbox_diagonal, average_mass
-// (17 doubles).  stats: newton iterations, newton steps, objective
+// dhat_epsilon, min_barrier_stiffness_scale, bbox_diagonal, average_mass,
+// newton_polish, ccd_rescale (18 doubles).  stats: newton iterations, newton steps, objective
 // evaluations, CCD calls.
-void orc_simulation_step(
-    void* p, const double* mass, const double* moment, double* pose, double* vel,
-    double* Qdot, const int* fixed, const int* type, const double* params, double* kappa,
-    long long* stats)
+static std::vector<BodyState> unpack_bodies(int nb, const double* mass, const double* moment,
+                                            const double* pose, const double* vel,
+                                            const double* Qdot, const int* fixed, const int* type)
 {
-    const Scene& s = static_cast<OwnedScene*>(p)->s;
-    std::vector<BodyState> bodies(s.nb);
-    for (int b = 0; b < s.nb; b++) {
+    std::vector<BodyState> bodies(nb);
+    for (int b = 0; b < nb; b++) {
         BodyState& B = bodies[b];
         B.mass = mass[b];
         for (int i = 0; i < 3; i++) B.moment[i] = moment[3 * b + i];
@@ -449,6 +447,11 @@ void orc_simulation_step(
         for (int i = 0; i < 9; i++) B.Qdot[i] = Qdot[9 * b + i];
         B.type = type[b];
     }
+    return bodies;
+}
+
+static SimParams unpack_params(const double* params)
+{
     SimParams sp;
     sp.h = params[0];
     for (int i = 0; i < 3; i++) sp.gravity[i] = params[1 + i];
@@ -464,8 +467,23 @@ void orc_simulation_step(
     sp.min_barrier_stiffness_scale = params[13];
     sp.bbox_diagonal = params[14];
     sp.average_mass = params[15];
+    sp.newton_polish = (int)params[16];
+    sp.ccd_rescale = params[17];
+    return sp;
+}
+
+// x_out (6 nb) and rec_out (kappa, d kappa / d kappa0) are optional
+void orc_simulation_step_rec(
+    void* p, const double* mass, const double* moment, double* pose, double* vel,
+    double* Qdot, const int* fixed, const int* type, const double* params, double* kappa,
+    long long* stats, double* x_out, double* rec_out)
+{
+    const Scene& s = static_cast<OwnedScene*>(p)->s;
+    std::vector<BodyState> bodies = unpack_bodies(s.nb, mass, moment, pose, vel, Qdot, fixed, type);
+    SimParams sp = unpack_params(params);
     SimStats st;
-    simulation_step(s, bodies, sp, *kappa, &st);
+    StepRecord rec;
+    simulation_step(s, bodies, sp, *kappa, &st, &rec);
     for (int b = 0; b < s.nb; b++) {
         for (int i = 0; i < 6; i++) {
             pose[6 * b + i] = bodies[b].pose_t0[i];
@@ -479,6 +497,50 @@ void orc_simulation_step(
         stats[2] = st.objective_evals;
         stats[3] = st.ccd_calls;
     }
+    if (x_out) std::memcpy(x_out, rec.x.data(), rec.x.size() * sizeof(double));
+    if (rec_out) {
+        rec_out[0] = rec.kappa;
+        rec_out[1] = rec.dkappa_dk0;
+    }
+}
+
+void orc_simulation_step(
+    void* p, const double* mass, const double* moment, double* pose, double* vel,
+    double* Qdot, const int* fixed, const int* type, const double* params, double* kappa,
+    long long* stats)
+{
+    orc_simulation_step_rec(p, mass, moment, pose, vel, Qdot, fixed, type, params, kappa, stats,
+                            nullptr, nullptr);
+}
+
+// adjoint of one step: the start-of-step state (pose, vel, Qdot), the step's
+// solution x (6 nb) and rec (kappa, d kappa / d kappa0); d_* in are the
+// gradients with respect to the state after the step, d_* out (overwritten)
+// those with respect to the state before.  Returns 0, or 1 when the Hessian
+// cannot be factorised.
+int orc_adjoint_step(
+    void* p, const double* mass, const double* moment, const double* pose, const double* vel,
+    const double* Qdot, const int* fixed, const int* type, const double* params,
+    const double* x, const double* rec, const double* d_pose_in, const double* d_vel_in,
+    const double* d_Qdot_in, double* d_pose_out, double* d_vel_out, double* d_Qdot_out)
+{
+    const Scene& s = static_cast<OwnedScene*>(p)->s;
+    const int nb = s.nb;
+    std::vector<BodyState> pre = unpack_bodies(nb, mass, moment, pose, vel, Qdot, fixed, type);
+    SimParams sp = unpack_params(params);
+    StepRecord r;
+    r.x.assign(x, x + 6 * (size_t)nb);
+    r.kappa = rec[0];
+    r.dkappa_dk0 = rec[1];
+    AdjointState in, out;
+    in.pose.assign(d_pose_in, d_pose_in + 6 * (size_t)nb);
+    in.vel.assign(d_vel_in, d_vel_in + 6 * (size_t)nb);
+    in.Qdot.assign(d_Qdot_in, d_Qdot_in + 9 * (size_t)nb);
+    if (!adjoint_step(s, pre, sp, r, in, out)) return 1;
+    std::memcpy(d_pose_out, out.pose.data(), out.pose.size() * sizeof(double));
+    std::memcpy(d_vel_out, out.vel.data(), out.vel.size() * sizeof(double));
+    std::memcpy(d_Qdot_out, out.Qdot.data(), out.Qdot.size() * sizeof(double));
+    return 0;
 }
 
 } // extern "C"

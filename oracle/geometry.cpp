@@ -811,6 +811,56 @@ double body_energy(
     return e.v;
 }
 
+// The same energy over 24 variables: the pose x6 (0-5), the start-of-step
+// pose (6-11), linear velocity (12-14) and Qdot (15-23), for the adjoint of
+// a time step (its mixed block d2E / dx ds and the Hessian at x = pose_t0).
+void body_energy_state_derivs(
+    const BodyState& b, const double* x6, const double gravity[3], double h,
+    double grad[24], double hess[576])
+{
+    using A = D2<24>;
+    A q[6], q0[6], v0[3], Qd[9];
+    for (int i = 0; i < 6; i++) q[i] = A::var(x6[i], i);
+    for (int i = 0; i < 6; i++) q0[i] = A::var(b.pose_t0[i], 6 + i);
+    for (int i = 0; i < 3; i++) v0[i] = A::var(b.vel_t0[i], 12 + i);
+    for (int i = 0; i < 9; i++) Qd[i] = A::var(b.Qdot[i], 15 + i);
+    A e(0.0);
+    bool pos_fixed = b.fixed[0] && b.fixed[1] && b.fixed[2];
+    bool rot_fixed = b.fixed[3] && b.fixed[4] && b.fixed[5];
+    if (b.type == 2) {
+        if (!pos_fixed)
+            for (int i = 0; i < 3; i++) {
+                A hat = q0[i] + h * (v0[i] + h * gravity[i]);
+                e = e + 0.5 * b.mass * (q[i] * q[i]) - b.mass * (q[i] * hat);
+            }
+        if (!rot_fixed) {
+            A Q[9], Q0[9];
+            rotation_matrix_ad<24>(q + 3, Q);
+            rotation_matrix_ad<24>(q0 + 3, Q0);
+            double J[3] = { 0.5 * (-b.moment[0] + b.moment[1] + b.moment[2]),
+                            0.5 * (b.moment[0] - b.moment[1] + b.moment[2]),
+                            0.5 * (b.moment[0] + b.moment[1] - b.moment[2]) };
+            for (int i = 0; i < 3; i++)
+                for (int k = 0; k < 3; k++) {
+                    A t = Q0[3 * i + k] + h * Qd[3 * i + k];
+                    e = e + J[k] * (0.5 * (Q[3 * i + k] * Q[3 * i + k]) - Q[3 * i + k] * t);
+                }
+        }
+    }
+    for (int i = 0; i < 24; i++) grad[i] = e.g[i];
+    for (int i = 0; i < 24; i++)
+        for (int j = 0; j < 24; j++) hess[24 * i + j] = e.h[i][j];
+}
+
+void rotation_matrix_jacobian(const double* theta, double dR[27])
+{
+    D2<3> t[3], R[9];
+    for (int i = 0; i < 3; i++) t[i] = D2<3>::var(theta[i], i);
+    rotation_matrix_ad<3>(t, R);
+    for (int a = 0; a < 3; a++)
+        for (int k = 0; k < 9; k++) dR[9 * a + k] = R[k].g[a];
+}
+
 
 // ---------------------------------------------------------------------------
 // lagged friction (IPC paper, Li et al. 2020 sec. 5, as ipc-toolkit provides

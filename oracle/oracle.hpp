@@ -274,12 +274,40 @@ struct SimParams {
     int velocity_conv_tol_abs;
     double line_search_lower_bound, dhat_epsilon, min_barrier_stiffness_scale;
     double bbox_diagonal, average_mass;
+    int newton_polish = 0;  // full Newton steps after convergence (0: the reference's solver)
+    double ccd_rescale = 1; // step bound s * toi when the CCD limits the step (1: the reference)
 };
 struct SimStats {
     long long newton_iterations = 0, newton_steps = 0, objective_evals = 0, ccd_calls = 0;
 };
+// what the adjoint of a step needs besides the start-of-step state: the
+// solution x (6 nb), the final barrier stiffness, and d kappa / d kappa0
+// (kappa0 = -gE.gB / gB.gB at the start of the step: 2^doublings while
+// kappa0 lies inside its clamp and no doubling reached the cap, else 0)
+struct StepRecord {
+    std::vector<double> x;
+    double kappa = 0, dkappa_dk0 = 0;
+};
 void simulation_step(const Scene& s, std::vector<BodyState>& bodies, const SimParams& p,
-                     double& kappa, SimStats* st);
+                     double& kappa, SimStats* st, StepRecord* rec = nullptr);
+
+// body energy over (x6, pose_t0, linear velocity, Qdot): gradient and Hessian
+// over these 24 variables
+void body_energy_state_derivs(
+    const BodyState& b, const double* x6, const double gravity[3], double h,
+    double grad[24], double hess[576]);
+// dR / dtheta_a (a = 0..2), each row-major 3 x 3
+void rotation_matrix_jacobian(const double* theta, double dR[27]);
+
+// Adjoint of one time step (implicit differentiation of the converged
+// Newton solve): given dL / d(state after the step) in `in` (poses 6 nb,
+// velocities 6 nb, Qdot 9 nb), accumulate dL / d(state before) into `out`.
+// Returns false when the Hessian of the free dofs cannot be factorised.
+struct AdjointState {
+    std::vector<double> pose, vel, Qdot;
+};
+bool adjoint_step(const Scene& s, const std::vector<BodyState>& pre, const SimParams& p,
+                  const StepRecord& rec, const AdjointState& in, AdjointState& out);
 
 // lagged friction constraints and their local terms
 struct FrictionConstraint {

@@ -65,6 +65,10 @@ def lib():
                                         _d, _d, _d, C.c_double, C.c_double, C.c_int, _d, _d, _i,
                                         _i, _d, C.c_longlong, _ll]
         L.orc_simulation_step.argtypes = [C.c_void_p, _d, _d, _d, _d, _d, _i, _i, _d, _d, _ll]
+        L.orc_simulation_step_rec.argtypes = [C.c_void_p, _d, _d, _d, _d, _d, _i, _i, _d, _d, _ll,
+                                              _d, _d]
+        L.orc_adjoint_step.argtypes = [C.c_void_p] + [_d] * 5 + [_i, _i] + [_d] * 9
+        L.orc_adjoint_step.restype = C.c_int
         L.orc_barrier_term.argtypes = [C.c_void_p, _d, C.c_longlong, _i, _i, _i, _i, _d, _d,
                                        C.c_double, C.c_double, C.c_int, _d, _d, _i, _i, _d,
                                        C.c_longlong, _ll]
@@ -383,7 +387,7 @@ def det_cos(x):
 SIM_DEFAULTS = dict(dmin=0.0, mu=0.0, epsv=1e-3, max_newton_iterations=3000,
                     velocity_conv_tol=1e-2, velocity_conv_tol_abs=0,
                     line_search_lower_bound=1e-12, dhat_epsilon=1e-9,
-                    min_barrier_stiffness_scale=1e11)
+                    min_barrier_stiffness_scale=1e11, newton_polish=0, ccd_rescale=1.0)
 
 
 class OracleSim:
@@ -409,6 +413,7 @@ class OracleSim:
         self.bbox_diagonal = float(np.linalg.norm(V.max(0) - V.min(0)))
         self.kappa = C.c_double(1.0)
         self.stats = np.zeros(4, np.int64)
+        self.tape = []
 
     def params(self):
         p = self.p
@@ -416,17 +421,55 @@ class OracleSim:
                     p["max_newton_iterations"], p["velocity_conv_tol"],
                     p["velocity_conv_tol_abs"], p["line_search_lower_bound"],
                     p["dhat_epsilon"], p["min_barrier_stiffness_scale"], self.bbox_diagonal,
-                    self.scene.average_mass, 0.0])
+                    self.scene.average_mass, p["newton_polish"], p["ccd_rescale"]])
 
-    def step(self):
+    def step(self, record=False):
+        """One time step; with record=True the start-of-step state and the
+        step's solution are kept for backward()."""
         prm = self.params()
         st = np.zeros(4, np.int64)
-        lib().orc_simulation_step(self.o.h, _p(self.mass, _d), _p(self.moment, _d),
-                                  _p(self.pose, _d), _p(self.vel, _d), _p(self.Qdot, _d),
-                                  _p(self.fixed, _i), _p(self.type, _i), _p(prm, _d),
-                                  C.byref(self.kappa), st.ctypes.data_as(_ll))
+        if record:
+            pre = (self.pose.copy(), self.vel.copy(), self.Qdot.copy())
+            x = np.empty(len(self.pose))
+            rec = np.empty(2)
+        else:
+            x = rec = None
+        lib().orc_simulation_step_rec(self.o.h, _p(self.mass, _d), _p(self.moment, _d),
+                                      _p(self.pose, _d), _p(self.vel, _d), _p(self.Qdot, _d),
+                                      _p(self.fixed, _i), _p(self.type, _i), _p(prm, _d),
+                                      C.byref(self.kappa), st.ctypes.data_as(_ll),
+                                      None if x is None else _p(x, _d),
+                                      None if rec is None else _p(rec, _d))
+        if record:
+            self.tape.append((pre, x, rec))
         self.stats += st
         return st
+
+    def rollout(self, steps, record=True):
+        self.tape = []
+        for _ in range(steps):
+            self.step(record=record)
+
+    def backward(self, d_pose, d_vel=None, d_Qdot=None):
+        """Gradients of a loss with respect to the state before the recorded
+        steps, from its gradients with respect to the state after them
+        (poses nb x 6, velocities nb x 6, Qdot nb x 9)."""
+        nb = len(self.mass)
+        dp = _dd(np.asarray(d_pose, np.float64).reshape(-1)).copy()
+        dv = np.zeros(6 * nb) if d_vel is None else _dd(np.asarray(d_vel).reshape(-1)).copy()
+        dq = np.zeros(9 * nb) if d_Qdot is None else _dd(np.asarray(d_Qdot).reshape(-1)).copy()
+        prm = self.params()
+        for (pose, vel, Qdot), x, rec in reversed(self.tape):
+            op, ov, oq = np.empty_like(dp), np.empty_like(dv), np.empty_like(dq)
+            rc = lib().orc_adjoint_step(self.o.h, _p(self.mass, _d), _p(self.moment, _d),
+                                        _p(pose, _d), _p(vel, _d), _p(Qdot, _d),
+                                        _p(self.fixed, _i), _p(self.type, _i), _p(prm, _d),
+                                        _p(x, _d), _p(rec, _d), _p(dp, _d), _p(dv, _d), _p(dq, _d),
+                                        _p(op, _d), _p(ov, _d), _p(oq, _d))
+            if rc != 0:
+                raise RuntimeError("adjoint: the Hessian of the free dofs is singular")
+            dp, dv, dq = op, ov, oq
+        return dp.reshape(nb, 6), dv.reshape(nb, 6), dq.reshape(nb, 9)
 
 
 def body_energy(body, x6, gravity, h):

@@ -206,7 +206,7 @@ struct Problem {
 } // namespace
 
 void simulation_step(const Scene& s, std::vector<BodyState>& bodies, const SimParams& p,
-                     double& kappa, SimStats* st)
+                     double& kappa, SimStats* st, StepRecord* rec)
 {
     const int nb = s.nb, N = 6 * nb;
     Problem pr(s, bodies, p, kappa, st);
@@ -224,6 +224,7 @@ void simulation_step(const Scene& s, std::vector<BodyState>& bodies, const SimPa
     }
 
     // IPCSolver::init_solve
+    double dk = 0;  // d kappa / d kappa0
     {
         std::vector<double> gE, gB;
         pr.energy_term(x0, &gE, nullptr);
@@ -245,6 +246,7 @@ void simulation_step(const Scene& s, std::vector<BodyState>& bodies, const SimPa
         }
         double k0 = gg > 0 ? -ge / gg : 1.0;
         pr.kappa = std::min(pr.kappa_max, std::max(kmin, k0));
+        dk = (gg > 0 && k0 > kmin && k0 < pr.kappa_max) ? 1.0 : 0.0;
     }
     double prev_min_distance = pr.min_distance(x0);
 
@@ -310,7 +312,8 @@ void simulation_step(const Scene& s, std::vector<BodyState>& bodies, const SimPa
             double lb = std::min(p.line_search_lower_bound / std::sqrt(std::fabs(gd)), 1e-1);
             std::vector<double> x1(N);
             for (int k = 0; k < N; k++) x1[k] = x[k] + d[k];
-            double tmax = std::min(pr.toi(x.data(), x1.data()), 1.0);
+            double tmax = pr.toi(x.data(), x1.data());
+            tmax = std::min(tmax < 1.0 ? p.ccd_rescale * tmax : tmax, 1.0);
             if (st) st->ccd_calls++;
             alpha = std::min(1.0, tmax);
             while (std::isfinite(lb) && alpha >= lb) {
@@ -333,11 +336,60 @@ void simulation_step(const Scene& s, std::vector<BodyState>& bodies, const SimPa
         // IPCSolver::post_step_update: adaptive stiffness
         double md = pr.min_distance(x.data());
         double eps = p.dhat_epsilon * (p.bbox_diagonal + p.dmin);
-        if (prev_min_distance < eps && md < eps && md < prev_min_distance)
+        if (prev_min_distance < eps && md < eps && md < prev_min_distance) {
+            dk = 2 * pr.kappa < pr.kappa_max ? 2 * dk : 0.0;
             pr.kappa = std::min(pr.kappa_max, 2 * pr.kappa);
+        }
         prev_min_distance = md;
     }
     if (st) st->newton_iterations += it;
+
+    // optional polish (not in the reference): full Newton steps with the
+    // unprojected Hessian while they keep contracting and the CCD admits the
+    // full step.  The line search's test f(x + a d) < f(x) stalls where the
+    // decrease falls below the rounding of f (|dx| ~ sqrt(eps)); these steps
+    // take the solution to the rounding of the gradient instead, which the
+    // adjoint and finite differences of the trajectory need.
+    double prev_step = INFINITY;
+    for (int k = 0; k < p.newton_polish; k++) {
+        std::vector<double> gp, Hp;
+        {
+            const double m = pr.s_average_mass;
+            pr.energy_term(x.data(), &gp, &Hp);
+            for (double& v : gp) v /= m;
+            for (double& v : Hp) v /= m;
+            std::vector<Constraint> cs = pr.constraints(x.data());
+            std::vector<double> gb;
+            BSR hb;
+            barrier_term(s, x.data(), cs, p.dhat, p.dmin, gb, hb, false);
+            for (int i = 0; i < N; i++) gp[i] += pr.kappa / m * gb[i];
+            Problem::add_bsr(hb, N, pr.kappa / m, Hp);
+        }
+        std::vector<double> gf(nf), Hf((size_t)nf * nf), df;
+        for (int i = 0; i < nf; i++) {
+            gf[i] = -gp[free_dof[i]];
+            for (int j = 0; j < nf; j++) Hf[(size_t)i * nf + j] = Hp[(size_t)free_dof[i] * N + free_dof[j]];
+        }
+        if (!ldlt_solve(nf, Hf, gf, df)) break;
+        double step = 0, gd = 0;
+        for (int i = 0; i < nf; i++) {
+            step = std::max(step, std::fabs(df[i]));
+            gd -= gf[i] * df[i];
+        }
+        if (!(step > 0) || gd > 0 || step >= 0.5 * prev_step) break;
+        std::vector<double> x1 = x;
+        for (int i = 0; i < nf; i++) x1[free_dof[i]] += df[i];
+        if (pr.toi(x.data(), x1.data()) < 1.0) break;
+        x = x1;
+        prev_step = step;
+        if (st) st->newton_steps++;
+    }
+
+    if (rec) {
+        rec->x = x;
+        rec->kappa = pr.kappa;
+        rec->dkappa_dk0 = dk;
+    }
 
     // take_step: implicit Euler velocities
     for (int b = 0; b < nb; b++) {
@@ -355,6 +407,157 @@ void simulation_step(const Scene& s, std::vector<BodyState>& bodies, const SimPa
         for (int k = 0; k < 6; k++) B.pose_t0[k] = x[6 * b + k];
     }
     kappa = pr.kappa;
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint of one step (new: the reference has no adjoint).  The step maps the
+// state s = (x0, v, Qdot) to x* = argmin f(x; s) over the free dofs, with
+// f = E(x; s) / m + kappa / m B(x) (no friction), then s' = (x*, (x* - x0) /
+// h, (R(theta*) - R(theta0)) / h).  With the gradient of f zero at x*:
+//   H_FF lambda = dL/dx*_F,   dL/ds = dL/ds|direct - (1/m) E_xs^T lambda,
+// where H is the unprojected Hessian of f at x*; fixed dofs keep x0, so they
+// pass dL/dx*_C - (H lambda)_C back to x0.  The initial stiffness kappa0 =
+// -gE.gB / gB.gB at x0 (inside its clamp) depends on s as well:
+//   dL/dkappa = -(1/m) lambda . gB(x*),
+//   dkappa0/ds = -(1/gB.gB) [P^T (H_B (gE + 2 kappa0 gB) + H_E gB) + E_xs^T gB]
+// at x0 (P: the pose part of s).
+bool adjoint_step(const Scene& s, const std::vector<BodyState>& pre, const SimParams& p,
+                  const StepRecord& rec, const AdjointState& in, AdjointState& out)
+{
+    const int nb = s.nb, N = 6 * nb;
+    const double M = p.average_mass, h = p.h;
+    const double* x = rec.x.data();
+    out.pose.assign(N, 0.0);
+    out.vel.assign(N, 0.0);
+    out.Qdot.assign(9 * (size_t)nb, 0.0);
+    std::vector<double> xbar(N, 0.0);
+    for (int b = 0; b < nb; b++) {
+        const BodyState& B = pre[b];
+        for (int k = 0; k < 6; k++) xbar[6 * b + k] = in.pose[6 * b + k];
+        if (B.type != 2) {
+            for (int k = 0; k < 6; k++) out.vel[6 * b + k] += in.vel[6 * b + k];
+            for (int k = 0; k < 9; k++) out.Qdot[9 * b + k] += in.Qdot[9 * b + k];
+            continue;
+        }
+        for (int k = 0; k < 3; k++) {
+            if (!B.fixed[k]) {
+                xbar[6 * b + k] += in.vel[6 * b + k] / h;
+                out.pose[6 * b + k] -= in.vel[6 * b + k] / h;
+            }
+            out.vel[6 * b + 3 + k] += in.vel[6 * b + 3 + k];  // angular velocity is kept
+        }
+        double dR1[27], dR0[27];
+        rotation_matrix_jacobian(x + 6 * b + 3, dR1);
+        rotation_matrix_jacobian(B.pose_t0 + 3, dR0);
+        for (int a = 0; a < 3; a++) {
+            double s1 = 0, s0 = 0;
+            for (int k = 0; k < 9; k++) {
+                s1 += in.Qdot[9 * b + k] * dR1[9 * a + k];
+                s0 += in.Qdot[9 * b + k] * dR0[9 * a + k];
+            }
+            xbar[6 * b + 3 + a] += s1 / h;
+            out.pose[6 * b + 3 + a] -= s0 / h;
+        }
+    }
+
+    Problem pr(s, pre, p, rec.kappa, nullptr);
+    // unprojected Hessian of f at x*
+    std::vector<double> H((size_t)N * N, 0.0), gBx;
+    for (int b = 0; b < nb; b++) {
+        double g6[6], h36[36];
+        body_energy(pre[b], x + 6 * b, p.gravity, h, g6, h36);
+        for (int r = 0; r < 6; r++)
+            for (int c = 0; c < 6; c++) H[(size_t)(6 * b + r) * N + 6 * b + c] = h36[6 * r + c] / M;
+    }
+    {
+        BSR hb;
+        std::vector<Constraint> cs = pr.constraints(x);
+        barrier_term(s, x, cs, p.dhat, p.dmin, gBx, hb, false);
+        Problem::add_bsr(hb, N, rec.kappa / M, H);
+    }
+    std::vector<int> F;
+    std::vector<char> is_free(N, 0);
+    for (int b = 0; b < nb; b++)
+        for (int k = 0; k < 6; k++)
+            if (!pre[b].fixed[k]) {
+                F.push_back(6 * b + k);
+                is_free[6 * b + k] = 1;
+            }
+    const int nf = (int)F.size();
+    std::vector<double> HF((size_t)nf * nf), rhs(nf), lf;
+    for (int i = 0; i < nf; i++) {
+        rhs[i] = xbar[F[i]];
+        for (int j = 0; j < nf; j++) HF[(size_t)i * nf + j] = H[(size_t)F[i] * N + F[j]];
+    }
+    if (nf > 0 && !ldlt_solve(nf, HF, rhs, lf)) return false;
+    std::vector<double> lam(N, 0.0);
+    for (int i = 0; i < nf; i++) lam[F[i]] = lf[i];
+    // fixed dofs: x*_C = x0_C
+    for (int i = 0; i < N; i++) {
+        if (is_free[i]) continue;
+        double hl = 0;
+        for (int j = 0; j < N; j++) hl += H[(size_t)i * N + j] * lam[j];
+        out.pose[i] += xbar[i] - hl;
+    }
+    // - (1/m) E_xs^T w at pose xe, added to out with a scale
+    auto add_exs = [&](const double* xe, const std::vector<double>& w, double scale) {
+        for (int b = 0; b < nb; b++) {
+            if (pre[b].type != 2) continue;
+            double g24[24];
+            std::vector<double> h24(576);
+            body_energy_state_derivs(pre[b], xe + 6 * b, p.gravity, h, g24, h24.data());
+            for (int j = 6; j < 24; j++) {
+                double acc = 0;
+                for (int i = 0; i < 6; i++) acc += w[6 * b + i] * h24[24 * i + j];
+                acc *= scale;
+                if (j < 12) out.pose[6 * b + j - 6] += acc;
+                else if (j < 15) out.vel[6 * b + j - 12] += acc;
+                else out.Qdot[9 * b + j - 15] += acc;
+            }
+        }
+    };
+    add_exs(x, lam, -1.0 / M);
+
+    // the initial stiffness
+    if (rec.dkappa_dk0 != 0) {
+        double kbar = 0;
+        for (int i = 0; i < N; i++) kbar += lam[i] * gBx[i];
+        kbar *= -rec.dkappa_dk0 / M;
+        if (kbar != 0) {
+            std::vector<double> x0(N);
+            for (int b = 0; b < nb; b++)
+                for (int k = 0; k < 6; k++) x0[6 * b + k] = pre[b].pose_t0[k];
+            std::vector<double> gE(N, 0.0), gB, HE((size_t)N * N, 0.0), HB((size_t)N * N, 0.0);
+            for (int b = 0; b < nb; b++) {
+                if (pre[b].type != 2) continue;
+                double g6[6], h36[36];
+                body_energy(pre[b], &x0[6 * b], p.gravity, h, g6, h36);
+                for (int r = 0; r < 6; r++) {
+                    gE[6 * b + r] = g6[r];
+                    for (int c = 0; c < 6; c++) HE[(size_t)(6 * b + r) * N + 6 * b + c] = h36[6 * r + c];
+                }
+            }
+            BSR hb;
+            std::vector<Constraint> cs = pr.constraints(x0.data());
+            barrier_term(s, x0.data(), cs, p.dhat, p.dmin, gB, hb, false);
+            Problem::add_bsr(hb, N, 1.0, HB);
+            double gg = 0, ge = 0;
+            for (int k = 0; k < N; k++) {
+                gg += gB[k] * gB[k];
+                ge += gB[k] * gE[k];
+            }
+            const double k0 = -ge / gg;
+            const double sc = -kbar / gg;
+            for (int i = 0; i < N; i++) {
+                double u = 0;
+                for (int j = 0; j < N; j++)
+                    u += HB[(size_t)i * N + j] * (gE[j] + 2 * k0 * gB[j]) + HE[(size_t)i * N + j] * gB[j];
+                out.pose[i] += sc * u;
+            }
+            add_exs(x0.data(), gB, sc);
+        }
+    }
+    return true;
 }
 
 } // namespace orc

@@ -28,6 +28,9 @@ int friction_term(Ctx& c, const double* x, double epsvh, int flags, rigc_barrier
 int sim_init(Ctx& c, const rigc_sim_params& p, const rigc_sim_state& s);
 int sim_step(Ctx& c, rigc_step_stats* stats);
 int sim_get_state(Ctx& c, double* poses, double* velocities, double* Qdot, double* kappa);
+int sim_rollout(Ctx& c, int steps, int every, rigc_step_stats* stats);
+int sim_backward(Ctx& c, const double* dp, const double* dv, const double* dq, double* gp,
+                 double* gv, double* gq);
 void sim_release(Ctx& c);
 
 static thread_local std::string g_last_error;
@@ -162,6 +165,7 @@ const char* rigc_status_string(int status)
     case RIGC_ERR_ITER_LIMIT: return "CCD box budget exhausted (conservative result)";
     case RIGC_ERR_NAN: return "non-finite input";
     case RIGC_ERR_TOO_LARGE: return "input exceeds the entry point's fixed capacity";
+    case RIGC_ERR_SOLVE: return "the Hessian of the free dofs could not be factorised";
     default: return "unknown status";
     }
 }
@@ -562,7 +566,8 @@ int rigc_sim_init(rigc_ctx* ctx, const rigc_sim_params* params, const rigc_sim_s
         return RIGC_ERR_ARG;
     const rigc_sim_params& p = *params;
     if (!(p.timestep > 0) || !(p.dhat > 0) || !(p.dmin >= 0) || !(p.average_mass > 0)
-        || !(p.world_bbox_diagonal > 0) || p.max_newton_iterations < 1)
+        || !(p.world_bbox_diagonal > 0) || p.max_newton_iterations < 1 || p.newton_polish < 0
+        || !(p.ccd_rescale > 0 && p.ccd_rescale <= 1))
         return RIGC_ERR_ARG;
     Ctx& c = *ctx_of(ctx);
     for (int i = 0; i < 6 * c.s.nb; i++)
@@ -584,6 +589,23 @@ int rigc_sim_get_state(rigc_ctx* ctx, double* poses, double* velocities, double*
 {
     if (!ctx) return RIGC_ERR_ARG;
     return sim_get_state(*ctx_of(ctx), poses, velocities, Qdot, barrier_stiffness);
+}
+
+int rigc_sim_rollout(rigc_ctx* ctx, int32_t num_steps, int32_t checkpoint_every,
+                     rigc_step_stats* stats)
+{
+    if (!ctx || num_steps < 0 || checkpoint_every < 1) return RIGC_ERR_ARG;
+    Ctx& c = *ctx_of(ctx);
+    if (stats) *stats = rigc_step_stats {};
+    return sim_rollout(c, num_steps, checkpoint_every, stats);
+}
+
+int rigc_sim_backward(rigc_ctx* ctx, const double* d_poses, const double* d_velocities,
+                      const double* d_Qdot, double* g_poses, double* g_velocities, double* g_Qdot)
+{
+    if (!ctx) return RIGC_ERR_ARG;
+    return sim_backward(*ctx_of(ctx), d_poses, d_velocities, d_Qdot, g_poses, g_velocities,
+                        g_Qdot);
 }
 
 int rigc_narrow_phase_host(rigc_ctx* ctx, const double* x0_host, const double* x1_host,

@@ -439,6 +439,155 @@ __global__ void k_scatter_free(int n6, const int* __restrict__ free_idx, const d
     if (i < n6) x[i] = free_idx[i] >= 0 ? xf[free_idx[i]] : 0.0;
 }
 
+// max |v_i| over the vector, as the bits of a non-negative double
+__global__ void k_max_abs(int64_t n, const double* __restrict__ v, unsigned long long* __restrict__ out)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double a = i < n ? fabs(v[i]) : 0.0;
+    for (int o = 16; o > 0; o >>= 1) a = fmax(a, __shfl_xor_sync(0xffffffffu, a, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(a));
+}
+
+// y = H x over every row and column (no fixed-dof masking)
+__global__ void k_hess_rows(HessView H, const double* __restrict__ x, double* __restrict__ y)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 6 * H.nb) return;
+    const int b = i / 6, r = i % 6;
+    double acc = 0;
+    if (H.sE != 0) {
+        const double* Bb = H.body + 36 * (size_t)b + 6 * r;
+        for (int c = 0; c < 6; c++) acc += H.sE * Bb[c] * x[6 * b + c];
+    }
+    if (H.brp)
+        for (int k = H.brp[b]; k < H.brp[b + 1]; k++) {
+            const double* V = H.bval + 36 * (size_t)k + 6 * r;
+            const int cb = H.bcol[k];
+            for (int c = 0; c < 6; c++) acc += H.sB * V[c] * x[6 * cb + c];
+        }
+    y[i] = acc + H.reg * x[i];
+}
+
+// ---------------------------------------------------------------------------
+// adjoint of one time step.  State layout per body: pose [p, theta] (6),
+// velocities [v, omega] (6), Qdot (9); the three arrays are stored one after
+// the other (6 nb, 6 nb, 9 nb).
+
+// the update s' = (x*, (p* - p0) / h, (R(theta*) - R(theta0)) / h) of a
+// dynamic body (the others keep their velocities and Qdot; omega is kept):
+// dL/dx* (xbar) and the direct part of dL/ds (out, overwritten)
+__global__ void k_adj_direct(int nb, const int* __restrict__ type, const int* __restrict__ fixed,
+                             const double* __restrict__ xs, const double* __restrict__ x0,
+                             const double* __restrict__ in, double h, double* __restrict__ xbar,
+                             double* __restrict__ out)
+{
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    const double* ap = in;
+    const double* av = in + 6 * (size_t)nb;
+    const double* aq = in + 12 * (size_t)nb;
+    double* op = out;
+    double* ov = out + 6 * (size_t)nb;
+    double* oq = out + 12 * (size_t)nb;
+    for (int k = 0; k < 6; k++) {
+        xbar[6 * b + k] = ap[6 * b + k];
+        op[6 * b + k] = 0;
+        ov[6 * b + k] = 0;
+    }
+    if (type[b] != RIGC_BODY_DYNAMIC) {
+        for (int k = 0; k < 6; k++) ov[6 * b + k] = av[6 * b + k];
+        for (int k = 0; k < 9; k++) oq[9 * b + k] = aq[9 * b + k];
+        return;
+    }
+    for (int k = 0; k < 9; k++) oq[9 * b + k] = 0;
+    const int fx = fixed[b];
+    for (int k = 0; k < 3; k++) {
+        if (!((fx >> k) & 1)) {
+            xbar[6 * b + k] += av[6 * b + k] / h;
+            op[6 * b + k] = -av[6 * b + k] / h;
+        }
+        ov[6 * b + 3 + k] = av[6 * b + 3 + k];
+    }
+    double F1[kFrameDoubles], F0[kFrameDoubles];
+    const double t1[3] = { xs[6 * b + 3], xs[6 * b + 4], xs[6 * b + 5] };
+    const double t0[3] = { x0[6 * b + 3], x0[6 * b + 4], x0[6 * b + 5] };
+    body_frame(t1, F1);
+    body_frame(t0, F0);
+    for (int a = 0; a < 3; a++) {
+        double s1 = 0, s0 = 0;
+        for (int k = 0; k < 9; k++) {
+            s1 += aq[9 * b + k] * F1[9 + 9 * a + k];
+            s0 += aq[9 * b + k] * F0[9 + 9 * a + k];
+        }
+        xbar[6 * b + 3 + a] += s1 / h;
+        op[6 * b + 3 + a] = -s0 / h;
+    }
+}
+
+// out += alpha (d2E / dx ds)^T w with E the body energy at pose xe and
+// start-of-step state (x0, v0, Qdot0):
+//   d2E/dp dp0 = -m I, d2E/dp dv0 = -m h I,
+//   d2E/dtheta_a dT_ik = -J_k dQ_ik/dtheta_a with T = R(theta0) + h Qdot0
+__global__ void k_adj_exs(int nb, const int* __restrict__ type, const int* __restrict__ fixed,
+                          const double* __restrict__ mass, const double* __restrict__ moment,
+                          const double* __restrict__ xe, const double* __restrict__ x0,
+                          const double* __restrict__ w, double alpha, double h,
+                          double* __restrict__ out)
+{
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb || type[b] != RIGC_BODY_DYNAMIC) return;
+    double* op = out;
+    double* ov = out + 6 * (size_t)nb;
+    double* oq = out + 12 * (size_t)nb;
+    const int fx = fixed[b];
+    const double m = mass[b];
+    if ((fx & 7) != 7)
+        for (int k = 0; k < 3; k++) {
+            op[6 * b + k] -= alpha * m * w[6 * b + k];
+            ov[6 * b + k] -= alpha * m * h * w[6 * b + k];
+        }
+    if ((fx & 56) != 56) {
+        const double* I = moment + 3 * b;
+        const double J[3] = { 0.5 * (-I[0] + I[1] + I[2]), 0.5 * (I[0] - I[1] + I[2]),
+                              0.5 * (I[0] + I[1] - I[2]) };
+        double F[kFrameDoubles], F0[kFrameDoubles];
+        const double te[3] = { xe[6 * b + 3], xe[6 * b + 4], xe[6 * b + 5] };
+        const double t0[3] = { x0[6 * b + 3], x0[6 * b + 4], x0[6 * b + 5] };
+        body_frame(te, F);
+        body_frame(t0, F0);
+        double Tb[9];
+        for (int i = 0; i < 3; i++)
+            for (int k = 0; k < 3; k++) {
+                double acc = 0;
+                for (int a = 0; a < 3; a++) acc += w[6 * b + 3 + a] * F[9 + 9 * a + 3 * i + k];
+                Tb[3 * i + k] = -alpha * J[k] * acc;
+            }
+        for (int e = 0; e < 9; e++) oq[9 * b + e] += h * Tb[e];
+        for (int cc = 0; cc < 3; cc++) {
+            double acc = 0;
+            for (int e = 0; e < 9; e++) acc += Tb[e] * F0[9 + 9 * cc + e];
+            op[6 * b + 3 + cc] += acc;
+        }
+    }
+}
+
+// fixed dofs keep x0: dL/dx0_C += dL/dx*_C - (H lambda)_C
+__global__ void k_adj_fixed(int nb, const int* __restrict__ fixed, const double* __restrict__ xbar,
+                            const double* __restrict__ Hl, double* __restrict__ op)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 6 * nb) return;
+    if ((fixed[i / 6] >> (i % 6)) & 1) op[i] += xbar[i] - Hl[i];
+}
+
+// op += s (u1 + u2) over the poses
+__global__ void k_adj_pose_add(int64_t n, double s, const double* __restrict__ u1,
+                               const double* __restrict__ u2, double* __restrict__ op)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) op[i] += s * (u1[i] + u2[i]);
+}
+
 double barrier_hessian_d(double d, double s)
 {
     if (d <= 0.0 || d >= s) return 0.0;
@@ -462,7 +611,15 @@ struct Sim {
     DevBuf r, z, pp, Ap, Minv, sol, part, scal;         // CG
     DevBuf V0, V1;                                      // world vertices
     double kappa = 1, kappa_max = 0;
+    double dk = 0;  // d kappa / d kappa0 of the current step (0 when kappa0 is clamped)
     std::vector<int> h_fixed;
+    // rollout tape: checkpoints (21 nb doubles each: poses, velocities, Qdot),
+    // the state after the rollout, and one recomputed segment
+    int tape_steps = 0, tape_every = 0;
+    DevBuf ckpt, final_state, seg_pre, seg_x;
+    std::vector<double> seg_kappa, seg_dk;
+    // adjoint vectors: dL/d(state) in and out, dL/dx*, scratch
+    DevBuf adj, adj_out, xbar, u1, u2;
 };
 
 namespace {
@@ -502,7 +659,7 @@ int read_scalars(Ctx& c, const double* dev, double* host, int n)
 }
 
 // objective (and optionally its gradient in S.g and the Hessian pieces)
-int objective(Ctx& c, Sim& S, const double* x, bool grad_hess, Objective& O)
+int objective(Ctx& c, Sim& S, const double* x, bool grad_hess, Objective& O, bool project = true)
 {
     const rigc_sim_params& p = S.p;
     const double m = p.average_mass;
@@ -511,7 +668,7 @@ int objective(Ctx& c, Sim& S, const double* x, bool grad_hess, Objective& O)
     RIGC_TRY(body_energy(c, bs, x, p.gravity, p.timestep, &E, grad_hess ? S.gE.as<double>() : nullptr,
                          grad_hess ? S.hE.as<double>() : nullptr));
     RIGC_TRY(build_constraints(c, x, p.dhat, p.dmin));
-    const int flags = grad_hess ? (RIGC_GRAD | RIGC_HESS | RIGC_PROJECT_PSD) : 0;
+    const int flags = grad_hess ? (RIGC_GRAD | RIGC_HESS | (project ? RIGC_PROJECT_PSD : 0)) : 0;
     RIGC_TRY(barrier_term_impl(c, x, p.dhat, p.dmin, flags, &O.bo));
     double D = 0;
     O.fo = rigc_barrier_out {};
@@ -690,6 +847,17 @@ int max_vertex_move(Ctx& c, Sim& S, const double* x, const double* x1, double* m
     return RIGC_OK;
 }
 
+int max_abs(Ctx& c, Sim& S, const double* v, double* m)
+{
+    const int64_t n = 6 * (int64_t)S.nb;
+    unsigned long long* out = reinterpret_cast<unsigned long long*>(S.scal.as<double>() + 14);
+    RIGC_CUDA(cudaMemsetAsync(out, 0, sizeof(unsigned long long), c.stream));
+    RIGC_COUNT_LAUNCH();
+    k_max_abs<<<grid_for(n, 256), 256, 0, c.stream>>>(n, v, out);
+    RIGC_TRY(read_scalars(c, reinterpret_cast<double*>(out), m, 1));
+    return RIGC_OK;
+}
+
 } // namespace
 
 int sim_init(Ctx& c, const rigc_sim_params& p, const rigc_sim_state& s)
@@ -741,6 +909,8 @@ int sim_init(Ctx& c, const rigc_sim_params& p, const rigc_sim_state& s)
     }
     RIGC_CUDA(cudaStreamSynchronize(st));
     S.kappa = 1;  // m_barrier_stiffness before the first solve
+    S.tape_steps = 0;
+    S.tape_every = 0;
     return RIGC_OK;
 }
 
@@ -785,6 +955,7 @@ int sim_step(Ctx& c, rigc_step_stats* stats)
         S.kappa_max = 100 * kmin;
         const double k0 = gg > 0 ? -ge / gg : 1.0;
         S.kappa = std::min(S.kappa_max, std::max(kmin, k0));
+        S.dk = (gg > 0 && k0 > kmin && k0 < S.kappa_max) ? 1.0 : 0.0;
     }
     double prev_min_distance;
     RIGC_TRY(min_distance(c, S, x0, &prev_min_distance));
@@ -843,7 +1014,7 @@ int sim_step(Ctx& c, rigc_step_stats* stats)
             int s2 = run_ccd(c, x, xt, 1e-4, 0, &toi, nullptr);
             if (s2 != RIGC_OK && s2 != RIGC_ERR_QUEUE_OVERFLOW && s2 != RIGC_ERR_ITER_LIMIT) return s2;
             local.ccd_calls++;
-            alpha = std::min(1.0, std::min(toi, 1.0));
+            alpha = std::min(1.0, toi < 1.0 ? p.ccd_rescale * toi : toi);
             while (std::isfinite(lb) && alpha >= lb) {
                 RIGC_COUNT_LAUNCH();
                 k_axpy<<<grid_for(n, 256), 256, 0, st>>>(n, alpha, dir, x, xt);
@@ -876,11 +1047,45 @@ int sim_step(Ctx& c, rigc_step_stats* stats)
         double md;
         RIGC_TRY(min_distance(c, S, x, &md));
         const double eps = p.dhat_epsilon * (p.world_bbox_diagonal + p.dmin);
-        if (prev_min_distance < eps && md < eps && md < prev_min_distance)
+        if (prev_min_distance < eps && md < eps && md < prev_min_distance) {
+            S.dk = 2 * S.kappa < S.kappa_max ? 2 * S.dk : 0.0;
             S.kappa = std::min(S.kappa_max, 2 * S.kappa);
+        }
         prev_min_distance = md;
     }
     local.newton_iterations = it;
+
+    // optional polish: full Newton steps with the unprojected Hessian while
+    // they keep contracting and the CCD admits the full step (the line
+    // search's decrease test stalls at |dx| ~ sqrt(eps))
+    double prev_step = INFINITY;
+    for (int k = 0; k < p.newton_polish; k++) {
+        Objective O;
+        RIGC_TRY(objective(c, S, x, true, O, false));
+        local.objective_evals++;
+        bool solved;
+        int64_t cgit = 0;
+        HessView H = hess_view(S, O, 0.0);
+        if (S.nfree <= kDenseMax) RIGC_TRY(dense_solve(c, S, H, solved));
+        else RIGC_TRY(pcg(c, S, H, solved, cgit));
+        local.cg_iterations += cgit;
+        if (!solved) break;
+        const double gd = host_dot(c, S, S.g.as<double>(), S.sol.as<double>());
+        double step;
+        RIGC_TRY(max_abs(c, S, S.sol.as<double>(), &step));
+        if (!(step > 0) || gd > 0 || step >= 0.5 * prev_step) break;
+        RIGC_COUNT_LAUNCH();
+        k_axpy<<<grid_for(n, 256), 256, 0, st>>>(n, 1.0, S.sol.as<double>(), x, xt);
+        double toi;
+        RIGC_TRY(detect_and_count(c, x, xt, true, p.dmin / 2.0));
+        int s2 = run_ccd(c, x, xt, 1e-4, 0, &toi, nullptr);
+        if (s2 != RIGC_OK && s2 != RIGC_ERR_QUEUE_OVERFLOW && s2 != RIGC_ERR_ITER_LIMIT) return s2;
+        local.ccd_calls++;
+        if (toi < 1.0) break;
+        RIGC_CUDA(cudaMemcpyAsync(x, xt, n * 8, cudaMemcpyDeviceToDevice, st));
+        prev_step = step;
+        local.newton_steps++;
+    }
 
     // take_step
     RIGC_COUNT_LAUNCH();
@@ -916,6 +1121,193 @@ int sim_get_state(Ctx& c, double* poses, double* velocities, double* Qdot, doubl
     return RIGC_OK;
 }
 
+// ---------------------------------------------------------------------------
+// rollout with checkpoints and its adjoint
+
+namespace {
+
+int save_state(Ctx& c, Sim& S, double* dst)
+{
+    const size_t nb = S.nb;
+    cudaStream_t st = c.stream;
+    RIGC_CUDA(cudaMemcpyAsync(dst, S.x0.ptr, 48 * nb, cudaMemcpyDeviceToDevice, st));
+    RIGC_CUDA(cudaMemcpyAsync(dst + 6 * nb, S.vel.ptr, 48 * nb, cudaMemcpyDeviceToDevice, st));
+    RIGC_CUDA(cudaMemcpyAsync(dst + 12 * nb, S.Qdot.ptr, 72 * nb, cudaMemcpyDeviceToDevice, st));
+    return RIGC_OK;
+}
+
+int load_state(Ctx& c, Sim& S, const double* src)
+{
+    const size_t nb = S.nb;
+    cudaStream_t st = c.stream;
+    RIGC_CUDA(cudaMemcpyAsync(S.x0.ptr, src, 48 * nb, cudaMemcpyDeviceToDevice, st));
+    RIGC_CUDA(cudaMemcpyAsync(S.vel.ptr, src + 6 * nb, 48 * nb, cudaMemcpyDeviceToDevice, st));
+    RIGC_CUDA(cudaMemcpyAsync(S.Qdot.ptr, src + 12 * nb, 72 * nb, cudaMemcpyDeviceToDevice, st));
+    return RIGC_OK;
+}
+
+// S.adj holds dL/d(state after the step); on return it holds dL/d(state
+// before).  pre: the state before the step (21 nb doubles), xs: its
+// solution, kappa / dk: the step's final stiffness and d kappa / d kappa0.
+int adjoint_step(Ctx& c, Sim& S, const double* pre, const double* xs, double kappa, double dk)
+{
+    const rigc_sim_params& p = S.p;
+    const int nb = S.nb;
+    const int64_t n = 6 * (int64_t)nb;
+    const double M = p.average_mass, h = p.timestep;
+    cudaStream_t st = c.stream;
+    const unsigned gb = grid_for(nb, 128), gn = grid_for(n, 256);
+    double* out = S.adj_out.as<double>();
+    double* xbar = S.xbar.as<double>();
+    double* lam = S.sol.as<double>();
+    RIGC_TRY(load_state(c, S, pre));
+    const double* x0 = S.x0.as<double>();
+    RIGC_COUNT_LAUNCH();
+    k_adj_direct<<<gb, 128, 0, st>>>(nb, c.s.type, S.fixed.as<int>(), xs, x0, S.adj.as<double>(), h,
+                                     xbar, out);
+    // unprojected Hessian of E/m + kappa/m B at x*, then H_FF lambda = xbar_F
+    S.kappa = kappa;
+    Objective O;
+    RIGC_TRY(objective(c, S, xs, true, O, false));
+    RIGC_COUNT_LAUNCH();
+    k_axpy<<<gn, 256, 0, st>>>(n, -2.0, xbar, xbar, S.g.as<double>());  // g = -xbar
+    HessView H = hess_view(S, O, 0.0);
+    bool solved;
+    int64_t cgit = 0;
+    if (S.nfree <= kDenseMax) RIGC_TRY(dense_solve(c, S, H, solved));
+    else RIGC_TRY(pcg(c, S, H, solved, cgit));
+    if (!solved) return RIGC_ERR_SOLVE;
+    RIGC_COUNT_LAUNCH();
+    k_hess_rows<<<gn, 256, 0, st>>>(H, lam, S.u1.as<double>());
+    RIGC_COUNT_LAUNCH();
+    k_adj_fixed<<<gn, 256, 0, st>>>(nb, S.fixed.as<int>(), xbar, S.u1.as<double>(), out);
+    RIGC_COUNT_LAUNCH();
+    k_adj_exs<<<gb, 128, 0, st>>>(nb, c.s.type, S.fixed.as<int>(), S.mass.as<double>(),
+                                  S.moment.as<double>(), xs, x0, lam, -1.0 / M, h, out);
+    // the initial stiffness kappa0 = -gE.gB / gB.gB at x0
+    if (dk != 0) {
+        const double kbar = -dk / M * host_dot(c, S, lam, O.bo.grad);
+        if (kbar != 0) {
+            rigc_body_state bs = state_of(S);
+            double E;
+            RIGC_TRY(body_energy(c, bs, x0, p.gravity, h, &E, S.gE.as<double>(), S.hE.as<double>()));
+            RIGC_TRY(build_constraints(c, x0, p.dhat, p.dmin));
+            rigc_barrier_out bo;
+            RIGC_TRY(barrier_term_impl(c, x0, p.dhat, p.dmin, RIGC_GRAD | RIGC_HESS, &bo));
+            double* gB = S.gtmp.as<double>();
+            RIGC_CUDA(cudaMemcpyAsync(gB, bo.grad, n * 8, cudaMemcpyDeviceToDevice, st));
+            const double gg = host_dot(c, S, gB, gB);
+            const double ge = host_dot(c, S, gB, S.gE.as<double>());
+            const double k0 = -ge / gg;
+            const double sc = -kbar / gg;
+            double* w = S.r.as<double>();
+            RIGC_COUNT_LAUNCH();
+            k_axpy<<<gn, 256, 0, st>>>(n, 2 * k0, gB, S.gE.as<double>(), w);
+            HessView HB {};
+            HB.body = S.hE.as<double>();
+            HB.brp = bo.nnzb > 0 ? bo.row_ptr : nullptr;
+            HB.bcol = bo.col;
+            HB.bval = bo.val;
+            HB.sB = 1.0;
+            HB.fixed = S.fixed.as<int>();
+            HB.nb = nb;
+            HessView HE = HB;
+            HE.brp = nullptr;
+            HE.sE = 1.0;
+            RIGC_COUNT_LAUNCH();
+            k_hess_rows<<<gn, 256, 0, st>>>(HB, w, S.u1.as<double>());
+            RIGC_COUNT_LAUNCH();
+            k_hess_rows<<<gn, 256, 0, st>>>(HE, gB, S.u2.as<double>());
+            RIGC_COUNT_LAUNCH();
+            k_adj_pose_add<<<gn, 256, 0, st>>>(n, sc, S.u1.as<double>(), S.u2.as<double>(), out);
+            RIGC_COUNT_LAUNCH();
+            k_adj_exs<<<gb, 128, 0, st>>>(nb, c.s.type, S.fixed.as<int>(), S.mass.as<double>(),
+                                          S.moment.as<double>(), x0, x0, gB, sc, h, out);
+        }
+    }
+    RIGC_CUDA(cudaGetLastError());
+    std::swap(S.adj, S.adj_out);
+    return RIGC_OK;
+}
+
+} // namespace
+
+int sim_rollout(Ctx& c, int steps, int every, rigc_step_stats* stats)
+{
+    if (!c.sim || steps < 0 || every < 1) return RIGC_ERR_ARG;
+    Sim& S = *c.sim;
+    const size_t w = 21 * (size_t)S.nb;
+    const int nck = (steps + every - 1) / every;
+    RIGC_TRY(S.ckpt.reserve((size_t)std::max(nck, 1) * w * sizeof(double)));
+    RIGC_TRY(S.final_state.reserve(w * sizeof(double)));
+    S.tape_steps = 0;
+    for (int k = 0; k < steps; k++) {
+        if (k % every == 0) RIGC_TRY(save_state(c, S, S.ckpt.as<double>() + (size_t)(k / every) * w));
+        RIGC_TRY(sim_step(c, stats));
+    }
+    RIGC_TRY(save_state(c, S, S.final_state.as<double>()));
+    RIGC_CUDA(cudaStreamSynchronize(c.stream));
+    S.tape_steps = steps;
+    S.tape_every = every;
+    return RIGC_OK;
+}
+
+int sim_backward(Ctx& c, const double* dp, const double* dv, const double* dq, double* gp,
+                 double* gv, double* gq)
+{
+    if (!c.sim || !dp || !gp || !gv || !gq) return RIGC_ERR_ARG;
+    Sim& S = *c.sim;
+    if (S.tape_every < 1 || S.p.coefficient_friction > 0) return RIGC_ERR_ARG;
+    const int nb = S.nb, K = S.tape_every, steps = S.tape_steps;
+    const size_t w = 21 * (size_t)nb;
+    cudaStream_t st = c.stream;
+    const size_t vb = w * sizeof(double) + 64;
+    DevBuf* vecs[] = { &S.adj, &S.adj_out, &S.xbar, &S.u1, &S.u2 };
+    for (DevBuf* b : vecs) RIGC_TRY(b->reserve(vb));
+    RIGC_TRY(S.seg_pre.reserve((size_t)K * w * sizeof(double)));
+    RIGC_TRY(S.seg_x.reserve((size_t)K * 6 * nb * sizeof(double)));
+    S.seg_kappa.assign(K, 0.0);
+    S.seg_dk.assign(K, 0.0);
+    double* a = S.adj.as<double>();
+    RIGC_CUDA(cudaMemcpyAsync(a, dp, 48 * (size_t)nb, cudaMemcpyHostToDevice, st));
+    if (dv) RIGC_CUDA(cudaMemcpyAsync(a + 6 * nb, dv, 48 * (size_t)nb, cudaMemcpyHostToDevice, st));
+    else RIGC_CUDA(cudaMemsetAsync(a + 6 * nb, 0, 48 * (size_t)nb, st));
+    if (dq) RIGC_CUDA(cudaMemcpyAsync(a + 12 * nb, dq, 72 * (size_t)nb, cudaMemcpyHostToDevice, st));
+    else RIGC_CUDA(cudaMemsetAsync(a + 12 * nb, 0, 72 * (size_t)nb, st));
+    const double kappa_after = S.kappa;
+    int status = RIGC_OK;
+    for (int seg = (steps + K - 1) / K - 1; seg >= 0 && status == RIGC_OK; seg--) {
+        const int s0 = seg * K, s1 = std::min(steps, s0 + K);
+        // recompute the segment from its checkpoint
+        RIGC_TRY(load_state(c, S, S.ckpt.as<double>() + (size_t)seg * w));
+        for (int j = s0; j < s1; j++) {
+            RIGC_TRY(save_state(c, S, S.seg_pre.as<double>() + (size_t)(j - s0) * w));
+            RIGC_TRY(sim_step(c, nullptr));
+            RIGC_CUDA(cudaMemcpyAsync(S.seg_x.as<double>() + (size_t)(j - s0) * 6 * nb, S.x0.ptr,
+                                      48 * (size_t)nb, cudaMemcpyDeviceToDevice, st));
+            S.seg_kappa[j - s0] = S.kappa;
+            S.seg_dk[j - s0] = S.dk;
+        }
+        for (int j = s1 - 1; j >= s0; j--) {
+            status = adjoint_step(c, S, S.seg_pre.as<double>() + (size_t)(j - s0) * w,
+                                  S.seg_x.as<double>() + (size_t)(j - s0) * 6 * nb,
+                                  S.seg_kappa[j - s0], S.seg_dk[j - s0]);
+            if (status != RIGC_OK) break;
+        }
+    }
+    if (status == RIGC_OK) {
+        a = S.adj.as<double>();
+        RIGC_CUDA(cudaMemcpyAsync(gp, a, 48 * (size_t)nb, cudaMemcpyDeviceToHost, st));
+        RIGC_CUDA(cudaMemcpyAsync(gv, a + 6 * nb, 48 * (size_t)nb, cudaMemcpyDeviceToHost, st));
+        RIGC_CUDA(cudaMemcpyAsync(gq, a + 12 * nb, 72 * (size_t)nb, cudaMemcpyDeviceToHost, st));
+    }
+    // leave the simulation where the rollout ended
+    RIGC_TRY(load_state(c, S, S.final_state.as<double>()));
+    RIGC_CUDA(cudaStreamSynchronize(st));
+    S.kappa = kappa_after;
+    return status;
+}
+
 void sim_release(Ctx& c)
 {
     if (!c.sim) return;
@@ -923,7 +1315,9 @@ void sim_release(Ctx& c)
     DevBuf* bufs[] = { &S.mass, &S.moment, &S.fixed, &S.x0, &S.vel, &S.Qdot, &S.x, &S.xt,
                        &S.dir, &S.g, &S.gE, &S.hE, &S.gtmp, &S.r, &S.z, &S.pp, &S.Ap,
                        &S.Minv, &S.sol, &S.part, &S.scal, &S.V0, &S.V1, &S.free_idx,
-                       &S.dense, &S.dense_b, &S.dense_x, &S.dense_d };
+                       &S.dense, &S.dense_b, &S.dense_x, &S.dense_d, &S.ckpt,
+                       &S.final_state, &S.seg_pre, &S.seg_x, &S.adj, &S.adj_out, &S.xbar,
+                       &S.u1, &S.u2 };
     for (DevBuf* b : bufs) b->release();
     delete c.sim;
     c.sim = nullptr;

@@ -315,8 +315,10 @@ class Context:
                  static_friction_speed_bound=1e-3, max_newton_iterations=3000,
                  velocity_conv_tol=1e-2, velocity_conv_tol_abs=False,
                  line_search_lower_bound=1e-12, dhat_epsilon=1e-9,
-                 min_barrier_stiffness_scale=1e11):
-        """Start a simulation from the scene's poses, velocities and Qdot."""
+                 min_barrier_stiffness_scale=1e11, newton_polish=0, ccd_rescale=1.0,
+                 poses=None, velocities=None, Qdot=None):
+        """Start a simulation from the scene's poses, velocities and Qdot (or
+        from the given host arrays: poses / velocities nb x 6, Qdot nb x 9)."""
         sc = self.scene
         V = sc.world_vertices(sc.poses())
         p = L.SimParams()
@@ -333,14 +335,22 @@ class Context:
         p.min_barrier_stiffness_scale = min_barrier_stiffness_scale
         p.average_mass = sc.average_mass
         p.world_bbox_diagonal = float(np.linalg.norm(V.max(0) - V.min(0)))
+        p.newton_polish = int(newton_polish)
+        p.ccd_rescale = float(ccd_rescale)
         fixed = np.array([int(sum(1 << k for k in range(6) if b.is_dof_fixed[k]))
                           for b in sc.bodies], dtype=np.int32)
+        if Qdot is None:
+            Qdot = np.concatenate([b.Qdot.reshape(-1) for b in sc.bodies])
         keep = [np.ascontiguousarray(sc.mass, np.float64),
                 np.ascontiguousarray(sc.moment.reshape(-1), np.float64), fixed,
-                np.ascontiguousarray(sc.poses(), np.float64),
-                np.ascontiguousarray(sc.velocities(), np.float64),
-                np.ascontiguousarray(np.concatenate([b.Qdot.reshape(-1) for b in sc.bodies]),
-                                     np.float64)]
+                np.ascontiguousarray(sc.poses() if poses is None else poses,
+                                     np.float64).reshape(-1),
+                np.ascontiguousarray(sc.velocities() if velocities is None else velocities,
+                                     np.float64).reshape(-1),
+                np.ascontiguousarray(Qdot, np.float64).reshape(-1)]
+        nb = sc.num_bodies
+        if keep[3].size != 6 * nb or keep[4].size != 6 * nb or keep[5].size != 9 * nb:
+            raise ValueError("sim_init: poses / velocities need nb x 6 values, Qdot nb x 9")
         s = L.SimState(*[k.ctypes.data for k in keep])
         L.check(self.lib.rigc_sim_init(self.h, C.byref(p), C.byref(s)), "rigc_sim_init")
         self.sim_params = p
@@ -349,6 +359,28 @@ class Context:
         st = L.StepStats()
         L.check(self.lib.rigc_sim_step(self.h, num_steps, C.byref(st)), "rigc_sim_step")
         return {f: getattr(st, f) for f, _ in L.StepStats._fields_}
+
+    def sim_rollout(self, num_steps, checkpoint_every=10):
+        """Advance num_steps steps, keeping checkpoints for sim_backward."""
+        st = L.StepStats()
+        L.check(self.lib.rigc_sim_rollout(self.h, num_steps, checkpoint_every, C.byref(st)),
+                "rigc_sim_rollout")
+        return {f: getattr(st, f) for f, _ in L.StepStats._fields_}
+
+    def sim_backward(self, d_poses, d_velocities=None, d_Qdot=None):
+        """Gradients with respect to the state before the last rollout from
+        those with respect to the state after it: (poses nb x 6, velocities
+        nb x 6, Qdot nb x 9)."""
+        nb = self.scene.num_bodies
+        dp = np.ascontiguousarray(d_poses, np.float64).reshape(nb, 6)
+        dv = None if d_velocities is None else np.ascontiguousarray(d_velocities, np.float64).reshape(nb, 6)
+        dq = None if d_Qdot is None else np.ascontiguousarray(d_Qdot, np.float64).reshape(nb, 9)
+        gp, gv, gq = np.empty((nb, 6)), np.empty((nb, 6)), np.empty((nb, 9))
+        L.check(self.lib.rigc_sim_backward(
+            self.h, dp.ctypes.data, None if dv is None else dv.ctypes.data,
+            None if dq is None else dq.ctypes.data, gp.ctypes.data, gv.ctypes.data,
+            gq.ctypes.data), "rigc_sim_backward")
+        return gp, gv, gq
 
     def sim_state(self):
         """(poses[nb, 6], velocities[nb, 6], Qdot[nb, 9], barrier stiffness)."""

@@ -35,9 +35,10 @@ EXPORTS = [
     "rigc_friction_setup", "rigc_get_friction", "rigc_friction_term", "rigc_friction_local_terms",
     "rigc_set_candidates", "rigc_set_ccd_budget", "rigc_sim_init", "rigc_sim_step",
     "rigc_sim_get_state", "rigc_ctx_create_batched", "rigc_num_scenes", "rigc_scene_tois",
-    "rigc_scene_barrier_energies",
+    "rigc_scene_barrier_energies", "rigc_sim_rollout", "rigc_sim_backward",
 ]
 RIGC_ERR_TOO_LARGE = 7
+RIGC_ERR_SOLVE = 8
 RIGC_NOALLOC_MAX_BODIES = 4096
 
 _vp = C.c_void_p
@@ -90,7 +91,8 @@ class SimParams(C.Structure):
                 ("velocity_conv_tol", C.c_double), ("velocity_conv_tol_abs", C.c_int32),
                 ("line_search_lower_bound", C.c_double), ("dhat_epsilon", C.c_double),
                 ("min_barrier_stiffness_scale", C.c_double), ("average_mass", C.c_double),
-                ("world_bbox_diagonal", C.c_double)]
+                ("world_bbox_diagonal", C.c_double), ("newton_polish", C.c_int32),
+                ("ccd_rescale", C.c_double)]
 
 
 class SimState(C.Structure):
@@ -156,6 +158,8 @@ def load():
     L.rigc_sim_init.argtypes = [_vp, C.POINTER(SimParams), C.POINTER(SimState)]
     L.rigc_sim_step.argtypes = [_vp, C.c_int32, C.POINTER(StepStats)]
     L.rigc_sim_get_state.argtypes = [_vp, _vp, _vp, _vp, _d]
+    L.rigc_sim_rollout.argtypes = [_vp, C.c_int32, C.c_int32, C.POINTER(StepStats)]
+    L.rigc_sim_backward.argtypes = [_vp] + [_vp] * 6
     L.rigc_ctx_create_batched.argtypes = [C.POINTER(SceneDesc), C.c_int32, _vp, C.POINTER(_vp)]
     L.rigc_num_scenes.argtypes = [_vp]
     L.rigc_scene_tois.argtypes = [_vp, _d]

@@ -1,0 +1,135 @@
+"""The device adjoint (rigc_sim_rollout / rigc_sim_backward through the C ABI,
+and the torch.autograd.Function over it) against the oracle's adjoint and
+against central finite differences (h = 1e-6) of the oracle's simulator.
+
+Bars: poses after the rollout within 1e-8 of the oracle's; gradients within
+1e-6 (max-norm relative) of the oracle's adjoint and within 1e-5 relative of
+the finite differences along random directions; checkpoint intervals give
+bit-identical gradients (the recomputed segments are bit-identical)."""
+import numpy as np
+import pytest
+
+from test_adjoint_oracle import (DHAT, DIFF, FD_RTOL, G, H, STEPS, TARGET, contact_pair,
+                                 fd_directional, fd_directions, omega_gradient,
+                                 oracle_gradient, oracle_rollout, qdot_of)
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_gradient(sc, steps=STEPS, every=10):
+    """(final poses, dL/d(v, omega) nb x 6, context) through the C ABI."""
+    import rigc
+
+    ctx = rigc.Context(sc)
+    nb = sc.num_bodies
+    poses = sc.poses().reshape(nb, 6)
+    vel = sc.velocities().reshape(nb, 6)
+    ctx.sim_init(H, G, DHAT, poses=poses, velocities=vel, Qdot=qdot_of(poses, vel[:, 3:]), **DIFF)
+    ctx.sim_rollout(steps, every)
+    P, V, Q, _ = ctx.sim_state()
+    dp = np.zeros((nb, 6))
+    dp[0, :3] = 2 * (P[0, :3] - TARGET)
+    gp, gv, gq = ctx.sim_backward(dp)
+    return P, np.concatenate([gv[:, :3], omega_gradient(poses, gq)], 1), ctx
+
+
+@pytest.fixture(scope="module")
+def pair():
+    return contact_pair()
+
+
+@pytest.fixture(scope="module")
+def oracle_pair(oracle, pair):
+    return oracle_gradient(oracle, pair)
+
+
+@pytest.fixture(scope="module")
+def gpu_pair(pair):
+    return gpu_gradient(pair)
+
+
+def test_rollout_matches_oracle(pair, oracle_pair, gpu_pair):
+    L, g_o, sim = oracle_pair
+    P, g, ctx = gpu_pair
+    nb = pair.num_bodies
+    assert np.abs(P - sim.pose.reshape(nb, 6)).max() <= 1e-8
+
+
+def test_gradient_matches_oracle_adjoint(oracle_pair, gpu_pair):
+    _, g_o, _ = oracle_pair
+    _, g, _ = gpu_pair
+    assert np.abs(g - g_o).max() <= 1e-6 * np.abs(g_o).max()
+
+
+def test_gradient_matches_finite_differences(oracle, pair, gpu_pair):
+    _, g, _ = gpu_pair
+    dyn = np.array([b.type == 2 for b in pair.bodies])
+    for d in fd_directions(pair.num_bodies, dyn):
+        ad = float((g * d).sum())
+        fd = fd_directional(oracle, pair, d)
+        assert abs(ad - fd) <= FD_RTOL * abs(fd), (ad, fd)
+
+
+def test_checkpoint_interval_bit_identical(pair, gpu_pair):
+    _, g10, _ = gpu_pair
+    for every in (1, 3):
+        _, g, _ = gpu_gradient(pair, every=every)
+        assert np.array_equal(g, g10)
+
+
+def test_backward_leaves_final_state(pair):
+    P, _, ctx = gpu_gradient(pair)
+    P2, V2, Q2, _ = ctx.sim_state()
+    assert np.array_equal(P, P2)
+    # and a second backward gives the same gradient
+    nb = pair.num_bodies
+    dp = np.zeros((nb, 6))
+    dp[0, :3] = 2 * (P[0, :3] - TARGET)
+    a = ctx.sim_backward(dp)
+    b = ctx.sim_backward(dp)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+
+
+def test_free_fall_closed_form():
+    from rigc import meshes, scene as S
+
+    V, F = meshes.cube()
+    sc = S.Scene(bodies=[S.make_body(V, F, position=(0, 5, 0), linear_velocity=(0.3, 1.0, -0.2))])
+    T = 5
+    P, g, _ = gpu_gradient(sc, steps=T, every=2)
+    assert np.allclose(g[0, :3], 2 * (P[0, :3] - TARGET) * T * H, rtol=1e-12, atol=1e-14)
+    assert np.abs(g[0, 3:]).max() <= 1e-12
+
+
+def test_autograd_function(pair, gpu_pair):
+    """loss.backward() through rigc.adjoint.DifferentiableSimulation gives the
+    C-ABI gradient; omega's gradient flows through qdot_from_omega in torch."""
+    import torch
+
+    from rigc.adjoint import DifferentiableSimulation, qdot_from_omega
+
+    _, g_ref, _ = gpu_pair
+    sim = DifferentiableSimulation(pair, H, G, DHAT, checkpoint_every=10, **DIFF)
+    nb = pair.num_bodies
+    dev = "cuda"
+    poses = torch.as_tensor(pair.poses().reshape(nb, 6), dtype=torch.float64, device=dev)
+    vel0 = pair.velocities().reshape(nb, 6)
+    v = torch.as_tensor(vel0[:, :3], dtype=torch.float64, device=dev).requires_grad_()
+    w = torch.as_tensor(vel0[:, 3:], dtype=torch.float64, device=dev).requires_grad_()
+    P, V, Q = sim(poses, torch.cat([v, w], 1), qdot_from_omega(poses, w), STEPS)
+    loss = ((P[0, :3] - torch.as_tensor(TARGET, dtype=torch.float64, device=dev)) ** 2).sum()
+    loss.backward()
+    g = torch.cat([v.grad, w.grad], 1).cpu().numpy()
+    assert np.abs(g - g_ref).max() <= 1e-10 * np.abs(g_ref).max()
+    assert sim.stats["newton_iterations"] > 0
+
+
+def test_backward_rejects_friction(pair):
+    import rigc
+
+    ctx = rigc.Context(pair)
+    ctx.sim_init(H, G, DHAT, coefficient_friction=0.5, **DIFF)
+    ctx.sim_rollout(1, 1)
+    with pytest.raises(RuntimeError):
+        ctx.sim_backward(np.zeros((pair.num_bodies, 6)))
