@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-sim", action="store_true", help="skip the steps/s measurement")
+    ap.add_argument("--no-adjoint", action="store_true",
+                    help="skip the differentiable rollout measurement")
     ap.add_argument("--sim-steps", type=int, default=20)
     ap.add_argument("--batch-scenes", type=int, default=256,
                     help="scenes of the batched-vs-plain measurement (0 skips it)")
@@ -209,6 +211,58 @@ def sim_rate(args, torch):
             sim.step()
             k += 1
         out["cpu_oracle_steps_per_s"] = k / (time.perf_counter() - t)
+    return out
+
+
+ADJOINT_WORKLOAD = ("64 unit cubes in a 4x4x4 lattice (spacing 1.05 m, seeded rotations, at rest) "
+                    "landing on a static plane; 50 steps of 0.01 s, dhat 1e-3; loss |c0(T) - "
+                    "(3, 0, 0.5)|^2; gradient over the 384 initial linear and angular velocities "
+                    "by the device adjoint (checkpoints every 10 steps)")
+
+
+def adjoint_rate(args, torch):
+    """Forward rollout and adjoint of the differentiation workload through the
+    torch.autograd.Function, and the oracle's rollout + adjoint on the host
+    cores as its baseline."""
+    from rigc import scene as S
+    from rigc.adjoint import DIFF_DEFAULTS, DifferentiableSimulation, qdot_from_omega
+
+    sc = S.scene_from_json(S.spec_cube_lattice(0))
+    nb = sc.num_bodies
+    steps = 50
+    sim = DifferentiableSimulation(sc, 0.01, (0.0, -9.81, 0.0), 1e-3, checkpoint_every=10)
+    dev = dict(dtype=torch.float64, device="cuda")
+    poses = torch.as_tensor(sc.poses().reshape(nb, 6), **dev)
+    vel = torch.as_tensor(sc.velocities().reshape(nb, 6), **dev)
+    v = vel[:, :3].clone().requires_grad_()
+    w = vel[:, 3:].clone().requires_grad_()
+    target = torch.tensor([3.0, 0.0, 0.5], **dev)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    P, _, _ = sim(poses, torch.cat([v, w], 1), qdot_from_omega(poses, w), steps)
+    loss = ((P[0, :3] - target) ** 2).sum()
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    loss.backward()
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    out = {"workload": ADJOINT_WORKLOAD, "parameters": 6 * (nb - 1), "steps": steps,
+           "forward_s": t1 - t0, "backward_s": t2 - t1, "gradients_per_s": 1.0 / (t2 - t0),
+           "newton_iterations": sim.stats["newton_iterations"], "loss": float(loss.detach())}
+    if not args.no_cpu_baseline:
+        import oracle as O
+
+        O.build()
+        osim = O.OracleSim(sc, h=0.01, gravity=(0.0, -9.81, 0.0), dhat=1e-3,
+                           **{k: int(v) if isinstance(v, bool) else v
+                              for k, v in DIFF_DEFAULTS.items()})
+        t = time.perf_counter()
+        osim.rollout(steps, record=True)
+        dp = np.zeros((nb, 6))
+        dp[0, :3] = 2 * (osim.pose.reshape(nb, 6)[0, :3] - np.array([3.0, 0.0, 0.5]))
+        osim.backward(dp)
+        out["cpu_oracle_s"] = time.perf_counter() - t
+        out["cpu_oracle_cores"] = os.cpu_count()
     return out
 
 
@@ -444,6 +498,8 @@ def main():
         line["steps_per_s"] = sim_rate(args, torch)
     if rank == 0 and args.batch_scenes > 0:
         line["batched"] = batched_rate(args, torch)
+    if rank == 0 and not args.no_adjoint:
+        line["adjoint"] = adjoint_rate(args, torch)
     if rank == 0 and not args.no_cpu_baseline:
         base = cpu_baseline(sc, x0, x1, dhat)
         v = combined_rate(n_ccd, n_disc, base["ccd_pairs_per_s"], base["barrier_pairs_per_s"])

@@ -351,6 +351,23 @@ template <class T> static T barrier_t(const T& d, double s)
 double barrier(double d, double s) { return barrier_t<double>(d, s); }
 
 // ---------------------------------------------------------------------------
+// squared distance of two segments by their closest features
+// (ipc-toolkit edge_edge_distance with the type computed)
+double edge_edge_sqdist(const double* a0, const double* a1, const double* b0, const double* b1)
+{
+    switch (edge_edge_distance_type(a0, a1, b0, b1)) {
+    case EE_EA0_EB0: return point_point_sqdist(a0, b0);
+    case EE_EA0_EB1: return point_point_sqdist(a0, b1);
+    case EE_EA1_EB0: return point_point_sqdist(a1, b0);
+    case EE_EA1_EB1: return point_point_sqdist(a1, b1);
+    case EE_EA_EB0: return point_line_sqdist(b0, a0, a1);
+    case EE_EA_EB1: return point_line_sqdist(b1, a0, a1);
+    case EE_EA0_EB: return point_line_sqdist(a0, b0, b1);
+    case EE_EA1_EB: return point_line_sqdist(a1, b0, b1);
+    default: return line_line_sqdist(a0, a1, b0, b1);
+    }
+}
+
 // constraint set from candidates (ipc::construct_constraint_set as called at
 // src/opt/distance_barrier_constraint.cpp:297, V_rest = V)
 
@@ -628,13 +645,46 @@ static AD constraint_potential_ad(const Constraint& c, const AD X[4][3], double 
         break;
     }
     case C_EE: {
-        AD a[3], b[3], n[3], w[3];
-        ad_sub(X[1], X[0], a);
-        ad_sub(X[3], X[2], b);
-        ad_cross(a, b, n);
-        ad_sub(X[2], X[0], w);
-        AD u = ad_dot(n, w);
-        d = (u * u) / ad_dot(n, n);
+        // the closest-feature distance of the two segments: near-parallel
+        // pairs whose closest points are endpoints are kept as (mollified)
+        // EE constraints, so the type is taken at the current positions
+        // (ipc-toolkit EdgeEdgeConstraint: "the distance type is unknown")
+        double P[4][3];
+        for (int i = 0; i < 4; i++)
+            for (int j = 0; j < 3; j++) P[i][j] = X[i][j].v;
+        const int t = edge_edge_distance_type(P[0], P[1], P[2], P[3]);
+        auto pp = [&](int i, int j) {
+            AD w[3];
+            ad_sub(X[i], X[j], w);
+            return ad_dot(w, w);
+        };
+        auto pl = [&](int p, int e0, int e1) {
+            AD a[3], b[3], n[3], e[3];
+            ad_sub(X[e0], X[p], a);
+            ad_sub(X[e1], X[p], b);
+            ad_cross(a, b, n);
+            ad_sub(X[e1], X[e0], e);
+            return ad_dot(n, n) / ad_dot(e, e);
+        };
+        switch (t) {
+        case EE_EA0_EB0: d = pp(0, 2); break;
+        case EE_EA0_EB1: d = pp(0, 3); break;
+        case EE_EA1_EB0: d = pp(1, 2); break;
+        case EE_EA1_EB1: d = pp(1, 3); break;
+        case EE_EA_EB0: d = pl(2, 0, 1); break;
+        case EE_EA_EB1: d = pl(3, 0, 1); break;
+        case EE_EA0_EB: d = pl(0, 2, 3); break;
+        case EE_EA1_EB: d = pl(1, 2, 3); break;
+        default: {
+            AD a[3], b[3], n[3], w[3];
+            ad_sub(X[1], X[0], a);
+            ad_sub(X[3], X[2], b);
+            ad_cross(a, b, n);
+            ad_sub(X[2], X[0], w);
+            AD u = ad_dot(n, w);
+            d = (u * u) / ad_dot(n, n);
+        }
+        }
         break;
     }
     default: {
@@ -942,7 +992,7 @@ void construct_friction_constraints(
             double det = aa * bb - ab * ab;
             f.p0 = (aw * bb - ab * bw) / det;
             f.p1 = (aw * ab - aa * bw) / det;
-            d = line_line_sqdist(a0, a1, b0, b1);
+            d = edge_edge_sqdist(a0, a1, b0, b1);
             cross3(a, b, n);
             for (int i = 0; i < 3; i++) t1[i] = a[i];
             normalize3(t1);
@@ -1134,7 +1184,7 @@ double barrier_energy(const Scene& s, const double* x, const std::vector<Constra
         switch (c.type) {
         case C_VV: d = point_point_sqdist(P(c.v[0]), P(c.v[1])); break;
         case C_EV: d = point_line_sqdist(P(c.v[0]), P(c.v[1]), P(c.v[2])); break;
-        case C_EE: d = line_line_sqdist(P(c.v[0]), P(c.v[1]), P(c.v[2]), P(c.v[3])); break;
+        case C_EE: d = edge_edge_sqdist(P(c.v[0]), P(c.v[1]), P(c.v[2]), P(c.v[3])); break;
         default: d = point_plane_sqdist(P(c.v[0]), P(c.v[1]), P(c.v[2]), P(c.v[3])); break;
         }
         double f = barrier_t<double>(d - dmin * dmin, 2 * dmin * dhat + dhat * dhat);

@@ -203,6 +203,9 @@ int point_triangle_distance_type(const double* p, const double* t0, const double
 int edge_edge_distance_type(const double* ea0, const double* ea1, const double* eb0, const double* eb1);
 double point_point_sqdist(const double* p, const double* q);
 double point_line_sqdist(const double* p, const double* e0, const double* e1);
+// segment-segment squared distance by the closest features (the distance of
+// an EE constraint)
+double edge_edge_sqdist(const double* a0, const double* a1, const double* b0, const double* b1);
 double point_plane_sqdist(const double* p, const double* t0, const double* t1, const double* t2);
 double line_line_sqdist(const double* ea0, const double* ea1, const double* eb0, const double* eb1);
 double ee_cross_sqnorm(const double* ea0, const double* ea1, const double* eb0, const double* eb1);

@@ -49,7 +49,7 @@ double constraint_sqdist(const Constraint& c, const std::vector<double>& V)
     switch (c.type) {
     case C_VV: return point_point_sqdist(P(0), P(1));
     case C_EV: return point_line_sqdist(P(0), P(1), P(2));
-    case C_EE: return line_line_sqdist(P(0), P(1), P(2), P(3));
+    case C_EE: return edge_edge_sqdist(P(0), P(1), P(2), P(3));
     default: return point_plane_sqdist(P(0), P(1), P(2), P(3));
     }
 }

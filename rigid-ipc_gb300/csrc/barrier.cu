@@ -29,6 +29,7 @@
 #include <algorithm>
 
 #include "common.cuh"
+#include "geometry_rn.cuh"
 #include "local_terms.cuh"
 #include "rotation.cuh"
 #include "sort.cuh"
@@ -78,6 +79,210 @@ __device__ __forceinline__ int local_body_of(int type, int i)
     return i == 0 ? 0 : 1;
 }
 
+// H += J_i^T Hb J_j (+ its transpose when i and j are different vertices),
+// J_i = [I | D_i], on the upper triangle
+__device__ __forceinline__ void add_vertex_block(SMat H, const Vtx& Vi, int oi, const Vtx& Vj, int oj,
+                                                 const double (*Hb)[3], bool same_vertex)
+{
+    double HD[3][3], DH[3][3], DHD[3][3];
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) {
+            HD[r][c] = Hb[r][0] * Vj.D[0][c] + Hb[r][1] * Vj.D[1][c] + Hb[r][2] * Vj.D[2][c];
+            DH[r][c] = Vi.D[0][r] * Hb[0][c] + Vi.D[1][r] * Hb[1][c] + Vi.D[2][r] * Hb[2][c];
+        }
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++)
+            DHD[r][c] = Vi.D[0][r] * HD[0][c] + Vi.D[1][r] * HD[1][c] + Vi.D[2][r] * HD[2][c];
+    for (int r = 0; r < 6; r++)
+        for (int c = 0; c < 6; c++) {
+            double v = r < 3 ? (c < 3 ? Hb[r][c] : HD[r][c - 3])
+                             : (c < 3 ? DH[r - 3][c] : DHD[r - 3][c - 3]);
+            int R = oi + r, C = oj + c;
+            if (same_vertex) {
+                if (R <= C) H.at(R, C) += v;
+            } else {
+                if (R <= C) H.at(R, C) += v;
+                if (C <= R) H.at(C, R) += v;
+            }
+        }
+}
+
+// A mollified EE constraint whose closest features are endpoints (kept as EE
+// by the constraint set because the edges are nearly parallel): f = w m(D)
+// b(d - dmin^2) with D = |A x B|^2 of the two edges and d the point-point or
+// point-edge squared distance of the closest features.  Vertex-space
+// gradients and 3x3 Hessian blocks in closed form:
+//   grad D_i = 2 M_i^T n, M_i = alpha_i (-[B]x) + beta_i [A]x,
+//   hess D_ij = 2 M_i^T M_j + 2 (beta_i alpha_j - alpha_i beta_j) [n]x,
+// and the same for N = |a x b|^2 of a point-edge distance d = N / |e|^2;
+// then J^T (.) J and the curvature term into body space.
+static __device__ __noinline__ bool ee_endpoint_build(const BarrierArgs& a, int64_t ci, SMat H,
+                                                      const Vtx* V, const double (*vrest)[3],
+                                                      const int* lbody, const double* const* fr,
+                                                      int dtype)
+{
+    const double weight = a.cweight[ci];
+    int kind = 1, p = 0, q = 0, e0 = 0, e1 = 0;
+    switch (dtype) {
+    case EE_EA0_EB0: kind = 0; p = 0; q = 2; break;
+    case EE_EA0_EB1: kind = 0; p = 0; q = 3; break;
+    case EE_EA1_EB0: kind = 0; p = 1; q = 2; break;
+    case EE_EA1_EB1: kind = 0; p = 1; q = 3; break;
+    case EE_EA_EB0: p = 2; e0 = 0; e1 = 1; break;
+    case EE_EA_EB1: p = 3; e0 = 0; e1 = 1; break;
+    case EE_EA0_EB: p = 0; e0 = 2; e1 = 3; break;
+    default: p = 1; e0 = 2; e1 = 3; break;
+    }
+    const double alD[4] = { -1, 1, 0, 0 }, beD[4] = { 0, 0, -1, 1 };
+    double A[3], B[3], n[3];
+    for (int j = 0; j < 3; j++) {
+        A[j] = V[1].X[j] - V[0].X[j];
+        B[j] = V[3].X[j] - V[2].X[j];
+    }
+    cross(A, B, n);
+    const double Dm = dot(n, n);
+    double gD[4][3], gd[4][3];
+    {
+        double Bn[3], nA[3];
+        cross(B, n, Bn);
+        cross(n, A, nA);
+        for (int i = 0; i < 4; i++)
+            for (int j = 0; j < 3; j++) {
+                gD[i][j] = 2 * (alD[i] * Bn[j] + beD[i] * nA[j]);
+                gd[i][j] = 0;
+            }
+    }
+    double d, N = 0, De = 1;
+    double pa[3], pb[3], c[3], e[3];
+    double alE[4] = { 0, 0, 0, 0 }, beE[4] = { 0, 0, 0, 0 }, gaE[4] = { 0, 0, 0, 0 };
+    double gN[4][3], gE[4][3];
+    if (kind == 0) {
+        double w[3];
+        for (int j = 0; j < 3; j++) w[j] = V[p].X[j] - V[q].X[j];
+        d = dot(w, w);
+        for (int j = 0; j < 3; j++) {
+            gd[p][j] = 2 * w[j];
+            gd[q][j] = -2 * w[j];
+        }
+    } else {
+        alE[p] = -1; alE[e0] = 1; beE[p] = -1; beE[e1] = 1; gaE[e0] = -1; gaE[e1] = 1;
+        for (int j = 0; j < 3; j++) {
+            pa[j] = V[e0].X[j] - V[p].X[j];
+            pb[j] = V[e1].X[j] - V[p].X[j];
+            e[j] = V[e1].X[j] - V[e0].X[j];
+        }
+        cross(pa, pb, c);
+        N = dot(c, c);
+        De = dot(e, e);
+        d = N / De;
+        double bc[3], ca[3];
+        cross(pb, c, bc);
+        cross(c, pa, ca);
+        for (int i = 0; i < 4; i++)
+            for (int j = 0; j < 3; j++) {
+                gN[i][j] = 2 * (alE[i] * bc[j] + beE[i] * ca[j]);
+                gE[i][j] = 2 * gaE[i] * e[j];
+                gd[i][j] = gN[i][j] / De - N / (De * De) * gE[i][j];
+            }
+    }
+    // barrier of the shifted squared distance and the mollifier
+    const double s = 2 * a.dmin * a.dhat + a.dhat * a.dhat;
+    const double dd = d - a.dmin * a.dmin;
+    double bv = 0, b1 = 0, b2 = 0;
+    bool active = dd < s;
+    if (dd <= 0.0) {
+        bv = INFINITY;
+        active = false;
+    } else if (active) {
+        double lg = log(dd / s);
+        double dm = dd - s;
+        bv = -dm * dm * lg;
+        b1 = (s - dd) * (2 * lg - s / dd + 1);
+        double sd = s / dd;
+        b2 = (sd + 2) * sd - 2 * lg - 3;
+    }
+    double m = 1, m1 = 0, m2 = 0;
+    if (Dm < a.ceps[ci]) {
+        double ie = 1.0 / a.ceps[ci];
+        double xe = Dm * ie;
+        m = (2 - xe) * xe;
+        m1 = (2 - 2 * xe) * ie;
+        m2 = -2 * ie * ie;
+    }
+    if (a.energy) a.energy[ci] = weight * m * bv;
+    const bool want_g = (a.flags & (RIGC_GRAD | RIGC_HESS)) != 0;
+    const bool want_h = (a.flags & RIGC_HESS) != 0;
+    if (!active) {
+        if (a.grad)
+            for (int k = 0; k < 12; k++) a.grad[ci * 12 + k] = 0;
+        if (a.blocks && want_h)
+            for (int k = 0; k < 144; k++) a.blocks[ci * 144 + k] = 0;
+        if (a.hess && want_h)
+            for (int k = 0; k < 144; k++) a.hess[ci * 144 + k] = 0;
+        return false;
+    }
+    if (!want_g) return false;
+    double gv[4][3];
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 3; j++) gv[i][j] = weight * (m * b1 * gd[i][j] + bv * m1 * gD[i][j]);
+    double G[12];
+    to_body(V, lbody, 4, gv, G);
+    if (a.grad)
+        for (int k = 0; k < 12; k++) a.grad[ci * 12 + k] = G[k];
+    if (!want_h) return false;
+
+    for (int r = 0; r < 12; r++)
+        for (int cc = r; cc < 12; cc++) H.at(r, cc) = 0;
+    // M_i = alpha_i (-[B]x) + beta_i [A]x (dn/dX_i), C_i likewise for c = a x b
+    auto skew_of = [](double sa, const double* Bv, double sb, const double* Av, double (*M)[3]) {
+        double v0 = -sa * Bv[0] + sb * Av[0], v1 = -sa * Bv[1] + sb * Av[1],
+               v2 = -sa * Bv[2] + sb * Av[2];
+        M[0][0] = 0; M[0][1] = -v2; M[0][2] = v1;
+        M[1][0] = v2; M[1][1] = 0; M[1][2] = -v0;
+        M[2][0] = -v1; M[2][1] = v0; M[2][2] = 0;
+    };
+    for (int i = 0; i < 4; i++)
+        for (int j = i; j < 4; j++) {
+            double Mi[3][3], Mj[3][3], Hb[3][3];
+            skew_of(alD[i], B, beD[i], A, Mi);
+            skew_of(alD[j], B, beD[j], A, Mj);
+            const double kD = 2 * (beD[i] * alD[j] - alD[i] * beD[j]);
+            const double nx[3][3] = { { 0, -n[2], n[1] }, { n[2], 0, -n[0] }, { -n[1], n[0], 0 } };
+            double Ci[3][3], Cj[3][3], kN = 0;
+            const double cx[3][3] = { { 0, -c[2], c[1] }, { c[2], 0, -c[0] }, { -c[1], c[0], 0 } };
+            if (kind == 1) {
+                skew_of(alE[i], pb, beE[i], pa, Ci);
+                skew_of(alE[j], pb, beE[j], pa, Cj);
+                kN = 2 * (beE[i] * alE[j] - alE[i] * beE[j]);
+            }
+            for (int r = 0; r < 3; r++)
+                for (int q2 = 0; q2 < 3; q2++) {
+                    // hess D block
+                    double hD = kD * nx[r][q2];
+                    for (int k = 0; k < 3; k++) hD += 2 * Mi[k][r] * Mj[k][q2];
+                    // hess d block
+                    double hd;
+                    if (kind == 0) {
+                        double si = i == p ? 1.0 : (i == q ? -1.0 : 0.0);
+                        double sj = j == p ? 1.0 : (j == q ? -1.0 : 0.0);
+                        hd = r == q2 ? 2 * si * sj : 0.0;
+                    } else {
+                        double hN = kN * cx[r][q2];
+                        for (int k = 0; k < 3; k++) hN += 2 * Ci[k][r] * Cj[k][q2];
+                        double hE = r == q2 ? 2 * gaE[i] * gaE[j] : 0.0;
+                        hd = hN / De - (gN[i][r] * gE[j][q2] + gE[i][r] * gN[j][q2]) / (De * De)
+                            + 2 * N / (De * De * De) * gE[i][r] * gE[j][q2] - N / (De * De) * hE;
+                    }
+                    Hb[r][q2] = weight * (m * b2 * gd[i][r] * gd[j][q2] + m * b1 * hd
+                                          + m1 * b1 * (gd[i][r] * gD[j][q2] + gD[i][r] * gd[j][q2])
+                                          + bv * m2 * gD[i][r] * gD[j][q2] + bv * m1 * hD);
+                }
+            add_vertex_block(H, V[i], 6 * lbody[i], V[j], 6 * lbody[j], Hb, i == j);
+        }
+    for (int i = 0; i < 4; i++) add_curvature(H, fr[lbody[i]], lbody[i], vrest[i], gv[i]);
+    return true;
+}
+
 // Energy, gradient and (upper triangle of the) unprojected body Hessian of
 // constraint ci into H; returns true when H holds a Hessian to project and
 // write, false when every output of the constraint is already written.
@@ -106,6 +311,11 @@ static __device__ __noinline__ bool barrier_build(const BarrierArgs& a, int64_t 
                 V[i].D[j][k] = dR[3 * j] * v[0] + dR[3 * j + 1] * v[1] + dR[3 * j + 2] * v[2];
             }
         }
+    }
+
+    if (type == 2) {
+        const int dt = ee_type_rn(V[0].X, V[1].X, V[2].X, V[3].X);
+        if (dt != EE_EA_EB) return ee_endpoint_build(a, ci, H, V, vrest, lbody, fr, dt);
     }
 
     // coefficient patterns: A = sum alpha_i X_i, B = sum beta_i X_i, w = sum gamma_i X_i

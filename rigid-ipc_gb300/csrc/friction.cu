@@ -116,7 +116,7 @@ __global__ void k_friction_setup(FrictionSetupArgs a)
         double det = RSUB(RMUL(aa, bb), RMUL(ab, ab));
         p0 = RDIV(RSUB(RMUL(aw, bb), RMUL(ab, bw)), det);
         p1 = RDIV(RSUB(RMUL(aw, ab), RMUL(aa, bw)), det);
-        d = ll_sqdist_rn(P[0], P[1], P[2], P[3]);
+        d = ee_sqdist_rn(P[0], P[1], P[2], P[3]);
         cross3_rn(ea, eb, n);
         for (int j = 0; j < 3; j++) t1[j] = ea[j];
         normalize3_rn(t1);

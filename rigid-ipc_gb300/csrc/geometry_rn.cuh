@@ -172,4 +172,24 @@ __device__ __forceinline__ int ee_type_rn(const double* ea0, const double* ea1,
     return def;
 }
 
+// squared distance of two segments by their closest features: the distance
+// of an EE constraint (ipc-toolkit EdgeEdgeConstraint computes the type at
+// the current positions, since near-parallel pairs whose closest points are
+// endpoints are kept as mollified EE constraints)
+__device__ __forceinline__ double ee_sqdist_rn(const double* a0, const double* a1,
+                                               const double* b0, const double* b1)
+{
+    switch (ee_type_rn(a0, a1, b0, b1)) {
+    case EE_EA0_EB0: return pp_sqdist_rn(a0, b0);
+    case EE_EA0_EB1: return pp_sqdist_rn(a0, b1);
+    case EE_EA1_EB0: return pp_sqdist_rn(a1, b0);
+    case EE_EA1_EB1: return pp_sqdist_rn(a1, b1);
+    case EE_EA_EB0: return pl_sqdist_rn(b0, a0, a1);
+    case EE_EA_EB1: return pl_sqdist_rn(b1, a0, a1);
+    case EE_EA0_EB: return pl_sqdist_rn(a0, b0, b1);
+    case EE_EA1_EB: return pl_sqdist_rn(a1, b0, b1);
+    default: return ll_sqdist_rn(a0, a1, b0, b1);
+    }
+}
+
 } // namespace rigc

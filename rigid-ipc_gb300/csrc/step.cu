@@ -301,7 +301,7 @@ __global__ void k_min_constraint_distance(int64_t n, const int* __restrict__ typ
         }
         if (t == 0) d = pp_sqdist_rn(P[0], P[1]);
         else if (t == 1) d = pl_sqdist_rn(P[0], P[1], P[2]);
-        else if (t == 2) d = ll_sqdist_rn(P[0], P[1], P[2], P[3]);
+        else if (t == 2) d = ee_sqdist_rn(P[0], P[1], P[2], P[3]);
         else d = ptplane_sqdist_rn(P[0], P[1], P[2], P[3]);
     }
     for (int o = 16; o > 0; o >>= 1) d = fmin(d, __shfl_xor_sync(0xffffffffu, d, o));

@@ -23,9 +23,12 @@ import torch
 
 from . import Context
 
-# settings under which each step's gradient vanishes to rounding: tight
-# velocity convergence and full Newton steps after the line search stalls
-DIFF_DEFAULTS = dict(velocity_conv_tol=1e-10, velocity_conv_tol_abs=True, newton_polish=8)
+# settings under which each step converges and its gradient vanishes to
+# rounding: tight velocity convergence, full Newton steps after the line
+# search stalls, and a CCD step bound of 0.8 toi (so the first step into a
+# contact does not end below the rigid CCD's resolution)
+DIFF_DEFAULTS = dict(velocity_conv_tol=1e-10, velocity_conv_tol_abs=True, newton_polish=8,
+                     ccd_rescale=0.8)
 
 
 def hat(w: torch.Tensor) -> torch.Tensor:

@@ -165,6 +165,39 @@ def mass_properties(V, F):
     return mass, c, I
 
 
+def principal_frame(I):
+    """Eigenvalues (ascending) and a rotation whose columns are principal
+    axes of the symmetric inertia tensor I (RigidBody's
+    SelfAdjointEigenSolver, src/physics/rigid_body.cpp:97-117), made the same
+    on every machine: where eigenvalues coincide (within 1e-10 of the
+    largest) the axes are not determined by I, so an isotropic tensor takes
+    the identity and a two-fold degenerate one the distinct axis completed
+    by the world axis least aligned with it; each axis has its largest
+    component positive, and the frame is a rotation (det +1)."""
+    w, R = np.linalg.eigh(I)
+    tol = 1e-10 * max(float(np.abs(w).max()), 1e-300)
+    d01, d12 = w[1] - w[0] <= tol, w[2] - w[1] <= tol
+
+    def canon(v):
+        v = v / np.linalg.norm(v)
+        return v if v[np.argmax(np.abs(v))] > 0 else -v
+
+    if d01 and d12:
+        R = np.eye(3)
+    elif d01 or d12:
+        k = 2 if d01 else 0
+        v = canon(R[:, k])
+        a = np.eye(3)[int(np.argmin(np.abs(v)))]
+        u = canon(a - (a @ v) * v)
+        t = np.cross(v, u)
+        R = np.column_stack([u, t, v]) if d01 else np.column_stack([v, u, t])
+    else:
+        R = np.column_stack([canon(R[:, k]) for k in range(3)])
+    if np.linalg.det(R) < 0:
+        R[:, 0] *= -1.0
+    return w, R
+
+
 # --------------------------------------------------------------------------
 
 @dataclass
@@ -196,7 +229,6 @@ def make_body(vertices, faces, *, position=(0, 0, 0), rotation_deg=(0, 0, 0),
         np.asarray(scale, dtype=np.float64), (3,))
     F = np.asarray(faces, dtype=np.int32)
     R_model = euler_xyz_deg_to_matrix(rotation_deg)
-    V = V @ R_model.T
     E = meshes.edges_from_faces(F)
     F2E = meshes.faces_to_edges(F, E)
     if isinstance(is_dof_fixed, (bool, np.bool_)):
@@ -215,7 +247,8 @@ def make_body(vertices, faces, *, position=(0, 0, 0), rotation_deg=(0, 0, 0),
 
     closed = len(F) >= 4 and btype != BODY_STATIC
     if closed:
-        # centre on the centre of mass (a few passes, as the reference does)
+        # centre on the centre of mass in the model frame, a few passes
+        # (center_vertices, src/physics/rigid_body.cpp:16-43)
         V = V + pos
         pos = np.zeros(3)
         for _ in range(10):
@@ -228,15 +261,15 @@ def make_body(vertices, faces, *, position=(0, 0, 0), rotation_deg=(0, 0, 0),
         mass = vol * density
         thr = np.abs(I).max() * 1e-16
         I = np.where(np.abs(I) > thr, I, 0.0)
-        w, R0 = np.linalg.eigh(I)
+        w, R0 = principal_frame(I)
         moment = density * np.abs(w)
-        if np.linalg.det(R0) < 0:
-            R0[:, 0] *= -1.0
-        theta = matrix_to_rotvec(R0)
+        # R = R_pose R0, vertices V R0, omega = R0^T omega0 (rigid_body.cpp:132-141)
+        theta = matrix_to_rotvec(R_model @ R0)
         V = V @ R0
         vel[3:] = R0.T @ vel[3:]
     else:
         # open or static mesh: keep the model frame, nominal mass properties
+        V = V @ R_model.T
         area = 0.5 * np.linalg.norm(
             np.cross(V[F[:, 1]] - V[F[:, 0]], V[F[:, 2]] - V[F[:, 0]]), axis=1).sum()
         mass = max(area, 1e-12) * density

@@ -10,7 +10,8 @@ import math
 import numpy as np
 import pytest
 
-from test_oracle_pins import EE_Y1, EE_Z, FV_Y, FV_Z1, ee_case, fv_case
+from test_oracle_pins import (EE_Y1, EE_Z, FV_Y, FV_Z1, PARALLEL_CASES, ee_case, fv_case,
+                              parallel_edges)
 
 pytestmark = pytest.mark.gpu
 
@@ -99,6 +100,29 @@ def test_barrier_local_terms(oracle, cube_scene, cube_contact, ctx_c1, project):
         assert abs(e_g[i] - e_o[i]) <= ENERGY_RTOL * abs(e_o[i])
         assert _rel_err(g_g[i], g_o[i]) <= GRAD_RTOL
         assert np.linalg.norm(H_g[i] - H_o[i]) <= HESS_RTOL * np.linalg.norm(H_o[i])
+
+
+@pytest.mark.parametrize("project", [False, True])
+@pytest.mark.parametrize("case", sorted(PARALLEL_CASES))
+def test_barrier_mollified_ee_endpoint(oracle, case, project):
+    """Near-parallel EE constraints whose closest features are endpoints
+    (closest-feature distance with the mollifier) against the oracle."""
+    import rigc
+
+    sc = parallel_edges(PARALLEL_CASES[case])
+    o = oracle.OracleScene(sc)
+    x = np.zeros(12)
+    x[9:12] = [1e-6, -2e-6, 1.5e-6]
+    ee, fv = o.detect_candidates(x, continuous=False, inflation=5e-4)
+    cs = o.constraint_set(x, ee, fv, 1e-3)
+    assert list(cs.types) == [2]
+    ctx = rigc.Context(sc)
+    ctx.set_constraints(cs.types, cs.verts, cs.prims, cs.bodies, cs.weight, cs.eps)
+    e_o, g_o, H_o = o.local_terms(x, cs, 1e-3, project=project)
+    e_g, g_g, H_g = ctx.barrier_local_terms(x, len(cs), 1e-3, project=project)
+    assert abs(e_g[0] - e_o[0]) <= ENERGY_RTOL * abs(e_o[0])
+    assert _rel_err(g_g[0], g_o[0]) <= GRAD_RTOL
+    assert np.linalg.norm(H_g[0] - H_o[0]) <= HESS_RTOL * np.linalg.norm(H_o[0])
 
 
 def test_barrier_term_assembled(oracle, cube_scene, cube_contact, ctx_c1):

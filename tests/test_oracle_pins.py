@@ -282,3 +282,55 @@ def test_hash_grid_equals_brute_force(oracle, cube_scene):
         a = o.detect_candidates(x0, x1, cont, infl)
         b = o.detect_candidates(x0, x1, cont, infl, brute=True)
         assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def parallel_edges(offset, direction=(1.0, 2e-5, 1e-5)):
+    """Two single-edge bodies whose edges are nearly parallel (mollified) and
+    whose closest features are endpoints for the given offset of the second."""
+    from rigc import scene as S
+
+    a = S.raw_body([[0, 0, 0], [1, 0, 0]], edges=[[0, 1]], group_id=0)
+    b = S.raw_body(np.array([[0, 0, 0], direction]) + np.asarray(offset), edges=[[0, 1]],
+                   group_id=1)
+    return S.Scene(bodies=[a, b])
+
+
+PARALLEL_CASES = {"point-point": [1.0004, 3e-4, 0.0], "point-edge": [0.6, 4e-4, 1e-4]}
+
+
+@pytest.mark.parametrize("case", sorted(PARALLEL_CASES))
+def test_mollified_ee_endpoint_distance(oracle, case):
+    """Near-parallel EE pairs whose closest points are endpoints stay EE
+    constraints (mollified); their barrier uses the closest-feature distance,
+    so the energy is continuous as the pair enters the set and its
+    derivatives match finite differences."""
+    sc = parallel_edges(PARALLEL_CASES[case])
+    o = oracle.OracleScene(sc)
+    x = np.zeros(12)
+    x[9:12] = [1e-6, -2e-6, 1.5e-6]
+    ee, fv = o.detect_candidates(x, continuous=False, inflation=5e-4)
+    cs = o.constraint_set(x, ee, fv, 1e-3)
+    assert list(cs.types) == [2]
+    e, g, H = o.local_terms(x, cs, 1e-3, project=False)
+    h = 1e-7
+    for k in range(12):
+        xp, xm = x.copy(), x.copy()
+        xp[k] += h
+        xm[k] -= h
+        ep, gp, _ = o.local_terms(xp, cs, 1e-3, project=False)
+        em, gm, _ = o.local_terms(xm, cs, 1e-3, project=False)
+        assert g[0][k] == pytest.approx((ep[0] - em[0]) / (2 * h), rel=1e-4,
+                                        abs=1e-5 * np.abs(g[0]).max())
+        assert np.allclose(H[0][:, k], (gp[0] - gm[0]) / (2 * h), rtol=1e-4,
+                           atol=1e-5 * np.abs(H[0]).max())
+    # moving the pair apart to the activation distance takes the energy to 0
+    # smoothly: no jump where the segment distance crosses dhat
+    es = []
+    for t in np.linspace(0.0, 1.0, 41):
+        xt = x.copy()
+        xt[7] = t * 1e-3
+        ee, fv = o.detect_candidates(xt, continuous=False, inflation=5e-4)
+        cs_t = o.constraint_set(xt, ee, fv, 1e-3)
+        es.append(o.local_terms(xt, cs_t, 1e-3)[0].sum() if len(cs_t) else 0.0)
+    es = np.array(es)
+    assert es[-1] == 0.0 and np.all(np.diff(es) <= 1e-30)
