@@ -54,6 +54,10 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true",
                     help="skip the differentiable rollout measurement")
     ap.add_argument("--sim-steps", type=int, default=20)
+    ap.add_argument("--batch-sim-steps", type=int, default=2,
+                    help="timed steps of the batched time step (0 skips it)")
+    ap.add_argument("--batch-sim-plain-sample", type=int, default=16,
+                    help="scenes timed one context each for the plain steps/s")
     ap.add_argument("--batch-scenes", type=int, default=256,
                     help="scenes of the batched-vs-plain measurement (0 skips it)")
     return ap.parse_args()
@@ -332,9 +336,56 @@ def batched_rate(args, torch):
         pairs_p += run_pass(c, a, b)
     torch.cuda.synchronize()
     tp = time.perf_counter() - t
-    return {"workload": BATCH_WORKLOAD.format(n=args.batch_scenes), "bodies": big.num_bodies,
-            "pairs_per_pass": pairs_b, "batched_pairs_per_s": pairs_b / tb,
-            "plain_pairs_per_s": pairs_p / tp, "batched_ms": tb * 1e3, "plain_ms": tp * 1e3}
+    out = {"workload": BATCH_WORKLOAD.format(n=args.batch_scenes), "bodies": big.num_bodies,
+           "pairs_per_pass": pairs_b, "batched_pairs_per_s": pairs_b / tb,
+           "plain_pairs_per_s": pairs_p / tp, "batched_ms": tb * 1e3, "plain_ms": tp * 1e3}
+    del ctxs, dev, cb
+    if args.batch_sim_steps > 0:
+        out["sim"] = batched_sim_rate(args, torch, items, big, sob)
+    return out
+
+
+def batched_sim_rate(args, torch, items, big, sob):
+    """Simulated scene-steps per second: every scene from its contact pile
+    with its seeded velocities, one time step (the full IPC Newton solve) per
+    scene per step -- one batched context stepping all scenes at once
+    against one context per scene on a fixed sample of the scenes."""
+    import rigc
+
+    scenes = [sc for sc, _, _ in items]
+    X0 = np.concatenate([x for _, x, _ in items]).reshape(-1, 6)
+    dhat = scenes[0].dhat
+    grav = (0.0, -9.81, 0.0)
+    K = args.batch_sim_steps
+    cb = rigc.Context(big, scene_of_body=sob)
+    cb.sim_init(0.01, grav, dhat, poses=X0)
+    cb.sim_step(1)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    st = cb.sim_step(K)
+    torch.cuda.synchronize()
+    tb = time.perf_counter() - t
+    sample = list(range(0, len(scenes), max(1, len(scenes) // args.batch_sim_plain_sample)))
+    tp, its = 0.0, 0
+    for k in sample:
+        sc, x0, _ = items[k]
+        c = rigc.Context(sc)
+        c.sim_init(0.01, grav, dhat, poses=x0)
+        c.sim_step(1)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        sp = c.sim_step(K)
+        torch.cuda.synchronize()
+        tp += time.perf_counter() - t
+        its += sp["newton_iterations"]
+        del c
+    sb = sum(scenes[k].num_bodies for k in sample)
+    return {"steps": K, "scenes": len(scenes), "batched_scene_steps_per_s": len(scenes) * K / tb,
+            "batched_s_per_step": tb / K,
+            "batched_newton_iterations_per_scene_step": st["newton_iterations"] / (len(scenes) * K),
+            "plain_scene_steps_per_s": len(sample) * K / tp,
+            "plain_sample": f"{len(sample)} of the scenes ({sb} bodies), one context each",
+            "plain_newton_iterations_per_scene_step": its / (len(sample) * K)}
 
 
 def run_reference(args):

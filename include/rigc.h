@@ -360,6 +360,18 @@ int rigc_sim_step(rigc_ctx* ctx, int32_t num_steps, rigc_step_stats* stats);
 int rigc_sim_get_state(rigc_ctx* ctx, double* poses, double* velocities,
                        double* Qdot, double* barrier_stiffness);
 
+/* Batched contexts (rigc_ctx_create_batched): rigc_sim_step advances every
+ * scene as its own problem -- the reference's simulation_step per scene,
+ * with its own barrier stiffness, regularisation, CCD step bound, line
+ * search, convergence and stiffness updates -- while each kernel runs over
+ * all scenes at once; the per-scene linear solves are block-Jacobi PCG.
+ * Friction and newton_polish are not supported there (RIGC_ERR_ARG).  Each
+ * scene's average mass and world bounding-box diagonal (host arrays,
+ * num_scenes values; NULL keeps rigc_sim_params' value) set after
+ * rigc_sim_init. */
+int rigc_sim_scene_params(rigc_ctx* ctx, const double* average_mass,
+                          const double* bbox_diagonal);
+
 /* ---- differentiation (new: the reference has no adjoint).
  * rigc_sim_rollout advances the simulation by num_steps steps like
  * rigc_sim_step and keeps the state before every checkpoint_every-th step on

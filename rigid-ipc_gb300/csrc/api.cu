@@ -29,6 +29,7 @@ int sim_init(Ctx& c, const rigc_sim_params& p, const rigc_sim_state& s);
 int sim_step(Ctx& c, rigc_step_stats* stats);
 int sim_get_state(Ctx& c, double* poses, double* velocities, double* Qdot, double* kappa);
 int sim_rollout(Ctx& c, int steps, int every, rigc_step_stats* stats);
+int sim_scene_params(Ctx& c, const double* average_mass, const double* bbox_diagonal);
 int sim_backward(Ctx& c, const double* dp, const double* dv, const double* dq, double* gp,
                  double* gv, double* gq);
 void sim_release(Ctx& c);
@@ -589,6 +590,12 @@ int rigc_sim_get_state(rigc_ctx* ctx, double* poses, double* velocities, double*
 {
     if (!ctx) return RIGC_ERR_ARG;
     return sim_get_state(*ctx_of(ctx), poses, velocities, Qdot, barrier_stiffness);
+}
+
+int rigc_sim_scene_params(rigc_ctx* ctx, const double* average_mass, const double* bbox_diagonal)
+{
+    if (!ctx) return RIGC_ERR_ARG;
+    return sim_scene_params(*ctx_of(ctx), average_mass, bbox_diagonal);
 }
 
 int rigc_sim_rollout(rigc_ctx* ctx, int32_t num_steps, int32_t checkpoint_every,

@@ -23,8 +23,8 @@
 //    (ipc_solver.cpp:67-89: kappa doubles, up to 100 kappa_min, while the
 //    minimum distance keeps shrinking below dhat_epsilon (bbox + dmin));
 //  * take_step (:488-626): implicit-Euler v and Qdot.
-// The Newton system on the free dofs is factorised densely (LDL^T without
-// pivoting, one block) when it has at most kDenseMax unknowns, else solved by
+// The Newton system on the free dofs is factorised densely (blocked LDL^T
+// without pivoting) when it has at most kDenseMax unknowns, else solved by
 // preconditioned conjugate gradients on the block-sparse Hessian (6x6 blocks:
 // body energy + barrier + friction) with a block-Jacobi preconditioner, to a
 // relative residual of 1e-12.  A failed solve (zero pivot, non-positive
@@ -90,7 +90,31 @@ struct HessView {
     double sE, sB, sD, reg;  // scales and the regularisation c (H + c I)
     const int* fixed;
     int nb;
+    // batched contexts: per-scene scales and regularisation, by body scene
+    // (used instead of sE, sB, sD, reg when bscene is set)
+    const int* bscene = nullptr;
+    const double* scE = nullptr;
+    const double* scB = nullptr;
+    const double* scReg = nullptr;
 };
+
+// the scales of body b's rows: (sE, sB, sD, reg)
+__device__ __forceinline__ void row_scales(const HessView& H, int b, double& sE, double& sB,
+                                           double& sD, double& reg)
+{
+    if (H.bscene) {
+        const int sc = H.bscene[b];
+        sE = H.scE[sc];
+        sB = H.scB[sc];
+        sD = sE;
+        reg = H.scReg[sc];
+    } else {
+        sE = H.sE;
+        sB = H.sB;
+        sD = H.sD;
+        reg = H.reg;
+    }
+}
 
 // y = H x on the free degrees of freedom (fixed rows and columns removed)
 __global__ void k_hess_matvec(HessView H, const double* __restrict__ x, double* __restrict__ y)
@@ -102,22 +126,24 @@ __global__ void k_hess_matvec(HessView H, const double* __restrict__ x, double* 
         y[i] = 0;
         return;
     }
+    double sE, sB, sD, reg;
+    row_scales(H, b, sE, sB, sD, reg);
     double acc = 0;
     const double* Bb = H.body + 36 * (size_t)b + 6 * r;
-    for (int c = 0; c < 6; c++) acc += H.sE * Bb[c] * x[6 * b + c];
+    for (int c = 0; c < 6; c++) acc += sE * Bb[c] * x[6 * b + c];
     if (H.brp)
         for (int k = H.brp[b]; k < H.brp[b + 1]; k++) {
             const double* V = H.bval + 36 * (size_t)k + 6 * r;
             const int cb = H.bcol[k];
-            for (int c = 0; c < 6; c++) acc += H.sB * V[c] * x[6 * cb + c];
+            for (int c = 0; c < 6; c++) acc += sB * V[c] * x[6 * cb + c];
         }
     if (H.frp)
         for (int k = H.frp[b]; k < H.frp[b + 1]; k++) {
             const double* V = H.fval + 36 * (size_t)k + 6 * r;
             const int cb = H.fcol[k];
-            for (int c = 0; c < 6; c++) acc += H.sD * V[c] * x[6 * cb + c];
+            for (int c = 0; c < 6; c++) acc += sD * V[c] * x[6 * cb + c];
         }
-    y[i] = acc + H.reg * x[i];
+    y[i] = acc + reg * x[i];
 }
 
 // inverse of each body's diagonal 6x6 block (free part; fixed rows and
@@ -127,19 +153,21 @@ __global__ void k_block_jacobi(HessView H, double* __restrict__ Minv)
 {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= H.nb) return;
+    double sE, sB, sD, reg;
+    row_scales(H, b, sE, sB, sD, reg);
     double A[36];
-    for (int k = 0; k < 36; k++) A[k] = H.sE * H.body[36 * (size_t)b + k];
+    for (int k = 0; k < 36; k++) A[k] = sE * H.body[36 * (size_t)b + k];
     if (H.brp)
         for (int k = H.brp[b]; k < H.brp[b + 1]; k++)
             if (H.bcol[k] == b)
-                for (int e = 0; e < 36; e++) A[e] += H.sB * H.bval[36 * (size_t)k + e];
+                for (int e = 0; e < 36; e++) A[e] += sB * H.bval[36 * (size_t)k + e];
     if (H.frp)
         for (int k = H.frp[b]; k < H.frp[b + 1]; k++)
             if (H.fcol[k] == b)
-                for (int e = 0; e < 36; e++) A[e] += H.sD * H.fval[36 * (size_t)k + e];
+                for (int e = 0; e < 36; e++) A[e] += sD * H.fval[36 * (size_t)k + e];
     const int fx = H.fixed[b];
     for (int r = 0; r < 6; r++) {
-        A[7 * r] += H.reg;
+        A[7 * r] += reg;
         for (int c = 0; c < 6; c++)
             if (((fx >> r) & 1) || ((fx >> c) & 1)) A[6 * r + c] = r == c ? 1.0 : 0.0;
     }
@@ -374,55 +402,302 @@ __global__ void k_dense_fill(HessView H, const int* __restrict__ free_idx, int n
     row[fi] += H.reg;
 }
 
-// Dense LDL^T (no pivoting) and solve A x = b by one block, left-looking:
-// d_j = a_jj - sum_k l_jk^2 d_k, l_ij = (a_ij - sum_k l_ik l_jk d_k) / d_j,
-// each sum in increasing k by one thread.  flags[0] = 1 on a zero or
-// non-finite pivot.  A's lower triangle is overwritten by L.
-__global__ void __launch_bounds__(256) k_dense_ldlt(double* __restrict__ A, int n,
-                                                    const double* __restrict__ b,
-                                                    double* __restrict__ x, double* __restrict__ D,
-                                                    int* __restrict__ flags)
+// Dense LDL^T (no pivoting) of the free part of the Hessian, blocked: for
+// each panel of kPanel columns, k_ldlt_panel factorises the panel (rows
+// j0..n-1) in shared memory, one column at a time (d_c = a_cc,
+// l_rc = a_rc / d_c, then a_rc' -= l_rc d_c l_c'c within the panel), and
+// k_ldlt_update applies the panel to the trailing lower triangle
+// (A22 -= L21 D L21^T) in 32 x 32 tiles over many CTAs.  k_ldlt_solve then
+// solves L D L^T x = b with blocked forward and backward substitution in one
+// CTA.  flags[0] = 1 on a zero or non-finite pivot or a non-finite solution.
+// A's lower triangle is overwritten by L (unit diagonal implied), D by the
+// pivots.
+constexpr int kPanel = 32;
+constexpr int kPanelStride = kPanel + 1;  // shared-memory row stride (no bank conflicts down a column)
+
+__global__ void __launch_bounds__(512) k_ldlt_panel(double* __restrict__ A, int n, int j0,
+                                                    double* __restrict__ D, int* __restrict__ flags)
 {
-    __shared__ double dj;
-    __shared__ int fail;
-    if (threadIdx.x == 0) fail = 0;
+    extern __shared__ double P[];  // (n - j0) x kPanel, row stride kPanelStride
+    const int m = n - j0, w = min(kPanel, m);
+    if (flags[0]) return;
+    for (int e = threadIdx.x; e < m * w; e += blockDim.x) {
+        const int r = e / w, c = e % w;
+        P[r * kPanelStride + c] = r >= c ? A[(size_t)(j0 + r) * n + j0 + c] : 0.0;
+    }
     __syncthreads();
-    for (int j = 0; j < n; j++) {
-        if (threadIdx.x == 0) {
-            double d = A[(size_t)j * n + j];
-            for (int k = 0; k < j; k++) d -= A[(size_t)j * n + k] * A[(size_t)j * n + k] * D[k];
-            if (!(fabs(d) > 0) || !isfinite(d)) fail = 1;
-            D[j] = d;
-            dj = d;
+    bool bad = false;
+    for (int c = 0; c < w; c++) {
+        const double d = P[c * kPanelStride + c];
+        if (!(fabs(d) > 0) || !isfinite(d)) {
+            bad = true;
+            break;
         }
+        for (int r = c + 1 + threadIdx.x; r < m; r += blockDim.x) P[r * kPanelStride + c] /= d;
         __syncthreads();
-        if (fail) break;
-        for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x) {
-            double s = A[(size_t)i * n + j];
-            for (int k = 0; k < j; k++) s -= A[(size_t)i * n + k] * A[(size_t)j * n + k] * D[k];
-            A[(size_t)i * n + j] = s / dj;
+        // a_rc' -= l_rc d l_c'c for c < c' <= r
+        const int cols = w - c - 1;
+        for (int e = threadIdx.x; e < (m - c - 1) * cols; e += blockDim.x) {
+            const int r = c + 1 + e / cols, cc = c + 1 + e % cols;
+            if (cc <= r) P[r * kPanelStride + cc] -= P[r * kPanelStride + c] * d * P[cc * kPanelStride + c];
         }
         __syncthreads();
     }
-    if (fail) {
+    if (bad) {
         if (threadIdx.x == 0) flags[0] = 1;
         return;
     }
-    if (threadIdx.x == 0) {
-        for (int i = 0; i < n; i++) {
-            double s = b[i];
-            for (int k = 0; k < i; k++) s -= A[(size_t)i * n + k] * x[k];
-            x[i] = s;
-        }
-        for (int i = 0; i < n; i++) x[i] /= D[i];
-        for (int i = n - 1; i >= 0; i--) {
-            double s = x[i];
-            for (int k = i + 1; k < n; k++) s -= A[(size_t)k * n + i] * x[k];
-            x[i] = s;
-        }
-        for (int i = 0; i < n; i++)
-            if (!isfinite(x[i])) flags[0] = 1;
+    for (int e = threadIdx.x; e < m * w; e += blockDim.x) {
+        const int r = e / w, c = e % w;
+        if (r > c) A[(size_t)(j0 + r) * n + j0 + c] = P[r * kPanelStride + c];
+        else if (r == c) D[j0 + c] = P[r * kPanelStride + c];
     }
+}
+
+// A[i][k] -= sum_c L[i][c] D[c] L[k][c] over the panel columns c, for the
+// trailing lower triangle i >= k >= j0 + w; one 32 x 32 tile per CTA
+__global__ void __launch_bounds__(256) k_ldlt_update(double* __restrict__ A, int n, int j0, int w,
+                                                     const double* __restrict__ D,
+                                                     const int* __restrict__ flags)
+{
+    if (flags[0]) return;
+    // tile (bi, bk), bi >= bk, from the linear block index
+    const int t = blockIdx.x;
+    int bi = (int)((sqrt(8.0 * t + 1.0) - 1.0) * 0.5);
+    while ((bi + 1) * (bi + 2) / 2 <= t) bi++;
+    while (bi * (bi + 1) / 2 > t) bi--;
+    const int bk = t - bi * (bi + 1) / 2;
+    const int base = j0 + w;
+    const int i0 = base + 32 * bi, k0 = base + 32 * bk;
+    __shared__ double Li[32][kPanel + 1], Lk[32][kPanel + 1], d[kPanel];
+    for (int e = threadIdx.x; e < 32 * kPanel; e += blockDim.x) {
+        const int r = e / kPanel, c = e % kPanel;
+        Li[r][c] = (i0 + r < n && c < w) ? A[(size_t)(i0 + r) * n + j0 + c] : 0.0;
+        Lk[r][c] = (k0 + r < n && c < w) ? A[(size_t)(k0 + r) * n + j0 + c] : 0.0;
+    }
+    if (threadIdx.x < kPanel) d[threadIdx.x] = threadIdx.x < w ? D[j0 + threadIdx.x] : 0.0;
+    __syncthreads();
+    for (int e = threadIdx.x; e < 32 * 32; e += blockDim.x) {
+        const int r = e / 32, q = e % 32;
+        const int i = i0 + r, k = k0 + q;
+        if (i >= n || k >= n || k > i) continue;
+        double acc = 0;
+        for (int c = 0; c < w; c++) acc += Li[r][c] * d[c] * Lk[q][c];
+        A[(size_t)i * n + k] -= acc;
+    }
+}
+
+// L D L^T x = b by blocks of 32: y = L^-1 b, y /= D, x = L^-T y
+__global__ void __launch_bounds__(256) k_ldlt_solve(const double* __restrict__ A, int n,
+                                                    const double* __restrict__ D,
+                                                    const double* __restrict__ b,
+                                                    double* __restrict__ x, int* __restrict__ flags)
+{
+    if (flags[0]) return;
+    __shared__ double Lb[32][33];  // the diagonal block of the current block row
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = b[i];
+    __syncthreads();
+    // forward: rows of block [b0, b0 + 32) minus the solved columns [0, b0)
+    for (int b0 = 0; b0 < n; b0 += 32) {
+        const int nb = min(32, n - b0);
+        for (int r = warp; r < nb; r += 8) {
+            double acc = 0;
+            for (int k = lane; k < b0; k += 32) acc += A[(size_t)(b0 + r) * n + k] * x[k];
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0) x[b0 + r] -= acc;
+        }
+        for (int e = threadIdx.x; e < nb * 32; e += blockDim.x) {
+            const int r = e / 32, q = e % 32;
+            Lb[r][q] = q < nb ? A[(size_t)(b0 + r) * n + b0 + q] : 0.0;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            double y = lane < nb ? x[b0 + lane] : 0.0;
+            for (int r = 1; r < nb; r++) {
+                const double yr = __shfl_sync(0xffffffffu, y, r - 1);
+                // lanes >= r subtract column r - 1
+                if (lane >= r && lane < nb) y -= Lb[lane][r - 1] * yr;
+            }
+            if (lane < nb) x[b0 + lane] = y;
+        }
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] /= D[i];
+    __syncthreads();
+    // backward: block [b0, b0 + 32) minus the solved rows [b0 + 32, n)
+    for (int b0 = ((n - 1) / 32) * 32; b0 >= 0; b0 -= 32) {
+        const int nb = min(32, n - b0);
+        for (int r = warp; r < nb; r += 8) {
+            double acc = 0;
+            for (int k = b0 + 32 + lane; k < n; k += 32) acc += A[(size_t)k * n + b0 + r] * x[k];
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0) x[b0 + r] -= acc;
+        }
+        for (int e = threadIdx.x; e < nb * 32; e += blockDim.x) {
+            const int r = e / 32, q = e % 32;
+            Lb[r][q] = q < nb ? A[(size_t)(b0 + r) * n + b0 + q] : 0.0;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            double y = lane < nb ? x[b0 + lane] : 0.0;
+            for (int r = nb - 1; r > 0; r--) {
+                const double yr = __shfl_sync(0xffffffffu, y, r);
+                // lanes < r subtract row r's entry in their column
+                if (lane < r) y -= Lb[r][lane] * yr;
+            }
+            if (lane < nb) x[b0 + lane] = y;
+        }
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        if (!isfinite(x[i])) flags[0] = 1;
+}
+
+// ---------------------------------------------------------------------------
+// per-scene kernels of batched contexts (bodies ordered by scene)
+
+// out[s] = sum over scene s's dofs of a[i] b[i] (b null: sum of a), one block
+// per scene, in a fixed order
+__global__ void __launch_bounds__(256) k_seg_dot(const int* __restrict__ scene_bstart, int per_body,
+                                                 const double* __restrict__ a,
+                                                 const double* __restrict__ b,
+                                                 double* __restrict__ out)
+{
+    __shared__ double sh[256];
+    const int sc = blockIdx.x;
+    const int64_t lo = (int64_t)scene_bstart[sc] * per_body, hi = (int64_t)scene_bstart[sc + 1] * per_body;
+    double acc = 0;
+    for (int64_t i = lo + threadIdx.x; i < hi; i += 256) acc += b ? a[i] * b[i] : a[i];
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[sc] = sh[0];
+}
+
+// g = gE / m_s + (kappa_s / m_s) gB, zero on fixed dofs
+__global__ void k_combine_grad_sc(int nb, const double* __restrict__ gE, const double* __restrict__ gB,
+                                  const int* __restrict__ bscene, const double* __restrict__ scE,
+                                  const double* __restrict__ scB, const int* __restrict__ fixed,
+                                  double* __restrict__ g)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 6 * nb) return;
+    const int b = i / 6, sc = bscene[b];
+    double v = scE[sc] * gE[i];
+    if (gB) v += scB[sc] * gB[i];
+    g[i] = ((fixed[b] >> (i % 6)) & 1) ? 0.0 : v;
+}
+
+// out = y + alpha_s x (per-scene alpha)
+__global__ void k_axpy_sc(int nb, const int* __restrict__ bscene, const double* __restrict__ alpha,
+                          const double* __restrict__ x, const double* __restrict__ y,
+                          double* __restrict__ out)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < 6 * nb) out[i] = y[i] + alpha[bscene[i / 6]] * x[i];
+}
+
+// CG per scene: flags[2 s] breakdown, flags[2 s + 1] converged (scenes that
+// are not solved start converged and keep alpha = 0)
+__global__ void k_cg_alpha_sc(int ns, const double* __restrict__ rz, const double* __restrict__ pAp,
+                              const double* __restrict__ rr, const double* __restrict__ tol2,
+                              double* __restrict__ alpha, int* __restrict__ flags)
+{
+    int sc = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sc >= ns) return;
+    int* f = flags + 2 * sc;
+    if (f[0] || f[1] || rr[sc] <= tol2[sc]) {
+        if (!f[0]) f[1] = 1;
+        alpha[sc] = 0;
+        return;
+    }
+    const double d = pAp[sc];
+    if (!(d > 0) || !isfinite(d)) {
+        f[0] = 1;
+        alpha[sc] = 0;
+    } else {
+        alpha[sc] = rz[sc] / d;
+    }
+}
+
+__global__ void k_cg_update_sc(int nb, const int* __restrict__ bscene, const double* __restrict__ alpha,
+                               const double* __restrict__ p, const double* __restrict__ Ap,
+                               double* __restrict__ x, double* __restrict__ r)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 6 * nb) return;
+    const double a = alpha[bscene[i / 6]];
+    if (a == 0) return;
+    x[i] += a * p[i];
+    r[i] -= a * Ap[i];
+}
+
+__global__ void k_cg_direction_sc(int nb, const int* __restrict__ bscene,
+                                  const double* __restrict__ rz_new, const double* __restrict__ rz_old,
+                                  const double* __restrict__ z, const int* __restrict__ flags,
+                                  double* __restrict__ p)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 6 * nb) return;
+    const int sc = bscene[i / 6];
+    if (flags[2 * sc] || flags[2 * sc + 1]) return;
+    p[i] = z[i] + (rz_new[sc] / rz_old[sc]) * p[i];
+}
+
+// v[i] = 0 on the dofs of scenes whose mask differs from keep
+__global__ void k_mask_scenes(int nb, const int* __restrict__ bscene, const int* __restrict__ mask,
+                              int keep, double* __restrict__ v)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < 6 * nb && (mask[bscene[i / 6]] != 0) != (keep != 0)) v[i] = 0;
+}
+
+// largest |V1 - V0| coordinate per scene (one block per scene's vertex range)
+__global__ void __launch_bounds__(256) k_max_vertex_move_sc(const int* __restrict__ vstart,
+                                                            const double* __restrict__ V0,
+                                                            const double* __restrict__ V1,
+                                                            double* __restrict__ out)
+{
+    __shared__ double sh[256];
+    const int sc = blockIdx.x;
+    double m = 0;
+    for (int64_t i = 3 * (int64_t)vstart[sc] + threadIdx.x; i < 3 * (int64_t)vstart[sc + 1]; i += 256)
+        m = fmax(m, fabs(V1[i] - V0[i]));
+    sh[threadIdx.x] = m;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] = fmax(sh[threadIdx.x], sh[threadIdx.x + o]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[sc] = sh[0];
+}
+
+// smallest squared constraint distance per scene (bits of a non-negative double)
+__global__ void k_min_constraint_distance_sc(int64_t n, const int* __restrict__ type,
+                                             const int* __restrict__ verts,
+                                             const int* __restrict__ bodies,
+                                             const int* __restrict__ bscene,
+                                             const double* __restrict__ V,
+                                             unsigned long long* __restrict__ out)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int t = type[i];
+    const double* P[4];
+    for (int k = 0; k < 4; k++) {
+        int v = verts[4 * i + k];
+        P[k] = V + 3 * (size_t)(v < 0 ? 0 : v);
+    }
+    double d;
+    if (t == 0) d = pp_sqdist_rn(P[0], P[1]);
+    else if (t == 1) d = pl_sqdist_rn(P[0], P[1], P[2]);
+    else if (t == 2) d = ee_sqdist_rn(P[0], P[1], P[2], P[3]);
+    else d = ptplane_sqdist_rn(P[0], P[1], P[2], P[3]);
+    atomicMin(out + bscene[bodies[2 * i]], (unsigned long long)__double_as_longlong(d));
 }
 
 // rhs of the free dofs (-g) and the scatter of the solution back
@@ -600,7 +875,7 @@ double barrier_hessian_d(double d, double s)
 // ---------------------------------------------------------------------------
 
 // systems with at most this many free dofs are factorised densely
-constexpr int kDenseMax = 384;
+constexpr int kDenseMax = 768;
 
 struct Sim {
     rigc_sim_params p {};
@@ -620,6 +895,11 @@ struct Sim {
     std::vector<double> seg_kappa, seg_dk;
     // adjoint vectors: dL/d(state) in and out, dL/dx*, scratch
     DevBuf adj, adj_out, xbar, u1, u2;
+    // batched contexts: every scene is its own problem (own average mass,
+    // bounding-box diagonal, stiffness, regularisation, step length and
+    // convergence); per-scene device scalars and reduction outputs
+    std::vector<double> sc_mass, sc_bbox;
+    DevBuf sc_dev, sc_red, sc_vstart;
 };
 
 namespace {
@@ -776,6 +1056,31 @@ int pcg(Ctx& c, Sim& S, const HessView& H, bool& ok, int64_t& iters)
     return RIGC_OK;
 }
 
+int dense_ldlt(Ctx& c, double* A, int n, double* D, int* flags)
+{
+    static bool attr = false;
+    const size_t smem = (size_t)kDenseMax * kPanelStride * sizeof(double);
+    if (!attr) {
+        RIGC_CUDA(cudaFuncSetAttribute(k_ldlt_panel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem));
+        attr = true;
+    }
+    for (int j0 = 0; j0 < n; j0 += kPanel) {
+        const int w = std::min(kPanel, n - j0);
+        RIGC_COUNT_LAUNCH();
+        k_ldlt_panel<<<1, 512, (size_t)(n - j0) * kPanelStride * sizeof(double), c.stream>>>(
+            A, n, j0, D, flags);
+        const int rest = n - j0 - w;
+        if (rest > 0) {
+            const int tiles = (rest + 31) / 32;
+            RIGC_COUNT_LAUNCH();
+            k_ldlt_update<<<tiles * (tiles + 1) / 2, 256, 0, c.stream>>>(A, n, j0, w, D, flags);
+        }
+    }
+    RIGC_CUDA(cudaGetLastError());
+    return RIGC_OK;
+}
+
 // dense LDL^T solve of (H + reg I) d = -g on the free dofs into S.sol
 int dense_solve(Ctx& c, Sim& S, const HessView& H, bool& ok)
 {
@@ -790,9 +1095,10 @@ int dense_solve(Ctx& c, Sim& S, const HessView& H, bool& ok)
     RIGC_COUNT_LAUNCH();
     k_gather_neg<<<grid_for(n6, 256), 256, 0, st>>>(n6, S.free_idx.as<int>(), S.g.as<double>(),
                                                     S.dense_b.as<double>());
+    RIGC_TRY(dense_ldlt(c, S.dense.as<double>(), n, S.dense_d.as<double>(), flags));
     RIGC_COUNT_LAUNCH();
-    k_dense_ldlt<<<1, 256, 0, st>>>(S.dense.as<double>(), n, S.dense_b.as<double>(),
-                                    S.dense_x.as<double>(), S.dense_d.as<double>(), flags);
+    k_ldlt_solve<<<1, 256, 0, st>>>(S.dense.as<double>(), n, S.dense_d.as<double>(),
+                                    S.dense_b.as<double>(), S.dense_x.as<double>(), flags);
     RIGC_COUNT_LAUNCH();
     k_scatter_free<<<grid_for(n6, 256), 256, 0, st>>>(n6, S.free_idx.as<int>(), S.dense_x.as<double>(),
                                                       S.sol.as<double>());
@@ -858,6 +1164,467 @@ int max_abs(Ctx& c, Sim& S, const double* v, double* m)
     return RIGC_OK;
 }
 
+// ---- batched contexts: per-scene pieces of the driver
+
+// device layout of S.sc_dev (ns doubles each): 0 scE = 1/m, 1 scB = kappa/m,
+// 2 reg, 3 alpha, 4 rz, 5 rz_new, 6 pAp, 7 rr, 8 tol2, 9 cg alpha; then
+// 2 ns ints of CG flags and ns ints of masks
+struct ScenePtrs {
+    double *scE, *scB, *reg, *alpha, *rz, *rz_new, *pAp, *rr, *tol2, *cga;
+    int *flags, *mask;
+};
+
+ScenePtrs scene_ptrs(Sim& S, int ns)
+{
+    double* d = S.sc_dev.as<double>();
+    ScenePtrs P;
+    P.scE = d;
+    P.scB = d + ns;
+    P.reg = d + 2 * ns;
+    P.alpha = d + 3 * ns;
+    P.rz = d + 4 * ns;
+    P.rz_new = d + 5 * ns;
+    P.pAp = d + 6 * ns;
+    P.rr = d + 7 * ns;
+    P.tol2 = d + 8 * ns;
+    P.cga = d + 9 * ns;
+    P.flags = reinterpret_cast<int*>(d + 10 * ns);
+    P.mask = P.flags + 2 * ns;
+    return P;
+}
+
+int upload(Ctx& c, double* dst, const std::vector<double>& v)
+{
+    RIGC_CUDA(cudaMemcpyAsync(dst, v.data(), v.size() * 8, cudaMemcpyHostToDevice, c.stream));
+    return RIGC_OK;
+}
+
+// per-scene dot products of two dof vectors into host out (ns values)
+int seg_dot(Ctx& c, Sim& S, const double* a, const double* b, std::vector<double>& out)
+{
+    const int ns = c.s.nscenes;
+    RIGC_COUNT_LAUNCH();
+    k_seg_dot<<<ns, 256, 0, c.stream>>>(c.s.scene_bstart, 6, a, b, S.sc_red.as<double>());
+    out.resize(ns);
+    RIGC_CUDA(cudaMemcpyAsync(out.data(), S.sc_red.ptr, (size_t)ns * 8, cudaMemcpyDeviceToHost, c.stream));
+    RIGC_CUDA(cudaStreamSynchronize(c.stream));
+    return RIGC_OK;
+}
+
+// per-scene objective E_s / m_s + kappa_s / m_s B_s (host f), with the
+// gradient in S.g and the Hessian pieces when asked
+int objective_scenes(Ctx& c, Sim& S, const double* x, bool grad_hess, const std::vector<double>& kappa,
+                     std::vector<double>& f, Objective& O)
+{
+    const rigc_sim_params& p = S.p;
+    const int ns = c.s.nscenes;
+    rigc_body_state bs = state_of(S);
+    double E;
+    RIGC_TRY(body_energy(c, bs, x, p.gravity, p.timestep, &E, grad_hess ? S.gE.as<double>() : nullptr,
+                         grad_hess ? S.hE.as<double>() : nullptr));
+    std::vector<double> Es;
+    RIGC_COUNT_LAUNCH();
+    k_seg_dot<<<ns, 256, 0, c.stream>>>(c.s.scene_bstart, 1, c.scratch[0].as<double>(), nullptr,
+                                        S.sc_red.as<double>());
+    Es.resize(ns);
+    RIGC_CUDA(cudaMemcpyAsync(Es.data(), S.sc_red.ptr, (size_t)ns * 8, cudaMemcpyDeviceToHost, c.stream));
+    RIGC_TRY(build_constraints(c, x, p.dhat, p.dmin));
+    const int flags = grad_hess ? (RIGC_GRAD | RIGC_HESS | RIGC_PROJECT_PSD) : 0;
+    RIGC_TRY(barrier_term_impl(c, x, p.dhat, p.dmin, flags, &O.bo));  // syncs the stream
+    O.fo = rigc_barrier_out {};
+    f.resize(ns);
+    for (int k = 0; k < ns; k++) {
+        const double m = S.sc_mass[k];
+        const double B = k < (int)c.h_scene_energy.size() ? c.h_scene_energy[k] : 0.0;
+        f[k] = Es[k] / m + kappa[k] / m * B;
+    }
+    O.grad_hess = grad_hess;
+    if (grad_hess) {
+        ScenePtrs P = scene_ptrs(S, ns);
+        RIGC_COUNT_LAUNCH();
+        k_combine_grad_sc<<<grid_for(6 * S.nb, 256), 256, 0, c.stream>>>(
+            S.nb, S.gE.as<double>(), O.bo.grad, c.s.bscene, P.scE, P.scB, S.fixed.as<int>(),
+            S.g.as<double>());
+        RIGC_CUDA(cudaGetLastError());
+    }
+    return RIGC_OK;
+}
+
+HessView hess_view_scenes(Sim& S, const Ctx& c, const Objective& O)
+{
+    const int ns = c.s.nscenes;
+    ScenePtrs P = scene_ptrs(S, ns);
+    HessView H {};
+    H.body = S.hE.as<double>();
+    H.brp = O.bo.nnzb > 0 ? O.bo.row_ptr : nullptr;
+    H.bcol = O.bo.col;
+    H.bval = O.bo.val;
+    H.frp = nullptr;
+    H.fixed = S.fixed.as<int>();
+    H.nb = S.nb;
+    H.bscene = c.s.bscene;
+    H.scE = P.scE;
+    H.scB = P.scB;
+    H.scReg = P.reg;
+    return H;
+}
+
+// block-Jacobi PCG per scene for (H + reg_s I) d = -g on the scenes with
+// solve[s] set (the others keep S.sol); solved[s] on return
+int pcg_scenes(Ctx& c, Sim& S, const HessView& H, const std::vector<int>& solve,
+               std::vector<int>& solved, int64_t& iters)
+{
+    const int ns = c.s.nscenes;
+    const int nb = S.nb;
+    const int64_t n = 6 * (int64_t)nb;
+    cudaStream_t st = c.stream;
+    const unsigned gn = grid_for(n, 256), gs = grid_for(ns, 128);
+    ScenePtrs P = scene_ptrs(S, ns);
+    double* d = S.sol.as<double>();
+    double* r = S.r.as<double>();
+    double* z = S.z.as<double>();
+    double* pp = S.pp.as<double>();
+    double* Ap = S.Ap.as<double>();
+    // flags: scenes not solved start converged
+    std::vector<int> fl(2 * ns, 0);
+    for (int k = 0; k < ns; k++) fl[2 * k + 1] = solve[k] ? 0 : 1;
+    RIGC_CUDA(cudaMemcpyAsync(P.flags, fl.data(), fl.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    RIGC_CUDA(cudaMemcpyAsync(P.mask, solve.data(), ns * sizeof(int), cudaMemcpyHostToDevice, st));
+    // r = -g on the solved scenes (0 elsewhere); d = 0 there (the other
+    // scenes keep their solution)
+    RIGC_COUNT_LAUNCH();
+    k_axpy<<<gn, 256, 0, st>>>(n, -2.0, S.g.as<double>(), S.g.as<double>(), r);
+    RIGC_COUNT_LAUNCH();
+    k_mask_scenes<<<gn, 256, 0, st>>>(nb, c.s.bscene, P.mask, 1, r);
+    RIGC_COUNT_LAUNCH();
+    k_mask_scenes<<<gn, 256, 0, st>>>(nb, c.s.bscene, P.mask, 0, d);
+    RIGC_COUNT_LAUNCH();
+    k_block_jacobi<<<grid_for(nb, 64), 64, 0, st>>>(H, S.Minv.as<double>());
+    RIGC_COUNT_LAUNCH();
+    k_block_apply<<<gn, 256, 0, st>>>(nb, S.Minv.as<double>(), r, H.fixed, z);
+    RIGC_CUDA(cudaMemcpyAsync(pp, z, n * 8, cudaMemcpyDeviceToDevice, st));
+    RIGC_COUNT_LAUNCH();
+    k_seg_dot<<<ns, 256, 0, st>>>(c.s.scene_bstart, 6, r, z, P.rz);
+    RIGC_COUNT_LAUNCH();
+    k_seg_dot<<<ns, 256, 0, st>>>(c.s.scene_bstart, 6, r, r, P.rr);
+    std::vector<double> bb(ns);
+    RIGC_CUDA(cudaMemcpyAsync(bb.data(), P.rr, ns * 8, cudaMemcpyDeviceToHost, st));
+    RIGC_CUDA(cudaStreamSynchronize(st));
+    std::vector<double> tol2(ns);
+    for (int k = 0; k < ns; k++) tol2[k] = 1e-24 * bb[k];  // relative residual 1e-12
+    RIGC_TRY(upload(c, P.tol2, tol2));
+    solved.assign(ns, 0);
+    for (int k = 0; k < ns; k++)
+        if (solve[k] && bb[k] == 0) solved[k] = 1;
+    iters = 0;
+    const int64_t max_it = std::max<int64_t>(1000, 4 * n);
+    std::vector<double> rr(ns);
+    for (int64_t it = 0; it < max_it; it++) {
+        RIGC_COUNT_LAUNCH();
+        k_hess_matvec<<<gn, 256, 0, st>>>(H, pp, Ap);
+        RIGC_COUNT_LAUNCH();
+        k_seg_dot<<<ns, 256, 0, st>>>(c.s.scene_bstart, 6, pp, Ap, P.pAp);
+        RIGC_COUNT_LAUNCH();
+        k_cg_alpha_sc<<<gs, 128, 0, st>>>(ns, P.rz, P.pAp, P.rr, P.tol2, P.cga, P.flags);
+        RIGC_COUNT_LAUNCH();
+        k_cg_update_sc<<<gn, 256, 0, st>>>(nb, c.s.bscene, P.cga, pp, Ap, d, r);
+        RIGC_COUNT_LAUNCH();
+        k_block_apply<<<gn, 256, 0, st>>>(nb, S.Minv.as<double>(), r, H.fixed, z);
+        RIGC_COUNT_LAUNCH();
+        k_seg_dot<<<ns, 256, 0, st>>>(c.s.scene_bstart, 6, r, z, P.rz_new);
+        RIGC_COUNT_LAUNCH();
+        k_seg_dot<<<ns, 256, 0, st>>>(c.s.scene_bstart, 6, r, r, P.rr);
+        RIGC_COUNT_LAUNCH();
+        k_cg_direction_sc<<<gn, 256, 0, st>>>(nb, c.s.bscene, P.rz_new, P.rz, z, P.flags, pp);
+        RIGC_CUDA(cudaMemcpyAsync(P.rz, P.rz_new, ns * 8, cudaMemcpyDeviceToDevice, st));
+        iters = it + 1;
+        if ((it & 7) == 7 || it + 1 == max_it) {
+            RIGC_CUDA(cudaMemcpyAsync(fl.data(), P.flags, 2 * ns * sizeof(int), cudaMemcpyDeviceToHost, st));
+            RIGC_CUDA(cudaMemcpyAsync(rr.data(), P.rr, ns * 8, cudaMemcpyDeviceToHost, st));
+            RIGC_CUDA(cudaStreamSynchronize(st));
+            bool all = true;
+            for (int k = 0; k < ns; k++) {
+                if (!solve[k]) continue;
+                if (fl[2 * k] || !std::isfinite(rr[k])) continue;  // broken down: not solved
+                if (fl[2 * k + 1] || rr[k] <= tol2[k]) solved[k] = 1;
+                else all = false;
+            }
+            if (all) break;
+        }
+    }
+    RIGC_CUDA(cudaGetLastError());
+    return RIGC_OK;
+}
+
+// per-scene minimum constraint distance at x (-1 without constraints)
+int min_distance_scenes(Ctx& c, Sim& S, const double* x, std::vector<double>& md)
+{
+    const int ns = c.s.nscenes;
+    RIGC_TRY(build_constraints(c, x, S.p.dhat, S.p.dmin));
+    md.assign(ns, -1.0);
+    const int64_t n = c.cons.num;
+    if (n == 0) return RIGC_OK;
+    RIGC_TRY(compute_world_vertices_rn(c, x, S.V0.as<double>(), c.scratch[5]));
+    unsigned long long* out = reinterpret_cast<unsigned long long*>(S.sc_red.as<double>());
+    std::vector<unsigned long long> inf(ns, 0x7ff0000000000000ull);
+    RIGC_CUDA(cudaMemcpyAsync(out, inf.data(), ns * 8, cudaMemcpyHostToDevice, c.stream));
+    RIGC_COUNT_LAUNCH();
+    k_min_constraint_distance_sc<<<grid_for(n, 256), 256, 0, c.stream>>>(
+        n, c.cons.type.as<int>(), c.cons.verts.as<int>(), c.cons.bodies.as<int>(), c.s.bscene,
+        S.V0.as<double>(), out);
+    std::vector<double> d2(ns);
+    RIGC_CUDA(cudaMemcpyAsync(d2.data(), out, ns * 8, cudaMemcpyDeviceToHost, c.stream));
+    RIGC_CUDA(cudaStreamSynchronize(c.stream));
+    for (int k = 0; k < ns; k++) md[k] = std::isfinite(d2[k]) ? std::sqrt(d2[k]) : -1;
+    return RIGC_OK;
+}
+
+int max_vertex_move_scenes(Ctx& c, Sim& S, const double* x, const double* x1, std::vector<double>& m)
+{
+    const int ns = c.s.nscenes;
+    RIGC_TRY(compute_world_vertices_rn(c, x, S.V0.as<double>(), c.scratch[5]));
+    RIGC_TRY(compute_world_vertices_rn(c, x1, S.V1.as<double>(), c.scratch[5]));
+    RIGC_COUNT_LAUNCH();
+    k_max_vertex_move_sc<<<ns, 256, 0, c.stream>>>(S.sc_vstart.as<int>(), S.V0.as<double>(),
+                                                   S.V1.as<double>(), S.sc_red.as<double>());
+    m.resize(ns);
+    RIGC_CUDA(cudaMemcpyAsync(m.data(), S.sc_red.ptr, ns * 8, cudaMemcpyDeviceToHost, c.stream));
+    RIGC_CUDA(cudaStreamSynchronize(c.stream));
+    return RIGC_OK;
+}
+
+// One time step of every scene of a batched context, each scene as its own
+// problem: the same solver as sim_step with per-scene stiffness (from the
+// scene's average mass and bounding-box diagonal), regularisation, CCD
+// step bound, line search, convergence and stiffness updates; the kernels
+// run over all scenes at once.  Friction and the polish are not supported
+// here (RIGC_ERR_ARG).  Per-scene linear solves by block-Jacobi PCG.
+int sim_step_scenes(Ctx& c, rigc_step_stats* stats)
+{
+    Sim& S = *c.sim;
+    const rigc_sim_params& p = S.p;
+    if (p.coefficient_friction > 0 || p.newton_polish > 0) return RIGC_ERR_ARG;
+    const int ns = c.s.nscenes, nb = S.nb;
+    const int64_t n = 6 * (int64_t)nb;
+    cudaStream_t st = c.stream;
+    const unsigned gn = grid_for(n, 256);
+    ScenePtrs P = scene_ptrs(S, ns);
+    double* x0 = S.x0.as<double>();
+    double* x = S.x.as<double>();
+    double* xt = S.xt.as<double>();
+    double* dir = S.dir.as<double>();
+    rigc_step_stats local {};
+    std::vector<double> kappa(ns), kmax(ns), prev_md(ns), coeff(ns, 0.0), alpha(ns), lb(ns), f, ft;
+    std::vector<double> scE(ns), scB(ns), reg(ns, 0.0);
+    auto upload_scales = [&]() -> int {
+        for (int k = 0; k < ns; k++) {
+            scE[k] = 1.0 / S.sc_mass[k];
+            scB[k] = kappa[k] / S.sc_mass[k];
+        }
+        RIGC_TRY(upload(c, P.scE, scE));
+        RIGC_TRY(upload(c, P.scB, scB));
+        return RIGC_OK;
+    };
+
+    // IPCSolver::init_solve per scene
+    {
+        rigc_body_state bs = state_of(S);
+        double E;
+        RIGC_TRY(body_energy(c, bs, x0, p.gravity, p.timestep, &E, S.gE.as<double>(), nullptr));
+        RIGC_TRY(build_constraints(c, x0, p.dhat, p.dmin));
+        rigc_barrier_out bo;
+        RIGC_TRY(barrier_term_impl(c, x0, p.dhat, p.dmin, RIGC_GRAD, &bo));
+        RIGC_CUDA(cudaMemcpyAsync(S.gtmp.ptr, bo.grad, n * 8, cudaMemcpyDeviceToDevice, st));
+        std::vector<double> gg, ge;
+        RIGC_TRY(seg_dot(c, S, S.gtmp.as<double>(), S.gtmp.as<double>(), gg));
+        RIGC_TRY(seg_dot(c, S, S.gtmp.as<double>(), S.gE.as<double>(), ge));
+        const double dmin = p.dmin;
+        for (int k = 0; k < ns; k++) {
+            double d0 = 1e-8 * S.sc_bbox[k] + dmin;
+            d0 *= d0;
+            const double sb = 2 * dmin * p.dhat + p.dhat * p.dhat;
+            if (d0 - dmin * dmin >= sb) d0 = dmin * p.dhat + 0.5 * p.dhat * p.dhat;
+            double kmin = 4 * d0 * barrier_hessian_d(d0 - dmin * dmin, sb);
+            kmin = p.min_barrier_stiffness_scale * S.sc_mass[k] / kmin;
+            kmax[k] = 100 * kmin;
+            const double k0 = gg[k] > 0 ? -ge[k] / gg[k] : 1.0;
+            kappa[k] = std::min(kmax[k], std::max(kmin, k0));
+        }
+    }
+    RIGC_TRY(min_distance_scenes(c, S, x0, prev_md));
+
+    RIGC_CUDA(cudaMemcpyAsync(x, x0, n * 8, cudaMemcpyDeviceToDevice, st));
+    // state per scene: 0 iterating, 1 done
+    std::vector<int> done(ns, 0), solve(ns), solved, mask(ns);
+    std::vector<double> gdv;
+    int it = 0;
+    for (; it < p.max_newton_iterations; it++) {
+        int active = 0;
+        for (int k = 0; k < ns; k++) active += !done[k];
+        if (!active) break;
+        RIGC_TRY(upload_scales());
+        Objective O;
+        RIGC_TRY(objective_scenes(c, S, x, true, kappa, f, O));
+        local.objective_evals++;
+        // compute_regularized_direction per scene
+        for (int k = 0; k < ns; k++) solve[k] = !done[k];
+        std::vector<int> ok(ns, 0);
+        for (;;) {
+            int any = 0;
+            for (int k = 0; k < ns; k++) any |= solve[k];
+            if (!any) break;
+            for (int k = 0; k < ns; k++) reg[k] = coeff[k];
+            RIGC_TRY(upload(c, P.reg, reg));
+            HessView H = hess_view_scenes(S, c, O);
+            int64_t cgit;
+            RIGC_TRY(pcg_scenes(c, S, H, solve, solved, cgit));
+            local.cg_iterations += cgit;
+            RIGC_TRY(seg_dot(c, S, S.g.as<double>(), S.sol.as<double>(), gdv));
+            for (int k = 0; k < ns; k++) {
+                if (!solve[k]) continue;
+                const bool good = solved[k] && gdv[k] <= 0;
+                if (good) {
+                    coeff[k] /= 2;
+                    if (coeff[k] < 1e-8) coeff[k] = 0;
+                    ok[k] = 1;
+                    solve[k] = 0;
+                } else {
+                    coeff[k] = std::max(2 * coeff[k], 1e-8);
+                    if (!std::isfinite(coeff[k])) {
+                        solve[k] = 0;  // regularisation failed: the scene stops
+                        done[k] = 1;
+                    }
+                }
+            }
+        }
+        for (int k = 0; k < ns; k++) mask[k] = !done[k] && ok[k];
+        RIGC_CUDA(cudaMemcpyAsync(P.mask, mask.data(), ns * sizeof(int), cudaMemcpyHostToDevice, st));
+        RIGC_CUDA(cudaMemcpyAsync(dir, S.sol.ptr, n * 8, cudaMemcpyDeviceToDevice, st));
+        RIGC_COUNT_LAUNCH();
+        k_mask_scenes<<<gn, 256, 0, st>>>(nb, c.s.bscene, P.mask, 1, dir);
+        // velocity convergence
+        if (it > 0) {
+            RIGC_COUNT_LAUNCH();
+            k_axpy<<<gn, 256, 0, st>>>(n, 1.0, dir, x, xt);
+            std::vector<double> mv;
+            RIGC_TRY(max_vertex_move_scenes(c, S, x, xt, mv));
+            for (int k = 0; k < ns; k++) {
+                if (!mask[k]) continue;
+                const double tol = p.velocity_conv_tol * (p.velocity_conv_tol_abs ? 1.0 : S.sc_bbox[k]);
+                if (mv[k] / p.timestep <= tol) {
+                    done[k] = 1;
+                    mask[k] = 0;
+                }
+            }
+        }
+        // line search per scene over the scenes in mask (the gradient on the
+        // free dofs is S.g); found[k] and alpha[k] on return
+        std::vector<int> found(ns, 0);
+        auto line_search = [&](std::vector<int>& search) -> int {
+            RIGC_TRY(seg_dot(c, S, S.g.as<double>(), dir, gdv));
+            RIGC_COUNT_LAUNCH();
+            k_axpy<<<gn, 256, 0, st>>>(n, 1.0, dir, x, xt);
+            double toi;
+            RIGC_TRY(detect_and_count(c, x, xt, true, p.dmin / 2.0));
+            int s2 = run_ccd(c, x, xt, 1e-4, 0, &toi, nullptr);
+            if (s2 != RIGC_OK && s2 != RIGC_ERR_QUEUE_OVERFLOW && s2 != RIGC_ERR_ITER_LIMIT) return s2;
+            local.ccd_calls++;
+            for (int k = 0; k < ns; k++) {
+                if (!search[k]) continue;
+                lb[k] = std::min(p.line_search_lower_bound / std::sqrt(std::fabs(gdv[k])), 1e-1);
+                const double tk = k < (int)c.h_scene_toi.size() ? c.h_scene_toi[k] : toi;
+                alpha[k] = std::min(1.0, tk < 1.0 ? p.ccd_rescale * tk : tk);
+            }
+            for (;;) {
+                std::vector<double> a(ns, 0.0);
+                int any = 0;
+                for (int k = 0; k < ns; k++)
+                    if (search[k] && !found[k] && std::isfinite(lb[k]) && alpha[k] >= lb[k]) {
+                        a[k] = alpha[k];
+                        any = 1;
+                    }
+                if (!any) break;
+                RIGC_TRY(upload(c, P.alpha, a));
+                RIGC_COUNT_LAUNCH();
+                k_axpy_sc<<<gn, 256, 0, st>>>(nb, c.s.bscene, P.alpha, dir, x, xt);
+                Objective Oi;
+                RIGC_TRY(objective_scenes(c, S, xt, false, kappa, ft, Oi));
+                local.objective_evals++;
+                for (int k = 0; k < ns; k++) {
+                    if (a[k] == 0) continue;
+                    if (ft[k] < f[k]) found[k] = 1;
+                    else alpha[k] /= 2.0;
+                }
+            }
+            return RIGC_OK;
+        };
+        std::vector<int> search = mask;
+        RIGC_TRY(line_search(search));
+        // gradient fallback: d = -g on the scenes without a step
+        std::vector<int> retry(ns, 0);
+        int any_retry = 0;
+        for (int k = 0; k < ns; k++) {
+            retry[k] = mask[k] && !found[k];
+            any_retry |= retry[k];
+        }
+        if (any_retry) {
+            RIGC_CUDA(cudaMemcpyAsync(P.mask, retry.data(), ns * sizeof(int), cudaMemcpyHostToDevice, st));
+            RIGC_COUNT_LAUNCH();
+            k_axpy<<<gn, 256, 0, st>>>(n, -2.0, S.g.as<double>(), S.g.as<double>(), xt);
+            // dir = -g on the retried scenes, unchanged elsewhere
+            RIGC_COUNT_LAUNCH();
+            k_mask_scenes<<<gn, 256, 0, st>>>(nb, c.s.bscene, P.mask, 1, xt);
+            RIGC_COUNT_LAUNCH();
+            k_mask_scenes<<<gn, 256, 0, st>>>(nb, c.s.bscene, P.mask, 0, dir);
+            RIGC_COUNT_LAUNCH();
+            k_axpy<<<gn, 256, 0, st>>>(n, 1.0, xt, dir, dir);
+            RIGC_TRY(line_search(retry));
+            for (int k = 0; k < ns; k++)
+                if (retry[k] && !found[k]) done[k] = 1;  // line search failed: the scene stops
+        }
+        // x += alpha_s d on the scenes with a step
+        std::vector<double> a(ns, 0.0);
+        // (an iteration counts once it takes its step, as in sim_step)
+        for (int k = 0; k < ns; k++)
+            if (found[k]) {
+                a[k] = alpha[k];
+                local.newton_steps++;
+                local.newton_iterations++;
+            }
+        RIGC_TRY(upload(c, P.alpha, a));
+        RIGC_COUNT_LAUNCH();
+        k_axpy_sc<<<gn, 256, 0, st>>>(nb, c.s.bscene, P.alpha, dir, x, x);
+        // adaptive stiffness per scene
+        std::vector<double> md;
+        RIGC_TRY(min_distance_scenes(c, S, x, md));
+        for (int k = 0; k < ns; k++) {
+            if (!found[k]) continue;
+            const double eps = p.dhat_epsilon * (S.sc_bbox[k] + p.dmin);
+            if (prev_md[k] < eps && md[k] < eps && md[k] < prev_md[k])
+                kappa[k] = std::min(kmax[k], 2 * kappa[k]);
+            prev_md[k] = md[k];
+        }
+    }
+
+    // take_step
+    RIGC_COUNT_LAUNCH();
+    k_take_step<<<grid_for(nb, 128), 128, 0, st>>>(nb, c.s.type, S.fixed.as<int>(), x, x0,
+                                                   S.vel.as<double>(), S.Qdot.as<double>(),
+                                                   p.timestep);
+    RIGC_CUDA(cudaGetLastError());
+    RIGC_CUDA(cudaStreamSynchronize(st));
+    S.kappa = *std::max_element(kappa.begin(), kappa.end());
+    if (stats) {
+        stats->newton_iterations += local.newton_iterations;
+        stats->newton_steps += local.newton_steps;
+        stats->objective_evals += local.objective_evals;
+        stats->ccd_calls += local.ccd_calls;
+        stats->cg_iterations += local.cg_iterations;
+        stats->barrier_stiffness = S.kappa;
+    }
+    return RIGC_OK;
+}
+
 } // namespace
 
 int sim_init(Ctx& c, const rigc_sim_params& p, const rigc_sim_state& s)
@@ -908,6 +1675,21 @@ int sim_init(Ctx& c, const rigc_sim_params& p, const rigc_sim_state& s)
         RIGC_TRY(S.dense_d.reserve((size_t)nf * sizeof(double) + 8));
     }
     RIGC_CUDA(cudaStreamSynchronize(st));
+    // per-scene set-up of batched contexts (average mass and bounding-box
+    // diagonal default to the global ones; rigc_sim_scene_params sets them)
+    const int ns = c.s.nscenes;
+    S.sc_mass.assign(ns, p.average_mass);
+    S.sc_bbox.assign(ns, p.world_bbox_diagonal);
+    RIGC_TRY(S.sc_dev.reserve((size_t)ns * 13 * 8 + 64));
+    RIGC_TRY(S.sc_red.reserve((size_t)ns * 8 + 64));
+    {
+        std::vector<int> vs(ns + 1);
+        for (int k = 0; k <= ns; k++) vs[k] = c.s.h_bvs[c.s.h_scene_bstart[k]];
+        RIGC_TRY(S.sc_vstart.reserve((size_t)(ns + 1) * sizeof(int) + 8));
+        RIGC_CUDA(cudaMemcpyAsync(S.sc_vstart.ptr, vs.data(), vs.size() * sizeof(int),
+                                  cudaMemcpyHostToDevice, st));
+        RIGC_CUDA(cudaStreamSynchronize(st));
+    }
     S.kappa = 1;  // m_barrier_stiffness before the first solve
     S.tape_steps = 0;
     S.tape_every = 0;
@@ -917,6 +1699,7 @@ int sim_init(Ctx& c, const rigc_sim_params& p, const rigc_sim_state& s)
 int sim_step(Ctx& c, rigc_step_stats* stats)
 {
     if (!c.sim) return RIGC_ERR_ARG;
+    if (c.s.nscenes > 1) return sim_step_scenes(c, stats);
     Sim& S = *c.sim;
     const rigc_sim_params& p = S.p;
     const int nb = S.nb;
@@ -1102,6 +1885,21 @@ int sim_step(Ctx& c, rigc_step_stats* stats)
         stats->ccd_calls += local.ccd_calls;
         stats->cg_iterations += local.cg_iterations;
         stats->barrier_stiffness = local.barrier_stiffness;
+    }
+    return RIGC_OK;
+}
+
+int sim_scene_params(Ctx& c, const double* average_mass, const double* bbox_diagonal)
+{
+    if (!c.sim) return RIGC_ERR_ARG;
+    Sim& S = *c.sim;
+    for (int k = 0; k < c.s.nscenes; k++) {
+        if (average_mass && !(average_mass[k] > 0)) return RIGC_ERR_ARG;
+        if (bbox_diagonal && !(bbox_diagonal[k] > 0)) return RIGC_ERR_ARG;
+    }
+    for (int k = 0; k < c.s.nscenes; k++) {
+        if (average_mass) S.sc_mass[k] = average_mass[k];
+        if (bbox_diagonal) S.sc_bbox[k] = bbox_diagonal[k];
     }
     return RIGC_OK;
 }
@@ -1317,7 +2115,7 @@ void sim_release(Ctx& c)
                        &S.Minv, &S.sol, &S.part, &S.scal, &S.V0, &S.V1, &S.free_idx,
                        &S.dense, &S.dense_b, &S.dense_x, &S.dense_d, &S.ckpt,
                        &S.final_state, &S.seg_pre, &S.seg_x, &S.adj, &S.adj_out, &S.xbar,
-                       &S.u1, &S.u2 };
+                       &S.u1, &S.u2, &S.sc_dev, &S.sc_red, &S.sc_vstart };
     for (DevBuf* b : bufs) b->release();
     delete c.sim;
     c.sim = nullptr;

@@ -73,6 +73,7 @@ class Context:
         else:
             sob = np.ascontiguousarray(scene_of_body, dtype=np.int32)
             self._keep.append(sob)
+            self.scene_of_body = sob
             self.num_scenes = int(sob.max()) + 1 if len(sob) else 1
             L.check(self.lib.rigc_ctx_create_batched(C.byref(d), self.num_scenes, sob.ctypes.data,
                                                      C.byref(h)), "rigc_ctx_create_batched")
@@ -320,7 +321,8 @@ class Context:
         """Start a simulation from the scene's poses, velocities and Qdot (or
         from the given host arrays: poses / velocities nb x 6, Qdot nb x 9)."""
         sc = self.scene
-        V = sc.world_vertices(sc.poses())
+        V = sc.world_vertices(sc.poses() if poses is None
+                              else np.asarray(poses, np.float64).reshape(-1))
         p = L.SimParams()
         p.timestep = timestep
         p.gravity[:] = list(gravity)
@@ -354,6 +356,26 @@ class Context:
         s = L.SimState(*[k.ctypes.data for k in keep])
         L.check(self.lib.rigc_sim_init(self.h, C.byref(p), C.byref(s)), "rigc_sim_init")
         self.sim_params = p
+        if self.num_scenes > 1:
+            # each scene's average mass (RigidBodyAssembler::average_mass over
+            # its free dofs) and initial bounding-box diagonal
+            sob = self.scene_of_body
+            Vw = sc.world_vertices(keep[3].reshape(nb, 6))
+            vs = sc.body_vertex_start
+            free = ~sc.is_dof_fixed
+            md = np.concatenate([np.c_[sc.mass, sc.mass, sc.mass], sc.moment], 1)
+            am = np.ones(self.num_scenes)
+            bb = np.ones(self.num_scenes)
+            for k in range(self.num_scenes):
+                bodies = np.flatnonzero(sob == k)
+                f = free[bodies]
+                if f.any():
+                    am[k] = float(md[bodies][f].mean())
+                Vk = Vw[vs[bodies[0]]:vs[bodies[-1] + 1]]
+                bb[k] = float(np.linalg.norm(Vk.max(0) - Vk.min(0)))
+            self._keep_sim = (am, bb)
+            L.check(self.lib.rigc_sim_scene_params(self.h, am.ctypes.data, bb.ctypes.data),
+                    "rigc_sim_scene_params")
 
     def sim_step(self, num_steps=1):
         st = L.StepStats()

@@ -36,6 +36,7 @@ EXPORTS = [
     "rigc_set_candidates", "rigc_set_ccd_budget", "rigc_sim_init", "rigc_sim_step",
     "rigc_sim_get_state", "rigc_ctx_create_batched", "rigc_num_scenes", "rigc_scene_tois",
     "rigc_scene_barrier_energies", "rigc_sim_rollout", "rigc_sim_backward",
+    "rigc_sim_scene_params",
 ]
 RIGC_ERR_TOO_LARGE = 7
 RIGC_ERR_SOLVE = 8
@@ -160,6 +161,7 @@ def load():
     L.rigc_sim_get_state.argtypes = [_vp, _vp, _vp, _vp, _d]
     L.rigc_sim_rollout.argtypes = [_vp, C.c_int32, C.c_int32, C.POINTER(StepStats)]
     L.rigc_sim_backward.argtypes = [_vp] + [_vp] * 6
+    L.rigc_sim_scene_params.argtypes = [_vp, _vp, _vp]
     L.rigc_ctx_create_batched.argtypes = [C.POINTER(SceneDesc), C.c_int32, _vp, C.POINTER(_vp)]
     L.rigc_num_scenes.argtypes = [_vp]
     L.rigc_scene_tois.argtypes = [_vp, _d]
