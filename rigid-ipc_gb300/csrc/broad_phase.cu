@@ -86,11 +86,13 @@ __global__ void k_body_boxes(const double* __restrict__ x0, const double* __rest
 // one thread per (body, later body of the same scene)
 __global__ void k_close_bodies(const double* __restrict__ box, const int* __restrict__ group,
                                const int* __restrict__ bscene, const int* __restrict__ scene_bstart,
-                               int nb, int chunk, double infl, int* __restrict__ body_in)
+                               const int* __restrict__ scene_on, int nb, int chunk, double infl,
+                               int* __restrict__ body_in)
 {
     int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int i = (int)(t / chunk);
     if (i >= nb) return;
+    if (scene_on && !scene_on[bscene[i]]) return;
     const int end = scene_bstart[bscene[i] + 1];
     for (int j = i + 1 + (int)(t % chunk); j < end; j += chunk) {
         if (group[i] == group[j]) continue;
@@ -647,8 +649,8 @@ int detect_candidates(Ctx& c, const double* x0, const double* x1, bool continuou
         const int chunk = std::min(256, maxs);
         RIGC_COUNT_LAUNCH();
         k_close_bodies<<<grid_for((int64_t)s.nb * chunk, 256), 256, 0, st>>>(
-            c.body_box.as<double>(), s.group, s.bscene, s.scene_bstart, s.nb, chunk, infl,
-            c.body_in.as<int>());
+            c.body_box.as<double>(), s.group, s.bscene, s.scene_bstart, c.scene_on, s.nb, chunk,
+            infl, c.body_in.as<int>());
     }
     std::vector<int> h_in(s.nb);
     RIGC_CUDA(cudaMemcpyAsync(h_in.data(), c.body_in.ptr, (size_t)s.nb * sizeof(int),

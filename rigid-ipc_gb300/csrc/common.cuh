@@ -163,6 +163,9 @@ struct Ctx {
     Sim* sim = nullptr;
     // batched contexts: per-scene results of the last calls
     DevBuf scene_toi, scene_energy;
+    // batched time step: scenes whose bodies enter the broad phase (device,
+    // one int per scene; null: all)
+    const int* scene_on = nullptr;
     std::vector<double> h_scene_toi, h_scene_energy;
 };
 

@@ -1171,7 +1171,7 @@ int max_abs(Ctx& c, Sim& S, const double* v, double* m)
 // 2 ns ints of CG flags and ns ints of masks
 struct ScenePtrs {
     double *scE, *scB, *reg, *alpha, *rz, *rz_new, *pAp, *rr, *tol2, *cga;
-    int *flags, *mask;
+    int *flags, *mask, *on;
 };
 
 ScenePtrs scene_ptrs(Sim& S, int ns)
@@ -1190,8 +1190,21 @@ ScenePtrs scene_ptrs(Sim& S, int ns)
     P.cga = d + 9 * ns;
     P.flags = reinterpret_cast<int*>(d + 10 * ns);
     P.mask = P.flags + 2 * ns;
+    P.on = reinterpret_cast<int*>(d + 12 * ns);
     return P;
 }
+
+// restrict the broad phase (hence constraints, energies and the CCD) to the
+// scenes in on (a host mask); restored by scene_all
+int scene_only(Ctx& c, Sim& S, const std::vector<int>& on)
+{
+    ScenePtrs P = scene_ptrs(S, c.s.nscenes);
+    RIGC_CUDA(cudaMemcpyAsync(P.on, on.data(), on.size() * sizeof(int), cudaMemcpyHostToDevice,
+                              c.stream));
+    c.scene_on = P.on;
+    return RIGC_OK;
+}
+void scene_all(Ctx& c) { c.scene_on = nullptr; }
 
 int upload(Ctx& c, double* dst, const std::vector<double>& v)
 {
@@ -1414,6 +1427,11 @@ int sim_step_scenes(Ctx& c, rigc_step_stats* stats)
     double* xt = S.xt.as<double>();
     double* dir = S.dir.as<double>();
     rigc_step_stats local {};
+    struct AllScenesOnExit {
+        Ctx& c;
+        ~AllScenesOnExit() { scene_all(c); }
+    } guard { c };
+    scene_all(c);
     std::vector<double> kappa(ns), kmax(ns), prev_md(ns), coeff(ns, 0.0), alpha(ns), lb(ns), f, ft;
     std::vector<double> scE(ns), scB(ns), reg(ns, 0.0);
     auto upload_scales = [&]() -> int {
@@ -1464,6 +1482,9 @@ int sim_step_scenes(Ctx& c, rigc_step_stats* stats)
         if (!active) break;
         RIGC_TRY(upload_scales());
         Objective O;
+        std::vector<int> on(ns);
+        for (int k = 0; k < ns; k++) on[k] = !done[k];
+        RIGC_TRY(scene_only(c, S, on));
         RIGC_TRY(objective_scenes(c, S, x, true, kappa, f, O));
         local.objective_evals++;
         // compute_regularized_direction per scene
@@ -1525,6 +1546,7 @@ int sim_step_scenes(Ctx& c, rigc_step_stats* stats)
             RIGC_COUNT_LAUNCH();
             k_axpy<<<gn, 256, 0, st>>>(n, 1.0, dir, x, xt);
             double toi;
+            RIGC_TRY(scene_only(c, S, search));
             RIGC_TRY(detect_and_count(c, x, xt, true, p.dmin / 2.0));
             int s2 = run_ccd(c, x, xt, 1e-4, 0, &toi, nullptr);
             if (s2 != RIGC_OK && s2 != RIGC_ERR_QUEUE_OVERFLOW && s2 != RIGC_ERR_ITER_LIMIT) return s2;
@@ -1547,6 +1569,9 @@ int sim_step_scenes(Ctx& c, rigc_step_stats* stats)
                 RIGC_TRY(upload(c, P.alpha, a));
                 RIGC_COUNT_LAUNCH();
                 k_axpy_sc<<<gn, 256, 0, st>>>(nb, c.s.bscene, P.alpha, dir, x, xt);
+                std::vector<int> on_t(ns);
+                for (int k = 0; k < ns; k++) on_t[k] = a[k] != 0;
+                RIGC_TRY(scene_only(c, S, on_t));
                 Objective Oi;
                 RIGC_TRY(objective_scenes(c, S, xt, false, kappa, ft, Oi));
                 local.objective_evals++;
@@ -1596,7 +1621,9 @@ int sim_step_scenes(Ctx& c, rigc_step_stats* stats)
         k_axpy_sc<<<gn, 256, 0, st>>>(nb, c.s.bscene, P.alpha, dir, x, x);
         // adaptive stiffness per scene
         std::vector<double> md;
+        RIGC_TRY(scene_only(c, S, found));
         RIGC_TRY(min_distance_scenes(c, S, x, md));
+        scene_all(c);
         for (int k = 0; k < ns; k++) {
             if (!found[k]) continue;
             const double eps = p.dhat_epsilon * (S.sc_bbox[k] + p.dmin);
@@ -1607,6 +1634,7 @@ int sim_step_scenes(Ctx& c, rigc_step_stats* stats)
     }
 
     // take_step
+    scene_all(c);
     RIGC_COUNT_LAUNCH();
     k_take_step<<<grid_for(nb, 128), 128, 0, st>>>(nb, c.s.type, S.fixed.as<int>(), x, x0,
                                                    S.vel.as<double>(), S.Qdot.as<double>(),
