@@ -314,17 +314,23 @@ def batched_rate(args, torch):
 
     cb = rigc.Context(big, scene_of_body=sob)
     x0d, x1d = cb.device(X0), cb.device(X1)
-    for _ in range(2):
-        run_pass(cb, x0d, x1d)
-    torch.cuda.synchronize()
-    t = time.perf_counter()
-    pairs_b = 0
-    reps = 3
-    for _ in range(reps):
-        pairs_b += run_pass(cb, x0d, x1d)
-    torch.cuda.synchronize()
-    tb = (time.perf_counter() - t) / reps
-    pairs_b //= reps
+
+    def timed_passes():
+        for _ in range(2):
+            run_pass(cb, x0d, x1d)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        pairs = 0
+        reps = 3
+        for _ in range(reps):
+            pairs += run_pass(cb, x0d, x1d)
+        torch.cuda.synchronize()
+        return pairs // reps, (time.perf_counter() - t) / reps
+
+    pairs_untuned, t_untuned = timed_passes()
+    # launch shapes chosen by the autotuner on this batch
+    tune = cb.autotune(x0d, x1d, dhat)
+    pairs_b, tb = timed_passes()
     ctxs = [(rigc.Context(sc), None) for sc in scenes]
     dev = [(c.device(x0), c.device(x1)) for (c, _), (_, x0, x1) in zip(ctxs, items)]
     for (c, _), (a, b) in zip(ctxs, dev):
@@ -338,14 +344,15 @@ def batched_rate(args, torch):
     tp = time.perf_counter() - t
     out = {"workload": BATCH_WORKLOAD.format(n=args.batch_scenes), "bodies": big.num_bodies,
            "pairs_per_pass": pairs_b, "batched_pairs_per_s": pairs_b / tb,
-           "plain_pairs_per_s": pairs_p / tp, "batched_ms": tb * 1e3, "plain_ms": tp * 1e3}
+           "plain_pairs_per_s": pairs_p / tp, "batched_ms": tb * 1e3, "plain_ms": tp * 1e3,
+           "batched_untuned_ms": t_untuned * 1e3, "autotune": tune}
     del ctxs, dev, cb
     if args.batch_sim_steps > 0:
-        out["sim"] = batched_sim_rate(args, torch, items, big, sob)
+        out["sim"] = batched_sim_rate(args, torch, items, big, sob, tune)
     return out
 
 
-def batched_sim_rate(args, torch, items, big, sob):
+def batched_sim_rate(args, torch, items, big, sob, tune):
     """Simulated scene-steps per second: every scene from its contact pile
     with its seeded velocities, one time step (the full IPC Newton solve) per
     scene per step -- one batched context stepping all scenes at once
@@ -358,6 +365,7 @@ def batched_sim_rate(args, torch, items, big, sob):
     grav = (0.0, -9.81, 0.0)
     K = args.batch_sim_steps
     cb = rigc.Context(big, scene_of_body=sob)
+    cb.set_tune(tune["ccd_blocks_per_sm"], tune["cache_slots_per_body"], tune["barrier_per_warp"])
     cb.sim_init(0.01, grav, dhat, poses=X0)
     cb.sim_step(1)
     torch.cuda.synchronize()

@@ -372,6 +372,22 @@ int rigc_sim_get_state(rigc_ctx* ctx, double* poses, double* velocities,
 int rigc_sim_scene_params(rigc_ctx* ctx, const double* average_mass,
                           const double* bbox_diagonal);
 
+/* ---- autotuner (new).  Times the narrow phase's launch shapes on the
+ * context's own workload -- k_ccd's resident blocks per SM, the CCD frame
+ * cache's slots per body, k_barrier_local's constraints per warp -- one
+ * after the other (median of three runs each), over the continuous
+ * candidates of x0 -> x1 and the constraint set at x0 (device poses), and
+ * keeps the fastest in the context for every later call.  rigc_set_tune
+ * sets them directly (0: the built-in choice). */
+typedef struct rigc_tune_report {
+    int32_t ccd_blocks_per_sm, cache_slots_per_body, barrier_per_warp;
+    double ccd_ms_default, ccd_ms, barrier_ms_default, barrier_ms;
+} rigc_tune_report;
+int rigc_autotune(rigc_ctx* ctx, const double* x0, const double* x1, double dhat, double dmin,
+                  rigc_tune_report* report);
+int rigc_set_tune(rigc_ctx* ctx, int32_t ccd_blocks_per_sm, int32_t cache_slots_per_body,
+                  int32_t barrier_per_warp);
+
 /* ---- differentiation (new: the reference has no adjoint).
  * rigc_sim_rollout advances the simulation by num_steps steps like
  * rigc_sim_step and keeps the state before every checkpoint_every-th step on

@@ -32,6 +32,7 @@ UNITS = {
     "body.cu": ["--fmad=true"],
     "friction.cu": ["--fmad=true"],
     "step.cu": ["--fmad=false"],
+    "autotune.cu": ["--fmad=false"],
 }
 
 

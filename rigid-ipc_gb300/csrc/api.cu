@@ -30,6 +30,8 @@ int sim_step(Ctx& c, rigc_step_stats* stats);
 int sim_get_state(Ctx& c, double* poses, double* velocities, double* Qdot, double* kappa);
 int sim_rollout(Ctx& c, int steps, int every, rigc_step_stats* stats);
 int sim_scene_params(Ctx& c, const double* average_mass, const double* bbox_diagonal);
+int autotune(Ctx& c, const double* x0, const double* x1, double dhat, double dmin,
+             rigc_tune_report* rep);
 int sim_backward(Ctx& c, const double* dp, const double* dv, const double* dq, double* gp,
                  double* gv, double* gq);
 void sim_release(Ctx& c);
@@ -590,6 +592,26 @@ int rigc_sim_get_state(rigc_ctx* ctx, double* poses, double* velocities, double*
 {
     if (!ctx) return RIGC_ERR_ARG;
     return sim_get_state(*ctx_of(ctx), poses, velocities, Qdot, barrier_stiffness);
+}
+
+int rigc_autotune(rigc_ctx* ctx, const double* x0, const double* x1, double dhat, double dmin,
+                  rigc_tune_report* report)
+{
+    if (!ctx || !x0 || !x1 || !(dhat > 0) || !(dmin >= 0)) return RIGC_ERR_ARG;
+    return autotune(*ctx_of(ctx), x0, x1, dhat, dmin, report);
+}
+
+int rigc_set_tune(rigc_ctx* ctx, int32_t ccd_blocks_per_sm, int32_t cache_slots_per_body,
+                  int32_t barrier_per_warp)
+{
+    if (!ctx || ccd_blocks_per_sm < 0 || cache_slots_per_body < 0 || barrier_per_warp < 0
+        || barrier_per_warp > 32 || cache_slots_per_body > (1 << 16))
+        return RIGC_ERR_ARG;
+    Ctx& c = *ctx_of(ctx);
+    c.tune.ccd_blocks_per_sm = ccd_blocks_per_sm;
+    c.tune.cache_slots_per_body = cache_slots_per_body;
+    c.tune.barrier_per_warp = barrier_per_warp;
+    return RIGC_OK;
 }
 
 int rigc_sim_scene_params(rigc_ctx* ctx, const double* average_mass, const double* bbox_diagonal)

@@ -625,7 +625,8 @@ int launch_barrier_local(Ctx& c, const double* x, double dhat, double dmin, int 
     a.grad = grad;
     a.blocks = blocks;
     a.hess = hess;
-    const int pw = local_terms_per_warp(c.cons.num);
+    const int pw = c.tune.barrier_per_warp > 0 ? std::min(c.tune.barrier_per_warp, kBarrierTPB)
+                                               : local_terms_per_warp(c.cons.num);
     RIGC_COUNT_LAUNCH();
     k_barrier_local<<<grid_for(c.cons.num, pw), kBarrierTPB, local_terms_smem_bytes(), c.stream>>>(a, pw);
     RIGC_CUDA(cudaGetLastError());

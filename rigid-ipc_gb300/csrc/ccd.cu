@@ -767,6 +767,18 @@ __global__ void k_fill_inf(double* __restrict__ v, int64_t n)
     if (i < n) v[i] = INFINITY;
 }
 
+// resident k_ccd blocks per SM at full occupancy
+int ccd_max_blocks_per_sm(int* out)
+{
+    static int blocks_per_sm = 0;
+    if (!blocks_per_sm) {
+        RIGC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_ccd, kCCDThreads, 0));
+        if (blocks_per_sm < 1) blocks_per_sm = 1;
+    }
+    *out = blocks_per_sm;
+    return RIGC_OK;
+}
+
 // counters layout in the context's device scalars (byte offset 256):
 // [0] gmin bits, [1] boxes, [2] hits, [3] status, [4] next candidate
 int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flags,
@@ -826,9 +838,11 @@ int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flag
         k_rot_table<<<grid_for((int64_t)c.s.nb * kTableSlots, 128), 128, 0, st>>>(
             x0, x1, c.s.nb, toi_tol, const_cast<double*>(a.table), const_cast<double*>(a.traj),
             const_cast<int*>(a.bfixed));
-        // frame cache: 1024 slots per body, at least 2^16, at most 2^22
+        // frame cache: 1024 slots per body (or the tuned count), at least
+        // 2^16, at most 2^22
+        const size_t per_body = c.tune.cache_slots_per_body > 0 ? c.tune.cache_slots_per_body : 1024;
         size_t slots = 1u << 16;
-        while (slots < (size_t)c.s.nb * 1024 && slots < (1u << 22)) slots <<= 1;
+        while (slots < (size_t)c.s.nb * per_body && slots < (1u << 22)) slots <<= 1;
         RIGC_TRY(c.frame_keys.reserve(slots * sizeof(unsigned long long)));
         RIGC_TRY(c.frame_vals.reserve(slots * kTableEntry * sizeof(double)));
         RIGC_CUDA(cudaMemsetAsync(c.frame_keys.ptr, 0, slots * sizeof(unsigned long long), st));
@@ -842,17 +856,15 @@ int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flag
             RIGC_COUNT_LAUNCH();
             k_fill_inf<<<grid_for(n, 256), 256, 0, st>>>(per, n);
         }
-        static int blocks_per_sm = 0;
-        if (!blocks_per_sm) {
-            RIGC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_ccd,
-                                                                    kCCDThreads, 0));
-            if (blocks_per_sm < 1) blocks_per_sm = 1;
-        }
+        int blocks_per_sm;
+        RIGC_TRY(ccd_max_blocks_per_sm(&blocks_per_sm));
         int dev = 0, sms = kNumSMs;
         RIGC_CUDA(cudaGetDevice(&dev));
         RIGC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         int64_t want = (n + kCCDThreads - 1) / kCCDThreads;
-        int64_t full = (int64_t)sms * blocks_per_sm;
+        const int bps = c.tune.ccd_blocks_per_sm > 0 ? std::min(c.tune.ccd_blocks_per_sm, blocks_per_sm)
+                                                     : blocks_per_sm;
+        int64_t full = (int64_t)sms * bps;
         RIGC_COUNT_LAUNCH();
         k_ccd<<<(unsigned)std::min(want, full), kCCDThreads, 0, st>>>(a);
         RIGC_CUDA(cudaGetLastError());

@@ -160,6 +160,12 @@ struct Ctx {
     DevBuf frame_keys, frame_vals;  // CCD frame cache (hash table)
     Friction fric;
     int64_t ccd_max_boxes = int64_t(1) << 22;  // per-candidate CCD box budget
+    // launch shapes chosen by rigc_autotune (0: the built-in choice)
+    struct Tune {
+        int ccd_blocks_per_sm = 0;     // resident k_ccd blocks per SM (0: occupancy limit)
+        int cache_slots_per_body = 0;  // CCD frame-cache slots per body (0: 1024)
+        int barrier_per_warp = 0;      // constraints per warp of k_barrier_local (0: by count)
+    } tune;
     Sim* sim = nullptr;
     // batched contexts: per-scene results of the last calls
     DevBuf scene_toi, scene_energy;

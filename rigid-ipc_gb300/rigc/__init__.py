@@ -382,6 +382,19 @@ class Context:
         L.check(self.lib.rigc_sim_step(self.h, num_steps, C.byref(st)), "rigc_sim_step")
         return {f: getattr(st, f) for f, _ in L.StepStats._fields_}
 
+    def autotune(self, x0, x1, dhat, dmin=0.0):
+        """Choose the narrow phase's launch shapes on this workload (kept for
+        later calls); returns the choice and the timings."""
+        x0d, x1d = self.device(x0), self.device(x1)
+        r = L.TuneReport()
+        L.check(self.lib.rigc_autotune(self.h, x0d.data_ptr(), x1d.data_ptr(), dhat, dmin,
+                                       C.byref(r)), "rigc_autotune")
+        return {f: getattr(r, f) for f, _ in L.TuneReport._fields_}
+
+    def set_tune(self, ccd_blocks_per_sm=0, cache_slots_per_body=0, barrier_per_warp=0):
+        L.check(self.lib.rigc_set_tune(self.h, ccd_blocks_per_sm, cache_slots_per_body,
+                                       barrier_per_warp), "rigc_set_tune")
+
     def sim_rollout(self, num_steps, checkpoint_every=10):
         """Advance num_steps steps, keeping checkpoints for sim_backward."""
         st = L.StepStats()

@@ -36,7 +36,7 @@ EXPORTS = [
     "rigc_set_candidates", "rigc_set_ccd_budget", "rigc_sim_init", "rigc_sim_step",
     "rigc_sim_get_state", "rigc_ctx_create_batched", "rigc_num_scenes", "rigc_scene_tois",
     "rigc_scene_barrier_energies", "rigc_sim_rollout", "rigc_sim_backward",
-    "rigc_sim_scene_params",
+    "rigc_sim_scene_params", "rigc_autotune", "rigc_set_tune",
 ]
 RIGC_ERR_TOO_LARGE = 7
 RIGC_ERR_SOLVE = 8
@@ -101,6 +101,13 @@ class SimState(C.Structure):
                 ("velocities", _vp), ("Qdot", _vp)]
 
 
+class TuneReport(C.Structure):
+    _fields_ = [("ccd_blocks_per_sm", C.c_int32), ("cache_slots_per_body", C.c_int32),
+                ("barrier_per_warp", C.c_int32), ("ccd_ms_default", C.c_double),
+                ("ccd_ms", C.c_double), ("barrier_ms_default", C.c_double),
+                ("barrier_ms", C.c_double)]
+
+
 class StepStats(C.Structure):
     _fields_ = [("newton_iterations", C.c_int64), ("newton_steps", C.c_int64),
                 ("objective_evals", C.c_int64), ("ccd_calls", C.c_int64),
@@ -162,6 +169,8 @@ def load():
     L.rigc_sim_rollout.argtypes = [_vp, C.c_int32, C.c_int32, C.POINTER(StepStats)]
     L.rigc_sim_backward.argtypes = [_vp] + [_vp] * 6
     L.rigc_sim_scene_params.argtypes = [_vp, _vp, _vp]
+    L.rigc_autotune.argtypes = [_vp, _vp, _vp, C.c_double, C.c_double, C.POINTER(TuneReport)]
+    L.rigc_set_tune.argtypes = [_vp, C.c_int32, C.c_int32, C.c_int32]
     L.rigc_ctx_create_batched.argtypes = [C.POINTER(SceneDesc), C.c_int32, _vp, C.POINTER(_vp)]
     L.rigc_num_scenes.argtypes = [_vp]
     L.rigc_scene_tois.argtypes = [_vp, _d]

@@ -116,3 +116,36 @@ def test_batched_sim_rejects_friction():
     cb.sim_init(0.01, (0.0, -9.81, 0.0), DHAT, coefficient_friction=0.5)
     with pytest.raises(RuntimeError):
         cb.sim_step(1)
+
+
+def test_autotune_keeps_results():
+    """rigc_autotune only changes launch shapes: the earliest times of impact
+    (per scene), the constraint set and the barrier term are the same after
+    it, bit for bit."""
+    import rigc
+    from rigc import scene as S
+
+    items = _scenes()
+    big, sob = S.concat_scenes([sc for sc, _ in items])
+    x0 = np.concatenate([x for _, x in items])
+    x1 = np.concatenate([sc.predictor_poses(x) for sc, x in items])
+    cb = rigc.Context(big, scene_of_body=sob)
+
+    def run():
+        toi = cb.compute_earliest_toi(x0, x1)
+        st = cb.scene_tois()
+        cs = cb.construct_constraint_set(x0, DHAT)
+        e, g, _ = cb.compute_barrier_term(x0, DHAT)
+        return toi, st, cs, e, g
+
+    a = run()
+    rep = cb.autotune(x0, x1, DHAT)
+    assert rep["ccd_ms"] <= rep["ccd_ms_default"] and rep["barrier_ms"] <= rep["barrier_ms_default"]
+    b = run()
+    assert a[0] == b[0] and np.array_equal(a[1], b[1])
+    for u, v in zip(a[2], b[2]):
+        assert np.array_equal(u, v)
+    assert a[3] == b[3] and np.array_equal(a[4], b[4])
+    cb.set_tune(1, 256, 4)
+    c = run()
+    assert a[0] == c[0] and a[3] == c[3] and np.array_equal(a[4], c[4])
