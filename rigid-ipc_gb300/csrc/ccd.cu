@@ -61,6 +61,8 @@ struct CCDArgs {
     int64_t nee, nfv;
     double toi_tol;
     int prune;
+    int seeds_log2;             // prune mode: each candidate's search starts from the
+                                // 2^seeds_log2 boxes of its subdivision tree at that depth
     long long max_boxes;
     unsigned long long* gmin;   // running minimum time of impact (double bits)
     unsigned long long* scene_gmin;  // batched contexts: the same per scene, else null
@@ -544,6 +546,33 @@ __device__ __forceinline__ void record_min(const CCDArgs& a, const Query& q, dou
     atomicMin(a.gmin, b);
 }
 
+// The box of the candidate's subdivision tree at depth d reached by the
+// branches in the bits of j (most significant first, 0 = lower half).  The
+// split rule depends only on the widths and tolerances, so every box of a
+// level splits along the same dimension and these boxes are exactly the
+// tree's nodes at depth d: searching them one by one visits the tree's
+// leaves below them, hence finds the same earliest root box.
+__device__ __forceinline__ Box seed_box(int d, int64_t j, const double* tol)
+{
+    Box x { 0.0, 1.0, 0.0, 1.0, 0.0, 1.0 };
+    for (int l = d - 1; l >= 0; l--) {
+        double w[3] = { sub_up(x.t1, x.t0), sub_up(x.a1, x.a0), sub_up(x.b1, x.b0) };
+        bool all_tol = le_nn(w[0], tol[0]) && le_nn(w[1], tol[1]) && le_nn(w[2], tol[2]);
+        int split = -1;
+        for (int k = 0; k < 3; k++)
+            if ((all_tol || !le_nn(w[k], tol[k]))
+                && (split == -1 || !le_nn(RMUL(w[k], tol[split]), RMUL(w[split], tol[k]))))
+                split = k;
+        const bool hi = (j >> l) & 1;
+        double* lo_ = split == 0 ? &x.t0 : (split == 1 ? &x.a0 : &x.b0);
+        double* hi_ = split == 0 ? &x.t1 : (split == 1 ? &x.a1 : &x.b1);
+        const double m = RMUL(0.5, RADD(*lo_, *hi_));
+        if (hi) *lo_ = m;
+        else *hi_ = m;
+    }
+    return x;
+}
+
 // Persistent kernel: each lane takes the next unprocessed candidate from a
 // global counter whenever its box stack runs empty.  Every iteration each
 // lane pops boxes until one survives the cheap tests (or takes a new
@@ -655,10 +684,13 @@ k_ccd(CCDArgs a)
                                   (unsigned long long)__double_as_longlong(toi));
                     if (status != RIGC_OK) atomicMax(a.status, status);
                 }
-                cur = (int64_t)atomicAdd(a.next, 1ull);
-                if (cur >= n) {
+                // work item w: seed w / n of candidate w % n (seed-major, so
+                // early times of every candidate come first)
+                const int64_t w = (int64_t)atomicAdd(a.next, 1ull);
+                if (w >= (n << a.seeds_log2)) {
                     done = true;
                 } else {
+                    cur = w % n;
                     load_candidate(a, cur, q);
                     tol[0] = a.ctol[3 * cur];
                     tol[1] = a.ctol[3 * cur + 1];
@@ -669,8 +701,12 @@ k_ccd(CCDArgs a)
                     status = RIGC_OK;
                     cboxes = 0;
                     sb = sp = 0;
-                    x = Box { 0.0, 1.0, 0.0, 1.0, 0.0, 1.0 };
+                    x = seed_box(a.seeds_log2, w / n, tol);
                     have = !(a.prune && le_nn(gbound, x.t0));
+                    if (have && q.fv) {
+                        double sl = add_dn(x.a0, x.b0), sh = add_up(x.a1, x.b1);
+                        have = le_nn(sl, 1.0) && !is_neg(sh);
+                    }
                 }
             }
         }
@@ -861,10 +897,15 @@ int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flag
         int dev = 0, sms = kNumSMs;
         RIGC_CUDA(cudaGetDevice(&dev));
         RIGC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        int64_t want = (n + kCCDThreads - 1) / kCCDThreads;
         const int bps = c.tune.ccd_blocks_per_sm > 0 ? std::min(c.tune.ccd_blocks_per_sm, blocks_per_sm)
                                                      : blocks_per_sm;
         int64_t full = (int64_t)sms * bps;
+        // few candidates: start each search from 2^d boxes of its tree so
+        // that the searches fill the GPU (prune mode; at most 32 per candidate)
+        a.seeds_log2 = 0;
+        if (a.prune)
+            while (a.seeds_log2 < 5 && (n << a.seeds_log2) * 4 < full * kCCDThreads) a.seeds_log2++;
+        int64_t want = ((n << a.seeds_log2) + kCCDThreads - 1) / kCCDThreads;
         RIGC_COUNT_LAUNCH();
         k_ccd<<<(unsigned)std::min(want, full), kCCDThreads, 0, st>>>(a);
         RIGC_CUDA(cudaGetLastError());
