@@ -51,6 +51,10 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-sim", action="store_true", help="skip the steps/s measurement")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the built-in launch shapes for the headline pass")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the per-configuration pass rates")
     ap.add_argument("--no-adjoint", action="store_true",
                     help="skip the differentiable rollout measurement")
     ap.add_argument("--sim-steps", type=int, default=20)
@@ -223,6 +227,99 @@ def sim_rate(args, torch):
     return out
 
 
+def pass_rates(ctx, x0, x1, dhat, torch, reps=3):
+    """ccd_pairs/s (continuous candidates x0 -> x1 through the CCD) and
+    barrier_pairs/s (active constraints at x0 through energy, gradient, PSD
+    12x12 Hessians, chain rule and BSR assembly), median of reps passes."""
+    x0d, x1d = ctx.device(x0), ctx.device(x1)
+
+    def timed(fn):
+        ts = []
+        for _ in range(reps + 1):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t)
+        return statistics.median(ts[1:])
+
+    t_ccd = timed(lambda: ctx.compute_earliest_toi(x0d, x1d))
+    s = ctx.stats()
+    n_ccd = s["cand_ee"] + s["cand_fv"]
+    cs = ctx.construct_constraint_set(x0d, dhat)
+    n_con = len(cs["type"])
+    t_bar = timed(lambda: (ctx.construct_constraint_set(x0d, dhat),
+                           ctx.compute_barrier_term(x0d, dhat)))
+    return {"ccd_candidates": n_ccd, "ccd_pairs_per_s": n_ccd / t_ccd, "ccd_ms": t_ccd * 1e3,
+            "constraints": n_con, "barrier_pairs_per_s": n_con / t_bar, "barrier_ms": t_bar * 1e3}
+
+
+def pass_rates_tuned(ctx, x0, x1, dhat, torch):
+    """pass_rates with the built-in launch shapes, then after rigc_autotune
+    on the same workload."""
+    r = pass_rates(ctx, x0, x1, dhat, torch)
+    tune = ctx.autotune(x0, x1, dhat)
+    t = pass_rates(ctx, x0, x1, dhat, torch)
+    r["tuned"] = {"ccd_pairs_per_s": t["ccd_pairs_per_s"],
+                  "barrier_pairs_per_s": t["barrier_pairs_per_s"],
+                  "choice": {k: tune[k] for k in ("ccd_blocks_per_sm", "cache_slots_per_body",
+                                                  "ccd_seeds_log2", "barrier_per_warp")}}
+    return r
+
+
+def settled(sc, steps, dhat, dt):
+    """Poses after steps device time steps, and the explicit predictor from
+    there (velocities of that state, gravity included) for the CCD pass."""
+    import rigc
+
+    c = rigc.Context(sc)
+    c.sim_init(dt, (0.0, -9.81, 0.0), dhat)
+    c.sim_step(steps)
+    P, V, Q, _ = c.sim_state()
+    x1 = P.copy()
+    dyn = np.array([b.type == 2 for b in sc.bodies])
+    x1[dyn, :3] += dt * V[dyn, :3]
+    x1[dyn, 1] -= 9.81 * dt * dt
+    return P.reshape(-1), x1.reshape(-1)
+
+
+def per_config(args, torch):
+    """Narrow-phase pass rates of the plain configurations beside the
+    headline one: the 27-cube lattice and the 64-cube lattice after their
+    landings (40 steps), and the 200-link chain (links 1.501 m apart: at 1.5
+    they touch, see scene.spec_chain) after 10 steps of hanging."""
+    import rigc
+    from rigc import scene as S
+
+    out = {}
+    sc = S.scene_from_json(S.spec_cubes(args.seed))
+    x0, x1 = settled(sc, 40, 1e-3, 0.01)
+    out["cubes_27"] = pass_rates_tuned(rigc.Context(sc), x0, x1, 1e-3, torch)
+    sc = S.scene_from_json(S.spec_cube_lattice(0))
+    x0, x1 = settled(sc, 40, 1e-3, 0.01)
+    out["cubes_64"] = pass_rates_tuned(rigc.Context(sc), x0, x1, 1e-3, torch)
+    sc = S.scene_from_json(S.spec_chain(spacing=1.499))
+    c = rigc.Context(sc)
+    c.sim_init(0.005, (0.0, -9.81, 0.0), 1e-4)
+    c.sim_step(5)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    st = c.sim_step(5)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t
+    P, V, Q, _ = c.sim_state()
+    x1 = P.copy()
+    dyn = np.array([b.type == 2 for b in sc.bodies])
+    x1[dyn, :3] += 0.005 * V[dyn, :3]
+    x1[dyn, 1] -= 9.81 * 0.005 ** 2
+    r = pass_rates_tuned(rigc.Context(sc), P.reshape(-1), x1.reshape(-1), 1e-4, torch)
+    r["steps_per_s"] = 5 / dt
+    r["newton_iterations_per_step"] = st["newton_iterations"] / 5
+    r["cg_iterations_per_newton"] = st["cg_iterations"] / max(1, st["newton_iterations"])
+    out["chain_200"] = r
+    return out
+
+
 ADJOINT_WORKLOAD = ("64 unit cubes in a 4x4x4 lattice (spacing 1.05 m, seeded rotations, at rest) "
                     "landing on a static plane; 50 steps of 0.01 s, dhat 1e-3; loss |c0(T) - "
                     "(3, 0, 0.5)|^2; gradient over the 384 initial linear and angular velocities "
@@ -370,7 +467,8 @@ def batched_sim_rate(args, torch, items, big, sob, tune):
     grav = (0.0, -9.81, 0.0)
     K = args.batch_sim_steps
     cb = rigc.Context(big, scene_of_body=sob)
-    cb.set_tune(tune["ccd_blocks_per_sm"], tune["cache_slots_per_body"], tune["barrier_per_warp"])
+    cb.set_tune(tune["ccd_blocks_per_sm"], tune["cache_slots_per_body"], tune["barrier_per_warp"],
+                tune["ccd_seeds_log2"])
     cb.sim_init(0.01, grav, dhat, poses=X0)
     cb.sim_step(1)
     torch.cuda.synchronize()
@@ -470,6 +568,9 @@ def main():
     n_disc = len(ee_d) + len(fv_d)
     cs = ctx.construct_constraint_set(x0d, dhat)
     n_cons = len(cs["type"])
+    # launch shapes chosen by the autotuner on this workload (part of the
+    # framework's set-up, before the warm-up)
+    tune = ctx.autotune(x0d, x1d, dhat) if not args.no_autotune else None
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -557,6 +658,7 @@ def main():
                 "d2h_bytes_per_step": d2h},
         "clocks": clk.summary(),
         "gpu_launches": launches,
+        "autotune": tune,
     }
     if rank == 0 and not args.no_sim:
         line["steps_per_s"] = sim_rate(args, torch)
@@ -564,6 +666,8 @@ def main():
         line["batched"] = batched_rate(args, torch)
     if rank == 0 and not args.no_adjoint:
         line["adjoint"] = adjoint_rate(args, torch)
+    if rank == 0 and not args.no_configs:
+        line["per_config"] = per_config(args, torch)
     if rank == 0 and not args.no_cpu_baseline:
         base = cpu_baseline(sc, x0, x1, dhat)
         v = combined_rate(n_ccd, n_disc, base["ccd_pairs_per_s"], base["barrier_pairs_per_s"])

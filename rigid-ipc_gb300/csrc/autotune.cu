@@ -7,6 +7,9 @@
 //    leave the FP64 pipes less contended, more hide latency;
 //  * the CCD frame cache's slots per body (256 .. 4096): fewer slots clear
 //    faster, more keep frames of deep searches;
+//  * the CCD searches per candidate (1 .. 32, from the nodes of its
+//    subdivision tree at that depth): more fill the GPU when candidates are
+//    few or deep, fewer skip the nodes above that depth;
 //  * k_barrier_local's constraints per warp (1 .. 32): one thread per
 //    constraint fills the SMs for small sets, a full warp per 32 constraints
 //    shares the PSD projections for large ones.
@@ -86,6 +89,17 @@ int autotune(Ctx& c, const double* x0, const double* x1, double dhat, double dmi
         }
     }
     c.tune.cache_slots_per_body = best_slots;
+    int best_seeds = -1;
+    for (int d = 0; d <= 5; d++) {
+        c.tune.ccd_seeds_log2 = d;
+        double ms;
+        RIGC_TRY(median_ms(ccd, &ms));
+        if (ms < best) {
+            best = ms;
+            best_seeds = d;
+        }
+    }
+    c.tune.ccd_seeds_log2 = best_seeds;
     r.ccd_ms = best;
     // barrier terms over the constraint set at x0
     RIGC_TRY(detect_and_count(c, x0, x0, false, (dhat + dmin) / 2.0));
@@ -111,6 +125,7 @@ int autotune(Ctx& c, const double* x0, const double* x1, double dhat, double dmi
     r.ccd_blocks_per_sm = c.tune.ccd_blocks_per_sm;
     r.cache_slots_per_body = c.tune.cache_slots_per_body;
     r.barrier_per_warp = c.tune.barrier_per_warp;
+    r.ccd_seeds_log2 = c.tune.ccd_seeds_log2;
     if (rep) *rep = r;
     return RIGC_OK;
 }

@@ -903,8 +903,11 @@ int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flag
         // few candidates: start each search from 2^d boxes of its tree so
         // that the searches fill the GPU (prune mode; at most 32 per candidate)
         a.seeds_log2 = 0;
-        if (a.prune)
-            while (a.seeds_log2 < 5 && (n << a.seeds_log2) * 4 < full * kCCDThreads) a.seeds_log2++;
+        if (a.prune) {
+            if (c.tune.ccd_seeds_log2 >= 0) a.seeds_log2 = std::min(c.tune.ccd_seeds_log2, 5);
+            else
+                while (a.seeds_log2 < 5 && (n << a.seeds_log2) * 4 < full * kCCDThreads) a.seeds_log2++;
+        }
         int64_t want = ((n << a.seeds_log2) + kCCDThreads - 1) / kCCDThreads;
         RIGC_COUNT_LAUNCH();
         k_ccd<<<(unsigned)std::min(want, full), kCCDThreads, 0, st>>>(a);

@@ -165,6 +165,7 @@ struct Ctx {
         int ccd_blocks_per_sm = 0;     // resident k_ccd blocks per SM (0: occupancy limit)
         int cache_slots_per_body = 0;  // CCD frame-cache slots per body (0: 1024)
         int barrier_per_warp = 0;      // constraints per warp of k_barrier_local (0: by count)
+        int ccd_seeds_log2 = -1;       // CCD searches per candidate, log2 (-1: by count)
     } tune;
     Sim* sim = nullptr;
     // batched contexts: per-scene results of the last calls

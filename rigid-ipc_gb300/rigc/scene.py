@@ -605,13 +605,19 @@ def spec_icospheres(seed=0, n=1000, box=(20.0, 40.0, 20.0), dt=0.01, dhat=1e-3,
     return spec
 
 
-def spec_chain(n=200, dt=0.005, dhat=1e-4, steps=400):
-    """Hanging chain of tori; link 0 fixed, odd links turned 90 deg about x."""
+def spec_chain(n=200, dt=0.005, dhat=1e-4, steps=400, spacing=1.5):
+    """Hanging chain of tori; link 0 fixed, odd links turned 90 deg about x.
+
+    At spacing 1.5 neighbouring links touch: the tubes (major radius 1, minor
+    0.25) meet at (0.75 + 1.5 i, 0, 0), where both 48 x 24 meshes have a
+    vertex, so the initial distance is zero up to rounding.  A spacing a
+    little below 1.5 leaves a gap of (1.5 - spacing) (a larger one makes the
+    links interpenetrate)."""
     spec = _base_spec(dt, dhat, steps)
     Vt, Ft = meshes.torus(1.0, 0.25, 48, 24)
     bodies = spec["rigid_body_problem"]["rigid_bodies"]
     for i in range(n):
-        d = _rb(Vt, Ft, position=[1.5 * i, 0, 0],
+        d = _rb(Vt, Ft, position=[spacing * i, 0, 0],
                 rotation=[90.0 if i % 2 else 0.0, 0, 0])
         if i == 0:
             d["type"] = "kinematic"

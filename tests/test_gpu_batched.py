@@ -143,9 +143,9 @@ def test_autotune_keeps_results():
     assert rep["ccd_ms"] <= rep["ccd_ms_default"] and rep["barrier_ms"] <= rep["barrier_ms_default"]
     b = run()
     assert a[0] == b[0] and np.array_equal(a[1], b[1])
-    for u, v in zip(a[2], b[2]):
-        assert np.array_equal(u, v)
+    for k in a[2]:
+        assert np.array_equal(np.asarray(a[2][k]), np.asarray(b[2][k])), k
     assert a[3] == b[3] and np.array_equal(a[4], b[4])
-    cb.set_tune(1, 256, 4)
+    cb.set_tune(1, 256, 4, 3)
     c = run()
     assert a[0] == c[0] and a[3] == c[3] and np.array_equal(a[4], c[4])

@@ -252,3 +252,45 @@ def test_error_statuses(cube_scene, ctx_c1):
     with pytest.raises(L.RigcError) as e:
         ctx_c1.narrow_phase_host(x, x, 1e-3)
     assert e.value.status == L.RIGC_ERR_NAN
+
+
+def test_chain_links_parity(oracle):
+    """Three links of the hanging chain (interlocked 48 x 24 tori with a 1 mm
+    gap, the edge-edge-dominated configuration; dhat 2e-3 so that the links
+    are in the constraint set): candidate sets, per-candidate times of impact
+    (a box budget of 2^14, the same on both sides), the constraint set and
+    the barrier term against the oracle."""
+    import rigc
+    from rigc import scene as S
+
+    sc = S.scene_from_json(S.spec_chain(3, spacing=1.499))
+    o = oracle.OracleScene(sc)
+    x0 = sc.poses()
+    x1 = x0.reshape(-1, 6).copy()
+    x1[1:, 1] -= 9.81 * 0.005 ** 2
+    x1[2, 4] += 1e-3  # and a small turn of the last link
+    x1 = x1.reshape(-1)
+    ctx = rigc.Context(sc)
+    ee_g, fv_g = ctx.detect_collision_candidates_rigid(x0, x1, True, 0.0)
+    ee_o, fv_o = o.detect_candidates(x0, x1, True, 0.0)
+    assert len(ee_o) > 100 and np.array_equal(ee_g, ee_o) and np.array_equal(fv_g, fv_o)
+    budget = 1 << 14
+    ctx.set_ccd_budget(budget)
+    toi_o, per_o, _, st_o = o.earliest_toi(x0, x1, ee_o, fv_o, per_candidate=True, nthreads=8,
+                                           max_boxes=budget, with_status=True)
+    toi_g, per_g, st_g = ctx.earliest_toi(x0, x1, prune=False, per_candidate=True)
+    assert np.array_equal(per_g, per_o) and toi_g == toi_o and st_g == st_o
+    dhat = 2e-3
+    cs = ctx.construct_constraint_set(x0, dhat)
+    ee, fv = o.detect_candidates(x0, continuous=False, inflation=dhat / 2)
+    cs_o = o.constraint_set(x0, ee, fv, dhat)
+    assert len(cs_o) > 0
+    a = _canon_constraints(cs_o.types, cs_o.verts, cs_o.prims, cs_o.bodies, cs_o.weight, cs_o.eps)
+    b = _canon_constraints(cs["type"], cs["verts"], cs["prims"], cs["bodies"], cs["weight"],
+                           cs["eps"])
+    for u, v in zip(a, b):
+        assert np.array_equal(u, v)
+    e_g, g_g, _ = ctx.compute_barrier_term(x0, dhat)
+    e_o, g_o, _ = o.barrier_term(x0, cs_o, dhat)
+    assert abs(e_g - e_o) <= ENERGY_RTOL * abs(e_o)
+    assert _rel_err(g_g, g_o) <= GRAD_RTOL
