@@ -38,6 +38,13 @@ import numpy as np  # noqa: E402
 METRIC = "candidate pairs/s (CCD+barrier grad/Hess)"
 UNIT = "pairs/s"
 CCD_BYTES_PER_PAIR = 304        # ids + 4 rest vertices + 4 poses + toi
+# DRAM bytes (read + write) per continuous candidate of one k_ccd launch,
+# from the ncu capture of the 200-icosphere pile (built-in shapes: 0.768 GB
+# read + 2.119 GB written for 132,242 candidates; profiles/
+# k_ccd_icosphere_pile_200.md); the traffic of a full launch is this times
+# its candidates (it is the box stacks' local memory, which grows with the
+# boxes, 42 per candidate there)
+K_CCD_DRAM_BYTES_PER_CANDIDATE = (0.768274e9 + 2.118710e9) / 132242
 BARRIER_BYTES_PER_CONSTRAINT = 1456
 
 
@@ -651,9 +658,12 @@ def main():
         "phases_s": {"ccd_narrow": t_ccd, "ccd_broad": t_bp, "barrier_and_assembly": t_bar},
         "ccd_pairs_per_s": n_ccd / t_ccd, "barrier_constraints_per_s": n_cons / t_bar,
         "roofline": {"bound": "hbm", "kernel": "k_ccd", "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                     "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": K_CCD_DRAM_BYTES_PER_CANDIDATE * n_ccd,
+                     "traffic_source": "ncu capture of the 200-icosphere pile scaled by candidates",
                      "peak_source": peak_kind,
-                     "note": "FP64-issue bound: algorithmic bytes are 304 B per candidate"},
+                     "note": "issue-bound (instruction fetch and FP64), not HBM: algorithmic bytes "
+                             "are 304 B per candidate; the DRAM traffic is the box stacks"},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "clocks": clk.summary(),
