@@ -350,6 +350,11 @@ def adjoint_rate(args, torch):
     v = vel[:, :3].clone().requires_grad_()
     w = vel[:, 3:].clone().requires_grad_()
     target = torch.tensor([3.0, 0.0, 0.5], **dev)
+    # warm-up: a short rollout and its backward (first-call set-up)
+    Pw, _, _ = sim(poses, torch.cat([v, w], 1), qdot_from_omega(poses, w), 2)
+    ((Pw[0, :3] - target) ** 2).sum().backward()
+    v.grad = None
+    w.grad = None
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     P, _, _ = sim(poses, torch.cat([v, w], 1), qdot_from_omega(poses, w), steps)
