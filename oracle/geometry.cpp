@@ -902,6 +902,16 @@ void body_energy_state_derivs(
         for (int j = 0; j < 24; j++) hess[24 * i + j] = e.h[i][j];
 }
 
+void rotation_matrix_hessian(const double* theta, double d2R[81])
+{
+    D2<3> t[3], R[9];
+    for (int i = 0; i < 3; i++) t[i] = D2<3>::var(theta[i], i);
+    rotation_matrix_ad<3>(t, R);
+    for (int a = 0; a < 3; a++)
+        for (int c = 0; c < 3; c++)
+            for (int k = 0; k < 9; k++) d2R[27 * a + 9 * c + k] = R[k].h[a][c];
+}
+
 void rotation_matrix_jacobian(const double* theta, double dR[27])
 {
     D2<3> t[3], R[9];

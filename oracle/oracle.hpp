@@ -301,11 +301,14 @@ void body_energy_state_derivs(
     double grad[24], double hess[576]);
 // dR / dtheta_a (a = 0..2), each row-major 3 x 3
 void rotation_matrix_jacobian(const double* theta, double dR[27]);
+// d2R / dtheta_a dtheta_c, [a][c] each row-major 3 x 3
+void rotation_matrix_hessian(const double* theta, double d2R[81]);
 
 // Adjoint of one time step (implicit differentiation of the converged
 // Newton solve): given dL / d(state after the step) in `in` (poses 6 nb,
 // velocities 6 nb, Qdot 9 nb), accumulate dL / d(state before) into `out`.
-// Returns false when the Hessian of the free dofs cannot be factorised.
+// Returns false when the Hessian of the free dofs cannot be factorised, or
+// when the scene has kinematic bodies (their targets are not differentiated).
 struct AdjointState {
     std::vector<double> pose, vel, Qdot;
 };

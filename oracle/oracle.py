@@ -467,7 +467,7 @@ class OracleSim:
                                         _p(x, _d), _p(rec, _d), _p(dp, _d), _p(dv, _d), _p(dq, _d),
                                         _p(op, _d), _p(ov, _d), _p(oq, _d))
             if rc != 0:
-                raise RuntimeError("adjoint: the Hessian of the free dofs is singular")
+                raise RuntimeError("adjoint: singular Hessian of the free dofs, or kinematic bodies")
             dp, dv, dq = op, ov, oq
         return dp.reshape(nb, 6), dv.reshape(nb, 6), dq.reshape(nb, 9)
 

@@ -90,6 +90,13 @@ struct Problem {
     std::vector<double> x0;
     SimStats* st;
     double s_average_mass;
+    // augmented Lagrangian of the kinematic bodies (init_augmented_lagrangian,
+    // distance_barrier_rb_problem.cpp:190-235): targets x_pred = x0 + h v,
+    // penalties, multipliers (3 per body linear, 3 x 3 angular), and whether
+    // the linear / angular constraints are satisfied
+    std::vector<double> x_pred, lam, Lam;
+    double kq = 1e3, kQ = 1e3;
+    bool sat_q = false, sat_Q = false, has_kinematic = false;
 
     Problem(const Scene& s_, const std::vector<BodyState>& b, const SimParams& p_, double k,
             SimStats* st_)
@@ -159,12 +166,142 @@ struct Problem {
                         H[(size_t)(6 * r + i) * N + 6 * h.col[k] + j] += scale * h.val[36 * k + 6 * i + j];
     }
 
+    static void jhalf(const double* I, double J[3], double Js[3])
+    {
+        J[0] = 0.5 * (-I[0] + I[1] + I[2]);
+        J[1] = 0.5 * (I[0] - I[1] + I[2]);
+        J[2] = 0.5 * (I[0] + I[1] - I[2]);
+        for (int k = 0; k < 3; k++) Js[k] = std::sqrt(std::max(J[k], 0.0));
+    }
+
+    // compute_augmented_lagrangian (:946-1109), added to g and H (unscaled);
+    // zero once every kinematic constraint is satisfied
+    double augmented_lagrangian(const double* x, std::vector<double>* g, std::vector<double>* H) const
+    {
+        if (!has_kinematic || (sat_q && sat_Q)) return 0.0;
+        const int N = n();
+        double e = 0;
+        for (int b = 0; b < s.nb; b++) {
+            if (bodies[b].type != 1) continue;
+            const double m = bodies[b].mass, sm = std::sqrt(m);
+            const double* q = x + 6 * b;
+            const double* qp = &x_pred[6 * b];
+            for (int i = 0; i < 3; i++) {
+                const double d = q[i] - qp[i];
+                e += kq / 2 * m * d * d - sm * lam[3 * b + i] * d;
+                if (g) (*g)[6 * b + i] += kq * m * d - sm * lam[3 * b + i];
+                if (H) (*H)[(size_t)(6 * b + i) * N + 6 * b + i] += kq * m;
+            }
+            double J[3], Js[3];
+            jhalf(bodies[b].moment, J, Js);
+            double Qp[9], Qv[9], dQ[27];
+            rotation_matrix(qp + 3, Qp);
+            rotation_matrix(q + 3, Qv);
+            rotation_matrix_jacobian(q + 3, dQ);
+            // kQ/2 tr((Q - Qp) J (Q - Qp)^T) - tr(Lam^T (Q - Qp) Js)
+            double ga[3] = { 0, 0, 0 };
+            for (int i = 0; i < 3; i++)
+                for (int k = 0; k < 3; k++) {
+                    const double d = Qv[3 * i + k] - Qp[3 * i + k];
+                    const double L = Lam[9 * b + 3 * i + k];
+                    e += kQ / 2 * J[k] * d * d - L * d * Js[k];
+                    const double c = kQ * J[k] * d - L * Js[k];
+                    for (int a = 0; a < 3; a++) ga[a] += c * dQ[9 * a + 3 * i + k];
+                }
+            if (g)
+                for (int a = 0; a < 3; a++) (*g)[6 * b + 3 + a] += ga[a];
+            if (H) {
+                double d2Q[81];
+                rotation_matrix_hessian(q + 3, d2Q);
+                for (int a = 0; a < 3; a++)
+                    for (int c2 = 0; c2 < 3; c2++) {
+                        double h = 0;
+                        for (int i = 0; i < 3; i++)
+                            for (int k = 0; k < 3; k++) {
+                                const double d = Qv[3 * i + k] - Qp[3 * i + k];
+                                const double c = kQ * J[k] * d - Lam[9 * b + 3 * i + k] * Js[k];
+                                h += kQ * J[k] * dQ[9 * a + 3 * i + k] * dQ[9 * c2 + 3 * i + k]
+                                    + c * d2Q[27 * a + 9 * c2 + 3 * i + k];
+                            }
+                        (*H)[(size_t)(6 * b + 3 + a) * N + 6 * b + 3 + c2] += h;
+                    }
+            }
+        }
+        return e;
+    }
+
+    // compute_{linear,angular}_augment_lagrangian_progress (:265-337)
+    void al_progress(const double* x, double& eq, double& eQ) const
+    {
+        double aq = 0, bq = 0, aQ = 0, bQ = 0;
+        for (int b = 0; b < s.nb; b++) {
+            if (bodies[b].type != 1) continue;
+            for (int i = 0; i < 3; i++) {
+                aq += (x_pred[6 * b + i] - x[6 * b + i]) * (x_pred[6 * b + i] - x[6 * b + i]);
+                bq += (x_pred[6 * b + i] - x0[6 * b + i]) * (x_pred[6 * b + i] - x0[6 * b + i]);
+            }
+            double Qp[9], Qv[9], Q0[9];
+            rotation_matrix(&x_pred[6 * b + 3], Qp);
+            rotation_matrix(x + 6 * b + 3, Qv);
+            rotation_matrix(&x0[6 * b + 3], Q0);
+            for (int k = 0; k < 9; k++) {
+                aQ += (Qv[k] - Qp[k]) * (Qv[k] - Qp[k]);
+                bQ += (Q0[k] - Qp[k]) * (Q0[k] - Qp[k]);
+            }
+        }
+        eq = (aq == 0 && bq == 0) ? 1.0 : 1 - std::sqrt(aq / (bq == 0 ? 1 : bq));
+        eQ = (aQ == 0 && bQ == 0) ? 1.0 : 1 - std::sqrt(aQ / (bQ == 0 ? 1 : bQ));
+    }
+
+    bool al_satisfied(const double* x) const
+    {
+        if (!has_kinematic) return true;
+        double eq, eQ;
+        al_progress(x, eq, eQ);
+        return eq >= 0.999 && eQ >= 0.999;
+    }
+
+    // update_augmented_lagrangian (:339-423)
+    void al_update(const double* x)
+    {
+        double eq, eQ;
+        al_progress(x, eq, eQ);
+        if (eq >= 0.999) {
+            sat_q = true;
+        } else if (eq < 0.99 && kq < 1e8) {
+            kq *= 2;
+        } else {
+            for (int b = 0; b < s.nb; b++)
+                if (bodies[b].type == 1)
+                    for (int i = 0; i < 3; i++)
+                        lam[3 * b + i] -= kq * std::sqrt(bodies[b].mass) * (x[6 * b + i] - x_pred[6 * b + i]);
+        }
+        if (eQ >= 0.999) {
+            sat_Q = true;
+        } else if (eQ < 0.99 && kQ < 1e8) {
+            kQ *= 2;
+        } else {
+            for (int b = 0; b < s.nb; b++) {
+                if (bodies[b].type != 1) continue;
+                double Qp[9], Qv[9], J[3], Js[3];
+                rotation_matrix(&x_pred[6 * b + 3], Qp);
+                rotation_matrix(x + 6 * b + 3, Qv);
+                jhalf(bodies[b].moment, J, Js);
+                for (int i = 0; i < 3; i++)
+                    for (int k = 0; k < 3; k++)
+                        Lam[9 * b + 3 * i + k] -= kQ * (Qv[3 * i + k] - Qp[3 * i + k]) * Js[k];
+            }
+        }
+    }
+
     // compute_objective (:633-703)
     double objective(const double* x, std::vector<double>* g, std::vector<double>* H) const
     {
         const int N = n();
         const double m = s_average_mass;
-        double f = energy_term(x, g, H) / m;
+        double f = energy_term(x, g, H);
+        f += augmented_lagrangian(x, g, H);
+        f /= m;
         if (g)
             for (double& v : *g) v /= m;
         if (H)
@@ -214,6 +351,15 @@ void simulation_step(const Scene& s, std::vector<BodyState>& bodies, const SimPa
     for (int b = 0; b < nb; b++)
         for (int k = 0; k < 6; k++) pr.x0[6 * b + k] = bodies[b].pose_t0[k];
     const double* x0 = pr.x0.data();
+    // init_augmented_lagrangian: kinematic targets x0 + h v
+    pr.x_pred = pr.x0;
+    pr.lam.assign(3 * (size_t)nb, 0.0);
+    pr.Lam.assign(9 * (size_t)nb, 0.0);
+    for (int b = 0; b < nb; b++)
+        if (bodies[b].type == 1) {
+            pr.has_kinematic = true;
+            for (int k = 0; k < 6; k++) pr.x_pred[6 * b + k] += p.h * bodies[b].vel_t0[k];
+        }
 
     // update_constraints: lagged friction at x0 with the current stiffness
     if (p.mu > 0) {
@@ -259,6 +405,7 @@ void simulation_step(const Scene& s, std::vector<BodyState>& bodies, const SimPa
 
     std::vector<double> x = pr.x0, g, H, dir(N, 0.0), gdir(N, 0.0);
     double coeff = 0;
+    bool energy_converged = false;
     int it = 0;
     for (; it < p.max_newton_iterations; it++) {
         double fx = pr.objective(x.data(), &g, &H);
@@ -304,7 +451,10 @@ void simulation_step(const Scene& s, std::vector<BodyState>& bodies, const SimPa
             double m = 0;
             for (size_t k = 0; k < V.size(); k++) m = std::max(m, std::fabs(V1[k] - V[k]));
             double tol = p.velocity_conv_tol * (p.velocity_conv_tol_abs ? 1.0 : p.bbox_diagonal);
-            if (m / p.h <= tol) break;
+            // converged (:95-156): the velocity test and the kinematic
+            // equality constraints
+            energy_converged = m / p.h <= tol;
+            if (energy_converged && pr.al_satisfied(x.data())) break;
         }
         auto line_search = [&](const std::vector<double>& d, double& alpha) {
             double gd = 0;
@@ -333,6 +483,8 @@ void simulation_step(const Scene& s, std::vector<BodyState>& bodies, const SimPa
         }
         for (int k = 0; k < N; k++) x[k] += alpha * dir[k];
         if (st) st->newton_steps++;
+        // NewtonSolver::post_step_update (:606-612): augmented Lagrangian
+        if (energy_converged && !pr.al_satisfied(x.data())) pr.al_update(x.data());
         // IPCSolver::post_step_update: adaptive stiffness
         double md = pr.min_distance(x.data());
         double eps = p.dhat_epsilon * (p.bbox_diagonal + p.dmin);
@@ -356,6 +508,7 @@ void simulation_step(const Scene& s, std::vector<BodyState>& bodies, const SimPa
         {
             const double m = pr.s_average_mass;
             pr.energy_term(x.data(), &gp, &Hp);
+            pr.augmented_lagrangian(x.data(), &gp, &Hp);
             for (double& v : gp) v /= m;
             for (double& v : Hp) v /= m;
             std::vector<Constraint> cs = pr.constraints(x.data());
@@ -395,6 +548,8 @@ void simulation_step(const Scene& s, std::vector<BodyState>& bodies, const SimPa
     for (int b = 0; b < nb; b++) {
         BodyState& B = bodies[b];
         if (B.type != 2) {
+            // set_rb_poses moves every body; only dynamic ones get velocities
+            for (int k = 0; k < 6; k++) B.pose_t0[k] = x[6 * b + k];
             continue;
         }
         double Q[9], Qp[9];
@@ -425,6 +580,8 @@ bool adjoint_step(const Scene& s, const std::vector<BodyState>& pre, const SimPa
                   const StepRecord& rec, const AdjointState& in, AdjointState& out)
 {
     const int nb = s.nb, N = 6 * nb;
+    for (int b = 0; b < nb; b++)
+        if (pre[b].type == 1) return false;  // kinematic bodies are not differentiated
     const double M = p.average_mass, h = p.h;
     const double* x = rec.x.data();
     out.pose.assign(N, 0.0);

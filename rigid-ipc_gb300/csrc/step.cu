@@ -555,6 +555,157 @@ __global__ void __launch_bounds__(256) k_ldlt_solve(const double* __restrict__ A
 }
 
 // ---------------------------------------------------------------------------
+// augmented Lagrangian of kinematic bodies
+// (DistanceBarrierRBProblem::compute_augmented_lagrangian,
+// src/problems/distance_barrier_rb_problem.cpp:946-1109): for a kinematic
+// body with target x_pred = x0 + h v (init_augmented_lagrangian, :190-235)
+//   kq/2 m |q - q_pred|^2 - sqrt(m) lam.(q - q_pred)
+//   + kQ/2 tr((Q - Q_pred) J (Q - Q_pred)^T) - tr(Lam^T (Q - Q_pred) Js)
+// with J = diag(1/2 (-I0 + I1 + I2), ...) and Js = sqrt(J).
+
+__device__ __forceinline__ void al_J(const double* I, double J[3], double Js[3])
+{
+    J[0] = 0.5 * (-I[0] + I[1] + I[2]);
+    J[1] = 0.5 * (I[0] - I[1] + I[2]);
+    J[2] = 0.5 * (I[0] + I[1] - I[2]);
+    for (int k = 0; k < 3; k++) Js[k] = sqrt(fmax(J[k], 0.0));
+}
+
+__global__ void k_al_init(int nb, const int* __restrict__ type, const double* __restrict__ x0,
+                          const double* __restrict__ v, double h, double* __restrict__ xpred,
+                          double* __restrict__ lam, double* __restrict__ Lam)
+{
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    for (int k = 0; k < 6; k++) xpred[6 * b + k] = x0[6 * b + k] + (type[b] == RIGC_BODY_KINEMATIC ? h * v[6 * b + k] : 0.0);
+    for (int k = 0; k < 3; k++) lam[3 * b + k] = 0;
+    for (int k = 0; k < 9; k++) Lam[9 * b + k] = 0;
+}
+
+// energies (per body, 0 for the others) and, when asked, gradient and
+// Hessian blocks added into the body-energy arrays
+__global__ void k_al_terms(int nb, const int* __restrict__ type, const double* __restrict__ x,
+                           const double* __restrict__ xpred, const double* __restrict__ mass,
+                           const double* __restrict__ moment, const double* __restrict__ lam,
+                           const double* __restrict__ Lam, double kq, double kQ,
+                           double* __restrict__ energy, double* __restrict__ grad,
+                           double* __restrict__ hess)
+{
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    if (type[b] != RIGC_BODY_KINEMATIC) {
+        energy[b] = 0;
+        return;
+    }
+    const double m = mass[b], sm = sqrt(m);
+    const double* q = x + 6 * b;
+    const double* qp = xpred + 6 * b;
+    double e = 0;
+    for (int i = 0; i < 3; i++) {
+        const double d = q[i] - qp[i];
+        e += kq / 2 * m * d * d - sm * lam[3 * b + i] * d;
+        if (grad) grad[6 * b + i] += kq * m * d - sm * lam[3 * b + i];
+        if (hess) hess[36 * (size_t)b + 7 * i] += kq * m;
+    }
+    double J[3], Js[3];
+    al_J(moment + 3 * b, J, Js);
+    double F[kFrameDoubles], Qp[9];
+    const double t[3] = { q[3], q[4], q[5] };
+    const double tp[3] = { qp[3], qp[4], qp[5] };
+    body_frame(t, F);
+    rot_rn(tp, Qp);
+    double c[9];
+    for (int i = 0; i < 3; i++)
+        for (int k = 0; k < 3; k++) {
+            const double d = F[3 * i + k] - Qp[3 * i + k];
+            const double L = Lam[9 * b + 3 * i + k];
+            e += kQ / 2 * J[k] * d * d - L * d * Js[k];
+            c[3 * i + k] = kQ * J[k] * d - L * Js[k];
+        }
+    energy[b] = e;
+    if (grad)
+        for (int a = 0; a < 3; a++) {
+            double acc = 0;
+            for (int r = 0; r < 9; r++) acc += c[r] * F[9 + 9 * a + r];
+            grad[6 * b + 3 + a] += acc;
+        }
+    if (hess)
+        for (int a = 0; a < 3; a++)
+            for (int cc = 0; cc < 3; cc++) {
+                const double* d2 = F + 36 + 9 * sym_index(a, cc);
+                double acc = 0;
+                for (int i = 0; i < 3; i++)
+                    for (int k = 0; k < 3; k++)
+                        acc += kQ * J[k] * F[9 + 9 * a + 3 * i + k] * F[9 + 9 * cc + 3 * i + k]
+                            + c[3 * i + k] * d2[3 * i + k];
+                hess[36 * (size_t)b + 6 * (3 + a) + 3 + cc] += acc;
+            }
+}
+
+// progress sums (compute_{linear,angular}_augment_lagrangian_progress,
+// :265-337): out = (|q_pred - q|^2, |q_pred - q0|^2, |Q - Q_pred|^2,
+// |Q0 - Q_pred|^2) over the kinematic bodies, one block
+__global__ void __launch_bounds__(256) k_al_progress(int nb, const int* __restrict__ type,
+                                                     const double* __restrict__ x,
+                                                     const double* __restrict__ xpred,
+                                                     const double* __restrict__ x0,
+                                                     double* __restrict__ out)
+{
+    __shared__ double sh[4][256];
+    double a[4] = { 0, 0, 0, 0 };
+    for (int b = threadIdx.x; b < nb; b += 256) {
+        if (type[b] != RIGC_BODY_KINEMATIC) continue;
+        for (int i = 0; i < 3; i++) {
+            const double d = xpred[6 * b + i] - x[6 * b + i], d0 = xpred[6 * b + i] - x0[6 * b + i];
+            a[0] += d * d;
+            a[1] += d0 * d0;
+        }
+        double Q[9], Qp[9], Q0[9];
+        const double t[3] = { x[6 * b + 3], x[6 * b + 4], x[6 * b + 5] };
+        const double tp[3] = { xpred[6 * b + 3], xpred[6 * b + 4], xpred[6 * b + 5] };
+        const double t0[3] = { x0[6 * b + 3], x0[6 * b + 4], x0[6 * b + 5] };
+        rot_rn(t, Q);
+        rot_rn(tp, Qp);
+        rot_rn(t0, Q0);
+        for (int k = 0; k < 9; k++) {
+            a[2] += (Q[k] - Qp[k]) * (Q[k] - Qp[k]);
+            a[3] += (Q0[k] - Qp[k]) * (Q0[k] - Qp[k]);
+        }
+    }
+    for (int j = 0; j < 4; j++) sh[j][threadIdx.x] = a[j];
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o)
+            for (int j = 0; j < 4; j++) sh[j][threadIdx.x] += sh[j][threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x < 4) out[threadIdx.x] = sh[threadIdx.x][0];
+}
+
+// multiplier updates of update_augmented_lagrangian (:339-423)
+__global__ void k_al_update(int nb, const int* __restrict__ type, const double* __restrict__ x,
+                            const double* __restrict__ xpred, const double* __restrict__ mass,
+                            const double* __restrict__ moment, int upd_q, int upd_Q, double kq,
+                            double kQ, double* __restrict__ lam, double* __restrict__ Lam)
+{
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb || type[b] != RIGC_BODY_KINEMATIC) return;
+    if (upd_q)
+        for (int i = 0; i < 3; i++)
+            lam[3 * b + i] -= kq * sqrt(mass[b]) * (x[6 * b + i] - xpred[6 * b + i]);
+    if (upd_Q) {
+        double J[3], Js[3], Q[9], Qp[9];
+        al_J(moment + 3 * b, J, Js);
+        const double t[3] = { x[6 * b + 3], x[6 * b + 4], x[6 * b + 5] };
+        const double tp[3] = { xpred[6 * b + 3], xpred[6 * b + 4], xpred[6 * b + 5] };
+        rot_rn(t, Q);
+        rot_rn(tp, Qp);
+        for (int i = 0; i < 3; i++)
+            for (int k = 0; k < 3; k++) Lam[9 * b + 3 * i + k] -= kQ * (Q[3 * i + k] - Qp[3 * i + k]) * Js[k];
+    }
+}
+
+// ---------------------------------------------------------------------------
 // per-scene kernels of batched contexts (bodies ordered by scene)
 
 // out[s] = sum over scene s's dofs of a[i] b[i] (b null: sum of a), one block
@@ -900,6 +1051,10 @@ struct Sim {
     // convergence); per-scene device scalars and reduction outputs
     std::vector<double> sc_mass, sc_bbox;
     DevBuf sc_dev, sc_red, sc_vstart;
+    // augmented Lagrangian of kinematic bodies (per step)
+    bool has_kinematic = false, al_sat_q = false, al_sat_Q = false;
+    double al_kq = 1e3, al_kQ = 1e3;
+    DevBuf al_xpred, al_lam, al_Lam, al_e;
 };
 
 namespace {
@@ -947,6 +1102,18 @@ int objective(Ctx& c, Sim& S, const double* x, bool grad_hess, Objective& O, boo
     double E;
     RIGC_TRY(body_energy(c, bs, x, p.gravity, p.timestep, &E, grad_hess ? S.gE.as<double>() : nullptr,
                          grad_hess ? S.hE.as<double>() : nullptr));
+    if (S.has_kinematic && !(S.al_sat_q && S.al_sat_Q)) {
+        RIGC_COUNT_LAUNCH();
+        k_al_terms<<<grid_for(S.nb, 128), 128, 0, c.stream>>>(
+            S.nb, c.s.type, x, S.al_xpred.as<double>(), S.mass.as<double>(), S.moment.as<double>(),
+            S.al_lam.as<double>(), S.al_Lam.as<double>(), S.al_kq, S.al_kQ, S.al_e.as<double>(),
+            grad_hess ? S.gE.as<double>() : nullptr, grad_hess ? S.hE.as<double>() : nullptr);
+        double* e_dev = reinterpret_cast<double*>(c.d_scalars.as<char>() + 2568);
+        RIGC_TRY(sum_f64(S.al_e.as<double>(), S.nb, e_dev, c.scratch[1], c.stream));
+        double al;
+        RIGC_TRY(read_scalars(c, e_dev, &al, 1));
+        E += al;
+    }
     RIGC_TRY(build_constraints(c, x, p.dhat, p.dmin));
     const int flags = grad_hess ? (RIGC_GRAD | RIGC_HESS | (project ? RIGC_PROJECT_PSD : 0)) : 0;
     RIGC_TRY(barrier_term_impl(c, x, p.dhat, p.dmin, flags, &O.bo));
@@ -1150,6 +1317,53 @@ int max_vertex_move(Ctx& c, Sim& S, const double* x, const double* x1, double* m
     k_max_vertex_move<<<grid_for(3 * (int64_t)S.nv, 256), 256, 0, c.stream>>>(
         S.nv, S.V0.as<double>(), S.V1.as<double>(), out);
     RIGC_TRY(read_scalars(c, reinterpret_cast<double*>(out), m, 1));
+    return RIGC_OK;
+}
+
+int al_progress(Ctx& c, Sim& S, const double* x, double& eq, double& eQ)
+{
+    double* out = S.scal.as<double>() + 16;
+    RIGC_COUNT_LAUNCH();
+    k_al_progress<<<1, 256, 0, c.stream>>>(S.nb, c.s.type, x, S.al_xpred.as<double>(),
+                                           S.x0.as<double>(), out);
+    double a[4];
+    RIGC_TRY(read_scalars(c, out, a, 4));
+    eq = (a[0] == 0 && a[1] == 0) ? 1.0 : 1 - std::sqrt(a[0] / (a[1] == 0 ? 1 : a[1]));
+    eQ = (a[2] == 0 && a[3] == 0) ? 1.0 : 1 - std::sqrt(a[2] / (a[3] == 0 ? 1 : a[3]));
+    return RIGC_OK;
+}
+
+// are_equality_constraints_satisfied (:425-431)
+int al_satisfied(Ctx& c, Sim& S, const double* x, bool& sat)
+{
+    sat = true;
+    if (!S.has_kinematic) return RIGC_OK;
+    double eq, eQ;
+    RIGC_TRY(al_progress(c, S, x, eq, eQ));
+    sat = eq >= 0.999 && eQ >= 0.999;
+    return RIGC_OK;
+}
+
+// update_augmented_lagrangian (:339-423)
+int al_update(Ctx& c, Sim& S, const double* x)
+{
+    double eq, eQ;
+    RIGC_TRY(al_progress(c, S, x, eq, eQ));
+    int upd_q = 0, upd_Q = 0;
+    const double kq = S.al_kq, kQ = S.al_kQ;
+    if (eq >= 0.999) S.al_sat_q = true;
+    else if (eq < 0.99 && S.al_kq < 1e8) S.al_kq *= 2;
+    else upd_q = 1;
+    if (eQ >= 0.999) S.al_sat_Q = true;
+    else if (eQ < 0.99 && S.al_kQ < 1e8) S.al_kQ *= 2;
+    else upd_Q = 1;
+    if (upd_q || upd_Q) {
+        RIGC_COUNT_LAUNCH();
+        k_al_update<<<grid_for(S.nb, 128), 128, 0, c.stream>>>(
+            S.nb, c.s.type, x, S.al_xpred.as<double>(), S.mass.as<double>(), S.moment.as<double>(),
+            upd_q, upd_Q, kq, kQ, S.al_lam.as<double>(), S.al_Lam.as<double>());
+        RIGC_CUDA(cudaGetLastError());
+    }
     return RIGC_OK;
 }
 
@@ -1416,7 +1630,7 @@ int sim_step_scenes(Ctx& c, rigc_step_stats* stats)
 {
     Sim& S = *c.sim;
     const rigc_sim_params& p = S.p;
-    if (p.coefficient_friction > 0 || p.newton_polish > 0) return RIGC_ERR_ARG;
+    if (p.coefficient_friction > 0 || p.newton_polish > 0 || S.has_kinematic) return RIGC_ERR_ARG;
     const int ns = c.s.nscenes, nb = S.nb;
     const int64_t n = 6 * (int64_t)nb;
     cudaStream_t st = c.stream;
@@ -1718,6 +1932,12 @@ int sim_init(Ctx& c, const rigc_sim_params& p, const rigc_sim_state& s)
                                   cudaMemcpyHostToDevice, st));
         RIGC_CUDA(cudaStreamSynchronize(st));
     }
+    S.has_kinematic = false;
+    for (int b = 0; b < nb; b++) S.has_kinematic |= c.s.h_type[b] == RIGC_BODY_KINEMATIC;
+    RIGC_TRY(S.al_xpred.reserve((size_t)nb * 48 + 64));
+    RIGC_TRY(S.al_lam.reserve((size_t)nb * 24 + 64));
+    RIGC_TRY(S.al_Lam.reserve((size_t)nb * 72 + 64));
+    RIGC_TRY(S.al_e.reserve((size_t)nb * 8 + 64));
     S.kappa = 1;  // m_barrier_stiffness before the first solve
     S.tape_steps = 0;
     S.tape_every = 0;
@@ -1743,6 +1963,15 @@ int sim_step(Ctx& c, rigc_step_stats* stats)
     if (p.coefficient_friction > 0) {
         RIGC_TRY(build_constraints(c, x0, p.dhat, p.dmin));
         RIGC_TRY(friction_setup(c, x0, p.dhat, S.kappa, p.coefficient_friction, 0.0));
+    }
+    // init_augmented_lagrangian: kinematic targets x0 + h v
+    S.al_kq = S.al_kQ = 1e3;
+    S.al_sat_q = S.al_sat_Q = false;
+    if (S.has_kinematic) {
+        RIGC_COUNT_LAUNCH();
+        k_al_init<<<grid_for(nb, 128), 128, 0, st>>>(nb, c.s.type, x0, S.vel.as<double>(), p.timestep,
+                                                     S.al_xpred.as<double>(), S.al_lam.as<double>(),
+                                                     S.al_Lam.as<double>());
     }
 
     // IPCSolver::init_solve
@@ -1773,6 +2002,7 @@ int sim_step(Ctx& c, rigc_step_stats* stats)
 
     RIGC_CUDA(cudaMemcpyAsync(x, x0, n * 8, cudaMemcpyDeviceToDevice, st));
     double coeff = 0;
+    bool energy_converged = false;
     int it = 0;
     for (; it < p.max_newton_iterations; it++) {
         Objective O;
@@ -1811,7 +2041,10 @@ int sim_step(Ctx& c, rigc_step_stats* stats)
             double mv;
             RIGC_TRY(max_vertex_move(c, S, x, xt, &mv));
             const double tol = p.velocity_conv_tol * (p.velocity_conv_tol_abs ? 1.0 : p.world_bbox_diagonal);
-            if (mv / p.timestep <= tol) break;
+            energy_converged = mv / p.timestep <= tol;
+            bool sat;
+            RIGC_TRY(al_satisfied(c, S, x, sat));
+            if (energy_converged && sat) break;
         }
         // line search (the gradient on the free dofs is S.g)
         auto line_search = [&](double& alpha, bool& found) -> int {
@@ -1854,6 +2087,12 @@ int sim_step(Ctx& c, rigc_step_stats* stats)
         RIGC_COUNT_LAUNCH();
         k_axpy<<<grid_for(n, 256), 256, 0, st>>>(n, alpha, dir, x, x);
         local.newton_steps++;
+        // NewtonSolver::post_step_update: augmented Lagrangian
+        if (energy_converged && S.has_kinematic) {
+            bool sat;
+            RIGC_TRY(al_satisfied(c, S, x, sat));
+            if (!sat) RIGC_TRY(al_update(c, S, x));
+        }
         // adaptive stiffness
         double md;
         RIGC_TRY(min_distance(c, S, x, &md));
@@ -2083,7 +2322,7 @@ int sim_backward(Ctx& c, const double* dp, const double* dv, const double* dq, d
 {
     if (!c.sim || !dp || !gp || !gv || !gq) return RIGC_ERR_ARG;
     Sim& S = *c.sim;
-    if (S.tape_every < 1 || S.p.coefficient_friction > 0) return RIGC_ERR_ARG;
+    if (S.tape_every < 1 || S.p.coefficient_friction > 0 || S.has_kinematic) return RIGC_ERR_ARG;
     const int nb = S.nb, K = S.tape_every, steps = S.tape_steps;
     const size_t w = 21 * (size_t)nb;
     cudaStream_t st = c.stream;
@@ -2143,7 +2382,8 @@ void sim_release(Ctx& c)
                        &S.Minv, &S.sol, &S.part, &S.scal, &S.V0, &S.V1, &S.free_idx,
                        &S.dense, &S.dense_b, &S.dense_x, &S.dense_d, &S.ckpt,
                        &S.final_state, &S.seg_pre, &S.seg_x, &S.adj, &S.adj_out, &S.xbar,
-                       &S.u1, &S.u2, &S.sc_dev, &S.sc_red, &S.sc_vstart };
+                       &S.u1, &S.u2, &S.sc_dev, &S.sc_red, &S.sc_vstart, &S.al_xpred,
+                       &S.al_lam, &S.al_Lam, &S.al_e };
     for (DevBuf* b : bufs) b->release();
     delete c.sim;
     c.sim = nullptr;

@@ -43,3 +43,25 @@ def test_cube_lattice_matches_oracle(oracle, cube_scene):
         assert err <= 1e-7, (k, err, st_o, st_g)
         assert kappa == pytest.approx(sim.kappa.value, rel=1e-12)
         assert np.abs(V.reshape(-1)[:] - sim.vel).reshape(-1, 6)[:, :3].max() <= 1e-5
+
+
+def test_kinematic_bodies_match_oracle(oracle):
+    """A kinematic cube (the augmented Lagrangian toward x0 + h v) pushing a
+    dynamic one across a plane: device poses after 3 steps against the
+    oracle's."""
+    import rigc
+
+    from test_kinematic_oracle import paddle_scene
+
+    sc = paddle_scene()
+    sim = oracle.OracleSim(sc, h=0.01, gravity=(0.0, -9.81, 0.0), dhat=1e-3)
+    ctx = rigc.Context(sc)
+    ctx.sim_init(0.01, (0.0, -9.81, 0.0), 1e-3)
+    for _ in range(3):
+        sim.step()
+        ctx.sim_step(1)
+        P, V, Q, k = ctx.sim_state()
+        assert np.abs(P.reshape(-1) - sim.pose).max() <= 1e-7
+    with pytest.raises(RuntimeError):  # kinematic bodies are not differentiated
+        ctx.sim_rollout(1, 1)
+        ctx.sim_backward(np.zeros((sc.num_bodies, 6)))
