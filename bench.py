@@ -211,10 +211,13 @@ def sim_rate(args, torch):
     ctx.sim_init(0.01, (0.0, -9.81, 0.0), 1e-3)
     ctx.sim_step(SIM_FIRST)  # the timed steps include the landings on the plane
     torch.cuda.synchronize()
+    # the timed steps are the NVTX range "sim_steps" (ncu --nvtx-include sim_steps/)
+    torch.cuda.nvtx.range_push("sim_steps")
     t = time.perf_counter()
     st = ctx.sim_step(args.sim_steps)
     torch.cuda.synchronize()
     dt = time.perf_counter() - t
+    torch.cuda.nvtx.range_pop()
     out = {"workload": SIM_WORKLOAD, "steps": args.sim_steps, "first_step": SIM_FIRST,
            "steps_per_s": args.sim_steps / dt,
            "newton_iterations_per_step": st["newton_iterations"] / args.sim_steps,

@@ -40,6 +40,7 @@ static thread_local std::string g_last_error;
 static std::atomic<int64_t> g_launches { 0 };
 
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void count_launches(int64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 int64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 // broad phase, then record the candidate counts (also on an early exit)

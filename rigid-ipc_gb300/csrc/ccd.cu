@@ -18,8 +18,9 @@
 // not depend on the order boxes are visited, so boxes whose t.lo is not below
 // the running minimum over all candidates can be skipped too: that never
 // changes the minimum.  One thread per candidate at a time, a depth-first
-// stack in local memory, the interval vertex positions cached per time
-// interval; the warp advances in lock step, one box per lane per iteration
+// search whose pending boxes are encoded as bits of the current tree path (in
+// registers, no stack in memory), the interval vertex positions cached per
+// time interval; the warp advances in lock step, one box per lane per iteration
 // (a lane whose search ends takes the next candidate in the same iteration),
 // and the per-candidate set-up that needs no search (tolerances, the
 // tolerance test) runs beforehand in a kernel of its own.  The
@@ -30,10 +31,10 @@
 // that is not there yet pushes the box back; at the top of the next
 // iteration the whole warp computes that frame together with its sibling and
 // their descendants three levels down (one converged pass instead of many
-// single-lane ones) and publishes them.  Every
-// stack and every search is bounded: on overflow or budget exhaustion the
-// candidate reports the smallest t.lo still unexplored (a conservative time
-// of impact) and an error status.
+// single-lane ones) and publishes them.  Every search is bounded in depth
+// (kMaxDepth splits, kMaxLevel per dimension) and in boxes: on overflow or
+// budget exhaustion the candidate reports the smallest t.lo still unexplored
+// (a conservative time of impact) and an error status.
 #include <algorithm>
 #include <cstring>
 
@@ -42,7 +43,6 @@
 
 namespace rigc {
 
-constexpr int kCCDStack = 128;
 constexpr int kCCDThreads = 128;
 
 struct CCDArgs {
@@ -546,37 +546,150 @@ __device__ __forceinline__ void record_min(const CCDArgs& a, const Query& q, dou
     atomicMin(a.gmin, b);
 }
 
-// The box of the candidate's subdivision tree at depth d reached by the
+// Search tree nodes.  Every box of a candidate's search is dyadic: per
+// dimension (t, alpha, beta) it is [i 2^-l, (i + 1) 2^-l] for a level l and
+// an index i, because the root is [0, 1]^3 and a split halves one dimension
+// at its midpoint, which is exact while l <= kMaxLevel.  So a box is a node
+// (levels, indices, depth = number of splits from the root), and the
+// depth-first search needs no box stack: the boxes a stack would hold are
+// the upper children of the depths at which the current path went to the
+// lower child.  A lane keeps the current node, a 128-bit mask of the depths
+// whose upper child is still pending, and two masks recording which depths
+// split t and which split alpha (the others split beta); a pending box is
+// rebuilt from the current node by undoing the splits below its depth.
+// Popping the deepest pending depth visits boxes in the order of a stack
+// that pushes the upper half first; the shallowest pending depth is the
+// stack's bottom, the box a work-sharing lane takes.
+typedef unsigned __int128 u128;
+constexpr int kMaxDepth = 120;  // splits along one path (mask bits)
+constexpr int kMaxLevel = 52;   // splits along one dimension (exact bounds)
+
+struct Node {
+    int lv[3];
+    unsigned long long ix[3];
+    int depth;
+};
+
+__device__ __forceinline__ u128 bit128(int k) { return (u128)1 << k; }
+
+__device__ __forceinline__ int popc128(u128 m)
+{
+    return __popcll((unsigned long long)m) + __popcll((unsigned long long)(m >> 64));
+}
+
+__device__ __forceinline__ int msb128(u128 m)
+{
+    const unsigned long long h = (unsigned long long)(m >> 64);
+    return h ? 127 - __clzll((long long)h) : 63 - __clzll((long long)(unsigned long long)m);
+}
+
+__device__ __forceinline__ int lsb128(u128 m)
+{
+    const unsigned long long l = (unsigned long long)m;
+    return l ? __ffsll((long long)l) - 1 : 63 + __ffsll((long long)(unsigned long long)(m >> 64));
+}
+
+// mask of the depths [lo, hi), hi <= kMaxDepth + 1
+__device__ __forceinline__ u128 range128(int lo, int hi) { return (bit128(hi) - 1) & ~(bit128(lo) - 1); }
+
+// i 2^-l for i <= 2^52, l <= kMaxLevel, assembled from its bits with integer
+// operations (off the FP64 pipe): exponent from the leading one, mantissa
+// from the bits below it
+__device__ __forceinline__ double dyadic(unsigned long long i, int l)
+{
+    const int e = 63 - __clzll((long long)(i | 1ull));  // i in [2^e, 2^(e + 1))
+    const unsigned long long m = (i << (52 - e)) & 0xfffffffffffffull;
+    const double v = __longlong_as_double((long long)(((unsigned long long)(1023 + e - l) << 52) | m));
+    return i ? v : 0.0;
+}
+
+// The box widths of the root finder, sub_up(hi, lo): the exact difference
+// 2^-l stepped one ulp up (the bit pattern of 2^-l plus one)
+__device__ __forceinline__ void node_widths(const Node& c, double w[3])
+{
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+        w[k] = __longlong_as_double((long long)(((unsigned long long)(1023 - c.lv[k]) << 52) + 1ull));
+}
+
+__device__ __forceinline__ Box node_box(const Node& c)
+{
+    return Box { dyadic(c.ix[0], c.lv[0]), dyadic(c.ix[0] + 1, c.lv[0]),
+                 dyadic(c.ix[1], c.lv[1]), dyadic(c.ix[1] + 1, c.lv[1]),
+                 dyadic(c.ix[2], c.lv[2]), dyadic(c.ix[2] + 1, c.lv[2]) };
+}
+
+// The split rule of interval_root_finder.cpp:151-178: the dimension with the
+// largest width / tolerance among those above tolerance (among all when
+// every width is within tolerance).
+__device__ __forceinline__ int split_dim(const double w[3], const double tol[3], bool all_tol)
+{
+    int split = -1;
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+        if ((all_tol || !le_nn(w[d], tol[d]))
+            && (split == -1 || !le_nn(RMUL(w[d], tol[split]), RMUL(w[split], tol[d]))))
+            split = d;
+    return split;
+}
+
+// record that depth k splits dimension s
+__device__ __forceinline__ void record_split(u128& mt, u128& ma, int k, int s)
+{
+    const u128 b = bit128(k);
+    mt = s == 0 ? (mt | b) : (mt & ~b);
+    ma = s == 1 ? (ma | b) : (ma & ~b);
+}
+
+// The upper child of c's ancestor at depth j, where c's path went to the
+// lower child: c's node at depth j + 1 with the splits of depths
+// j + 1 .. c.depth - 1 undone and its last index bit set.
+__device__ __forceinline__ Node pending_node(const Node& c, u128 mt, u128 ma, int j)
+{
+    const u128 r = range128(j + 1, c.depth);
+    const int ct = popc128(mt & r), ca = popc128(ma & r);
+    const int cb = c.depth - j - 1 - ct - ca;
+    Node g;
+    g.lv[0] = c.lv[0] - ct;
+    g.lv[1] = c.lv[1] - ca;
+    g.lv[2] = c.lv[2] - cb;
+    g.ix[0] = c.ix[0] >> ct;
+    g.ix[1] = c.ix[1] >> ca;
+    g.ix[2] = c.ix[2] >> cb;
+    const int s = (mt & bit128(j)) ? 0 : ((ma & bit128(j)) ? 1 : 2);
+    g.ix[s] |= 1ull;
+    g.depth = j + 1;
+    return g;
+}
+
+// The node of the candidate's subdivision tree at depth d reached by the
 // branches in the bits of j (most significant first, 0 = lower half).  The
 // split rule depends only on the widths and tolerances, so every box of a
 // level splits along the same dimension and these boxes are exactly the
 // tree's nodes at depth d: searching them one by one visits the tree's
 // leaves below them, hence finds the same earliest root box.
-__device__ __forceinline__ Box seed_box(int d, int64_t j, const double* tol)
+__device__ __forceinline__ Node seed_node(int d, int64_t j, const double* tol, u128& mt, u128& ma)
 {
-    Box x { 0.0, 1.0, 0.0, 1.0, 0.0, 1.0 };
+    Node c { { 0, 0, 0 }, { 0ull, 0ull, 0ull }, 0 };
     for (int l = d - 1; l >= 0; l--) {
-        double w[3] = { sub_up(x.t1, x.t0), sub_up(x.a1, x.a0), sub_up(x.b1, x.b0) };
-        bool all_tol = le_nn(w[0], tol[0]) && le_nn(w[1], tol[1]) && le_nn(w[2], tol[2]);
-        int split = -1;
-        for (int k = 0; k < 3; k++)
-            if ((all_tol || !le_nn(w[k], tol[k]))
-                && (split == -1 || !le_nn(RMUL(w[k], tol[split]), RMUL(w[split], tol[k]))))
-                split = k;
-        const bool hi = (j >> l) & 1;
-        double* lo_ = split == 0 ? &x.t0 : (split == 1 ? &x.a0 : &x.b0);
-        double* hi_ = split == 0 ? &x.t1 : (split == 1 ? &x.a1 : &x.b1);
-        const double m = RMUL(0.5, RADD(*lo_, *hi_));
-        if (hi) *lo_ = m;
-        else *hi_ = m;
+        double w[3];
+        node_widths(c, w);
+        const bool all_tol = le_nn(w[0], tol[0]) && le_nn(w[1], tol[1]) && le_nn(w[2], tol[2]);
+        const int s = split_dim(w, tol, all_tol);
+        record_split(mt, ma, c.depth, s);
+        c.lv[s]++;
+        c.ix[s] = 2 * c.ix[s] + (unsigned long long)((j >> l) & 1);
+        c.depth++;
     }
-    return x;
+    return c;
 }
 
 // Persistent kernel: each lane takes the next unprocessed candidate from a
-// global counter whenever its box stack runs empty.  Every iteration each
+// global counter whenever its search runs out of boxes.  Every iteration each
 // lane pops boxes until one survives the cheap tests (or takes a new
-// candidate's root box), then all lanes evaluate their boxes together.
+// candidate's root box), then all lanes evaluate their boxes together.  The
+// search state is the current node, the pending mask and the split masks
+// (all in registers): no box stack in local memory.
 __global__ void __launch_bounds__(kCCDThreads)
 k_ccd(CCDArgs a)
 {
@@ -584,8 +697,10 @@ k_ccd(CCDArgs a)
     unsigned long long tot_boxes = 0, tot_hits = 0, pops = 0;
     Query q;
     double tol[3] = { 0, 0, 0 };
-    Box stack[kCCDStack];  // boxes stack[sb .. sp): pop at sp, shared from sb
-    int sp = 0, sb = 0;
+    Node cn { { 0, 0, 0 }, { 0ull, 0ull, 0ull }, 0 };  // current node
+    bool has_cn = false;      // cn is still to be processed (lower child, retry, taken box)
+    u128 pend_hi = 0;         // depths whose upper child is pending
+    u128 mt = 0, ma = 0;      // depths that split t / alpha
     int64_t cur = -1;
     double earliest = INFINITY;
     bool found = false;
@@ -614,7 +729,8 @@ k_ccd(CCDArgs a)
         if (a.prune) {
             const unsigned idle = __ballot_sync(0xffffffffu, done);
             if (idle) {
-                int best = done ? 0 : sp - sb - 1, bl = lane;
+                // boxes left in a lane's search: pending upper children + cn
+                int best = done ? 0 : popc128(pend_hi) + (has_cn ? 1 : 0) - 1, bl = lane;
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) {
                     const int ob = __shfl_xor_sync(0xffffffffu, best, o);
@@ -626,16 +742,22 @@ k_ccd(CCDArgs a)
                 }
                 if (best >= 1) {
                     const int thief = __ffs(idle) - 1;
-                    Box g = stack[sb < sp ? sb : 0];
-                    if (lane == bl) sb++;
+                    // the victim's shallowest pending upper child (best >= 1
+                    // leaves at least one pending depth)
+                    Node g = cn;
+                    if (lane == bl) {
+                        const int j = lsb128(pend_hi);
+                        g = pending_node(cn, mt, ma, j);
+                        pend_hi &= ~bit128(j);
+                    }
                     const double e = __shfl_sync(0xffffffffu, earliest, bl);
                     const long long c = __shfl_sync(0xffffffffu, (long long)cur, bl);
-                    g.t0 = __shfl_sync(0xffffffffu, g.t0, bl);
-                    g.t1 = __shfl_sync(0xffffffffu, g.t1, bl);
-                    g.a0 = __shfl_sync(0xffffffffu, g.a0, bl);
-                    g.a1 = __shfl_sync(0xffffffffu, g.a1, bl);
-                    g.b0 = __shfl_sync(0xffffffffu, g.b0, bl);
-                    g.b1 = __shfl_sync(0xffffffffu, g.b1, bl);
+#pragma unroll
+                    for (int k = 0; k < 3; k++) {
+                        g.lv[k] = __shfl_sync(0xffffffffu, g.lv[k], bl);
+                        g.ix[k] = __shfl_sync(0xffffffffu, g.ix[k], bl);
+                    }
+                    g.depth = __shfl_sync(0xffffffffu, g.depth, bl);
                     if (lane == thief) {
                         cur = c;
                         load_candidate(a, cur, q);
@@ -647,9 +769,9 @@ k_ccd(CCDArgs a)
                         found = false;
                         status = RIGC_OK;
                         cboxes = 0;
-                        sb = 0;
-                        sp = 0;
-                        stack[sp++] = g;
+                        cn = g;
+                        has_cn = true;
+                        pend_hi = 0;
                         done = false;
                     }
                 }
@@ -658,8 +780,15 @@ k_ccd(CCDArgs a)
         bool have = false;
         Box x;
         if (!done) {
-            while (sp > sb) {
-                x = stack[--sp];
+            while (has_cn || pend_hi != 0) {
+                if (has_cn) {
+                    has_cn = false;
+                } else {
+                    const int j = msb128(pend_hi);
+                    pend_hi &= ~bit128(j);
+                    cn = pending_node(cn, mt, ma, j);
+                }
+                x = node_box(cn);
                 if (le_nn(earliest, x.t0)) continue;
                 if (a.prune) {
                     if ((++pops & 7) == 0) gbound = load_gmin(a, q);
@@ -700,8 +829,10 @@ k_ccd(CCDArgs a)
                     found = false;
                     status = RIGC_OK;
                     cboxes = 0;
-                    sb = sp = 0;
-                    x = seed_box(a.seeds_log2, w / n, tol);
+                    pend_hi = 0;
+                    has_cn = false;
+                    cn = seed_node(a.seeds_log2, w / n, tol, mt, ma);
+                    x = node_box(cn);
                     have = !(a.prune && le_nn(gbound, x.t0));
                     if (have && q.fv) {
                         double sl = add_dn(x.a0, x.b0), sh = add_up(x.a1, x.b1);
@@ -716,18 +847,22 @@ k_ccd(CCDArgs a)
         if (cboxes >= (unsigned long long)a.max_boxes) {
             // budget exhausted: the earliest unexplored t.lo is conservative
             double m = x.t0;
-            for (int s = sb; s < sp; s++) m = smin(m, stack[s].t0);
+            for (u128 r = pend_hi; r != 0; r &= r - 1) {
+                const Node g = pending_node(cn, mt, ma, lsb128(r));
+                m = smin(m, dyadic(g.ix[0], g.lv[0]));
+            }
             earliest = smin(earliest, m);
             found = true;
             status = RIGC_ERR_ITER_LIMIT;
-            sp = sb = 0;
+            pend_hi = 0;
+            has_cn = false;
             continue;
         }
         if (!(dbits(x.t0) == dbits(q.ct0) && dbits(x.t1) == dbits(q.ct1))) {
             const int miss = eval_vertices(a, own, q, Itv { x.t0, x.t1 });
             if (miss) {
                 // retry the box once the warp has computed the frame
-                stack[sp++] = x;
+                has_cn = true;
                 pend = true;
                 req_side = (miss & 1) ? 0 : 1;
                 req_body = req_side ? q.body_b : q.body_a;
@@ -738,7 +873,8 @@ k_ccd(CCDArgs a)
         cboxes++;
         tot_boxes++;
         if (!f_zero(q, x)) continue;
-        double w[3] = { sub_up(x.t1, x.t0), sub_up(x.a1, x.a0), sub_up(x.b1, x.b0) };
+        double w[3];
+        node_widths(cn, w);
         bool all_tol = le_nn(w[0], tol[0]) && le_nn(w[1], tol[1]) && le_nn(w[2], tol[2]);
         bool all_zero = le_nn(w[0], 1e-10) && le_nn(w[1], 1e-10) && le_nn(w[2], 1e-10);
         if ((is_pos(x.t0) || all_zero) && all_tol) {
@@ -750,40 +886,21 @@ k_ccd(CCDArgs a)
             }
             continue;
         }
-        int split = -1;
-#pragma unroll
-        for (int d = 0; d < 3; d++)
-            if ((all_tol || !le_nn(w[d], tol[d]))
-                && (split == -1 || !le_nn(RMUL(w[d], tol[split]), RMUL(w[split], tol[d]))))
-                split = d;
-        Box lo = x, hi = x;
-        if (split == 0) {
-            double m = RMUL(0.5, RADD(x.t0, x.t1));
-            lo.t1 = m;
-            hi.t0 = m;
-        } else if (split == 1) {
-            double m = RMUL(0.5, RADD(x.a0, x.a1));
-            lo.a1 = m;
-            hi.a0 = m;
-        } else {
-            double m = RMUL(0.5, RADD(x.b0, x.b1));
-            lo.b1 = m;
-            hi.b0 = m;
-        }
-        if (sp + 2 > kCCDStack && sb > 0) {
-            for (int s2 = sb; s2 < sp; s2++) stack[s2 - sb] = stack[s2];
-            sp -= sb;
-            sb = 0;
-        }
-        if (sp + 2 > kCCDStack) {
+        const int split = split_dim(w, tol, all_tol);
+        if (cn.depth >= kMaxDepth || cn.lv[split] >= kMaxLevel) {
             // cannot descend: keep the box's start as a conservative root
             earliest = smin(earliest, x.t0);
             found = true;
             status = RIGC_ERR_QUEUE_OVERFLOW;
             continue;
         }
-        stack[sp++] = hi;
-        stack[sp++] = lo;
+        // go to the lower half; the upper half is pending at this depth
+        record_split(mt, ma, cn.depth, split);
+        pend_hi |= bit128(cn.depth);
+        cn.lv[split]++;
+        cn.ix[split] <<= 1;
+        cn.depth++;
+        has_cn = true;
     }
     // warp-aggregated counters
 #pragma unroll

@@ -46,6 +46,8 @@ void set_error(int code, const char* what, const char* file, int line);
 
 // number of kernels this library has launched (for measurement)
 void count_launch();
+// kernels run by graph launches (counted after they ran)
+void count_launches(int64_t n);
 int64_t launch_count();
 #define RIGC_COUNT_LAUNCH() ::rigc::count_launch()
 

@@ -116,11 +116,11 @@ __device__ __forceinline__ void row_scales(const HessView& H, int b, double& sE,
     }
 }
 
-// y = H x on the free degrees of freedom (fixed rows and columns removed)
-__global__ void k_hess_matvec(HessView H, const double* __restrict__ x, double* __restrict__ y)
+// row i of y = H x on the free degrees of freedom (fixed rows and columns
+// removed)
+__device__ __forceinline__ void hess_row(const HessView& H, int i, const double* __restrict__ x,
+                                         double* __restrict__ y)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= 6 * H.nb) return;
     const int b = i / 6, r = i % 6;
     if ((H.fixed[b] >> r) & 1) {
         y[i] = 0;
@@ -144,6 +144,22 @@ __global__ void k_hess_matvec(HessView H, const double* __restrict__ x, double* 
             for (int c = 0; c < 6; c++) acc += sD * V[c] * x[6 * cb + c];
         }
     y[i] = acc + reg * x[i];
+}
+
+__global__ void k_hess_matvec(HessView H, const double* __restrict__ x, double* __restrict__ y)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < 6 * H.nb) hess_row(H, i, x, y);
+}
+
+// the same with the view read from device memory (the CG graphs keep their
+// arguments fixed; the view's scales change between solves)
+__global__ void k_hess_matvec_dev(const HessView* __restrict__ Hp, const double* __restrict__ x,
+                                  double* __restrict__ y)
+{
+    const HessView H = *Hp;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < 6 * H.nb) hess_row(H, i, x, y);
 }
 
 // inverse of each body's diagonal 6x6 block (free part; fixed rows and
@@ -261,10 +277,10 @@ __global__ void k_dot_final(const double* __restrict__ part, int m, double* __re
 // is within the tolerance (then the iteration has converged, and a zero
 // direction is not a breakdown)
 __global__ void k_cg_alpha(const double* __restrict__ rz, const double* __restrict__ pAp,
-                           const double* __restrict__ rr, double tol2,
+                           const double* __restrict__ rr, const double* __restrict__ tol2,
                            double* __restrict__ alpha, int* __restrict__ flags)
 {
-    if (flags[1] || *rr <= tol2) {
+    if (flags[1] || *rr <= *tol2) {
         flags[1] = 1;  // converged
         *alpha = 0;
         return;
@@ -298,6 +314,19 @@ __global__ void k_cg_direction(int64_t n, const double* __restrict__ rz_new,
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || flags[0] || flags[1]) return;
     p[i] = z[i] + (*rz_new / *rz_old) * p[i];
+}
+
+// Last node of the CG graph's loop body: counts the iteration and ends the
+// loop once the solve converged (flag or residual within tolerance), broke
+// down (flag or a non-finite residual) or ran max_it iterations.
+__global__ void k_cg_continue(const int* __restrict__ flags, const double* __restrict__ rr,
+                              const double* __restrict__ tol2, long long* __restrict__ iters,
+                              long long max_it, cudaGraphConditionalHandle loop)
+{
+    const long long it = ++*iters;
+    const double v = *rr;
+    const bool end = flags[0] || flags[1] || v <= *tol2 || !isfinite(v) || it >= max_it;
+    cudaGraphSetConditional(loop, end ? 0u : 1u);
 }
 
 // largest |V(x1) - V(x0)| coordinate over all vertices (max of non-negative
@@ -799,6 +828,30 @@ __global__ void k_cg_direction_sc(int nb, const int* __restrict__ bscene,
     p[i] = z[i] + (rz_new[sc] / rz_old[sc]) * p[i];
 }
 
+// Last node of the per-scene CG graph's loop body (one block): the loop
+// ends once every solved scene (mask) has converged or broken down, or after
+// max_it iterations.
+__global__ void __launch_bounds__(256) k_cg_continue_sc(int ns, const int* __restrict__ mask,
+                                                        const int* __restrict__ flags,
+                                                        const double* __restrict__ rr,
+                                                        const double* __restrict__ tol2,
+                                                        long long* __restrict__ iters,
+                                                        long long max_it,
+                                                        cudaGraphConditionalHandle loop)
+{
+    int open = 0;
+    for (int k = threadIdx.x; k < ns; k += blockDim.x) {
+        if (!mask[k]) continue;
+        const double v = rr[k];
+        if (!(flags[2 * k] || flags[2 * k + 1] || v <= tol2[k] || !isfinite(v))) open = 1;
+    }
+    open = __syncthreads_or(open);
+    if (threadIdx.x == 0) {
+        const long long it = ++*iters;
+        cudaGraphSetConditional(loop, (open && it < max_it) ? 1u : 0u);
+    }
+}
+
 // v[i] = 0 on the dofs of scenes whose mask differs from keep
 __global__ void k_mask_scenes(int nb, const int* __restrict__ bscene, const int* __restrict__ mask,
                               int keep, double* __restrict__ v)
@@ -1055,6 +1108,27 @@ struct Sim {
     bool has_kinematic = false, al_sat_q = false, al_sat_Q = false;
     double al_kq = 1e3, al_kQ = 1e3;
     DevBuf al_xpred, al_lam, al_Lam, al_e;
+    // CUDA graphs of the CG solvers' iteration loops (single problem, per
+    // scene): one while node whose body is one CG iteration ending in its
+    // continuation test.  Rebuilt when an argument (a buffer address or a
+    // size, the key) changes; the Hessian view they read is hview.
+    struct LoopGraph {
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        std::vector<unsigned long long> key;
+        int kernels = 0;  // kernel nodes per iteration
+        void release()
+        {
+            if (exec) cudaGraphExecDestroy(exec);
+            if (graph) cudaGraphDestroy(graph);
+            exec = nullptr;
+            graph = nullptr;
+            key.clear();
+        }
+    };
+    LoopGraph cg_one, cg_sc;
+    DevBuf hview;
+    cudaStream_t cap = nullptr;  // the stream graphs are captured on
 };
 
 namespace {
@@ -1090,6 +1164,54 @@ int read_scalars(Ctx& c, const double* dev, double* host, int n)
 {
     RIGC_CUDA(cudaMemcpyAsync(host, dev, n * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     RIGC_CUDA(cudaStreamSynchronize(c.stream));
+    return RIGC_OK;
+}
+
+std::vector<unsigned long long> graph_key(std::initializer_list<const void*> ptrs,
+                                          std::initializer_list<long long> sizes)
+{
+    std::vector<unsigned long long> k;
+    for (const void* p : ptrs) k.push_back((unsigned long long)(uintptr_t)p);
+    for (long long s : sizes) k.push_back((unsigned long long)s);
+    return k;
+}
+
+// G holds (or is given) an executable graph whose only node is a while loop
+// around the launches body(stream, loop handle) issues; a graph built for the
+// same key is reused.  Its launches are captured, not run: nothing executes
+// until the graph is launched.  The handle's default value is 1, so every
+// launch runs the body at least once; the body's last kernel decides whether
+// it runs again.
+template <class Body>
+int loop_graph(Sim& S, Sim::LoopGraph& G, const std::vector<unsigned long long>& key, int kernels,
+               Body body)
+{
+    if (G.exec && G.key == key) return RIGC_OK;
+    G.release();
+    if (!S.cap) RIGC_CUDA(cudaStreamCreateWithFlags(&S.cap, cudaStreamNonBlocking));
+    RIGC_CUDA(cudaGraphCreate(&G.graph, 0));
+    cudaGraphConditionalHandle loop;
+    RIGC_CUDA(cudaGraphConditionalHandleCreate(&loop, G.graph, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = loop;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    RIGC_CUDA(cudaGraphAddNode(&node, G.graph, nullptr, nullptr, 0, &cp));
+    cudaGraph_t bodyg = cp.conditional.phGraph_out[0];
+    RIGC_CUDA(cudaStreamBeginCaptureToGraph(S.cap, bodyg, nullptr, nullptr, 0,
+                                            cudaStreamCaptureModeThreadLocal));
+    body(S.cap, loop);
+    cudaGraph_t captured = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(S.cap, &captured);
+    if (e != cudaSuccess) {
+        G.release();
+        RIGC_CUDA(e);
+    }
+    RIGC_CUDA(cudaGraphInstantiate(&G.exec, G.graph, 0));
+    G.key = key;
+    G.kernels = kernels;
     return RIGC_OK;
 }
 
@@ -1189,37 +1311,50 @@ int pcg(Ctx& c, Sim& S, const HessView& H, bool& ok, int64_t& iters)
     iters = 0;
     if (bnorm2 == 0) return RIGC_OK;
     const double tol2 = 1e-24 * bnorm2;  // relative residual 1e-12
-    const int64_t max_it = std::max<int64_t>(1000, 4 * n);
-    for (int64_t it = 0; it < max_it; it++) {
-        RIGC_COUNT_LAUNCH();
-        k_hess_matvec<<<gn, 256, 0, st>>>(H, pp, Ap);
-        RIGC_TRY(dot_dev(c, S, n, pp, Ap, sc + 2));
-        RIGC_COUNT_LAUNCH();
-        k_cg_alpha<<<1, 1, 0, st>>>(sc + 0, sc + 2, sc + 4, tol2, sc + 3, flags);
-        RIGC_COUNT_LAUNCH();
-        k_cg_update<<<gn, 256, 0, st>>>(n, sc + 3, pp, Ap, d, r);
-        RIGC_COUNT_LAUNCH();
-        k_block_apply<<<gn, 256, 0, st>>>(S.nb, S.Minv.as<double>(), r, H.fixed, z);
-        RIGC_TRY(dot_dev(c, S, n, r, z, sc + 1));
-        RIGC_TRY(dot_dev(c, S, n, r, r, sc + 4));
-        RIGC_COUNT_LAUNCH();
-        k_cg_direction<<<gn, 256, 0, st>>>(n, sc + 1, sc + 0, z, flags, pp);
-        RIGC_CUDA(cudaMemcpyAsync(sc + 0, sc + 1, sizeof(double), cudaMemcpyDeviceToDevice, st));
-        iters = it + 1;
-        if ((it & 7) == 7 || it + 1 == max_it) {
-            double rr;
-            int fl[2];
-            RIGC_CUDA(cudaMemcpyAsync(&rr, sc + 4, sizeof(double), cudaMemcpyDeviceToHost, st));
-            RIGC_CUDA(cudaMemcpyAsync(fl, flags, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
-            RIGC_CUDA(cudaStreamSynchronize(st));
-            if (fl[1] || rr <= tol2) return RIGC_OK;
-            if (fl[0] || !std::isfinite(rr)) {
-                ok = false;
-                return RIGC_OK;
-            }
-        }
-    }
-    ok = false;
+    const long long max_it = std::max<long long>(1000, 4 * n);
+    // the iteration loop runs on the device as one graph launch: its
+    // arguments are fixed, so the view, the tolerance and the iteration
+    // count live in device memory (sc[7] tolerance, sc[20] iterations)
+    double* tol2_dev = sc + 7;
+    long long* it_dev = reinterpret_cast<long long*>(sc + 20);
+    RIGC_TRY(S.hview.reserve(sizeof(HessView)));
+    HessView* Hd = S.hview.as<HessView>();
+    const double* Minv = S.Minv.as<double>();
+    const int nb = S.nb;
+    const int* fixed = H.fixed;
+    double* part = S.part.as<double>();
+    const std::vector<unsigned long long> key = graph_key(
+        { (const void*)Hd, d, r, z, pp, Ap, sc, Minv, fixed, part }, { n, max_it });
+    auto body = [&](cudaStream_t cs, cudaGraphConditionalHandle loop) {
+        k_hess_matvec_dev<<<gn, 256, 0, cs>>>(Hd, pp, Ap);
+        k_dot_partial<<<64, 256, 0, cs>>>(n, pp, Ap, part);
+        k_dot_final<<<1, 256, 0, cs>>>(part, 64, sc + 2);
+        k_cg_alpha<<<1, 1, 0, cs>>>(sc + 0, sc + 2, sc + 4, tol2_dev, sc + 3, flags);
+        k_cg_update<<<gn, 256, 0, cs>>>(n, sc + 3, pp, Ap, d, r);
+        k_block_apply<<<gn, 256, 0, cs>>>(nb, Minv, r, fixed, z);
+        k_dot_partial<<<64, 256, 0, cs>>>(n, r, z, part);
+        k_dot_final<<<1, 256, 0, cs>>>(part, 64, sc + 1);
+        k_dot_partial<<<64, 256, 0, cs>>>(n, r, r, part);
+        k_dot_final<<<1, 256, 0, cs>>>(part, 64, sc + 4);
+        k_cg_direction<<<gn, 256, 0, cs>>>(n, sc + 1, sc + 0, z, flags, pp);
+        cudaMemcpyAsync(sc + 0, sc + 1, sizeof(double), cudaMemcpyDeviceToDevice, cs);
+        k_cg_continue<<<1, 1, 0, cs>>>(flags, sc + 4, tol2_dev, it_dev, max_it, loop);
+    };
+    RIGC_TRY(loop_graph(S, S.cg_one, key, 12, body));
+    RIGC_CUDA(cudaMemcpyAsync(Hd, &H, sizeof(HessView), cudaMemcpyHostToDevice, st));
+    RIGC_CUDA(cudaMemcpyAsync(tol2_dev, &tol2, sizeof(double), cudaMemcpyHostToDevice, st));
+    RIGC_CUDA(cudaMemsetAsync(it_dev, 0, sizeof(long long), st));
+    RIGC_CUDA(cudaGraphLaunch(S.cg_one.exec, st));
+    double rr;
+    int fl[2];
+    long long its;
+    RIGC_CUDA(cudaMemcpyAsync(&rr, sc + 4, sizeof(double), cudaMemcpyDeviceToHost, st));
+    RIGC_CUDA(cudaMemcpyAsync(fl, flags, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
+    RIGC_CUDA(cudaMemcpyAsync(&its, it_dev, sizeof(long long), cudaMemcpyDeviceToHost, st));
+    RIGC_CUDA(cudaStreamSynchronize(st));
+    iters = its;
+    count_launches(its * S.cg_one.kernels);
+    ok = fl[1] || rr <= tol2;
     return RIGC_OK;
 }
 
@@ -1544,42 +1679,48 @@ int pcg_scenes(Ctx& c, Sim& S, const HessView& H, const std::vector<int>& solve,
     for (int k = 0; k < ns; k++)
         if (solve[k] && bb[k] == 0) solved[k] = 1;
     iters = 0;
-    const int64_t max_it = std::max<int64_t>(1000, 4 * n);
+    const long long max_it = std::max<long long>(1000, 4 * n);
+    // the iteration loop is one graph launch (a while node): the view and
+    // the iteration count live in device memory (sc[20] iterations)
+    long long* it_dev = reinterpret_cast<long long*>(S.scal.as<double>() + 20);
+    RIGC_TRY(S.hview.reserve(sizeof(HessView)));
+    HessView* Hd = S.hview.as<HessView>();
+    const double* Minv = S.Minv.as<double>();
+    const int* fixed = H.fixed;
+    const int* bscene = c.s.bscene;
+    const int* sbs = c.s.scene_bstart;
+    const std::vector<unsigned long long> key = graph_key(
+        { (const void*)Hd, d, r, z, pp, Ap, Minv, fixed, bscene, sbs, P.rz, P.flags, it_dev },
+        { n, ns, max_it });
+    auto body = [&](cudaStream_t cs, cudaGraphConditionalHandle loop) {
+        k_hess_matvec_dev<<<gn, 256, 0, cs>>>(Hd, pp, Ap);
+        k_seg_dot<<<ns, 256, 0, cs>>>(sbs, 6, pp, Ap, P.pAp);
+        k_cg_alpha_sc<<<gs, 128, 0, cs>>>(ns, P.rz, P.pAp, P.rr, P.tol2, P.cga, P.flags);
+        k_cg_update_sc<<<gn, 256, 0, cs>>>(nb, bscene, P.cga, pp, Ap, d, r);
+        k_block_apply<<<gn, 256, 0, cs>>>(nb, Minv, r, fixed, z);
+        k_seg_dot<<<ns, 256, 0, cs>>>(sbs, 6, r, z, P.rz_new);
+        k_seg_dot<<<ns, 256, 0, cs>>>(sbs, 6, r, r, P.rr);
+        k_cg_direction_sc<<<gn, 256, 0, cs>>>(nb, bscene, P.rz_new, P.rz, z, P.flags, pp);
+        cudaMemcpyAsync(P.rz, P.rz_new, ns * 8, cudaMemcpyDeviceToDevice, cs);
+        k_cg_continue_sc<<<1, 256, 0, cs>>>(ns, P.mask, P.flags, P.rr, P.tol2, it_dev, max_it, loop);
+    };
+    RIGC_TRY(loop_graph(S, S.cg_sc, key, 9, body));
+    RIGC_CUDA(cudaMemcpyAsync(Hd, &H, sizeof(HessView), cudaMemcpyHostToDevice, st));
+    RIGC_CUDA(cudaMemsetAsync(it_dev, 0, sizeof(long long), st));
+    RIGC_CUDA(cudaGraphLaunch(S.cg_sc.exec, st));
     std::vector<double> rr(ns);
-    for (int64_t it = 0; it < max_it; it++) {
-        RIGC_COUNT_LAUNCH();
-        k_hess_matvec<<<gn, 256, 0, st>>>(H, pp, Ap);
-        RIGC_COUNT_LAUNCH();
-        k_seg_dot<<<ns, 256, 0, st>>>(c.s.scene_bstart, 6, pp, Ap, P.pAp);
-        RIGC_COUNT_LAUNCH();
-        k_cg_alpha_sc<<<gs, 128, 0, st>>>(ns, P.rz, P.pAp, P.rr, P.tol2, P.cga, P.flags);
-        RIGC_COUNT_LAUNCH();
-        k_cg_update_sc<<<gn, 256, 0, st>>>(nb, c.s.bscene, P.cga, pp, Ap, d, r);
-        RIGC_COUNT_LAUNCH();
-        k_block_apply<<<gn, 256, 0, st>>>(nb, S.Minv.as<double>(), r, H.fixed, z);
-        RIGC_COUNT_LAUNCH();
-        k_seg_dot<<<ns, 256, 0, st>>>(c.s.scene_bstart, 6, r, z, P.rz_new);
-        RIGC_COUNT_LAUNCH();
-        k_seg_dot<<<ns, 256, 0, st>>>(c.s.scene_bstart, 6, r, r, P.rr);
-        RIGC_COUNT_LAUNCH();
-        k_cg_direction_sc<<<gn, 256, 0, st>>>(nb, c.s.bscene, P.rz_new, P.rz, z, P.flags, pp);
-        RIGC_CUDA(cudaMemcpyAsync(P.rz, P.rz_new, ns * 8, cudaMemcpyDeviceToDevice, st));
-        iters = it + 1;
-        if ((it & 7) == 7 || it + 1 == max_it) {
-            RIGC_CUDA(cudaMemcpyAsync(fl.data(), P.flags, 2 * ns * sizeof(int), cudaMemcpyDeviceToHost, st));
-            RIGC_CUDA(cudaMemcpyAsync(rr.data(), P.rr, ns * 8, cudaMemcpyDeviceToHost, st));
-            RIGC_CUDA(cudaStreamSynchronize(st));
-            bool all = true;
-            for (int k = 0; k < ns; k++) {
-                if (!solve[k]) continue;
-                if (fl[2 * k] || !std::isfinite(rr[k])) continue;  // broken down: not solved
-                if (fl[2 * k + 1] || rr[k] <= tol2[k]) solved[k] = 1;
-                else all = false;
-            }
-            if (all) break;
-        }
+    long long its = 0;
+    RIGC_CUDA(cudaMemcpyAsync(fl.data(), P.flags, 2 * ns * sizeof(int), cudaMemcpyDeviceToHost, st));
+    RIGC_CUDA(cudaMemcpyAsync(rr.data(), P.rr, ns * 8, cudaMemcpyDeviceToHost, st));
+    RIGC_CUDA(cudaMemcpyAsync(&its, it_dev, sizeof(long long), cudaMemcpyDeviceToHost, st));
+    RIGC_CUDA(cudaStreamSynchronize(st));
+    iters = its;
+    count_launches(its * S.cg_sc.kernels);
+    for (int k = 0; k < ns; k++) {
+        if (!solve[k]) continue;
+        if (fl[2 * k] || !std::isfinite(rr[k])) continue;  // broken down: not solved
+        if (fl[2 * k + 1] || rr[k] <= tol2[k]) solved[k] = 1;
     }
-    RIGC_CUDA(cudaGetLastError());
     return RIGC_OK;
 }
 
@@ -2383,8 +2524,11 @@ void sim_release(Ctx& c)
                        &S.dense, &S.dense_b, &S.dense_x, &S.dense_d, &S.ckpt,
                        &S.final_state, &S.seg_pre, &S.seg_x, &S.adj, &S.adj_out, &S.xbar,
                        &S.u1, &S.u2, &S.sc_dev, &S.sc_red, &S.sc_vstart, &S.al_xpred,
-                       &S.al_lam, &S.al_Lam, &S.al_e };
+                       &S.al_lam, &S.al_Lam, &S.al_e, &S.hview };
     for (DevBuf* b : bufs) b->release();
+    S.cg_one.release();
+    S.cg_sc.release();
+    if (S.cap) cudaStreamDestroy(S.cap);
     delete c.sim;
     c.sim = nullptr;
 }

@@ -45,6 +45,30 @@ def test_cube_lattice_matches_oracle(oracle, cube_scene):
         assert np.abs(V.reshape(-1)[:] - sim.vel).reshape(-1, 6)[:, :3].max() <= 1e-5
 
 
+def test_large_lattice_cg_graph_matches_oracle(oracle):
+    """216 cubes (1296 free dofs): the Newton systems go to the conjugate
+    gradient solver, whose iteration loop runs as one CUDA graph launch (a
+    device-side while loop); poses after 2 steps against the oracle's dense
+    LDL^T solve."""
+    import rigc
+    from rigc import scene as S
+
+    sc = S.scene_from_json(S.spec_cubes(3, n=6, vel_sigma=0.5))
+    sim = oracle.OracleSim(sc, h=H, gravity=G, dhat=1e-3)
+    ctx = rigc.Context(sc)
+    ctx.sim_init(H, G, 1e-3)
+    cg = 0
+    for k in range(2):
+        st_o = sim.step()
+        st_g = ctx.sim_step(1)
+        cg += st_g["cg_iterations"]
+        P, V, Q, kappa = ctx.sim_state()
+        err = np.abs(P.reshape(-1) - sim.pose).max()
+        assert err <= 1e-7, (k, err, st_o, st_g)
+        assert kappa == pytest.approx(sim.kappa.value, rel=1e-12)
+    assert cg > 0  # the CG path ran
+
+
 def test_kinematic_bodies_match_oracle(oracle):
     """A kinematic cube (the augmented Lagrangian toward x0 + h v) pushing a
     dynamic one across a plane: device poses after 3 steps against the
