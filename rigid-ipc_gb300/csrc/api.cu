@@ -139,7 +139,7 @@ static void release_all(Ctx* c)
                        &c->d_scalars, &c->body_box, &c->body_in, &c->vbox, &c->ebox, &c->fbox,
                        &c->vin, &c->ein, &c->fin, &c->items_key, &c->items_val, &c->items_key2,
                        &c->items_val2, &c->seg, &c->pair_out, &c->pair_key, &c->large_list,
-                       &c->x0_dev, &c->x1_dev, &c->rot_table, &c->cand_tol, &c->frame_keys,
+                       &c->x0_dev, &c->x1_dev, &c->rot_table, &c->cand_tol, &c->frame_keys, &c->ccd_pieces[0], &c->ccd_pieces[1],
                        &c->frame_vals, &c->fric.type, &c->fric.verts, &c->fric.bodies,
                        &c->fric.coef, &c->fric.v0c, &c->fric.V0, &c->fric.c_energy,
                        &c->fric.c_grad, &c->fric.c_blocks, &c->fric.grad, &c->fric.row_ptr,
@@ -603,17 +603,18 @@ int rigc_autotune(rigc_ctx* ctx, const double* x0, const double* x1, double dhat
 }
 
 int rigc_set_tune(rigc_ctx* ctx, int32_t ccd_blocks_per_sm, int32_t cache_slots_per_body,
-                  int32_t barrier_per_warp, int32_t ccd_seeds_log2)
+                  int32_t barrier_per_warp, int32_t ccd_seeds_log2, int32_t ccd_hand_off)
 {
     if (!ctx || ccd_blocks_per_sm < 0 || cache_slots_per_body < 0 || barrier_per_warp < 0
         || barrier_per_warp > 32 || cache_slots_per_body > (1 << 16) || ccd_seeds_log2 < -1
-        || ccd_seeds_log2 > 5)
+        || ccd_seeds_log2 > 5 || ccd_hand_off < -1)
         return RIGC_ERR_ARG;
     Ctx& c = *ctx_of(ctx);
     c.tune.ccd_blocks_per_sm = ccd_blocks_per_sm;
     c.tune.cache_slots_per_body = cache_slots_per_body;
     c.tune.barrier_per_warp = barrier_per_warp;
     c.tune.ccd_seeds_log2 = ccd_seeds_log2;
+    c.tune.ccd_hand_off = ccd_hand_off;
     return RIGC_OK;
 }
 

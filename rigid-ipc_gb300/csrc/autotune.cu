@@ -10,6 +10,9 @@
 //  * the CCD searches per candidate (1 .. 32, from the nodes of its
 //    subdivision tree at that depth): more fill the GPU when candidates are
 //    few or deep, fewer skip the nodes above that depth;
+//  * the CCD boxes a search piece evaluates before it hands its pending
+//    boxes to a further launch (never, 16, the built-in 64, 256): short
+//    pieces spread deep searches over the GPU, each hand-off costs a launch;
 //  * k_barrier_local's constraints per warp (1 .. 32): one thread per
 //    constraint fills the SMs for small sets, a full warp per 32 constraints
 //    shares the PSD projections for large ones.
@@ -100,6 +103,17 @@ int autotune(Ctx& c, const double* x0, const double* x1, double dhat, double dmi
         }
     }
     c.tune.ccd_seeds_log2 = best_seeds;
+    int best_ho = -1;
+    for (int ho : { 0, 16, 256 }) {
+        c.tune.ccd_hand_off = ho;
+        double ms;
+        RIGC_TRY(median_ms(ccd, &ms));
+        if (ms < best) {
+            best = ms;
+            best_ho = ho;
+        }
+    }
+    c.tune.ccd_hand_off = best_ho;
     r.ccd_ms = best;
     // barrier terms over the constraint set at x0
     RIGC_TRY(detect_and_count(c, x0, x0, false, (dhat + dmin) / 2.0));
@@ -126,6 +140,7 @@ int autotune(Ctx& c, const double* x0, const double* x1, double dhat, double dmi
     r.cache_slots_per_body = c.tune.cache_slots_per_body;
     r.barrier_per_warp = c.tune.barrier_per_warp;
     r.ccd_seeds_log2 = c.tune.ccd_seeds_log2;
+    r.ccd_hand_off = c.tune.ccd_hand_off;
     if (rep) *rep = r;
     return RIGC_OK;
 }

@@ -44,6 +44,11 @@
 namespace rigc {
 
 constexpr int kCCDThreads = 128;
+// search pieces: boxes a piece evaluates before handing off its pending
+// boxes (built-in choice), slots per hand-off buffer, launches per call
+constexpr int kHandOff = 64;
+constexpr unsigned long long kPiecesCap = 1ull << 18;
+constexpr int kMaxLaunches = 32;
 
 struct CCDArgs {
     const double* rest;
@@ -79,10 +84,33 @@ struct CCDArgs {
     const double* traj;         // per body: x0 (6), I(x1) - I(x0) (6 intervals)
     const int* bfixed;          // per body: 1 when the body does not move
     double* ctol;               // per candidate: the three tolerances
+    // Search pieces (prune mode).  A lane whose current piece has evaluated
+    // hand_off boxes writes its pending boxes to pieces_out and ends the
+    // piece; the next launch of the call searches pieces_in instead of the
+    // candidates' seeds, so deep searches spread over the whole GPU.
+    const struct Piece* pieces_in;
+    long long n_pieces;         // pieces in pieces_in (launch 0: none, seeds)
+    struct Piece* pieces_out;
+    unsigned long long* n_out;
+    unsigned long long out_cap;
+    unsigned long long hand_off;  // boxes per piece before a hand-off (0: never)
 };
 
 struct Box {
     double t0, t1, a0, a1, b0, b1;
+};
+
+// One piece of a candidate's search: the subtree below a node, the earliest
+// root time found so far (boxes at or after it are skipped) and the boxes
+// the search path leading to it has evaluated (the budget counts along
+// every path).  cand < 0 marks an unused slot.
+struct Piece {
+    long long cand;
+    double earliest;
+    unsigned long long ix[3];
+    int lv[3];
+    int depth;
+    unsigned long long boxes;
 };
 
 struct BodyTraj {
@@ -705,7 +733,9 @@ k_ccd(CCDArgs a)
     double earliest = INFINITY;
     bool found = false;
     int status = RIGC_OK;
-    unsigned long long cboxes = 0;
+    unsigned long long cboxes = 0;  // boxes of the current piece
+    unsigned long long cbase = 0;   // boxes of the path before the piece
+    bool hand_ok = a.hand_off != 0;
     double gbound = INFINITY;
     bool done = false;
     OwnFrames own;
@@ -769,6 +799,7 @@ k_ccd(CCDArgs a)
                         found = false;
                         status = RIGC_OK;
                         cboxes = 0;
+                        cbase = 0;
                         cn = g;
                         has_cn = true;
                         pend_hi = 0;
@@ -779,6 +810,43 @@ k_ccd(CCDArgs a)
         }
         bool have = false;
         Box x;
+        if (!done && hand_ok && cboxes >= a.hand_off && (pend_hi != 0 || has_cn)) {
+            // hand the pending boxes to the next launch and end this piece
+            const int k = popc128(pend_hi) + (has_cn ? 1 : 0);
+            const unsigned long long s = atomicAdd(a.n_out, (unsigned long long)k);
+            if (s + k <= a.out_cap) {
+                Piece pc;
+                pc.cand = cur;
+                pc.earliest = earliest;
+                pc.boxes = cbase + cboxes;
+                unsigned long long o = s;
+                for (u128 r = pend_hi; r != 0; r &= r - 1) {
+                    const Node g = pending_node(cn, mt, ma, lsb128(r));
+#pragma unroll
+                    for (int d = 0; d < 3; d++) {
+                        pc.ix[d] = g.ix[d];
+                        pc.lv[d] = g.lv[d];
+                    }
+                    pc.depth = g.depth;
+                    a.pieces_out[o++] = pc;
+                }
+                if (has_cn) {
+#pragma unroll
+                    for (int d = 0; d < 3; d++) {
+                        pc.ix[d] = cn.ix[d];
+                        pc.lv[d] = cn.lv[d];
+                    }
+                    pc.depth = cn.depth;
+                    a.pieces_out[o++] = pc;
+                }
+                pend_hi = 0;
+                has_cn = false;
+            } else {
+                // no room: the reserved slots stay unused, the lane keeps searching
+                for (unsigned long long t = s; t < s + k && t < a.out_cap; t++) a.pieces_out[t].cand = -1;
+                hand_ok = false;
+            }
+        }
         if (!done) {
             while (has_cn || pend_hi != 0) {
                 if (has_cn) {
@@ -814,10 +882,34 @@ k_ccd(CCDArgs a)
                     if (status != RIGC_OK) atomicMax(a.status, status);
                 }
                 // work item w: seed w / n of candidate w % n (seed-major, so
-                // early times of every candidate come first)
+                // early times of every candidate come first), or piece w
                 const int64_t w = (int64_t)atomicAdd(a.next, 1ull);
-                if (w >= (n << a.seeds_log2)) {
+                if (w >= (a.pieces_in ? a.n_pieces : (n << a.seeds_log2))) {
                     done = true;
+                } else if (a.pieces_in) {
+                    // the piece's node is popped (and tested) in the next iteration
+                    const Piece pc = a.pieces_in[w];
+                    cur = pc.cand;
+                    if (cur >= 0) {
+                        load_candidate(a, cur, q);
+                        tol[0] = a.ctol[3 * cur];
+                        tol[1] = a.ctol[3 * cur + 1];
+                        tol[2] = a.ctol[3 * cur + 2];
+                        gbound = load_gmin(a, q);
+                        earliest = pc.earliest;
+                        found = false;
+                        status = RIGC_OK;
+                        cboxes = 0;
+                        cbase = pc.boxes;
+                        pend_hi = 0;
+#pragma unroll
+                        for (int d = 0; d < 3; d++) {
+                            cn.ix[d] = pc.ix[d];
+                            cn.lv[d] = pc.lv[d];
+                        }
+                        cn.depth = pc.depth;
+                        has_cn = true;
+                    }
                 } else {
                     cur = w % n;
                     load_candidate(a, cur, q);
@@ -829,6 +921,7 @@ k_ccd(CCDArgs a)
                     found = false;
                     status = RIGC_OK;
                     cboxes = 0;
+                    cbase = 0;
                     pend_hi = 0;
                     has_cn = false;
                     cn = seed_node(a.seeds_log2, w / n, tol, mt, ma);
@@ -844,7 +937,7 @@ k_ccd(CCDArgs a)
         // every lane reaches this point once per iteration
         if (__all_sync(0xffffffffu, done)) break;
         if (!have) continue;
-        if (cboxes >= (unsigned long long)a.max_boxes) {
+        if (cbase + cboxes >= (unsigned long long)a.max_boxes) {
             // budget exhausted: the earliest unexplored t.lo is conservative
             double m = x.t0;
             for (u128 r = pend_hi; r != 0; r &= r - 1) {
@@ -933,14 +1026,15 @@ int ccd_max_blocks_per_sm(int* out)
 }
 
 // counters layout in the context's device scalars (byte offset 256):
-// [0] gmin bits, [1] boxes, [2] hits, [3] status, [4] next candidate
+// [0] gmin bits, [1] boxes, [2] hits, [3] status, [4] next work item,
+// [5] search pieces handed off
 int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flags,
             double* toi_host, double* per)
 {
     cudaStream_t st = c.stream;
     const int64_t n = c.cand.num_ee + c.cand.num_fv;
     unsigned long long* cnt = reinterpret_cast<unsigned long long*>(c.d_scalars.as<char>() + 256);
-    unsigned long long init[5] = { (unsigned long long)0x7ff0000000000000ull, 0, 0, 0, 0 };
+    unsigned long long init[6] = { (unsigned long long)0x7ff0000000000000ull, 0, 0, 0, 0, 0 };
     RIGC_CUDA(cudaMemcpyAsync(cnt, init, sizeof(init), cudaMemcpyHostToDevice, st));
     if (n > 0) {
         CCDArgs a;
@@ -1025,10 +1119,45 @@ int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flag
             else
                 while (a.seeds_log2 < 5 && (n << a.seeds_log2) * 4 < full * kCCDThreads) a.seeds_log2++;
         }
+        // search pieces (prune mode): launch 0 searches the seeds and hands
+        // the rest of every search that reaches hand_off boxes to launch 1,
+        // and so on; the last launch hands nothing off
+        a.pieces_in = nullptr;
+        a.n_pieces = 0;
+        a.hand_off = 0;
+        a.n_out = cnt + 5;
+        a.out_cap = 0;
+        a.pieces_out = nullptr;
+        if (a.prune) {
+            const int ho = c.tune.ccd_hand_off >= 0 ? c.tune.ccd_hand_off : kHandOff;
+            if (ho > 0) {
+                RIGC_TRY(c.ccd_pieces[0].reserve(kPiecesCap * sizeof(Piece)));
+                RIGC_TRY(c.ccd_pieces[1].reserve(kPiecesCap * sizeof(Piece)));
+                a.hand_off = (unsigned long long)ho;
+                a.out_cap = kPiecesCap;
+                a.pieces_out = c.ccd_pieces[0].as<Piece>();
+            }
+        }
         int64_t want = ((n << a.seeds_log2) + kCCDThreads - 1) / kCCDThreads;
-        RIGC_COUNT_LAUNCH();
-        k_ccd<<<(unsigned)std::min(want, full), kCCDThreads, 0, st>>>(a);
-        RIGC_CUDA(cudaGetLastError());
+        for (int launch = 0;; launch++) {
+            RIGC_COUNT_LAUNCH();
+            k_ccd<<<(unsigned)std::min(want, full), kCCDThreads, 0, st>>>(a);
+            RIGC_CUDA(cudaGetLastError());
+            if (!a.hand_off) break;
+            unsigned long long np = 0;
+            RIGC_CUDA(cudaMemcpyAsync(&np, a.n_out, sizeof(np), cudaMemcpyDeviceToHost, st));
+            RIGC_CUDA(cudaStreamSynchronize(st));
+            np = std::min(np, a.out_cap);
+            if (np == 0) break;
+            // the pieces just written become the next launch's work
+            const unsigned long long zero[2] = { 0, 0 };
+            RIGC_CUDA(cudaMemcpyAsync(a.next, zero, sizeof(zero), cudaMemcpyHostToDevice, st));
+            a.pieces_in = a.pieces_out;
+            a.n_pieces = (long long)np;
+            a.pieces_out = c.ccd_pieces[(launch + 1) & 1].as<Piece>();
+            if (launch + 1 >= kMaxLaunches - 1) a.hand_off = 0;
+            want = ((int64_t)np + kCCDThreads - 1) / kCCDThreads;
+        }
     }
     unsigned long long out[4];
     RIGC_CUDA(cudaMemcpyAsync(out, cnt, sizeof(out), cudaMemcpyDeviceToHost, st));

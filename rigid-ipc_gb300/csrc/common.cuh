@@ -160,6 +160,7 @@ struct Ctx {
     DevBuf rot_table;
     DevBuf cand_tol;  // CCD: per-candidate tolerances
     DevBuf frame_keys, frame_vals;  // CCD frame cache (hash table)
+    DevBuf ccd_pieces[2];           // CCD search pieces handed between launches
     Friction fric;
     int64_t ccd_max_boxes = int64_t(1) << 22;  // per-candidate CCD box budget
     // launch shapes chosen by rigc_autotune (0: the built-in choice)
@@ -168,6 +169,7 @@ struct Ctx {
         int cache_slots_per_body = 0;  // CCD frame-cache slots per body (0: 1024)
         int barrier_per_warp = 0;      // constraints per warp of k_barrier_local (0: by count)
         int ccd_seeds_log2 = -1;       // CCD searches per candidate, log2 (-1: by count)
+        int ccd_hand_off = -1;         // CCD boxes per search piece before a hand-off (-1: default, 0: never)
     } tune;
     Sim* sim = nullptr;
     // batched contexts: per-scene results of the last calls
