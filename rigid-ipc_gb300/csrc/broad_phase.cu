@@ -26,6 +26,8 @@
 namespace rigc {
 
 constexpr int kLargeCells = 64;
+// item counts up to which cell pairs are enumerated by a warp per item
+constexpr int64_t kWarpPairItems = 1 << 16;
 
 // ---------------------------------------------------------------------------
 // 1. body boxes and inclusion
@@ -544,6 +546,40 @@ __global__ void k_cell_pairs(const uint64_t* __restrict__ keys, const uint32_t* 
     }
 }
 
+// The same with one warp per sorted item, its lanes striding over the later
+// items of the cell: for small item counts, where the cells are few and
+// full and one thread per item would walk a whole cell alone.
+__global__ void k_cell_pairs_warp(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ vals,
+                                  int64_t m, PairCtx P, Grid g, ElemScene es, uint64_t ncells,
+                                  PairOut o)
+{
+    const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= m) return;
+    const uint64_t key = keys[i];
+    const uint32_t a = vals[i];
+    long long a0[3], a1[3];
+    bool have_a = false;
+    for (int64_t j = i + 1 + lane; j < m && keys[j] == key; j += 32) {
+        uint32_t b = vals[j];
+        bool is_ee;
+        unsigned long long pk;
+        int ta = a >> 30, tb = b >> 30;
+        if (!((ta == 1 && tb == 1) || (ta + tb == 2 && ta != tb))) continue;
+        if (!pair_filter(P, a, b, is_ee, pk)) continue;
+        if (!have_a) {
+            cell_range(elem_box(a, P.vb, P.eb, P.fb), g, a0, a1);
+            have_a = true;
+        }
+        long long b0[3], b1[3];
+        cell_range(elem_box(b, P.vb, P.eb, P.fb), g, b0, b1);
+        long long fx = max(a0[0], b0[0]), fy = max(a0[1], b0[1]), fz = max(a0[2], b0[2]);
+        uint64_t first = es.of(a) * ncells + (uint64_t)((fz * g.dims[1] + fy) * g.dims[0] + fx);
+        if (first != key) continue;
+        push_pair(o, is_ee, pk);
+    }
+}
+
 // large elements against every included element of the matching type in
 // their scene: grid row y = large element, its blocks stride over the range;
 // range[s * 3 + t] is the first
@@ -808,7 +844,11 @@ int detect_candidates(Ctx& c, const double* x0, const double* x1, bool continuou
         PairOut o { c.pair_out.as<unsigned long long>(), c.pair_out.as<unsigned long long>() + cap_ee,
                     cap_ee, cap_fv, pn, pn + 1 };
         RIGC_CUDA(cudaMemsetAsync(pn, 0, 2 * sizeof(unsigned long long), st));
-        if (nitems > 0) {
+        if (nitems > 0 && nitems <= kWarpPairItems) {
+            RIGC_COUNT_LAUNCH();
+            k_cell_pairs_warp<<<grid_for(nitems * 32, 128), 128, 0, st>>>(
+                c.items_key2.as<uint64_t>(), c.items_val2.as<uint32_t>(), nitems, P, g, es, ncells, o);
+        } else if (nitems > 0) {
             RIGC_COUNT_LAUNCH();
             k_cell_pairs<<<grid_for(nitems, 128), 128, 0, st>>>(c.items_key2.as<uint64_t>(),
                                                               c.items_val2.as<uint32_t>(), nitems, P, g,

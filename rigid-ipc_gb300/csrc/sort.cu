@@ -87,6 +87,87 @@ k_scatter(const Key* __restrict__ kin, const uint32_t* __restrict__ vin,
 int64_t scan_tiles(int64_t n);
 int scan_in_place(int32_t* a, int64_t n, int32_t* sums, cudaStream_t stream);
 
+// Inputs of at most one tile (the sorts of small scenes) are sorted by one
+// block in one launch: per pass the tile's digit histogram, its exclusive
+// scan over the 256 digits and the stable scatter of k_scatter, passes
+// separated by block barriers (global writes of a block are visible to it
+// after __syncthreads).  Same passes and the same stable order as the
+// multi-launch sort.
+template <class Key>
+__global__ void __launch_bounds__(kSortThreads)
+k_sort_tile(const Key* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
+            Key* keys_out, uint32_t* vals_out, Key* tmp_k, uint32_t* tmp_v, int n, int passes)
+{
+    __shared__ uint32_t cnt[256];
+    __shared__ uint32_t base[256];
+    __shared__ uint32_t wsum[kWarps];
+    __shared__ uint32_t wcnt[kWarps][256];
+    __shared__ uint32_t woff[kWarps][256];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const unsigned lt = (1u << lane) - 1u;
+    const Key* src_k = keys_in;
+    const uint32_t* src_v = vals_in;
+    for (int p = 0; p < passes; p++) {
+        const bool to_out = ((passes - 1 - p) % 2) == 0;
+        Key* dk = to_out ? keys_out : tmp_k;
+        uint32_t* dv = to_out ? vals_out : tmp_v;
+        const int shift = 8 * p;
+        cnt[tid] = 0;
+#pragma unroll
+        for (int w = 0; w < kWarps; w++) wcnt[w][tid] = 0;
+        __syncthreads();
+        for (int r = 0; r < kSortRounds; r++) {
+            const int i = r * kSortThreads + tid;
+            if (i < n) atomicAdd(&cnt[(uint32_t)(src_k[i] >> shift) & 0xffu], 1u);
+        }
+        __syncthreads();
+        // exclusive scan of the 256 digit counts
+        uint32_t x = cnt[tid];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) wsum[warp] = x;
+        __syncthreads();
+        uint32_t before = 0;
+        for (int w = 0; w < warp; w++) before += wsum[w];
+        base[tid] = before + x - cnt[tid];
+        __syncthreads();
+        for (int r = 0; r < kSortRounds; r++) {
+            const int i = r * kSortThreads + tid;
+            const bool valid = i < n;
+            const Key k = valid ? src_k[i] : Key(0);
+            const uint32_t v = valid ? src_v[i] : 0u;
+            const uint32_t d = valid ? ((uint32_t)(k >> shift) & 0xffu) : 256u;
+            const unsigned peers = __match_any_sync(0xffffffffu, d);
+            const uint32_t rank = __popc(peers & lt);
+            if (valid && rank == 0) wcnt[warp][d] = __popc(peers);
+            __syncthreads();
+            {
+                uint32_t run = base[tid];
+#pragma unroll
+                for (int w = 0; w < kWarps; w++) {
+                    const uint32_t c = wcnt[w][tid];
+                    woff[w][tid] = run;
+                    run += c;
+                    wcnt[w][tid] = 0;
+                }
+                base[tid] = run;
+            }
+            __syncthreads();
+            if (valid) {
+                const uint32_t pos = woff[warp][d] + rank;
+                dk[pos] = k;
+                dv[pos] = v;
+            }
+            __syncthreads();
+        }
+        src_k = dk;
+        src_v = dv;
+    }
+}
+
 } // namespace
 
 template <class Key>
@@ -101,6 +182,14 @@ int radix_sort_pairs(const Key* keys_in, const uint32_t* vals_in, Key* keys_out,
     const int ntiles = (int)((n + kSortTile - 1) / kSortTile);
     RIGC_TRY(tmp_keys.reserve(n * sizeof(Key)));
     RIGC_TRY(tmp_vals.reserve(n * sizeof(uint32_t)));
+    if (ntiles == 1) {
+        RIGC_COUNT_LAUNCH();
+        k_sort_tile<Key><<<1, kSortThreads, 0, stream>>>(keys_in, vals_in, keys_out, vals_out,
+                                                         tmp_keys.as<Key>(), tmp_vals.as<uint32_t>(),
+                                                         (int)n, passes);
+        RIGC_CUDA(cudaGetLastError());
+        return RIGC_OK;
+    }
     // digit-major histogram followed by the tile sums of its scan
     const int64_t m = (int64_t)256 * ntiles;
     RIGC_TRY(hist.reserve((size_t)(m + scan_tiles(m)) * sizeof(uint32_t)));
@@ -224,12 +313,51 @@ __global__ void k_tile_scan(const int32_t* in, int32_t* out, int64_t n,
     }
 }
 
+// Short arrays (at most kSmallScan items, the histograms and flags of small
+// scenes) are scanned by one block in one launch, tile after tile with a
+// running carry: the same integer sums as the three-kernel scan, a third of
+// the launches.
+constexpr int64_t kSmallScan = 4 * kScanTile;
+
+__global__ void k_scan_small(const int32_t* in, int32_t* out, int64_t n, int32_t* total_dev)
+{
+    __shared__ int32_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int64_t b = 0; b < n; b += kScanTile) {
+        const int64_t base = b + threadIdx.x * kScanItems;
+        int32_t v[kScanItems];
+        int32_t s = 0;
+#pragma unroll
+        for (int k = 0; k < kScanItems; k++) {
+            v[k] = base + k < n ? in[base + k] : 0;
+            s += v[k];
+        }
+        int32_t tot;
+        int32_t ex = block_exclusive_scan(s, &tot) + carry;  // reads precede the writes
+#pragma unroll
+        for (int k = 0; k < kScanItems; k++) {
+            if (base + k < n) out[base + k] = ex;
+            ex += v[k];
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) carry += tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && total_dev) *total_dev = carry;
+}
+
 int64_t scan_tiles(int64_t n) { return (n + kScanTile - 1) / kScanTile; }
 
 // exclusive scan of a[0..n) in place (each tile is read before it is written);
 // sums holds scan_tiles(n) entries
 int scan_in_place(int32_t* a, int64_t n, int32_t* sums, cudaStream_t stream)
 {
+    if (n <= kSmallScan) {
+        RIGC_COUNT_LAUNCH();
+        k_scan_small<<<1, kScanThreads, 0, stream>>>(a, a, n, nullptr);
+        return RIGC_OK;
+    }
     const int64_t tiles = scan_tiles(n);
     RIGC_COUNT_LAUNCH();
     k_tile_sums<<<(unsigned)tiles, kScanThreads, 0, stream>>>(a, n, sums);
@@ -247,6 +375,12 @@ int exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, int32_t* tota
 {
     if (n <= 0) {
         if (total_dev) RIGC_CUDA(cudaMemsetAsync(total_dev, 0, sizeof(int32_t), stream));
+        return RIGC_OK;
+    }
+    if (n <= kSmallScan) {
+        RIGC_COUNT_LAUNCH();
+        k_scan_small<<<1, kScanThreads, 0, stream>>>(in, out, n, total_dev);
+        RIGC_CUDA(cudaGetLastError());
         return RIGC_OK;
     }
     int64_t tiles = (n + kScanTile - 1) / kScanTile;
