@@ -629,6 +629,12 @@ def main():
         return statistics.median(best)
 
     ctx.detect_collision_candidates_rigid(x0d, x1d, True, 0.0)
+    # one untimed CCD call in the NVTX range "ccd_call": its k_ccd launches
+    # (ncu --nvtx-include ccd_call/) give the DRAM traffic of one call
+    torch.cuda.nvtx.range_push("ccd_call")
+    ctx.earliest_toi(x0d, x1d)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     t_ccd = timed(lambda: ctx.earliest_toi(x0d, x1d))
     st = ctx.stats()
     t_bp = timed(lambda: ctx.detect_collision_candidates_rigid(x0d, x1d, True, 0.0))

@@ -84,10 +84,11 @@ struct CCDArgs {
     const double* traj;         // per body: x0 (6), I(x1) - I(x0) (6 intervals)
     const int* bfixed;          // per body: 1 when the body does not move
     double* ctol;               // per candidate: the three tolerances
-    // Search pieces (prune mode).  A lane whose current piece has evaluated
-    // hand_off boxes writes its pending boxes to pieces_out and ends the
-    // piece; the next launch of the call searches pieces_in instead of the
-    // candidates' seeds, so deep searches spread over the whole GPU.
+    // Search pieces (prune mode).  Once the work list is exhausted (a lane of
+    // the warp is idle), a lane whose current piece has evaluated hand_off
+    // boxes writes its pending boxes to pieces_out and ends the piece; the
+    // next launch of the call searches pieces_in instead of the candidates'
+    // seeds, so the deep searches of the tail spread over the whole GPU.
     const struct Piece* pieces_in;
     long long n_pieces;         // pieces in pieces_in (launch 0: none, seeds)
     struct Piece* pieces_out;
@@ -756,8 +757,10 @@ k_ccd(CCDArgs a)
         // with its candidate.  Prune mode only: split searches find the same
         // earliest time of impact, but a search stopped by the box budget
         // would not report what one search reports.
+        bool tail = false;  // a lane of this warp found no work left
         if (a.prune) {
             const unsigned idle = __ballot_sync(0xffffffffu, done);
+            tail = idle != 0;
             if (idle) {
                 // boxes left in a lane's search: pending upper children + cn
                 int best = done ? 0 : popc128(pend_hi) + (has_cn ? 1 : 0) - 1, bl = lane;
@@ -810,8 +813,10 @@ k_ccd(CCDArgs a)
         }
         bool have = false;
         Box x;
-        if (!done && hand_ok && cboxes >= a.hand_off && (pend_hi != 0 || has_cn)) {
-            // hand the pending boxes to the next launch and end this piece
+        if (!done && tail && hand_ok && cboxes >= a.hand_off && (pend_hi != 0 || has_cn)) {
+            // Once the work list runs dry (idle lanes in the warp), a long
+            // piece hands its pending boxes to the next launch, which spreads
+            // them over the whole GPU, and ends
             const int k = popc128(pend_hi) + (has_cn ? 1 : 0);
             const unsigned long long s = atomicAdd(a.n_out, (unsigned long long)k);
             if (s + k <= a.out_cap) {
