@@ -38,13 +38,13 @@ import numpy as np  # noqa: E402
 METRIC = "candidate pairs/s (CCD+barrier grad/Hess)"
 UNIT = "pairs/s"
 CCD_BYTES_PER_PAIR = 304        # ids + 4 rest vertices + 4 poses + toi
-# DRAM bytes (read + write) per continuous candidate of one k_ccd launch,
-# from the ncu capture of the 200-icosphere pile (built-in shapes: 0.768 GB
-# read + 2.119 GB written for 132,242 candidates; profiles/
-# k_ccd_icosphere_pile_200.md); the traffic of a full launch is this times
-# its candidates (it is the box stacks' local memory, which grows with the
-# boxes, 42 per candidate there)
-K_CCD_DRAM_BYTES_PER_CANDIDATE = (0.768274e9 + 2.118710e9) / 132242
+# DRAM bytes (read + write) per continuous candidate of one CCD call (its
+# k_ccd launches), from the ncu capture of the 200-icosphere pile (built-in
+# shapes: 56.95 MB read + 311.51 MB written over two launches for 132,242
+# candidates; profiles/k_ccd_icosphere_pile_200.md); the traffic of a full
+# call is this times its candidates (per-lane candidate state spilling from
+# L1 and the frame cache, which grow with the boxes searched)
+K_CCD_DRAM_BYTES_PER_CANDIDATE = (42209536 + 14743808 + 310226176 + 1279232) / 132242
 BARRIER_BYTES_PER_CONSTRAINT = 1456
 
 
@@ -677,8 +677,11 @@ def main():
                      "traffic": K_CCD_DRAM_BYTES_PER_CANDIDATE * n_ccd,
                      "traffic_source": "ncu capture of the 200-icosphere pile scaled by candidates",
                      "peak_source": peak_kind,
-                     "note": "issue-bound (instruction fetch and FP64), not HBM: algorithmic bytes "
-                             "are 304 B per candidate; the DRAM traffic is the box stacks"},
+                     "note": "issue-bound (instruction fetch, FP64 at 1/64 rate, 11 of 32 lanes "
+                             "active), not HBM: algorithmic bytes are 304 B per candidate, DRAM "
+                             "traffic 2.8 KB per candidate (per-lane state spilling from L1)",
+                     "fp64": {"pipe_active": 0.233, "lane_gflops": 53.0, "nominal_gflops": 1250.0,
+                              "source": "ncu capture of the 200-icosphere pile"}},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "clocks": clk.summary(),
