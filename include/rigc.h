@@ -376,7 +376,8 @@ int rigc_sim_scene_params(rigc_ctx* ctx, const double* average_mass,
  * context's own workload -- k_ccd's resident blocks per SM, the CCD frame
  * cache's slots per body, the CCD searches per candidate,
  * k_barrier_local's constraints per warp, the CCD boxes a search piece
- * evaluates before handing its pending boxes to the next launch -- one
+ * evaluates before handing its pending boxes to the next launch, one CCD
+ * search per lane or per warp -- one
  * after the other (median of three runs each), over the continuous
  * candidates of x0 -> x1 and the constraint set at x0 (device poses), and
  * keeps the fastest in the context for every later call.  rigc_set_tune
@@ -386,6 +387,7 @@ typedef struct rigc_tune_report {
     double ccd_ms_default, ccd_ms, barrier_ms_default, barrier_ms;
     int32_t ccd_seeds_log2;
     int32_t ccd_hand_off;
+    int32_t ccd_warp;
 } rigc_tune_report;
 int rigc_autotune(rigc_ctx* ctx, const double* x0, const double* x1, double dhat, double dmin,
                   rigc_tune_report* report);
@@ -394,9 +396,14 @@ int rigc_autotune(rigc_ctx* ctx, const double* x0, const double* x1, double dhat
  * candidate count).  ccd_hand_off: a search piece that has evaluated this
  * many boxes hands its pending boxes to a further k_ccd launch, so that deep
  * searches spread over the whole GPU (0: never; -1: the built-in 64).  The
- * earliest time of impact depends on neither. */
+ * earliest time of impact depends on neither.  ccd_warp: 0 searches one
+ * candidate per lane (k_ccd), 1 one per warp with the lanes
+ * evaluating each box together (k_ccd_warp: a tenth of the FP64 chain per
+ * box; the built-in choice, -1).
+ * The results are the same bits either way. */
 int rigc_set_tune(rigc_ctx* ctx, int32_t ccd_blocks_per_sm, int32_t cache_slots_per_body,
-                  int32_t barrier_per_warp, int32_t ccd_seeds_log2, int32_t ccd_hand_off);
+                  int32_t barrier_per_warp, int32_t ccd_seeds_log2, int32_t ccd_hand_off,
+                  int32_t ccd_warp);
 
 /* ---- differentiation (new: the reference has no adjoint).
  * rigc_sim_rollout advances the simulation by num_steps steps like

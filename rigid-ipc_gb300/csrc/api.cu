@@ -603,11 +603,12 @@ int rigc_autotune(rigc_ctx* ctx, const double* x0, const double* x1, double dhat
 }
 
 int rigc_set_tune(rigc_ctx* ctx, int32_t ccd_blocks_per_sm, int32_t cache_slots_per_body,
-                  int32_t barrier_per_warp, int32_t ccd_seeds_log2, int32_t ccd_hand_off)
+                  int32_t barrier_per_warp, int32_t ccd_seeds_log2, int32_t ccd_hand_off,
+                  int32_t ccd_warp)
 {
     if (!ctx || ccd_blocks_per_sm < 0 || cache_slots_per_body < 0 || barrier_per_warp < 0
         || barrier_per_warp > 32 || cache_slots_per_body > (1 << 16) || ccd_seeds_log2 < -1
-        || ccd_seeds_log2 > 5 || ccd_hand_off < -1)
+        || ccd_seeds_log2 > 5 || ccd_hand_off < -1 || ccd_warp < -1 || ccd_warp > 1)
         return RIGC_ERR_ARG;
     Ctx& c = *ctx_of(ctx);
     c.tune.ccd_blocks_per_sm = ccd_blocks_per_sm;
@@ -615,6 +616,7 @@ int rigc_set_tune(rigc_ctx* ctx, int32_t ccd_blocks_per_sm, int32_t cache_slots_
     c.tune.barrier_per_warp = barrier_per_warp;
     c.tune.ccd_seeds_log2 = ccd_seeds_log2;
     c.tune.ccd_hand_off = ccd_hand_off;
+    c.tune.ccd_warp = ccd_warp;
     return RIGC_OK;
 }
 

@@ -10,6 +10,7 @@
 //  * the CCD searches per candidate (1 .. 32, from the nodes of its
 //    subdivision tree at that depth): more fill the GPU when candidates are
 //    few or deep, fewer skip the nodes above that depth;
+//  * one CCD search per lane (k_ccd) or per warp (k_ccd_warp), first;
 //  * the CCD boxes a search piece evaluates before it hands its pending
 //    boxes to a further launch (never, 16, the built-in 64, 256): short
 //    pieces spread deep searches over the GPU, each hand-off costs a launch;
@@ -31,7 +32,8 @@ int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flag
             double* per);
 int barrier_term_impl(Ctx& c, const double* x, double dhat, double dmin, int flags,
                       rigc_barrier_out* out);
-int ccd_max_blocks_per_sm(int* out);
+int ccd_max_blocks_per_sm(int* out, bool warp);
+bool ccd_warp_mode(const Ctx& c, int64_t n);
 
 namespace {
 
@@ -67,9 +69,19 @@ int autotune(Ctx& c, const double* x0, const double* x1, double dhat, double dmi
         return (s == RIGC_ERR_QUEUE_OVERFLOW || s == RIGC_ERR_ITER_LIMIT) ? RIGC_OK : s;
     };
     RIGC_TRY(median_ms(ccd, &r.ccd_ms_default));
-    int occ;
-    RIGC_TRY(ccd_max_blocks_per_sm(&occ));
     double best = r.ccd_ms_default;
+    // one search per lane or per warp (the default: per warp)
+    const int64_t ncand = c.cand.num_ee + c.cand.num_fv;
+    const int mode0 = ccd_warp_mode(c, ncand) ? 1 : 0;
+    c.tune.ccd_warp = 1 - mode0;
+    {
+        double ms;
+        RIGC_TRY(median_ms(ccd, &ms));
+        if (ms < best) best = ms;
+        else c.tune.ccd_warp = mode0;
+    }
+    int occ;
+    RIGC_TRY(ccd_max_blocks_per_sm(&occ, c.tune.ccd_warp == 1));
     int best_bps = 0;
     for (int bps = 1; bps <= occ; bps++) {
         c.tune.ccd_blocks_per_sm = bps;
@@ -141,6 +153,7 @@ int autotune(Ctx& c, const double* x0, const double* x1, double dhat, double dmi
     r.barrier_per_warp = c.tune.barrier_per_warp;
     r.ccd_seeds_log2 = c.tune.ccd_seeds_log2;
     r.ccd_hand_off = c.tune.ccd_hand_off;
+    r.ccd_warp = c.tune.ccd_warp;
     if (rep) *rep = r;
     return RIGC_OK;
 }

@@ -413,13 +413,14 @@ static __device__ __noinline__ int eval_vertices(const CCDArgs& a, const OwnFram
 // with a missing frame (body, node n at depth d), the 31 lanes compute the
 // frames of the five-level subtree below n's parent (n, its sibling and
 // their descendants down to depth d + 3), publish them in the cache, and the
-// requesting lane receives n's frame.  The depth-first search keeps asking
+// requesting lane (every lane with to_all) receives n's frame.  The depth-first search keeps asking
 // for those nodes, so one converged pass replaces up to 31 single-lane
 // rotation enclosures.
 static __device__ __noinline__ void warp_compute_frames(const CCDArgs& a, OwnFrames& own,
                                                         unsigned req, int req_side,
                                                         int req_body,
-                                                        unsigned long long req_node)
+                                                        unsigned long long req_node,
+                                                        bool to_all = false)
 {
     const int lane = threadIdx.x & 31;
     while (req) {
@@ -455,7 +456,7 @@ static __device__ __noinline__ void warp_compute_frames(const CCDArgs& a, OwnFra
             f[18 + 2 * j] = __shfl_sync(0xffffffffu, p[j].lo, owner);
             f[19 + 2 * j] = __shfl_sync(0xffffffffu, p[j].hi, owner);
         }
-        if (lane == src) {
+        if (to_all || lane == src) {
             own.key[side] = frame_key(body, node);
 #pragma unroll
             for (int j = 0; j < kTableEntry; j++) own.f[side][j] = f[j];
@@ -1012,6 +1013,370 @@ k_ccd(CCDArgs a)
     }
 }
 
+// ---------------------------------------------------------------------------
+// One search per warp.  The same branch and bound, pruning, seeds, budget and
+// search pieces as k_ccd, but a box is evaluated by the whole warp: lane
+// 3 v + c (v < 4, c < 3) computes coordinate c of vertex v's interval
+// position (the coordinate expression of iworld_vertex) and lanes 0..2 the
+// interval distance function's coordinate c (the expression of f_zero), so
+// the chain of FP64 instructions per box is about a tenth of one lane's and
+// the lanes stay converged.  The search state is identical in every lane;
+// lane 0 does the atomics.  Same bits as k_ccd for every box.
+
+// rest vertex v of a candidate (EE: a0 a1 b0 b1; FV: v f0 f1 f2), its bodies
+// and kind
+__device__ __forceinline__ void warp_candidate(const CCDArgs& a, int64_t i, int vtx, bool& fv,
+                                               int& body_a, int& body_b, double rv[3])
+{
+    int vid;
+    if (i < a.nee) {
+        fv = false;
+        const int ea = a.ee[i].x, eb = a.ee[i].y;
+        const int e = vtx < 2 ? ea : eb;
+        vid = a.edges[2 * e + (vtx & 1)];
+        body_a = a.ebody[ea];
+        body_b = a.ebody[eb];
+    } else {
+        fv = true;
+        const int64_t k = i - a.nee;
+        const int f = a.fv[k].x, v = a.fv[k].y;
+        vid = vtx == 0 ? v : a.faces[3 * f + (vtx - 1)];
+        body_a = a.vbody[v];
+        body_b = a.fbody[f];
+    }
+#pragma unroll
+    for (int j = 0; j < 3; j++) rv[j] = a.rest[3 * (size_t)vid + j];
+}
+
+// row c of R and p[c] of a frame entry (kTableEntry doubles)
+__device__ __forceinline__ void frame_row(const double* e, int c, Itv r[3], Itv& pc, bool cg)
+{
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+        r[k] = cg ? Itv { __ldcg(e + 6 * c + 2 * k), __ldcg(e + 6 * c + 2 * k + 1) }
+                  : Itv { e[6 * c + 2 * k], e[6 * c + 2 * k + 1] };
+    pc = cg ? Itv { __ldcg(e + 18 + 2 * c), __ldcg(e + 19 + 2 * c) } : Itv { e[18 + 2 * c], e[19 + 2 * c] };
+}
+
+// Row c of the frame of a body over t: the table, the warp's own frames, the
+// cache; a time interval that is not a tree node is computed on the spot.
+// False when the frame still has to be computed.
+__device__ __forceinline__ bool frame_find_row(const CCDArgs& a, const OwnFrames& own, int side,
+                                              int body, unsigned long long node, const Itv& t, int c,
+                                              Itv r[3], Itv& pc)
+{
+    if (node != 0 && node < (1ull << kTableDepth)) {
+        frame_row(a.table + ((size_t)body * kTableSlots + (node - 1)) * kTableEntry, c, r, pc, false);
+        return true;
+    }
+    if (node == 0) {
+        Itv R[9], p[3];
+        frame_compute(a, body, t, R, p);
+#pragma unroll
+        for (int k = 0; k < 3; k++) r[k] = R[3 * c + k];
+        pc = p[c];
+        return true;
+    }
+    const unsigned long long key = frame_key(body, node);
+    if (own.key[side] == key) {
+        frame_row(own.f[side], c, r, pc, false);
+        return true;
+    }
+    unsigned long long h = mix64(key);
+    for (int probe = 0; probe < kProbes; probe++, h++) {
+        const unsigned long long k = ld_acquire(a.fkeys + (h & a.fmask));
+        if (k == key) {
+            frame_row(a.fvals + (h & a.fmask) * kTableEntry, c, r, pc, true);
+            return true;
+        }
+        if (k == 0 || k == (key | kPending)) return false;
+    }
+    return false;
+}
+
+__device__ __forceinline__ unsigned long long* gmin_body(const CCDArgs& a, int body_a)
+{
+    return a.scene_gmin ? a.scene_gmin + a.bscene[body_a] : a.gmin;
+}
+
+__global__ void __launch_bounds__(kCCDThreads)
+k_ccd_warp(CCDArgs a)
+{
+    const int64_t n = a.nee + a.nfv;
+    const int64_t nwork = a.pieces_in ? a.n_pieces : (n << a.seeds_log2);
+    const int lane = threadIdx.x & 31;
+    const int vtx = lane / 3, crd = lane - 3 * (lane / 3);
+    const bool vlane = lane < 12;
+    unsigned long long tot_boxes = 0, tot_hits = 0, pops = 0;
+    // search state (the same in every lane)
+    Node cn { { 0, 0, 0 }, { 0ull, 0ull, 0ull }, 0 };
+    bool has_cn = false;
+    u128 pend_hi = 0, mt = 0, ma = 0;
+    long long cur = -1;
+    double earliest = INFINITY;
+    bool found = false;
+    int status = RIGC_OK;
+    unsigned long long cboxes = 0, cbase = 0;
+    bool hand_ok = a.hand_off != 0, tail = false;
+    double gbound = INFINITY;
+    double tol[3] = { 0, 0, 0 };
+    bool fv = false, a_fixed = false, b_fixed = false;
+    int body_a = 0, body_b = 0;
+    // this lane's vertex and its coordinate interval over [ct0, ct1]
+    double rv[3] = { 0, 0, 0 };
+    Itv pcrd { 0, 0 };
+    const double nan = __longlong_as_double(0x7ff8000000000000ll);
+    double ct0 = nan, ct1 = nan;
+    bool fresh = true;
+    OwnFrames own;
+    own.key[0] = own.key[1] = 0;
+    while (true) {
+        // hand the pending boxes of a long piece to the next launch once
+        // the work list has run dry
+        if (tail && hand_ok && cboxes >= a.hand_off && (pend_hi != 0 || has_cn)) {
+            const int k = popc128(pend_hi) + (has_cn ? 1 : 0);
+            unsigned long long s = 0;
+            if (lane == 0) s = atomicAdd(a.n_out, (unsigned long long)k);
+            s = __shfl_sync(0xffffffffu, s, 0);
+            if (s + k <= a.out_cap) {
+                if (lane == 0) {
+                    Piece pc;
+                    pc.cand = cur;
+                    pc.earliest = earliest;
+                    pc.boxes = cbase + cboxes;
+                    unsigned long long o = s;
+                    for (u128 r = pend_hi; r != 0; r &= r - 1) {
+                        const Node g = pending_node(cn, mt, ma, lsb128(r));
+                        for (int d = 0; d < 3; d++) {
+                            pc.ix[d] = g.ix[d];
+                            pc.lv[d] = g.lv[d];
+                        }
+                        pc.depth = g.depth;
+                        a.pieces_out[o++] = pc;
+                    }
+                    if (has_cn) {
+                        for (int d = 0; d < 3; d++) {
+                            pc.ix[d] = cn.ix[d];
+                            pc.lv[d] = cn.lv[d];
+                        }
+                        pc.depth = cn.depth;
+                        a.pieces_out[o++] = pc;
+                    }
+                }
+                pend_hi = 0;
+                has_cn = false;
+            } else {
+                if (lane == 0)
+                    for (unsigned long long t = s; t < s + k && t < a.out_cap; t++) a.pieces_out[t].cand = -1;
+                hand_ok = false;
+            }
+        }
+        bool have = false;
+        Box x;
+        while (has_cn || pend_hi != 0) {
+            if (has_cn) {
+                has_cn = false;
+            } else {
+                const int j = msb128(pend_hi);
+                pend_hi &= ~bit128(j);
+                cn = pending_node(cn, mt, ma, j);
+            }
+            x = node_box(cn);
+            if (le_nn(earliest, x.t0)) continue;
+            if (a.prune) {
+                if ((++pops & 7) == 0) {
+                    // values read while other warps write them: lane 0's
+                    // copy for all, so that the warp's state stays uniform
+                    gbound = __shfl_sync(0xffffffffu, __longlong_as_double(
+                        (long long)*(volatile unsigned long long*)gmin_body(a, body_a)), 0);
+                    tail = __shfl_sync(0xffffffffu,
+                        (int)(*(volatile unsigned long long*)a.next >= (unsigned long long)nwork), 0) != 0;
+                }
+                if (le_nn(gbound, x.t0)) continue;
+            }
+            if (fv) {
+                double sl = add_dn(x.a0, x.b0), sh = add_up(x.a1, x.b1);
+                if (!(le_nn(sl, 1.0) && !is_neg(sh))) continue;
+            }
+            have = true;
+            break;
+        }
+        if (!have) {
+            if (cur >= 0 && lane == 0) {
+                if (found) {
+                    unsigned long long* g = gmin_body(a, body_a);
+                    const unsigned long long b = (unsigned long long)__double_as_longlong(earliest);
+                    if (a.scene_gmin) atomicMin(g, b);
+                    atomicMin(a.gmin, b);
+                    tot_hits++;
+                    if (a.per) atomicMin(reinterpret_cast<unsigned long long*>(a.per) + cur, b);
+                }
+                if (status != RIGC_OK) atomicMax(a.status, status);
+            }
+            // next work item: seed w / n of candidate w % n, or piece w
+            long long w = 0;
+            if (lane == 0) w = (long long)atomicAdd(a.next, 1ull);
+            w = __shfl_sync(0xffffffffu, w, 0);
+            if (w >= nwork) break;  // the warp is done
+            tail = tail || w + 1 >= nwork;
+            found = false;
+            status = RIGC_OK;
+            cboxes = 0;
+            pend_hi = 0;
+            has_cn = false;
+            if (a.pieces_in) {
+                const Piece pc = a.pieces_in[w];
+                cur = pc.cand;
+                if (cur < 0) continue;
+                earliest = pc.earliest;
+                cbase = pc.boxes;
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    cn.ix[d] = pc.ix[d];
+                    cn.lv[d] = pc.lv[d];
+                }
+                cn.depth = pc.depth;
+                has_cn = true;
+            } else {
+                cur = w % n;
+                earliest = INFINITY;
+                cbase = 0;
+            }
+            warp_candidate(a, cur, vlane ? vtx : 0, fv, body_a, body_b, rv);
+            a_fixed = a.bfixed[body_a] != 0;
+            b_fixed = a.bfixed[body_b] != 0;
+            fresh = true;
+            ct0 = ct1 = nan;
+            tol[0] = a.ctol[3 * cur];
+            tol[1] = a.ctol[3 * cur + 1];
+            tol[2] = a.ctol[3 * cur + 2];
+            if (a.prune)
+                gbound = __shfl_sync(0xffffffffu, __longlong_as_double(
+                    (long long)*(volatile unsigned long long*)gmin_body(a, body_a)), 0);
+            if (a.pieces_in) continue;  // the piece's node is popped next
+            cn = seed_node(a.seeds_log2, w / n, tol, mt, ma);
+            x = node_box(cn);
+            have = !(a.prune && le_nn(gbound, x.t0));
+            if (have && fv) {
+                double sl = add_dn(x.a0, x.b0), sh = add_up(x.a1, x.b1);
+                have = le_nn(sl, 1.0) && !is_neg(sh);
+            }
+            if (!have) continue;
+        }
+        if (cbase + cboxes >= (unsigned long long)a.max_boxes) {
+            // budget exhausted: the earliest unexplored t.lo is conservative
+            double m = x.t0;
+            for (u128 r = pend_hi; r != 0; r &= r - 1) {
+                const Node g = pending_node(cn, mt, ma, lsb128(r));
+                m = smin(m, dyadic(g.ix[0], g.lv[0]));
+            }
+            earliest = smin(earliest, m);
+            found = true;
+            status = RIGC_ERR_ITER_LIMIT;
+            pend_hi = 0;
+            has_cn = false;
+            continue;
+        }
+        // vertex coordinates over the box's time interval
+        if (!(dbits(x.t0) == dbits(ct0) && dbits(x.t1) == dbits(ct1))) {
+            const int na = fv ? 1 : 2;
+            const int side = vtx < na ? 0 : 1;
+            const bool need = vlane && (fresh || !(side ? b_fixed : a_fixed));
+            const Itv t { x.t0, x.t1 };
+            const unsigned long long node = time_node(x.t0, x.t1);
+            bool miss = false;
+            if (need) {
+                Itv r[3], pc;
+                if (frame_find_row(a, own, side, side ? body_b : body_a, node, t, crd, r, pc))
+                    pcrd = iadd(iadd(iadd(imul(rv[0], r[0]), imul(rv[1], r[1])), imul(rv[2], r[2])), pc);
+                else
+                    miss = true;
+            }
+            const unsigned mm = __ballot_sync(0xffffffffu, miss);
+            if (mm) {
+                // the warp computes the missing frames (lane 0 asks for body
+                // A's, lane 1 for body B's), every lane keeps them; retry
+                bool miss_a = false, miss_b = false;
+#pragma unroll
+                for (int l = 0; l < 12; l++)
+                    if ((mm >> l) & 1) {
+                        if (l / 3 < na) miss_a = true;
+                        else miss_b = true;
+                    }
+                const unsigned req = (miss_a ? 1u : 0u) | (miss_b ? 2u : 0u);
+                warp_compute_frames(a, own, req, lane == 1 ? 1 : 0, lane == 1 ? body_b : body_a, node,
+                                    true);
+                ct0 = ct1 = nan;
+                has_cn = true;
+                continue;
+            }
+            fresh = false;
+            ct0 = x.t0;
+            ct1 = x.t1;
+        }
+        cboxes++;
+        if (lane == 0) tot_boxes++;
+        // f(box) contains zero: lanes 0..2 take coordinate c of the four
+        // vertices and evaluate the distance function's coordinate c
+        Itv P[4];
+#pragma unroll
+        for (int v = 0; v < 4; v++) {
+            P[v].lo = __shfl_sync(0xffffffffu, pcrd.lo, 3 * v + crd);
+            P[v].hi = __shfl_sync(0xffffffffu, pcrd.hi, 3 * v + crd);
+        }
+        bool zin = true;
+        if (lane < 3) {
+            const Itv al { x.a0, x.a1 }, be { x.b0, x.b1 };
+            Itv y;
+            if (fv) {
+                Itv fp = iadd(iadd(imul_nonneg(isub(P[2], P[1]), al), imul_nonneg(isub(P[3], P[1]), be)),
+                              P[1]);
+                y = isub(P[0], fp);
+            } else {
+                Itv ea = iadd(imul_nonneg(isub(P[1], P[0]), al), P[0]);
+                Itv eb = iadd(imul_nonneg(isub(P[3], P[2]), be), P[2]);
+                y = isub(ea, eb);
+            }
+            zin = zero_in(y);
+        }
+        if (!__all_sync(0xffffffffu, zin)) continue;
+        double w[3];
+        node_widths(cn, w);
+        bool all_tol = le_nn(w[0], tol[0]) && le_nn(w[1], tol[1]) && le_nn(w[2], tol[2]);
+        bool all_zero = le_nn(w[0], 1e-10) && le_nn(w[1], 1e-10) && le_nn(w[2], 1e-10);
+        if ((is_pos(x.t0) || all_zero) && all_tol) {
+            earliest = x.t0;
+            found = true;
+            if (a.prune) {
+                if (lane == 0) {
+                    const unsigned long long b = (unsigned long long)__double_as_longlong(earliest);
+                    if (a.scene_gmin) atomicMin(gmin_body(a, body_a), b);
+                    atomicMin(a.gmin, b);
+                }
+                gbound = smin(gbound, earliest);
+            }
+            continue;
+        }
+        const int split = split_dim(w, tol, all_tol);
+        if (cn.depth >= kMaxDepth || cn.lv[split] >= kMaxLevel) {
+            earliest = smin(earliest, x.t0);
+            found = true;
+            status = RIGC_ERR_QUEUE_OVERFLOW;
+            continue;
+        }
+        record_split(mt, ma, cn.depth, split);
+        pend_hi |= bit128(cn.depth);
+        cn.lv[split]++;
+        cn.ix[split] <<= 1;
+        cn.depth++;
+        has_cn = true;
+    }
+    if (lane == 0) {
+        if (tot_boxes) atomicAdd(a.boxes, tot_boxes);
+        if (tot_hits) atomicAdd(a.hits, tot_hits);
+    }
+}
+
 __global__ void k_fill_inf(double* __restrict__ v, int64_t n)
 {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1019,15 +1384,25 @@ __global__ void k_fill_inf(double* __restrict__ v, int64_t n)
 }
 
 // resident k_ccd blocks per SM at full occupancy
-int ccd_max_blocks_per_sm(int* out)
+int ccd_max_blocks_per_sm(int* out, bool warp)
 {
-    static int blocks_per_sm = 0;
-    if (!blocks_per_sm) {
-        RIGC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_ccd, kCCDThreads, 0));
-        if (blocks_per_sm < 1) blocks_per_sm = 1;
+    static int blocks_per_sm[2] = { 0, 0 };
+    int& b = blocks_per_sm[warp ? 1 : 0];
+    if (!b) {
+        if (warp) RIGC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_ccd_warp, kCCDThreads, 0));
+        else RIGC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_ccd, kCCDThreads, 0));
+        if (b < 1) b = 1;
     }
-    *out = blocks_per_sm;
+    *out = b;
     return RIGC_OK;
+}
+
+// one search per warp (k_ccd_warp) unless the context's tuning asks for one
+// per lane: per warp measured faster on every workload here (the 1000-
+// icosphere pile, the 256-scene batch, the cube lattices, the chain)
+bool ccd_warp_mode(const Ctx& c, int64_t)
+{
+    return c.tune.ccd_warp >= 0 ? c.tune.ccd_warp == 1 : true;
 }
 
 // counters layout in the context's device scalars (byte offset 256):
@@ -1108,8 +1483,10 @@ int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flag
             RIGC_COUNT_LAUNCH();
             k_fill_inf<<<grid_for(n, 256), 256, 0, st>>>(per, n);
         }
+        const bool warp_mode = ccd_warp_mode(c, n);
+        const int per_block = warp_mode ? kCCDThreads / 32 : kCCDThreads;  // searches per block
         int blocks_per_sm;
-        RIGC_TRY(ccd_max_blocks_per_sm(&blocks_per_sm));
+        RIGC_TRY(ccd_max_blocks_per_sm(&blocks_per_sm, warp_mode));
         int dev = 0, sms = kNumSMs;
         RIGC_CUDA(cudaGetDevice(&dev));
         RIGC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -1122,7 +1499,7 @@ int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flag
         if (a.prune) {
             if (c.tune.ccd_seeds_log2 >= 0) a.seeds_log2 = std::min(c.tune.ccd_seeds_log2, 5);
             else
-                while (a.seeds_log2 < 5 && (n << a.seeds_log2) * 4 < full * kCCDThreads) a.seeds_log2++;
+                while (a.seeds_log2 < 5 && (n << a.seeds_log2) * 4 < full * per_block) a.seeds_log2++;
         }
         // search pieces (prune mode): launch 0 searches the seeds and hands
         // the rest of every search that reaches hand_off boxes to launch 1,
@@ -1143,10 +1520,11 @@ int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flag
                 a.pieces_out = c.ccd_pieces[0].as<Piece>();
             }
         }
-        int64_t want = ((n << a.seeds_log2) + kCCDThreads - 1) / kCCDThreads;
+        int64_t want = ((n << a.seeds_log2) + per_block - 1) / per_block;
         for (int launch = 0;; launch++) {
             RIGC_COUNT_LAUNCH();
-            k_ccd<<<(unsigned)std::min(want, full), kCCDThreads, 0, st>>>(a);
+            if (warp_mode) k_ccd_warp<<<(unsigned)std::min(want, full), kCCDThreads, 0, st>>>(a);
+            else k_ccd<<<(unsigned)std::min(want, full), kCCDThreads, 0, st>>>(a);
             RIGC_CUDA(cudaGetLastError());
             if (!a.hand_off) break;
             unsigned long long np = 0;
@@ -1161,7 +1539,7 @@ int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flag
             a.n_pieces = (long long)np;
             a.pieces_out = c.ccd_pieces[(launch + 1) & 1].as<Piece>();
             if (launch + 1 >= kMaxLaunches - 1) a.hand_off = 0;
-            want = ((int64_t)np + kCCDThreads - 1) / kCCDThreads;
+            want = ((int64_t)np + per_block - 1) / per_block;
         }
     }
     unsigned long long out[4];

@@ -392,9 +392,9 @@ class Context:
         return {f: getattr(r, f) for f, _ in L.TuneReport._fields_}
 
     def set_tune(self, ccd_blocks_per_sm=0, cache_slots_per_body=0, barrier_per_warp=0,
-                 ccd_seeds_log2=-1, ccd_hand_off=-1):
+                 ccd_seeds_log2=-1, ccd_hand_off=-1, ccd_warp=-1):
         L.check(self.lib.rigc_set_tune(self.h, ccd_blocks_per_sm, cache_slots_per_body,
-                                       barrier_per_warp, ccd_seeds_log2, ccd_hand_off),
+                                       barrier_per_warp, ccd_seeds_log2, ccd_hand_off, ccd_warp),
                 "rigc_set_tune")
 
     def sim_rollout(self, num_steps, checkpoint_every=10):

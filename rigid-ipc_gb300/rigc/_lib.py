@@ -106,7 +106,7 @@ class TuneReport(C.Structure):
                 ("barrier_per_warp", C.c_int32), ("ccd_ms_default", C.c_double),
                 ("ccd_ms", C.c_double), ("barrier_ms_default", C.c_double),
                 ("barrier_ms", C.c_double), ("ccd_seeds_log2", C.c_int32),
-                ("ccd_hand_off", C.c_int32)]
+                ("ccd_hand_off", C.c_int32), ("ccd_warp", C.c_int32)]
 
 
 class StepStats(C.Structure):
@@ -171,7 +171,7 @@ def load():
     L.rigc_sim_backward.argtypes = [_vp] + [_vp] * 6
     L.rigc_sim_scene_params.argtypes = [_vp, _vp, _vp]
     L.rigc_autotune.argtypes = [_vp, _vp, _vp, C.c_double, C.c_double, C.POINTER(TuneReport)]
-    L.rigc_set_tune.argtypes = [_vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
+    L.rigc_set_tune.argtypes = [_vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
     L.rigc_ctx_create_batched.argtypes = [C.POINTER(SceneDesc), C.c_int32, _vp, C.POINTER(_vp)]
     L.rigc_num_scenes.argtypes = [_vp]
     L.rigc_scene_tois.argtypes = [_vp, _d]

@@ -1,7 +1,8 @@
 """The CUDA path on the reference's own CCD test data (fixtures packed by
 tests/golden/make_reference_fixtures.py, oracle results stored with them):
 per-query and per-candidate times of impact bit-exact, the wrecking-ball
-scene's candidate set identical."""
+scene's candidate set identical, with one search per lane (k_ccd) and one
+per warp (k_ccd_warp) alike."""
 import os
 
 import numpy as np
@@ -12,7 +13,8 @@ from test_reference_fixtures import queries, scene_fixture
 pytestmark = pytest.mark.gpu
 
 
-def test_reference_queries_gpu():
+@pytest.mark.parametrize("warp", [0, 1])
+def test_reference_queries_gpu(warp):
     """All 403 queries in one context, candidates given explicitly."""
     import make_reference_fixtures as M
     import rigc
@@ -40,6 +42,7 @@ def test_reference_queries_gpu():
         x1 += [P[0, 1], P[1, 1]]
     scene = S.Scene(bodies=bodies)
     ctx = rigc.Context(scene)
+    ctx.set_tune(ccd_warp=warp)
     ctx.set_ccd_budget(int(q["budget"]))
     ctx.set_candidates(ee, fv)
     x0 = np.concatenate(x0)
@@ -52,13 +55,15 @@ def test_reference_queries_gpu():
     assert toi == expect.min()
 
 
-def test_wrecking_ball_scene_gpu():
+@pytest.mark.parametrize("warp", [0, 1])
+def test_wrecking_ball_scene_gpu(warp):
     import make_reference_fixtures as M
     import rigc
 
     d = scene_fixture()
     sc = M.scene_from_fixture(d)
     ctx = rigc.Context(sc)
+    ctx.set_tune(ccd_warp=warp)
     x0 = d["pose_t0"].reshape(-1)
     x1 = d["pose_t1"].reshape(-1)
     ee, fv = ctx.detect_collision_candidates_rigid(x0, x1, True, 0.0)
