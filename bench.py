@@ -44,7 +44,8 @@ CCD_BYTES_PER_PAIR = 304        # ids + 4 rest vertices + 4 poses + toi
 # candidates; profiles/k_ccd_icosphere_pile_200.md); the traffic of a full
 # call is this times its candidates (per-lane candidate state spilling from
 # L1 and the frame cache, which grow with the boxes searched)
-K_CCD_DRAM_BYTES_PER_CANDIDATE = (42209536 + 14743808 + 310226176 + 1279232) / 132242
+K_CCD_DRAM_BYTES_PER_CANDIDATE = {"k_ccd": (42209536 + 14743808 + 310226176 + 1279232) / 132242,
+                                  "k_ccd_warp": (42209536 + 14743808 + 310226176 + 1279232) / 132242}
 BARRIER_BYTES_PER_CONSTRAINT = 1456
 
 
@@ -657,6 +658,9 @@ def main():
     d2h = 6 * nb * 8 + (nb + 1) * 4 + nnzb * (4 + 36 * 8)
 
     peak, peak_kind = measured_peaks()
+    # the CCD kernel the context launches: one search per warp unless tuned
+    # to one per lane
+    ccd_kernel = "k_ccd" if (tune and tune.get("ccd_warp") == 0) else "k_ccd_warp"
     ccd_bytes = CCD_BYTES_PER_PAIR * n_ccd
     achieved = ccd_bytes / t_ccd / 1e9
     line = {
@@ -672,9 +676,9 @@ def main():
                    "before every timed step", "parallelism": "replicas" if world > 1 else "1 GPU"},
         "phases_s": {"ccd_narrow": t_ccd, "ccd_broad": t_bp, "barrier_and_assembly": t_bar},
         "ccd_pairs_per_s": n_ccd / t_ccd, "barrier_constraints_per_s": n_cons / t_bar,
-        "roofline": {"bound": "hbm", "kernel": "k_ccd", "achieved": achieved, "peak": peak,
+        "roofline": {"bound": "hbm", "kernel": ccd_kernel, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": K_CCD_DRAM_BYTES_PER_CANDIDATE * n_ccd,
+                     "traffic": K_CCD_DRAM_BYTES_PER_CANDIDATE[ccd_kernel] * n_ccd,
                      "traffic_source": "ncu capture of the 200-icosphere pile scaled by candidates",
                      "peak_source": peak_kind,
                      "note": "issue-bound (instruction fetch, FP64 at 1/64 rate, 11 of 32 lanes "
