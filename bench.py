@@ -38,14 +38,19 @@ import numpy as np  # noqa: E402
 METRIC = "candidate pairs/s (CCD+barrier grad/Hess)"
 UNIT = "pairs/s"
 CCD_BYTES_PER_PAIR = 304        # ids + 4 rest vertices + 4 poses + toi
-# DRAM bytes (read + write) per continuous candidate of one CCD call (its
-# k_ccd launches), from the ncu capture of the 200-icosphere pile (built-in
-# shapes: 56.95 MB read + 311.51 MB written over two launches for 132,242
-# candidates; profiles/k_ccd_icosphere_pile_200.md); the traffic of a full
-# call is this times its candidates (per-lane candidate state spilling from
-# L1 and the frame cache, which grow with the boxes searched)
-K_CCD_DRAM_BYTES_PER_CANDIDATE = {"k_ccd": (42209536 + 14743808 + 310226176 + 1279232) / 132242,
-                                  "k_ccd_warp": (42209536 + 14743808 + 310226176 + 1279232) / 132242}
+# DRAM bytes (read + write) per continuous candidate of one CCD call (all its
+# launches), from ncu captures of the 200-icosphere pile with the built-in
+# shapes (132,242 candidates; profiles/k_ccd_icosphere_pile_200.md):
+# k_ccd 56.95 MB read + 311.51 MB written over two launches (per-lane
+# candidate state spilling from L1, the frame cache); k_ccd_warp 20.95 MB +
+# 15.81 MB over three.  The traffic of a full call is this times its
+# candidates.  FP64 figures of the same captures: pipe active (fraction of
+# peak) and lane-level GFLOP/s (dadd + dmul + 2 dfma over the launch).
+K_CCD_DRAM_BYTES_PER_CANDIDATE = {
+    "k_ccd": (42209536 + 14743808 + 310226176 + 1279232) / 132242,
+    "k_ccd_warp": (17837312 + 2597632 + 512000 + 15804928 + 1792) / 132242}
+K_CCD_FP64 = {"k_ccd": {"pipe_active": 0.233, "lane_gflops": 53.0},
+              "k_ccd_warp": {"pipe_active": 0.496, "lane_gflops": 98.4}}
 BARRIER_BYTES_PER_CONSTRAINT = 1456
 
 
@@ -681,11 +686,11 @@ def main():
                      "traffic": K_CCD_DRAM_BYTES_PER_CANDIDATE[ccd_kernel] * n_ccd,
                      "traffic_source": "ncu capture of the 200-icosphere pile scaled by candidates",
                      "peak_source": peak_kind,
-                     "note": "issue-bound (instruction fetch, FP64 at 1/64 rate, 11 of 32 lanes "
-                             "active), not HBM: algorithmic bytes are 304 B per candidate, DRAM "
-                             "traffic 2.8 KB per candidate (per-lane state spilling from L1)",
-                     "fp64": {"pipe_active": 0.233, "lane_gflops": 53.0, "nominal_gflops": 1250.0,
-                              "source": "ncu capture of the 200-icosphere pile"}},
+                     "note": "FP64-issue-bound (an FP64 warp instruction holds its SM "
+                             "sub-partition's FP64 unit 64 cycles on GB300), not HBM: algorithmic "
+                             "bytes are 304 B per candidate",
+                     "fp64": dict(K_CCD_FP64[ccd_kernel], nominal_gflops=1250.0,
+                                  source="ncu capture of the 200-icosphere pile")},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "clocks": clk.summary(),

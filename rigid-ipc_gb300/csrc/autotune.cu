@@ -10,7 +10,8 @@
 //  * the CCD searches per candidate (1 .. 32, from the nodes of its
 //    subdivision tree at that depth): more fill the GPU when candidates are
 //    few or deep, fewer skip the nodes above that depth;
-//  * one CCD search per lane (k_ccd) or per warp (k_ccd_warp), first;
+//  * one CCD search per lane (k_ccd) or per warp (k_ccd_warp, as compiled
+//    or fitted to 4 blocks per SM), first;
 //  * the CCD boxes a search piece evaluates before it hands its pending
 //    boxes to a further launch (never, 16, the built-in 64, 256): short
 //    pieces spread deep searches over the GPU, each hand-off costs a launch;
@@ -32,8 +33,8 @@ int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flag
             double* per);
 int barrier_term_impl(Ctx& c, const double* x, double dhat, double dmin, int flags,
                       rigc_barrier_out* out);
-int ccd_max_blocks_per_sm(int* out, bool warp);
-bool ccd_warp_mode(const Ctx& c, int64_t n);
+int ccd_max_blocks_per_sm(int* out, int mode);
+int ccd_search_mode(const Ctx& c);
 
 namespace {
 
@@ -70,18 +71,22 @@ int autotune(Ctx& c, const double* x0, const double* x1, double dhat, double dmi
     };
     RIGC_TRY(median_ms(ccd, &r.ccd_ms_default));
     double best = r.ccd_ms_default;
-    // one search per lane or per warp (the default: per warp)
-    const int64_t ncand = c.cand.num_ee + c.cand.num_fv;
-    const int mode0 = ccd_warp_mode(c, ncand) ? 1 : 0;
-    c.tune.ccd_warp = 1 - mode0;
-    {
+    // one search per lane, per warp, or per warp at 4 blocks per SM (the
+    // default: per warp)
+    int best_mode = ccd_search_mode(c);
+    for (int mode : { 0, 1, 2 }) {
+        if (mode == best_mode) continue;
+        c.tune.ccd_warp = mode;
         double ms;
         RIGC_TRY(median_ms(ccd, &ms));
-        if (ms < best) best = ms;
-        else c.tune.ccd_warp = mode0;
+        if (ms < best) {
+            best = ms;
+            best_mode = mode;
+        }
     }
+    c.tune.ccd_warp = best_mode;
     int occ;
-    RIGC_TRY(ccd_max_blocks_per_sm(&occ, c.tune.ccd_warp == 1));
+    RIGC_TRY(ccd_max_blocks_per_sm(&occ, c.tune.ccd_warp));
     int best_bps = 0;
     for (int bps = 1; bps <= occ; bps++) {
         c.tune.ccd_blocks_per_sm = bps;

@@ -1099,7 +1099,10 @@ __device__ __forceinline__ unsigned long long* gmin_body(const CCDArgs& a, int b
     return a.scene_gmin ? a.scene_gmin + a.bscene[body_a] : a.gmin;
 }
 
-__global__ void __launch_bounds__(kCCDThreads)
+// MinBlocks > 1 asks the compiler to fit that many blocks per SM (fewer
+// registers, some spilled to local memory, more warps to hide latency)
+template <int MinBlocks>
+__global__ void __launch_bounds__(kCCDThreads, MinBlocks)
 k_ccd_warp(CCDArgs a)
 {
     const int64_t n = a.nee + a.nfv;
@@ -1384,12 +1387,17 @@ __global__ void k_fill_inf(double* __restrict__ v, int64_t n)
 }
 
 // resident k_ccd blocks per SM at full occupancy
-int ccd_max_blocks_per_sm(int* out, bool warp)
+// resident blocks per SM of the CCD kernel of a search mode (0: k_ccd,
+// 1: k_ccd_warp, 2: k_ccd_warp fitted to 4 blocks per SM)
+int ccd_max_blocks_per_sm(int* out, int mode)
 {
-    static int blocks_per_sm[2] = { 0, 0 };
-    int& b = blocks_per_sm[warp ? 1 : 0];
+    static int blocks_per_sm[3] = { 0, 0, 0 };
+    int& b = blocks_per_sm[mode];
     if (!b) {
-        if (warp) RIGC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_ccd_warp, kCCDThreads, 0));
+        if (mode == 2)
+            RIGC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_ccd_warp<4>, kCCDThreads, 0));
+        else if (mode == 1)
+            RIGC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_ccd_warp<1>, kCCDThreads, 0));
         else RIGC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_ccd, kCCDThreads, 0));
         if (b < 1) b = 1;
     }
@@ -1397,12 +1405,13 @@ int ccd_max_blocks_per_sm(int* out, bool warp)
     return RIGC_OK;
 }
 
-// one search per warp (k_ccd_warp) unless the context's tuning asks for one
-// per lane: per warp measured faster on every workload here (the 1000-
-// icosphere pile, the 256-scene batch, the cube lattices, the chain)
-bool ccd_warp_mode(const Ctx& c, int64_t)
+// the search mode: one search per warp (k_ccd_warp) unless the context's
+// tuning asks for another; per warp measured faster than per lane on every
+// workload here (the 1000-icosphere pile, the 256-scene batch, the cube
+// lattices, the chain)
+int ccd_search_mode(const Ctx& c)
 {
-    return c.tune.ccd_warp >= 0 ? c.tune.ccd_warp == 1 : true;
+    return c.tune.ccd_warp >= 0 ? c.tune.ccd_warp : 1;
 }
 
 // counters layout in the context's device scalars (byte offset 256):
@@ -1483,10 +1492,10 @@ int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flag
             RIGC_COUNT_LAUNCH();
             k_fill_inf<<<grid_for(n, 256), 256, 0, st>>>(per, n);
         }
-        const bool warp_mode = ccd_warp_mode(c, n);
-        const int per_block = warp_mode ? kCCDThreads / 32 : kCCDThreads;  // searches per block
+        const int mode = ccd_search_mode(c);
+        const int per_block = mode ? kCCDThreads / 32 : kCCDThreads;  // searches per block
         int blocks_per_sm;
-        RIGC_TRY(ccd_max_blocks_per_sm(&blocks_per_sm, warp_mode));
+        RIGC_TRY(ccd_max_blocks_per_sm(&blocks_per_sm, mode));
         int dev = 0, sms = kNumSMs;
         RIGC_CUDA(cudaGetDevice(&dev));
         RIGC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -1523,8 +1532,10 @@ int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flag
         int64_t want = ((n << a.seeds_log2) + per_block - 1) / per_block;
         for (int launch = 0;; launch++) {
             RIGC_COUNT_LAUNCH();
-            if (warp_mode) k_ccd_warp<<<(unsigned)std::min(want, full), kCCDThreads, 0, st>>>(a);
-            else k_ccd<<<(unsigned)std::min(want, full), kCCDThreads, 0, st>>>(a);
+            const unsigned grid = (unsigned)std::min(want, full);
+            if (mode == 2) k_ccd_warp<4><<<grid, kCCDThreads, 0, st>>>(a);
+            else if (mode == 1) k_ccd_warp<1><<<grid, kCCDThreads, 0, st>>>(a);
+            else k_ccd<<<grid, kCCDThreads, 0, st>>>(a);
             RIGC_CUDA(cudaGetLastError());
             if (!a.hand_off) break;
             unsigned long long np = 0;
