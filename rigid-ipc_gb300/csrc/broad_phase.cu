@@ -526,11 +526,17 @@ __global__ void k_cell_pairs(const uint64_t* __restrict__ keys, const uint32_t* 
     uint32_t a = vals[i];
     long long a0[3], a1[3];
     bool have_a = false;
+    // Within a cell the items keep the element order of the emission (the
+    // radix sort is stable, elements are ordered vertices, edges, faces):
+    // a face's later items are faces (no pair), an edge's are edges, then
+    // faces (no more pairs), a vertex's reach the faces after the edges.
+    if ((a >> 30) == 2) return;
     for (int64_t j = i + 1; j < m && keys[j] == key; j++) {
         uint32_t b = vals[j];
         bool is_ee;
         unsigned long long pk;
         int ta = a >> 30, tb = b >> 30;
+        if (ta == 1 && tb == 2) break;
         if (!((ta == 1 && tb == 1) || (ta + tb == 2 && ta != tb))) continue;
         if (!pair_filter(P, a, b, is_ee, pk)) continue;
         if (!have_a) {
@@ -560,11 +566,13 @@ __global__ void k_cell_pairs_warp(const uint64_t* __restrict__ keys, const uint3
     const uint32_t a = vals[i];
     long long a0[3], a1[3];
     bool have_a = false;
+    if ((a >> 30) == 2) return;  // faces: only faces follow in the cell
     for (int64_t j = i + 1 + lane; j < m && keys[j] == key; j += 32) {
         uint32_t b = vals[j];
         bool is_ee;
         unsigned long long pk;
         int ta = a >> 30, tb = b >> 30;
+        if (ta == 1 && tb == 2) break;  // an edge's later items: edges, then faces
         if (!((ta == 1 && tb == 1) || (ta + tb == 2 && ta != tb))) continue;
         if (!pair_filter(P, a, b, is_ee, pk)) continue;
         if (!have_a) {
