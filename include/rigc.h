@@ -399,7 +399,8 @@ int rigc_autotune(rigc_ctx* ctx, const double* x0, const double* x1, double dhat
  * earliest time of impact depends on neither.  ccd_warp: 0 searches one
  * candidate per lane (k_ccd), 1 one per warp with the lanes
  * evaluating each box together (k_ccd_warp: a tenth of the FP64 chain per
- * box; the built-in choice, -1), 2 the same fitted to 4 blocks per SM.
+ * box; the built-in choice, -1), 2 / 3 the same fitted to 4 / 5 blocks per
+ * SM (fewer registers, more warps to hide latency).
  * The results are the same bits either way. */
 int rigc_set_tune(rigc_ctx* ctx, int32_t ccd_blocks_per_sm, int32_t cache_slots_per_body,
                   int32_t barrier_per_warp, int32_t ccd_seeds_log2, int32_t ccd_hand_off,

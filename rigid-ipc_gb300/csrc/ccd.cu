@@ -1388,13 +1388,15 @@ __global__ void k_fill_inf(double* __restrict__ v, int64_t n)
 
 // resident k_ccd blocks per SM at full occupancy
 // resident blocks per SM of the CCD kernel of a search mode (0: k_ccd,
-// 1: k_ccd_warp, 2: k_ccd_warp fitted to 4 blocks per SM)
+// 1: k_ccd_warp, 2 / 3: k_ccd_warp fitted to 4 / 5 blocks per SM)
 int ccd_max_blocks_per_sm(int* out, int mode)
 {
-    static int blocks_per_sm[3] = { 0, 0, 0 };
+    static int blocks_per_sm[4] = { 0, 0, 0, 0 };
     int& b = blocks_per_sm[mode];
     if (!b) {
-        if (mode == 2)
+        if (mode == 3)
+            RIGC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_ccd_warp<5>, kCCDThreads, 0));
+        else if (mode == 2)
             RIGC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_ccd_warp<4>, kCCDThreads, 0));
         else if (mode == 1)
             RIGC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_ccd_warp<1>, kCCDThreads, 0));
@@ -1533,7 +1535,8 @@ int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flag
         for (int launch = 0;; launch++) {
             RIGC_COUNT_LAUNCH();
             const unsigned grid = (unsigned)std::min(want, full);
-            if (mode == 2) k_ccd_warp<4><<<grid, kCCDThreads, 0, st>>>(a);
+            if (mode == 3) k_ccd_warp<5><<<grid, kCCDThreads, 0, st>>>(a);
+            else if (mode == 2) k_ccd_warp<4><<<grid, kCCDThreads, 0, st>>>(a);
             else if (mode == 1) k_ccd_warp<1><<<grid, kCCDThreads, 0, st>>>(a);
             else k_ccd<<<grid, kCCDThreads, 0, st>>>(a);
             RIGC_CUDA(cudaGetLastError());

@@ -2,7 +2,8 @@
 tests/golden/make_reference_fixtures.py, oracle results stored with them):
 per-query and per-candidate times of impact bit-exact, the wrecking-ball
 scene's candidate set identical, with one search per lane (k_ccd) and one
-per warp (k_ccd_warp, as compiled and fitted to 4 blocks per SM) alike."""
+per warp (k_ccd_warp, as compiled and fitted to 4 or 5 blocks per SM)
+alike."""
 import os
 
 import numpy as np
@@ -13,7 +14,7 @@ from test_reference_fixtures import queries, scene_fixture
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("warp", [0, 1, 2])
+@pytest.mark.parametrize("warp", [0, 1, 2, 3])
 def test_reference_queries_gpu(warp):
     """All 403 queries in one context, candidates given explicitly."""
     import make_reference_fixtures as M
@@ -55,7 +56,7 @@ def test_reference_queries_gpu(warp):
     assert toi == expect.min()
 
 
-@pytest.mark.parametrize("warp", [0, 1, 2])
+@pytest.mark.parametrize("warp", [0, 1, 2, 3])
 def test_wrecking_ball_scene_gpu(warp):
     import make_reference_fixtures as M
     import rigc
