@@ -1319,27 +1319,33 @@ k_ccd_warp(CCDArgs a)
         }
         cboxes++;
         if (lane == 0) tot_boxes++;
-        // f(box) contains zero: lanes 0..2 take coordinate c of the four
-        // vertices and evaluate the distance function's coordinate c
+        // f(box) contains zero: lanes 0..5 take coordinate c = lane % 3 of
+        // the four vertices; lanes c and c + 3 evaluate the two halves of
+        // the distance function's coordinate c (EE: the two edge points; FV:
+        // the two face-edge terms), lane c combines them (the expressions
+        // and operand order of f_zero)
         Itv P[4];
 #pragma unroll
         for (int v = 0; v < 4; v++) {
             P[v].lo = __shfl_sync(0xffffffffu, pcrd.lo, 3 * v + crd);
             P[v].hi = __shfl_sync(0xffffffffu, pcrd.hi, 3 * v + crd);
         }
+        const bool h1 = lane >= 3;  // the second half (lanes 3..5)
+        const Itv al { x.a0, x.a1 }, be { x.b0, x.b1 };
+        const Itv& pw = h1 ? be : al;
+        Itv part;
+        if (fv) {
+            part = imul_nonneg(isub(h1 ? P[3] : P[2], P[1]), pw);
+        } else {
+            const Itv& q0 = h1 ? P[2] : P[0];
+            part = iadd(imul_nonneg(isub(h1 ? P[3] : P[1], q0), pw), q0);
+        }
+        Itv other;
+        other.lo = __shfl_sync(0xffffffffu, part.lo, (lane + 3) & 31);
+        other.hi = __shfl_sync(0xffffffffu, part.hi, (lane + 3) & 31);
         bool zin = true;
         if (lane < 3) {
-            const Itv al { x.a0, x.a1 }, be { x.b0, x.b1 };
-            Itv y;
-            if (fv) {
-                Itv fp = iadd(iadd(imul_nonneg(isub(P[2], P[1]), al), imul_nonneg(isub(P[3], P[1]), be)),
-                              P[1]);
-                y = isub(P[0], fp);
-            } else {
-                Itv ea = iadd(imul_nonneg(isub(P[1], P[0]), al), P[0]);
-                Itv eb = iadd(imul_nonneg(isub(P[3], P[2]), be), P[2]);
-                y = isub(ea, eb);
-            }
+            const Itv y = fv ? isub(P[0], iadd(iadd(part, other), P[1])) : isub(part, other);
             zin = zero_in(y);
         }
         if (!__all_sync(0xffffffffu, zin)) continue;
