@@ -40,6 +40,7 @@
 
 #include "common.cuh"
 #include "interval.cuh"
+#include "search_tree.cuh"
 
 namespace rigc {
 
@@ -576,72 +577,8 @@ __device__ __forceinline__ void record_min(const CCDArgs& a, const Query& q, dou
     atomicMin(a.gmin, b);
 }
 
-// Search tree nodes.  Every box of a candidate's search is dyadic: per
-// dimension (t, alpha, beta) it is [i 2^-l, (i + 1) 2^-l] for a level l and
-// an index i, because the root is [0, 1]^3 and a split halves one dimension
-// at its midpoint, which is exact while l <= kMaxLevel.  So a box is a node
-// (levels, indices, depth = number of splits from the root), and the
-// depth-first search needs no box stack: the boxes a stack would hold are
-// the upper children of the depths at which the current path went to the
-// lower child.  A lane keeps the current node, a 128-bit mask of the depths
-// whose upper child is still pending, and two masks recording which depths
-// split t and which split alpha (the others split beta); a pending box is
-// rebuilt from the current node by undoing the splits below its depth.
-// Popping the deepest pending depth visits boxes in the order of a stack
-// that pushes the upper half first; the shallowest pending depth is the
-// stack's bottom, the box a work-sharing lane takes.
-typedef unsigned __int128 u128;
-constexpr int kMaxDepth = 120;  // splits along one path (mask bits)
-constexpr int kMaxLevel = 52;   // splits along one dimension (exact bounds)
-
-struct Node {
-    int lv[3];
-    unsigned long long ix[3];
-    int depth;
-};
-
-__device__ __forceinline__ u128 bit128(int k) { return (u128)1 << k; }
-
-__device__ __forceinline__ int popc128(u128 m)
-{
-    return __popcll((unsigned long long)m) + __popcll((unsigned long long)(m >> 64));
-}
-
-__device__ __forceinline__ int msb128(u128 m)
-{
-    const unsigned long long h = (unsigned long long)(m >> 64);
-    return h ? 127 - __clzll((long long)h) : 63 - __clzll((long long)(unsigned long long)m);
-}
-
-__device__ __forceinline__ int lsb128(u128 m)
-{
-    const unsigned long long l = (unsigned long long)m;
-    return l ? __ffsll((long long)l) - 1 : 63 + __ffsll((long long)(unsigned long long)(m >> 64));
-}
-
-// mask of the depths [lo, hi), hi <= kMaxDepth + 1
-__device__ __forceinline__ u128 range128(int lo, int hi) { return (bit128(hi) - 1) & ~(bit128(lo) - 1); }
-
-// i 2^-l for i <= 2^52, l <= kMaxLevel, assembled from its bits with integer
-// operations (off the FP64 pipe): exponent from the leading one, mantissa
-// from the bits below it
-__device__ __forceinline__ double dyadic(unsigned long long i, int l)
-{
-    const int e = 63 - __clzll((long long)(i | 1ull));  // i in [2^e, 2^(e + 1))
-    const unsigned long long m = (i << (52 - e)) & 0xfffffffffffffull;
-    const double v = __longlong_as_double((long long)(((unsigned long long)(1023 + e - l) << 52) | m));
-    return i ? v : 0.0;
-}
-
-// The box widths of the root finder, sub_up(hi, lo): the exact difference
-// 2^-l stepped one ulp up (the bit pattern of 2^-l plus one)
-__device__ __forceinline__ void node_widths(const Node& c, double w[3])
-{
-#pragma unroll
-    for (int k = 0; k < 3; k++)
-        w[k] = __longlong_as_double((long long)(((unsigned long long)(1023 - c.lv[k]) << 52) + 1ull));
-}
-
+// Search tree nodes and the path-encoded depth-first search: see
+// search_tree.cuh.  The boxes of nodes, and the root finder's split rule.
 __device__ __forceinline__ Box node_box(const Node& c)
 {
     return Box { dyadic(c.ix[0], c.lv[0]), dyadic(c.ix[0] + 1, c.lv[0]),
@@ -661,35 +598,6 @@ __device__ __forceinline__ int split_dim(const double w[3], const double tol[3],
             && (split == -1 || !le_nn(RMUL(w[d], tol[split]), RMUL(w[split], tol[d]))))
             split = d;
     return split;
-}
-
-// record that depth k splits dimension s
-__device__ __forceinline__ void record_split(u128& mt, u128& ma, int k, int s)
-{
-    const u128 b = bit128(k);
-    mt = s == 0 ? (mt | b) : (mt & ~b);
-    ma = s == 1 ? (ma | b) : (ma & ~b);
-}
-
-// The upper child of c's ancestor at depth j, where c's path went to the
-// lower child: c's node at depth j + 1 with the splits of depths
-// j + 1 .. c.depth - 1 undone and its last index bit set.
-__device__ __forceinline__ Node pending_node(const Node& c, u128 mt, u128 ma, int j)
-{
-    const u128 r = range128(j + 1, c.depth);
-    const int ct = popc128(mt & r), ca = popc128(ma & r);
-    const int cb = c.depth - j - 1 - ct - ca;
-    Node g;
-    g.lv[0] = c.lv[0] - ct;
-    g.lv[1] = c.lv[1] - ca;
-    g.lv[2] = c.lv[2] - cb;
-    g.ix[0] = c.ix[0] >> ct;
-    g.ix[1] = c.ix[1] >> ca;
-    g.ix[2] = c.ix[2] >> cb;
-    const int s = (mt & bit128(j)) ? 0 : ((ma & bit128(j)) ? 1 : 2);
-    g.ix[s] |= 1ull;
-    g.depth = j + 1;
-    return g;
 }
 
 // The node of the candidate's subdivision tree at depth d reached by the
@@ -994,11 +902,7 @@ k_ccd(CCDArgs a)
             continue;
         }
         // go to the lower half; the upper half is pending at this depth
-        record_split(mt, ma, cn.depth, split);
-        pend_hi |= bit128(cn.depth);
-        cn.lv[split]++;
-        cn.ix[split] <<= 1;
-        cn.depth++;
+        descend(cn, pend_hi, mt, ma, split);
         has_cn = true;
     }
     // warp-aggregated counters
@@ -1373,11 +1277,7 @@ k_ccd_warp(CCDArgs a)
             status = RIGC_ERR_QUEUE_OVERFLOW;
             continue;
         }
-        record_split(mt, ma, cn.depth, split);
-        pend_hi |= bit128(cn.depth);
-        cn.lv[split]++;
-        cn.ix[split] <<= 1;
-        cn.depth++;
+        descend(cn, pend_hi, mt, ma, split);
         has_cn = true;
     }
     if (lane == 0) {
