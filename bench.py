@@ -48,9 +48,9 @@ CCD_BYTES_PER_PAIR = 304        # ids + 4 rest vertices + 4 poses + toi
 # peak) and lane-level GFLOP/s (dadd + dmul + 2 dfma over the launch).
 K_CCD_DRAM_BYTES_PER_CANDIDATE = {
     "k_ccd": (42209536 + 14743808 + 310226176 + 1279232) / 132242,
-    "k_ccd_warp": (17837312 + 2597632 + 512000 + 15804928 + 1792) / 132242}
+    "k_ccd_warp<1>": (17837312 + 2597632 + 512000 + 15804928 + 1792) / 132242}
 K_CCD_FP64 = {"k_ccd": {"pipe_active": 0.233, "lane_gflops": 53.0},
-              "k_ccd_warp": {"pipe_active": 0.496, "lane_gflops": 98.4}}
+              "k_ccd_warp<1>": {"pipe_active": 0.496, "lane_gflops": 98.4}}
 BARRIER_BYTES_PER_CONSTRAINT = 1456
 
 
@@ -66,6 +66,10 @@ def parse():
     ap.add_argument("--no-sim", action="store_true", help="skip the steps/s measurement")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the built-in launch shapes for the headline pass")
+    ap.add_argument("--ccd-warp", type=int, default=None,
+                    help="CCD kernel variant for the headline pass instead of the autotuner's "
+                         "(rigc_set_tune's ccd_warp: 0 per lane, 1 per warp, 2 / 3 per warp "
+                         "fitted to 4 / 5 blocks per SM)")
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the per-configuration pass rates")
     ap.add_argument("--no-adjoint", action="store_true",
@@ -147,6 +151,21 @@ def measured_peaks():
             d = json.load(f)
         return float(d.get("hbm_gbs", 6800.0)), "measured"
     return 6800.0, "fallback"
+
+
+def fp64_peak():
+    """The device's FP64 issue rate measured by the library's own DFMA / DADD
+    chains (rigc_fp64_throughput): all lanes of every warp, then 16 and 1
+    active lanes per warp, which shows whether a warp instruction costs the
+    FP64 unit the same time whatever its active lanes."""
+    import rigc
+
+    out = {}
+    for op, lanes in (("dfma", 32), ("dfma", 16), ("dfma", 1), ("dadd", 32)):
+        r = rigc.fp64_throughput(op, lanes, 4096)
+        out[f"{op}_{lanes}"] = {"gflops": r["gflops"], "warp_inst_per_s": r["warp_inst_per_s"],
+                                "ms": r["ms"]}
+    return out
 
 
 def cpu_baseline(sc, x0, x1, dhat, budget_s=15.0):
@@ -592,7 +611,12 @@ def main():
     n_cons = len(cs["type"])
     # launch shapes chosen by the autotuner on this workload (part of the
     # framework's set-up, before the warm-up)
-    tune = ctx.autotune(x0d, x1d, dhat) if not args.no_autotune else None
+    tune = None
+    if args.ccd_warp is not None:
+        ctx.set_tune(0, 0, 0, -1, -1, args.ccd_warp)
+        tune = {"ccd_warp": args.ccd_warp, "forced": True}
+    elif not args.no_autotune:
+        tune = ctx.autotune(x0d, x1d, dhat)
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -665,7 +689,9 @@ def main():
     peak, peak_kind = measured_peaks()
     # the CCD kernel the context launches: one search per warp unless tuned
     # to one per lane
-    ccd_kernel = "k_ccd" if (tune and tune.get("ccd_warp") == 0) else "k_ccd_warp"
+    ccd_mode = tune.get("ccd_warp", -1) if tune else -1
+    ccd_kernel = {0: "k_ccd", 2: "k_ccd_warp<4>", 3: "k_ccd_warp<5>"}.get(ccd_mode, "k_ccd_warp<1>")
+    fp64 = fp64_peak() if rank == 0 else None
     ccd_bytes = CCD_BYTES_PER_PAIR * n_ccd
     achieved = ccd_bytes / t_ccd / 1e9
     line = {
@@ -683,17 +709,19 @@ def main():
         "ccd_pairs_per_s": n_ccd / t_ccd, "barrier_constraints_per_s": n_cons / t_bar,
         "roofline": {"bound": "hbm", "kernel": ccd_kernel, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": K_CCD_DRAM_BYTES_PER_CANDIDATE[ccd_kernel] * n_ccd,
+                     "traffic": (K_CCD_DRAM_BYTES_PER_CANDIDATE[ccd_kernel] * n_ccd
+                                 if ccd_kernel in K_CCD_DRAM_BYTES_PER_CANDIDATE else None),
                      "traffic_source": "ncu capture of the 200-icosphere pile scaled by candidates",
                      "peak_source": peak_kind,
                      "note": "FP64-issue-bound (an FP64 warp instruction holds its SM "
                              "sub-partition's FP64 unit 64 cycles on GB300), not HBM: algorithmic "
                              "bytes are 304 B per candidate",
-                     "fp64": dict(K_CCD_FP64[ccd_kernel], nominal_gflops=1250.0,
+                     "fp64": dict(K_CCD_FP64.get(ccd_kernel, {}), nominal_gflops=1250.0,
                                   source="ncu capture of the 200-icosphere pile")},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "clocks": clk.summary(),
+        "fp64_peak": fp64,
         "gpu_launches": launches,
         "autotune": tune,
     }

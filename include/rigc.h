@@ -205,6 +205,29 @@ int rigc_compute_earliest_toi(rigc_ctx* ctx, const double* x0,
 int rigc_construct_constraint_set(rigc_ctx* ctx, const double* x, double dhat,
                                   double dmin, rigc_constraints* out);
 
+/* ---- minimum distance: DistanceBarrierRBProblem::compute_min_distance(x)
+ * (src/problems/distance_barrier_rb_problem.cpp:1583-1589) over
+ * DistanceBarrierConstraint::compute_minimum_distance
+ * (src/opt/distance_barrier_constraint.cpp:308-323), called by
+ * IPCSolver::init_solve / post_step_update (src/solvers/ipc_solver.cpp:36-89):
+ * the constraint set at x (device poses), the smallest constraint distance
+ * over it; -1 when the set is empty, as the reference returns for an
+ * infinite minimum.  Leaves that constraint set in the context. */
+int rigc_min_distance(rigc_ctx* ctx, const double* x, double dhat, double dmin,
+                      double* min_distance);
+
+/* ---- intersection check: RigidBodyProblem::detect_intersections
+ * (src/physics/rigid_body_problem.cpp:289-360), run at the end of every
+ * time step (SimState::simulation_step, src/SimState.cpp:374-395, logs
+ * has_intersections): edge-face candidates of the bodies
+ * at x (device poses; close bodies and element boxes with no inflation) and
+ * a segment-triangle crossing test on each.  Writes the number of crossing
+ * (edge, face) pairs; the poses are intersection-free when it is 0.  The
+ * segment-triangle test is the orientation-based one: the edge's endpoints
+ * on different sides of the face's plane (coplanar pairs do not count) and
+ * the edge's line inside the face. */
+int rigc_detect_intersections(rigc_ctx* ctx, const double* x, int64_t* num_crossings);
+
 /* Replace the context's constraint set with host arrays (same layout as
  * rigc_constraints). */
 int rigc_set_constraints(rigc_ctx* ctx, int64_t num, const int32_t* type,
@@ -297,7 +320,7 @@ int rigc_friction_local_terms(rigc_ctx* ctx, const double* x,
  * solver (src/solvers/ipc_solver.cpp, src/solvers/newton_solver.cpp) for the
  * default settings: implicit Euler, velocity convergence, one friction
  * lagging iteration, no kinematic bodies.  Every term, the CCD line-search
- * filter and the Newton linear solve (a dense LDL^T for at most 384 free
+ * filter and the Newton linear solve (a dense LDL^T for at most 768 free
  * dofs, else block-Jacobi preconditioned conjugate gradients on the
  * block-sparse Hessian, relative residual 1e-12) run on the device; the solver's scalar decisions run on the host.  Field names follow
  * the reference's JSON settings; average_mass and world_bbox_diagonal are the
@@ -381,7 +404,10 @@ int rigc_sim_scene_params(rigc_ctx* ctx, const double* average_mass,
  * after the other (median of three runs each), over the continuous
  * candidates of x0 -> x1 and the constraint set at x0 (device poses), and
  * keeps the fastest in the context for every later call.  rigc_set_tune
- * sets them directly (0: the built-in choice). */
+ * sets them directly: for ccd_blocks_per_sm, cache_slots_per_body and
+ * barrier_per_warp 0 is the built-in choice; for ccd_seeds_log2,
+ * ccd_hand_off and ccd_warp the built-in choice is -1 (0 means something
+ * else there: one seed, never hand off, one search per lane). */
 typedef struct rigc_tune_report {
     int32_t ccd_blocks_per_sm, cache_slots_per_body, barrier_per_warp;
     double ccd_ms_default, ccd_ms, barrier_ms_default, barrier_ms;
@@ -442,6 +468,17 @@ int rigc_narrow_phase_host(rigc_ctx* ctx, const double* x0_host,
                            int32_t* col_host, double* val_host,
                            int64_t nnzb_cap, int64_t* nnzb_host);
 
+/* ---- FP64 issue throughput (new: a measurement of the part, for the
+ * rooflines of the FP64-bound kernels).  Runs independent chains of DFMA
+ * (op 0) or DADD (op 1) on every resident warp of the device, with only
+ * active_lanes lanes of each warp working, iters x 8 instructions per
+ * thread, timed with CUDA events on the legacy default stream (one warm-up
+ * launch first).  Outputs: elapsed ms, warp-level FP64 instructions issued
+ * and lane-level FLOPs (2 per DFMA).  Allocates and frees a small device
+ * buffer; synchronises the device. */
+int rigc_fp64_throughput(int32_t op, int32_t active_lanes, int32_t iters, double* ms,
+                         double* warp_instructions, double* lane_flops);
+
 /* ---- per-constraint barrier terms without any device allocation.
  * No counterpart in the reference: the reference allocates freely on the
  * host.  This entry point is for callers that must not allocate device
@@ -460,6 +497,11 @@ int rigc_narrow_phase_host(rigc_ctx* ctx, const double* x0_host,
  * bodies x 2, weight, eps_x).  Outputs (device, any may be NULL): energy
  * (num_constraints), grad (x 12), hess (x 144).  flags as rigc_barrier_term.
  * Returns RIGC_ERR_TOO_LARGE when num_bodies > RIGC_NOALLOC_MAX_BODIES.
+ * Preconditions: 0 <= type <= 3, every body index in [0, num_bodies), every
+ * vertex index the type uses in [0, num_vertices).  The arrays are on the
+ * device, so the kernel checks them: a constraint that breaks one gets NaN
+ * energy, gradient and Hessian and reads nothing out of range; the status
+ * returned cannot report it (that would need a synchronisation).
  *
  * The first call on a device looks up the device address of the working
  * array (a one-time set-up per device); make that first call before any
@@ -469,7 +511,7 @@ int rigc_narrow_phase_host(rigc_ctx* ctx, const double* x0_host,
  * each call overwrites every frame it reads. */
 #define RIGC_NOALLOC_MAX_BODIES 4096
 int rigc_barrier_local_terms_noalloc(
-    const double* rest_vertices, int32_t num_bodies, const double* x,
+    const double* rest_vertices, int64_t num_vertices, int32_t num_bodies, const double* x,
     int64_t num_constraints, const int32_t* type, const int32_t* verts,
     const int32_t* bodies, const double* weight, const double* eps_x,
     double dhat, double dmin, int flags, double* energy, double* grad,

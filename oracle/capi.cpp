@@ -211,6 +211,26 @@ int orc_constraint_set(
     return 0;
 }
 
+// DistanceBarrierRBProblem::compute_min_distance(x)
+// (src/problems/distance_barrier_rb_problem.cpp:1583-1589) over
+// DistanceBarrierConstraint::compute_minimum_distance
+// (src/opt/distance_barrier_constraint.cpp:308-323): the constraint set at x
+// (discrete candidates inflated by (dhat + dmin) / 2), the smallest squared
+// distance over it, its square root; -1 when the set is empty.
+double orc_min_distance(void* p, const double* x, double dhat, double dmin)
+{
+    const Scene& s = static_cast<OwnedScene*>(p)->s;
+    Candidates cand;
+    detect_candidates(s, x, x, false, (dhat + dmin) / 2, false, cand);
+    std::vector<double> V;
+    world_vertices(s, x, V);
+    std::vector<Constraint> cs;
+    construct_constraint_set(s, cand, V, dhat, dmin, cs);
+    double m = INFINITY;
+    for (const auto& c : cs) m = std::min(m, constraint_sqdist(c, V));
+    return std::isfinite(m) ? std::sqrt(m) : -1.0;
+}
+
 void orc_local_terms(
     void* p, const double* x, long long n, const int* types, const int* verts,
     const int* prims, const int* bodies, const double* weight,

@@ -212,6 +212,8 @@ double ee_cross_sqnorm(const double* ea0, const double* ea1, const double* eb0, 
 
 // barrier b(d; s) of ipc-toolkit (log barrier of the squared distance)
 double barrier(double d, double s);
+// squared distance of one constraint (the distance its barrier uses)
+double constraint_sqdist(const Constraint& c, const std::vector<double>& V);
 
 // candidates (ipc-toolkit Candidates)
 struct Candidates {

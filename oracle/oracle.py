@@ -54,6 +54,8 @@ def lib():
         L.orc_constraint_set.argtypes = [C.c_void_p, _d, _i, C.c_longlong, _i, C.c_longlong,
                                          C.c_double, C.c_double, _i, _i, _i, _i, _d, _d,
                                          C.c_longlong, _ll]
+        L.orc_min_distance.restype = C.c_double
+        L.orc_min_distance.argtypes = [C.c_void_p, _d, C.c_double, C.c_double]
         L.orc_local_terms.argtypes = [C.c_void_p, _d, C.c_longlong, _i, _i, _i, _i, _d, _d,
                                       C.c_double, C.c_double, C.c_int, _d, _d, _d]
         L.orc_friction_constraints.argtypes = [C.c_void_p, _d, C.c_longlong, _i, _i, _i, _i, _d,
@@ -213,6 +215,11 @@ class OracleScene:
         assert rc == 0
         m = n.value
         return Constraints(types[:m], verts[:m], prims[:m], bodies[:m], w[:m], eps[:m])
+
+    def min_distance(self, x, dhat, dmin=0.0):
+        """compute_min_distance(x): the smallest constraint distance at x, -1
+        when the constraint set is empty."""
+        return lib().orc_min_distance(self.h, _p(_dd(x), _d), dhat, dmin)
 
     def local_terms(self, x, cs: Constraints, dhat, dmin=0.0, project=True):
         x = _dd(x)

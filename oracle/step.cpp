@@ -42,6 +42,8 @@ double barrier_hessian_d(double d, double s)
     return (sd + 2) * sd - 2 * std::log(d / s) - 3;
 }
 
+} // namespace
+
 // squared distance of one constraint (the distance its barrier uses)
 double constraint_sqdist(const Constraint& c, const std::vector<double>& V)
 {
@@ -53,6 +55,8 @@ double constraint_sqdist(const Constraint& c, const std::vector<double>& V)
     default: return point_plane_sqdist(P(0), P(1), P(2), P(3));
     }
 }
+
+namespace {
 
 // dense LDL^T (no pivoting) of a symmetric matrix; false on a zero pivot
 bool ldlt_solve(int n, std::vector<double> A, const std::vector<double>& b,

@@ -33,6 +33,8 @@ UNITS = {
     "friction.cu": ["--fmad=true"],
     "step.cu": ["--fmad=false"],
     "autotune.cu": ["--fmad=false"],
+    "fp64_peak.cu": ["--fmad=false"],
+    "intersect.cu": ["--fmad=false"],
 }
 
 

@@ -1,4 +1,5 @@
 // C ABI of the rigc library (declared in include/rigc.h).
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <atomic>
@@ -124,7 +125,7 @@ template <class T> static int upload(T*& dst, const T* src, size_t n)
 
 static void free_scene(Scene& s)
 {
-    void* ptrs[] = { s.rest, s.edges, s.faces, s.f2e, s.bvs, s.bes, s.bfs, s.group,
+    void* ptrs[] = { s.rest, s.edges, s.faces, s.f2e, s.bvs, s.bes, s.bfs, s.group, s.grank,
                      s.type, s.rmax, s.vbody, s.ebody, s.fbody, s.edge_len, s.bscene,
                      s.scene_bstart };
     for (void* p : ptrs)
@@ -143,7 +144,10 @@ static void release_all(Ctx* c)
                        &c->frame_vals, &c->fric.type, &c->fric.verts, &c->fric.bodies,
                        &c->fric.coef, &c->fric.v0c, &c->fric.V0, &c->fric.c_energy,
                        &c->fric.c_grad, &c->fric.c_blocks, &c->fric.grad, &c->fric.row_ptr,
-                       &c->fric.col, &c->fric.val, &c->scene_toi, &c->scene_energy };
+                       &c->fric.col, &c->fric.val, &c->scene_toi, &c->scene_energy,
+                       &c->bp_misc, &c->bp_frames, &c->bp_deeper, &c->bp_sig, &c->bp_ec0,
+                       &c->bp_eext, &c->bp_f32, &c->bp_cnt, &c->md_V, &c->md_rot,
+                       &c->md_out, &c->isect.ee, &c->isect.fv };
     for (DevBuf* b : bufs) b->release();
     for (auto& b : c->scratch) b.release();
     sim_release(*c);
@@ -262,6 +266,19 @@ static int ctx_create(const rigc_scene_desc* d, int num_scenes, const int32_t* b
     chk(upload(s.bes, d->body_edge_start, (size_t)nb + 1));
     chk(upload(s.bfs, d->body_face_start, (size_t)nb + 1));
     chk(upload(s.group, d->group_ids, (size_t)nb));
+    {
+        // dense ranks of the group ids: the hash grid keys items by group
+        std::vector<int> ids(d->group_ids, d->group_ids + nb);
+        std::sort(ids.begin(), ids.end());
+        ids.erase(std::unique(ids.begin(), ids.end()), ids.end());
+        std::vector<int> rank(nb);
+        for (int b = 0; b < nb; b++)
+            rank[b] = (int)(std::lower_bound(ids.begin(), ids.end(), d->group_ids[b]) - ids.begin());
+        int bits = 1;
+        while (bits < 31 && ((int64_t)1 << bits) < (int64_t)ids.size()) bits++;
+        s.group_bits = bits;
+        chk(upload(s.grank, rank.data(), (size_t)nb));
+    }
     chk(upload(s.type, d->body_types, (size_t)nb));
     chk(upload(s.rmax, d->r_max, (size_t)nb));
     chk(upload(s.vbody, vbody.data(), (size_t)nv));

@@ -71,7 +71,30 @@ struct BarrierArgs {
     double* grad;     // n x 12
     double* blocks;   // n x 4 x 36 (blocks (0,0) (0,1) (1,0) (1,1))
     double* hess;     // optional n x 144 (full local Hessian)
+    // index limits checked on the device when check_nv >= 0 (callers whose
+    // constraint arrays were not validated on the host): a constraint with a
+    // type, vertex or body index out of range reads nothing and gets NaN
+    // outputs
+    int check_nb = 0;
+    int64_t check_nv = -1;
 };
+
+// the index check of a constraint (see BarrierArgs::check_nv)
+static __device__ bool constraint_in_range(const BarrierArgs& a, int64_t ci)
+{
+    const int type = a.ctype[ci];
+    if (type < 0 || type > 3) return false;
+    const int nvc = type == 0 ? 2 : (type == 1 ? 3 : 4);
+    for (int i = 0; i < 2; i++) {
+        const int b = a.cbodies[2 * ci + i];
+        if (b < 0 || b >= a.check_nb) return false;
+    }
+    for (int i = 0; i < nvc; i++) {
+        const int v = a.cverts[4 * ci + i];
+        if (v < 0 || (int64_t)v >= a.check_nv) return false;
+    }
+    return true;
+}
 
 __device__ __forceinline__ int local_body_of(int type, int i)
 {
@@ -288,6 +311,19 @@ static __device__ __noinline__ bool ee_endpoint_build(const BarrierArgs& a, int6
 // write, false when every output of the constraint is already written.
 static __device__ __noinline__ bool barrier_build(const BarrierArgs& a, int64_t ci, SMat H)
 {
+    if (a.check_nv >= 0 && !constraint_in_range(a, ci)) {
+        const double nan = __longlong_as_double(0x7ff8000000000000ll);
+        if (a.energy) a.energy[ci] = nan;
+        if (a.grad)
+            for (int k = 0; k < 12; k++) a.grad[ci * 12 + k] = nan;
+        if (a.flags & RIGC_HESS) {
+            if (a.blocks)
+                for (int k = 0; k < 144; k++) a.blocks[ci * 144 + k] = nan;
+            if (a.hess)
+                for (int k = 0; k < 144; k++) a.hess[ci * 144 + k] = nan;
+        }
+        return false;
+    }
     const int type = a.ctype[ci];
     const int nvc = type == 0 ? 2 : (type == 1 ? 3 : 4);
     const double weight = a.cweight[ci];
@@ -636,7 +672,7 @@ int launch_barrier_local(Ctx& c, const double* x, double dhat, double dmin, int 
 // Frames and per-constraint terms with every buffer supplied by the caller
 // (the frames array holds 96 doubles per body); used by the entry point that
 // allocates nothing.
-int launch_barrier_local_raw(const double* rest, int nb, const double* x, int64_t n,
+int launch_barrier_local_raw(const double* rest, int64_t nv, int nb, const double* x, int64_t n,
                              const int* ctype, const int* cverts, const int* cbodies,
                              const double* cweight, const double* ceps, double dhat, double dmin,
                              int flags, double* frames, double* energy, double* grad,
@@ -664,6 +700,8 @@ int launch_barrier_local_raw(const double* rest, int nb, const double* x, int64_
     a.grad = grad;
     a.blocks = nullptr;
     a.hess = hess;
+    a.check_nb = nb;
+    a.check_nv = nv;
     const int pw = local_terms_per_warp(n);
     RIGC_COUNT_LAUNCH();
     k_barrier_local<<<grid_for(n, pw), kBarrierTPB, local_terms_smem_bytes(), stream>>>(a, pw);

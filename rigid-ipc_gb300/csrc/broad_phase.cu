@@ -9,16 +9,30 @@
 //  2. vertex boxes: continuous -- interval positions over t in [0, 1] with one
 //     forced bisection, bisected further while a body's vertices leave the
 //     padded scene box (RigidBodyHashGrid::compute_vertices_intervals,
-//     src/ccd/rigid/rigid_body_hash_grid.cpp:164-246), one CUDA block per
-//     body; discrete -- the world vertex +- inflation.  Edge and face boxes are
-//     unions of their vertex boxes (:265-344);
+//     src/ccd/rigid/rigid_body_hash_grid.cpp:164-246): a thread per vertex
+//     over the two forced halves, and one CUDA block per body for the bodies
+//     that need deeper bisection; discrete -- the world vertex +- inflation.
+//     Edge and face boxes are unions of their vertex boxes (:265-344);
 //  3. pairs: ipc-toolkit's HashGrid reports element pairs that share a cell,
 //     belong to different groups and whose boxes overlap (center /
-//     half-extent test).  Here elements are binned into cells (radix sort of
-//     (cell, element) items), each pair is reported once, in the first cell
-//     both elements cover, and elements spanning more than kLargeCells cells
-//     are tested against all elements instead of being binned.  The output is
-//     the same set, sorted: ee as (edge0 < edge1), fv as (face, vertex).
+//     half-extent test).  Because the boxes overlap, that set does not depend
+//     on the cell layout, which leaves the grid free:
+//     * the grid (origin, cell size) is computed on the device from the
+//       element boxes;
+//     * a cell filter marks every cell that elements of two or more groups
+//       cover (one int per cell, or per hashed slot of cells: a collision
+//       only marks more cells); only marked cells are binned, so cells
+//       inside one body's surface -- most of a contact scene -- cost nothing;
+//     * items are sorted by (scene, cell, group, first-cell bits); an item
+//       pairs only with items of later groups of its cell, and a pair is
+//       reported in the first cell both elements cover (the cell where each
+//       axis starts one of the two ranges: three bits per item);
+//     * a conservative single-precision box test (outward-rounded floats)
+//       rejects most pairs before the double-precision overlap test;
+//     * elements spanning more than kLargeCells cells are tested against all
+//       elements of their scene instead of being binned.
+//     The output is the same set, sorted: ee as (edge0 < edge1), fv as
+//     (face, vertex).
 #include "common.cuh"
 #include "interval.cuh"
 #include "sort.cuh"
@@ -26,8 +40,6 @@
 namespace rigc {
 
 constexpr int kLargeCells = 64;
-// item counts up to which cell pairs are enumerated by a warp per item
-constexpr int64_t kWarpPairItems = 1 << 16;
 
 // ---------------------------------------------------------------------------
 // 1. body boxes and inclusion
@@ -147,21 +159,74 @@ __global__ void k_scene_box(const double* __restrict__ box, const int* __restric
 // 2. vertex boxes
 
 constexpr int kVBThreads = 256;
-constexpr int kMaxTNodes = 40;
+constexpr int kHalfFrame = 24;                   // doubles per interval frame: R (9 intervals), p (3)
+constexpr int kVBBatch = 32;                     // time nodes evaluated together
+constexpr int kMaxTNodes = 17 * 2 * kVBBatch;    // pending nodes (see below)
+constexpr int kMaxTDepth = 16;                   // bisection stops at this depth
 
-// one block per included body; vbox holds lo[3], hi[3] per vertex
+// interval frame (R as 9 intervals, p as 3) of body b over the time
+// interval [tl, th]: the interpolated pose of PoseI::interpolate
+// (src/physics/pose.tpp:142-148) through the rotation-vector map
+__device__ void body_time_frame(const double* __restrict__ x0, const double* __restrict__ x1, int b,
+                                double tl, double th, double* __restrict__ out)
+{
+    const Itv t { tl, th };
+    Itv r[3], p[3];
+    for (int k = 0; k < 3; k++) {
+        double a = x0[6 * b + k], c = x1[6 * b + k];
+        p[k] = iadd(imul(Itv { sub_dn(c, a), sub_up(c, a) }, t), pt(a));
+        double ar = x0[6 * b + 3 + k], cr = x1[6 * b + 3 + k];
+        r[k] = iadd(imul(Itv { sub_dn(cr, ar), sub_up(cr, ar) }, t), pt(ar));
+    }
+    Itv R[9];
+    irotation(r, R);
+    for (int k = 0; k < 9; k++) {
+        out[2 * k] = R[k].lo;
+        out[2 * k + 1] = R[k].hi;
+    }
+    for (int k = 0; k < 3; k++) {
+        out[18 + 2 * k] = p[k].lo;
+        out[19 + 2 * k] = p[k].hi;
+    }
+}
+
+__device__ __forceinline__ void vertex_at_frame(const double* f, const double rv[3], Itv w[3])
+{
+    Itv R[9], p[3];
+    for (int k = 0; k < 9; k++) R[k] = Itv { f[2 * k], f[2 * k + 1] };
+    for (int k = 0; k < 3; k++) p[k] = Itv { f[18 + 2 * k], f[19 + 2 * k] };
+    iworld_vertex(R, p, rv, w);
+}
+
+// The whole bisection of RigidBodyHashGrid::compute_vertices_intervals for
+// one body per block: block b handles body b when it is included and
+// k_vertex_boxes_half flagged it (a vertex of one of the forced halves left
+// the padded scene box).  A time node is accepted when every vertex fits
+// the padded scene box (or at depth 16), else both halves are visited; the
+// result per vertex is the hull over the accepted nodes, which does not
+// depend on the order nodes are visited.  So nodes are taken from the stack
+// kVBBatch at a time: warp 0 computes their frames in parallel (one interval
+// rotation is a long chain of dependent FP64 operations), then the block
+// checks and hulls every (node, vertex) pair.  Each round pops up to
+// kVBBatch nodes and pushes at most twice as many one level deeper, so the
+// stack never holds more than 2 kVBBatch nodes per depth.
+// vbox holds lo[3], hi[3] per vertex.
 __global__ void __launch_bounds__(kVBThreads)
 k_vertex_boxes_cont(const double* __restrict__ x0, const double* __restrict__ x1,
                     const double* __restrict__ rest, const int* __restrict__ bvs,
-                    const int* __restrict__ body_list, const double* __restrict__ domain,
-                    double infl, double* __restrict__ vbox, char* __restrict__ vin)
+                    const int* __restrict__ body_in, const int* __restrict__ deeper,
+                    const double* __restrict__ domain, double infl, double* __restrict__ vbox,
+                    char* __restrict__ vin)
 {
     __shared__ double st_lo[kMaxTNodes], st_hi[kMaxTNodes];
     __shared__ int st_depth[kMaxTNodes];
-    __shared__ int sp;
-    __shared__ Itv sR[9], sp3[3];
-    const int b = body_list[blockIdx.x];
-    const int v0 = bvs[b], v1 = bvs[b + 1];
+    __shared__ int sp, nbat;
+    __shared__ double b_lo[kVBBatch], b_hi[kVBBatch];
+    __shared__ int b_depth[kVBBatch], b_fail[kVBBatch];
+    __shared__ double sF[kVBBatch][kHalfFrame];
+    const int b = blockIdx.x;
+    if (!body_in[b] || !deeper[b]) return;  // uniform over the block
+    const int v0 = bvs[b], v1 = bvs[b + 1], nvb = v1 - v0;
     double dlo[3] = { domain[0], domain[1], domain[2] }, dhi[3] = { domain[3], domain[4], domain[5] };
     // hull accumulators in the output array
     for (int v = v0 + threadIdx.x; v < v1; v += blockDim.x)
@@ -176,57 +241,63 @@ k_vertex_boxes_cont(const double* __restrict__ x0, const double* __restrict__ x1
         st_lo[sp] = m; st_hi[sp] = 1.0; st_depth[sp] = 1; sp++;
         st_lo[sp] = 0.0; st_hi[sp] = m; st_depth[sp] = 1; sp++;
     }
-    __syncthreads();
     while (true) {
         __syncthreads();
         if (sp == 0) break;
-        double tl = st_lo[sp - 1], th = st_hi[sp - 1];
-        int depth = st_depth[sp - 1];
+        // pop up to kVBBatch nodes
+        if (threadIdx.x < kVBBatch) {
+            const int nb_ = min(sp, kVBBatch);
+            if ((int)threadIdx.x < nb_) {
+                const int q = sp - nb_ + threadIdx.x;
+                b_lo[threadIdx.x] = st_lo[q];
+                b_hi[threadIdx.x] = st_hi[q];
+                b_depth[threadIdx.x] = st_depth[q];
+                b_fail[threadIdx.x] = 0;
+            }
+        }
         __syncthreads();
         if (threadIdx.x == 0) {
-            sp--;
-            Itv t { tl, th };
-            Itv r[3];
-            for (int k = 0; k < 3; k++) {
-                double a = x0[6 * b + k], c = x1[6 * b + k];
-                sp3[k] = iadd(imul(Itv { sub_dn(c, a), sub_up(c, a) }, t), pt(a));
-                double ar = x0[6 * b + 3 + k], cr = x1[6 * b + 3 + k];
-                r[k] = iadd(imul(Itv { sub_dn(cr, ar), sub_up(cr, ar) }, t), pt(ar));
-            }
-            Itv R[9];
-            irotation(r, R);
-            for (int k = 0; k < 9; k++) sR[k] = R[k];
+            nbat = min(sp, kVBBatch);
+            sp -= nbat;
         }
         __syncthreads();
-        Itv R[9], p[3];
-        for (int k = 0; k < 9; k++) R[k] = sR[k];
-        for (int k = 0; k < 3; k++) p[k] = sp3[k];
-        bool fits = true;
-        for (int v = v0 + threadIdx.x; v < v1; v += blockDim.x) {
-            double rv[3] = { rest[3 * (size_t)v], rest[3 * (size_t)v + 1], rest[3 * (size_t)v + 2] };
+        const int nq = nbat;
+        if ((int)threadIdx.x < nq)
+            body_time_frame(x0, x1, b, b_lo[threadIdx.x], b_hi[threadIdx.x], sF[threadIdx.x]);
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < nq * nvb; idx += blockDim.x) {
+            const int k = idx / nvb, v = v0 + idx % nvb;
+            const double rv[3] = { rest[3 * (size_t)v], rest[3 * (size_t)v + 1], rest[3 * (size_t)v + 2] };
             Itv w[3];
-            iworld_vertex(R, p, rv, w);
+            vertex_at_frame(sF[k], rv, w);
             for (int j = 0; j < 3; j++)
-                if (RSUB(w[j].lo, infl) < dlo[j] || RADD(w[j].hi, infl) > dhi[j]) fits = false;
+                if (RSUB(w[j].lo, infl) < dlo[j] || RADD(w[j].hi, infl) > dhi[j]) b_fail[k] = 1;
         }
-        bool all_fit = __syncthreads_and(fits) != 0;
-        if (all_fit || depth >= 16) {
-            for (int v = v0 + threadIdx.x; v < v1; v += blockDim.x) {
-                double rv[3] = { rest[3 * (size_t)v], rest[3 * (size_t)v + 1], rest[3 * (size_t)v + 2] };
+        __syncthreads();
+        // accepted nodes: hull into the vertex boxes (each thread owns its vertices)
+        for (int v = v0 + threadIdx.x; v < v1; v += blockDim.x) {
+            const double rv[3] = { rest[3 * (size_t)v], rest[3 * (size_t)v + 1], rest[3 * (size_t)v + 2] };
+            for (int k = 0; k < nq; k++) {
+                if (b_fail[k] && b_depth[k] < kMaxTDepth) continue;
                 Itv w[3];
-                iworld_vertex(R, p, rv, w);
+                vertex_at_frame(sF[k], rv, w);
                 for (int j = 0; j < 3; j++) {
                     vbox[6 * (size_t)v + j] = smin(vbox[6 * (size_t)v + j], w[j].lo);
                     vbox[6 * (size_t)v + 3 + j] = smax(vbox[6 * (size_t)v + 3 + j], w[j].hi);
                 }
             }
-        } else if (threadIdx.x == 0) {
-            double m = RMUL(0.5, RADD(tl, th));
-            if (sp + 2 <= kMaxTNodes) {
-                st_lo[sp] = m; st_hi[sp] = th; st_depth[sp] = depth + 1; sp++;
-                st_lo[sp] = tl; st_hi[sp] = m; st_depth[sp] = depth + 1; sp++;
-            }
         }
+        // rejected nodes: both halves, one level deeper
+        if (threadIdx.x == 0)
+            for (int k = 0; k < nq; k++) {
+                if (!b_fail[k] || b_depth[k] >= kMaxTDepth) continue;
+                const double tl = b_lo[k], th = b_hi[k];
+                const double m = RMUL(0.5, RADD(tl, th));
+                if (sp + 2 <= kMaxTNodes) {
+                    st_lo[sp] = m; st_hi[sp] = th; st_depth[sp] = b_depth[k] + 1; sp++;
+                    st_lo[sp] = tl; st_hi[sp] = m; st_depth[sp] = b_depth[k] + 1; sp++;
+                }
+            }
     }
     // inflate; a vertex with an empty coordinate stays excluded
     for (int v = v0 + threadIdx.x; v < v1; v += blockDim.x) {
@@ -239,6 +310,60 @@ k_vertex_boxes_cont(const double* __restrict__ x0, const double* __restrict__ x1
         }
         vin[v] = ok ? 1 : 0;
     }
+}
+
+// interval frames of the two forced halves [0, 1/2] and [1/2, 1]: one thread
+// per (included body, half)
+__global__ void k_half_frames(const double* __restrict__ x0, const double* __restrict__ x1,
+                              const int* __restrict__ body_in, int nb, double* __restrict__ fr)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 2 * nb) return;
+    const int b = t >> 1, half = t & 1;
+    if (!body_in[b]) return;
+    const double m = RMUL(0.5, RADD(0.0, 1.0));
+    body_time_frame(x0, x1, b, half ? m : 0.0, half ? 1.0 : m, fr + (size_t)t * kHalfFrame);
+}
+
+// One thread per vertex: its interval positions over the two forced halves,
+// their hull, inflated.  When every vertex of a body stays inside the padded
+// scene box on both halves, this is the body's whole bisection (both halves
+// accepted at depth 1, hulled in the order the stack visits them: [0, 1/2]
+// first); otherwise the body is flagged in `deeper` and k_vertex_boxes_cont
+// redoes it.
+__global__ void k_vertex_boxes_half(const double* __restrict__ rest, const int* __restrict__ vbody,
+                                    const int* __restrict__ body_in, int nv,
+                                    const double* __restrict__ fr, const double* __restrict__ domain,
+                                    double infl, double* __restrict__ vbox, char* __restrict__ vin,
+                                    int* __restrict__ deeper)
+{
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nv) return;
+    const int b = vbody[v];
+    if (!body_in[b]) {
+        vin[v] = 0;
+        return;
+    }
+    const double rv[3] = { rest[3 * (size_t)v], rest[3 * (size_t)v + 1], rest[3 * (size_t)v + 2] };
+    double lo[3] = { INFINITY, INFINITY, INFINITY }, hi[3] = { -INFINITY, -INFINITY, -INFINITY };
+    bool fits = true;
+    for (int half = 0; half < 2; half++) {
+        Itv w[3];
+        vertex_at_frame(fr + (size_t)(2 * b + half) * kHalfFrame, rv, w);
+        for (int j = 0; j < 3; j++) {
+            if (RSUB(w[j].lo, infl) < domain[j] || RADD(w[j].hi, infl) > domain[3 + j]) fits = false;
+            lo[j] = smin(lo[j], w[j].lo);
+            hi[j] = smax(hi[j], w[j].hi);
+        }
+    }
+    if (!fits) atomicOr(&deeper[b], 1);
+    bool ok = true;
+    for (int j = 0; j < 3; j++) {
+        if (!(lo[j] <= hi[j])) ok = false;
+        vbox[6 * (size_t)v + j] = RSUB(lo[j], infl);
+        vbox[6 * (size_t)v + 3 + j] = RADD(hi[j], infl);
+    }
+    vin[v] = ok ? 1 : 0;
 }
 
 __global__ void k_vertex_boxes_disc(const double* __restrict__ rot, const double* __restrict__ rest,
@@ -266,12 +391,6 @@ __global__ void k_vertex_boxes_disc(const double* __restrict__ rot, const double
         vbox[6 * (size_t)v + 3 + j] = RADD(w[j], infl);
     }
     vin[v] = 1;
-}
-
-__global__ void k_clear_flags(char* __restrict__ f, int n)
-{
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) f[i] = 0;
 }
 
 __global__ void k_edge_face_boxes(const int* __restrict__ E, int ne, const int* __restrict__ F, int nf,
@@ -308,21 +427,60 @@ __global__ void k_edge_face_boxes(const int* __restrict__ E, int ne, const int* 
 // ---------------------------------------------------------------------------
 // 3. hash grid
 
+// The grid of one call, computed on the device from the element boxes.
 struct Grid {
     double lo[3];
     double cell, grow;
     long long dims[3];
+    unsigned long long ncells;  // dims[0] * dims[1] * dims[2]
+    int dense;                  // cell-filter slot = (scene, cell) key; else a hash of it
+    int key_bits;               // bits of the largest (scene, cell) key
 };
+
+constexpr int kStatBlocks = 256;
+constexpr int kStatThreads = 256;
+constexpr long long kMaxAxisCells = 1ll << 21;
+// cell-filter slot states; a group rank (>= 0) otherwise
+constexpr int kSlotEmpty = -1;
+constexpr int kSlotMulti = -2;
 
 // element tags: type in the top 2 bits (0 vertex, 1 edge, 2 face)
 __device__ __forceinline__ uint32_t tag(int type, int id) { return ((uint32_t)type << 30) | (uint32_t)id; }
 
-__device__ __forceinline__ const double* elem_box(uint32_t t, const double* vb, const double* eb,
-                                                  const double* fb)
-{
-    int type = t >> 30, id = t & 0x3fffffff;
-    return (type == 0 ? vb : (type == 1 ? eb : fb)) + 6 * (size_t)id;
-}
+// every element in one index space: vertices, then edges, then faces
+struct Elems {
+    const double* vb;
+    const double* eb;
+    const double* fb;
+    const char* vin;
+    const char* ein;
+    const char* fin;
+    const int* vbody;
+    const int* ebody;
+    const int* fbody;
+    int nv, ne, nf;
+    __device__ __forceinline__ int type(int64_t e) const { return e < nv ? 0 : (e < nv + ne ? 1 : 2); }
+    __device__ __forceinline__ int id(int64_t e, int t) const
+    {
+        return (int)(t == 0 ? e : (t == 1 ? e - nv : e - nv - ne));
+    }
+    __device__ __forceinline__ int64_t index(int t, int i) const
+    {
+        return t == 0 ? i : (t == 1 ? (int64_t)nv + i : (int64_t)nv + ne + i);
+    }
+    __device__ __forceinline__ const double* box(int t, int i) const
+    {
+        return (t == 0 ? vb : (t == 1 ? eb : fb)) + 6 * (size_t)i;
+    }
+    __device__ __forceinline__ bool in(int t, int i) const
+    {
+        return (t == 0 ? vin : (t == 1 ? ein : fin))[i] != 0;
+    }
+    __device__ __forceinline__ int body(int t, int i) const
+    {
+        return (t == 0 ? vbody : (t == 1 ? ebody : fbody))[i];
+    }
+};
 
 __device__ __forceinline__ long long cell_of(double x, const Grid& g, int j)
 {
@@ -338,6 +496,7 @@ __device__ __forceinline__ void cell_range(const double* b, const Grid& g, long 
     }
 }
 
+// ipc-toolkit's AABB overlap test (center / half-extent), in round-to-nearest
 __device__ __forceinline__ bool boxes_overlap(const double* a, const double* b)
 {
 #pragma unroll
@@ -349,108 +508,271 @@ __device__ __forceinline__ bool boxes_overlap(const double* a, const double* b)
     return true;
 }
 
-// element list: all included vertices, edges, faces (tags)
-__global__ void k_elem_flags(const char* __restrict__ vin, const char* __restrict__ ein,
-                             const char* __restrict__ fin, int nv, int ne, int nf,
-                             int32_t* __restrict__ flag)
+// Single-precision boxes rounded outward.  If they are disjoint on an axis,
+// a float lies strictly between the two double intervals, so their gap is
+// at least one float ulp of the coordinates -- far beyond the few double
+// ulps by which the round-to-nearest test above can misjudge a gap -- and
+// that test rejects the pair too.  So this test only drops pairs the exact
+// test drops.
+__device__ __forceinline__ bool fboxes_disjoint(const float* a, const float* b)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int n = nv + ne + nf;
-    if (i >= n) return;
-    flag[i] = i < nv ? vin[i] : (i < nv + ne ? ein[i - nv] : fin[i - nv - ne]);
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+        if (a[i] > b[3 + i] || b[i] > a[3 + i]) return true;
+    return false;
 }
 
-__global__ void k_elem_list(const int32_t* __restrict__ flag, const int32_t* __restrict__ pos, int nv,
-                            int ne, int nf, uint32_t* __restrict__ elems)
+__device__ __forceinline__ uint64_t mix64(uint64_t x)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int n = nv + ne + nf;
-    if (i >= n || !flag[i]) return;
-    uint32_t t = i < nv ? tag(0, i) : (i < nv + ne ? tag(1, i - nv) : tag(2, i - nv - ne));
-    elems[pos[i]] = t;
+    x ^= x >> 30;
+    x *= 0xbf58476d1ce4e5b9ull;
+    x ^= x >> 27;
+    x *= 0x94d049bb133111ebull;
+    x ^= x >> 31;
+    return x;
 }
 
-// extent statistics: bounds of all element boxes, sum of edge box extents
-__global__ void k_elem_bounds(const uint32_t* __restrict__ elems, int m, const double* __restrict__ vb,
-                              const double* __restrict__ eb, const double* __restrict__ fb,
-                              double* __restrict__ part, double* __restrict__ ext)
+__device__ __forceinline__ uint64_t slot_of(uint64_t key, const Grid& g, uint64_t mask)
 {
-    // part: per block lo[3], hi[3]; ext: per element extent (edges only, else 0)
-    __shared__ double sh[6][256];
+    return g.dense ? key : (mix64(key) & mask);
+}
+
+// bounds of the included element boxes and the sum of the included edges'
+// largest box extents (fixed grid, fixed reduction order: deterministic)
+__global__ void __launch_bounds__(kStatThreads) k_elem_stats(Elems E, double* __restrict__ part,
+                                                             int* __restrict__ part_n)
+{
+    __shared__ double sh[7][kStatThreads];
+    __shared__ int shn[kStatThreads];
     double lo[3] = { INFINITY, INFINITY, INFINITY }, hi[3] = { -INFINITY, -INFINITY, -INFINITY };
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
-        const double* b = elem_box(elems[i], vb, eb, fb);
-        double e = 0;
+    double ext = 0;
+    int ned = 0;
+    const int64_t n = (int64_t)E.nv + E.ne + E.nf;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int t = E.type(e), i = E.id(e, t);
+        if (!E.in(t, i)) continue;
+        const double* b = E.box(t, i);
+        double x = 0;
         for (int j = 0; j < 3; j++) {
             lo[j] = smin(lo[j], b[j]);
             hi[j] = smax(hi[j], b[3 + j]);
-            e = smax(e, RSUB(b[3 + j], b[j]));
+            x = smax(x, RSUB(b[3 + j], b[j]));
         }
-        ext[i] = (elems[i] >> 30) == 1 ? e : 0.0;
+        if (t == 1) {
+            ext = RADD(ext, x);
+            ned++;
+        }
     }
     for (int j = 0; j < 3; j++) {
         sh[j][threadIdx.x] = lo[j];
         sh[3 + j][threadIdx.x] = hi[j];
     }
+    sh[6][threadIdx.x] = ext;
+    shn[threadIdx.x] = ned;
     __syncthreads();
-    for (int o = 128; o > 0; o >>= 1) {
-        if (threadIdx.x < o)
+    for (int o = kStatThreads / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) {
             for (int j = 0; j < 3; j++) {
                 sh[j][threadIdx.x] = smin(sh[j][threadIdx.x], sh[j][threadIdx.x + o]);
                 sh[3 + j][threadIdx.x] = smax(sh[3 + j][threadIdx.x], sh[3 + j][threadIdx.x + o]);
             }
+            sh[6][threadIdx.x] = RADD(sh[6][threadIdx.x], sh[6][threadIdx.x + o]);
+            shn[threadIdx.x] += shn[threadIdx.x + o];
+        }
         __syncthreads();
     }
-    if (threadIdx.x == 0)
-        for (int j = 0; j < 6; j++) part[6 * blockIdx.x + j] = sh[j][0];
-}
-
-__global__ void k_count_cells(const uint32_t* __restrict__ elems, int m, const double* __restrict__ vb,
-                              const double* __restrict__ eb, const double* __restrict__ fb, Grid g,
-                              int32_t* __restrict__ cnt, int32_t* __restrict__ large_flag)
-{
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m) return;
-    long long c0[3], c1[3];
-    cell_range(elem_box(elems[i], vb, eb, fb), g, c0, c1);
-    long long k = (c1[0] - c0[0] + 1) * (c1[1] - c0[1] + 1) * (c1[2] - c0[2] + 1);
-    bool large = k > kLargeCells;
-    cnt[i] = large ? 0 : (int32_t)k;
-    large_flag[i] = large ? 1 : 0;
-}
-
-// scene of an element (tag: type << 30 | index)
-struct ElemScene {
-    const int* vbody;
-    const int* ebody;
-    const int* fbody;
-    const int* bscene;
-    __device__ __forceinline__ uint64_t of(uint32_t tag) const
-    {
-        const int t = tag >> 30, i = tag & 0x3fffffff;
-        const int b = t == 0 ? vbody[i] : (t == 1 ? ebody[i] : fbody[i]);
-        return (uint64_t)bscene[b];
+    if (threadIdx.x == 0) {
+        for (int j = 0; j < 7; j++) part[7 * blockIdx.x + j] = sh[j][0];
+        part_n[blockIdx.x] = shn[0];
     }
-};
+}
 
-// (scene, cell) keys: elements of different scenes never share a key
-__global__ void k_emit_items(const uint32_t* __restrict__ elems, int m, const double* __restrict__ vb,
-                             const double* __restrict__ eb, const double* __restrict__ fb, Grid g,
-                             ElemScene es, uint64_t ncells, const int32_t* __restrict__ cnt,
-                             const int32_t* __restrict__ off, uint64_t* __restrict__ keys,
-                             uint32_t* __restrict__ vals)
+__device__ __forceinline__ int dbits_for(unsigned long long v)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m || cnt[i] == 0) return;
+    return v == 0 ? 1 : 64 - __clzll((long long)v);
+}
+
+// Grid from the partial statistics: cell = the mean extent of the included
+// edge boxes (at least half the mean rest edge length), doubled while the
+// grid is too large for the keys (a cell size changes only the work, never
+// the pairs); one thread
+__global__ void k_grid_setup(const double* __restrict__ part, const int* __restrict__ part_n, int nblk,
+                             double avg_edge_len, int nscenes, int group_bits, uint64_t nslots,
+                             Grid* __restrict__ out)
+{
+    double lo[3] = { INFINITY, INFINITY, INFINITY }, hi[3] = { -INFINITY, -INFINITY, -INFINITY };
+    double ext = 0;
+    long long ned = 0;
+    for (int b = 0; b < nblk; b++) {
+        for (int j = 0; j < 3; j++) {
+            lo[j] = smin(lo[j], part[7 * b + j]);
+            hi[j] = smax(hi[j], part[7 * b + 3 + j]);
+        }
+        ext = RADD(ext, part[7 * b + 6]);
+        ned += part_n[b];
+    }
+    Grid g;
+    bool empty = false;
+    for (int j = 0; j < 3; j++)
+        if (!(lo[j] <= hi[j]) || !isfinite(lo[j]) || !isfinite(hi[j])) empty = true;
+    double cell = ned > 0 ? ext / (double)ned : 0.0;
+    cell = fmax(cell, avg_edge_len * 0.5);
+    cell = fmax(cell, 1e-9);
+    if (!isfinite(cell)) empty = true;
+    unsigned long long tot = 1;
+    // each doubling shrinks the grid; 2100 doublings exceed any double range
+    for (int it = 0;; it++) {
+        if (it == 2100) empty = true;
+        bool ok = true;
+        tot = 1;
+        for (int j = 0; j < 3; j++) {
+            double d = empty ? 1.0 : ceil((hi[j] - lo[j]) / cell) + 1.0;
+            if (!(d <= (double)kMaxAxisCells)) {
+                ok = false;
+                d = 1;
+            }
+            g.dims[j] = (long long)d;
+            tot *= (unsigned long long)g.dims[j];
+        }
+        if (ok) {
+            const unsigned long long keys = (unsigned long long)nscenes * tot;
+            ok = dbits_for(keys - 1) + group_bits + 3 <= 64 && keys / (unsigned long long)nscenes == tot;
+        }
+        if (ok) break;
+        cell *= 2;
+    }
+    for (int j = 0; j < 3; j++) g.lo[j] = empty ? 0.0 : lo[j];
+    g.cell = cell;
+    g.grow = 1e-9 * cell;
+    g.ncells = tot;
+    const unsigned long long keys = (unsigned long long)nscenes * tot;
+    g.dense = keys <= nslots ? 1 : 0;
+    g.key_bits = dbits_for(keys - 1);
+    *out = g;
+}
+
+// The cell filter.  A thread per element: its float box, its cell range
+// (first cell packed 21 bits per axis; extents 6 bits per axis, flags in the
+// top bits), and for every cell it covers the slot's group: empty -> this
+// element's group rank -> kSlotMulti once a second group arrives.  Elements
+// spanning more than kLargeCells cells go to the large list instead.
+constexpr uint32_t kExtActive = 1u << 31;  // included and binned
+constexpr uint32_t kExtLarge = 1u << 30;   // included, tested against all elements
+
+__global__ void k_mark_cells(Elems E, const int* __restrict__ bscene, const int* __restrict__ grank,
+                             const Grid* __restrict__ gp, int* __restrict__ sig, uint64_t mask,
+                             uint64_t* __restrict__ ec0, uint32_t* __restrict__ eext,
+                             float* __restrict__ f32, uint32_t* __restrict__ large_list,
+                             int* __restrict__ nlarge)
+{
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t n = (int64_t)E.nv + E.ne + E.nf;
+    if (e >= n) return;
+    const int t = E.type(e), i = E.id(e, t);
+    if (!E.in(t, i)) {
+        eext[e] = 0;
+        return;
+    }
+    const Grid g = *gp;
+    const double* b = E.box(t, i);
+    for (int j = 0; j < 3; j++) {
+        f32[6 * e + j] = __double2float_rd(b[j]);
+        f32[6 * e + 3 + j] = __double2float_ru(b[3 + j]);
+    }
     long long c0[3], c1[3];
-    cell_range(elem_box(elems[i], vb, eb, fb), g, c0, c1);
-    const uint64_t base = es.of(elems[i]) * ncells;
-    int o = off[i];
+    cell_range(b, g, c0, c1);
+    const long long k = (c1[0] - c0[0] + 1) * (c1[1] - c0[1] + 1) * (c1[2] - c0[2] + 1);
+    if (k > kLargeCells) {
+        eext[e] = kExtLarge;
+        large_list[atomicAdd(nlarge, 1)] = tag(t, i);
+        return;
+    }
+    ec0[e] = (uint64_t)c0[0] | ((uint64_t)c0[1] << 21) | ((uint64_t)c0[2] << 42);
+    eext[e] = kExtActive | (uint32_t)(c1[0] - c0[0]) | ((uint32_t)(c1[1] - c0[1]) << 6)
+              | ((uint32_t)(c1[2] - c0[2]) << 12);
+    const int body = E.body(t, i);
+    const int gr = grank[body];
+    const uint64_t base = (uint64_t)bscene[body] * g.ncells;
     for (long long z = c0[2]; z <= c1[2]; z++)
         for (long long y = c0[1]; y <= c1[1]; y++)
             for (long long x = c0[0]; x <= c1[0]; x++) {
-                keys[o] = base + (uint64_t)((z * g.dims[1] + y) * g.dims[0] + x);
-                vals[o] = elems[i];
+                const uint64_t key = base + (uint64_t)((z * g.dims[1] + y) * g.dims[0] + x);
+                int* sl = sig + slot_of(key, g, mask);
+                const int s = *sl;
+                if (s == gr || s == kSlotMulti) continue;
+                const int old = atomicCAS(sl, kSlotEmpty, gr);
+                if (old != kSlotEmpty && old != gr && old != kSlotMulti) atomicExch(sl, kSlotMulti);
+            }
+}
+
+__device__ __forceinline__ void unpack_range(uint64_t c0p, uint32_t ext, long long c0[3], long long c1[3])
+{
+    for (int j = 0; j < 3; j++) {
+        c0[j] = (long long)((c0p >> (21 * j)) & ((1ull << 21) - 1));
+        c1[j] = c0[j] + (long long)((ext >> (6 * j)) & 63u);
+    }
+}
+
+// items per element: the marked cells it covers
+__global__ void k_count_items(Elems E, const int* __restrict__ bscene, const Grid* __restrict__ gp,
+                              const int* __restrict__ sig, uint64_t mask,
+                              const uint64_t* __restrict__ ec0, const uint32_t* __restrict__ eext,
+                              int32_t* __restrict__ cnt)
+{
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t n = (int64_t)E.nv + E.ne + E.nf;
+    if (e >= n) return;
+    const uint32_t ext = eext[e];
+    if (!(ext & kExtActive)) {
+        cnt[e] = 0;
+        return;
+    }
+    const Grid g = *gp;
+    const int t = E.type(e), i = E.id(e, t);
+    const uint64_t base = (uint64_t)bscene[E.body(t, i)] * g.ncells;
+    long long c0[3], c1[3];
+    unpack_range(ec0[e], ext, c0, c1);
+    int k = 0;
+    for (long long z = c0[2]; z <= c1[2]; z++)
+        for (long long y = c0[1]; y <= c1[1]; y++)
+            for (long long x = c0[0]; x <= c1[0]; x++) {
+                const uint64_t key = base + (uint64_t)((z * g.dims[1] + y) * g.dims[0] + x);
+                k += sig[slot_of(key, g, mask)] == kSlotMulti;
+            }
+    cnt[e] = k;
+}
+
+// items of the marked cells: key ((scene, cell) << group_bits | group rank)
+// << 3 | first-cell bits (bit j: the cell is the first of the element's range
+// along axis j); value the element tag
+__global__ void k_emit_items(Elems E, const int* __restrict__ bscene, const int* __restrict__ grank,
+                             const Grid* __restrict__ gp, const int* __restrict__ sig, uint64_t mask,
+                             const uint64_t* __restrict__ ec0, const uint32_t* __restrict__ eext,
+                             const int32_t* __restrict__ cnt, const int32_t* __restrict__ off,
+                             int group_bits, uint64_t* __restrict__ keys, uint32_t* __restrict__ vals)
+{
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t n = (int64_t)E.nv + E.ne + E.nf;
+    if (e >= n || cnt[e] == 0) return;
+    const Grid g = *gp;
+    const int t = E.type(e), i = E.id(e, t);
+    const int body = E.body(t, i);
+    const uint64_t gr = (uint64_t)grank[body];
+    const uint64_t base = (uint64_t)bscene[body] * g.ncells;
+    long long c0[3], c1[3];
+    unpack_range(ec0[e], eext[e], c0, c1);
+    const uint32_t tg = tag(t, i);
+    int64_t o = off[e];
+    for (long long z = c0[2]; z <= c1[2]; z++)
+        for (long long y = c0[1]; y <= c1[1]; y++)
+            for (long long x = c0[0]; x <= c1[0]; x++) {
+                const uint64_t key = base + (uint64_t)((z * g.dims[1] + y) * g.dims[0] + x);
+                if (sig[slot_of(key, g, mask)] != kSlotMulti) continue;
+                const uint64_t first = (uint64_t)(x == c0[0]) | ((uint64_t)(y == c0[1]) << 1)
+                                       | ((uint64_t)(z == c0[2]) << 2);
+                keys[o] = (((key << group_bits) | gr) << 3) | first;
+                vals[o] = tg;
                 o++;
             }
 }
@@ -474,178 +796,95 @@ __device__ __forceinline__ void push_pair(const PairOut& o, bool is_ee, unsigned
     }
 }
 
-struct PairCtx {
-    const double* vb;
-    const double* eb;
-    const double* fb;
-    const int* vbody;
-    const int* ebody;
-    const int* fbody;
-    const int* group;
-    int nv, ne;
-};
+// The pair kinds of a call: EE and FV (collision candidates), or EF (edge,
+// face: intersection candidates).
+constexpr int kPairsEEFV = 0;
+constexpr int kPairsEF = 1;
 
-// test one element pair (any order); returns true and the output if it is an
-// EE or FV candidate passing the group and overlap filters
-__device__ __forceinline__ bool pair_filter(const PairCtx& P, uint32_t a, uint32_t b, bool& is_ee,
-                                            unsigned long long& key)
+__device__ __forceinline__ bool pair_types(int kind, int ta, int tb)
 {
-    int ta = a >> 30, tb = b >> 30;
-    int ia = a & 0x3fffffff, ib = b & 0x3fffffff;
-    int ga, gb;
-    if (ta == 1 && tb == 1) {
-        if (ia == ib) return false;
-        ga = P.group[P.ebody[ia]];
-        gb = P.group[P.ebody[ib]];
-        if (ga == gb) return false;
-        if (!boxes_overlap(P.eb + 6 * (size_t)ia, P.eb + 6 * (size_t)ib)) return false;
-        is_ee = true;
-        int lo = min(ia, ib), hi = max(ia, ib);
-        key = (unsigned long long)lo * (unsigned long long)P.ne + (unsigned long long)hi;
-        return true;
-    }
-    if ((ta == 2 && tb == 0) || (ta == 0 && tb == 2)) {
-        int f = ta == 2 ? ia : ib, v = ta == 2 ? ib : ia;
-        if (P.group[P.fbody[f]] == P.group[P.vbody[v]]) return false;
-        if (!boxes_overlap(P.fb + 6 * (size_t)f, P.vb + 6 * (size_t)v)) return false;
-        is_ee = false;
-        key = (unsigned long long)f * (unsigned long long)P.nv + (unsigned long long)v;
-        return true;
-    }
-    return false;
+    return kind == kPairsEF ? ta + tb == 3 : ((ta == 1 && tb == 1) || (ta + tb == 2 && ta != tb));
 }
 
-// one thread per sorted item: pairs with later items of the same cell,
-// reported only in the first cell both elements cover
+// an EE (edges) or FV (face, vertex in either order) pair of elements whose
+// groups differ, or an EF pair (edge, face in either order; output in the FV
+// stream, key face * ne + edge): the overlap tests and the output key
+__device__ __forceinline__ void test_pair(const Elems& E, const float* __restrict__ f32, int ta, int ia,
+                                          int tb, int ib, const PairOut& o)
+{
+    if (fboxes_disjoint(f32 + 6 * E.index(ta, ia), f32 + 6 * E.index(tb, ib))) return;
+    if (!boxes_overlap(E.box(ta, ia), E.box(tb, ib))) return;
+    if (ta + tb == 3) {
+        const int f = ta == 2 ? ia : ib, e = ta == 2 ? ib : ia;
+        push_pair(o, false, (unsigned long long)f * (unsigned long long)E.ne + (unsigned long long)e);
+    } else if (ta == 1) {
+        const int lo = min(ia, ib), hi = max(ia, ib);
+        push_pair(o, true, (unsigned long long)lo * (unsigned long long)E.ne + (unsigned long long)hi);
+    } else {
+        const int f = ta == 2 ? ia : ib, v = ta == 2 ? ib : ia;
+        push_pair(o, false, (unsigned long long)f * (unsigned long long)E.nv + (unsigned long long)v);
+    }
+}
+
+// One thread per sorted item: pairs with the items of later groups in its
+// cell (the earlier groups' items pair with it), reported in the first cell
+// both elements cover.
 __global__ void k_cell_pairs(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ vals,
-                             int64_t m, PairCtx P, Grid g, ElemScene es, uint64_t ncells, PairOut o)
+                             int64_t m, int group_bits, int kind, Elems E,
+                             const float* __restrict__ f32, PairOut o)
 {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m) return;
-    uint64_t key = keys[i];
-    uint32_t a = vals[i];
-    long long a0[3], a1[3];
-    bool have_a = false;
-    // Within a cell the items keep the element order of the emission (the
-    // radix sort is stable, elements are ordered vertices, edges, faces):
-    // a face's later items are faces (no pair), an edge's are edges, then
-    // faces (no more pairs), a vertex's reach the faces after the edges.
-    if ((a >> 30) == 2) return;
-    for (int64_t j = i + 1; j < m && keys[j] == key; j++) {
-        uint32_t b = vals[j];
-        bool is_ee;
-        unsigned long long pk;
-        int ta = a >> 30, tb = b >> 30;
-        if (ta == 1 && tb == 2) break;
-        if (!((ta == 1 && tb == 1) || (ta + tb == 2 && ta != tb))) continue;
-        if (!pair_filter(P, a, b, is_ee, pk)) continue;
-        if (!have_a) {
-            cell_range(elem_box(a, P.vb, P.eb, P.fb), g, a0, a1);
-            have_a = true;
-        }
-        long long b0[3], b1[3];
-        cell_range(elem_box(b, P.vb, P.eb, P.fb), g, b0, b1);
-        long long fx = max(a0[0], b0[0]), fy = max(a0[1], b0[1]), fz = max(a0[2], b0[2]);
-        uint64_t first = es.of(a) * ncells + (uint64_t)((fz * g.dims[1] + fy) * g.dims[0] + fx);
-        if (first != key) continue;
-        push_pair(o, is_ee, pk);
-    }
-}
-
-// The same with one warp per sorted item, its lanes striding over the later
-// items of the cell: for small item counts, where the cells are few and
-// full and one thread per item would walk a whole cell alone.
-__global__ void k_cell_pairs_warp(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ vals,
-                                  int64_t m, PairCtx P, Grid g, ElemScene es, uint64_t ncells,
-                                  PairOut o)
-{
-    const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (i >= m) return;
-    const uint64_t key = keys[i];
+    const uint64_t ki = keys[i];
+    const uint64_t run = ki >> 3;                 // (scene, cell, group)
+    const uint64_t cellk = ki >> (3 + group_bits);  // (scene, cell)
+    const unsigned fa = (unsigned)(ki & 7);
+    int64_t j = i + 1;
+    while (j < m && (keys[j] >> 3) == run) j++;
     const uint32_t a = vals[i];
-    long long a0[3], a1[3];
-    bool have_a = false;
-    if ((a >> 30) == 2) return;  // faces: only faces follow in the cell
-    for (int64_t j = i + 1 + lane; j < m && keys[j] == key; j += 32) {
-        uint32_t b = vals[j];
-        bool is_ee;
-        unsigned long long pk;
-        int ta = a >> 30, tb = b >> 30;
-        if (ta == 1 && tb == 2) break;  // an edge's later items: edges, then faces
-        if (!((ta == 1 && tb == 1) || (ta + tb == 2 && ta != tb))) continue;
-        if (!pair_filter(P, a, b, is_ee, pk)) continue;
-        if (!have_a) {
-            cell_range(elem_box(a, P.vb, P.eb, P.fb), g, a0, a1);
-            have_a = true;
-        }
-        long long b0[3], b1[3];
-        cell_range(elem_box(b, P.vb, P.eb, P.fb), g, b0, b1);
-        long long fx = max(a0[0], b0[0]), fy = max(a0[1], b0[1]), fz = max(a0[2], b0[2]);
-        uint64_t first = es.of(a) * ncells + (uint64_t)((fz * g.dims[1] + fy) * g.dims[0] + fx);
-        if (first != key) continue;
-        push_pair(o, is_ee, pk);
+    const int ta = a >> 30, ia = a & 0x3fffffff;
+    for (; j < m; j++) {
+        const uint64_t kj = keys[j];
+        if ((kj >> (3 + group_bits)) != cellk) break;
+        if ((fa | (unsigned)(kj & 7)) != 7) continue;
+        const uint32_t b = vals[j];
+        const int tb = b >> 30;
+        if (!pair_types(kind, ta, tb)) continue;
+        test_pair(E, f32, ta, ia, tb, b & 0x3fffffff, o);
     }
 }
 
 // large elements against every included element of the matching type in
-// their scene: grid row y = large element, its blocks stride over the range;
-// range[s * 3 + t] is the first
-// position in elems of scene s's type-t elements (vertices, edges, faces;
-// elems is ordered by type, then by element index, hence by scene)
-__global__ void k_large_pairs(const uint32_t* __restrict__ large, int nl, int row0,
-                              const uint32_t* __restrict__ elems, const int32_t* __restrict__ is_large,
-                              const int32_t* __restrict__ range, int nscenes, ElemScene es, PairCtx P,
+// their scene: grid row y = large element, its blocks stride over the
+// scene's element range (from the per-body prefix arrays)
+__global__ void k_large_pairs(const uint32_t* __restrict__ large, int nl, int row0, int kind, Elems E,
+                              const int* __restrict__ bscene, const int* __restrict__ scene_bstart,
+                              const int* __restrict__ bvs, const int* __restrict__ bes,
+                              const int* __restrict__ bfs, const int* __restrict__ grank,
+                              const uint32_t* __restrict__ eext, const float* __restrict__ f32,
                               PairOut o)
 {
     const int li = row0 + blockIdx.y;
     if (li >= nl) return;
     const uint32_t a = large[li];
-    const int ta = a >> 30;
-    const int s = (int)es.of(a);
-    // edges meet edges, faces meet vertices (and vertices faces)
-    const int tb = ta == 1 ? 1 : (ta == 2 ? 0 : 2);
-    const int lo = range[3 * s + tb];
-    const int hi = range[3 * (s + 1) + tb];
-    for (int ei = lo + blockIdx.x * blockDim.x + threadIdx.x; ei < hi; ei += gridDim.x * blockDim.x) {
-        const uint32_t b = elems[ei];
+    const int ta = a >> 30, ia = a & 0x3fffffff;
+    const int body_a = E.body(ta, ia);
+    const int s = bscene[body_a];
+    const int ga = grank[body_a];
+    // EE / FV: edges meet edges, faces meet vertices (and vertices faces);
+    // EF: edges meet faces (and faces edges), vertices nothing
+    const int tb = kind == kPairsEF ? 3 - ta : (ta == 1 ? 1 : (ta == 2 ? 0 : 2));
+    if (tb > 2) return;
+    const int* start = tb == 0 ? bvs : (tb == 1 ? bes : bfs);
+    const int lo = start[scene_bstart[s]], hi = start[scene_bstart[s + 1]];
+    for (int ib = lo + blockIdx.x * blockDim.x + threadIdx.x; ib < hi; ib += gridDim.x * blockDim.x) {
+        const uint32_t ext = eext[E.index(tb, ib)];
+        if (!(ext & (kExtActive | kExtLarge))) continue;  // not included
         // a pair of two large elements is reported by the one with the smaller tag
-        if (is_large[ei] && b < a) continue;
-        bool is_ee;
-        unsigned long long pk;
-        if (pair_filter(P, a, b, is_ee, pk)) push_pair(o, is_ee, pk);
+        if ((ext & kExtLarge) && tag(tb, ib) < a) continue;
+        if (grank[E.body(tb, ib)] == ga) continue;
+        test_pair(E, f32, ta, ia, tb, ib, o);
     }
-}
-
-// positions in elems of each scene's first vertex, edge and face (from the
-// exclusive scan of the inclusion flags over all elements); row nscenes
-// holds the end of each type
-__global__ void k_scene_ranges(const int32_t* __restrict__ pos, const int* __restrict__ scene_bstart,
-                               const int* __restrict__ bvs, const int* __restrict__ bes,
-                               const int* __restrict__ bfs, int nscenes, int nv, int ne, int nf,
-                               int m, int32_t* __restrict__ range)
-{
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s > nscenes) return;
-    const int ntot = nv + ne + nf;
-    auto at = [&](int idx) { return idx < ntot ? pos[idx] : m; };
-    if (s == nscenes) {
-        range[3 * s] = at(nv);
-        range[3 * s + 1] = at(nv + ne);
-        range[3 * s + 2] = m;
-        return;
-    }
-    const int b = scene_bstart[s];
-    range[3 * s] = at(bvs[b]);
-    range[3 * s + 1] = at(nv + bes[b]);
-    range[3 * s + 2] = at(nv + ne + bfs[b]);
-}
-
-__global__ void k_large_list(const uint32_t* __restrict__ elems, const int32_t* __restrict__ flag,
-                             const int32_t* __restrict__ pos, int m, uint32_t* __restrict__ out)
-{
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < m && flag[i]) out[pos[i]] = elems[i];
 }
 
 __global__ void k_decode_pairs(const unsigned long long* __restrict__ keys, int64_t n,
@@ -665,19 +904,42 @@ __global__ void k_iota(uint32_t* __restrict__ v, int64_t n)
 
 // ---------------------------------------------------------------------------
 
-int compute_world_vertices_rn(Ctx& c, const double* x, double* V, DevBuf& rotbuf);
 int body_rot_rn(Ctx& c, const double* x, double* out);
 
-int detect_candidates(Ctx& c, const double* x0, const double* x1, bool continuous, double infl)
+// slots of the cell filter for ntot elements: a power of two, about four per
+// element (elements cover a few cells each), 2^16 .. 2^27
+static uint64_t filter_slots(int64_t ntot)
+{
+    uint64_t t = 1u << 16;
+    while (t < (uint64_t)ntot * 4 && t < (1ull << 27)) t <<= 1;
+    return t;
+}
+
+// Candidate pairs of the kind (kPairsEEFV: out.ee, out.fv; kPairsEF: (face,
+// edge) pairs in out.fv) between x0 and x1 (continuous) or at x0.
+int detect_pairs(Ctx& c, const double* x0, const double* x1, bool continuous, double infl, int kind,
+                 Candidates& out)
 {
     Scene& s = c.s;
     cudaStream_t st = c.stream;
-    c.cand.num_ee = c.cand.num_fv = 0;
+    out.num_ee = out.num_fv = 0;
     c.stats.grid_items = 0;
     c.stats.large_elements = 0;
     if (s.nb <= 1) return RIGC_OK;
     if (!continuous) x1 = x0;
     DevBuf* S = c.scratch;
+    const int64_t ntot = (int64_t)s.nv + s.ne + s.nf;
+    // small device state of the call: domain (6 doubles), grid, statistics,
+    // counters
+    constexpr size_t kOffGrid = 64, kOffPart = 256, kOffPartN = kOffPart + 7 * 8 * kStatBlocks,
+                     kOffCount = kOffPartN + 4 * kStatBlocks, kMiscBytes = kOffCount + 64;
+    RIGC_TRY(c.bp_misc.reserve(kMiscBytes));
+    char* misc = c.bp_misc.as<char>();
+    double* d_domain = reinterpret_cast<double*>(misc);
+    Grid* d_grid = reinterpret_cast<Grid*>(misc + kOffGrid);
+    double* d_part = reinterpret_cast<double*>(misc + kOffPart);
+    int* d_part_n = reinterpret_cast<int*>(misc + kOffPartN);
+    int32_t* d_count = reinterpret_cast<int32_t*>(misc + kOffCount);  // [0] items, [1] large
     // ---- 1. bodies
     RIGC_TRY(c.body_box.reserve((size_t)6 * s.nb * sizeof(double)));
     RIGC_TRY(c.body_in.reserve((size_t)(s.nb + 1) * sizeof(int)));
@@ -696,36 +958,30 @@ int detect_candidates(Ctx& c, const double* x0, const double* x1, bool continuou
             c.body_box.as<double>(), s.group, s.bscene, s.scene_bstart, c.scene_on, s.nb, chunk,
             infl, c.body_in.as<int>());
     }
-    std::vector<int> h_in(s.nb);
-    RIGC_CUDA(cudaMemcpyAsync(h_in.data(), c.body_in.ptr, (size_t)s.nb * sizeof(int),
-                              cudaMemcpyDeviceToHost, st));
-    RIGC_CUDA(cudaStreamSynchronize(st));
-    std::vector<int> blist;
-    for (int b = 0; b < s.nb; b++)
-        if (h_in[b]) blist.push_back(b);
-    if (blist.empty()) return RIGC_OK;
     // ---- 2. element boxes
-    RIGC_TRY(c.vbox.reserve((size_t)6 * s.nv * sizeof(double)));
+    RIGC_TRY(c.vbox.reserve((size_t)6 * s.nv * sizeof(double) + 8));
     RIGC_TRY(c.ebox.reserve((size_t)6 * s.ne * sizeof(double) + 8));
     RIGC_TRY(c.fbox.reserve((size_t)6 * s.nf * sizeof(double) + 8));
     RIGC_TRY(c.vin.reserve((size_t)s.nv + 8));
     RIGC_TRY(c.ein.reserve((size_t)s.ne + 8));
     RIGC_TRY(c.fin.reserve((size_t)s.nf + 8));
     if (continuous) {
-        RIGC_TRY(S[0].reserve((size_t)blist.size() * sizeof(int) + 64 * sizeof(double)));
-        int* d_list = S[0].as<int>();
-        double* d_domain = reinterpret_cast<double*>(S[0].as<char>() + ((blist.size() * sizeof(int) + 63) / 64) * 64);
-        RIGC_CUDA(cudaMemcpyAsync(d_list, blist.data(), blist.size() * sizeof(int),
-                                  cudaMemcpyHostToDevice, st));
+        RIGC_TRY(c.bp_frames.reserve((size_t)2 * s.nb * kHalfFrame * sizeof(double)));
+        RIGC_TRY(c.bp_deeper.reserve((size_t)s.nb * sizeof(int)));
         RIGC_COUNT_LAUNCH();
         k_scene_box<<<1, 256, 0, st>>>(c.body_box.as<double>(), c.body_in.as<int>(), s.nb, d_domain);
         RIGC_COUNT_LAUNCH();
-        k_clear_flags<<<grid_for(s.nv, 256), 256, 0, st>>>(c.vin.as<char>(), s.nv);
+        k_half_frames<<<grid_for(2 * (int64_t)s.nb, 128), 128, 0, st>>>(
+            x0, x1, c.body_in.as<int>(), s.nb, c.bp_frames.as<double>());
+        RIGC_CUDA(cudaMemsetAsync(c.bp_deeper.ptr, 0, (size_t)s.nb * sizeof(int), st));
         RIGC_COUNT_LAUNCH();
-        k_vertex_boxes_cont<<<(unsigned)blist.size(), kVBThreads, 0, st>>>(
-            x0, x1, s.rest, s.bvs, d_list, d_domain, infl, c.vbox.as<double>(), c.vin.as<char>());
-        // the host copy of blist must outlive the async copy
-        RIGC_CUDA(cudaStreamSynchronize(st));
+        k_vertex_boxes_half<<<grid_for(s.nv, 128), 128, 0, st>>>(
+            s.rest, s.vbody, c.body_in.as<int>(), s.nv, c.bp_frames.as<double>(), d_domain, infl,
+            c.vbox.as<double>(), c.vin.as<char>(), c.bp_deeper.as<int>());
+        RIGC_COUNT_LAUNCH();
+        k_vertex_boxes_cont<<<(unsigned)s.nb, kVBThreads, 0, st>>>(
+            x0, x1, s.rest, s.bvs, c.body_in.as<int>(), c.bp_deeper.as<int>(), d_domain, infl,
+            c.vbox.as<double>(), c.vin.as<char>());
     } else {
         RIGC_TRY(S[0].reserve((size_t)12 * s.nb * sizeof(double)));
         RIGC_TRY(body_rot_rn(c, x0, S[0].as<double>()));
@@ -739,138 +995,89 @@ int detect_candidates(Ctx& c, const double* x0, const double* x1, bool continuou
         s.edges, s.ne, s.faces, s.nf, c.vbox.as<double>(), c.vin.as<char>(), c.ebox.as<double>(),
         c.ein.as<char>(), c.fbox.as<double>(), c.fin.as<char>());
     RIGC_CUDA(cudaGetLastError());
-    // ---- 3. element list
-    const int ntot = s.nv + s.ne + s.nf;
-    RIGC_TRY(S[1].reserve((size_t)(2 * ntot + 16) * sizeof(int32_t)));
-    int32_t* flag = S[1].as<int32_t>();
-    int32_t* pos = flag + ntot;
-    int32_t* cnt_dev = c.d_scalars.as<int32_t>();
+    const Elems E { c.vbox.as<double>(), c.ebox.as<double>(), c.fbox.as<double>(),
+                    c.vin.as<char>(), c.ein.as<char>(), c.fin.as<char>(),
+                    s.vbody, s.ebody, s.fbody, s.nv, s.ne, s.nf };
+    // ---- 3. grid and cell filter
     RIGC_COUNT_LAUNCH();
-    k_elem_flags<<<grid_for(ntot, 256), 256, 0, st>>>(c.vin.as<char>(), c.ein.as<char>(),
-                                                     c.fin.as<char>(), s.nv, s.ne, s.nf, flag);
-    RIGC_TRY(exclusive_scan_i32(flag, pos, ntot, cnt_dev, S[7], st));
-    int32_t m, epos[2];
-    RIGC_CUDA(cudaMemcpyAsync(&m, cnt_dev, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-    RIGC_CUDA(cudaMemcpyAsync(epos, pos + s.nv, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-    if (s.nf > 0)
-        RIGC_CUDA(cudaMemcpyAsync(epos + 1, pos + s.nv + s.ne, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-    RIGC_CUDA(cudaStreamSynchronize(st));
-    if (s.nf == 0) epos[1] = m;
-    const int n_edges_in = epos[1] - epos[0];
-    if (m == 0) return RIGC_OK;
-    RIGC_TRY(S[2].reserve((size_t)m * sizeof(uint32_t) + (size_t)m * sizeof(double) + 4096 * 6 * 8));
-    uint32_t* elems = S[2].as<uint32_t>();
-    double* ext = reinterpret_cast<double*>(S[2].as<char>() + (((size_t)m * 4 + 255) / 256) * 256);
-    double* part = ext + m;
+    k_elem_stats<<<kStatBlocks, kStatThreads, 0, st>>>(E, d_part, d_part_n);
+    const uint64_t nslots = filter_slots(ntot);
     RIGC_COUNT_LAUNCH();
-    k_elem_list<<<grid_for(ntot, 256), 256, 0, st>>>(flag, pos, s.nv, s.ne, s.nf, elems);
-    const int nbk = 256;
+    k_grid_setup<<<1, 1, 0, st>>>(d_part, d_part_n, kStatBlocks, s.avg_edge_len, s.nscenes,
+                                   s.group_bits, nslots, d_grid);
+    RIGC_TRY(c.bp_sig.reserve(nslots * sizeof(int)));
+    RIGC_TRY(c.bp_ec0.reserve((size_t)ntot * sizeof(uint64_t) + 8));
+    RIGC_TRY(c.bp_eext.reserve((size_t)ntot * sizeof(uint32_t) + 8));
+    RIGC_TRY(c.bp_f32.reserve((size_t)ntot * 6 * sizeof(float) + 8));
+    RIGC_TRY(c.bp_cnt.reserve((size_t)(2 * ntot + 2) * sizeof(int32_t)));
+    RIGC_TRY(c.large_list.reserve((size_t)(ntot + 1) * sizeof(uint32_t)));
+    RIGC_CUDA(cudaMemsetAsync(c.bp_sig.ptr, 0xff, nslots * sizeof(int), st));
+    RIGC_CUDA(cudaMemsetAsync(d_count, 0, 2 * sizeof(int32_t), st));
+    int32_t* icnt = c.bp_cnt.as<int32_t>();
+    int32_t* ioff = icnt + ntot + 1;
     RIGC_COUNT_LAUNCH();
-    k_elem_bounds<<<nbk, 256, 0, st>>>(elems, m, c.vbox.as<double>(), c.ebox.as<double>(),
-                                       c.fbox.as<double>(), part, ext);
-    double* d_sum = reinterpret_cast<double*>(c.d_scalars.as<char>() + 512);
-    RIGC_TRY(sum_f64(ext, m, d_sum, S[7], st));
-    std::vector<double> hpart(6 * nbk);
-    double hsum;
-    RIGC_CUDA(cudaMemcpyAsync(hpart.data(), part, hpart.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
-    RIGC_CUDA(cudaMemcpyAsync(&hsum, d_sum, sizeof(double), cudaMemcpyDeviceToHost, st));
-    // count included edges for the mean extent
-    RIGC_CUDA(cudaStreamSynchronize(st));
-    Grid g;
-    double glo[3] = { INFINITY, INFINITY, INFINITY }, ghi[3] = { -INFINITY, -INFINITY, -INFINITY };
-    for (int b = 0; b < nbk; b++)
-        for (int j = 0; j < 3; j++) {
-            glo[j] = std::min(glo[j], hpart[6 * b + j]);
-            ghi[j] = std::max(ghi[j], hpart[6 * b + 3 + j]);
-        }
-    // cell size: mean extent of the included edge boxes
-    double cell = hsum / std::max(1, n_edges_in);
-    cell = std::max(cell, s.avg_edge_len * 0.5);
-    cell = std::max(cell, 1e-9);
-    for (int j = 0; j < 3; j++) g.lo[j] = glo[j];
-    for (;;) {
-        double tot = 1;
-        for (int j = 0; j < 3; j++) {
-            g.dims[j] = (long long)std::ceil((ghi[j] - glo[j]) / cell) + 1;
-            tot *= (double)g.dims[j];
-        }
-        if (tot < 4e12) break;
-        cell *= 2;
-    }
-    g.cell = cell;
-    g.grow = 1e-9 * cell;
-    uint64_t ncells = (uint64_t)g.dims[0] * g.dims[1] * g.dims[2];
-    const ElemScene es { s.vbody, s.ebody, s.fbody, s.bscene };
-    // positions of each scene's elements in elems, per type
-    RIGC_TRY(c.seg.reserve((size_t)(3 * (s.nscenes + 1) + 8) * sizeof(int32_t)));
-    int32_t* srange = c.seg.as<int32_t>();
+    k_mark_cells<<<grid_for(ntot, 256), 256, 0, st>>>(
+        E, s.bscene, s.grank, d_grid, c.bp_sig.as<int>(), nslots - 1, c.bp_ec0.as<uint64_t>(),
+        c.bp_eext.as<uint32_t>(), c.bp_f32.as<float>(), c.large_list.as<uint32_t>(), d_count + 1);
     RIGC_COUNT_LAUNCH();
-    k_scene_ranges<<<grid_for(s.nscenes + 1, 128), 128, 0, st>>>(
-        pos, s.scene_bstart, s.bvs, s.bes, s.bfs, s.nscenes, s.nv, s.ne, s.nf, m, srange);
-    // ---- 4. items
-    RIGC_TRY(S[3].reserve((size_t)(3 * m + 16) * sizeof(int32_t)));
-    int32_t* icnt = S[3].as<int32_t>();
-    int32_t* ioff = icnt + m;
-    int32_t* lflag = ioff + m;
-    RIGC_COUNT_LAUNCH();
-    k_count_cells<<<grid_for(m, 256), 256, 0, st>>>(elems, m, c.vbox.as<double>(), c.ebox.as<double>(),
-                                                   c.fbox.as<double>(), g, icnt, lflag);
-    RIGC_TRY(exclusive_scan_i32(icnt, ioff, m, cnt_dev, S[7], st));
-    RIGC_TRY(S[6].reserve((size_t)(m + 16) * sizeof(int32_t)));
-    int32_t* lpos = S[6].as<int32_t>();
-    RIGC_TRY(exclusive_scan_i32(lflag, lpos, m, cnt_dev + 1, S[7], st));
+    k_count_items<<<grid_for(ntot, 256), 256, 0, st>>>(
+        E, s.bscene, d_grid, c.bp_sig.as<int>(), nslots - 1, c.bp_ec0.as<uint64_t>(),
+        c.bp_eext.as<uint32_t>(), icnt);
+    RIGC_TRY(exclusive_scan_i32(icnt, ioff, ntot, d_count, S[7], st));
+    // the host sizes the item buffers and the sort: one read-back
+    Grid hg;
     int32_t counts[2];
-    RIGC_CUDA(cudaMemcpyAsync(counts, cnt_dev, sizeof(counts), cudaMemcpyDeviceToHost, st));
+    RIGC_CUDA(cudaMemcpyAsync(counts, d_count, sizeof(counts), cudaMemcpyDeviceToHost, st));
+    RIGC_CUDA(cudaMemcpyAsync(&hg, d_grid, sizeof(Grid), cudaMemcpyDeviceToHost, st));
     RIGC_CUDA(cudaStreamSynchronize(st));
     const int64_t nitems = counts[0];
     const int nlarge = counts[1];
     c.stats.grid_items = nitems;
     c.stats.large_elements = nlarge;
+    // ---- 4. items of the marked cells, sorted
     RIGC_TRY(c.items_key.reserve((size_t)nitems * 8 + 8));
     RIGC_TRY(c.items_val.reserve((size_t)nitems * 4 + 8));
     RIGC_TRY(c.items_key2.reserve((size_t)nitems * 8 + 8));
     RIGC_TRY(c.items_val2.reserve((size_t)nitems * 4 + 8));
-    RIGC_COUNT_LAUNCH();
-    k_emit_items<<<grid_for(m, 256), 256, 0, st>>>(elems, m, c.vbox.as<double>(), c.ebox.as<double>(),
-                                                  c.fbox.as<double>(), g, es, ncells, icnt, ioff,
-                                                  c.items_key.as<uint64_t>(), c.items_val.as<uint32_t>());
-    RIGC_TRY(radix_sort_pairs<uint64_t>(c.items_key.as<uint64_t>(), c.items_val.as<uint32_t>(),
-                                        c.items_key2.as<uint64_t>(), c.items_val2.as<uint32_t>(),
-                                        nitems, bits_for(ncells * (uint64_t)s.nscenes - 1), S[4],
-                                        S[5], S[7], st));
-    RIGC_TRY(c.large_list.reserve((size_t)(nlarge + 1) * sizeof(uint32_t)));
-    RIGC_COUNT_LAUNCH();
-    k_large_list<<<grid_for(m, 256), 256, 0, st>>>(elems, lflag, lpos, m, c.large_list.as<uint32_t>());
+    if (nitems > 0) {
+        RIGC_COUNT_LAUNCH();
+        k_emit_items<<<grid_for(ntot, 256), 256, 0, st>>>(
+            E, s.bscene, s.grank, d_grid, c.bp_sig.as<int>(), nslots - 1, c.bp_ec0.as<uint64_t>(),
+            c.bp_eext.as<uint32_t>(), icnt, ioff, s.group_bits, c.items_key.as<uint64_t>(),
+            c.items_val.as<uint32_t>());
+        RIGC_TRY(radix_sort_pairs<uint64_t>(c.items_key.as<uint64_t>(), c.items_val.as<uint32_t>(),
+                                            c.items_key2.as<uint64_t>(), c.items_val2.as<uint32_t>(),
+                                            nitems, hg.key_bits + s.group_bits + 3, S[4], S[5], S[7],
+                                            st));
+    }
     // ---- 5. pairs (retry once with exact capacity on overflow)
-    PairCtx P { c.vbox.as<double>(), c.ebox.as<double>(), c.fbox.as<double>(), s.vbody, s.ebody,
-                s.fbody, s.group, s.nv, s.ne };
     unsigned long long* pn = reinterpret_cast<unsigned long long*>(c.d_scalars.as<char>() + 1024);
     unsigned long long cap_ee = std::max<unsigned long long>(1 << 16, (unsigned long long)nitems);
     unsigned long long cap_fv = cap_ee;
+    cap_ee = std::max<unsigned long long>(cap_ee, (unsigned long long)c.bp_pair_hint[0]);
+    cap_fv = std::max<unsigned long long>(cap_fv, (unsigned long long)c.bp_pair_hint[1]);
+    const float* f32 = c.bp_f32.as<float>();
     for (int attempt = 0; attempt < 3; attempt++) {
         RIGC_TRY(c.pair_out.reserve((size_t)(cap_ee + cap_fv) * 8));
         PairOut o { c.pair_out.as<unsigned long long>(), c.pair_out.as<unsigned long long>() + cap_ee,
                     cap_ee, cap_fv, pn, pn + 1 };
         RIGC_CUDA(cudaMemsetAsync(pn, 0, 2 * sizeof(unsigned long long), st));
-        if (nitems > 0 && nitems <= kWarpPairItems) {
+        if (nitems > 0) {
             RIGC_COUNT_LAUNCH();
-            k_cell_pairs_warp<<<grid_for(nitems * 32, 128), 128, 0, st>>>(
-                c.items_key2.as<uint64_t>(), c.items_val2.as<uint32_t>(), nitems, P, g, es, ncells, o);
-        } else if (nitems > 0) {
-            RIGC_COUNT_LAUNCH();
-            k_cell_pairs<<<grid_for(nitems, 128), 128, 0, st>>>(c.items_key2.as<uint64_t>(),
-                                                              c.items_val2.as<uint32_t>(), nitems, P, g,
-                                                              es, ncells, o);
+            k_cell_pairs<<<grid_for(nitems, 128), 128, 0, st>>>(
+                c.items_key2.as<uint64_t>(), c.items_val2.as<uint32_t>(), nitems, s.group_bits, kind,
+                E, f32, o);
         }
         if (nlarge > 0) {
             // enough blocks per large element to cover a whole scene's elements
             const unsigned bx = (unsigned)std::min<int64_t>(
-                1024, std::max<int64_t>(1, ((int64_t)m / s.nscenes + 255) / 256));
+                1024, std::max<int64_t>(1, (ntot / s.nscenes + 255) / 256));
             for (int row0 = 0; row0 < nlarge; row0 += 65535) {
                 const unsigned rows = (unsigned)std::min(65535, nlarge - row0);
                 RIGC_COUNT_LAUNCH();
-                k_large_pairs<<<dim3(bx, rows), 256, 0, st>>>(c.large_list.as<uint32_t>(), nlarge, row0,
-                                                            elems, lflag, srange, s.nscenes, es, P, o);
+                k_large_pairs<<<dim3(bx, rows), 256, 0, st>>>(
+                    c.large_list.as<uint32_t>(), nlarge, row0, kind, E, s.bscene, s.scene_bstart, s.bvs,
+                    s.bes, s.bfs, s.grank, c.bp_eext.as<uint32_t>(), f32, o);
             }
         }
         RIGC_CUDA(cudaGetLastError());
@@ -878,20 +1085,26 @@ int detect_candidates(Ctx& c, const double* x0, const double* x1, bool continuou
         RIGC_CUDA(cudaMemcpyAsync(hn, pn, sizeof(hn), cudaMemcpyDeviceToHost, st));
         RIGC_CUDA(cudaStreamSynchronize(st));
         if (hn[0] <= cap_ee && hn[1] <= cap_fv) {
-            c.cand.num_ee = (int64_t)hn[0];
-            c.cand.num_fv = (int64_t)hn[1];
+            out.num_ee = (int64_t)hn[0];
+            out.num_fv = (int64_t)hn[1];
             break;
         }
         cap_ee = std::max(cap_ee, hn[0]);
         cap_fv = std::max(cap_fv, hn[1]);
+        c.bp_pair_hint[0] = std::max<int64_t>(c.bp_pair_hint[0], (int64_t)hn[0]);
+        c.bp_pair_hint[1] = std::max<int64_t>(c.bp_pair_hint[1], (int64_t)hn[1]);
         if (attempt == 2) return RIGC_ERR_OOM;
     }
     // ---- 6. canonical order
-    const int64_t nee = c.cand.num_ee, nfv = c.cand.num_fv;
+    const int64_t nee = out.num_ee, nfv = out.num_fv;
     unsigned long long* kee = c.pair_out.as<unsigned long long>();
     unsigned long long* kfv = kee + cap_ee;
-    RIGC_TRY(c.cand.ee.reserve((size_t)nee * sizeof(int2) + 8));
-    RIGC_TRY(c.cand.fv.reserve((size_t)nfv * sizeof(int2) + 8));
+    RIGC_TRY(out.ee.reserve((size_t)nee * sizeof(int2) + 8));
+    RIGC_TRY(out.fv.reserve((size_t)nfv * sizeof(int2) + 8));
+    // the second stream: (face, vertex) keys f * nv + v, or (face, edge)
+    // keys f * ne + e
+    const unsigned long long fv_stride = kind == kPairsEF ? (unsigned long long)s.ne
+                                                          : (unsigned long long)s.nv;
     int64_t nmax = std::max(nee, nfv);
     RIGC_TRY(c.pair_key.reserve((size_t)nmax * 8 + 8));
     RIGC_TRY(S[0].reserve((size_t)nmax * 4 + 8));
@@ -904,20 +1117,25 @@ int detect_candidates(Ctx& c, const double* x0, const double* x1, bool continuou
                                             bits_for((uint64_t)s.ne * (uint64_t)s.ne), S[4], S[5], S[7], st));
         RIGC_COUNT_LAUNCH();
         k_decode_pairs<<<grid_for(nee, 256), 256, 0, st>>>(c.pair_key.as<unsigned long long>(), nee,
-                                                          (unsigned long long)s.ne, c.cand.ee.as<int2>());
+                                                          (unsigned long long)s.ne, out.ee.as<int2>());
     }
     if (nfv > 0) {
         RIGC_COUNT_LAUNCH();
         k_iota<<<grid_for(nfv, 256), 256, 0, st>>>(S[0].as<uint32_t>(), nfv);
         RIGC_TRY(radix_sort_pairs<uint64_t>(reinterpret_cast<uint64_t*>(kfv), S[0].as<uint32_t>(), c.pair_key.as<uint64_t>(),
                                             S[1].as<uint32_t>(), nfv,
-                                            bits_for((uint64_t)s.nf * (uint64_t)s.nv), S[4], S[5], S[7], st));
+                                            bits_for((uint64_t)s.nf * fv_stride), S[4], S[5], S[7], st));
         RIGC_COUNT_LAUNCH();
         k_decode_pairs<<<grid_for(nfv, 256), 256, 0, st>>>(c.pair_key.as<unsigned long long>(), nfv,
-                                                          (unsigned long long)s.nv, c.cand.fv.as<int2>());
+                                                          fv_stride, out.fv.as<int2>());
     }
     RIGC_CUDA(cudaGetLastError());
     return RIGC_OK;
+}
+
+int detect_candidates(Ctx& c, const double* x0, const double* x1, bool continuous, double infl)
+{
+    return detect_pairs(c, x0, x1, continuous, infl, kPairsEEFV, c.cand);
 }
 
 } // namespace rigc

@@ -94,6 +94,8 @@ struct Scene {
     int* bes = nullptr;
     int* bfs = nullptr;
     int* group = nullptr;          // nb
+    int* grank = nullptr;          // nb: rank of the body's group among the distinct group ids
+    int group_bits = 1;            // bits of the largest rank
     int* type = nullptr;           // nb
     double* rmax = nullptr;        // nb
     int* vbody = nullptr;          // nv
@@ -154,6 +156,14 @@ struct Ctx {
     DevBuf body_box, body_in, vbox, ebox, fbox, vin, ein, fin;
     DevBuf items_key, items_val, items_key2, items_val2, seg, pair_out, pair_key;
     DevBuf large_list;
+    // hash grid: call state, half-interval frames, deeper-bisection flags,
+    // cell filter, per-element cell ranges, float boxes, item counts
+    DevBuf bp_misc, bp_frames, bp_deeper, bp_sig, bp_ec0, bp_eext, bp_f32, bp_cnt;
+    int64_t bp_pair_hint[2] = { 0, 0 };  // largest EE / FV pair counts seen
+    // rigc_min_distance / rigc_detect_intersections: world vertices, their
+    // rotation frames, the result; the edge-face intersection candidates
+    DevBuf md_V, md_rot, md_out;
+    Candidates isect;
     // temporary pose buffers for host entry points
     DevBuf x0_dev, x1_dev;
     // CCD: body frames over the top dyadic time intervals

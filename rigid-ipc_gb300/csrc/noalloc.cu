@@ -20,6 +20,10 @@
 //  * every call shares the array and it keeps the last call's contents;
 //    each call rewrites all frames it reads before reading them, and calls
 //    that overlap on the GPU race, so serialise them on one stream;
+//  * constraint indices are checked on the device against num_bodies and
+//    num_vertices; a constraint with an index out of range gets NaN energy,
+//    gradient and Hessian and reads nothing (a host-side check would need a
+//    copy of the device arrays and a synchronisation);
 //  * nothing here allocates: no cudaMalloc, cudaFree or allocating library
 //    call.
 #include <mutex>
@@ -34,7 +38,7 @@ constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) double g_noalloc_frames[(size_t)kMaxBodies * kFrameStride];
 
-int launch_barrier_local_raw(const double* rest, int nb, const double* x, int64_t n,
+int launch_barrier_local_raw(const double* rest, int64_t nv, int nb, const double* x, int64_t n,
                              const int* ctype, const int* cverts, const int* cbodies,
                              const double* cweight, const double* ceps, double dhat, double dmin,
                              int flags, double* frames, double* energy, double* grad,
@@ -61,13 +65,15 @@ static int frames_address(double** out)
 } // namespace rigc
 
 extern "C" int rigc_barrier_local_terms_noalloc(
-    const double* rest_vertices, int32_t num_bodies, const double* x, int64_t num_constraints,
+    const double* rest_vertices, int64_t num_vertices, int32_t num_bodies, const double* x,
+    int64_t num_constraints,
     const int32_t* type, const int32_t* verts, const int32_t* bodies, const double* weight,
     const double* eps_x, double dhat, double dmin, int flags, double* energy, double* grad,
     double* hess, void* cuda_stream)
 {
     using namespace rigc;
-    if (num_bodies < 0 || num_constraints < 0 || !(dhat > 0) || !(dmin >= 0)) return RIGC_ERR_ARG;
+    if (num_bodies < 0 || num_vertices < 0 || num_constraints < 0 || !(dhat > 0) || !(dmin >= 0))
+        return RIGC_ERR_ARG;
     if (num_bodies > kMaxBodies) {
         set_error(RIGC_ERR_TOO_LARGE, "num_bodies exceeds RIGC_NOALLOC_MAX_BODIES", __FILE__,
                   __LINE__);
@@ -80,7 +86,12 @@ extern "C" int rigc_barrier_local_terms_noalloc(
     if (num_bodies == 0) return num_constraints == 0 ? RIGC_OK : RIGC_ERR_ARG;
     double* frames = nullptr;
     RIGC_TRY(frames_address(&frames));
-    return launch_barrier_local_raw(rest_vertices, num_bodies, x, num_constraints, type, verts,
+    // the constraint arrays are device memory the host cannot inspect without
+    // a copy and a synchronisation: the kernel checks every type, vertex and
+    // body index against these limits and gives an out-of-range constraint
+    // NaN outputs instead of reading past an array
+    return launch_barrier_local_raw(rest_vertices, num_vertices, num_bodies, x, num_constraints,
+                                    type, verts,
                                     bodies, weight, eps_x, dhat, dmin, flags, frames, energy,
                                     grad, hess, static_cast<cudaStream_t>(cuda_stream));
 }

@@ -2534,3 +2534,38 @@ void sim_release(Ctx& c)
 }
 
 } // namespace rigc
+
+// DistanceBarrierRBProblem::compute_min_distance(x)
+// (src/problems/distance_barrier_rb_problem.cpp:1583-1589) over
+// DistanceBarrierConstraint::compute_minimum_distance
+// (src/opt/distance_barrier_constraint.cpp:308-323): the constraint set at x,
+// the smallest squared distance over it, its square root, -1 when the set is
+// empty (an infinite minimum).
+extern "C" int rigc_min_distance(rigc_ctx* ctx, const double* x, double dhat, double dmin,
+                                 double* min_distance)
+{
+    using namespace rigc;
+    if (!ctx || !x || !min_distance || !(dhat > 0) || !(dmin >= 0)) return RIGC_ERR_ARG;
+    Ctx& c = *ctx_of(ctx);
+    RIGC_TRY(build_constraints(c, x, dhat, dmin));
+    const int64_t n = c.cons.num;
+    if (n == 0) {
+        *min_distance = -1;
+        return RIGC_OK;
+    }
+    RIGC_TRY(c.md_V.reserve((size_t)3 * c.s.nv * sizeof(double) + 8));
+    RIGC_TRY(c.md_out.reserve(sizeof(unsigned long long)));
+    RIGC_TRY(compute_world_vertices_rn(c, x, c.md_V.as<double>(), c.md_rot));
+    unsigned long long* out = c.md_out.as<unsigned long long>();
+    const unsigned long long inf = 0x7ff0000000000000ull;
+    RIGC_CUDA(cudaMemcpyAsync(out, &inf, sizeof(inf), cudaMemcpyHostToDevice, c.stream));
+    RIGC_COUNT_LAUNCH();
+    k_min_constraint_distance<<<grid_for(n, 256), 256, 0, c.stream>>>(
+        n, c.cons.type.as<int>(), c.cons.verts.as<int>(), c.md_V.as<double>(), out);
+    RIGC_CUDA(cudaGetLastError());
+    double d2;
+    RIGC_CUDA(cudaMemcpyAsync(&d2, out, sizeof(d2), cudaMemcpyDeviceToHost, c.stream));
+    RIGC_CUDA(cudaStreamSynchronize(c.stream));
+    *min_distance = std::isfinite(d2) ? std::sqrt(d2) : -1;
+    return RIGC_OK;
+}

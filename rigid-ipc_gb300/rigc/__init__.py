@@ -16,7 +16,7 @@ import numpy as np
 from . import _lib as L
 from .scene import Scene  # noqa: F401
 
-__all__ = ["Context", "Scene", "L"]
+__all__ = ["Context", "Scene", "L", "fp64_throughput"]
 
 
 def _torch():
@@ -25,6 +25,20 @@ def _torch():
     if not torch.cuda.is_available():
         raise RuntimeError("rigc needs a CUDA device")
     return torch
+
+
+def fp64_throughput(op="dfma", active_lanes=32, iters=4096):
+    """FP64 issue throughput of the current device (rigc_fp64_throughput):
+    dict with ms, warp-level instructions per second and lane-level GFLOP/s."""
+    _torch()
+    lib = L.load()
+    ms, wi, fl = C.c_double(), C.c_double(), C.c_double()
+    L.check(lib.rigc_fp64_throughput({"dfma": 0, "dadd": 1}[op], active_lanes, iters,
+                                     C.byref(ms), C.byref(wi), C.byref(fl)),
+            "rigc_fp64_throughput")
+    return {"op": op, "active_lanes": active_lanes, "ms": ms.value,
+            "warp_inst_per_s": wi.value / (ms.value * 1e-3),
+            "gflops": fl.value / (ms.value * 1e-3) / 1e9}
 
 
 class Context:
@@ -211,6 +225,24 @@ class Context:
             eps=self.copy_out(v.eps_x, (n,), np.float64),
             counts=(v.num_vv, v.num_ev, v.num_ee, v.num_fv),
         )
+
+    def compute_min_distance(self, x, dhat, dmin=0.0):
+        """DistanceBarrierRBProblem::compute_min_distance(x): the smallest
+        constraint distance at x, -1 when the constraint set is empty."""
+        xd = self.device(x)
+        d = C.c_double()
+        L.check(self.lib.rigc_min_distance(self.h, C.c_void_p(xd.data_ptr()), dhat, dmin,
+                                           C.byref(d)), "rigc_min_distance")
+        return d.value
+
+    def detect_intersections(self, x):
+        """RigidBodyProblem::detect_intersections: the number of (edge, face)
+        pairs of different bodies that cross at poses x (0: intersection-free)."""
+        xd = self.device(x)
+        n = C.c_int64()
+        L.check(self.lib.rigc_detect_intersections(self.h, C.c_void_p(xd.data_ptr()), C.byref(n)),
+                "rigc_detect_intersections")
+        return n.value
 
     def set_constraints(self, types, verts, prims, bodies, weight, eps):
         arrs = [np.ascontiguousarray(types, np.int32), np.ascontiguousarray(verts, np.int32),

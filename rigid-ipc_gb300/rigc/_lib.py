@@ -36,7 +36,8 @@ EXPORTS = [
     "rigc_set_candidates", "rigc_set_ccd_budget", "rigc_sim_init", "rigc_sim_step",
     "rigc_sim_get_state", "rigc_ctx_create_batched", "rigc_num_scenes", "rigc_scene_tois",
     "rigc_scene_barrier_energies", "rigc_sim_rollout", "rigc_sim_backward",
-    "rigc_sim_scene_params", "rigc_autotune", "rigc_set_tune",
+    "rigc_sim_scene_params", "rigc_autotune", "rigc_set_tune", "rigc_fp64_throughput",
+    "rigc_min_distance", "rigc_detect_intersections",
 ]
 RIGC_ERR_TOO_LARGE = 7
 RIGC_ERR_SOLVE = 8
@@ -155,8 +156,11 @@ def load():
     L.rigc_narrow_phase_host.argtypes = [_vp, _vp, _vp, C.c_double, C.c_double, _d, _d, _vp, _vp,
                                          _vp, _vp, C.c_int64, _i64]
     L.rigc_body_energy.argtypes = [_vp, C.POINTER(BodyState), _vp, _d, C.c_double, _d, _vp, _vp]
+    L.rigc_fp64_throughput.argtypes = [C.c_int32, C.c_int32, C.c_int32, _d, _d, _d]
+    L.rigc_min_distance.argtypes = [_vp, _vp, C.c_double, C.c_double, _d]
+    L.rigc_detect_intersections.argtypes = [_vp, _vp, _i64]
     L.rigc_barrier_local_terms_noalloc.argtypes = [
-        _vp, C.c_int32, _vp, C.c_int64, _vp, _vp, _vp, _vp, _vp, C.c_double, C.c_double,
+        _vp, C.c_int64, C.c_int32, _vp, C.c_int64, _vp, _vp, _vp, _vp, _vp, C.c_double, C.c_double,
         C.c_int, _vp, _vp, _vp, _vp]
     L.rigc_friction_setup.argtypes = [_vp, _vp, C.c_double, C.c_double, C.c_double, _i64]
     L.rigc_get_friction.argtypes = [_vp, C.POINTER(FrictionView)]

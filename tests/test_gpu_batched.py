@@ -3,6 +3,8 @@ context give exactly the per-scene results of one context per scene --
 candidate sets (with index offsets), per-scene earliest times of impact,
 constraint sets, per-scene barrier energies (1e-12: summed in another order)
 and the gradient (bit for bit)."""
+import os
+
 import numpy as np
 import pytest
 
@@ -11,6 +13,7 @@ from conftest import contact_poses
 pytestmark = pytest.mark.gpu
 
 DHAT = 1e-3
+ENERGY_RTOL = 1e-10
 
 
 def _scenes():
@@ -149,3 +152,71 @@ def test_autotune_keeps_results():
     cb.set_tune(1, 256, 4, 3)
     c = run()
     assert a[0] == c[0] and a[3] == c[3] and np.array_equal(a[4], c[4])
+
+
+def test_batched_hull_scenes_match_oracle(oracle):
+    """Eight scenes of the batched benchmark (convex hulls of 32 random
+    unit-sphere points in seeded piles on their own planes, bench._hull_scene)
+    in one batched context, each scene against the oracle run on that scene
+    alone: continuous and discrete candidate sets and per-scene earliest
+    times of impact bit for bit, constraint sets bit for bit, per-scene
+    barrier energies and the gradient to 1e-10."""
+    import bench
+    import rigc
+    from rigc import scene as S
+
+    from test_gpu_parity import _canon_constraints
+
+    items = [bench._hull_scene(10_000 + k) for k in range(8)]
+    scenes = [sc for sc, _, _ in items]
+    big, sob = S.concat_scenes(scenes)
+    X0 = np.concatenate([x for _, x, _ in items])
+    X1 = np.concatenate([x for _, _, x in items])
+    cb = rigc.Context(big, scene_of_body=sob)
+    ee_b, fv_b = cb.detect_collision_candidates_rigid(X0, X1, True, 0.0)
+    cb.compute_earliest_toi(X0, X1)
+    tois_b = cb.scene_tois()
+    eed_b, fvd_b = cb.detect_collision_candidates_rigid(X0, X0, False, DHAT / 2)
+    cs_b = cb.construct_constraint_set(X0, DHAT)
+    e_b, g_b, _ = cb.compute_barrier_term(X0, DHAT)
+    se_b = cb.scene_barrier_energies()
+
+    ee_o, fv_o, eed_o, fvd_o, tois_o, grads_o, cons_o = [], [], [], [], [], [], []
+    vo = eo = fo = bo = 0
+    for sc, x0, x1 in items:
+        o = oracle.OracleScene(sc)
+        ee, fv = o.detect_candidates(x0, x1, True, 0.0)
+        tois_o.append(o.earliest_toi(x0, x1, ee, fv, nthreads=os.cpu_count() or 1,
+                                     max_boxes=1 << 22))
+        ee_o.append(ee + eo)
+        fv_o.append(fv + np.array([fo, vo]))
+        eed, fvd = o.detect_candidates(x0, continuous=False, inflation=DHAT / 2)
+        eed_o.append(eed + eo)
+        fvd_o.append(fvd + np.array([fo, vo]))
+        cs = o.constraint_set(x0, eed, fvd, DHAT)
+        e, g, _ = o.barrier_term(x0, cs, DHAT)
+        grads_o.append((e, g))
+        # global indices: vertices, edges, faces and bodies after the
+        # earlier scenes' (prims: VV (v, v), EV (e, v), EE (e, e), FV (f, v))
+        prim_off = np.array([[vo, vo], [eo, vo], [eo, eo], [fo, vo]])[cs.types]
+        cons_o.append((cs.types, np.where(cs.verts >= 0, cs.verts + vo, cs.verts),
+                       cs.prims + prim_off, cs.bodies + bo, cs.weight, cs.eps))
+        vo += sc.num_vertices
+        eo += len(sc.edges)
+        fo += len(sc.faces)
+        bo += sc.num_bodies
+    assert sum(len(e) for e in ee_o) > 0 and sum(len(f) for f in fv_o) > 0
+    assert np.array_equal(ee_b, np.concatenate(ee_o))
+    assert np.array_equal(fv_b, np.concatenate(fv_o))
+    assert np.array_equal(eed_b, np.concatenate(eed_o))
+    assert np.array_equal(fvd_b, np.concatenate(fvd_o))
+    assert np.array_equal(tois_b, np.array(tois_o))
+    a = _canon_constraints(*[np.concatenate([c[k] for c in cons_o]) for k in range(6)])
+    b = _canon_constraints(cs_b["type"], cs_b["verts"], cs_b["prims"], cs_b["bodies"],
+                           cs_b["weight"], cs_b["eps"])
+    for u, v in zip(a, b):
+        assert np.array_equal(u, v)
+    for k, (e, g) in enumerate(grads_o):
+        assert abs(se_b[k] - e) <= ENERGY_RTOL * max(abs(e), 1e-300)
+    g_o = np.concatenate([g for _, g in grads_o])
+    assert np.abs(g_b - g_o).max() <= ENERGY_RTOL * max(np.abs(g_o).max(), 1e-300)

@@ -294,3 +294,22 @@ def test_chain_links_parity(oracle):
     e_o, g_o, _ = o.barrier_term(x0, cs_o, dhat)
     assert abs(e_g - e_o) <= ENERGY_RTOL * abs(e_o)
     assert _rel_err(g_g, g_o) <= GRAD_RTOL
+
+
+def test_min_distance(oracle, cube_scene, cube_contact, ctx_c1):
+    """compute_min_distance at the stacked contact (constraints present) and
+    at the lattice poses (no constraint: -1) against the oracle; the minimum
+    is bit-exact (the same round-to-nearest distances, a min)."""
+    dhat = 1e-3
+    o = oracle.OracleScene(cube_scene)
+    d_o = o.min_distance(cube_contact, dhat)
+    d_g = ctx_c1.compute_min_distance(cube_contact, dhat)
+    assert 0 < d_o < dhat
+    assert d_g == d_o
+    x = cube_scene.poses()
+    assert o.min_distance(x, dhat) == -1
+    assert ctx_c1.compute_min_distance(x, dhat) == -1
+    # with dmin the set grows (inflation (dhat + dmin) / 2) and the same
+    # distances enter it
+    assert ctx_c1.compute_min_distance(cube_contact, dhat, 2e-4) == o.min_distance(
+        cube_contact, dhat, 2e-4)
