@@ -74,6 +74,8 @@ def parse():
                     help="skip the per-configuration pass rates")
     ap.add_argument("--no-adjoint", action="store_true",
                     help="skip the differentiable rollout measurement")
+    ap.add_argument("--no-barrier", action="store_true",
+                    help="skip the barrier-terms-at-scale measurement (slab stacks)")
     ap.add_argument("--sim-steps", type=int, default=20)
     ap.add_argument("--batch-sim-steps", type=int, default=2,
                     help="timed steps of the batched time step (0 skips it)")
@@ -151,6 +153,18 @@ def measured_peaks():
             d = json.load(f)
         return float(d.get("hbm_gbs", 6800.0)), "measured"
     return 6800.0, "fallback"
+
+
+def broad_phase_roofline(sc, n_pairs, t, peak, peak_kind):
+    """The continuous broad phase against its algorithmic bytes: rest
+    vertices read (24 B each), two poses per body (96 B), an interval box
+    written per vertex, edge and face (48 B), a candidate pair written (8 B)."""
+    nv, ne, nf, nb = sc.num_vertices, len(sc.edges), len(sc.faces), sc.num_bodies
+    b = nv * 24 + nb * 96 + (nv + ne + nf) * 48 + n_pairs * 8
+    achieved = b / t / 1e9
+    return {"kernel": "continuous broad phase (all its launches)", "bound": "hbm",
+            "algorithmic_bytes": b, "ms": t * 1e3, "achieved": achieved, "peak": peak,
+            "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind}
 
 
 def fp64_peak():
@@ -319,11 +333,70 @@ def settled(sc, steps, dhat, dt):
     return P.reshape(-1), x1.reshape(-1)
 
 
+BARRIER_WORKLOAD = ("{n}x{n} columns of 2 tessellated slabs (1 x 0.2 x 1 m, faces of 32 x 32 "
+                    "quads, 2,562 vertices each) resting 0.3 mm apart and on a static plane; "
+                    "dhat 1e-3: constraint set, barrier energy, gradient, PSD-projected 12x12 "
+                    "Hessians with the rigid chain rule, BSR assembly")
+
+
+def barrier_rate(torch, n=4, reps=5):
+    """The barrier terms at scale: the slab stacks' constraint set (some 10^5
+    constraints), k_barrier_local alone (rigc_barrier_local_terms into device
+    buffers, CUDA events on the context's stream) against its algorithmic
+    bytes (1456 B per constraint), and the whole barrier pass (constraint set
+    + compute_barrier_term with the BSR assembly)."""
+    import rigc
+    from rigc import scene as S
+
+    sc = S.scene_from_json(S.spec_slab_stacks(0, nx=n, nz=n))
+    ctx = rigc.Context(sc)
+    dhat = sc.dhat
+    x0 = sc.poses()
+    xd = ctx.device(x0)
+    cs = ctx.construct_constraint_set(xd, dhat)
+    nc = len(cs["type"])
+    dev = dict(dtype=torch.float64, device="cuda")
+    e = torch.empty(nc, **dev)
+    g = torch.empty((nc, 12), **dev)
+    H = torch.empty((nc, 144), **dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    ctx.barrier_local_terms_device(xd, nc, dhat, e, g, H)  # warm-up
+
+    def timed(fn):
+        ts = []
+        for _ in range(reps):
+            flush.fill_(1.0)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b) / 1e3)
+        return statistics.median(ts)
+
+    t_local = timed(lambda: ctx.barrier_local_terms_device(xd, nc, dhat, e, g, H))
+    t_pass = timed(lambda: (ctx.construct_constraint_set(xd, dhat),
+                            ctx.compute_barrier_term(xd, dhat)))
+    peak, kind = measured_peaks()
+    achieved = BARRIER_BYTES_PER_CONSTRAINT * nc / t_local / 1e9
+    types = np.bincount(np.asarray(cs["type"]), minlength=4)
+    return {"workload": BARRIER_WORKLOAD.format(n=n), "bodies": sc.num_bodies,
+            "constraints": nc,
+            "constraint_types": {k: int(v) for k, v in zip(("vv", "ev", "ee", "fv"), types)},
+            "k_barrier_local_ms": t_local * 1e3, "barrier_pass_ms": t_pass * 1e3,
+            "barrier_constraints_per_s": nc / t_pass,
+            "roofline": {"kernel": "k_body_frames + k_barrier_local", "bound": "hbm",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": kind,
+                         "bytes_per_constraint": BARRIER_BYTES_PER_CONSTRAINT}}
+
+
 def per_config(args, torch):
     """Narrow-phase pass rates of the plain configurations beside the
     headline one: the 27-cube lattice and the 64-cube lattice after their
-    landings (40 steps), and the 200-link chain (links 1.501 m apart: at 1.5
-    they touch, see scene.spec_chain) after 10 steps of hanging."""
+    landings (40 steps), and the 200-link chain (links 1.499 m apart, a 1 mm
+    gap: at 1.5 they touch, see scene.spec_chain) once the links hang on each
+    other (the constraint set at the current poses is not empty)."""
     import rigc
     from rigc import scene as S
 
@@ -337,7 +410,13 @@ def per_config(args, torch):
     sc = S.scene_from_json(S.spec_chain(spacing=1.499))
     c = rigc.Context(sc)
     c.sim_init(0.005, (0.0, -9.81, 0.0), 1e-4)
-    c.sim_step(5)
+    hanging = 0
+    for _ in range(40):
+        c.sim_step(5)
+        hanging += 5
+        P, _, _, _ = c.sim_state()
+        if len(c.construct_constraint_set(P.reshape(-1), 1e-4)["type"]) > 0:
+            break
     torch.cuda.synchronize()
     t = time.perf_counter()
     st = c.sim_step(5)
@@ -349,6 +428,7 @@ def per_config(args, torch):
     x1[dyn, :3] += 0.005 * V[dyn, :3]
     x1[dyn, 1] -= 9.81 * 0.005 ** 2
     r = pass_rates_tuned(rigc.Context(sc), P.reshape(-1), x1.reshape(-1), 1e-4, torch)
+    r["steps_before"] = hanging
     r["steps_per_s"] = 5 / dt
     r["newton_iterations_per_step"] = st["newton_iterations"] / 5
     r["cg_iterations_per_newton"] = st["cg_iterations"] / max(1, st["newton_iterations"])
@@ -706,6 +786,7 @@ def main():
                    "ccd_collisions": st["ccd_collisions"], "l2": "flushed (512 MiB write) "
                    "before every timed step", "parallelism": "replicas" if world > 1 else "1 GPU"},
         "phases_s": {"ccd_narrow": t_ccd, "ccd_broad": t_bp, "barrier_and_assembly": t_bar},
+        "broad_phase_roofline": broad_phase_roofline(sc, n_ccd, t_bp, peak, peak_kind),
         "ccd_pairs_per_s": n_ccd / t_ccd, "barrier_constraints_per_s": n_cons / t_bar,
         "roofline": {"bound": "hbm", "kernel": ccd_kernel, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak,
@@ -733,6 +814,8 @@ def main():
         line["adjoint"] = adjoint_rate(args, torch)
     if rank == 0 and not args.no_configs:
         line["per_config"] = per_config(args, torch)
+    if rank == 0 and not args.no_barrier:
+        line["barrier_at_scale"] = barrier_rate(torch)
     if rank == 0 and not args.no_cpu_baseline:
         base = cpu_baseline(sc, x0, x1, dhat)
         v = combined_rate(n_ccd, n_disc, base["ccd_pairs_per_s"], base["barrier_pairs_per_s"])

@@ -151,8 +151,9 @@ const char* rigc_status_string(int status);
 int rigc_get_stats(const rigc_ctx* ctx, rigc_stats* out);
 
 /* Copy bytes between any two addresses the device can see (host, pinned or
- * device; cudaMemcpyDefault) on the context's stream, then synchronise.  For
- * FFI callers without CUDA bindings. */
+ * device; cudaMemcpyDefault) on the context's stream, then synchronise
+ * (bytes 0: only wait for the context's stream).  For FFI callers without
+ * CUDA bindings. */
 int rigc_copy(rigc_ctx* ctx, void* dst, const void* src, size_t bytes);
 
 /* World vertices V = R(theta) v + p for all vertices (device in/out).

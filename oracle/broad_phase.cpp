@@ -362,4 +362,32 @@ void detect_candidates(
     out.fv.erase(std::unique(out.fv.begin(), out.fv.end()), out.fv.end());
 }
 
+// Edge-face intersection candidates at poses x: close bodies and element
+// boxes with no inflation (detect_intersection_candidates_rigid_bvh,
+// src/ccd/rigid/broad_phase.cpp:265-302), every (face, edge) pair of
+// different groups whose boxes overlap, tested pairwise over the close body
+// pairs (test-sized scenes: no grid); sorted, unique.
+void edge_face_candidates(const Scene& s, const double* x, std::vector<std::array<int, 2>>& out)
+{
+    out.clear();
+    if (s.nb <= 1) return;
+    auto pairs = close_bodies(s, x, x, 0.0);
+    if (pairs.empty()) return;
+    std::vector<AABB> vb, eb, fb;
+    std::vector<char> vi, ei, fi;
+    element_aabbs(s, x, x, false, 0.0, pairs, vb, eb, fb, vi, ei, fi);
+    for (const auto& bp : pairs)
+        for (int side = 0; side < 2; side++) {
+            const int be = bp[side], bf = bp[1 - side];
+            if (s.group[be] == s.group[bf]) continue;
+            for (int e = s.bes[be]; e < s.bes[be + 1]; e++) {
+                if (!ei[e]) continue;
+                for (int f = s.bfs[bf]; f < s.bfs[bf + 1]; f++)
+                    if (fi[f] && aabb_overlap(eb[e], fb[f])) out.push_back({ f, e });
+            }
+        }
+    std::sort(out.begin(), out.end());
+    out.erase(std::unique(out.begin(), out.end()), out.end());
+}
+
 } // namespace orc

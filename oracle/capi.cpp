@@ -211,6 +211,54 @@ int orc_constraint_set(
     return 0;
 }
 
+// orientation of d against the plane a b c: the sign of det[b - a, c - a,
+// d - a] in round-to-nearest double, fixed order
+static int orient_sign(const double* a, const double* b, const double* c, const double* d)
+{
+    const double u0 = b[0] - a[0], u1 = b[1] - a[1], u2 = b[2] - a[2];
+    const double v0 = c[0] - a[0], v1 = c[1] - a[1], v2 = c[2] - a[2];
+    const double w0 = d[0] - a[0], w1 = d[1] - a[1], w2 = d[2] - a[2];
+    const double c0 = v1 * w2 - v2 * w1;
+    const double c1 = v2 * w0 - v0 * w2;
+    const double c2 = v0 * w1 - v1 * w0;
+    const double det = (u0 * c0 + u1 * c1) + u2 * c2;
+    return det > 0 ? 1 : (det < 0 ? -1 : 0);
+}
+
+// the segment e0 e1 crosses the triangle t0 t1 t2 (orientation test: the
+// endpoints on different sides of the plane, not both on it, and the line
+// inside the triangle)
+static bool edge_crosses_triangle(const double* e0, const double* e1, const double* t0,
+                                  const double* t1, const double* t2)
+{
+    const int s0 = orient_sign(t0, t1, t2, e0), s1 = orient_sign(t0, t1, t2, e1);
+    if (s0 == s1) return false;
+    const int a = orient_sign(e0, e1, t0, t1), b = orient_sign(e0, e1, t1, t2),
+              c = orient_sign(e0, e1, t2, t0);
+    return (a >= 0 && b >= 0 && c >= 0) || (a <= 0 && b <= 0 && c <= 0);
+}
+
+// RigidBodyProblem::detect_intersections (src/physics/rigid_body_problem.cpp:
+// 289-360), 3D: the number of crossing (edge, face) pairs at poses x
+long long orc_detect_intersections(void* p, const double* x)
+{
+    const Scene& s = static_cast<OwnedScene*>(p)->s;
+    std::vector<std::array<int, 2>> fe;
+    edge_face_candidates(s, x, fe);
+    if (fe.empty()) return 0;
+    std::vector<double> V;
+    world_vertices(s, x, V);
+    long long n = 0;
+    for (const auto& c : fe) {
+        const int f = c[0], e = c[1];
+        if (edge_crosses_triangle(&V[3 * s.edges[2 * e]], &V[3 * s.edges[2 * e + 1]],
+                                  &V[3 * s.faces[3 * f]], &V[3 * s.faces[3 * f + 1]],
+                                  &V[3 * s.faces[3 * f + 2]]))
+            n++;
+    }
+    return n;
+}
+
 // DistanceBarrierRBProblem::compute_min_distance(x)
 // (src/problems/distance_barrier_rb_problem.cpp:1583-1589) over
 // DistanceBarrierConstraint::compute_minimum_distance

@@ -347,6 +347,9 @@ void body_bounding_box(
     const Scene& s, int b, const double* x0, const double* x1, double lo[3],
     double hi[3]);
 // close body pairs (close_bodies_bvh, rigid_body_assembler.cpp:307-356)
+// (face, edge) pairs of different groups whose boxes at x overlap
+void edge_face_candidates(const Scene& s, const double* x, std::vector<std::array<int, 2>>& out);
+
 std::vector<std::array<int, 2>> close_bodies(
     const Scene& s, const double* x0, const double* x1, double inflation);
 // element boxes; included flags per vertex/edge/face

@@ -54,6 +54,8 @@ def lib():
         L.orc_constraint_set.argtypes = [C.c_void_p, _d, _i, C.c_longlong, _i, C.c_longlong,
                                          C.c_double, C.c_double, _i, _i, _i, _i, _d, _d,
                                          C.c_longlong, _ll]
+        L.orc_detect_intersections.restype = C.c_longlong
+        L.orc_detect_intersections.argtypes = [C.c_void_p, _d]
         L.orc_min_distance.restype = C.c_double
         L.orc_min_distance.argtypes = [C.c_void_p, _d, C.c_double, C.c_double]
         L.orc_local_terms.argtypes = [C.c_void_p, _d, C.c_longlong, _i, _i, _i, _i, _d, _d,
@@ -215,6 +217,10 @@ class OracleScene:
         assert rc == 0
         m = n.value
         return Constraints(types[:m], verts[:m], prims[:m], bodies[:m], w[:m], eps[:m])
+
+    def detect_intersections(self, x):
+        """detect_intersections: the number of crossing (edge, face) pairs at x."""
+        return int(lib().orc_detect_intersections(self.h, _p(_dd(x), _d)))
 
     def min_distance(self, x, dhat, dmin=0.0):
         """compute_min_distance(x): the smallest constraint distance at x, -1

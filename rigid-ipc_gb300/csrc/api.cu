@@ -145,7 +145,7 @@ static void release_all(Ctx* c)
                        &c->fric.coef, &c->fric.v0c, &c->fric.V0, &c->fric.c_energy,
                        &c->fric.c_grad, &c->fric.c_blocks, &c->fric.grad, &c->fric.row_ptr,
                        &c->fric.col, &c->fric.val, &c->scene_toi, &c->scene_energy,
-                       &c->bp_misc, &c->bp_frames, &c->bp_deeper, &c->bp_sig, &c->bp_ec0,
+                       &c->bp_misc, &c->bp_deeper, &c->bp_sig, &c->bp_ec0,
                        &c->bp_eext, &c->bp_f32, &c->bp_cnt, &c->md_V, &c->md_rot,
                        &c->md_out, &c->isect.ee, &c->isect.fv };
     for (DevBuf* b : bufs) b->release();
@@ -340,9 +340,8 @@ int rigc_get_stats(const rigc_ctx* ctx, rigc_stats* out)
 int rigc_copy(rigc_ctx* ctx, void* dst, const void* src, size_t bytes)
 {
     if (!ctx || (bytes && (!dst || !src))) return RIGC_ERR_ARG;
-    if (bytes == 0) return RIGC_OK;
     Ctx& c = *ctx_of(ctx);
-    RIGC_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, c.stream));
+    if (bytes) RIGC_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, c.stream));
     RIGC_CUDA(cudaStreamSynchronize(c.stream));
     return RIGC_OK;
 }
@@ -429,6 +428,9 @@ int rigc_earliest_toi(rigc_ctx* ctx, const double* x0, const double* x1, double 
 {
     if (!ctx || !x0 || !x1 || !toi_host || !(toi_tol > 0)) return RIGC_ERR_ARG;
     Ctx& c = *ctx_of(ctx);
+    // the poses may have changed since the candidates were found: no frames
+    // are taken over from the broad phase
+    c.bp_table.valid = false;
     return run_ccd(c, x0, x1, toi_tol, flags, toi_host, per_candidate);
 }
 

@@ -215,8 +215,8 @@ __global__ void __launch_bounds__(kVBThreads)
 k_vertex_boxes_cont(const double* __restrict__ x0, const double* __restrict__ x1,
                     const double* __restrict__ rest, const int* __restrict__ bvs,
                     const int* __restrict__ body_in, const int* __restrict__ deeper,
-                    const double* __restrict__ domain, double infl, double* __restrict__ vbox,
-                    char* __restrict__ vin)
+                    const double* __restrict__ table, const double* __restrict__ domain,
+                    double infl, double* __restrict__ vbox, char* __restrict__ vin)
 {
     __shared__ double st_lo[kMaxTNodes], st_hi[kMaxTNodes];
     __shared__ int st_depth[kMaxTNodes];
@@ -262,8 +262,19 @@ k_vertex_boxes_cont(const double* __restrict__ x0, const double* __restrict__ x1
         }
         __syncthreads();
         const int nq = nbat;
-        if ((int)threadIdx.x < nq)
-            body_time_frame(x0, x1, b, b_lo[threadIdx.x], b_hi[threadIdx.x], sF[threadIdx.x]);
+        if ((int)threadIdx.x < nq) {
+            // nodes of depth <= 6 from the table (their intervals are the
+            // dyadic [k 2^-d, (k + 1) 2^-d], midpoints being exact), deeper
+            // ones computed here
+            const int d = b_depth[threadIdx.x];
+            if (d < 7) {
+                const int k = (int)ldexp(b_lo[threadIdx.x], d);
+                const double* f = table + ((size_t)b * kRotTableSlots + (1 << d) - 1 + k) * kRotTableEntry;
+                for (int j = 0; j < kHalfFrame; j++) sF[threadIdx.x][j] = f[j];
+            } else {
+                body_time_frame(x0, x1, b, b_lo[threadIdx.x], b_hi[threadIdx.x], sF[threadIdx.x]);
+            }
+        }
         __syncthreads();
         for (int idx = threadIdx.x; idx < nq * nvb; idx += blockDim.x) {
             const int k = idx / nvb, v = v0 + idx % nvb;
@@ -312,17 +323,26 @@ k_vertex_boxes_cont(const double* __restrict__ x0, const double* __restrict__ x1
     }
 }
 
-// interval frames of the two forced halves [0, 1/2] and [1/2, 1]: one thread
-// per (included body, half)
-__global__ void k_half_frames(const double* __restrict__ x0, const double* __restrict__ x1,
-                              const int* __restrict__ body_in, int nb, double* __restrict__ fr)
+// Interval frames of every included body over the dyadic time nodes of
+// depth 0 .. 6 (table slot 2^d - 1 + k for [k 2^-d, (k + 1) 2^-d]): the
+// forced halves and the nodes the deeper bisection visits first.  They are
+// the CCD's frames for the same poses (PoseI::interpolate through the same
+// interval operations; a product with a non-negative time interval gives
+// the same bits in either form), so the CCD that follows on these poses
+// takes them over.  One thread per (included body, node).
+constexpr int kBPTableNodes = 127;  // slots 0 .. 126: depths 0 .. 6
+
+__global__ void k_bp_frames(const double* __restrict__ x0, const double* __restrict__ x1,
+                            const int* __restrict__ body_in, int nb, double* __restrict__ table)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= 2 * nb) return;
-    const int b = t >> 1, half = t & 1;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (int64_t)nb * kBPTableNodes) return;
+    const int b = (int)(i / kBPTableNodes), slot = (int)(i % kBPTableNodes);
     if (!body_in[b]) return;
-    const double m = RMUL(0.5, RADD(0.0, 1.0));
-    body_time_frame(x0, x1, b, half ? m : 0.0, half ? 1.0 : m, fr + (size_t)t * kHalfFrame);
+    const int d = 31 - __clz(slot + 1);
+    const int k = slot + 1 - (1 << d);
+    body_time_frame(x0, x1, b, ldexp((double)k, -d), ldexp((double)(k + 1), -d),
+                    table + ((size_t)b * kRotTableSlots + slot) * kRotTableEntry);
 }
 
 // One thread per vertex: its interval positions over the two forced halves,
@@ -349,7 +369,7 @@ __global__ void k_vertex_boxes_half(const double* __restrict__ rest, const int* 
     bool fits = true;
     for (int half = 0; half < 2; half++) {
         Itv w[3];
-        vertex_at_frame(fr + (size_t)(2 * b + half) * kHalfFrame, rv, w);
+        vertex_at_frame(fr + ((size_t)b * kRotTableSlots + 1 + half) * kRotTableEntry, rv, w);
         for (int j = 0; j < 3; j++) {
             if (RSUB(w[j].lo, infl) < domain[j] || RADD(w[j].hi, infl) > domain[3 + j]) fits = false;
             lo[j] = smin(lo[j], w[j].lo);
@@ -431,6 +451,7 @@ __global__ void k_edge_face_boxes(const int* __restrict__ E, int ne, const int* 
 struct Grid {
     double lo[3];
     double cell, grow;
+    double inv_cell;            // RN(1 / cell): cell indices by multiplication
     long long dims[3];
     unsigned long long ncells;  // dims[0] * dims[1] * dims[2]
     int dense;                  // cell-filter slot = (scene, cell) key; else a hash of it
@@ -482,9 +503,13 @@ struct Elems {
     }
 };
 
+// Cell index along axis j: floor((x - lo) / cell) computed as a product with
+// the reciprocal.  Any index function works as long as it is monotone in x
+// and the same for every element (two boxes sharing a point share that
+// point's cell); round-to-nearest subtraction and multiplication are.
 __device__ __forceinline__ long long cell_of(double x, const Grid& g, int j)
 {
-    long long c = (long long)floor(RDIV(RSUB(x, g.lo[j]), g.cell));
+    long long c = (long long)floor(RMUL(RSUB(x, g.lo[j]), g.inv_cell));
     return c < 0 ? 0 : (c >= g.dims[j] ? g.dims[j] - 1 : c);
 }
 
@@ -601,10 +626,13 @@ __global__ void k_grid_setup(const double* __restrict__ part, const int* __restr
                              double avg_edge_len, int nscenes, int group_bits, uint64_t nslots,
                              Grid* __restrict__ out)
 {
+    // one warp reduces the partials in a fixed order (lane-strided, then a
+    // butterfly), lane 0 sets the grid up
+    const int lane = threadIdx.x & 31;
     double lo[3] = { INFINITY, INFINITY, INFINITY }, hi[3] = { -INFINITY, -INFINITY, -INFINITY };
     double ext = 0;
     long long ned = 0;
-    for (int b = 0; b < nblk; b++) {
+    for (int b = lane; b < nblk; b += 32) {
         for (int j = 0; j < 3; j++) {
             lo[j] = smin(lo[j], part[7 * b + j]);
             hi[j] = smax(hi[j], part[7 * b + 3 + j]);
@@ -612,6 +640,17 @@ __global__ void k_grid_setup(const double* __restrict__ part, const int* __restr
         ext = RADD(ext, part[7 * b + 6]);
         ned += part_n[b];
     }
+    for (int o = 16; o > 0; o >>= 1) {
+        for (int j = 0; j < 3; j++) {
+            lo[j] = smin(lo[j], __shfl_xor_sync(0xffffffffu, lo[j], o));
+            hi[j] = smax(hi[j], __shfl_xor_sync(0xffffffffu, hi[j], o));
+        }
+        // the same sum in both lanes of a pair: lower lane's value first
+        const double e2 = __shfl_xor_sync(0xffffffffu, ext, o);
+        ext = (lane & o) ? RADD(e2, ext) : RADD(ext, e2);
+        ned += __shfl_xor_sync(0xffffffffu, ned, o);
+    }
+    if (lane != 0) return;
     Grid g;
     bool empty = false;
     for (int j = 0; j < 3; j++)
@@ -644,7 +683,11 @@ __global__ void k_grid_setup(const double* __restrict__ part, const int* __restr
     }
     for (int j = 0; j < 3; j++) g.lo[j] = empty ? 0.0 : lo[j];
     g.cell = cell;
-    g.grow = 1e-9 * cell;
+    g.inv_cell = 1.0 / cell;
+    // The margin makes boxes that the round-to-nearest overlap test accepts
+    // (disjoint by at most a few ulps) share a cell even after the rounding
+    // of the index computation (at most a few ulps of dims, 2^21 at most).
+    g.grow = 1e-7 * cell;
     g.ncells = tot;
     const unsigned long long keys = (unsigned long long)nscenes * tot;
     g.dense = keys <= nslots ? 1 : 0;
@@ -905,6 +948,7 @@ __global__ void k_iota(uint32_t* __restrict__ v, int64_t n)
 // ---------------------------------------------------------------------------
 
 int body_rot_rn(Ctx& c, const double* x, double* out);
+int reserve_rot_table(Ctx& c);
 
 // slots of the cell filter for ntot elements: a power of two, about four per
 // element (elements cover a few cells each), 2^16 .. 2^27
@@ -923,6 +967,7 @@ int detect_pairs(Ctx& c, const double* x0, const double* x1, bool continuous, do
     Scene& s = c.s;
     cudaStream_t st = c.stream;
     out.num_ee = out.num_fv = 0;
+    c.bp_table.valid = false;
     c.stats.grid_items = 0;
     c.stats.large_elements = 0;
     if (s.nb <= 1) return RIGC_OK;
@@ -966,22 +1011,23 @@ int detect_pairs(Ctx& c, const double* x0, const double* x1, bool continuous, do
     RIGC_TRY(c.ein.reserve((size_t)s.ne + 8));
     RIGC_TRY(c.fin.reserve((size_t)s.nf + 8));
     if (continuous) {
-        RIGC_TRY(c.bp_frames.reserve((size_t)2 * s.nb * kHalfFrame * sizeof(double)));
+        RIGC_TRY(reserve_rot_table(c));
         RIGC_TRY(c.bp_deeper.reserve((size_t)s.nb * sizeof(int)));
+        double* table = c.rot_table.as<double>();
         RIGC_COUNT_LAUNCH();
         k_scene_box<<<1, 256, 0, st>>>(c.body_box.as<double>(), c.body_in.as<int>(), s.nb, d_domain);
         RIGC_COUNT_LAUNCH();
-        k_half_frames<<<grid_for(2 * (int64_t)s.nb, 128), 128, 0, st>>>(
-            x0, x1, c.body_in.as<int>(), s.nb, c.bp_frames.as<double>());
+        k_bp_frames<<<grid_for((int64_t)s.nb * kBPTableNodes, 128), 128, 0, st>>>(
+            x0, x1, c.body_in.as<int>(), s.nb, table);
         RIGC_CUDA(cudaMemsetAsync(c.bp_deeper.ptr, 0, (size_t)s.nb * sizeof(int), st));
         RIGC_COUNT_LAUNCH();
         k_vertex_boxes_half<<<grid_for(s.nv, 128), 128, 0, st>>>(
-            s.rest, s.vbody, c.body_in.as<int>(), s.nv, c.bp_frames.as<double>(), d_domain, infl,
+            s.rest, s.vbody, c.body_in.as<int>(), s.nv, table, d_domain, infl,
             c.vbox.as<double>(), c.vin.as<char>(), c.bp_deeper.as<int>());
         RIGC_COUNT_LAUNCH();
         k_vertex_boxes_cont<<<(unsigned)s.nb, kVBThreads, 0, st>>>(
-            x0, x1, s.rest, s.bvs, c.body_in.as<int>(), c.bp_deeper.as<int>(), d_domain, infl,
-            c.vbox.as<double>(), c.vin.as<char>());
+            x0, x1, s.rest, s.bvs, c.body_in.as<int>(), c.bp_deeper.as<int>(), table, d_domain,
+            infl, c.vbox.as<double>(), c.vin.as<char>());
     } else {
         RIGC_TRY(S[0].reserve((size_t)12 * s.nb * sizeof(double)));
         RIGC_TRY(body_rot_rn(c, x0, S[0].as<double>()));
@@ -1003,7 +1049,7 @@ int detect_pairs(Ctx& c, const double* x0, const double* x1, bool continuous, do
     k_elem_stats<<<kStatBlocks, kStatThreads, 0, st>>>(E, d_part, d_part_n);
     const uint64_t nslots = filter_slots(ntot);
     RIGC_COUNT_LAUNCH();
-    k_grid_setup<<<1, 1, 0, st>>>(d_part, d_part_n, kStatBlocks, s.avg_edge_len, s.nscenes,
+    k_grid_setup<<<1, 32, 0, st>>>(d_part, d_part_n, kStatBlocks, s.avg_edge_len, s.nscenes,
                                    s.group_bits, nslots, d_grid);
     RIGC_TRY(c.bp_sig.reserve(nslots * sizeof(int)));
     RIGC_TRY(c.bp_ec0.reserve((size_t)ntot * sizeof(uint64_t) + 8));
@@ -1130,6 +1176,11 @@ int detect_pairs(Ctx& c, const double* x0, const double* x1, bool continuous, do
                                                           fv_stride, out.fv.as<int2>());
     }
     RIGC_CUDA(cudaGetLastError());
+    if (continuous && kind == kPairsEEFV) {
+        c.bp_table.x0 = x0;
+        c.bp_table.x1 = x1;
+        c.bp_table.valid = true;
+    }
     return RIGC_OK;
 }
 

@@ -237,10 +237,14 @@ constexpr int kTableDepth = 7;                          // levels 0..6
 constexpr int kTableNodes = (1 << kTableDepth) - 1;     // 127
 constexpr int kTableSlots = kTableNodes + 1;            // + [0, toi_tol]
 constexpr int kTableEntry = 24;                         // R (9 intervals) + p (3)
+static_assert(kTableSlots == kRotTableSlots && kTableEntry == kRotTableEntry, "table layout");
 
+// tree_ready: the slots of the tree nodes already hold these poses' frames
+// for every body a candidate can have (the continuous broad phase computed
+// them); only [0, toi_tol], the trajectories and the fixed flags are left
 __global__ void k_rot_table(const double* __restrict__ x0, const double* __restrict__ x1, int nb,
                             double toi_tol, double* __restrict__ table, double* __restrict__ traj,
-                            int* __restrict__ bfixed)
+                            int* __restrict__ bfixed, int tree_ready)
 {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (int64_t)nb * kTableSlots) return;
@@ -252,8 +256,10 @@ __global__ void k_rot_table(const double* __restrict__ x0, const double* __restr
     BodyTraj T;
     load_traj(x0, x1, b, T);
     Itv R[9], p[3];
-    body_at(T, t, R, p);
-    frame_store(table + (size_t)i * kTableEntry, R, p);
+    if (!tree_ready || node == kTableNodes) {
+        body_at(T, t, R, p);
+        frame_store(table + (size_t)i * kTableEntry, R, p);
+    }
     if (node == 0) {
         double* e = traj + (size_t)b * kTrajDoubles;
         bool fixed = true;
@@ -597,6 +603,50 @@ __device__ __forceinline__ int split_dim(const double w[3], const double tol[3],
         if ((all_tol || !le_nn(w[d], tol[d]))
             && (split == -1 || !le_nn(RMUL(w[d], tol[split]), RMUL(w[split], tol[d]))))
             split = d;
+    return split;
+}
+
+// split_dim without multiplications.  A node's width is w[k] =
+// (1 + 2^-52) 2^-lv[k] (node_widths), so RMUL(w[d], tol[s]) =
+// 2^-lv[d] RN((1 + 2^-52) tol[s]) exactly while the results stay normal,
+// and the comparison of split_dim orders the keys
+// K[k] = bits(RN((1 + 2^-52) tol[k])) + lv[k] 2^52 (a power-of-two scaling
+// adds to the exponent field): the split moves to d when K[d] < K[split].
+// tk[k] = bits(RN((1 + 2^-52) tol[k])); ok = every tk is at least 2^-960, so
+// that the scaled products are normal (else split_dim decides).
+struct TolKeys {
+    long long tk[3];
+    bool ok;
+};
+
+__device__ __forceinline__ TolKeys tol_keys(const double tol[3])
+{
+    TolKeys r;
+    const double wunit = __longlong_as_double(0x3ff0000000000001ll);  // 1 + 2^-52
+    r.ok = true;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const double t = RMUL(wunit, tol[k]);
+        r.tk[k] = __double_as_longlong(t);
+        r.ok = r.ok && is_pos(t) && r.tk[k] >= (63ll << 52) && r.tk[k] < (2046ll << 52);
+    }
+    return r;
+}
+
+__device__ __forceinline__ int split_dim_keys(const Node& c, const TolKeys& K, const double w[3],
+                                              const double tol[3], bool all_tol)
+{
+    if (!K.ok) return split_dim(w, tol, all_tol);
+    int split = -1;
+    long long ks = 0;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        const long long kd = K.tk[d] + ((long long)c.lv[d] << 52);
+        if ((all_tol || !le_nn(w[d], tol[d])) && (split == -1 || kd < ks)) {
+            split = d;
+            ks = kd;
+        }
+    }
     return split;
 }
 
@@ -1012,8 +1062,13 @@ k_ccd_warp(CCDArgs a)
     const int64_t n = a.nee + a.nfv;
     const int64_t nwork = a.pieces_in ? a.n_pieces : (n << a.seeds_log2);
     const int lane = threadIdx.x & 31;
-    const int vtx = lane / 3, crd = lane - 3 * (lane / 3);
-    const bool vlane = lane < 12;
+    // vertex lanes 0..23: bound vb (0 lower, 1 upper) of coordinate crd of
+    // vertex vtx; distance lanes 0..11: bound db of the half dh of the
+    // distance function's coordinate dc
+    const int vb = lane >= 12 ? 1 : 0;
+    const int vtx = (lane % 12) / 3, crd = lane % 3;
+    const bool vlane = lane < 24;
+    const int db = lane >= 6 ? 1 : 0, dh = (lane % 6) / 3, dc = lane % 3;
     unsigned long long tot_boxes = 0, tot_hits = 0, pops = 0;
     // search state (the same in every lane)
     Node cn { { 0, 0, 0 }, { 0ull, 0ull, 0ull }, 0 };
@@ -1027,11 +1082,12 @@ k_ccd_warp(CCDArgs a)
     bool hand_ok = a.hand_off != 0, tail = false;
     double gbound = INFINITY;
     double tol[3] = { 0, 0, 0 };
+    TolKeys tkeys { { 0, 0, 0 }, false };
     bool fv = false, a_fixed = false, b_fixed = false;
     int body_a = 0, body_b = 0;
-    // this lane's vertex and its coordinate interval over [ct0, ct1]
+    // this lane's vertex and its bound of the coordinate interval over [ct0, ct1]
     double rv[3] = { 0, 0, 0 };
-    Itv pcrd { 0, 0 };
+    double pcrd = 0;
     const double nan = __longlong_as_double(0x7ff8000000000000ll);
     double ct0 = nan, ct1 = nan;
     bool fresh = true;
@@ -1157,6 +1213,7 @@ k_ccd_warp(CCDArgs a)
             tol[0] = a.ctol[3 * cur];
             tol[1] = a.ctol[3 * cur + 1];
             tol[2] = a.ctol[3 * cur + 2];
+            tkeys = tol_keys(tol);
             if (a.prune)
                 gbound = __shfl_sync(0xffffffffu, __longlong_as_double(
                     (long long)*(volatile unsigned long long*)gmin_body(a, body_a)), 0);
@@ -1194,10 +1251,25 @@ k_ccd_warp(CCDArgs a)
             bool miss = false;
             if (need) {
                 Itv r[3], pc;
-                if (frame_find_row(a, own, side, side ? body_b : body_a, node, t, crd, r, pc))
-                    pcrd = iadd(iadd(iadd(imul(rv[0], r[0]), imul(rv[1], r[1])), imul(rv[2], r[2])), pc);
-                else
+                if (frame_find_row(a, own, side, side ? body_b : body_a, node, t, crd, r, pc)) {
+                    // one bound of iworld_vertex's coordinate expression
+                    // iadd(iadd(iadd(imul(v0, r0), imul(v1, r1)), imul(v2, r2)), p):
+                    // the lower bound takes only lower-bound operations, the
+                    // upper only upper
+                    if (vb == 0) {
+                        double q = mul_dn(rv[0], is_neg(rv[0]) ? r[0].hi : r[0].lo);
+                        q = add_dn(q, mul_dn(rv[1], is_neg(rv[1]) ? r[1].hi : r[1].lo));
+                        q = add_dn(q, mul_dn(rv[2], is_neg(rv[2]) ? r[2].hi : r[2].lo));
+                        pcrd = add_dn(q, pc.lo);
+                    } else {
+                        double q = mul_up(rv[0], is_neg(rv[0]) ? r[0].lo : r[0].hi);
+                        q = add_up(q, mul_up(rv[1], is_neg(rv[1]) ? r[1].lo : r[1].hi));
+                        q = add_up(q, mul_up(rv[2], is_neg(rv[2]) ? r[2].lo : r[2].hi));
+                        pcrd = add_up(q, pc.hi);
+                    }
+                } else {
                     miss = true;
+                }
             }
             const unsigned mm = __ballot_sync(0xffffffffu, miss);
             if (mm) {
@@ -1205,9 +1277,9 @@ k_ccd_warp(CCDArgs a)
                 // A's, lane 1 for body B's), every lane keeps them; retry
                 bool miss_a = false, miss_b = false;
 #pragma unroll
-                for (int l = 0; l < 12; l++)
+                for (int l = 0; l < 24; l++)
                     if ((mm >> l) & 1) {
-                        if (l / 3 < na) miss_a = true;
+                        if ((l % 12) / 3 < na) miss_a = true;
                         else miss_b = true;
                     }
                 const unsigned req = (miss_a ? 1u : 0u) | (miss_b ? 2u : 0u);
@@ -1223,34 +1295,44 @@ k_ccd_warp(CCDArgs a)
         }
         cboxes++;
         if (lane == 0) tot_boxes++;
-        // f(box) contains zero: lanes 0..5 take coordinate c = lane % 3 of
-        // the four vertices; lanes c and c + 3 evaluate the two halves of
-        // the distance function's coordinate c (EE: the two edge points; FV:
-        // the two face-edge terms), lane c combines them (the expressions
-        // and operand order of f_zero)
-        Itv P[4];
-#pragma unroll
-        for (int v = 0; v < 4; v++) {
-            P[v].lo = __shfl_sync(0xffffffffu, pcrd.lo, 3 * v + crd);
-            P[v].hi = __shfl_sync(0xffffffffu, pcrd.hi, 3 * v + crd);
-        }
-        const bool h1 = lane >= 3;  // the second half (lanes 3..5)
-        const Itv al { x.a0, x.a1 }, be { x.b0, x.b1 };
-        const Itv& pw = h1 ? be : al;
-        Itv part;
-        if (fv) {
-            part = imul_nonneg(isub(h1 ? P[3] : P[2], P[1]), pw);
+        // f(box) contains zero: the expressions and operand order of f_zero,
+        // each interval bound on its own lane.  Distance lane (db, dh, dc)
+        // evaluates bound db of half dh of coordinate dc (EE: the point of
+        // edge dh; FV: the face-edge term dh): d = A - B, m = d * w
+        // (w = alpha or beta, non-negative), EE adds q0 = B.  Lanes with
+        // dh = 0 then combine the halves: EE y = part0 - part1; FV
+        // y = P0 - ((part0 + part1) + P1).  A lower bound takes only lower
+        // bounds of its operands (and upper bounds of subtrahends), so the
+        // bits are those of the interval expressions.
+        // vertex v's bound b of coordinate c lives on lane 12 b + 3 v + c
+        const int va = fv ? (dh ? 3 : 2) : (dh ? 3 : 1);
+        const int vq = fv ? 1 : (dh ? 2 : 0);
+        const double A = __shfl_sync(0xffffffffu, pcrd, 12 * db + 3 * va + dc);
+        const double Bx = __shfl_sync(0xffffffffu, pcrd, 12 * (1 - db) + 3 * vq + dc);
+        const double Bs = __shfl_sync(0xffffffffu, pcrd, 12 * db + 3 * vq + dc);
+        const Itv pw = dh ? Itv { x.b0, x.b1 } : Itv { x.a0, x.a1 };
+        double part;
+        if (db == 0) {
+            const double d = sub_dn(A, Bx);
+            part = mul_dn(d, is_neg(d) ? pw.hi : pw.lo);
+            if (!fv) part = add_dn(part, Bs);
         } else {
-            const Itv& q0 = h1 ? P[2] : P[0];
-            part = iadd(imul_nonneg(isub(h1 ? P[3] : P[1], q0), pw), q0);
+            const double d = sub_up(A, Bx);
+            part = mul_up(d, is_neg(d) ? pw.lo : pw.hi);
+            if (!fv) part = add_up(part, Bs);
         }
-        Itv other;
-        other.lo = __shfl_sync(0xffffffffu, part.lo, (lane + 3) & 31);
-        other.hi = __shfl_sync(0xffffffffu, part.hi, (lane + 3) & 31);
+        // the other half's bound: EE the opposite bound, FV the same
+        const int osrc = 6 * (fv ? db : 1 - db) + 3 + dc;
+        const double other = __shfl_sync(0xffffffffu, part, osrc);
         bool zin = true;
-        if (lane < 3) {
-            const Itv y = fv ? isub(P[0], iadd(iadd(part, other), P[1])) : isub(part, other);
-            zin = zero_in(y);
+        if (fv) {
+            const double P1 = __shfl_sync(0xffffffffu, pcrd, 12 * db + 3 + dc);
+            const double P0 = __shfl_sync(0xffffffffu, pcrd, 12 * db + dc);
+            const double tb = db == 0 ? add_dn(add_dn(part, other), P1) : add_up(add_up(part, other), P1);
+            const double tx = __shfl_sync(0xffffffffu, tb, (6 * (1 - db) + dc) & 31);
+            if (lane < 12 && dh == 0) zin = db == 0 ? !is_pos(sub_dn(P0, tx)) : !is_neg(sub_up(P0, tx));
+        } else if (lane < 12 && dh == 0) {
+            zin = db == 0 ? !is_pos(sub_dn(part, other)) : !is_neg(sub_up(part, other));
         }
         if (!__all_sync(0xffffffffu, zin)) continue;
         double w[3];
@@ -1270,7 +1352,7 @@ k_ccd_warp(CCDArgs a)
             }
             continue;
         }
-        const int split = split_dim(w, tol, all_tol);
+        const int split = split_dim_keys(cn, tkeys, w, tol, all_tol);
         if (cn.depth >= kMaxDepth || cn.lv[split] >= kMaxLevel) {
             earliest = smin(earliest, x.t0);
             found = true;
@@ -1320,6 +1402,14 @@ int ccd_max_blocks_per_sm(int* out, int mode)
 int ccd_search_mode(const Ctx& c)
 {
     return c.tune.ccd_warp >= 0 ? c.tune.ccd_warp : 1;
+}
+
+// the frame table, the trajectories and the fixed flags (rot_table)
+int reserve_rot_table(Ctx& c)
+{
+    const size_t table_bytes = (size_t)c.s.nb * kTableSlots * kTableEntry * sizeof(double);
+    const size_t traj_bytes = (size_t)c.s.nb * kTrajDoubles * sizeof(double);
+    return c.rot_table.reserve(table_bytes + traj_bytes + (size_t)c.s.nb * sizeof(int) + 64);
 }
 
 // counters layout in the context's device scalars (byte offset 256):
@@ -1372,16 +1462,19 @@ int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flag
         // per-body trajectories and fixed flags, then per-candidate tolerances
         const size_t table_bytes = (size_t)c.s.nb * kTableSlots * kTableEntry * sizeof(double);
         const size_t traj_bytes = (size_t)c.s.nb * kTrajDoubles * sizeof(double);
-        RIGC_TRY(c.rot_table.reserve(table_bytes + traj_bytes + (size_t)c.s.nb * sizeof(int) + 64));
+        RIGC_TRY(reserve_rot_table(c));
         RIGC_TRY(c.cand_tol.reserve((size_t)n * 3 * sizeof(double)));
         a.table = c.rot_table.as<double>();
         a.traj = reinterpret_cast<double*>(c.rot_table.as<char>() + table_bytes);
         a.bfixed = reinterpret_cast<int*>(c.rot_table.as<char>() + table_bytes + traj_bytes);
         a.ctol = c.cand_tol.as<double>();
+        // the continuous broad phase just computed the tree nodes' frames of
+        // every body a candidate can have, for these poses
+        const int tree_ready = c.bp_table.valid && c.bp_table.x0 == x0 && c.bp_table.x1 == x1;
         RIGC_COUNT_LAUNCH();
         k_rot_table<<<grid_for((int64_t)c.s.nb * kTableSlots, 128), 128, 0, st>>>(
             x0, x1, c.s.nb, toi_tol, const_cast<double*>(a.table), const_cast<double*>(a.traj),
-            const_cast<int*>(a.bfixed));
+            const_cast<int*>(a.bfixed), tree_ready);
         // frame cache: 1024 slots per body (or the tuned count), at least
         // 2^16, at most 2^22
         const size_t per_body = c.tune.cache_slots_per_body > 0 ? c.tune.cache_slots_per_body : 1024;
@@ -1462,6 +1555,7 @@ int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flag
             want = ((int64_t)np + per_block - 1) / per_block;
         }
     }
+    c.bp_table.valid = false;
     unsigned long long out[4];
     RIGC_CUDA(cudaMemcpyAsync(out, cnt, sizeof(out), cudaMemcpyDeviceToHost, st));
     RIGC_CUDA(cudaStreamSynchronize(st));

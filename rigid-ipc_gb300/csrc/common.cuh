@@ -15,6 +15,12 @@ namespace rigc {
 
 constexpr int kNumSMs = 152;  // GB300: 2 dies x 76 SMs
 
+// CCD frame table: per body, interval frames (R as 9 intervals, p as 3) over
+// the dyadic time nodes [k 2^-d, (k + 1) 2^-d] of depth d < 7 (slot
+// 2^d - 1 + k) and over [0, toi_tol] (slot 127)
+constexpr int kRotTableSlots = 128;
+constexpr int kRotTableEntry = 24;
+
 // ---------------------------------------------------------------------------
 // error handling: every host function returns an int status; CUDA failures
 // are recorded in the context and surface as RIGC_ERR_CUDA / RIGC_ERR_OOM.
@@ -156,10 +162,18 @@ struct Ctx {
     DevBuf body_box, body_in, vbox, ebox, fbox, vin, ein, fin;
     DevBuf items_key, items_val, items_key2, items_val2, seg, pair_out, pair_key;
     DevBuf large_list;
-    // hash grid: call state, half-interval frames, deeper-bisection flags,
+    // hash grid: call state, deeper-bisection flags,
     // cell filter, per-element cell ranges, float boxes, item counts
-    DevBuf bp_misc, bp_frames, bp_deeper, bp_sig, bp_ec0, bp_eext, bp_f32, bp_cnt;
+    DevBuf bp_misc, bp_deeper, bp_sig, bp_ec0, bp_eext, bp_f32, bp_cnt;
     int64_t bp_pair_hint[2] = { 0, 0 };  // largest EE / FV pair counts seen
+    // The continuous broad phase leaves the interval frames of the included
+    // bodies over the dyadic time nodes of depth < 7 in rot_table (the CCD's
+    // layout); the CCD right after it on the same poses reuses them.
+    struct {
+        const double* x0 = nullptr;
+        const double* x1 = nullptr;
+        bool valid = false;
+    } bp_table;
     // rigc_min_distance / rigc_detect_intersections: world vertices, their
     // rotation frames, the result; the edge-face intersection candidates
     DevBuf md_V, md_rot, md_out;

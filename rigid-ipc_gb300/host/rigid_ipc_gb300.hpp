@@ -46,6 +46,9 @@ inline void check(int s, const char* where, bool allow_conservative = false)
 }
 
 // Device buffer owned by the host layer (only the pose uploads need one).
+// Uploads go through rigc_copy, on the context's stream: queued after the
+// context's earlier work (which may still read the previous poses when the
+// context runs on a caller stream) and finished when upload returns.
 class DeviceArray {
 public:
     DeviceArray() = default;
@@ -55,17 +58,21 @@ public:
     {
         if (ptr_) cudaFree(ptr_);
     }
-    double* upload(const std::vector<double>& v)
+    double* upload(rigc_ctx* ctx, const std::vector<double>& v)
     {
         size_t bytes = v.size() * sizeof(double);
         if (bytes > cap_) {
-            if (ptr_) cudaFree(ptr_);
+            // the old buffer may still be read by queued work: free it only
+            // after the context's stream has drained
+            if (ptr_) {
+                check(rigc_copy(ctx, nullptr, nullptr, 0), "rigc_copy");
+                cudaFree(ptr_);
+            }
             ptr_ = nullptr;
             if (cudaMalloc(&ptr_, bytes) != cudaSuccess) throw Error(RIGC_ERR_OOM, "DeviceArray");
             cap_ = bytes;
         }
-        if (cudaMemcpy(ptr_, v.data(), bytes, cudaMemcpyHostToDevice) != cudaSuccess)
-            throw Error(RIGC_ERR_CUDA, "DeviceArray::upload");
+        check(rigc_copy(ctx, ptr_, v.data(), bytes), "DeviceArray::upload");
         return static_cast<double*>(ptr_);
     }
 
@@ -123,7 +130,7 @@ public:
     // world_vertices(poses): nv x 3, row-major
     std::vector<double> world_vertices(const std::vector<double>& dofs) const
     {
-        double* x = x0_.upload(dofs);
+        double* x = x0_.upload(ctx_, dofs);
         double* V = nullptr;
         size_t bytes = 3 * num_vertices() * sizeof(double);
         if (cudaMalloc(&V, bytes) != cudaSuccess) throw Error(RIGC_ERR_OOM, "world_vertices");
@@ -158,8 +165,8 @@ inline void detect_collision_candidates_rigid(
     DetectionMethod = DetectionMethod::HASH_GRID, double inflation_radius = 0.0,
     bool continuous = true)
 {
-    double* x0 = bodies.x0_.upload(poses_t0);
-    double* x1 = bodies.x1_.upload(poses_t1);
+    double* x0 = bodies.x0_.upload(bodies.ctx(), poses_t0);
+    double* x1 = bodies.x1_.upload(bodies.ctx(), poses_t1);
     rigc_candidates c {};
     check(rigc_detect_candidates(bodies.ctx(), x0, x1, continuous ? 1 : 0, inflation_radius, &c),
           "rigc_detect_candidates");
@@ -192,7 +199,7 @@ public:
         const RigidBodyAssembler& bodies, const std::vector<double>& poses,
         Constraints& out) const
     {
-        double* x = bodies.x0_.upload(poses);
+        double* x = bodies.x0_.upload(bodies.ctx(), poses);
         rigc_constraints c {};
         check(rigc_construct_constraint_set(bodies.ctx(), x, barrier_activation_distance(),
                                             minimum_separation_distance, &c),
@@ -217,8 +224,8 @@ public:
         const RigidBodyAssembler& bodies, const std::vector<double>& poses_t0,
         const std::vector<double>& poses_t1) const
     {
-        double* x0 = bodies.x0_.upload(poses_t0);
-        double* x1 = bodies.x1_.upload(poses_t1);
+        double* x0 = bodies.x0_.upload(bodies.ctx(), poses_t0);
+        double* x1 = bodies.x1_.upload(bodies.ctx(), poses_t1);
         double toi = INFINITY;
         check(rigc_compute_earliest_toi(bodies.ctx(), x0, x1, minimum_separation_distance, &toi),
               "rigc_compute_earliest_toi", true);
@@ -246,7 +253,7 @@ public:
         const std::vector<double>& x, std::vector<double>& grad, BlockSparse& hess,
         bool compute_grad = true, bool compute_hess = true)
     {
-        double* xd = assembler_.x0_.upload(x);
+        double* xd = assembler_.x0_.upload(assembler_.ctx(), x);
         rigc_ctx* k = assembler_.ctx();
         check(rigc_construct_constraint_set(k, xd, constraint_.barrier_activation_distance(),
                                             constraint_.minimum_separation_distance, nullptr),
@@ -280,6 +287,27 @@ public:
     bool has_collisions(const std::vector<double>& x_i, const std::vector<double>& x_j)
     {
         return constraint_.has_active_collisions(assembler_, x_i, x_j);
+    }
+
+    // compute_min_distance(x) (distance_barrier_rb_problem.cpp:1583-1589):
+    // the smallest constraint distance at x, -1 when the set is empty
+    double compute_min_distance(const std::vector<double>& x)
+    {
+        double* xd = assembler_.x0_.upload(assembler_.ctx(), x);
+        double d = -1;
+        check(rigc_min_distance(assembler_.ctx(), xd, constraint_.barrier_activation_distance(),
+                                constraint_.minimum_separation_distance, &d),
+              "rigc_min_distance");
+        return d;
+    }
+
+    // detect_intersections(poses) (rigid_body_problem.cpp:289-360)
+    bool detect_intersections(const std::vector<double>& x)
+    {
+        double* xd = assembler_.x0_.upload(assembler_.ctx(), x);
+        int64_t n = 0;
+        check(rigc_detect_intersections(assembler_.ctx(), xd, &n), "rigc_detect_intersections");
+        return n > 0;
     }
 
 private:

@@ -269,6 +269,16 @@ class Context:
                  self.copy_out(o.val, (o.nnzb, 6, 6), np.float64))
         return o.energy, g, H
 
+    def barrier_local_terms_device(self, xd, n, dhat, e, g, H, dmin=0.0, project=True):
+        """rigc_barrier_local_terms into caller-owned device tensors (energy
+        n, gradient n x 12, Hessian n x 144), with device poses; no copy."""
+        flags = L.RIGC_GRAD | L.RIGC_HESS | (L.RIGC_PROJECT_PSD if project else 0)
+        L.check(self.lib.rigc_barrier_local_terms(self.h, C.c_void_p(xd.data_ptr()), dhat, dmin,
+                                                  flags, C.c_void_p(e.data_ptr()),
+                                                  C.c_void_p(g.data_ptr()),
+                                                  C.c_void_p(H.data_ptr())),
+                "rigc_barrier_local_terms")
+
     def barrier_local_terms(self, x, n, dhat, dmin=0.0, project=True):
         torch = self.torch
         xd = self.device(x)

@@ -65,6 +65,41 @@ def cube(size: float = 1.0):
     return V, _orient_outward(V, F)
 
 
+def tessellated_box(size=(1.0, 0.2, 1.0), n=(32, 4, 32)):
+    """Box centred at the origin whose faces are grids of n[a] x n[b] quads
+    (two triangles each) along their two axes; vertices on the box's edges
+    are shared, so the mesh is closed.  size (1, 0.2, 1) with n (32, 4, 32):
+    2,562 vertices, 7,680 edges, 5,120 triangles."""
+    n = [int(k) for k in n]
+    ext = np.asarray(size, dtype=np.float64)
+    index = {}
+    V = []
+
+    def vid(i, j, k):
+        key = (i, j, k)
+        if key not in index:
+            index[key] = len(V)
+            V.append([(i / n[0] - 0.5) * ext[0], (j / n[1] - 0.5) * ext[1],
+                      (k / n[2] - 0.5) * ext[2]])
+        return index[key]
+
+    F = []
+    for ax in range(3):
+        a, b = [d for d in range(3) if d != ax]
+        for side in (0, n[ax]):
+            for u in range(n[a]):
+                for w in range(n[b]):
+                    q = []
+                    for du, dw in ((0, 0), (1, 0), (1, 1), (0, 1)):
+                        c = [0, 0, 0]
+                        c[ax], c[a], c[b] = side, u + du, w + dw
+                        q.append(vid(*c))
+                    F.append((q[0], q[1], q[2]))
+                    F.append((q[0], q[2], q[3]))
+    V = np.array(V, dtype=np.float64)
+    return V, _orient_outward(V, np.array(F, dtype=np.int32))
+
+
 def plane(size: float = 20.0):
     """Square in the y = 0 plane, normal +y: 4 vertices, 2 triangles."""
     h = 0.5 * size

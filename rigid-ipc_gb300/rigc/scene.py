@@ -674,6 +674,32 @@ def spec_cube_lattice(seed=0, n=4, spacing=1.05, dt=0.01, dhat=1e-3, steps=50):
 # --------------------------------------------------------------------------
 # synthetic contact-rich narrow-phase states
 
+def spec_slab_stacks(seed=0, nx=8, nz=8, layers=2, size=(1.0, 0.2, 1.0), n=(32, 4, 32),
+                     gap=3e-4, pitch=1.2, dt=0.01, dhat=1e-3, steps=100):
+    """A contact-heavy scene for the barrier terms: nx x nz columns of
+    `layers` tessellated slabs (faces of 32 x 32 quads), each resting `gap`
+    above the one below or the floor, every slab shifted by a seeded offset
+    in x and z so that the face grids do not line up.  Every vertex of a
+    slab's bottom face is within dhat of the face below: the 4 x 4 x 2
+    stack has some 1.6 x 10^5 constraints, the 8 x 8 x 2 one 6.4 x 10^5."""
+    rng = np.random.default_rng(seed)
+    spec = _base_spec(dt, dhat, steps)
+    Vs, Fs = meshes.tessellated_box(size, n)
+    bodies = spec["rigid_body_problem"]["rigid_bodies"]
+    for ix in range(nx):
+        for iz in range(nz):
+            y = 0.0
+            for _ in range(layers):
+                off = rng.uniform(-0.02, 0.02, 2)
+                y += gap + 0.5 * size[1]
+                bodies.append(_rb(Vs, Fs, position=[(ix - (nx - 1) / 2) * pitch + off[0], y,
+                                                    (iz - (nz - 1) / 2) * pitch + off[1]]))
+                y += 0.5 * size[1]
+    Vp, Fp = meshes.plane(max(nx, nz) * pitch + 2.0)
+    bodies.append(_rb(Vp, Fp, position=[0, 0, 0], is_dof_fixed=True, type="static"))
+    return spec
+
+
 def packed_pile_poses(scene: Scene, seed=0, gap=2e-4, iters=400):
     """Settle the dynamic bodies of an icosphere scene into a pile on the floor.
 

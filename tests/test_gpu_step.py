@@ -3,6 +3,8 @@ the closed-form free fall, and the 27-cube scene over several steps (poses
 within 1e-7: the Newton systems are solved by different methods, an LDL^T on
 the CPU and preconditioned conjugate gradients to a 1e-12 residual on the
 GPU, so the iterates agree to the solve accuracy, not bit for bit)."""
+import os
+
 import numpy as np
 import pytest
 
@@ -89,3 +91,138 @@ def test_kinematic_bodies_match_oracle(oracle):
     with pytest.raises(RuntimeError):  # kinematic bodies are not differentiated
         ctx.sim_rollout(1, 1)
         ctx.sim_backward(np.zeros((sc.num_bodies, 6)))
+
+
+# ---------------------------------------------------------------------------
+# whole runs against the oracle's trajectories (tests/golden/
+# step_trajectories.npz, made by make_step_fixtures.py), at the 1e-8 pose
+# bar, with the end-of-step intersection check
+
+POSE_ATOL = 1e-8
+FIXTURE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                       "step_trajectories.npz")
+
+
+def _fixture(key, sc, x0):
+    import make_step_fixtures as SF
+
+    fx = np.load(FIXTURE)
+    if SF.inputs_digest(sc, x0) != str(fx[key + "_digest"]):
+        pytest.skip("this machine builds a different scene (floating-point set-up differs)")
+    return fx
+
+
+def test_cube_lattice_whole_run_matches_oracle():
+    """All 100 steps of the 27-cube lattice (landings from step ~30) with
+    every Newton solve converged to rounding: poses within 1e-8 of the
+    oracle's after every step, no crossing edge and face after any step on
+    either side, and the same minimum distance."""
+    import rigc
+
+    import make_step_fixtures as SF
+
+    sc = SF.cubes_scene()
+    fx = _fixture("cubes_tight", sc, sc.poses())
+    ctx = rigc.Context(sc)
+    ctx.sim_init(SF.H, SF.G, SF.DHAT, **SF.TIGHT)
+    assert fx["cubes_tight_crossings"].max() == 0
+    landed = 0
+    for k in range(SF.CUBE_STEPS):
+        ctx.sim_step(1)
+        P, V, Q, kappa = ctx.sim_state()
+        x = P.reshape(-1)
+        err = np.abs(x - fx["cubes_tight_poses"][k + 1]).max()
+        assert err <= POSE_ATOL, (k, err)
+        assert ctx.detect_intersections(x) == 0, k
+        md_o = fx["cubes_tight_min_distance"][k]
+        md = ctx.compute_min_distance(x, SF.DHAT)
+        assert (md < 0) == (md_o < 0), k
+        if md_o > 0:
+            landed += 1
+            assert abs(md - md_o) <= 1e-9, (k, md, md_o)
+    assert landed > 20  # the cubes rest on the plane for the last steps
+
+
+def test_cube_lattice_default_solver():
+    """The same run with the reference's default Newton tolerance
+    (velocity_conv_tol 1e-2): the iterates are not converged, so any change
+    of rounding (1e-15 in the start poses) grows tenfold per contact step --
+    to 1e-8 by step 11 in the oracle itself.  The first 8 steps match the
+    oracle's within 1e-8; over all 100 steps the run stays intersection-free
+    and the cubes come to rest on the plane in the oracle's three layers."""
+    import rigc
+
+    import make_step_fixtures as SF
+
+    sc = SF.cubes_scene()
+    fx = _fixture("cubes", sc, sc.poses())
+    ctx = rigc.Context(sc)
+    ctx.sim_init(SF.H, SF.G, SF.DHAT)
+    assert fx["cubes_crossings"].max() == 0
+    for k in range(SF.CUBE_STEPS):
+        ctx.sim_step(1)
+        P, V, Q, kappa = ctx.sim_state()
+        x = P.reshape(-1)
+        if k < 8:
+            err = np.abs(x - fx["cubes_poses"][k + 1]).max()
+            assert err <= POSE_ATOL, (k, err)
+        assert ctx.detect_intersections(x) == 0, k
+    assert ctx.compute_min_distance(x, SF.DHAT) > 0
+    assert fx["cubes_min_distance"][-1] > 0
+    # resting heights: three layers of nine cubes on the plane at the end (a
+    # perturbed oracle run settles to the same heights within 1e-6)
+    dyn = np.array([b.type == 2 for b in sc.bodies])
+    y_g = P[dyn, 1]
+    y_o = fx["cubes_poses"][-1].reshape(-1, 6)[dyn, 1]
+    assert np.abs(np.sort(y_g) - np.sort(y_o)).max() < 1e-4
+
+
+def test_detect_intersections_matches_oracle(oracle):
+    """Crossing (edge, face) pairs at intersecting poses (every cube sunk
+    1 cm, one cube sunk 30 cm) and at the resting contact, GPU and oracle."""
+    import rigc
+    from conftest import contact_poses
+
+    import make_step_fixtures as SF
+
+    sc = SF.cubes_scene()
+    o = oracle.OracleScene(sc)
+    ctx = rigc.Context(sc)
+    x = contact_poses(sc).reshape(-1, 6)
+    dyn = np.array([b.type == 2 for b in sc.bodies])
+    sunk = x.copy()
+    sunk[dyn, 1] -= 0.01
+    deep = x.copy()
+    deep[np.where(dyn)[0][0], 1] -= 0.3
+    counts = []
+    for y in (x, sunk, deep):
+        n_o = o.detect_intersections(y.reshape(-1))
+        assert ctx.detect_intersections(y.reshape(-1)) == n_o
+        counts.append(n_o)
+    assert counts[0] == 0 and counts[1] > 0 and counts[2] > 0
+
+
+@pytest.mark.parametrize("case", ["pair", "pile"])
+def test_friction_steps_match_oracle(case):
+    """Time steps with friction (mu 0.5, one lagged friction iteration per
+    step): two cubes sliding into each other on the plane (10 steps) and 8
+    icospheres in a contact pile (2 steps), poses within 1e-8 of the
+    oracle's and intersection-free."""
+    import rigc
+
+    import make_step_fixtures as SF
+
+    if case == "pair":
+        sc, x0, steps = SF.pair_scene(), None, SF.PAIR_STEPS
+    else:
+        (sc, x0), steps = SF.pile_scene(), SF.PILE_STEPS
+    fx = _fixture(case, sc, sc.poses() if x0 is None else x0)
+    ctx = rigc.Context(sc)
+    ctx.sim_init(SF.H, SF.G, SF.DHAT, coefficient_friction=SF.MU, poses=x0)
+    for k in range(steps):
+        ctx.sim_step(1)
+        P, V, Q, kappa = ctx.sim_state()
+        err = np.abs(P.reshape(-1) - fx[case + "_poses"][k + 1]).max()
+        assert err <= POSE_ATOL, (k, err)
+        assert kappa == pytest.approx(float(fx[case + "_kappa"][k]), rel=1e-9)
+        assert ctx.detect_intersections(P.reshape(-1)) == 0
