@@ -39,18 +39,21 @@ METRIC = "candidate pairs/s (CCD+barrier grad/Hess)"
 UNIT = "pairs/s"
 CCD_BYTES_PER_PAIR = 304        # ids + 4 rest vertices + 4 poses + toi
 # DRAM bytes (read + write) per continuous candidate of one CCD call (all its
-# launches), from ncu captures of the 200-icosphere pile with the built-in
-# shapes (132,242 candidates; profiles/k_ccd_icosphere_pile_200.md):
-# k_ccd 56.95 MB read + 311.51 MB written over two launches (per-lane
-# candidate state spilling from L1, the frame cache); k_ccd_warp 20.95 MB +
-# 15.81 MB over three.  The traffic of a full call is this times its
-# candidates.  FP64 figures of the same captures: pipe active (fraction of
-# peak) and lane-level GFLOP/s (dadd + dmul + 2 dfma over the launch).
+# launches), from ncu captures of the 200-icosphere pile (132,242
+# candidates): k_ccd 56.95 MB read + 311.51 MB written over two launches
+# (per-lane candidate state spilling from L1, the frame cache);
+# k_ccd_warp<1> 20.95 MB + 15.81 MB over three; k_ccd_warp<4> (128
+# registers, one interval bound per lane) 27.51 MB + 43.86 MB over three,
+# most of the writes its spills.  The traffic of a full call is this times
+# its candidates.  FP64 figures of the same captures: pipe active (fraction
+# of peak) and lane-level GFLOP/s (dadd + dmul + 2 dfma over the launch).
 K_CCD_DRAM_BYTES_PER_CANDIDATE = {
     "k_ccd": (42209536 + 14743808 + 310226176 + 1279232) / 132242,
-    "k_ccd_warp<1>": (17837312 + 2597632 + 512000 + 15804928 + 1792) / 132242}
+    "k_ccd_warp<1>": (17837312 + 2597632 + 512000 + 15804928 + 1792) / 132242,
+    "k_ccd_warp<4>": (22857216 + 3941120 + 714752 + 43766272 + 90880 + 2304) / 132242}
 K_CCD_FP64 = {"k_ccd": {"pipe_active": 0.233, "lane_gflops": 53.0},
-              "k_ccd_warp<1>": {"pipe_active": 0.496, "lane_gflops": 98.4}}
+              "k_ccd_warp<1>": {"pipe_active": 0.496, "lane_gflops": 98.4},
+              "k_ccd_warp<4>": {"pipe_active": 0.381, "lane_gflops": 100.9}}
 BARRIER_BYTES_PER_CONSTRAINT = 1456
 
 
@@ -76,6 +79,8 @@ def parse():
                     help="skip the differentiable rollout measurement")
     ap.add_argument("--no-barrier", action="store_true",
                     help="skip the barrier-terms-at-scale measurement (slab stacks)")
+    ap.add_argument("--barrier-columns", type=int, default=4,
+                    help="slab stacks of the barrier measurement: N x N columns of 2 slabs")
     ap.add_argument("--sim-steps", type=int, default=20)
     ap.add_argument("--batch-sim-steps", type=int, default=2,
                     help="timed steps of the batched time step (0 skips it)")
@@ -815,7 +820,7 @@ def main():
     if rank == 0 and not args.no_configs:
         line["per_config"] = per_config(args, torch)
     if rank == 0 and not args.no_barrier:
-        line["barrier_at_scale"] = barrier_rate(torch)
+        line["barrier_at_scale"] = barrier_rate(torch, n=args.barrier_columns)
     if rank == 0 and not args.no_cpu_baseline:
         base = cpu_baseline(sc, x0, x1, dhat)
         v = combined_rate(n_ccd, n_disc, base["ccd_pairs_per_s"], base["barrier_pairs_per_s"])

@@ -140,16 +140,33 @@ __device__ __forceinline__ void add_curvature(SMat H, const double* frame, int l
 
 // ---------------------------------------------------------------------------
 // PSD projection of one 12x12 (upper triangle filled, in the entry-major
-// layout of its owner thread) by the whole warp: parallel cyclic Jacobi in
-// round-robin order (each round rotates six disjoint (p, q) planes at once,
-// eleven rounds visit all 66 pairs), then V max(L, 0) V^T.  As
-// project_to_psd does, a matrix whose eigenvalues are all >= 0 is left as it
-// is.  Rotation (c, s) per plane follows the textbook symmetric Schur step:
+// layout of its owner thread) by the whole warp: V max(L, 0) V^T from the
+// eigen-decomposition A = V L V^T.  As project_to_psd does, a matrix whose
+// eigenvalues are all >= 0 is left as it is.
+//
+// The decomposition is a parallel cyclic Jacobi in round-robin order (each
+// round rotates six disjoint (p, q) planes at once, eleven rounds visit all
+// 66 pairs), run twice:
+//  1. in single precision on A rounded to float, to convergence: it gives
+//     eigenvectors V32 accurate to single precision;
+//  2. in double precision on B = Q^T A Q, Q being V32 orthonormalised in
+//     double; B is diagonal up to the single-precision error, so the Jacobi
+//     sweeps converge quadratically from there (two or three sweeps where
+//     seven or eight were needed from A itself), the rotations accumulated
+//     into Q.
+// An FP64 warp instruction costs this GPU's FP64 unit 64 cycles whatever its
+// active lanes, a single-precision one one cycle of issue, so the sweeps of
+// step 1 are nearly free and the FP64 work drops to a few 12 x 12 products
+// and the refining sweeps.  The double-precision stopping rule is the one-step
+// method's (off-diagonal sum of squares <= 1e-30 of the diagonal's), so the
+// result is the same decomposition to rounding.
+// Rotation (c, s) per plane follows the textbook symmetric Schur step:
 // theta = (a_qq - a_pp) / (2 a_pq), t = sign(theta) / (|theta| +
 // sqrt(theta^2 + 1)), c = 1 / sqrt(t^2 + 1), s = t c.
 
 constexpr int kLd = 13;  // padded row stride of the warp's work matrices
-constexpr int kWorkDoubles = 2 * 12 * kLd + 16;
+// doubles: A, Q, T, U (12 x kLd each), 6 (c, s); then floats A32, V32, 6 (c, s)
+constexpr int kWorkDoubles = 4 * 12 * kLd + 16 + (2 * 12 * kLd + 16) / 2;
 
 // round-robin schedule over 12 indices: round r pairs (11, pos0) and
 // (pos_k, pos_{11-k}), pos_k = (k + r) mod 11, stored with p < q
@@ -167,45 +184,40 @@ static __constant__ unsigned char kRoundPairs[11][6][2] = {
     { { 10, 11 }, { 0, 9 }, { 1, 8 }, { 2, 7 }, { 3, 6 }, { 4, 5 } },
 };
 
-__device__ __forceinline__ double warp_sum(double v)
+template <class T> __device__ __forceinline__ T warp_sum(T v)
 {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
 
-static __device__ void warp_psd_project(SMat H, double* work, int lane)
+// Cyclic Jacobi on the warp's A (12 x kLd, symmetric) accumulating the
+// rotations into V, until the off-diagonal sum of squares is <= tol of the
+// diagonal's (or max_sweeps); cs holds 12 scalars of scratch.
+template <class T>
+__device__ void warp_jacobi(T* A, T* V, T* cs, int lane, T tol, int max_sweeps)
 {
-    double* A = work;
-    double* V = work + 12 * kLd;
-    double* cs = work + 24 * kLd;   // 6 x (c, s)
-    for (int e = lane; e < 144; e += 32) {
-        int r = e / 12, c = e % 12;
-        A[r * kLd + c] = r <= c ? H.at(r, c) : H.at(c, r);
-        V[r * kLd + c] = r == c ? 1.0 : 0.0;
-    }
-    __syncwarp();
-    for (int sweep = 0; sweep < 30; sweep++) {
-        double off = 0, diag = 0;
+    for (int sweep = 0; sweep < max_sweeps; sweep++) {
+        T off = 0, diag = 0;
         for (int e = lane; e < 144; e += 32) {
             int r = e / 12, c = e % 12;
-            double v = A[r * kLd + c];
+            T v = A[r * kLd + c];
             if (r == c) diag += v * v;
             else if (r < c) off += v * v;
         }
         off = warp_sum(off);
         diag = warp_sum(diag);
-        if (off <= 1e-30 * diag || off == 0.0) break;
+        if (off <= tol * diag || off == T(0)) break;
         for (int round = 0; round < 11; round++) {
             if (lane < 6) {
                 int p = kRoundPairs[round][lane][0], q = kRoundPairs[round][lane][1];
-                double apq = A[p * kLd + q];
-                double c = 1.0, sn = 0.0;
-                if (apq != 0.0) {
-                    double app = A[p * kLd + p], aqq = A[q * kLd + q];
-                    double theta = (aqq - app) / (2 * apq);
-                    double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1));
-                    c = 1.0 / sqrt(t * t + 1);
+                T apq = A[p * kLd + q];
+                T c = 1, sn = 0;
+                if (apq != T(0)) {
+                    T app = A[p * kLd + p], aqq = A[q * kLd + q];
+                    T theta = (aqq - app) / (2 * apq);
+                    T t = (theta >= 0 ? T(1) : T(-1)) / (fabs(theta) + sqrt(theta * theta + 1));
+                    c = T(1) / sqrt(t * t + 1);
                     sn = t * c;
                 }
                 cs[2 * lane] = c;
@@ -214,12 +226,12 @@ static __device__ void warp_psd_project(SMat H, double* work, int lane)
             __syncwarp();
             // columns of A and V: 2 x 6 planes x 12 rows
             for (int it = lane; it < 144; it += 32) {
-                double* M = it < 72 ? A : V;
+                T* M = it < 72 ? A : V;
                 int j = it < 72 ? it : it - 72;
                 int pr = j % 6, k = j / 6;
                 int p = kRoundPairs[round][pr][0], q = kRoundPairs[round][pr][1];
-                double c = cs[2 * pr], sn = cs[2 * pr + 1];
-                double mkp = M[k * kLd + p], mkq = M[k * kLd + q];
+                T c = cs[2 * pr], sn = cs[2 * pr + 1];
+                T mkp = M[k * kLd + p], mkq = M[k * kLd + q];
                 M[k * kLd + p] = c * mkp - sn * mkq;
                 M[k * kLd + q] = sn * mkp + c * mkq;
             }
@@ -228,17 +240,78 @@ static __device__ void warp_psd_project(SMat H, double* work, int lane)
             for (int it = lane; it < 72; it += 32) {
                 int pr = it % 6, k = it / 6;
                 int p = kRoundPairs[round][pr][0], q = kRoundPairs[round][pr][1];
-                double c = cs[2 * pr], sn = cs[2 * pr + 1];
-                double apk = A[p * kLd + k], aqk = A[q * kLd + k];
+                T c = cs[2 * pr], sn = cs[2 * pr + 1];
+                T apk = A[p * kLd + k], aqk = A[q * kLd + k];
                 A[p * kLd + k] = c * apk - sn * aqk;
                 A[q * kLd + k] = sn * apk + c * aqk;
             }
             __syncwarp();
         }
     }
+}
+
+// C = op(X) Y for 12 x 12 matrices with row stride kLd (op(X) = X or X^T),
+// by the warp, entry-strided over the lanes
+__device__ __forceinline__ void warp_mm(const double* X, bool xt, const double* Y, double* C, int lane)
+{
+    for (int e = lane; e < 144; e += 32) {
+        const int r = e / 12, c = e % 12;
+        double acc = 0;
+        for (int k = 0; k < 12; k++) acc += (xt ? X[k * kLd + r] : X[r * kLd + k]) * Y[k * kLd + c];
+        C[r * kLd + c] = acc;
+    }
+    __syncwarp();
+}
+
+static __device__ void warp_psd_project(SMat H, double* work, int lane)
+{
+    double* A = work;               // the matrix
+    double* Q = work + 12 * kLd;    // eigenvectors
+    double* T = work + 24 * kLd;    // scratch, then B = Q^T A Q
+    double* U = work + 36 * kLd;    // scratch
+    double* cs = work + 48 * kLd;   // 6 x (c, s)
+    float* A32 = reinterpret_cast<float*>(work + 48 * kLd + 16);
+    float* V32 = A32 + 12 * kLd;
+    float* cs32 = V32 + 12 * kLd;
+    // 1. single-precision eigenvectors
+    for (int e = lane; e < 144; e += 32) {
+        int r = e / 12, c = e % 12;
+        const double a = r <= c ? H.at(r, c) : H.at(c, r);
+        A[r * kLd + c] = a;
+        A32[r * kLd + c] = (float)a;
+        V32[r * kLd + c] = r == c ? 1.0f : 0.0f;
+    }
+    __syncwarp();
+    warp_jacobi<float>(A32, V32, cs32, lane, 1e-14f, 12);
+    // 2. orthonormalise them in double (two Newton-Schulz steps
+    // Q <- Q (3 I - Q^T Q) / 2: the single-precision rotations leave them
+    // orthogonal to ~1e-6, each step squares that)
+    for (int e = lane; e < 144; e += 32) Q[(e / 12) * kLd + e % 12] = (double)V32[(e / 12) * kLd + e % 12];
+    __syncwarp();
+    for (int step = 0; step < 2; step++) {
+        warp_mm(Q, true, Q, T, lane);
+        for (int e = lane; e < 144; e += 32) {
+            const int r = e / 12, c = e % 12;
+            T[r * kLd + c] = (r == c ? 1.5 : 0.0) - 0.5 * T[r * kLd + c];
+        }
+        __syncwarp();
+        warp_mm(Q, false, T, U, lane);
+        for (int e = lane; e < 144; e += 32) Q[(e / 12) * kLd + e % 12] = U[(e / 12) * kLd + e % 12];
+        __syncwarp();
+    }
+    // 3. B = Q^T A Q (symmetric: the upper triangle, mirrored), then the
+    // double-precision Jacobi from there, the rotations accumulated into Q
+    warp_mm(A, false, Q, U, lane);
+    warp_mm(Q, true, U, T, lane);
+    for (int e = lane; e < 144; e += 32) {
+        const int r = e / 12, c = e % 12;
+        if (r > c) T[r * kLd + c] = T[c * kLd + r];
+    }
+    __syncwarp();
+    warp_jacobi<double>(T, Q, cs, lane, 1e-30, 30);
     double wmin = INFINITY;
 #pragma unroll
-    for (int i = 0; i < 12; i++) wmin = fmin(wmin, A[i * kLd + i]);
+    for (int i = 0; i < 12; i++) wmin = fmin(wmin, T[i * kLd + i]);
     if (wmin >= 0.0) return;  // already PSD: keep the matrix as it is
     // rebuild the upper triangle: sum over positive eigenvalues
     for (int e = lane; e < 144; e += 32) {
@@ -246,8 +319,8 @@ static __device__ void warp_psd_project(SMat H, double* work, int lane)
         if (r > c) continue;
         double acc = 0;
         for (int k = 0; k < 12; k++) {
-            double w = A[k * kLd + k];
-            if (w > 0) acc += V[r * kLd + k] * w * V[c * kLd + k];
+            double w = T[k * kLd + k];
+            if (w > 0) acc += Q[r * kLd + k] * w * Q[c * kLd + k];
         }
         H.at(r, c) = acc;
     }

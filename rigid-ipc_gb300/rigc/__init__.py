@@ -359,9 +359,11 @@ class Context:
                  velocity_conv_tol=1e-2, velocity_conv_tol_abs=False,
                  line_search_lower_bound=1e-12, dhat_epsilon=1e-9,
                  min_barrier_stiffness_scale=1e11, newton_polish=0, ccd_rescale=1.0,
-                 poses=None, velocities=None, Qdot=None):
+                 poses=None, velocities=None, Qdot=None, world_bbox_diagonal=None):
         """Start a simulation from the scene's poses, velocities and Qdot (or
-        from the given host arrays: poses / velocities nb x 6, Qdot nb x 9)."""
+        from the given host arrays: poses / velocities nb x 6, Qdot nb x 9).
+        world_bbox_diagonal (default: that of the start poses) bounds the
+        barrier stiffness; a resumed run passes the one of the scene as read."""
         sc = self.scene
         V = sc.world_vertices(sc.poses() if poses is None
                               else np.asarray(poses, np.float64).reshape(-1))
@@ -378,7 +380,8 @@ class Context:
         p.dhat_epsilon = dhat_epsilon
         p.min_barrier_stiffness_scale = min_barrier_stiffness_scale
         p.average_mass = sc.average_mass
-        p.world_bbox_diagonal = float(np.linalg.norm(V.max(0) - V.min(0)))
+        p.world_bbox_diagonal = (float(np.linalg.norm(V.max(0) - V.min(0)))
+                                 if world_bbox_diagonal is None else float(world_bbox_diagonal))
         p.newton_polish = int(newton_polish)
         p.ccd_rescale = float(ccd_rescale)
         fixed = np.array([int(sum(1 << k for k in range(6) if b.is_dof_fixed[k]))
