@@ -5,6 +5,11 @@ Run from the repository root (CPU only; about ten minutes on 8 cores):
 
     python tests/golden/make_adjoint_fixture.py
 
+and, for the central differences of every parameter (1,536 rollouts, about
+an hour and a half on 8 cores):
+
+    python tests/golden/make_adjoint_fixture.py --all-parameters
+
 Workload: 64 unit cubes in a 4 x 4 x 4 lattice (spacing 1.05 m, seeded
 rotations, lowest layer 0.5 m above a static 20 x 20 m plane, at rest),
 50 implicit-Euler steps of 0.01 s, dhat = 1e-3, no friction; the lowest
@@ -170,5 +175,47 @@ def main():
                         **scene_arrays(sc))
 
 
+FD_ALL_OUT = os.path.join(HERE, "adjoint_cube_lattice_fd.npz")
+
+
+def _loss_param(job):
+    """Loss with one initial velocity component (body b, component k)
+    shifted by delta."""
+    b, k, delta = job
+    d = np.zeros((65, 6))
+    d[b, k] = delta
+    return _loss(d)
+
+
+def main_all_parameters(workers):
+    """Central differences of the loss for every one of the 384 parameters
+    (the 64 cubes' initial linear and angular velocities) at h = 1e-6 and at
+    h / 2, each from two rollouts of the oracle: 1,536 rollouts, spread over
+    `workers` processes.  Written to adjoint_cube_lattice_fd.npz: fd_h and
+    fd_h2 (64 x 6, the cubes' rows in the order of the scene), their
+    Richardson extrapolation (4 D(h/2) - D(h)) / 3, the step sizes."""
+    _paths()
+    import oracle as O
+
+    O.build()
+    sc = lattice_scene()
+    nb = sc.num_bodies
+    hs = (FD_H, FD_H / 2)
+    jobs = [(b, k, s * h) for h in hs for b in range(nb - 1) for k in range(6)
+            for s in (1.0, -1.0)]
+    t = time.time()
+    with mp.get_context("spawn").Pool(workers) as pool:
+        losses = np.array(pool.map(_loss_param, jobs, chunksize=4))
+    losses = losses.reshape(len(hs), nb - 1, 6, 2)
+    fd = np.array([(losses[i, :, :, 0] - losses[i, :, :, 1]) / (2 * h) for i, h in enumerate(hs)])
+    np.savez_compressed(FD_ALL_OUT, fd_h=fd[0], fd_h2=fd[1],
+                        fd_extrapolated=(4 * fd[1] - fd[0]) / 3, h=np.float64(hs[0]),
+                        steps=np.int64(STEPS), seed=np.int64(SEED))
+    print(f"wrote {FD_ALL_OUT}: {len(jobs)} rollouts in {time.time() - t:.0f}s")
+
+
 if __name__ == "__main__":
-    main()
+    if "--all-parameters" in sys.argv:
+        main_all_parameters(int(os.environ.get("FD_WORKERS", max(1, (os.cpu_count() or 2) - 1))))
+    else:
+        main()
