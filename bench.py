@@ -42,19 +42,23 @@ CCD_BYTES_PER_PAIR = 304        # ids + 4 rest vertices + 4 poses + toi
 # launches), from ncu captures of the 200-icosphere pile (132,242
 # candidates): k_ccd 56.95 MB read + 311.51 MB written over two launches
 # (per-lane candidate state spilling from L1, the frame cache);
-# k_ccd_warp<1> 20.95 MB + 15.81 MB over three; k_ccd_warp<4> (128
-# registers, one interval bound per lane) 27.51 MB + 43.86 MB over three,
+# k_ccd_group<32, 1> (one search per warp) 20.95 MB + 15.81 MB over
+# three; k_ccd_group<32, 4> (fitted to 4 blocks per SM: 128 registers, one
+# interval bound per lane) 27.51 MB + 43.86 MB over three,
 # most of the writes its spills.  The traffic of a full call is this times
 # its candidates.  FP64 figures of the same captures: pipe active (fraction
 # of peak) and lane-level GFLOP/s (dadd + dmul + 2 dfma over the launch).
 K_CCD_DRAM_BYTES_PER_CANDIDATE = {
     "k_ccd": (42209536 + 14743808 + 310226176 + 1279232) / 132242,
-    "k_ccd_warp<1>": (17837312 + 2597632 + 512000 + 15804928 + 1792) / 132242,
-    "k_ccd_warp<4>": (22857216 + 3941120 + 714752 + 43766272 + 90880 + 2304) / 132242}
+    "k_ccd_group<32, 1>": (17837312 + 2597632 + 512000 + 15804928 + 1792) / 132242,
+    "k_ccd_group<32, 4>": (22857216 + 3941120 + 714752 + 43766272 + 90880 + 2304) / 132242}
 K_CCD_FP64 = {"k_ccd": {"pipe_active": 0.233, "lane_gflops": 53.0},
-              "k_ccd_warp<1>": {"pipe_active": 0.496, "lane_gflops": 98.4},
-              "k_ccd_warp<4>": {"pipe_active": 0.381, "lane_gflops": 100.9}}
+              "k_ccd_group<32, 1>": {"pipe_active": 0.496, "lane_gflops": 98.4},
+              "k_ccd_group<32, 4>": {"pipe_active": 0.381, "lane_gflops": 100.9}}
 BARRIER_BYTES_PER_CONSTRAINT = 1456
+# the CCD kernel of each search mode (rigc_set_tune's ccd_warp)
+CCD_KERNELS = {0: "k_ccd", 1: "k_ccd_group<32, 1>", 2: "k_ccd_group<32, 4>",
+               3: "k_ccd_group<32, 5>", 4: "k_ccd_group<16, 1>", 5: "k_ccd_group<16, 4>"}
 
 
 def parse():
@@ -72,7 +76,8 @@ def parse():
     ap.add_argument("--ccd-warp", type=int, default=None,
                     help="CCD kernel variant for the headline pass instead of the autotuner's "
                          "(rigc_set_tune's ccd_warp: 0 per lane, 1 per warp, 2 / 3 per warp "
-                         "fitted to 4 / 5 blocks per SM)")
+                         "fitted to 4 / 5 blocks per SM, 4 per half-warp, 5 per half-warp "
+                         "fitted to 4 blocks per SM)")
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the per-configuration pass rates")
     ap.add_argument("--no-adjoint", action="store_true",
@@ -773,9 +778,9 @@ def main():
 
     peak, peak_kind = measured_peaks()
     # the CCD kernel the context launches: one search per warp unless tuned
-    # to one per lane
+    # otherwise
     ccd_mode = tune.get("ccd_warp", -1) if tune else -1
-    ccd_kernel = {0: "k_ccd", 2: "k_ccd_warp<4>", 3: "k_ccd_warp<5>"}.get(ccd_mode, "k_ccd_warp<1>")
+    ccd_kernel = CCD_KERNELS.get(ccd_mode, "k_ccd_group<32, 1>")
     fp64 = fp64_peak() if rank == 0 else None
     ccd_bytes = CCD_BYTES_PER_PAIR * n_ccd
     achieved = ccd_bytes / t_ccd / 1e9

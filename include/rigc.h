@@ -401,7 +401,7 @@ int rigc_sim_scene_params(rigc_ctx* ctx, const double* average_mass,
  * cache's slots per body, the CCD searches per candidate,
  * k_barrier_local's constraints per warp, the CCD boxes a search piece
  * evaluates before handing its pending boxes to the next launch, one CCD
- * search per lane or per warp -- one
+ * search per lane, per warp or per half-warp -- one
  * after the other (median of three runs each), over the continuous
  * candidates of x0 -> x1 and the constraint set at x0 (device poses), and
  * keeps the fastest in the context for every later call.  rigc_set_tune
@@ -425,9 +425,11 @@ int rigc_autotune(rigc_ctx* ctx, const double* x0, const double* x1, double dhat
  * searches spread over the whole GPU (0: never; -1: the built-in 64).  The
  * earliest time of impact depends on neither.  ccd_warp: 0 searches one
  * candidate per lane (k_ccd), 1 one per warp with the lanes
- * evaluating each box together (k_ccd_warp: a tenth of the FP64 chain per
- * box; the built-in choice, -1), 2 / 3 the same fitted to 4 / 5 blocks per
- * SM (fewer registers, more warps to hide latency).
+ * evaluating each box together (k_ccd_group<32>: a tenth of the FP64 chain
+ * per box; the built-in choice, -1), 2 / 3 the same fitted to 4 / 5 blocks
+ * per SM (fewer registers, more warps to hide latency), 4 one per half-warp
+ * (k_ccd_group<16>: two searches share each instruction of the warp), 5 the
+ * same fitted to 4 blocks per SM.
  * The results are the same bits either way. */
 int rigc_set_tune(rigc_ctx* ctx, int32_t ccd_blocks_per_sm, int32_t cache_slots_per_body,
                   int32_t barrier_per_warp, int32_t ccd_seeds_log2, int32_t ccd_hand_off,

@@ -627,7 +627,7 @@ int rigc_set_tune(rigc_ctx* ctx, int32_t ccd_blocks_per_sm, int32_t cache_slots_
 {
     if (!ctx || ccd_blocks_per_sm < 0 || cache_slots_per_body < 0 || barrier_per_warp < 0
         || barrier_per_warp > 32 || cache_slots_per_body > (1 << 16) || ccd_seeds_log2 < -1
-        || ccd_seeds_log2 > 5 || ccd_hand_off < -1 || ccd_warp < -1 || ccd_warp > 3)
+        || ccd_seeds_log2 > 5 || ccd_hand_off < -1 || ccd_warp < -1 || ccd_warp > 5)
         return RIGC_ERR_ARG;
     Ctx& c = *ctx_of(ctx);
     c.tune.ccd_blocks_per_sm = ccd_blocks_per_sm;

@@ -1,6 +1,6 @@
 // Autotuner of the narrow phase's launch shapes on a caller's workload.
 //
-// Three shapes are searched, one after the other, each by timing the call
+// Six shapes are searched, one after the other, each by timing the call
 // it shapes (one warm-up, then the median of three runs) on the context's
 // own scenes:
 //  * k_ccd's resident blocks per SM (1 .. the occupancy limit): fewer blocks
@@ -10,8 +10,9 @@
 //  * the CCD searches per candidate (1 .. 32, from the nodes of its
 //    subdivision tree at that depth): more fill the GPU when candidates are
 //    few or deep, fewer skip the nodes above that depth;
-//  * one CCD search per lane (k_ccd) or per warp (k_ccd_warp, as compiled
-//    or fitted to 4 or 5 blocks per SM), first;
+//  * one CCD search per lane (k_ccd), per warp (k_ccd_group<32>, as
+//    compiled or fitted to 4 or 5 blocks per SM) or per half-warp
+//    (k_ccd_group<16>, as compiled or fitted to 4 blocks per SM), first;
 //  * the CCD boxes a search piece evaluates before it hands its pending
 //    boxes to a further launch (never, 16, the built-in 64, 256): short
 //    pieces spread deep searches over the GPU, each hand-off costs a launch;
@@ -71,10 +72,10 @@ int autotune(Ctx& c, const double* x0, const double* x1, double dhat, double dmi
     };
     RIGC_TRY(median_ms(ccd, &r.ccd_ms_default));
     double best = r.ccd_ms_default;
-    // one search per lane, per warp, or per warp at 4 or 5 blocks per SM
-    // (the default: per warp)
+    // one search per lane, per warp (as compiled, at 4 or 5 blocks per SM)
+    // or per half-warp (as compiled, at 4 blocks per SM); the default: per warp
     int best_mode = ccd_search_mode(c);
-    for (int mode : { 0, 1, 2, 3 }) {
+    for (int mode : { 0, 1, 2, 3, 4, 5 }) {
         if (mode == best_mode) continue;
         c.tune.ccd_warp = mode;
         double ms;

@@ -601,7 +601,7 @@ k_barrier_local(BarrierArgs a, int per_warp)
     bool built = mine && barrier_build(a, ci, H);
     if (!(a.flags & RIGC_HESS)) return;  // uniform over the block
     if (a.flags & RIGC_PROJECT_PSD) {
-        double* work = smem + 144 * kBarrierTPB;
+        double* work = smem + kSymEntries * kBarrierTPB;
         unsigned todo = __ballot_sync(0xffffffffu, built);
         while (todo) {
             int t = __ffs(todo) - 1;
@@ -614,7 +614,7 @@ k_barrier_local(BarrierArgs a, int per_warp)
 
 size_t local_terms_smem_bytes()
 {
-    return (size_t)(144 * kBarrierTPB + kWorkDoubles) * sizeof(double);
+    return (size_t)(kSymEntries * kBarrierTPB + kWorkDoubles) * sizeof(double);
 }
 
 // constraints per warp: a thread per constraint once there are enough of

@@ -416,34 +416,38 @@ static __device__ __noinline__ int eval_vertices(const CCDArgs& a, const OwnFram
     return 0;
 }
 
-// Batched frame computation, executed by the whole warp.  For each lane
-// with a missing frame (body, node n at depth d), the 31 lanes compute the
-// frames of the five-level subtree below n's parent (n, its sibling and
-// their descendants down to depth d + 3), publish them in the cache, and the
-// requesting lane (every lane with to_all) receives n's frame.  The depth-first search keeps asking
-// for those nodes, so one converged pass replaces up to 31 single-lane
-// rotation enclosures.
-static __device__ __noinline__ void warp_compute_frames(const CCDArgs& a, OwnFrames& own,
-                                                        unsigned req, int req_side,
-                                                        int req_body,
-                                                        unsigned long long req_node,
-                                                        bool to_all = false)
+// Batched frame computation, executed by a group of W lanes (the whole
+// warp, or one half of it).  For each lane of the group with a missing frame
+// (body, node n at depth d), the W - 1 other lanes compute the frames of the
+// subtree below n's parent (n, its sibling and their descendants down to
+// depth d + 3 for a warp, d + 2 for a half-warp), publish them in the cache,
+// and the requesting lane (every lane of the group with to_all) receives n's
+// frame.  The depth-first search keeps asking for those nodes, so one
+// converged pass replaces up to W - 1 single-lane rotation enclosures.
+template <int W>
+static __device__ __noinline__ void group_compute_frames(const CCDArgs& a, OwnFrames& own,
+                                                         unsigned req, int req_side,
+                                                         int req_body,
+                                                         unsigned long long req_node,
+                                                         bool to_all = false)
 {
     const int lane = threadIdx.x & 31;
+    const int gl = lane & (W - 1);
+    const unsigned gmask = W == 32 ? 0xffffffffu : (0xffffu << (lane & 16));
     while (req) {
         const int src = __ffs(req) - 1;
         req &= req - 1;
-        const int side = __shfl_sync(0xffffffffu, req_side, src);
-        const int body = __shfl_sync(0xffffffffu, req_body, src);
-        const unsigned long long node = __shfl_sync(0xffffffffu, req_node, src);
+        const int side = __shfl_sync(gmask, req_side, src, W);
+        const int body = __shfl_sync(gmask, req_body, src, W);
+        const unsigned long long node = __shfl_sync(gmask, req_node, src, W);
         const int d = 63 - __clzll((long long)node);           // node depth (>= kTableDepth)
         const unsigned long long root = node >> 1;             // depth d - 1
-        // lane L < 31: subtree node L + 1 below root, level l = log2(L + 1)
-        const int l = 31 - __clz(lane + 1);
-        const unsigned long long mine = (root << l) + (unsigned long long)(lane + 1 - (1 << l));
+        // lane L < W - 1: subtree node L + 1 below root, level l = log2(L + 1)
+        const int l = 31 - __clz(gl + 1);
+        const unsigned long long mine = (root << l) + (unsigned long long)(gl + 1 - (1 << l));
         const int dm = d - 1 + l;
         Itv R[9], p[3];
-        const bool work = lane < 31 && l >= 1 && dm < kNodeDepth;
+        const bool work = gl < W - 1 && l >= 1 && dm < kNodeDepth;
         if (work) {
             const unsigned long long k = mine - (1ull << dm);
             const Itv t { ldexp((double)k, -dm), ldexp((double)(k + 1), -dm) };
@@ -455,15 +459,15 @@ static __device__ __noinline__ void warp_compute_frames(const CCDArgs& a, OwnFra
         double f[kTableEntry];
 #pragma unroll
         for (int j = 0; j < 9; j++) {
-            f[2 * j] = __shfl_sync(0xffffffffu, R[j].lo, owner);
-            f[2 * j + 1] = __shfl_sync(0xffffffffu, R[j].hi, owner);
+            f[2 * j] = __shfl_sync(gmask, R[j].lo, owner, W);
+            f[2 * j + 1] = __shfl_sync(gmask, R[j].hi, owner, W);
         }
 #pragma unroll
         for (int j = 0; j < 3; j++) {
-            f[18 + 2 * j] = __shfl_sync(0xffffffffu, p[j].lo, owner);
-            f[19 + 2 * j] = __shfl_sync(0xffffffffu, p[j].hi, owner);
+            f[18 + 2 * j] = __shfl_sync(gmask, p[j].lo, owner, W);
+            f[19 + 2 * j] = __shfl_sync(gmask, p[j].hi, owner, W);
         }
-        if (to_all || lane == src) {
+        if (to_all || gl == src) {
             own.key[side] = frame_key(body, node);
 #pragma unroll
             for (int j = 0; j < kTableEntry; j++) own.f[side][j] = f[j];
@@ -708,7 +712,7 @@ k_ccd(CCDArgs a)
         // frames asked for in the last iteration, computed by the whole warp
         const unsigned req = __ballot_sync(0xffffffffu, pend);
         if (req) {
-            warp_compute_frames(a, own, req, req_side, req_body, req_node);
+            group_compute_frames<32>(a, own, req, req_side, req_body, req_node);
             pend = false;
         }
         // Once the candidate list is exhausted, a lane with nothing left takes
@@ -968,14 +972,25 @@ k_ccd(CCDArgs a)
 }
 
 // ---------------------------------------------------------------------------
-// One search per warp.  The same branch and bound, pruning, seeds, budget and
-// search pieces as k_ccd, but a box is evaluated by the whole warp: lane
-// 3 v + c (v < 4, c < 3) computes coordinate c of vertex v's interval
-// position (the coordinate expression of iworld_vertex) and lanes 0..2 the
-// interval distance function's coordinate c (the expression of f_zero), so
-// the chain of FP64 instructions per box is about a tenth of one lane's and
-// the lanes stay converged.  The search state is identical in every lane;
-// lane 0 does the atomics.  Same bits as k_ccd for every box.
+// One search per group of W lanes: the whole warp (W = 32) or each half of
+// it (W = 16, two searches per warp).  The same branch and bound, pruning,
+// seeds, budget and search pieces as k_ccd, but a box is evaluated by the
+// group's lanes together, each FP64 expression of the box on its own lane:
+//  * W = 32: lane 12 b + 3 v + c computes bound b (0 lower, 1 upper) of
+//    coordinate c of vertex v's interval position (iworld_vertex's
+//    expression for that bound: a lower bound takes only lower-bound
+//    operations);
+//  * W = 16: lane 3 v + c computes that coordinate's interval (both bounds);
+//  * both: lane 6 b + 3 h + c computes bound b of half h of the interval
+//    distance function's coordinate c (f_zero's expressions), the lanes with
+//    h = 0 combine the halves, and a vote of the group decides.
+// The chain of FP64 instructions per box is a tenth of one lane's.  With
+// W = 16 the two searches of a warp share every instruction they execute
+// together (the search control, which all lanes of a group execute on the
+// same state, and the FP64 of the box), at the price of running apart where
+// their paths differ.  The search state is identical in every lane of a
+// group; the group's first lane does the atomics.  Same bits as k_ccd for
+// every box.
 
 // rest vertex v of a candidate (EE: a0 a1 b0 b1; FV: v f0 f1 f2), its bodies
 // and kind
@@ -1055,22 +1070,27 @@ __device__ __forceinline__ unsigned long long* gmin_body(const CCDArgs& a, int b
 
 // MinBlocks > 1 asks the compiler to fit that many blocks per SM (fewer
 // registers, some spilled to local memory, more warps to hide latency)
-template <int MinBlocks>
+template <int W, int MinBlocks>
 __global__ void __launch_bounds__(kCCDThreads, MinBlocks)
-k_ccd_warp(CCDArgs a)
+k_ccd_group(CCDArgs a)
 {
+    static_assert(W == 32 || W == 16, "a warp or a half-warp per search");
     const int64_t n = a.nee + a.nfv;
     const int64_t nwork = a.pieces_in ? a.n_pieces : (n << a.seeds_log2);
     const int lane = threadIdx.x & 31;
-    // vertex lanes 0..23: bound vb (0 lower, 1 upper) of coordinate crd of
-    // vertex vtx; distance lanes 0..11: bound db of the half dh of the
+    const int gl = lane & (W - 1);  // lane within the group
+    const unsigned gmask = W == 32 ? 0xffffffffu : (0xffffu << (lane & 16));
+    const int gshift = W == 32 ? 0 : (lane & 16);
+    // vertex lanes: W = 32, lanes 0..23: bound vb of coordinate crd of
+    // vertex vtx; W = 16, lanes 0..11: the interval of coordinate crd of
+    // vertex vtx.  Distance lanes 0..11: bound db of the half dh of the
     // distance function's coordinate dc
-    const int vb = lane >= 12 ? 1 : 0;
-    const int vtx = (lane % 12) / 3, crd = lane % 3;
-    const bool vlane = lane < 24;
-    const int db = lane >= 6 ? 1 : 0, dh = (lane % 6) / 3, dc = lane % 3;
+    const int vb = W == 32 && gl >= 12 ? 1 : 0;
+    const int vtx = (gl % 12) / 3, crd = gl % 3;
+    const bool vlane = gl < (W == 32 ? 24 : 12);
+    const int db = gl >= 6 ? 1 : 0, dh = (gl % 6) / 3, dc = gl % 3;
     unsigned long long tot_boxes = 0, tot_hits = 0, pops = 0;
-    // search state (the same in every lane)
+    // search state (the same in every lane of the group)
     Node cn { { 0, 0, 0 }, { 0ull, 0ull, 0ull }, 0 };
     bool has_cn = false;
     u128 pend_hi = 0, mt = 0, ma = 0;
@@ -1085,9 +1105,10 @@ k_ccd_warp(CCDArgs a)
     TolKeys tkeys { { 0, 0, 0 }, false };
     bool fv = false, a_fixed = false, b_fixed = false;
     int body_a = 0, body_b = 0;
-    // this lane's vertex and its bound of the coordinate interval over [ct0, ct1]
+    // this lane's vertex and its bound (W = 32) or interval (W = 16) of the
+    // coordinate over [ct0, ct1]
     double rv[3] = { 0, 0, 0 };
-    double pcrd = 0;
+    Itv pcrd { 0, 0 };
     const double nan = __longlong_as_double(0x7ff8000000000000ll);
     double ct0 = nan, ct1 = nan;
     bool fresh = true;
@@ -1099,10 +1120,10 @@ k_ccd_warp(CCDArgs a)
         if (tail && hand_ok && cboxes >= a.hand_off && (pend_hi != 0 || has_cn)) {
             const int k = popc128(pend_hi) + (has_cn ? 1 : 0);
             unsigned long long s = 0;
-            if (lane == 0) s = atomicAdd(a.n_out, (unsigned long long)k);
-            s = __shfl_sync(0xffffffffu, s, 0);
+            if (gl == 0) s = atomicAdd(a.n_out, (unsigned long long)k);
+            s = __shfl_sync(gmask, s, 0, W);
             if (s + k <= a.out_cap) {
-                if (lane == 0) {
+                if (gl == 0) {
                     Piece pc;
                     pc.cand = cur;
                     pc.earliest = earliest;
@@ -1129,7 +1150,7 @@ k_ccd_warp(CCDArgs a)
                 pend_hi = 0;
                 has_cn = false;
             } else {
-                if (lane == 0)
+                if (gl == 0)
                     for (unsigned long long t = s; t < s + k && t < a.out_cap; t++) a.pieces_out[t].cand = -1;
                 hand_ok = false;
             }
@@ -1148,12 +1169,12 @@ k_ccd_warp(CCDArgs a)
             if (le_nn(earliest, x.t0)) continue;
             if (a.prune) {
                 if ((++pops & 7) == 0) {
-                    // values read while other warps write them: lane 0's
-                    // copy for all, so that the warp's state stays uniform
-                    gbound = __shfl_sync(0xffffffffu, __longlong_as_double(
-                        (long long)*(volatile unsigned long long*)gmin_body(a, body_a)), 0);
-                    tail = __shfl_sync(0xffffffffu,
-                        (int)(*(volatile unsigned long long*)a.next >= (unsigned long long)nwork), 0) != 0;
+                    // values read while other warps write them: the group's
+                    // first lane's copy for all, so that its state stays uniform
+                    gbound = __shfl_sync(gmask, __longlong_as_double(
+                        (long long)*(volatile unsigned long long*)gmin_body(a, body_a)), 0, W);
+                    tail = __shfl_sync(gmask,
+                        (int)(*(volatile unsigned long long*)a.next >= (unsigned long long)nwork), 0, W) != 0;
                 }
                 if (le_nn(gbound, x.t0)) continue;
             }
@@ -1165,7 +1186,7 @@ k_ccd_warp(CCDArgs a)
             break;
         }
         if (!have) {
-            if (cur >= 0 && lane == 0) {
+            if (cur >= 0 && gl == 0) {
                 if (found) {
                     unsigned long long* g = gmin_body(a, body_a);
                     const unsigned long long b = (unsigned long long)__double_as_longlong(earliest);
@@ -1178,9 +1199,9 @@ k_ccd_warp(CCDArgs a)
             }
             // next work item: seed w / n of candidate w % n, or piece w
             long long w = 0;
-            if (lane == 0) w = (long long)atomicAdd(a.next, 1ull);
-            w = __shfl_sync(0xffffffffu, w, 0);
-            if (w >= nwork) break;  // the warp is done
+            if (gl == 0) w = (long long)atomicAdd(a.next, 1ull);
+            w = __shfl_sync(gmask, w, 0, W);
+            if (w >= nwork) break;  // the group is done
             tail = tail || w + 1 >= nwork;
             found = false;
             status = RIGC_OK;
@@ -1215,8 +1236,8 @@ k_ccd_warp(CCDArgs a)
             tol[2] = a.ctol[3 * cur + 2];
             tkeys = tol_keys(tol);
             if (a.prune)
-                gbound = __shfl_sync(0xffffffffu, __longlong_as_double(
-                    (long long)*(volatile unsigned long long*)gmin_body(a, body_a)), 0);
+                gbound = __shfl_sync(gmask, __longlong_as_double(
+                    (long long)*(volatile unsigned long long*)gmin_body(a, body_a)), 0, W);
             if (a.pieces_in) continue;  // the piece's node is popped next
             cn = seed_node(a.seeds_log2, w / n, tol, mt, ma);
             x = node_box(cn);
@@ -1252,39 +1273,42 @@ k_ccd_warp(CCDArgs a)
             if (need) {
                 Itv r[3], pc;
                 if (frame_find_row(a, own, side, side ? body_b : body_a, node, t, crd, r, pc)) {
-                    // one bound of iworld_vertex's coordinate expression
-                    // iadd(iadd(iadd(imul(v0, r0), imul(v1, r1)), imul(v2, r2)), p):
-                    // the lower bound takes only lower-bound operations, the
-                    // upper only upper
-                    if (vb == 0) {
+                    // W = 32 keeps its one bound in pcrd.lo
+                    if (W == 16) {
+                        pcrd = iadd(iadd(iadd(imul(rv[0], r[0]), imul(rv[1], r[1])), imul(rv[2], r[2])), pc);
+                    } else if (vb == 0) {
+                        // one bound of iworld_vertex's coordinate expression
+                        // iadd(iadd(iadd(imul(v0, r0), imul(v1, r1)), imul(v2, r2)), p):
+                        // the lower bound takes only lower-bound operations, the
+                        // upper only upper
                         double q = mul_dn(rv[0], is_neg(rv[0]) ? r[0].hi : r[0].lo);
                         q = add_dn(q, mul_dn(rv[1], is_neg(rv[1]) ? r[1].hi : r[1].lo));
                         q = add_dn(q, mul_dn(rv[2], is_neg(rv[2]) ? r[2].hi : r[2].lo));
-                        pcrd = add_dn(q, pc.lo);
+                        pcrd.lo = add_dn(q, pc.lo);
                     } else {
                         double q = mul_up(rv[0], is_neg(rv[0]) ? r[0].lo : r[0].hi);
                         q = add_up(q, mul_up(rv[1], is_neg(rv[1]) ? r[1].lo : r[1].hi));
                         q = add_up(q, mul_up(rv[2], is_neg(rv[2]) ? r[2].lo : r[2].hi));
-                        pcrd = add_up(q, pc.hi);
+                        pcrd.lo = add_up(q, pc.hi);
                     }
                 } else {
                     miss = true;
                 }
             }
-            const unsigned mm = __ballot_sync(0xffffffffu, miss);
+            const unsigned mm = __ballot_sync(gmask, miss) >> gshift;
             if (mm) {
-                // the warp computes the missing frames (lane 0 asks for body
-                // A's, lane 1 for body B's), every lane keeps them; retry
+                // the group computes the missing frames (its lane 0 asks for
+                // body A's, lane 1 for body B's), every lane keeps them; retry
                 bool miss_a = false, miss_b = false;
 #pragma unroll
-                for (int l = 0; l < 24; l++)
+                for (int l = 0; l < (W == 32 ? 24 : 12); l++)
                     if ((mm >> l) & 1) {
                         if ((l % 12) / 3 < na) miss_a = true;
                         else miss_b = true;
                     }
                 const unsigned req = (miss_a ? 1u : 0u) | (miss_b ? 2u : 0u);
-                warp_compute_frames(a, own, req, lane == 1 ? 1 : 0, lane == 1 ? body_b : body_a, node,
-                                    true);
+                group_compute_frames<W>(a, own, req, gl == 1 ? 1 : 0, gl == 1 ? body_b : body_a,
+                                        node, true);
                 ct0 = ct1 = nan;
                 has_cn = true;
                 continue;
@@ -1294,7 +1318,7 @@ k_ccd_warp(CCDArgs a)
             ct1 = x.t1;
         }
         cboxes++;
-        if (lane == 0) tot_boxes++;
+        if (gl == 0) tot_boxes++;
         // f(box) contains zero: the expressions and operand order of f_zero,
         // each interval bound on its own lane.  Distance lane (db, dh, dc)
         // evaluates bound db of half dh of coordinate dc (EE: the point of
@@ -1304,12 +1328,36 @@ k_ccd_warp(CCDArgs a)
         // y = P0 - ((part0 + part1) + P1).  A lower bound takes only lower
         // bounds of its operands (and upper bounds of subtrahends), so the
         // bits are those of the interval expressions.
-        // vertex v's bound b of coordinate c lives on lane 12 b + 3 v + c
         const int va = fv ? (dh ? 3 : 2) : (dh ? 3 : 1);
         const int vq = fv ? 1 : (dh ? 2 : 0);
-        const double A = __shfl_sync(0xffffffffu, pcrd, 12 * db + 3 * va + dc);
-        const double Bx = __shfl_sync(0xffffffffu, pcrd, 12 * (1 - db) + 3 * vq + dc);
-        const double Bs = __shfl_sync(0xffffffffu, pcrd, 12 * db + 3 * vq + dc);
+        double A, Bx, Bs, P0 = 0, P1 = 0;
+        if (W == 32) {
+            // vertex v's bound b of coordinate c lives on lane 12 b + 3 v + c
+            A = __shfl_sync(gmask, pcrd.lo, 12 * db + 3 * va + dc);
+            Bx = __shfl_sync(gmask, pcrd.lo, 12 * (1 - db) + 3 * vq + dc);
+            Bs = __shfl_sync(gmask, pcrd.lo, 12 * db + 3 * vq + dc);
+            if (fv) {
+                P1 = __shfl_sync(gmask, pcrd.lo, 12 * db + 3 + dc);
+                P0 = __shfl_sync(gmask, pcrd.lo, 12 * db + dc);
+            }
+        } else {
+            // vertex v's interval of coordinate c lives on lane 3 v + c
+            const double alo = __shfl_sync(gmask, pcrd.lo, 3 * va + dc, W);
+            const double ahi = __shfl_sync(gmask, pcrd.hi, 3 * va + dc, W);
+            const double qlo = __shfl_sync(gmask, pcrd.lo, 3 * vq + dc, W);
+            const double qhi = __shfl_sync(gmask, pcrd.hi, 3 * vq + dc, W);
+            A = db ? ahi : alo;
+            Bx = db ? qlo : qhi;
+            Bs = db ? qhi : qlo;
+            if (fv) {
+                const double p1lo = __shfl_sync(gmask, pcrd.lo, 3 + dc, W);
+                const double p1hi = __shfl_sync(gmask, pcrd.hi, 3 + dc, W);
+                const double p0lo = __shfl_sync(gmask, pcrd.lo, dc, W);
+                const double p0hi = __shfl_sync(gmask, pcrd.hi, dc, W);
+                P1 = db ? p1hi : p1lo;
+                P0 = db ? p0hi : p0lo;
+            }
+        }
         const Itv pw = dh ? Itv { x.b0, x.b1 } : Itv { x.a0, x.a1 };
         double part;
         if (db == 0) {
@@ -1323,18 +1371,16 @@ k_ccd_warp(CCDArgs a)
         }
         // the other half's bound: EE the opposite bound, FV the same
         const int osrc = 6 * (fv ? db : 1 - db) + 3 + dc;
-        const double other = __shfl_sync(0xffffffffu, part, osrc);
+        const double other = __shfl_sync(gmask, part, osrc, W);
         bool zin = true;
         if (fv) {
-            const double P1 = __shfl_sync(0xffffffffu, pcrd, 12 * db + 3 + dc);
-            const double P0 = __shfl_sync(0xffffffffu, pcrd, 12 * db + dc);
             const double tb = db == 0 ? add_dn(add_dn(part, other), P1) : add_up(add_up(part, other), P1);
-            const double tx = __shfl_sync(0xffffffffu, tb, (6 * (1 - db) + dc) & 31);
-            if (lane < 12 && dh == 0) zin = db == 0 ? !is_pos(sub_dn(P0, tx)) : !is_neg(sub_up(P0, tx));
-        } else if (lane < 12 && dh == 0) {
+            const double tx = __shfl_sync(gmask, tb, 6 * (1 - db) + dc, W);
+            if (gl < 12 && dh == 0) zin = db == 0 ? !is_pos(sub_dn(P0, tx)) : !is_neg(sub_up(P0, tx));
+        } else if (gl < 12 && dh == 0) {
             zin = db == 0 ? !is_pos(sub_dn(part, other)) : !is_neg(sub_up(part, other));
         }
-        if (!__all_sync(0xffffffffu, zin)) continue;
+        if (!__all_sync(gmask, zin)) continue;
         double w[3];
         node_widths(cn, w);
         bool all_tol = le_nn(w[0], tol[0]) && le_nn(w[1], tol[1]) && le_nn(w[2], tol[2]);
@@ -1343,7 +1389,7 @@ k_ccd_warp(CCDArgs a)
             earliest = x.t0;
             found = true;
             if (a.prune) {
-                if (lane == 0) {
+                if (gl == 0) {
                     const unsigned long long b = (unsigned long long)__double_as_longlong(earliest);
                     if (a.scene_gmin) atomicMin(gmin_body(a, body_a), b);
                     atomicMin(a.gmin, b);
@@ -1362,7 +1408,7 @@ k_ccd_warp(CCDArgs a)
         descend(cn, pend_hi, mt, ma, split);
         has_cn = true;
     }
-    if (lane == 0) {
+    if (gl == 0) {
         if (tot_boxes) atomicAdd(a.boxes, tot_boxes);
         if (tot_hits) atomicAdd(a.hits, tot_hits);
     }
@@ -1374,28 +1420,32 @@ __global__ void k_fill_inf(double* __restrict__ v, int64_t n)
     if (i < n) v[i] = INFINITY;
 }
 
-// resident k_ccd blocks per SM at full occupancy
-// resident blocks per SM of the CCD kernel of a search mode (0: k_ccd,
-// 1: k_ccd_warp, 2 / 3: k_ccd_warp fitted to 4 / 5 blocks per SM)
+// resident blocks per SM of the CCD kernel of a search mode (0: k_ccd;
+// 1, 2, 3: one search per warp, as compiled and fitted to 4 and 5 blocks per
+// SM; 4, 5: one search per half-warp, as compiled and fitted to 4 blocks)
+constexpr int kSearchModes = 6;
+
 int ccd_max_blocks_per_sm(int* out, int mode)
 {
-    static int blocks_per_sm[4] = { 0, 0, 0, 0 };
+    static int blocks_per_sm[kSearchModes] = { 0, 0, 0, 0, 0, 0 };
+    if (mode < 0 || mode >= kSearchModes) return RIGC_ERR_ARG;
     int& b = blocks_per_sm[mode];
     if (!b) {
-        if (mode == 3)
-            RIGC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_ccd_warp<5>, kCCDThreads, 0));
-        else if (mode == 2)
-            RIGC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_ccd_warp<4>, kCCDThreads, 0));
-        else if (mode == 1)
-            RIGC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_ccd_warp<1>, kCCDThreads, 0));
-        else RIGC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_ccd, kCCDThreads, 0));
+        switch (mode) {
+        case 5: RIGC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_ccd_group<16, 4>, kCCDThreads, 0)); break;
+        case 4: RIGC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_ccd_group<16, 1>, kCCDThreads, 0)); break;
+        case 3: RIGC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_ccd_group<32, 5>, kCCDThreads, 0)); break;
+        case 2: RIGC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_ccd_group<32, 4>, kCCDThreads, 0)); break;
+        case 1: RIGC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_ccd_group<32, 1>, kCCDThreads, 0)); break;
+        default: RIGC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_ccd, kCCDThreads, 0));
+        }
         if (b < 1) b = 1;
     }
     *out = b;
     return RIGC_OK;
 }
 
-// the search mode: one search per warp (k_ccd_warp) unless the context's
+// the search mode: one search per warp (k_ccd_group<32, 1>) unless the context's
 // tuning asks for another; per warp measured faster than per lane on every
 // workload here (the 1000-icosphere pile, the 256-scene batch, the cube
 // lattices, the chain)
@@ -1494,7 +1544,8 @@ int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flag
             k_fill_inf<<<grid_for(n, 256), 256, 0, st>>>(per, n);
         }
         const int mode = ccd_search_mode(c);
-        const int per_block = mode ? kCCDThreads / 32 : kCCDThreads;  // searches per block
+        // searches per block
+        const int per_block = mode >= 4 ? kCCDThreads / 16 : mode ? kCCDThreads / 32 : kCCDThreads;
         int blocks_per_sm;
         RIGC_TRY(ccd_max_blocks_per_sm(&blocks_per_sm, mode));
         int dev = 0, sms = kNumSMs;
@@ -1534,10 +1585,14 @@ int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flag
         for (int launch = 0;; launch++) {
             RIGC_COUNT_LAUNCH();
             const unsigned grid = (unsigned)std::min(want, full);
-            if (mode == 3) k_ccd_warp<5><<<grid, kCCDThreads, 0, st>>>(a);
-            else if (mode == 2) k_ccd_warp<4><<<grid, kCCDThreads, 0, st>>>(a);
-            else if (mode == 1) k_ccd_warp<1><<<grid, kCCDThreads, 0, st>>>(a);
-            else k_ccd<<<grid, kCCDThreads, 0, st>>>(a);
+            switch (mode) {
+            case 5: k_ccd_group<16, 4><<<grid, kCCDThreads, 0, st>>>(a); break;
+            case 4: k_ccd_group<16, 1><<<grid, kCCDThreads, 0, st>>>(a); break;
+            case 3: k_ccd_group<32, 5><<<grid, kCCDThreads, 0, st>>>(a); break;
+            case 2: k_ccd_group<32, 4><<<grid, kCCDThreads, 0, st>>>(a); break;
+            case 1: k_ccd_group<32, 1><<<grid, kCCDThreads, 0, st>>>(a); break;
+            default: k_ccd<<<grid, kCCDThreads, 0, st>>>(a);
+            }
             RIGC_CUDA(cudaGetLastError());
             if (!a.hand_off) break;
             unsigned long long np = 0;

@@ -275,7 +275,7 @@ k_friction_local(FrictionArgs a, int per_warp)
     bool built = mine && friction_build(a, ci, H);
     if (!(a.flags & RIGC_HESS)) return;  // uniform over the block
     if (a.flags & RIGC_PROJECT_PSD) {
-        double* work = smem + 144 * kBarrierTPB;
+        double* work = smem + kSymEntries * kBarrierTPB;
         unsigned todo = __ballot_sync(0xffffffffu, built);
         while (todo) {
             int t = __ffs(todo) - 1;

@@ -31,12 +31,14 @@ __device__ __forceinline__ double dot(const double* a, const double* b)
     return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
 }
 
-// shared-memory 12x12 accumulator, entry-major / thread-minor
+// shared-memory symmetric 12x12 accumulator: the upper triangle (r <= c)
+// packed row by row (78 entries), entry-major / thread-minor
+constexpr int kSymEntries = 78;
 struct SMat {
     double* base;
     __device__ __forceinline__ double& at(int r, int c) const
     {
-        return base[(r * 12 + c) * kBarrierTPB];
+        return base[(r * (23 - r) / 2 + c) * kBarrierTPB];
     }
 };
 
@@ -139,8 +141,8 @@ __device__ __forceinline__ void add_curvature(SMat H, const double* frame, int l
 }
 
 // ---------------------------------------------------------------------------
-// PSD projection of one 12x12 (upper triangle filled, in the entry-major
-// layout of its owner thread) by the whole warp: V max(L, 0) V^T from the
+// PSD projection of one 12x12 (upper triangle filled, in the packed layout
+// of its owner thread) by the whole warp: V max(L, 0) V^T from the
 // eigen-decomposition A = V L V^T.  As project_to_psd does, a matrix whose
 // eigenvalues are all >= 0 is left as it is.
 //
@@ -159,36 +161,79 @@ __device__ __forceinline__ void add_curvature(SMat H, const double* frame, int l
 // step 1 are nearly free and the FP64 work drops to a few 12 x 12 products
 // and the refining sweeps.  The double-precision stopping rule is the one-step
 // method's (off-diagonal sum of squares <= 1e-30 of the diagonal's), so the
-// result is the same decomposition to rounding.
+// result is the same decomposition to rounding.  (A double-precision
+// refinement of V32 by matrix products alone, with no rotations, does not
+// reach double precision when the eigenvalues span more decades than single
+// precision resolves, as these Hessians' do.)
 // Rotation (c, s) per plane follows the textbook symmetric Schur step:
 // theta = (a_qq - a_pp) / (2 a_pq), t = sign(theta) / (|theta| +
-// sqrt(theta^2 + 1)), c = 1 / sqrt(t^2 + 1), s = t c.
+// sqrt(theta^2 + 1)), c = 1 / sqrt(t^2 + 1), s = t c; the single-precision
+// sweeps take it with the fast reciprocal and reciprocal square root (they
+// only seed step 2).
 
 constexpr int kLd = 13;  // padded row stride of the warp's work matrices
-// doubles: A, Q, T, U (12 x kLd each), 6 (c, s); then floats A32, V32, 6 (c, s)
+// doubles: A, Q, T, U (12 x kLd each), 6 (c, s) + 4; then floats A32, V32
+// (12 x kLd each), 6 (c, s) + 4
 constexpr int kWorkDoubles = 4 * 12 * kLd + 16 + (2 * 12 * kLd + 16) / 2;
 
-// round-robin schedule over 12 indices: round r pairs (11, pos0) and
-// (pos_k, pos_{11-k}), pos_k = (k + r) mod 11, stored with p < q
-static __constant__ unsigned char kRoundPairs[11][6][2] = {
-    { { 0, 11 }, { 1, 10 }, { 2, 9 }, { 3, 8 }, { 4, 7 }, { 5, 6 } },
-    { { 1, 11 }, { 0, 2 }, { 3, 10 }, { 4, 9 }, { 5, 8 }, { 6, 7 } },
-    { { 2, 11 }, { 1, 3 }, { 0, 4 }, { 5, 10 }, { 6, 9 }, { 7, 8 } },
-    { { 3, 11 }, { 2, 4 }, { 1, 5 }, { 0, 6 }, { 7, 10 }, { 8, 9 } },
-    { { 4, 11 }, { 3, 5 }, { 2, 6 }, { 1, 7 }, { 0, 8 }, { 9, 10 } },
-    { { 5, 11 }, { 4, 6 }, { 3, 7 }, { 2, 8 }, { 1, 9 }, { 0, 10 } },
-    { { 6, 11 }, { 5, 7 }, { 4, 8 }, { 3, 9 }, { 2, 10 }, { 0, 1 } },
-    { { 7, 11 }, { 6, 8 }, { 5, 9 }, { 4, 10 }, { 0, 3 }, { 1, 2 } },
-    { { 8, 11 }, { 7, 9 }, { 6, 10 }, { 0, 5 }, { 1, 4 }, { 2, 3 } },
-    { { 9, 11 }, { 8, 10 }, { 0, 7 }, { 1, 6 }, { 2, 5 }, { 3, 4 } },
-    { { 10, 11 }, { 0, 9 }, { 1, 8 }, { 2, 7 }, { 3, 6 }, { 4, 5 } },
-};
+// round-robin schedule over 12 indices: round r pairs (r, 11) and
+// (pos_k, pos_{11-k}) for k = 1 .. 5, pos_k = (k + r) mod 11; (p, q) with p < q
+__device__ __forceinline__ void round_pair(int round, int k, int& p, int& q)
+{
+    if (k == 0) {
+        p = round;
+        q = 11;
+        return;
+    }
+    int a = k + round, b = 11 - k + round;
+    a = a >= 11 ? a - 11 : a;
+    b = b >= 11 ? b - 11 : b;
+    p = min(a, b);
+    q = max(a, b);
+}
+
+// row and column of upper-triangle entry u (row-major, 0 <= u < 78)
+__device__ __forceinline__ void upper_rc(int u, int& r, int& c)
+{
+    r = 0;
+    int start = 0;
+    while (u >= start + 12 - r) {
+        start += 12 - r;
+        r++;
+    }
+    c = r + (u - start);
+}
 
 template <class T> __device__ __forceinline__ T warp_sum(T v)
 {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
+}
+
+__device__ __forceinline__ void jacobi_angle(float app, float aqq, float apq, float& c, float& s)
+{
+    const float theta = __fdividef(aqq - app, 2.0f * apq);
+    const float at = fabsf(theta);
+    // |theta| > 2^40: t = 1 / (2 theta) to single precision (and theta^2 is
+    // not formed)
+    float t;
+    if (at > 1.0995116e12f) {
+        t = __fdividef(0.5f, at);
+    } else {
+        const float h = fmaf(theta, theta, 1.0f);
+        t = __frcp_rn(at + h * rsqrtf(h));
+    }
+    t = theta >= 0.0f ? t : -t;
+    c = rsqrtf(fmaf(t, t, 1.0f));
+    s = t * c;
+}
+__device__ __forceinline__ void jacobi_angle(double app, double aqq, double apq, double& c, double& s)
+{
+    const double theta = (aqq - app) / (2 * apq);
+    const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1));
+    c = 1.0 / sqrt(t * t + 1);
+    s = t * c;
 }
 
 // Cyclic Jacobi on the warp's A (12 x kLd, symmetric) accumulating the
@@ -210,16 +255,11 @@ __device__ void warp_jacobi(T* A, T* V, T* cs, int lane, T tol, int max_sweeps)
         if (off <= tol * diag || off == T(0)) break;
         for (int round = 0; round < 11; round++) {
             if (lane < 6) {
-                int p = kRoundPairs[round][lane][0], q = kRoundPairs[round][lane][1];
+                int p, q;
+                round_pair(round, lane, p, q);
                 T apq = A[p * kLd + q];
                 T c = 1, sn = 0;
-                if (apq != T(0)) {
-                    T app = A[p * kLd + p], aqq = A[q * kLd + q];
-                    T theta = (aqq - app) / (2 * apq);
-                    T t = (theta >= 0 ? T(1) : T(-1)) / (fabs(theta) + sqrt(theta * theta + 1));
-                    c = T(1) / sqrt(t * t + 1);
-                    sn = t * c;
-                }
+                if (apq != T(0)) jacobi_angle(A[p * kLd + p], A[q * kLd + q], apq, c, sn);
                 cs[2 * lane] = c;
                 cs[2 * lane + 1] = sn;
             }
@@ -229,7 +269,8 @@ __device__ void warp_jacobi(T* A, T* V, T* cs, int lane, T tol, int max_sweeps)
                 T* M = it < 72 ? A : V;
                 int j = it < 72 ? it : it - 72;
                 int pr = j % 6, k = j / 6;
-                int p = kRoundPairs[round][pr][0], q = kRoundPairs[round][pr][1];
+                int p, q;
+                round_pair(round, pr, p, q);
                 T c = cs[2 * pr], sn = cs[2 * pr + 1];
                 T mkp = M[k * kLd + p], mkq = M[k * kLd + q];
                 M[k * kLd + p] = c * mkp - sn * mkq;
@@ -239,7 +280,8 @@ __device__ void warp_jacobi(T* A, T* V, T* cs, int lane, T tol, int max_sweeps)
             // rows of A: 6 planes x 12 columns
             for (int it = lane; it < 72; it += 32) {
                 int pr = it % 6, k = it / 6;
-                int p = kRoundPairs[round][pr][0], q = kRoundPairs[round][pr][1];
+                int p, q;
+                round_pair(round, pr, p, q);
                 T c = cs[2 * pr], sn = cs[2 * pr + 1];
                 T apk = A[p * kLd + k], aqk = A[q * kLd + k];
                 A[p * kLd + k] = c * apk - sn * aqk;
@@ -314,12 +356,12 @@ static __device__ void warp_psd_project(SMat H, double* work, int lane)
     for (int i = 0; i < 12; i++) wmin = fmin(wmin, T[i * kLd + i]);
     if (wmin >= 0.0) return;  // already PSD: keep the matrix as it is
     // rebuild the upper triangle: sum over positive eigenvalues
-    for (int e = lane; e < 144; e += 32) {
-        int r = e / 12, c = e % 12;
-        if (r > c) continue;
+    for (int u = lane; u < kSymEntries; u += 32) {
+        int r, c;
+        upper_rc(u, r, c);
         double acc = 0;
         for (int k = 0; k < 12; k++) {
-            double w = T[k * kLd + k];
+            const double w = T[k * kLd + k];
             if (w > 0) acc += Q[r * kLd + k] * w * Q[c * kLd + k];
         }
         H.at(r, c) = acc;

@@ -1,9 +1,10 @@
 """The CUDA path on the reference's own CCD test data (fixtures packed by
 tests/golden/make_reference_fixtures.py, oracle results stored with them):
 per-query and per-candidate times of impact bit-exact, the wrecking-ball
-scene's candidate set identical, with one search per lane (k_ccd) and one
-per warp (k_ccd_warp, as compiled and fitted to 4 or 5 blocks per SM)
-alike."""
+scene's candidate set identical, with one search per lane (k_ccd), one
+per warp (k_ccd_group<32>, as compiled and fitted to 4 or 5 blocks per SM)
+and one per half-warp (k_ccd_group<16>, as compiled and fitted to 4 blocks
+per SM) alike."""
 import os
 
 import numpy as np
@@ -14,7 +15,7 @@ from test_reference_fixtures import queries, scene_fixture
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("warp", [0, 1, 2, 3])
+@pytest.mark.parametrize("warp", [0, 1, 2, 3, 4, 5])
 def test_reference_queries_gpu(warp):
     """All 403 queries in one context, candidates given explicitly."""
     import make_reference_fixtures as M
@@ -56,7 +57,7 @@ def test_reference_queries_gpu(warp):
     assert toi == expect.min()
 
 
-@pytest.mark.parametrize("warp", [0, 1, 2, 3])
+@pytest.mark.parametrize("warp", [0, 1, 2, 3, 4, 5])
 def test_wrecking_ball_scene_gpu(warp):
     import make_reference_fixtures as M
     import rigc
