@@ -15,8 +15,18 @@ it):
   differentiation form).  With the reference's default tolerance (1e-2) a
   perturbation of 1e-15 in the initial poses grows to 1e-8 by step 11 and
   to 1e-2 by step 39 (the iterates are not converged, so rounding changes
-  the Newton decisions); with these settings it stays near 1e-12 over all
-  100 steps, so two implementations can be compared over the whole run;
+  the Newton decisions).  With these settings it stays below 1e-13 until
+  the landing steps, jumps to ~2e-8 in one of them and then grows linearly
+  (a difference of ~1e-7 m/s in a frictionless sliding velocity) to ~1e-6
+  by step 100;
+* cubes_tight_branches: that sensitivity, resolved: the landing step where
+  the jump happens ends its Newton solve at one of two iterations (the line
+  search compares energies at the rounding level), and the two outcomes
+  differ by 2e-8; the runs from initial poses perturbed by 1e-15 N(0, 1)
+  (four seeds) that took the other outcome, with their minimum distances.
+  A run that differs from the oracle's only in rounding follows one of
+  these trajectories (to ~1e-13 per step), not necessarily the unperturbed
+  one;
 * pair: two cubes landing on the plane and sliding into each other with
   friction (mu 0.5), 10 steps;
 * pile: 8 subdivision-3 icospheres in a seeded contact pile (2e-4 m gaps)
@@ -118,10 +128,49 @@ def main():
     out["cubes_tight_digest"] = out["cubes_digest"]
     (out["cubes_tight_poses"], out["cubes_tight_kappa"], out["cubes_tight_crossings"],
      out["cubes_tight_min_distance"]) = run(sc, CUBE_STEPS, probes=True, **TIGHT)
+    add_branches(out)
     np.savez_compressed(OUT, **out)
     print(f"wrote {OUT}: crossings per cube step {out['cubes_crossings'].max()}, "
           f"{out['cubes_tight_crossings'].max()} (tight)")
 
 
+BRANCH_SEEDS = (1, 2, 3, 4)
+
+
+def _perturbed_run(seed):
+    sc = cubes_scene()
+    x0 = sc.poses() + 1e-15 * np.random.default_rng(seed).standard_normal(sc.poses().shape)
+    poses, _, _, md = run(sc, CUBE_STEPS, x0=x0, probes=True, **TIGHT)
+    return poses, md
+
+
+def add_branches(out):
+    """cubes_tight_branches / cubes_tight_branches_min_distance: the
+    perturbed runs (one process per seed) that leave the unperturbed one by
+    more than 1e-10 at some step, one per distinct trajectory."""
+    import multiprocessing as mp
+
+    with mp.get_context("spawn").Pool(len(BRANCH_SEEDS)) as pool:
+        runs = pool.map(_perturbed_run, BRANCH_SEEDS)
+    kept = [out["cubes_tight_poses"]]
+    poses, md = [], []
+    for p, m in runs:
+        if min(np.abs(p[1:] - k[1:]).max() for k in kept) > 1e-10:
+            kept.append(p)
+            poses.append(p)
+            md.append(m)
+        print("seed run: largest difference to the unperturbed run",
+              np.abs(p - out["cubes_tight_poses"]).max())
+    out["cubes_tight_branches"] = np.array(poses).reshape(-1, *out["cubes_tight_poses"].shape)
+    out["cubes_tight_branches_min_distance"] = np.array(md).reshape(-1, CUBE_STEPS)
+
+
 if __name__ == "__main__":
-    main()
+    if "--branches" in sys.argv:
+        # only the branch entries, added to the existing file
+        out = dict(np.load(OUT))
+        add_branches(out)
+        np.savez_compressed(OUT, **out)
+        print(f"{len(out['cubes_tight_branches'])} branch trajectories")
+    else:
+        main()

@@ -1,8 +1,9 @@
 """The device time step (rigc_sim_*) against the oracle's restated step:
-the closed-form free fall, and the 27-cube scene over several steps (poses
-within 1e-7: the Newton systems are solved by different methods, an LDL^T on
-the CPU and preconditioned conjugate gradients to a 1e-12 residual on the
-GPU, so the iterates agree to the solve accuracy, not bit for bit)."""
+the closed-form free fall, a few steps of the 27-cube scene, of a 216-cube
+lattice (the conjugate-gradient path) and of kinematic bodies (poses within
+1e-7: the iterates agree to the accuracy of the Newton solves, not bit for
+bit), and whole runs against the oracle's trajectories in
+tests/golden/step_trajectories.npz at 1e-8."""
 import os
 
 import numpy as np
@@ -113,16 +114,22 @@ def _fixture(key, sc, x0):
 
 
 def test_cube_lattice_whole_run_matches_oracle():
-    """All 100 steps of the 27-cube lattice (landings from step ~30) with
-    every Newton solve converged to rounding: poses within 1e-8 of the
-    oracle's after every step, no crossing edge and face after any step on
-    either side, and the same minimum distance."""
+    """All 100 steps of the 27-cube lattice (landings from step ~20) with
+    every Newton solve converged to rounding: after every step the poses are
+    within 1e-8 of one of the oracle's trajectories -- the unperturbed run or
+    a run from start poses perturbed by 1e-15 that took the other outcome of
+    the landing step whose Newton solve ends at one of two iterations (the
+    two outcomes differ by 2e-8); no crossing edge and face after any step on
+    either side; the minimum distance of the matched oracle run."""
     import rigc
 
     import make_step_fixtures as SF
 
     sc = SF.cubes_scene()
     fx = _fixture("cubes_tight", sc, sc.poses())
+    runs = [fx["cubes_tight_poses"], *fx["cubes_tight_branches"]]
+    mds = [fx["cubes_tight_min_distance"], *fx["cubes_tight_branches_min_distance"]]
+    assert len(runs) >= 2  # the fixture resolves the two outcomes
     ctx = rigc.Context(sc)
     ctx.sim_init(SF.H, SF.G, SF.DHAT, **SF.TIGHT)
     assert fx["cubes_tight_crossings"].max() == 0
@@ -131,10 +138,11 @@ def test_cube_lattice_whole_run_matches_oracle():
         ctx.sim_step(1)
         P, V, Q, kappa = ctx.sim_state()
         x = P.reshape(-1)
-        err = np.abs(x - fx["cubes_tight_poses"][k + 1]).max()
-        assert err <= POSE_ATOL, (k, err)
+        errs = [np.abs(x - r[k + 1]).max() for r in runs]
+        j = int(np.argmin(errs))
+        assert errs[j] <= POSE_ATOL, (k, errs)
         assert ctx.detect_intersections(x) == 0, k
-        md_o = fx["cubes_tight_min_distance"][k]
+        md_o = mds[j][k]
         md = ctx.compute_min_distance(x, SF.DHAT)
         assert (md < 0) == (md_o < 0), k
         if md_o > 0:
