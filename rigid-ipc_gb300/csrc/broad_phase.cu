@@ -877,13 +877,26 @@ __global__ void k_cell_pairs(const uint64_t* __restrict__ keys, const uint32_t* 
                              const float* __restrict__ f32, PairOut o)
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m) return;
-    const uint64_t ki = keys[i];
+    // the end of each item's run (same scene, cell and group): the warp's 32
+    // consecutive items mark where a run ends, and an item takes the first
+    // mark at or after it; a run that goes on past the warp's items is
+    // followed in memory
+    const int lane = threadIdx.x & 31;
+    const bool valid = i < m;
+    const uint64_t ki = valid ? keys[i] : 0;
+    const bool last = !valid || i + 1 >= m || (keys[i + 1] >> 3) != (ki >> 3);
+    const unsigned ends = __ballot_sync(0xffffffffu, last) & (0xffffffffu << lane);
+    if (!valid) return;
     const uint64_t run = ki >> 3;                 // (scene, cell, group)
     const uint64_t cellk = ki >> (3 + group_bits);  // (scene, cell)
     const unsigned fa = (unsigned)(ki & 7);
-    int64_t j = i + 1;
-    while (j < m && (keys[j] >> 3) == run) j++;
+    int64_t j;
+    if (ends) {
+        j = i - lane + (__ffs(ends) - 1) + 1;
+    } else {
+        j = i - lane + 32;
+        while (j < m && (keys[j] >> 3) == run) j++;
+    }
     const uint32_t a = vals[i];
     const int ta = a >> 30, ia = a & 0x3fffffff;
     for (; j < m; j++) {
@@ -930,13 +943,28 @@ __global__ void k_large_pairs(const uint32_t* __restrict__ large, int nl, int ro
     }
 }
 
-__global__ void k_decode_pairs(const unsigned long long* __restrict__ keys, int64_t n,
-                               unsigned long long stride, int2* __restrict__ out)
+// the two pair streams as one array of sort keys: EE keys as they are, FV
+// keys with bit tbit set (above every key of either stream), values 0 .. n-1
+__global__ void k_pack_pairs(const unsigned long long* __restrict__ kee, int64_t nee,
+                             const unsigned long long* __restrict__ kfv, int64_t nfv, int tbit,
+                             unsigned long long* __restrict__ keys, uint32_t* __restrict__ vals)
 {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    unsigned long long k = keys[i];
-    out[i] = make_int2((int)(k / stride), (int)(k % stride));
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nee + nfv) return;
+    keys[i] = i < nee ? kee[i] : (kfv[i - nee] | (1ull << tbit));
+    vals[i] = (uint32_t)i;
+}
+
+// sorted keys back to (first, second) pairs: EE first (stride ne), then FV
+__global__ void k_decode_pairs(const unsigned long long* __restrict__ keys, int64_t nee, int64_t nfv,
+                               int tbit, unsigned long long ee_stride, unsigned long long fv_stride,
+                               int2* __restrict__ out_ee, int2* __restrict__ out_fv)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nee + nfv) return;
+    const unsigned long long k = keys[i] & ((1ull << tbit) - 1);
+    if (i < nee) out_ee[i] = make_int2((int)(k / ee_stride), (int)(k % ee_stride));
+    else out_fv[i - nee] = make_int2((int)(k / fv_stride), (int)(k % fv_stride));
 }
 
 __global__ void k_iota(uint32_t* __restrict__ v, int64_t n)
@@ -1151,29 +1179,24 @@ int detect_pairs(Ctx& c, const double* x0, const double* x1, bool continuous, do
     // keys f * ne + e
     const unsigned long long fv_stride = kind == kPairsEF ? (unsigned long long)s.ne
                                                           : (unsigned long long)s.nv;
-    int64_t nmax = std::max(nee, nfv);
-    RIGC_TRY(c.pair_key.reserve((size_t)nmax * 8 + 8));
-    RIGC_TRY(S[0].reserve((size_t)nmax * 4 + 8));
-    RIGC_TRY(S[1].reserve((size_t)nmax * 4 + 8));
-    if (nee > 0) {
+    // one sort of both streams (FV keys above EE keys by a type bit)
+    const int tbit = std::max(bits_for((uint64_t)s.ne * (uint64_t)s.ne),
+                              bits_for((uint64_t)s.nf * fv_stride));
+    const int64_t np = nee + nfv;
+    RIGC_TRY(c.pair_key.reserve((size_t)np * 8 + 8));
+    RIGC_TRY(S[0].reserve((size_t)np * 4 + 8));
+    RIGC_TRY(S[1].reserve((size_t)np * 4 + 8));
+    if (np > 0) {
         RIGC_COUNT_LAUNCH();
-        k_iota<<<grid_for(nee, 256), 256, 0, st>>>(S[0].as<uint32_t>(), nee);
-        RIGC_TRY(radix_sort_pairs<uint64_t>(reinterpret_cast<uint64_t*>(kee), S[0].as<uint32_t>(), c.pair_key.as<uint64_t>(),
-                                            S[1].as<uint32_t>(), nee,
-                                            bits_for((uint64_t)s.ne * (uint64_t)s.ne), S[4], S[5], S[7], st));
+        k_pack_pairs<<<grid_for(np, 256), 256, 0, st>>>(kee, nee, kfv, nfv, tbit, c.pair_key.as<unsigned long long>(),
+                                                        S[0].as<uint32_t>());
+        // the packed keys sort into the pair buffer (its streams are consumed)
+        RIGC_TRY(radix_sort_pairs<uint64_t>(c.pair_key.as<uint64_t>(), S[0].as<uint32_t>(),
+                                            reinterpret_cast<uint64_t*>(kee), S[1].as<uint32_t>(), np,
+                                            tbit + 1, S[4], S[5], S[7], st));
         RIGC_COUNT_LAUNCH();
-        k_decode_pairs<<<grid_for(nee, 256), 256, 0, st>>>(c.pair_key.as<unsigned long long>(), nee,
-                                                          (unsigned long long)s.ne, out.ee.as<int2>());
-    }
-    if (nfv > 0) {
-        RIGC_COUNT_LAUNCH();
-        k_iota<<<grid_for(nfv, 256), 256, 0, st>>>(S[0].as<uint32_t>(), nfv);
-        RIGC_TRY(radix_sort_pairs<uint64_t>(reinterpret_cast<uint64_t*>(kfv), S[0].as<uint32_t>(), c.pair_key.as<uint64_t>(),
-                                            S[1].as<uint32_t>(), nfv,
-                                            bits_for((uint64_t)s.nf * fv_stride), S[4], S[5], S[7], st));
-        RIGC_COUNT_LAUNCH();
-        k_decode_pairs<<<grid_for(nfv, 256), 256, 0, st>>>(c.pair_key.as<unsigned long long>(), nfv,
-                                                          fv_stride, out.fv.as<int2>());
+        k_decode_pairs<<<grid_for(np, 256), 256, 0, st>>>(kee, nee, nfv, tbit, (unsigned long long)s.ne,
+                                                          fv_stride, out.ee.as<int2>(), out.fv.as<int2>());
     }
     RIGC_CUDA(cudaGetLastError());
     if (continuous && kind == kPairsEEFV) {
