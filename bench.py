@@ -82,6 +82,8 @@ def parse():
                     help="skip the per-configuration pass rates")
     ap.add_argument("--no-adjoint", action="store_true",
                     help="skip the differentiable rollout measurement")
+    ap.add_argument("--no-pl", action="store_true",
+                    help="skip the piecewise-linear trajectory CCD measurement")
     ap.add_argument("--no-barrier", action="store_true",
                     help="skip the barrier-terms-at-scale measurement (slab stacks)")
     ap.add_argument("--barrier-columns", type=int, default=4,
@@ -189,6 +191,37 @@ def fp64_peak():
         r = rigc.fp64_throughput(op, lanes, 4096)
         out[f"{op}_{lanes}"] = {"gflops": r["gflops"], "warp_inst_per_s": r["warp_inst_per_s"],
                                 "ms": r["ms"]}
+    return out
+
+
+def pl_rate(ctx, sc, x0, x1, x0d, x1d, timed, with_cpu=True, sample=2000):
+    """The piecewise-linear trajectory CCD (the reference's JSON default
+    trajectory) over the headline's continuous candidates: one narrow-phase
+    call, device-timed; the oracle on a seeded sample of the same candidates
+    on every host core beside it."""
+    ee, fv = ctx.detect_collision_candidates_rigid(x0d, x1d, True, 0.0)
+    n = len(ee) + len(fv)
+    t_pl = timed(lambda: ctx.earliest_toi_piecewise_linear(x0d, x1d), reps=1)
+    st = ctx.stats()
+    out = {"workload": "the headline pile's continuous candidates, trajectory PIECEWISE_LINEAR, "
+                       "dmin 0, every candidate searched in full",
+           "candidates": n, "ms": t_pl * 1e3, "pairs_per_s": n / t_pl,
+           "linear_ccd_boxes": st["ccd_boxes"], "kernel": "k_pl_ccd (one candidate per warp)"}
+    if with_cpu:
+        import oracle as O
+
+        O.build()
+        o = O.OracleScene(sc)
+        rng = np.random.default_rng(0)
+        sel = rng.choice(n, size=min(sample, n), replace=False)
+        e_s, f_s = ee[sel[sel < len(ee)]], fv[sel[sel >= len(ee)] - len(ee)]
+        cores = os.cpu_count() or 1
+        t = time.perf_counter()
+        o.pl_earliest_toi(x0, x1, e_s, f_s, nthreads=cores)
+        t = time.perf_counter() - t
+        out["cpu_oracle_pairs_per_s"] = len(sel) / t
+        out["cpu_oracle_cores"] = cores
+        out["cpu_oracle_sample"] = f"{len(sel)} seeded candidates"
     return out
 
 
@@ -826,6 +859,9 @@ def main():
         line["per_config"] = per_config(args, torch)
     if rank == 0 and not args.no_barrier:
         line["barrier_at_scale"] = barrier_rate(torch, n=args.barrier_columns)
+    if rank == 0 and not args.no_pl:
+        line["piecewise_linear"] = pl_rate(ctx, sc, x0, x1, x0d, x1d, timed,
+                                           with_cpu=not args.no_cpu_baseline)
     if rank == 0 and not args.no_cpu_baseline:
         base = cpu_baseline(sc, x0, x1, dhat)
         v = combined_rate(n_ccd, n_disc, base["ccd_pairs_per_s"], base["barrier_pairs_per_s"])

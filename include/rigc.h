@@ -200,6 +200,34 @@ int rigc_compute_earliest_toi(rigc_ctx* ctx, const double* x0,
                               const double* x1, double dmin,
                               double* toi_host);
 
+/* ---- narrow phase CCD, trajectory PIECEWISE_LINEAR (the reference's JSON
+ * default): compute_earliest_toi_narrow_phase over the candidates of the
+ * last rigc_detect_candidates / rigc_set_candidates call with
+ * compute_piecewise_linear_edge_edge_time_of_impact /
+ * compute_piecewise_linear_face_vertex_time_of_impact
+ * (src/ccd/piecewise_linear/time_of_impact.cpp:326-651), minimum separation
+ * dmin.  Each body's pose moves linearly over pieces of [0, 1] halved until
+ * the rigid trajectory's deviation from the straight line is below half the
+ * features' distance; a linear CCD (the inclusion-based method of
+ * Tight-Inclusion, with the deviation + dmin as minimum separation and a
+ * co-domain tolerance of 1e-6) finds each piece's first impact.  Every
+ * candidate searches t in [0, 1]; *toi_host = INFINITY when nothing
+ * collides; per_candidate (device, optional, num_ee + num_fv doubles, ee
+ * first).  RIGC_ERR_ITER_LIMIT when a linear CCD used its 10^6 boxes,
+ * RIGC_ERR_QUEUE_OVERFLOW when a piece or box could not be halved further
+ * (results kept: the earliest unexplored time, conservative). */
+int rigc_earliest_toi_piecewise_linear(rigc_ctx* ctx, const double* x0,
+                                       const double* x1, double dmin,
+                                       double* toi_host, double* per_candidate);
+
+/* DistanceBarrierConstraint::compute_earliest_toi
+ * (src/opt/distance_barrier_constraint.cpp:130-149) with trajectory
+ * PIECEWISE_LINEAR: continuous broad phase with inflation dmin / 2, then the
+ * piecewise-linear narrow phase. */
+int rigc_compute_earliest_toi_piecewise_linear(rigc_ctx* ctx, const double* x0,
+                                               const double* x1, double dmin,
+                                               double* toi_host);
+
 /* ---- constraint set: DistanceBarrierConstraint::construct_constraint_set
  * (src/opt/distance_barrier_constraint.cpp:267-306): discrete broad phase
  * with inflation (dhat + dmin) / 2, then ipc::construct_constraint_set. */

@@ -376,6 +376,55 @@ double orc_earliest_toi(
     return t;
 }
 
+// piecewise-linear CCD: one candidate (kind 0 EE (a, b) = edges, 1 FV
+// (a, b) = (face, vertex)), stats = { boxes, pieces, status }
+int orc_pl_toi(void* p, const double* x0, const double* x1, int kind, int a, int b, double bound,
+               double dmin, double* toi, long long* stats)
+{
+    PLStats st;
+    const Scene& s = static_cast<OwnedScene*>(p)->s;
+    const bool hit = kind == 0 ? pl_edge_edge_toi(s, x0, x1, a, b, bound, dmin, *toi, &st)
+                               : pl_face_vertex_toi(s, x0, x1, a, b, bound, dmin, *toi, &st);
+    if (stats) {
+        stats[0] = st.boxes;
+        stats[1] = st.pieces;
+        stats[2] = st.status;
+    }
+    return hit ? 1 : 0;
+}
+
+int orc_linear_ccd(int fv, const double* p0, const double* p1, double ms, double* toi,
+                   long long* stats)
+{
+    long long boxes = 0;
+    int status = 0;
+    const bool hit = linear_ccd(fv != 0, p0, p1, ms, *toi, boxes, status);
+    if (stats) {
+        stats[0] = boxes;
+        stats[1] = 0;
+        stats[2] = status;
+    }
+    return hit ? 1 : 0;
+}
+
+double orc_pl_earliest_toi(void* p, const double* x0, const double* x1, const int* ee, long long nee,
+                           const int* fv, long long nfv, double dmin, int nthreads, double* per,
+                           long long* stats)
+{
+    std::vector<double> tois;
+    PLStats st;
+    const double t = pl_earliest_toi(static_cast<OwnedScene*>(p)->s, x0, x1,
+                                     pack_candidates(ee, nee, fv, nfv), dmin, nthreads,
+                                     per ? &tois : nullptr, &st);
+    if (per) std::memcpy(per, tois.data(), tois.size() * sizeof(double));
+    if (stats) {
+        stats[0] = st.boxes;
+        stats[1] = st.pieces;
+        stats[2] = st.status;
+    }
+    return t;
+}
+
 // interval primitives: op 0 add, 1 sub, 2 mul, 3 div, 4 sqrt, 5 cos, 6 sin,
 // 7 sinc, 8 abs
 void orc_interval_op(int op, double al, double ah, double bl, double bh, double* out)

@@ -388,4 +388,22 @@ double earliest_toi(
     double toi_tol, int nthreads, std::vector<double>* per_candidate,
     CCDStats* st);
 
+// piecewise-linear trajectory CCD (pl_ccd.cpp)
+struct PLStats {
+    long long boxes = 0;   // boxes of the linear CCDs
+    long long pieces = 0;  // pieces (including halvings)
+    int status = 0;        // 5: a linear CCD ran out of boxes; 4: a piece
+                           // could not be halved further (conservative start)
+};
+// the linear CCD alone: points p0 -> p1 (4 x 3 each; EE a0 a1 b0 b1, FV v
+// f0 f1 f2) moving on straight lines over t in [0, 1], minimum separation ms
+bool linear_ccd(bool fv, const double* p0, const double* p1, double ms, double& toi,
+                long long& boxes, int& status);
+bool pl_edge_edge_toi(const Scene& s, const double* x0, const double* x1, int ea, int eb,
+                      double earliest_bound, double dmin, double& toi, PLStats* st);
+bool pl_face_vertex_toi(const Scene& s, const double* x0, const double* x1, int f, int v,
+                        double earliest_bound, double dmin, double& toi, PLStats* st);
+double pl_earliest_toi(const Scene& s, const double* x0, const double* x1, const Candidates& c,
+                       double dmin, int nthreads, std::vector<double>* per, PLStats* st);
+
 } // namespace orc

@@ -85,6 +85,12 @@ def lib():
         L.orc_earliest_toi.restype = C.c_double
         L.orc_earliest_toi.argtypes = [C.c_void_p, _d, _d, _i, C.c_longlong, _i, C.c_longlong,
                                        C.c_double, C.c_int, _d, _ll, C.c_longlong, _i]
+        L.orc_pl_toi.argtypes = [C.c_void_p, _d, _d, C.c_int, C.c_int, C.c_int, C.c_double,
+                                 C.c_double, _d, _ll]
+        L.orc_linear_ccd.argtypes = [C.c_int, _d, _d, C.c_double, _d, _ll]
+        L.orc_pl_earliest_toi.restype = C.c_double
+        L.orc_pl_earliest_toi.argtypes = [C.c_void_p, _d, _d, _i, C.c_longlong, _i, C.c_longlong,
+                                          C.c_double, C.c_int, _d, _ll]
         L.orc_interval_op.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, _d]
         L.orc_interval_rotation.argtypes = [_d, _d, _d, _d]
         L.orc_det_sin.restype = C.c_double
@@ -325,6 +331,27 @@ class OracleScene:
                                         C.byref(toi), C.byref(boxes))
         return bool(hit), toi.value, boxes.value
 
+    def pl_toi(self, x0, x1, kind, a, b, bound=1.0, dmin=0.0):
+        """Piecewise-linear time of impact of one candidate (kind 0: edges a,
+        b; kind 1: face a, vertex b): (hit, toi, {boxes, pieces, status})."""
+        x0, x1 = _dd(x0), _dd(x1)
+        toi = C.c_double()
+        st = np.zeros(3, np.int64)
+        hit = lib().orc_pl_toi(self.h, _p(x0, _d), _p(x1, _d), int(kind), int(a), int(b),
+                               float(bound), float(dmin), C.byref(toi), _p(st, _ll))
+        return bool(hit), toi.value, dict(boxes=int(st[0]), pieces=int(st[1]), status=int(st[2]))
+
+    def pl_earliest_toi(self, x0, x1, ee, fv, dmin=0.0, nthreads=1):
+        """Piecewise-linear earliest time of impact over the candidates:
+        (toi, per-candidate tois (ee first), {boxes, pieces, status})."""
+        x0, x1, ee, fv = _dd(x0), _dd(x1), _ii(ee), _ii(fv)
+        per = np.empty(len(ee) + len(fv))
+        st = np.zeros(3, np.int64)
+        t = lib().orc_pl_earliest_toi(self.h, _p(x0, _d), _p(x1, _d), _p(ee, _i), len(ee),
+                                      _p(fv, _i), len(fv), float(dmin), int(nthreads),
+                                      _p(per, _d), _p(st, _ll))
+        return t, per, dict(boxes=int(st[0]), pieces=int(st[1]), status=int(st[2]))
+
     def earliest_toi(self, x0, x1, ee, fv, tol=1e-4, nthreads=1, per_candidate=False,
                      max_boxes=0, with_status=False):
         """Earliest time of impact (per candidate too with per_candidate=True).
@@ -401,6 +428,18 @@ SIM_DEFAULTS = dict(dmin=0.0, mu=0.0, epsv=1e-3, max_newton_iterations=3000,
                     velocity_conv_tol=1e-2, velocity_conv_tol_abs=0,
                     line_search_lower_bound=1e-12, dhat_epsilon=1e-9,
                     min_barrier_stiffness_scale=1e11, newton_polish=0, ccd_rescale=1.0)
+
+
+def linear_ccd(p0, p1, ms=0.0, fv=False):
+    """The piecewise-linear CCD's linear CCD alone: the four points p0 -> p1
+    (EE a0 a1 b0 b1; FV v f0 f1 f2) on straight lines over t in [0, 1]:
+    (hit, toi, boxes, status)."""
+    p0, p1 = _dd(np.asarray(p0, np.float64).reshape(12)), _dd(np.asarray(p1, np.float64).reshape(12))
+    toi = C.c_double()
+    st = np.zeros(3, np.int64)
+    hit = lib().orc_linear_ccd(1 if fv else 0, _p(p0, _d), _p(p1, _d), float(ms), C.byref(toi),
+                               _p(st, _ll))
+    return bool(hit), toi.value, int(st[0]), int(st[2])
 
 
 class OracleSim:

@@ -35,6 +35,7 @@ UNITS = {
     "autotune.cu": ["--fmad=false"],
     "fp64_peak.cu": ["--fmad=false"],
     "intersect.cu": ["--fmad=false"],
+    "pl_ccd.cu": ["--fmad=false"],
 }
 
 

@@ -18,6 +18,7 @@ int scene_sums(Ctx& c, const double* val, const int* bodies, int64_t n, const in
                std::vector<double>& out);
 int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flags,
             double* toi_host, double* per);
+int run_pl_ccd(Ctx& c, const double* x0, const double* x1, double dmin, double* toi_host, double* per);
 int compute_world_vertices_rn(Ctx& c, const double* x, double* V, DevBuf& rotbuf);
 int sum_f64(const double* in, int64_t n, double* out_dev, DevBuf& tmp, cudaStream_t stream);
 int body_energy(Ctx& c, const rigc_body_state& s, const double* x, const double gravity[3],
@@ -441,6 +442,23 @@ int rigc_compute_earliest_toi(rigc_ctx* ctx, const double* x0, const double* x1,
     Ctx& c = *ctx_of(ctx);
     RIGC_TRY(detect_and_count(c, x0, x1, true, dmin / 2.0));
     return run_ccd(c, x0, x1, 1e-4, 0, toi_host, nullptr);
+}
+
+int rigc_earliest_toi_piecewise_linear(rigc_ctx* ctx, const double* x0, const double* x1,
+                                       double dmin, double* toi_host, double* per_candidate)
+{
+    if (!ctx || !x0 || !x1 || !toi_host || !(dmin >= 0)) return RIGC_ERR_ARG;
+    return run_pl_ccd(*ctx_of(ctx), x0, x1, dmin, toi_host, per_candidate);
+}
+
+int rigc_compute_earliest_toi_piecewise_linear(rigc_ctx* ctx, const double* x0, const double* x1,
+                                               double dmin, double* toi_host)
+{
+    if (!ctx || !x0 || !x1 || !toi_host || !(dmin >= 0)) return RIGC_ERR_ARG;
+    Ctx& c = *ctx_of(ctx);
+    RIGC_TRY(detect_and_count(c, x0, x1, true, dmin / 2.0));
+    c.bp_table.valid = false;
+    return run_pl_ccd(c, x0, x1, dmin, toi_host, nullptr);
 }
 
 int rigc_construct_constraint_set(rigc_ctx* ctx, const double* x, double dhat, double dmin,

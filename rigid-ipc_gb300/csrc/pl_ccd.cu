@@ -1,0 +1,467 @@
+// Piecewise-linear trajectory CCD over EE and FV candidates.
+//
+// Replaces compute_earliest_toi_narrow_phase
+// (src/opt/distance_barrier_constraint.cpp:151-265) with trajectory
+// PIECEWISE_LINEAR: compute_piecewise_linear_edge_edge_time_of_impact and
+// compute_piecewise_linear_face_vertex_time_of_impact
+// (src/ccd/piecewise_linear/time_of_impact.cpp:326-651).  The time interval
+// is cut into pieces over which each body's pose moves linearly
+// (Pose::interpolate), the vertices move on straight lines between their
+// positions at a piece's ends, and a linear CCD with a minimum separation
+// (the interval bound of the rigid trajectory's deviation from the straight
+// line, plus dmin) finds the first time the straight-line motions come that
+// close.  Piece rules: an impact at the start of a piece whose features came
+// below 0.2 of their initial distance (after t = 1e-6); a piece whose
+// deviation is >= 0.5 of the features' distance at its start is halved
+// (while fewer than 1000 halvings were made, or always at t = 0); an impact
+// of the linear CCD at the piece's start halves the piece.
+//
+// The reference's linear CCD is Tight-Inclusion's inclusion-based root
+// finder (Wang et al. 2021); the one here keeps its published method: the
+// distance function F(t, u, v) of the straight-line motions is multilinear,
+// so its range over a box is the hull of its values at the eight corners
+// (evaluated in interval arithmetic); a box whose range misses [-ms, ms]^3
+// holds no impact; one inside [-ms, ms]^3 or no wider than 1e-6 + ms in
+// every coordinate is a root; others are halved along the dimension with the
+// largest change of F between opposite corners, earlier half first; at most
+// 10^6 boxes per piece (then the smallest unexplored t.lo, a conservative
+// time).
+//
+// One candidate per warp.  The search state is the same in every lane; a
+// box's 8 corners x 3 coordinates are evaluated on 24 lanes (lane 8 j + k:
+// coordinate j at corner k), the hull and the changes by shuffles.  The
+// piece's straight-line end points come from 4 lanes per end (one vertex
+// each) and its deviation bound from 4 (one vertex each: its body's interval
+// pose and rotation over the piece).  Every candidate searches t in [0, 1],
+// the reference's first candidate's domain; the operations and their order
+// are the oracle's, so the per-candidate times of impact are the same bits.
+#include <algorithm>
+
+#include "common.cuh"
+#include "geometry_rn.cuh"
+#include "interval.cuh"
+#include "search_tree.cuh"
+
+namespace rigc {
+
+namespace {
+
+constexpr int kPLThreads = 128;
+constexpr double kLinearTol = 1e-6;
+constexpr long long kLinearMaxBoxes = 1000000;
+constexpr int kMaxSubdivisions = 1000;
+constexpr int kMaxPieceDepth = 60;
+constexpr double kTrajectoryFactor = 0.5;
+constexpr double kDecreasingFactor = 0.2;
+constexpr double kDecreasingMinTime = 1e-6;
+
+struct PLArgs {
+    const double* rest;
+    const int* edges;
+    const int* faces;
+    const int* vbody;
+    const int* ebody;
+    const int* fbody;
+    const double* x0;
+    const double* x1;
+    const int2* ee;
+    const int2* fv;
+    int64_t nee, nfv;
+    double dmin;
+    double* per;                 // per-candidate time of impact (INFINITY: none)
+    unsigned long long* gmin;    // earliest over all candidates (double bits)
+    unsigned long long* next;    // next candidate
+    unsigned long long* boxes;   // linear-CCD boxes over all candidates
+    unsigned long long* pieces;  // pieces over all candidates
+    int* status;                 // worst status
+};
+
+__device__ __forceinline__ double shfl(double v, int src)
+{
+    return __shfl_sync(0xffffffffu, v, src);
+}
+
+// (x1 - x0) t + x0, round to nearest
+__device__ __forceinline__ double lerp_rn(double a, double b, double t)
+{
+    return RADD(RMUL(RSUB(b, a), t), a);
+}
+
+__device__ __forceinline__ double pt_sqdist_rn(const double* p, const double* t0, const double* t1,
+                                               const double* t2)
+{
+    switch (pt_type_rn(p, t0, t1, t2)) {
+    case PT_P_T0: return pp_sqdist_rn(p, t0);
+    case PT_P_T1: return pp_sqdist_rn(p, t1);
+    case PT_P_T2: return pp_sqdist_rn(p, t2);
+    case PT_P_E0: return pl_sqdist_rn(p, t0, t1);
+    case PT_P_E1: return pl_sqdist_rn(p, t1, t2);
+    case PT_P_E2: return pl_sqdist_rn(p, t2, t0);
+    default: return ptplane_sqdist_rn(p, t0, t1, t2);
+    }
+}
+
+__device__ __forceinline__ double feature_distance(bool fv, const double P[4][3])
+{
+    return __dsqrt_rn(fv ? pt_sqdist_rn(P[0], P[1], P[2], P[3]) : ee_sqdist_rn(P[0], P[1], P[2], P[3]));
+}
+
+// Every lane gets the four points at the poses pa (body A) and pb (body B):
+// lane m < 4 computes point m, the others take it by shuffles.
+__device__ void gather_points(const PLArgs& a, const int vid[4], int na, const double* pa,
+                              const double* pb, int lane, double P[4][3])
+{
+    double w[3] = { 0, 0, 0 };
+    if (lane < 4) {
+        const double* x = lane < na ? pa : pb;
+        double R[9], v[3];
+        rot_rn(x + 3, R);
+#pragma unroll
+        for (int c = 0; c < 3; c++) v[c] = a.rest[3 * (size_t)vid[lane] + c];
+        world_vertex_rn(R, x, v, w);
+    }
+#pragma unroll
+    for (int m = 0; m < 4; m++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) P[m][c] = shfl(w[c], m);
+}
+
+// The largest deviation of each side's vertices from their straight lines
+// over the piece between the poses at its ends (pa0 -> pa1, pb0 -> pb1):
+// lane m < 4 bounds vertex m; returns the sum of the two sides' largest.
+__device__ double piece_deviation(const PLArgs& a, const int vid[4], int na, const double* pa0,
+                                  const double* pa1, const double* pb0, const double* pb1,
+                                  const double P0[4][3], const double P1[4][3], int lane)
+{
+    double dev = 0;
+    if (lane < 4) {
+        const double* xa = lane < na ? pa0 : pb0;
+        const double* xb = lane < na ? pa1 : pb1;
+        const Itv t { 0.0, 1.0 };
+        Itv p[3], r[3], R[9];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            p[k] = iadd(imul_nonneg(isub(pt(xb[k]), pt(xa[k])), t), pt(xa[k]));
+            r[k] = iadd(imul_nonneg(isub(pt(xb[3 + k]), pt(xa[3 + k])), t), pt(xa[3 + k]));
+        }
+        irotation(r, R);
+        double v[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) v[c] = a.rest[3 * (size_t)vid[lane] + c];
+        Itv w[3];
+        iworld_vertex(R, p, v, w);
+        Itv sq { 0.0, 0.0 };
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            const Itv line = iadd(imul_nonneg(isub(pt(P1[lane][j]), pt(P0[lane][j])), t), pt(P0[lane][j]));
+            const Itv e = isub(w[j], line);
+            sq = j == 0 ? imul(e, e) : iadd(sq, imul(e, e));
+        }
+        dev = isqrt(sq).hi;
+    }
+    // largest of each side (lanes 0 .. na-1: A; na .. 3: B), then their sum
+    double da = 0, db = 0;
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+        const double d = shfl(dev, m);
+        if (m < na) da = da < d ? d : da;
+        else db = db < d ? d : db;
+    }
+    return RADD(da, db);
+}
+
+// The linear CCD of one piece by the warp: the first t in [0, 1] at which
+// the straight-line motions P0 -> P1 come within ms (INFINITY: none).
+__device__ double linear_toi(bool fv, const double P0[4][3], const double P1[4][3], double ms,
+                             int lane, long long& boxes, int& status)
+{
+    const int j = lane >> 3, k = lane & 7;  // lane 8 j + k: coordinate j at corner k (lanes < 24)
+    const bool clane = lane < 24;
+    double p0[4] = { 0, 0, 0, 0 }, p1[4] = { 0, 0, 0, 0 };
+    if (clane) {
+#pragma unroll
+        for (int m = 0; m < 4; m++) {
+            p0[m] = P0[m][j];
+            p1[m] = P1[m][j];
+        }
+    }
+    Node cn { { 0, 0, 0 }, { 0ull, 0ull, 0ull }, 0 };
+    bool has_cn = true;
+    u128 pend = 0, mt = 0, ma = 0;
+    double earliest = INFINITY;
+    long long n = 0;
+    while (has_cn || pend != 0) {
+        if (has_cn) {
+            has_cn = false;
+        } else {
+            const int b = msb128(pend);
+            pend &= ~bit128(b);
+            cn = pending_node(cn, mt, ma, b);
+        }
+        const double t0 = dyadic(cn.ix[0], cn.lv[0]), t1 = dyadic(cn.ix[0] + 1, cn.lv[0]);
+        const double u0 = dyadic(cn.ix[1], cn.lv[1]), u1 = dyadic(cn.ix[1] + 1, cn.lv[1]);
+        const double v0 = dyadic(cn.ix[2], cn.lv[2]), v1 = dyadic(cn.ix[2] + 1, cn.lv[2]);
+        if (t0 >= earliest) continue;
+        if (fv && !(add_dn(u0, v0) <= 1.0)) continue;
+        if (n >= kLinearMaxBoxes) {
+            double m = t0;
+            for (u128 r = pend; r != 0; r &= r - 1) {
+                const Node g = pending_node(cn, mt, ma, lsb128(r));
+                const double g0 = dyadic(g.ix[0], g.lv[0]);
+                m = g0 < m ? g0 : m;
+            }
+            earliest = m < earliest ? m : earliest;
+            status = status > 5 ? status : 5;
+            break;
+        }
+        n++;
+        // F at this lane's corner
+        Itv y { 0.0, 0.0 };
+        if (clane) {
+            const Itv t = pt((k & 1) ? t1 : t0), u = pt((k & 2) ? u1 : u0), v = pt((k & 4) ? v1 : v0);
+            Itv q[4];
+#pragma unroll
+            for (int m = 0; m < 4; m++) q[m] = iadd(imul_nonneg(isub(pt(p1[m]), pt(p0[m])), t), pt(p0[m]));
+            if (fv) {
+                const Itv fp = iadd(iadd(imul_nonneg(isub(q[2], q[1]), u), imul_nonneg(isub(q[3], q[1]), v)), q[1]);
+                y = isub(q[0], fp);
+            } else {
+                const Itv ea = iadd(imul_nonneg(isub(q[1], q[0]), u), q[0]);
+                const Itv eb = iadd(imul_nonneg(isub(q[3], q[2]), v), q[2]);
+                y = isub(ea, eb);
+            }
+        }
+        // the changes of F along t, u, v: |mid(corner with the bit) -
+        // mid(corner without)|, largest over the lanes
+        const double mid = RMUL(0.5, RADD(y.lo, y.hi));
+        double ch[3];
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            const double other = __shfl_xor_sync(0xffffffffu, mid, 1 << d);
+            double c = (clane && !(k & (1 << d))) ? fabs(RSUB(other, mid)) : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const double w = __shfl_xor_sync(0xffffffffu, c, o);
+                c = c < w ? w : c;
+            }
+            ch[d] = c;
+        }
+        // hull over the corners of each coordinate (the 8 lanes of j)
+        double lo = y.lo, hi = y.hi;
+#pragma unroll
+        for (int o = 4; o > 0; o >>= 1) {
+            const double l = __shfl_xor_sync(0xffffffffu, lo, o);
+            const double h = __shfl_xor_sync(0xffffffffu, hi, o);
+            lo = l < lo ? l : lo;
+            hi = hi < h ? h : hi;
+        }
+        const bool meets_j = !clane || (lo <= ms && hi >= -ms);
+        const bool inside_j = !clane || (lo >= -ms && hi <= ms);
+        const bool small_j = !clane || sub_up(hi, lo) <= RADD(kLinearTol, ms);
+        if (!__all_sync(0xffffffffu, meets_j)) continue;
+        if (__all_sync(0xffffffffu, inside_j) || __all_sync(0xffffffffu, small_j)) {
+            earliest = t0;
+            continue;
+        }
+        int split = 0;
+        if (ch[1] > ch[split]) split = 1;
+        if (ch[2] > ch[split]) split = 2;
+        if (cn.depth >= kMaxDepth || cn.lv[split] >= kMaxLevel) {
+            earliest = t0;
+            status = status > 4 ? status : 4;
+            continue;
+        }
+        descend(cn, pend, mt, ma, split);
+        has_cn = true;
+    }
+    boxes += n;
+    return earliest;
+}
+
+// the piecewise-linear time of impact of one candidate (INFINITY: none)
+__device__ double pl_toi(const PLArgs& a, bool fv, const int vid[4], int A, int B, int lane,
+                         long long& boxes, long long& npieces, int& status)
+{
+    const int na = fv ? 1 : 2;
+    const double* xa0 = a.x0 + 6 * A;
+    const double* xa1 = a.x1 + 6 * A;
+    const double* xb0 = a.x0 + 6 * B;
+    const double* xb1 = a.x1 + 6 * B;
+    double P0[4][3], P1[4][3];
+    gather_points(a, vid, na, xa0, xb0, lane, P0);
+    const double distance_t0 = feature_distance(fv, P0);
+    if (distance_t0 <= a.dmin) return 0.0;
+    double ts[kMaxPieceDepth + 1];
+    int top = 0;
+    ts[0] = 1.0;
+    int subdivisions = 1;
+    double ti0 = 0;
+    double pa0[6], pb0[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        pa0[k] = xa0[k];
+        pb0[k] = xb0[k];
+    }
+    double result = INFINITY;
+    // the points and the distance at ti0 change only when a piece is passed
+    // (a halving keeps ti0): P0 holds them for the current ti0
+    double distance_ti0 = distance_t0;
+    while (top >= 0) {
+        const double ti1 = ts[top];
+        double pa1[6], pb1[6];
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            pa1[k] = lerp_rn(xa0[k], xa1[k], ti1);
+            pb1[k] = lerp_rn(xb0[k], xb1[k], ti1);
+        }
+        if (distance_ti0 < RMUL(kDecreasingFactor, distance_t0) && ti0 >= kDecreasingMinTime) {
+            result = ti0;
+            break;
+        }
+        gather_points(a, vid, na, pa1, pb1, lane, P1);
+        const double dev = piece_deviation(a, vid, na, pa0, pa1, pb0, pb1, P0, P1, lane);
+        const bool may_split = top < kMaxPieceDepth;
+        if (dev >= RMUL(kTrajectoryFactor, distance_ti0) && (subdivisions < kMaxSubdivisions || ti0 == 0)) {
+            if (!may_split) {
+                result = ti0;
+                status = status > 4 ? status : 4;
+                break;
+            }
+            ts[++top] = RMUL(0.5, RADD(ti1, ti0));
+            subdivisions++;
+            continue;
+        }
+        const double t = linear_toi(fv, P0, P1, RADD(dev, a.dmin), lane, boxes, status);
+        if (t < INFINITY) {
+            const double tt = RADD(RMUL(RSUB(ti1, ti0), t), ti0);
+            if (tt == 0) {
+                if (!may_split) {
+                    result = 0;
+                    status = status > 4 ? status : 4;
+                    break;
+                }
+                ts[++top] = RMUL(0.5, RADD(ti1, ti0));
+                subdivisions++;
+                continue;
+            }
+            result = tt;
+            break;
+        }
+        top--;
+        ti0 = ti1;
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            pa0[k] = pa1[k];
+            pb0[k] = pb1[k];
+        }
+#pragma unroll
+        for (int m = 0; m < 4; m++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) P0[m][c] = P1[m][c];
+        distance_ti0 = feature_distance(fv, P0);
+    }
+    npieces += subdivisions;
+    return result;
+}
+
+__global__ void __launch_bounds__(kPLThreads) k_pl_ccd(PLArgs a)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t n = a.nee + a.nfv;
+    long long boxes = 0, npieces = 0;
+    int status = RIGC_OK;
+    double local_min = INFINITY;
+    while (true) {
+        long long w = 0;
+        if (lane == 0) w = (long long)atomicAdd(a.next, 1ull);
+        w = __shfl_sync(0xffffffffu, w, 0);
+        if (w >= n) break;
+        bool fv;
+        int vid[4], A, B;
+        if (w < a.nee) {
+            fv = false;
+            const int ea = a.ee[w].x, eb = a.ee[w].y;
+            vid[0] = a.edges[2 * ea];
+            vid[1] = a.edges[2 * ea + 1];
+            vid[2] = a.edges[2 * eb];
+            vid[3] = a.edges[2 * eb + 1];
+            A = a.ebody[ea];
+            B = a.ebody[eb];
+        } else {
+            fv = true;
+            const int f = a.fv[w - a.nee].x, v = a.fv[w - a.nee].y;
+            vid[0] = v;
+            vid[1] = a.faces[3 * f];
+            vid[2] = a.faces[3 * f + 1];
+            vid[3] = a.faces[3 * f + 2];
+            A = a.vbody[v];
+            B = a.fbody[f];
+        }
+        const double toi = pl_toi(a, fv, vid, A, B, lane, boxes, npieces, status);
+        if (lane == 0 && a.per) a.per[w] = toi;
+        local_min = toi < local_min ? toi : local_min;
+    }
+    if (lane == 0) {
+        if (local_min < INFINITY) atomicMin(a.gmin, (unsigned long long)__double_as_longlong(local_min));
+        atomicAdd(a.boxes, (unsigned long long)boxes);
+        atomicAdd(a.pieces, (unsigned long long)npieces);
+        if (status != RIGC_OK) atomicMax(a.status, status);
+    }
+}
+
+} // namespace
+
+// counters in the context's device scalars (byte offset 512): [0] earliest
+// time of impact (bits), [1] boxes, [2] pieces, [3] status, [4] next
+int run_pl_ccd(Ctx& c, const double* x0, const double* x1, double dmin, double* toi_host, double* per)
+{
+    cudaStream_t st = c.stream;
+    const int64_t n = c.cand.num_ee + c.cand.num_fv;
+    unsigned long long* cnt = reinterpret_cast<unsigned long long*>(c.d_scalars.as<char>() + 512);
+    const unsigned long long init[5] = { 0x7ff0000000000000ull, 0, 0, 0, 0 };
+    RIGC_CUDA(cudaMemcpyAsync(cnt, init, sizeof(init), cudaMemcpyHostToDevice, st));
+    if (n > 0) {
+        PLArgs a;
+        a.rest = c.s.rest;
+        a.edges = c.s.edges;
+        a.faces = c.s.faces;
+        a.vbody = c.s.vbody;
+        a.ebody = c.s.ebody;
+        a.fbody = c.s.fbody;
+        a.x0 = x0;
+        a.x1 = x1;
+        a.ee = c.cand.ee.as<int2>();
+        a.fv = c.cand.fv.as<int2>();
+        a.nee = c.cand.num_ee;
+        a.nfv = c.cand.num_fv;
+        a.dmin = dmin;
+        a.per = per;
+        a.gmin = cnt;
+        a.boxes = cnt + 1;
+        a.pieces = cnt + 2;
+        a.status = reinterpret_cast<int*>(cnt + 3);
+        a.next = cnt + 4;
+        int blocks = 0;
+        RIGC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_pl_ccd, kPLThreads, 0));
+        int dev = 0, sms = kNumSMs;
+        RIGC_CUDA(cudaGetDevice(&dev));
+        RIGC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        const int64_t want = (n + kPLThreads / 32 - 1) / (kPLThreads / 32);  // a warp per candidate
+        const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)sms * std::max(1, blocks)));
+        RIGC_COUNT_LAUNCH();
+        k_pl_ccd<<<grid, kPLThreads, 0, st>>>(a);
+        RIGC_CUDA(cudaGetLastError());
+    }
+    unsigned long long out[4];
+    RIGC_CUDA(cudaMemcpyAsync(out, cnt, sizeof(out), cudaMemcpyDeviceToHost, st));
+    RIGC_CUDA(cudaStreamSynchronize(st));
+    double g;
+    std::memcpy(&g, &out[0], sizeof(g));
+    *toi_host = g;
+    c.stats.ccd_boxes = (int64_t)out[1];
+    c.stats.ccd_candidates = n;
+    c.stats.last_status = (int)(out[3] & 0xffffffffu);
+    return c.stats.last_status;
+}
+
+} // namespace rigc

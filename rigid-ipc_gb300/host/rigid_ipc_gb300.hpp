@@ -158,6 +158,10 @@ struct Candidates {
 
 enum class DetectionMethod { HASH_GRID };
 
+// TrajectoryType (src/ccd/ccd.hpp:31-47) of the narrow phase: the rigid
+// interval trajectory or the piecewise-linear one (the JSON default)
+enum class TrajectoryType { RIGID, PIECEWISE_LINEAR };
+
 // detect_collision_candidates_rigid (continuous when poses differ)
 inline void detect_collision_candidates_rigid(
     const RigidBodyAssembler& bodies, const std::vector<double>& poses_t0,
@@ -193,6 +197,8 @@ class DistanceBarrierConstraint {
 public:
     double initial_barrier_activation_distance = 1e-3;
     double minimum_separation_distance = 0.0;
+    // CollisionConstraint's default (src/opt/collision_constraint.cpp:7)
+    TrajectoryType trajectory_type = TrajectoryType::RIGID;
     double barrier_activation_distance() const { return initial_barrier_activation_distance; }
 
     void construct_constraint_set(
@@ -224,19 +230,33 @@ public:
         const RigidBodyAssembler& bodies, const std::vector<double>& poses_t0,
         const std::vector<double>& poses_t1) const
     {
-        double* x0 = bodies.x0_.upload(bodies.ctx(), poses_t0);
-        double* x1 = bodies.x1_.upload(bodies.ctx(), poses_t1);
-        double toi = INFINITY;
-        check(rigc_compute_earliest_toi(bodies.ctx(), x0, x1, minimum_separation_distance, &toi),
-              "rigc_compute_earliest_toi", true);
-        return toi;
+        return earliest_toi(bodies, poses_t0, poses_t1, trajectory_type);
     }
 
+    // has_active_collisions_narrow_phase runs the rigid CCD for the
+    // piecewise-linear trajectory too (src/opt/distance_barrier_constraint.cpp:91-95)
     bool has_active_collisions(
         const RigidBodyAssembler& bodies, const std::vector<double>& poses_t0,
         const std::vector<double>& poses_t1) const
     {
-        return std::isfinite(compute_earliest_toi(bodies, poses_t0, poses_t1));
+        return std::isfinite(earliest_toi(bodies, poses_t0, poses_t1, TrajectoryType::RIGID));
+    }
+
+private:
+    double earliest_toi(const RigidBodyAssembler& bodies, const std::vector<double>& poses_t0,
+                        const std::vector<double>& poses_t1, TrajectoryType trajectory) const
+    {
+        double* x0 = bodies.x0_.upload(bodies.ctx(), poses_t0);
+        double* x1 = bodies.x1_.upload(bodies.ctx(), poses_t1);
+        double toi = INFINITY;
+        if (trajectory == TrajectoryType::PIECEWISE_LINEAR)
+            check(rigc_compute_earliest_toi_piecewise_linear(bodies.ctx(), x0, x1,
+                                                             minimum_separation_distance, &toi),
+                  "rigc_compute_earliest_toi_piecewise_linear", true);
+        else
+            check(rigc_compute_earliest_toi(bodies.ctx(), x0, x1, minimum_separation_distance, &toi),
+                  "rigc_compute_earliest_toi", true);
+        return toi;
     }
 };
 

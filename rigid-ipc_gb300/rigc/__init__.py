@@ -208,6 +208,35 @@ class Context:
                 allow=(L.RIGC_ERR_QUEUE_OVERFLOW, L.RIGC_ERR_ITER_LIMIT))
         return toi.value
 
+    def earliest_toi_piecewise_linear(self, x0, x1, dmin=0.0, per_candidate=False):
+        """compute_earliest_toi_narrow_phase with trajectory PIECEWISE_LINEAR over
+        the last continuous candidates (minimum separation dmin)."""
+        x0d, x1d = self.device(x0), self.device(x1)
+        toi = C.c_double()
+        s = self.stats()
+        n = s["cand_ee"] + s["cand_fv"]
+        per = self.torch.empty(max(n, 1), dtype=self.torch.float64, device="cuda") if per_candidate else None
+        st = self.lib.rigc_earliest_toi_piecewise_linear(
+            self.h, C.c_void_p(x0d.data_ptr()), C.c_void_p(x1d.data_ptr()), float(dmin), C.byref(toi),
+            C.c_void_p(per.data_ptr()) if per is not None else None)
+        L.check(st, "rigc_earliest_toi_piecewise_linear",
+                allow=(L.RIGC_ERR_QUEUE_OVERFLOW, L.RIGC_ERR_ITER_LIMIT))
+        if per_candidate:
+            return toi.value, per[:n].cpu().numpy(), st
+        return toi.value
+
+    def compute_earliest_toi_piecewise_linear(self, x0, x1, dmin=0.0):
+        """DistanceBarrierConstraint::compute_earliest_toi with trajectory
+        PIECEWISE_LINEAR (broad phase with inflation dmin / 2, then the narrow
+        phase)."""
+        x0d, x1d = self.device(x0), self.device(x1)
+        toi = C.c_double()
+        st = self.lib.rigc_compute_earliest_toi_piecewise_linear(
+            self.h, C.c_void_p(x0d.data_ptr()), C.c_void_p(x1d.data_ptr()), float(dmin), C.byref(toi))
+        L.check(st, "rigc_compute_earliest_toi_piecewise_linear",
+                allow=(L.RIGC_ERR_QUEUE_OVERFLOW, L.RIGC_ERR_ITER_LIMIT))
+        return toi.value
+
     def construct_constraint_set(self, x, dhat, dmin=0.0):
         """Returns the constraint arrays (numpy): type, verts, prims, bodies, weight, eps."""
         xd = self.device(x)

@@ -53,6 +53,10 @@ int main(int argc, char** argv)
         DistanceBarrierRBProblem p(s);
         p.constraint().initial_barrier_activation_distance = dhat;
         const double toi = p.compute_earliest_toi(x0, x1);
+        p.constraint().trajectory_type = TrajectoryType::PIECEWISE_LINEAR;
+        const double toi_pl = p.compute_earliest_toi(x0, x1);
+        const bool active = p.has_collisions(x0, x1);  // rigid CCD for either trajectory
+        p.constraint().trajectory_type = TrajectoryType::RIGID;
         std::vector<double> g;
         BlockSparse H;
         const double e = p.compute_barrier_term(x0, g, H, true, true);
@@ -62,7 +66,7 @@ int main(int argc, char** argv)
         const bool isect = p.detect_intersections(x0);
         FILE* out = std::fopen(argv[2], "wb");
         if (!out) return 2;
-        write_vec(out, std::vector<double> { toi, e, md, isect ? 1.0 : 0.0 });
+        write_vec(out, std::vector<double> { toi, e, md, isect ? 1.0 : 0.0, toi_pl, active ? 1.0 : 0.0 });
         write_vec(out, g);
         write_vec(out, H.row_ptr);
         write_vec(out, H.col);

@@ -65,8 +65,9 @@ def test_host_layer_runs_and_matches_binding(tmp_path):
     """Build the C++ caller against librigc.so, run one narrow-phase pass
     of the stacked 27-cube contact through the reference-named classes, and
     compare every output with the Python binding's on the same inputs: time
-    of impact, barrier energy, gradient, block-sparse Hessian, candidates,
-    minimum distance and the intersection check, bit for bit."""
+    of impact (rigid and piecewise-linear trajectories), barrier energy,
+    gradient, block-sparse Hessian, candidates, minimum distance and the
+    intersection check, bit for bit."""
     import numpy as np
 
     import rigc
@@ -107,12 +108,14 @@ def test_host_layer_runs_and_matches_binding(tmp_path):
     r = subprocess.run([str(exe), str(inp), str(outp)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     with open(outp, "rb") as f:
-        toi, e, md, isect = _read_vec(f, np.float64)
+        toi, e, md, isect, toi_pl, active = _read_vec(f, np.float64)
         g = _read_vec(f, np.float64)
         rp, col, val = _read_vec(f, np.int32), _read_vec(f, np.int32), _read_vec(f, np.float64)
         ee, fv = _read_vec(f, np.int32), _read_vec(f, np.int32)
     ctx = rigc.Context(sc)
     assert toi == ctx.compute_earliest_toi(x0, x1)
+    assert toi_pl == ctx.compute_earliest_toi_piecewise_linear(x0, x1)
+    assert active == (1.0 if np.isfinite(toi) else 0.0)
     ctx.construct_constraint_set(x0, dhat)
     e2, g2, (rp2, col2, val2) = ctx.compute_barrier_term(x0, dhat)
     assert e == e2 and np.array_equal(g, g2)
