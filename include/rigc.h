@@ -220,6 +220,12 @@ int rigc_earliest_toi_piecewise_linear(rigc_ctx* ctx, const double* x0,
                                        const double* x1, double dmin,
                                        double* toi_host, double* per_candidate);
 
+/* How the piecewise-linear CCD spreads its searches: 1 one candidate per
+ * lane (many candidates: each lane's FP64 work is its own), 0 one per warp
+ * (few candidates: the warp evaluates each box's corners together), -1 by
+ * the candidate count (the default).  The results are the same bits. */
+int rigc_set_pl_search(rigc_ctx* ctx, int32_t per_lane);
+
 /* DistanceBarrierConstraint::compute_earliest_toi
  * (src/opt/distance_barrier_constraint.cpp:130-149) with trajectory
  * PIECEWISE_LINEAR: continuous broad phase with inflation dmin / 2, then the

@@ -451,6 +451,13 @@ int rigc_earliest_toi_piecewise_linear(rigc_ctx* ctx, const double* x0, const do
     return run_pl_ccd(*ctx_of(ctx), x0, x1, dmin, toi_host, per_candidate);
 }
 
+int rigc_set_pl_search(rigc_ctx* ctx, int32_t per_lane)
+{
+    if (!ctx || per_lane < -1 || per_lane > 1) return RIGC_ERR_ARG;
+    ctx_of(ctx)->tune.pl_per_lane = per_lane;
+    return RIGC_OK;
+}
+
 int rigc_compute_earliest_toi_piecewise_linear(rigc_ctx* ctx, const double* x0, const double* x1,
                                                double dmin, double* toi_host)
 {

@@ -364,6 +364,294 @@ __device__ double pl_toi(const PLArgs& a, bool fv, const int vid[4], int A, int 
     return result;
 }
 
+// ---------------------------------------------------------------------------
+// One candidate per lane: the same operations in the same order, each lane
+// on its own candidate (its corners, points and deviations one after the
+// other).  An FP64 warp instruction costs the same 64 cycles with one lane
+// active as with 32, so with thousands of candidates the lanes' own searches
+// use the FP64 unit ~10x better than the warp's shared one (whose piece
+// phase runs on 4 lanes); with few candidates the warp's is faster.
+
+__device__ __forceinline__ void lane_points(const PLArgs& a, const int vid[4], int na,
+                                            const double* pa, const double* pb, double P[4][3])
+{
+    double RA[9], RB[9];
+    rot_rn(pa + 3, RA);
+    rot_rn(pb + 3, RB);
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+        double v[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) v[c] = a.rest[3 * (size_t)vid[m] + c];
+        world_vertex_rn(m < na ? RA : RB, m < na ? pa : pb, v, P[m]);
+    }
+}
+
+// the largest deviation of one side's vertices m0 .. m1-1 over the piece
+__device__ double lane_side_deviation(const PLArgs& a, const int vid[4], int m0, int m1,
+                                      const double* xa, const double* xb, const double P0[4][3],
+                                      const double P1[4][3])
+{
+    const Itv t { 0.0, 1.0 };
+    Itv p[3], r[3], R[9];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        p[k] = iadd(imul_nonneg(isub(pt(xb[k]), pt(xa[k])), t), pt(xa[k]));
+        r[k] = iadd(imul_nonneg(isub(pt(xb[3 + k]), pt(xa[3 + k])), t), pt(xa[3 + k]));
+    }
+    irotation(r, R);
+    double dev = 0;
+    for (int m = m0; m < m1; m++) {
+        double v[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) v[c] = a.rest[3 * (size_t)vid[m] + c];
+        Itv w[3];
+        iworld_vertex(R, p, v, w);
+        Itv sq { 0.0, 0.0 };
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            const Itv line = iadd(imul_nonneg(isub(pt(P1[m][j]), pt(P0[m][j])), t), pt(P0[m][j]));
+            const Itv e = isub(w[j], line);
+            sq = j == 0 ? imul(e, e) : iadd(sq, imul(e, e));
+        }
+        const double d = isqrt(sq).hi;
+        dev = dev < d ? d : dev;
+    }
+    return dev;
+}
+
+__device__ double lane_linear_toi(bool fv, const double P0[4][3], const double P1[4][3], double ms,
+                                  long long& boxes, int& status)
+{
+    Node cn { { 0, 0, 0 }, { 0ull, 0ull, 0ull }, 0 };
+    bool has_cn = true;
+    u128 pend = 0, mt = 0, ma = 0;
+    double earliest = INFINITY;
+    long long n = 0;
+    while (has_cn || pend != 0) {
+        if (has_cn) {
+            has_cn = false;
+        } else {
+            const int b = msb128(pend);
+            pend &= ~bit128(b);
+            cn = pending_node(cn, mt, ma, b);
+        }
+        const double t0 = dyadic(cn.ix[0], cn.lv[0]), t1 = dyadic(cn.ix[0] + 1, cn.lv[0]);
+        const double u0 = dyadic(cn.ix[1], cn.lv[1]), u1 = dyadic(cn.ix[1] + 1, cn.lv[1]);
+        const double v0 = dyadic(cn.ix[2], cn.lv[2]), v1 = dyadic(cn.ix[2] + 1, cn.lv[2]);
+        if (t0 >= earliest) continue;
+        if (fv && !(add_dn(u0, v0) <= 1.0)) continue;
+        if (n >= kLinearMaxBoxes) {
+            double m = t0;
+            for (u128 r = pend; r != 0; r &= r - 1) {
+                const Node g = pending_node(cn, mt, ma, lsb128(r));
+                const double g0 = dyadic(g.ix[0], g.lv[0]);
+                m = g0 < m ? g0 : m;
+            }
+            earliest = m < earliest ? m : earliest;
+            status = status > 5 ? status : 5;
+            break;
+        }
+        n++;
+        // F at the 8 corners: the hull per coordinate and the corner midpoints
+        double mid[8][3], lo[3], hi[3];
+        for (int k = 0; k < 8; k++) {
+            const Itv t = pt((k & 1) ? t1 : t0), u = pt((k & 2) ? u1 : u0), v = pt((k & 4) ? v1 : v0);
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                Itv q[4];
+#pragma unroll
+                for (int m = 0; m < 4; m++)
+                    q[m] = iadd(imul_nonneg(isub(pt(P1[m][j]), pt(P0[m][j])), t), pt(P0[m][j]));
+                Itv y;
+                if (fv) {
+                    const Itv fp = iadd(iadd(imul_nonneg(isub(q[2], q[1]), u), imul_nonneg(isub(q[3], q[1]), v)), q[1]);
+                    y = isub(q[0], fp);
+                } else {
+                    const Itv ea = iadd(imul_nonneg(isub(q[1], q[0]), u), q[0]);
+                    const Itv eb = iadd(imul_nonneg(isub(q[3], q[2]), v), q[2]);
+                    y = isub(ea, eb);
+                }
+                mid[k][j] = RMUL(0.5, RADD(y.lo, y.hi));
+                if (k == 0) {
+                    lo[j] = y.lo;
+                    hi[j] = y.hi;
+                } else {
+                    lo[j] = y.lo < lo[j] ? y.lo : lo[j];
+                    hi[j] = hi[j] < y.hi ? y.hi : hi[j];
+                }
+            }
+        }
+        double ch[3];
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            double c = 0;
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                if (k & (1 << d)) continue;
+#pragma unroll
+                for (int j = 0; j < 3; j++) {
+                    const double x = fabs(RSUB(mid[k | (1 << d)][j], mid[k][j]));
+                    c = c < x ? x : c;
+                }
+            }
+            ch[d] = c;
+        }
+        bool meets = true, inside = true, small = true;
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            meets = meets && lo[j] <= ms && hi[j] >= -ms;
+            inside = inside && lo[j] >= -ms && hi[j] <= ms;
+            small = small && sub_up(hi[j], lo[j]) <= RADD(kLinearTol, ms);
+        }
+        if (!meets) continue;
+        if (inside || small) {
+            earliest = t0;
+            continue;
+        }
+        int split = 0;
+        if (ch[1] > ch[split]) split = 1;
+        if (ch[2] > ch[split]) split = 2;
+        if (cn.depth >= kMaxDepth || cn.lv[split] >= kMaxLevel) {
+            earliest = t0;
+            status = status > 4 ? status : 4;
+            continue;
+        }
+        descend(cn, pend, mt, ma, split);
+        has_cn = true;
+    }
+    boxes += n;
+    return earliest;
+}
+
+__device__ double lane_pl_toi(const PLArgs& a, bool fv, const int vid[4], int A, int B,
+                              long long& boxes, long long& npieces, int& status)
+{
+    const int na = fv ? 1 : 2;
+    const double* xa0 = a.x0 + 6 * A;
+    const double* xa1 = a.x1 + 6 * A;
+    const double* xb0 = a.x0 + 6 * B;
+    const double* xb1 = a.x1 + 6 * B;
+    double P0[4][3], P1[4][3];
+    lane_points(a, vid, na, xa0, xb0, P0);
+    const double distance_t0 = feature_distance(fv, P0);
+    if (distance_t0 <= a.dmin) return 0.0;
+    double ts[kMaxPieceDepth + 1];
+    int top = 0;
+    ts[0] = 1.0;
+    int subdivisions = 1;
+    double ti0 = 0;
+    double pa0[6], pb0[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        pa0[k] = xa0[k];
+        pb0[k] = xb0[k];
+    }
+    double result = INFINITY;
+    double distance_ti0 = distance_t0;
+    while (top >= 0) {
+        const double ti1 = ts[top];
+        double pa1[6], pb1[6];
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            pa1[k] = lerp_rn(xa0[k], xa1[k], ti1);
+            pb1[k] = lerp_rn(xb0[k], xb1[k], ti1);
+        }
+        if (distance_ti0 < RMUL(kDecreasingFactor, distance_t0) && ti0 >= kDecreasingMinTime) {
+            result = ti0;
+            break;
+        }
+        lane_points(a, vid, na, pa1, pb1, P1);
+        const double dev = RADD(lane_side_deviation(a, vid, 0, na, pa0, pa1, P0, P1),
+                                lane_side_deviation(a, vid, na, 4, pb0, pb1, P0, P1));
+        const bool may_split = top < kMaxPieceDepth;
+        if (dev >= RMUL(kTrajectoryFactor, distance_ti0) && (subdivisions < kMaxSubdivisions || ti0 == 0)) {
+            if (!may_split) {
+                result = ti0;
+                status = status > 4 ? status : 4;
+                break;
+            }
+            ts[++top] = RMUL(0.5, RADD(ti1, ti0));
+            subdivisions++;
+            continue;
+        }
+        const double t = lane_linear_toi(fv, P0, P1, RADD(dev, a.dmin), boxes, status);
+        if (t < INFINITY) {
+            const double tt = RADD(RMUL(RSUB(ti1, ti0), t), ti0);
+            if (tt == 0) {
+                if (!may_split) {
+                    result = 0;
+                    status = status > 4 ? status : 4;
+                    break;
+                }
+                ts[++top] = RMUL(0.5, RADD(ti1, ti0));
+                subdivisions++;
+                continue;
+            }
+            result = tt;
+            break;
+        }
+        top--;
+        ti0 = ti1;
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            pa0[k] = pa1[k];
+            pb0[k] = pb1[k];
+        }
+#pragma unroll
+        for (int m = 0; m < 4; m++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) P0[m][c] = P1[m][c];
+        distance_ti0 = feature_distance(fv, P0);
+    }
+    npieces += subdivisions;
+    return result;
+}
+
+// the candidate's vertices (EE: a0 a1 b0 b1; FV: v f0 f1 f2) and bodies
+__device__ __forceinline__ bool pl_candidate(const PLArgs& a, int64_t w, int vid[4], int& A, int& B)
+{
+    if (w < a.nee) {
+        const int ea = a.ee[w].x, eb = a.ee[w].y;
+        vid[0] = a.edges[2 * ea];
+        vid[1] = a.edges[2 * ea + 1];
+        vid[2] = a.edges[2 * eb];
+        vid[3] = a.edges[2 * eb + 1];
+        A = a.ebody[ea];
+        B = a.ebody[eb];
+        return false;
+    }
+    const int f = a.fv[w - a.nee].x, v = a.fv[w - a.nee].y;
+    vid[0] = v;
+    vid[1] = a.faces[3 * f];
+    vid[2] = a.faces[3 * f + 1];
+    vid[3] = a.faces[3 * f + 2];
+    A = a.vbody[v];
+    B = a.fbody[f];
+    return true;
+}
+
+__global__ void __launch_bounds__(kPLThreads) k_pl_ccd_lane(PLArgs a)
+{
+    const int64_t n = a.nee + a.nfv;
+    long long boxes = 0, npieces = 0;
+    int status = RIGC_OK;
+    double local_min = INFINITY;
+    while (true) {
+        const long long w = (long long)atomicAdd(a.next, 1ull);
+        if (w >= n) break;
+        int vid[4], A, B;
+        const bool fv = pl_candidate(a, w, vid, A, B);
+        const double toi = lane_pl_toi(a, fv, vid, A, B, boxes, npieces, status);
+        if (a.per) a.per[w] = toi;
+        local_min = toi < local_min ? toi : local_min;
+    }
+    if (local_min < INFINITY) atomicMin(a.gmin, (unsigned long long)__double_as_longlong(local_min));
+    atomicAdd(a.boxes, (unsigned long long)boxes);
+    atomicAdd(a.pieces, (unsigned long long)npieces);
+    if (status != RIGC_OK) atomicMax(a.status, status);
+}
+
 __global__ void __launch_bounds__(kPLThreads) k_pl_ccd(PLArgs a)
 {
     const int lane = threadIdx.x & 31;
@@ -376,27 +664,8 @@ __global__ void __launch_bounds__(kPLThreads) k_pl_ccd(PLArgs a)
         if (lane == 0) w = (long long)atomicAdd(a.next, 1ull);
         w = __shfl_sync(0xffffffffu, w, 0);
         if (w >= n) break;
-        bool fv;
         int vid[4], A, B;
-        if (w < a.nee) {
-            fv = false;
-            const int ea = a.ee[w].x, eb = a.ee[w].y;
-            vid[0] = a.edges[2 * ea];
-            vid[1] = a.edges[2 * ea + 1];
-            vid[2] = a.edges[2 * eb];
-            vid[3] = a.edges[2 * eb + 1];
-            A = a.ebody[ea];
-            B = a.ebody[eb];
-        } else {
-            fv = true;
-            const int f = a.fv[w - a.nee].x, v = a.fv[w - a.nee].y;
-            vid[0] = v;
-            vid[1] = a.faces[3 * f];
-            vid[2] = a.faces[3 * f + 1];
-            vid[3] = a.faces[3 * f + 2];
-            A = a.vbody[v];
-            B = a.fbody[f];
-        }
+        const bool fv = pl_candidate(a, w, vid, A, B);
         const double toi = pl_toi(a, fv, vid, A, B, lane, boxes, npieces, status);
         if (lane == 0 && a.per) a.per[w] = toi;
         local_min = toi < local_min ? toi : local_min;
@@ -441,15 +710,24 @@ int run_pl_ccd(Ctx& c, const double* x0, const double* x1, double dmin, double* 
         a.pieces = cnt + 2;
         a.status = reinterpret_cast<int*>(cnt + 3);
         a.next = cnt + 4;
-        int blocks = 0;
-        RIGC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_pl_ccd, kPLThreads, 0));
         int dev = 0, sms = kNumSMs;
         RIGC_CUDA(cudaGetDevice(&dev));
         RIGC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        const int64_t want = (n + kPLThreads / 32 - 1) / (kPLThreads / 32);  // a warp per candidate
+        // one candidate per lane once there are enough candidates to fill the
+        // GPU's lanes a few times over, else one per warp (or as tuned)
+        const bool per_lane = c.tune.pl_per_lane >= 0 ? c.tune.pl_per_lane != 0
+                                                      : n >= (int64_t)sms * 4 * kPLThreads;
+        int blocks = 0;
+        if (per_lane)
+            RIGC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_pl_ccd_lane, kPLThreads, 0));
+        else
+            RIGC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_pl_ccd, kPLThreads, 0));
+        const int per_block = per_lane ? kPLThreads : kPLThreads / 32;
+        const int64_t want = (n + per_block - 1) / per_block;
         const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)sms * std::max(1, blocks)));
         RIGC_COUNT_LAUNCH();
-        k_pl_ccd<<<grid, kPLThreads, 0, st>>>(a);
+        if (per_lane) k_pl_ccd_lane<<<grid, kPLThreads, 0, st>>>(a);
+        else k_pl_ccd<<<grid, kPLThreads, 0, st>>>(a);
         RIGC_CUDA(cudaGetLastError());
     }
     unsigned long long out[4];

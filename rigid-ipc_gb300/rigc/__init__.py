@@ -225,6 +225,11 @@ class Context:
             return toi.value, per[:n].cpu().numpy(), st
         return toi.value
 
+    def set_pl_search(self, per_lane=-1):
+        """Piecewise-linear CCD: a candidate per lane (1), per warp (0), or by
+        the candidate count (-1)."""
+        L.check(self.lib.rigc_set_pl_search(self.h, int(per_lane)), "rigc_set_pl_search")
+
     def compute_earliest_toi_piecewise_linear(self, x0, x1, dmin=0.0):
         """DistanceBarrierConstraint::compute_earliest_toi with trajectory
         PIECEWISE_LINEAR (broad phase with inflation dmin / 2, then the narrow

@@ -38,7 +38,7 @@ EXPORTS = [
     "rigc_scene_barrier_energies", "rigc_sim_rollout", "rigc_sim_backward",
     "rigc_sim_scene_params", "rigc_autotune", "rigc_set_tune", "rigc_fp64_throughput",
     "rigc_min_distance", "rigc_detect_intersections", "rigc_earliest_toi_piecewise_linear",
-    "rigc_compute_earliest_toi_piecewise_linear",
+    "rigc_compute_earliest_toi_piecewise_linear", "rigc_set_pl_search",
 ]
 RIGC_ERR_TOO_LARGE = 7
 RIGC_ERR_SOLVE = 8
@@ -150,6 +150,7 @@ def load():
     L.rigc_compute_earliest_toi.argtypes = [_vp, _vp, _vp, C.c_double, _d]
     L.rigc_earliest_toi_piecewise_linear.argtypes = [_vp, _vp, _vp, C.c_double, _d, _vp]
     L.rigc_compute_earliest_toi_piecewise_linear.argtypes = [_vp, _vp, _vp, C.c_double, _d]
+    L.rigc_set_pl_search.argtypes = [_vp, C.c_int32]
     L.rigc_construct_constraint_set.argtypes = [_vp, _vp, C.c_double, C.c_double,
                                                 C.POINTER(ConstraintsView)]
     L.rigc_set_constraints.argtypes = [_vp, C.c_int64, _vp, _vp, _vp, _vp, _vp, _vp]

@@ -12,8 +12,10 @@ from test_reference_fixtures import queries, scene_fixture
 pytestmark = pytest.mark.gpu
 
 
-def test_pl_reference_queries_gpu():
-    """All 403 queries in one context, candidates given explicitly."""
+@pytest.mark.parametrize("per_lane", [0, 1])
+def test_pl_reference_queries_gpu(per_lane):
+    """All 403 queries in one context, candidates given explicitly, one
+    candidate per warp and per lane."""
     import make_reference_fixtures as M
     import oracle as O
     import rigc
@@ -45,6 +47,7 @@ def test_pl_reference_queries_gpu():
         x0 += [P[0, 0], P[1, 0]]
         x1 += [P[0, 1], P[1, 1]]
     ctx = rigc.Context(S.Scene(bodies=bodies))
+    ctx.set_pl_search(per_lane)
     ctx.set_candidates(ee, fv)
     toi, per, st = ctx.earliest_toi_piecewise_linear(np.concatenate(x0), np.concatenate(x1),
                                                      per_candidate=True)
@@ -54,8 +57,10 @@ def test_pl_reference_queries_gpu():
     assert np.isfinite(want).sum() > 100
 
 
-def test_pl_wrecking_ball_scene_gpu(oracle):
-    """The 66,536 continuous candidates of the 575-body wrecking-ball scene."""
+@pytest.mark.parametrize("per_lane", [0, 1])
+def test_pl_wrecking_ball_scene_gpu(oracle, per_lane):
+    """The 66,536 continuous candidates of the 575-body wrecking-ball scene,
+    one candidate per warp and per lane."""
     import make_reference_fixtures as M
     import rigc
 
@@ -64,6 +69,7 @@ def test_pl_wrecking_ball_scene_gpu(oracle):
     x0 = d["pose_t0"].reshape(-1)
     x1 = d["pose_t1"].reshape(-1)
     ctx = rigc.Context(sc)
+    ctx.set_pl_search(per_lane)
     ee, fv = ctx.detect_collision_candidates_rigid(x0, x1, True, 0.0)
     toi, per, st = ctx.earliest_toi_piecewise_linear(x0, x1, per_candidate=True)
     o = oracle.OracleScene(sc)
