@@ -220,10 +220,9 @@ int rigc_earliest_toi_piecewise_linear(rigc_ctx* ctx, const double* x0,
                                        const double* x1, double dmin,
                                        double* toi_host, double* per_candidate);
 
-/* How the piecewise-linear CCD spreads its searches: 1 one candidate per
- * lane (many candidates: each lane's FP64 work is its own), 0 one per warp
- * (few candidates: the warp evaluates each box's corners together), -1 by
- * the candidate count (the default).  The results are the same bits. */
+/* How the piecewise-linear CCD spreads its searches: 0 one candidate per
+ * warp (the warp evaluates each box's corners together; the default, also
+ * for -1), 1 one per lane.  The results are the same bits. */
 int rigc_set_pl_search(rigc_ctx* ctx, int32_t per_lane);
 
 /* DistanceBarrierConstraint::compute_earliest_toi

@@ -141,7 +141,7 @@ static void release_all(Ctx* c)
                        &c->d_scalars, &c->body_box, &c->body_in, &c->vbox, &c->ebox, &c->fbox,
                        &c->vin, &c->ein, &c->fin, &c->items_key, &c->items_val, &c->items_key2,
                        &c->items_val2, &c->seg, &c->pair_out, &c->pair_key, &c->large_list,
-                       &c->x0_dev, &c->x1_dev, &c->rot_table, &c->cand_tol, &c->frame_keys, &c->ccd_pieces[0], &c->ccd_pieces[1],
+                       &c->x0_dev, &c->x1_dev, &c->rot_table, &c->cand_tol, &c->frame_keys, &c->ccd_pieces[0], &c->ccd_pieces[1], &c->pl_table,
                        &c->frame_vals, &c->fric.type, &c->fric.verts, &c->fric.bodies,
                        &c->fric.coef, &c->fric.v0c, &c->fric.V0, &c->fric.c_energy,
                        &c->fric.c_grad, &c->fric.c_blocks, &c->fric.grad, &c->fric.row_ptr,

@@ -226,8 +226,8 @@ class Context:
         return toi.value
 
     def set_pl_search(self, per_lane=-1):
-        """Piecewise-linear CCD: a candidate per lane (1), per warp (0), or by
-        the candidate count (-1)."""
+        """Piecewise-linear CCD: a candidate per lane (1) or per warp (0, and
+        -1: the default)."""
         L.check(self.lib.rigc_set_pl_search(self.h, int(per_lane)), "rigc_set_pl_search")
 
     def compute_earliest_toi_piecewise_linear(self, x0, x1, dmin=0.0):
