@@ -1268,7 +1268,9 @@ k_ccd_group(CCDArgs a)
             const int side = vtx < na ? 0 : 1;
             const bool need = vlane && (fresh || !(side ? b_fixed : a_fixed));
             const Itv t { x.t0, x.t1 };
-            const unsigned long long node = time_node(x.t0, x.t1);
+            // the time interval's tree node straight from the box's node
+            // (time_node(x.t0, x.t1) gives the same: t0 = ix 2^-lv, t1 = (ix + 1) 2^-lv)
+            const unsigned long long node = cn.lv[0] < kNodeDepth ? (1ull << cn.lv[0]) + cn.ix[0] : 0ull;
             bool miss = false;
             if (need) {
                 Itv r[3], pc;
