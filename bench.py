@@ -42,19 +42,16 @@ CCD_BYTES_PER_PAIR = 304        # ids + 4 rest vertices + 4 poses + toi
 # launches), from ncu captures of the 200-icosphere pile (132,242
 # candidates): k_ccd 56.95 MB read + 311.51 MB written over two launches
 # (per-lane candidate state spilling from L1, the frame cache);
-# k_ccd_group<32, 1> (one search per warp) 20.95 MB + 15.81 MB over
-# three; k_ccd_group<32, 4> (fitted to 4 blocks per SM: 128 registers, one
-# interval bound per lane) 27.51 MB + 43.86 MB over three,
+# k_ccd_group<32, 4> (one search per warp fitted to 4 blocks per SM: 128
+# registers, one interval bound per lane) 27.94 MB + 45.73 MB over three,
 # most of the writes its spills.  The traffic of a full call is this times
 # its candidates.  FP64 figures of the same captures: pipe active (fraction
 # of peak) and lane-level GFLOP/s (dadd + dmul + 2 dfma over the launch).
 K_CCD_DRAM_BYTES_PER_CANDIDATE = {
     "k_ccd": (42209536 + 14743808 + 310226176 + 1279232) / 132242,
-    "k_ccd_group<32, 1>": (17837312 + 2597632 + 512000 + 15804928 + 1792) / 132242,
-    "k_ccd_group<32, 4>": (22857216 + 3941120 + 714752 + 43766272 + 90880 + 2304) / 132242}
+    "k_ccd_group<32, 4>": (23012864 + 3960320 + 968448 + 45619968 + 103680 + 5632) / 132242}
 K_CCD_FP64 = {"k_ccd": {"pipe_active": 0.233, "lane_gflops": 53.0},
-              "k_ccd_group<32, 1>": {"pipe_active": 0.496, "lane_gflops": 98.4},
-              "k_ccd_group<32, 4>": {"pipe_active": 0.381, "lane_gflops": 100.9}}
+              "k_ccd_group<32, 4>": {"pipe_active": 0.384, "lane_gflops": 99.5}}
 BARRIER_BYTES_PER_CONSTRAINT = 1456
 # the CCD kernel of each search mode (rigc_set_tune's ccd_warp)
 CCD_KERNELS = {0: "k_ccd", 1: "k_ccd_group<32, 1>", 2: "k_ccd_group<32, 4>",
@@ -191,6 +188,20 @@ def fp64_peak():
         r = rigc.fp64_throughput(op, lanes, 4096)
         out[f"{op}_{lanes}"] = {"gflops": r["gflops"], "warp_inst_per_s": r["warp_inst_per_s"],
                                 "ms": r["ms"]}
+    return out
+
+
+def fp64_roofline(captured, measured):
+    """The CCD kernel's FP64 side: its pipe-active fraction and lane-level
+    FP64 rate from the ncu capture, against the FP64 peak measured in this
+    run (all-lane DFMA chains)."""
+    if not captured:
+        return None
+    out = dict(captured, source="ncu capture of the 200-icosphere pile", nominal_gflops=1250.0)
+    if measured:
+        peak = measured["dfma_32"]["gflops"]
+        out["measured_peak_gflops"] = peak
+        out["frac_of_measured"] = captured["lane_gflops"] / peak
     return out
 
 
@@ -840,8 +851,7 @@ def main():
                      "note": "FP64-issue-bound (an FP64 warp instruction holds its SM "
                              "sub-partition's FP64 unit 64 cycles on GB300), not HBM: algorithmic "
                              "bytes are 304 B per candidate",
-                     "fp64": dict(K_CCD_FP64.get(ccd_kernel, {}), nominal_gflops=1250.0,
-                                  source="ncu capture of the 200-icosphere pile")},
+                     "fp64": fp64_roofline(K_CCD_FP64.get(ccd_kernel), fp64)},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "clocks": clk.summary(),
