@@ -47,6 +47,10 @@ extern "C" {
 #define RIGC_HESS 2
 #define RIGC_PROJECT_PSD 4 /* project each 12x12 pair Hessian to PSD       */
 
+/* rigc_sim_params.trajectory_type (TrajectoryType, src/ccd/ccd.hpp:31-47) */
+#define RIGC_TRAJECTORY_RIGID 0
+#define RIGC_TRAJECTORY_PIECEWISE_LINEAR 1
+
 /* rigc_earliest_toi flags */
 #define RIGC_TOI_NO_PRUNE 1 /* search every candidate in full (per-candidate
                                times of impact become exact, slower)         */
@@ -389,6 +393,10 @@ typedef struct rigc_sim_params {
      * rigid CCD's spatial resolution (1e-4 m), where the CCD's conservative
      * time of impact shrinks every following step. */
     double ccd_rescale;
+    /* The line search's CCD: RIGC_TRAJECTORY_RIGID (0, the interval rigid
+     * trajectory) or RIGC_TRAJECTORY_PIECEWISE_LINEAR (1, the reference's
+     * JSON default; minimum separation dmin).  Plain contexts only. */
+    int32_t trajectory_type;
 } rigc_sim_params;
 
 /* Bodies' state (host pointers, copied by rigc_sim_init). */

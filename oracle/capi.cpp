@@ -545,7 +545,7 @@ int orc_friction_term(
 // h, gravity (3), dhat, dmin, mu, epsv, max_newton_iterations,
 // velocity_conv_tol, velocity_conv_tol_abs, line_search_lower_bound,
 // dhat_epsilon, min_barrier_stiffness_scale, bbox_diagonal, average_mass,
-// newton_polish, ccd_rescale (18 doubles).  stats: newton iterations, newton steps, objective
+// newton_polish, ccd_rescale, trajectory (19 doubles).  stats: newton iterations, newton steps, objective
 // evaluations, CCD calls.
 static std::vector<BodyState> unpack_bodies(int nb, const double* mass, const double* moment,
                                             const double* pose, const double* vel,
@@ -586,6 +586,7 @@ static SimParams unpack_params(const double* params)
     sp.average_mass = params[15];
     sp.newton_polish = (int)params[16];
     sp.ccd_rescale = params[17];
+    sp.trajectory = (int)params[18];
     return sp;
 }
 

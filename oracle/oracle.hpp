@@ -281,6 +281,7 @@ struct SimParams {
     double bbox_diagonal, average_mass;
     int newton_polish = 0;  // full Newton steps after convergence (0: the reference's solver)
     double ccd_rescale = 1; // step bound s * toi when the CCD limits the step (1: the reference)
+    int trajectory = 0;     // line-search CCD: 0 RIGID, 1 PIECEWISE_LINEAR (minimum separation dmin)
 };
 struct SimStats {
     long long newton_iterations = 0, newton_steps = 0, objective_evals = 0, ccd_calls = 0;

@@ -427,7 +427,8 @@ def det_cos(x):
 SIM_DEFAULTS = dict(dmin=0.0, mu=0.0, epsv=1e-3, max_newton_iterations=3000,
                     velocity_conv_tol=1e-2, velocity_conv_tol_abs=0,
                     line_search_lower_bound=1e-12, dhat_epsilon=1e-9,
-                    min_barrier_stiffness_scale=1e11, newton_polish=0, ccd_rescale=1.0)
+                    min_barrier_stiffness_scale=1e11, newton_polish=0, ccd_rescale=1.0,
+                    trajectory=0)
 
 
 def linear_ccd(p0, p1, ms=0.0, fv=False):
@@ -473,7 +474,8 @@ class OracleSim:
                     p["max_newton_iterations"], p["velocity_conv_tol"],
                     p["velocity_conv_tol_abs"], p["line_search_lower_bound"],
                     p["dhat_epsilon"], p["min_barrier_stiffness_scale"], self.bbox_diagonal,
-                    self.scene.average_mass, p["newton_polish"], p["ccd_rescale"]])
+                    self.scene.average_mass, p["newton_polish"], p["ccd_rescale"],
+                    p["trajectory"]])
 
     def step(self, record=False):
         """One time step; with record=True the start-of-step state and the

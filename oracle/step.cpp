@@ -340,6 +340,7 @@ struct Problem {
         Candidates cand;
         detect_candidates(s, x, x1, true, p.dmin / 2, false, cand);
         const int nt = std::max(1, (int)std::thread::hardware_concurrency());
+        if (p.trajectory == 1) return pl_earliest_toi(s, x, x1, cand, p.dmin, nt, nullptr, nullptr);
         return earliest_toi(s, x, x1, cand, 1e-4, nt, nullptr, nullptr);
     }
 };

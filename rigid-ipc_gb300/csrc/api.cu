@@ -615,9 +615,12 @@ int rigc_sim_init(rigc_ctx* ctx, const rigc_sim_params* params, const rigc_sim_s
     const rigc_sim_params& p = *params;
     if (!(p.timestep > 0) || !(p.dhat > 0) || !(p.dmin >= 0) || !(p.average_mass > 0)
         || !(p.world_bbox_diagonal > 0) || p.max_newton_iterations < 1 || p.newton_polish < 0
-        || !(p.ccd_rescale > 0 && p.ccd_rescale <= 1))
+        || !(p.ccd_rescale > 0 && p.ccd_rescale <= 1)
+        || (p.trajectory_type != RIGC_TRAJECTORY_RIGID && p.trajectory_type != RIGC_TRAJECTORY_PIECEWISE_LINEAR))
         return RIGC_ERR_ARG;
     Ctx& c = *ctx_of(ctx);
+    // the batched step takes per-scene times of impact from the rigid CCD only
+    if (c.s.nscenes > 1 && p.trajectory_type != RIGC_TRAJECTORY_RIGID) return RIGC_ERR_ARG;
     for (int i = 0; i < 6 * c.s.nb; i++)
         if (!std::isfinite(state->poses[i]) || !std::isfinite(state->velocities[i])) return RIGC_ERR_NAN;
     return sim_init(c, p, *state);

@@ -53,6 +53,19 @@ int barrier_term_impl(Ctx& c, const double* x, double dhat, double dmin, int fla
                       rigc_barrier_out* out);
 int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flags,
             double* toi_host, double* per);
+int run_pl_ccd(Ctx& c, const double* x0, const double* x1, double dmin, double* toi_host, double* per);
+
+// the line search's CCD over the candidates just found: the rigid interval
+// trajectory (time tolerance 1e-4) or the piecewise-linear one with minimum
+// separation dmin (DistanceBarrierConstraint::compute_earliest_toi with the
+// scene's trajectory_type)
+static int line_search_ccd(Ctx& c, const rigc_sim_params& p, const double* x, const double* xt,
+                           double* toi)
+{
+    if (p.trajectory_type == RIGC_TRAJECTORY_PIECEWISE_LINEAR)
+        return run_pl_ccd(c, x, xt, p.dmin, toi, nullptr);
+    return run_ccd(c, x, xt, 1e-4, 0, toi, nullptr);
+}
 
 namespace {
 
@@ -2196,7 +2209,7 @@ int sim_step(Ctx& c, rigc_step_stats* stats)
             k_axpy<<<grid_for(n, 256), 256, 0, st>>>(n, 1.0, dir, x, xt);
             double toi;
             RIGC_TRY(detect_and_count(c, x, xt, true, p.dmin / 2.0));
-            int s2 = run_ccd(c, x, xt, 1e-4, 0, &toi, nullptr);
+            int s2 = line_search_ccd(c, p, x, xt, &toi);
             if (s2 != RIGC_OK && s2 != RIGC_ERR_QUEUE_OVERFLOW && s2 != RIGC_ERR_ITER_LIMIT) return s2;
             local.ccd_calls++;
             alpha = std::min(1.0, toi < 1.0 ? p.ccd_rescale * toi : toi);
@@ -2269,7 +2282,7 @@ int sim_step(Ctx& c, rigc_step_stats* stats)
         k_axpy<<<grid_for(n, 256), 256, 0, st>>>(n, 1.0, S.sol.as<double>(), x, xt);
         double toi;
         RIGC_TRY(detect_and_count(c, x, xt, true, p.dmin / 2.0));
-        int s2 = run_ccd(c, x, xt, 1e-4, 0, &toi, nullptr);
+        int s2 = line_search_ccd(c, p, x, xt, &toi);
         if (s2 != RIGC_OK && s2 != RIGC_ERR_QUEUE_OVERFLOW && s2 != RIGC_ERR_ITER_LIMIT) return s2;
         local.ccd_calls++;
         if (toi < 1.0) break;

@@ -393,11 +393,14 @@ class Context:
                  velocity_conv_tol=1e-2, velocity_conv_tol_abs=False,
                  line_search_lower_bound=1e-12, dhat_epsilon=1e-9,
                  min_barrier_stiffness_scale=1e11, newton_polish=0, ccd_rescale=1.0,
-                 poses=None, velocities=None, Qdot=None, world_bbox_diagonal=None):
+                 poses=None, velocities=None, Qdot=None, world_bbox_diagonal=None,
+                 trajectory="rigid"):
         """Start a simulation from the scene's poses, velocities and Qdot (or
         from the given host arrays: poses / velocities nb x 6, Qdot nb x 9).
         world_bbox_diagonal (default: that of the start poses) bounds the
-        barrier stiffness; a resumed run passes the one of the scene as read."""
+        barrier stiffness; a resumed run passes the one of the scene as read.
+        trajectory: the line search's CCD, "rigid" or "piecewise_linear" (the
+        reference's JSON default)."""
         sc = self.scene
         V = sc.world_vertices(sc.poses() if poses is None
                               else np.asarray(poses, np.float64).reshape(-1))
@@ -418,6 +421,7 @@ class Context:
                                  if world_bbox_diagonal is None else float(world_bbox_diagonal))
         p.newton_polish = int(newton_polish)
         p.ccd_rescale = float(ccd_rescale)
+        p.trajectory_type = {"rigid": 0, "piecewise_linear": 1}[trajectory]
         fixed = np.array([int(sum(1 << k for k in range(6) if b.is_dof_fixed[k]))
                           for b in sc.bodies], dtype=np.int32)
         if Qdot is None:

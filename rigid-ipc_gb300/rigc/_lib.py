@@ -95,7 +95,7 @@ class SimParams(C.Structure):
                 ("line_search_lower_bound", C.c_double), ("dhat_epsilon", C.c_double),
                 ("min_barrier_stiffness_scale", C.c_double), ("average_mass", C.c_double),
                 ("world_bbox_diagonal", C.c_double), ("newton_polish", C.c_int32),
-                ("ccd_rescale", C.c_double)]
+                ("ccd_rescale", C.c_double), ("trajectory_type", C.c_int32)]
 
 
 class SimState(C.Structure):

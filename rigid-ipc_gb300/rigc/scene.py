@@ -348,6 +348,9 @@ class Scene:
     friction: float = 0.0
     num_steps: int = 100
     name: str = "scene"
+    # the CCD trajectory of the line search ("rigid" or "piecewise_linear";
+    # CollisionConstraint's own default is rigid)
+    trajectory: str = "rigid"
 
     def __post_init__(self):
         self.refresh()
@@ -490,7 +493,8 @@ def scene_from_json(spec) -> Scene:
         gravity=tuple(rbp.get("gravity", [0, -9.81, 0])),
         friction=rbp.get("coefficient_friction", 0.0),
         num_steps=int(round(spec.get("max_time", 1.0) / spec.get("timestep", 0.01))),
-        name=spec.get("name", "scene"))
+        name=spec.get("name", "scene"),
+        trajectory=dbc.get("trajectory_type", "rigid"))
 
 
 def named_mesh(name: str):

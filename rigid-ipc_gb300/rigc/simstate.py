@@ -43,7 +43,8 @@ class SimState:
     """One simulation of a reference-format scene on the device.
 
     solver: keyword arguments of Context.sim_init (Newton tolerances and the
-    like); the time step, gravity, dhat, dmin and friction come from the
+    like); the time step, gravity, dhat, dmin, friction and the CCD
+    trajectory (distance_barrier_constraint.trajectory_type) come from the
     scene."""
 
     def __init__(self, spec, **solver):
@@ -67,9 +68,11 @@ class SimState:
 
     def _init(self, poses, velocities, Qdot):
         sc = self.scene
+        solver = dict(self.solver)
+        solver.setdefault("trajectory", sc.trajectory)
         self.ctx.sim_init(sc.timestep, sc.gravity, sc.dhat, sc.dmin,
                           coefficient_friction=sc.friction, poses=poses, velocities=velocities,
-                          Qdot=Qdot, world_bbox_diagonal=self.bbox_diagonal, **self.solver)
+                          Qdot=Qdot, world_bbox_diagonal=self.bbox_diagonal, **solver)
 
     @property
     def num_steps(self):

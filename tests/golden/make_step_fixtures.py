@@ -27,6 +27,10 @@ it):
   A run that differs from the oracle's only in rounding follows one of
   these trajectories (to ~1e-13 per step), not necessarily the unperturbed
   one;
+* cubes_pl_tight: the cubes_tight run with the line search's CCD on the
+  piecewise-linear trajectory (the reference's JSON default), 40 steps
+  through the landings; a 1e-15 perturbation of the start poses stays below
+  2e-13 over them;
 * pair: two cubes landing on the plane and sliding into each other with
   friction (mu 0.5), 10 steps;
 * pile: 8 subdivision-3 icospheres in a seeded contact pile (2e-4 m gaps)
@@ -87,6 +91,9 @@ def inputs_digest(sc, x0):
     return digest(sc.rest_vertices, np.asarray(x0, np.float64), sc.velocities())
 
 
+PL_STEPS = 40
+
+
 def run(sc, steps, x0=None, mu=0.0, probes=False, **solver):
     import oracle as O
 
@@ -129,9 +136,18 @@ def main():
     (out["cubes_tight_poses"], out["cubes_tight_kappa"], out["cubes_tight_crossings"],
      out["cubes_tight_min_distance"]) = run(sc, CUBE_STEPS, probes=True, **TIGHT)
     add_branches(out)
+    add_pl(out)
     np.savez_compressed(OUT, **out)
     print(f"wrote {OUT}: crossings per cube step {out['cubes_crossings'].max()}, "
           f"{out['cubes_tight_crossings'].max()} (tight)")
+
+
+def add_pl(out):
+    """cubes_pl_tight_poses / _crossings / _min_distance: the converged run
+    with the piecewise-linear line-search CCD."""
+    sc = cubes_scene()
+    (out["cubes_pl_tight_poses"], _, out["cubes_pl_tight_crossings"],
+     out["cubes_pl_tight_min_distance"]) = run(sc, PL_STEPS, probes=True, trajectory=1, **TIGHT)
 
 
 BRANCH_SEEDS = (1, 2, 3, 4)
@@ -166,7 +182,13 @@ def add_branches(out):
 
 
 if __name__ == "__main__":
-    if "--branches" in sys.argv:
+    if "--pl" in sys.argv:
+        # only the piecewise-linear entries, added to the existing file
+        out = dict(np.load(OUT))
+        add_pl(out)
+        np.savez_compressed(OUT, **out)
+        print("piecewise-linear run", out["cubes_pl_tight_poses"].shape)
+    elif "--branches" in sys.argv:
         # only the branch entries, added to the existing file
         out = dict(np.load(OUT))
         add_branches(out)

@@ -151,6 +151,46 @@ def test_cube_lattice_whole_run_matches_oracle():
     assert landed > 20  # the cubes rest on the plane for the last steps
 
 
+def test_cube_lattice_piecewise_linear_matches_oracle():
+    """The converged 27-cube run with the line search's CCD on the
+    piecewise-linear trajectory (the reference's JSON default): poses within
+    1e-10 of the oracle's after each of 40 steps through the landings (a
+    1e-15 perturbation of the oracle's start stays below 2e-13 here), no
+    crossing edge and face after any step, the oracle's minimum distance."""
+    import rigc
+
+    import make_step_fixtures as SF
+
+    sc = SF.cubes_scene()
+    fx = _fixture("cubes", sc, sc.poses())
+    ctx = rigc.Context(sc)
+    ctx.sim_init(SF.H, SF.G, SF.DHAT, trajectory="piecewise_linear", **SF.TIGHT)
+    assert fx["cubes_pl_tight_crossings"].max() == 0
+    for k in range(SF.PL_STEPS):
+        ctx.sim_step(1)
+        P, V, Q, kappa = ctx.sim_state()
+        x = P.reshape(-1)
+        err = np.abs(x - fx["cubes_pl_tight_poses"][k + 1]).max()
+        assert err <= 1e-10, (k, err)
+        assert ctx.detect_intersections(x) == 0, k
+        md_o = fx["cubes_pl_tight_min_distance"][k]
+        md = ctx.compute_min_distance(x, SF.DHAT)
+        assert (md < 0) == (md_o < 0), k
+        if md_o > 0:
+            assert abs(md - md_o) <= 1e-9, (k, md, md_o)
+
+
+def test_piecewise_linear_rejected_on_batched_context():
+    import rigc
+    from rigc import scene as S
+
+    scenes = [S.scene_from_json(S.spec_cubes(seed)) for seed in range(2)]
+    big, sob = S.concat_scenes(scenes)
+    ctx = rigc.Context(big, scene_of_body=sob)
+    with pytest.raises(RuntimeError):
+        ctx.sim_init(0.01, (0, -9.81, 0), 1e-3, trajectory="piecewise_linear")
+
+
 def test_cube_lattice_default_solver():
     """The same run with the reference's default Newton tolerance
     (velocity_conv_tol 1e-2): the iterates are not converged, so any change
