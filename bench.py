@@ -315,6 +315,18 @@ def sim_rate(args, torch):
            "steps_per_s": args.sim_steps / dt,
            "newton_iterations_per_step": st["newton_iterations"] / args.sim_steps,
            "cg_iterations_per_newton": st["cg_iterations"] / max(st["newton_iterations"], 1)}
+    # the same window with the line search's CCD on the piecewise-linear
+    # trajectory (the reference's JSON default)
+    ctx = rigc.Context(sc)
+    ctx.sim_init(0.01, (0.0, -9.81, 0.0), 1e-3, trajectory="piecewise_linear")
+    ctx.sim_step(SIM_FIRST)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    st = ctx.sim_step(args.sim_steps)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t
+    out["piecewise_linear"] = {"steps_per_s": args.sim_steps / dt,
+                               "newton_iterations_per_step": st["newton_iterations"] / args.sim_steps}
     if not args.no_cpu_baseline:
         import oracle as O
 

@@ -288,16 +288,18 @@ __device__ double piece_deviation(const PLArgs& a, const int vid[4], int na, int
 __device__ double linear_toi(bool fv, const double P0[4][3], const double P1[4][3], double ms,
                              int lane, long long& boxes, int& status)
 {
-    const int j = lane >> 3, k = lane & 7;  // lane 8 j + k: coordinate j at corner k (lanes < 24)
+    // lanes < 24 in three roles per box, lane = 8 j + r for coordinate j:
+    //  1. r = 4 it + m: point m's position at t = t_it (it 0: t0, 1: t1);
+    //  2. r = 4 it + 2 iw + ab: the edge terms a(t_it, u_iw) (ab = 0) and
+    //     b(t_it, v_iw) (ab = 1) of the distance function;
+    //  3. r = k: F at corner k = it + 2 iu + 4 iv, b - a combined.
+    // The same operations on the same operands as corner by corner.
+    const int j = lane >> 3, k = lane & 7;
     const bool clane = lane < 24;
-    double p0[4] = { 0, 0, 0, 0 }, p1[4] = { 0, 0, 0, 0 };
-    if (clane) {
-#pragma unroll
-        for (int m = 0; m < 4; m++) {
-            p0[m] = P0[m][j];
-            p1[m] = P1[m][j];
-        }
-    }
+    const int it1 = (k >> 2) & 1, m1 = k & 3;         // role 1
+    const int iw2 = (k >> 1) & 1, ab2 = k & 1;        // role 2 (it = it1)
+    const int iu3 = (k >> 1) & 1, iv3 = (k >> 2) & 1, it3 = k & 1;  // role 3
+    const double p0m = clane ? P0[m1][j] : 0.0, p1m = clane ? P1[m1][j] : 0.0;
     Node cn { { 0, 0, 0 }, { 0ull, 0ull, 0ull }, 0 };
     bool has_cn = true;
     u128 pend = 0, mt = 0, ma = 0;
@@ -328,21 +330,30 @@ __device__ double linear_toi(bool fv, const double P0[4][3], const double P1[4][
             break;
         }
         n++;
-        // F at this lane's corner
+        // 1. the points at t0 and t1
+        const Itv q = iadd(imul_nonneg(isub(pt(p1m), pt(p0m)), pt(it1 ? t1 : t0)), pt(p0m));
+        // 2. the edge terms: EE a = (q1 - q0) u + q0, b = (q3 - q2) v + q2;
+        //    FV a = (q2 - q1) u, b = (q3 - q1) v
+        const int qb = 8 * j + 4 * it1;  // role-1 lanes of (j, t_it)
+        const int sa = fv ? (ab2 ? 3 : 2) : (ab2 ? 3 : 1);
+        const int sb = fv ? 1 : (ab2 ? 2 : 0);
+        const Itv qa { __shfl_sync(0xffffffffu, q.lo, qb + sa), __shfl_sync(0xffffffffu, q.hi, qb + sa) };
+        const Itv qs { __shfl_sync(0xffffffffu, q.lo, qb + sb), __shfl_sync(0xffffffffu, q.hi, qb + sb) };
+        const Itv w = pt(ab2 ? (iw2 ? v1 : v0) : (iw2 ? u1 : u0));
+        const Itv d = imul_nonneg(isub(qa, qs), w);
+        const Itv term = fv ? d : iadd(d, qs);
+        // 3. F at corner k
+        const int tb0 = 8 * j + 4 * it3;  // role-2 and role-1 lanes of (j, t_it)
+        const Itv ta { __shfl_sync(0xffffffffu, term.lo, tb0 + 2 * iu3), __shfl_sync(0xffffffffu, term.hi, tb0 + 2 * iu3) };
+        const Itv tb { __shfl_sync(0xffffffffu, term.lo, tb0 + 2 * iv3 + 1),
+                       __shfl_sync(0xffffffffu, term.hi, tb0 + 2 * iv3 + 1) };
         Itv y { 0.0, 0.0 };
-        if (clane) {
-            const Itv t = pt((k & 1) ? t1 : t0), u = pt((k & 2) ? u1 : u0), v = pt((k & 4) ? v1 : v0);
-            Itv q[4];
-#pragma unroll
-            for (int m = 0; m < 4; m++) q[m] = iadd(imul_nonneg(isub(pt(p1[m]), pt(p0[m])), t), pt(p0[m]));
-            if (fv) {
-                const Itv fp = iadd(iadd(imul_nonneg(isub(q[2], q[1]), u), imul_nonneg(isub(q[3], q[1]), v)), q[1]);
-                y = isub(q[0], fp);
-            } else {
-                const Itv ea = iadd(imul_nonneg(isub(q[1], q[0]), u), q[0]);
-                const Itv eb = iadd(imul_nonneg(isub(q[3], q[2]), v), q[2]);
-                y = isub(ea, eb);
-            }
+        if (fv) {
+            const Itv q0 { __shfl_sync(0xffffffffu, q.lo, tb0), __shfl_sync(0xffffffffu, q.hi, tb0) };
+            const Itv q1 { __shfl_sync(0xffffffffu, q.lo, tb0 + 1), __shfl_sync(0xffffffffu, q.hi, tb0 + 1) };
+            if (clane) y = isub(q0, iadd(iadd(ta, tb), q1));
+        } else if (clane) {
+            y = isub(ta, tb);
         }
         // the changes of F along t, u, v: |mid(corner with the bit) -
         // mid(corner without)|, largest over the lanes
