@@ -3,8 +3,10 @@ and the torch.autograd.Function over it) against the oracle's adjoint and
 against central finite differences (h = 1e-6) of the oracle's simulator.
 
 Bars: poses after the rollout within 1e-8 of the oracle's; gradients within
-1e-6 (max-norm relative) of the oracle's adjoint and within 1e-5 relative of
-the finite differences along random directions; checkpoint intervals give
+1e-6 (max-norm relative) of the oracle's adjoint, within 1e-5 relative of
+the finite differences along random directions, within 1e-7 of the largest
+component of the extrapolated differences in every one of the differentiation
+workload's 384 parameters; checkpoint intervals give
 bit-identical gradients (the recomputed segments are bit-identical)."""
 import numpy as np
 import pytest
@@ -139,7 +141,9 @@ def test_cube_lattice_adjoint_matches_fixture():
     """The differentiation workload (64 cubes landing on a plane, 50 steps,
     384 velocity parameters): the device gradient against the oracle's
     adjoint and against central differences (h = 1e-6) of the oracle's
-    simulator, both committed in tests/golden/adjoint_cube_lattice.npz."""
+    simulator along random directions (tests/golden/adjoint_cube_lattice.npz)
+    and in every one of the 384 parameters at h = 1e-6 and h / 2
+    (tests/golden/adjoint_cube_lattice_fd.npz)."""
     import os
 
     import make_adjoint_fixture as F
@@ -170,3 +174,12 @@ def test_cube_lattice_adjoint_matches_fixture():
         # the plain ones at h = 1e-6 are truncation-limited (~2e-5) here
         assert abs(ad - fd_x) <= FD_RTOL * abs(fd_x), (ad, fd_x)
         assert abs(ad - fd) <= 1e-4 * abs(fd), (ad, fd)
+    # every one of the 384 parameters: central differences of the oracle's
+    # simulator at h = 1e-6 and h / 2 (adjoint_cube_lattice_fd.npz) and
+    # their extrapolation
+    fd_all = np.load(os.path.join(os.path.dirname(F.__file__), "adjoint_cube_lattice_fd.npz"))
+    ga = g[:64]
+    scale = np.abs(fd_all["fd_extrapolated"]).max()
+    assert np.abs(ga - fd_all["fd_h"]).max() <= 1e-5 * scale
+    assert np.abs(ga - fd_all["fd_h2"]).max() <= 3e-6 * scale
+    assert np.abs(ga - fd_all["fd_extrapolated"]).max() <= 1e-7 * scale
