@@ -379,7 +379,7 @@ def pass_rates_tuned(ctx, x0, x1, dhat, torch):
                   "barrier_pairs_per_s": t["barrier_pairs_per_s"],
                   "choice": {k: tune[k] for k in ("ccd_blocks_per_sm", "cache_slots_per_body",
                                                   "ccd_seeds_log2", "ccd_hand_off", "ccd_warp",
-                                                  "barrier_per_warp")}}
+                                                  "ccd_window_log2", "barrier_per_warp")}}
     return r
 
 
@@ -656,6 +656,7 @@ def batched_sim_rate(args, torch, items, big, sob, tune):
     cb = rigc.Context(big, scene_of_body=sob)
     cb.set_tune(tune["ccd_blocks_per_sm"], tune["cache_slots_per_body"], tune["barrier_per_warp"],
                 tune["ccd_seeds_log2"], tune["ccd_hand_off"], tune["ccd_warp"])
+    cb.set_ccd_window(tune["ccd_window_log2"])
     cb.sim_init(0.01, grav, dhat, poses=X0)
     cb.sim_step(1)
     torch.cuda.synchronize()

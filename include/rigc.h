@@ -127,6 +127,8 @@ typedef struct rigc_stats {
     int64_t cand_fv;
     int64_t kernel_launches;  /* kernels launched by this library so far     */
     int32_t last_status;
+    int32_t ccd_launches;     /* search launches of the last earliest-toi    */
+    int64_t ccd_pieces;       /* search pieces those launches took up        */
 } rigc_stats;
 
 /* ---- context (replaces the RigidBodyAssembler set-up,
@@ -228,6 +230,18 @@ int rigc_earliest_toi_piecewise_linear(rigc_ctx* ctx, const double* x0,
  * warp (the warp evaluates each box's corners together; the default, also
  * for -1), 1 one per lane.  The results are the same bits. */
 int rigc_set_pl_search(rigc_ctx* ctx, int32_t per_lane);
+
+/* Time windows of the rigid CCD's pruned searches (the earliest time of
+ * impact; no counterpart in the reference, whose candidates run in any
+ * order under one running minimum, compute_earliest_toi in
+ * src/ccd/rigid/time_of_impact.cpp): the first launch searches only the boxes
+ * that start before 2^-window_log2 and defers the others, each later launch
+ * doubles the window, so the boxes of all candidates are searched roughly in
+ * time order and the running minimum, once found, skips every later box.
+ * -1 the built-in choice (2^-6 from 65,536 candidates on, else none), 0 no
+ * windows.  The earliest time of impact
+ * is the same bits either way; only the work differs. */
+int rigc_set_ccd_window(rigc_ctx* ctx, int32_t window_log2);
 
 /* DistanceBarrierConstraint::compute_earliest_toi
  * (src/opt/distance_barrier_constraint.cpp:130-149) with trajectory
@@ -456,6 +470,7 @@ typedef struct rigc_tune_report {
     int32_t ccd_seeds_log2;
     int32_t ccd_hand_off;
     int32_t ccd_warp;
+    int32_t ccd_window_log2;  /* rigc_set_ccd_window's choice (-1: built-in) */
 } rigc_tune_report;
 int rigc_autotune(rigc_ctx* ctx, const double* x0, const double* x1, double dhat, double dmin,
                   rigc_tune_report* report);

@@ -141,7 +141,7 @@ static void release_all(Ctx* c)
                        &c->d_scalars, &c->body_box, &c->body_in, &c->vbox, &c->ebox, &c->fbox,
                        &c->vin, &c->ein, &c->fin, &c->items_key, &c->items_val, &c->items_key2,
                        &c->items_val2, &c->seg, &c->pair_out, &c->pair_key, &c->large_list,
-                       &c->x0_dev, &c->x1_dev, &c->rot_table, &c->cand_tol, &c->frame_keys, &c->ccd_pieces[0], &c->ccd_pieces[1], &c->pl_table,
+                       &c->x0_dev, &c->x1_dev, &c->rot_table, &c->cand_tol, &c->frame_keys, &c->ccd_pieces[0], &c->ccd_pieces[1], &c->ccd_pieces[2], &c->ccd_pieces[3], &c->pl_table,
                        &c->frame_vals, &c->fric.type, &c->fric.verts, &c->fric.bodies,
                        &c->fric.coef, &c->fric.v0c, &c->fric.V0, &c->fric.c_energy,
                        &c->fric.c_grad, &c->fric.c_blocks, &c->fric.grad, &c->fric.row_ptr,
@@ -455,6 +455,13 @@ int rigc_set_pl_search(rigc_ctx* ctx, int32_t per_lane)
 {
     if (!ctx || per_lane < -1 || per_lane > 1) return RIGC_ERR_ARG;
     ctx_of(ctx)->tune.pl_per_lane = per_lane;
+    return RIGC_OK;
+}
+
+int rigc_set_ccd_window(rigc_ctx* ctx, int32_t window_log2)
+{
+    if (!ctx || window_log2 < -1 || window_log2 > 30) return RIGC_ERR_ARG;
+    ctx_of(ctx)->tune.ccd_window_log2 = window_log2;
     return RIGC_OK;
 }
 

@@ -1,6 +1,6 @@
 // Autotuner of the narrow phase's launch shapes on a caller's workload.
 //
-// Six shapes are searched, one after the other, each by timing the call
+// Seven shapes are searched, one after the other, each by timing the call
 // it shapes (one warm-up, then the median of three runs) on the context's
 // own scenes:
 //  * k_ccd's resident blocks per SM (1 .. the occupancy limit): fewer blocks
@@ -13,6 +13,9 @@
 //  * one CCD search per lane (k_ccd), per warp (k_ccd_group<32>, as
 //    compiled or fitted to 4 or 5 blocks per SM) or per half-warp
 //    (k_ccd_group<16>, as compiled or fitted to 4 blocks per SM), first;
+//  * the CCD's first time window (none, 2^-4 .. 2^-8): small windows search
+//    the boxes of all candidates closer to time order, so the running minimum
+//    skips more of them, each window costs a launch;
 //  * the CCD boxes a search piece evaluates before it hands its pending
 //    boxes to a further launch (never, 16, the built-in 64, 256): short
 //    pieces spread deep searches over the GPU, each hand-off costs a launch;
@@ -86,6 +89,19 @@ int autotune(Ctx& c, const double* x0, const double* x1, double dhat, double dmi
         }
     }
     c.tune.ccd_warp = best_mode;
+    // the CCD's first time window (searches of one search per lane take none)
+    int best_window = -1;
+    if (best_mode != 0)
+        for (int w : { 0, 4, 5, 7, 8 }) {
+            c.tune.ccd_window_log2 = w;
+            double ms;
+            RIGC_TRY(median_ms(ccd, &ms));
+            if (ms < best) {
+                best = ms;
+                best_window = w;
+            }
+        }
+    c.tune.ccd_window_log2 = best_window;
     int occ;
     RIGC_TRY(ccd_max_blocks_per_sm(&occ, c.tune.ccd_warp));
     int best_bps = 0;
@@ -160,6 +176,7 @@ int autotune(Ctx& c, const double* x0, const double* x1, double dhat, double dmi
     r.ccd_seeds_log2 = c.tune.ccd_seeds_log2;
     r.ccd_hand_off = c.tune.ccd_hand_off;
     r.ccd_warp = c.tune.ccd_warp;
+    r.ccd_window_log2 = c.tune.ccd_window_log2;
     if (rep) *rep = r;
     return RIGC_OK;
 }

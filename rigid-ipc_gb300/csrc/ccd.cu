@@ -50,6 +50,13 @@ constexpr int kCCDThreads = 128;
 constexpr int kHandOff = 64;
 constexpr unsigned long long kPiecesCap = 1ull << 18;
 constexpr int kMaxLaunches = 32;
+// time windows (search groups, prune mode): the first window 2^-k (built-in
+// k, from kWindowMinCandidates candidates on: below, the launches they add
+// cost more than the boxes they skip), each later launch's twice the last
+// one's, none from 1 on; slots per piece buffer at most kWindowCap
+constexpr int kWindowLog2 = 6;
+constexpr int64_t kWindowMinCandidates = 1 << 16;
+constexpr unsigned long long kWindowCap = 1ull << 22;
 
 struct CCDArgs {
     const double* rest;
@@ -96,6 +103,13 @@ struct CCDArgs {
     unsigned long long* n_out;
     unsigned long long out_cap;
     unsigned long long hand_off;  // boxes per piece before a hand-off (0: never)
+    // Time window (prune mode, search groups): a box starting at or after
+    // it is written to pieces_out instead of being searched, and the next
+    // launch searches it under a later window (+inf: no window).  The boxes
+    // of all candidates are so searched roughly in time order, and the
+    // running minimum, once some candidate's root is found, skips the boxes
+    // after it in every candidate.
+    double window;
 };
 
 struct Box {
@@ -1182,6 +1196,28 @@ k_ccd_group(CCDArgs a)
                 double sl = add_dn(x.a0, x.b0), sh = add_up(x.a1, x.b1);
                 if (!(le_nn(sl, 1.0) && !is_neg(sh))) continue;
             }
+            if (x.t0 >= a.window) {
+                // after the window: a piece of the next launch (searched
+                // now when there is no room for it)
+                unsigned long long s = 0;
+                if (gl == 0) s = atomicAdd(a.n_out, 1ull);
+                s = __shfl_sync(gmask, s, 0, W);
+                if (s < a.out_cap) {
+                    if (gl == 0) {
+                        Piece pc;
+                        pc.cand = cur;
+                        pc.earliest = earliest;
+                        pc.boxes = cbase + cboxes;
+                        for (int d = 0; d < 3; d++) {
+                            pc.ix[d] = cn.ix[d];
+                            pc.lv[d] = cn.lv[d];
+                        }
+                        pc.depth = cn.depth;
+                        a.pieces_out[s] = pc;
+                    }
+                    continue;
+                }
+            }
             have = true;
             break;
         }
@@ -1212,6 +1248,15 @@ k_ccd_group(CCDArgs a)
                 const Piece pc = a.pieces_in[w];
                 cur = pc.cand;
                 if (cur < 0) continue;
+                if (a.prune && !a.scene_gmin) {
+                    // the group's first lane's copy of the running minimum
+                    const double g = __shfl_sync(gmask, __longlong_as_double(
+                        (long long)*(volatile unsigned long long*)a.gmin), 0, W);
+                    if (le_nn(g, dyadic(pc.ix[0], pc.lv[0]))) {
+                        cur = -1;  // the piece starts at or after it
+                        continue;
+                    }
+                }
                 earliest = pc.earliest;
                 cbase = pc.boxes;
 #pragma unroll
@@ -1416,6 +1461,59 @@ k_ccd_group(CCDArgs a)
     }
 }
 
+// The pieces of the last launch (out, *n_out of them, at most cap) and those
+// kept for later windows (kept, n_kept): the ones that start before `window`
+// go to `now`, the others to `later`, the ones that start at or after the
+// running minimum `gmin` (single scene; null: none) nowhere.  A list that is
+// full takes the piece into the other (their capacities sum to at least
+// the pieces given); counts[0] / counts[1] end as the appends to now / later
+// (above cap: only the first cap slots were written).
+__global__ void __launch_bounds__(256) k_split_pieces(
+    const Piece* __restrict__ out, const unsigned long long* __restrict__ n_out, unsigned long long cap,
+    const Piece* __restrict__ kept, unsigned long long n_kept, double window,
+    const unsigned long long* __restrict__ gmin, Piece* __restrict__ now, Piece* __restrict__ later,
+    unsigned long long* __restrict__ counts)
+{
+    const unsigned long long n0 = n_out ? (*n_out < cap ? *n_out : cap) : 0ull;
+    const unsigned long long total = n0 + n_kept;
+    const double g = gmin ? __longlong_as_double((long long)*gmin) : INFINITY;
+    const int lane = threadIdx.x & 31;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    // whole warps iterate together (the ballots below)
+    const unsigned long long span = (total + 31) & ~31ull;
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < span;
+         i += stride) {
+        Piece pc;
+        bool keep = false, soon = false;
+        if (i < total) {
+            pc = i < n0 ? out[i] : kept[i - n0];
+            const double t0 = dyadic(pc.ix[0], pc.lv[0]);
+            keep = pc.cand >= 0 && t0 < g;
+            soon = t0 < window;
+        }
+        // one append per warp and list
+        const unsigned m_now = __ballot_sync(0xffffffffu, keep && soon);
+        const unsigned m_later = __ballot_sync(0xffffffffu, keep && !soon);
+        unsigned long long b_now = 0, b_later = 0;
+        if (lane == 0) {
+            if (m_now) b_now = atomicAdd(counts, (unsigned long long)__popc(m_now));
+            if (m_later) b_later = atomicAdd(counts + 1, (unsigned long long)__popc(m_later));
+        }
+        b_now = __shfl_sync(0xffffffffu, b_now, 0);
+        b_later = __shfl_sync(0xffffffffu, b_later, 0);
+        if (!keep) continue;
+        const unsigned below = (1u << lane) - 1u;
+        unsigned long long slot = soon ? b_now + __popc(m_now & below) : b_later + __popc(m_later & below);
+        bool to_now = soon;
+        if (slot >= cap) {
+            // that list is full: the other one
+            to_now = !soon;
+            slot = atomicAdd(counts + (to_now ? 0 : 1), 1ull);
+        }
+        if (slot < cap) (to_now ? now : later)[slot] = pc;
+    }
+}
+
 __global__ void k_fill_inf(double* __restrict__ v, int64_t n)
 {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1564,26 +1662,54 @@ int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flag
             else
                 while (a.seeds_log2 < 5 && (n << a.seeds_log2) * 4 < full * per_block) a.seeds_log2++;
         }
-        // search pieces (prune mode): launch 0 searches the seeds and hands
-        // the rest of every search that reaches hand_off boxes to launch 1,
-        // and so on; the last launch hands nothing off
+        // search pieces (prune mode): launch 0 searches the seeds; a search
+        // that reaches hand_off boxes once the work list has run dry hands its
+        // pending boxes on, and boxes after the launch's time window are
+        // deferred; k_split_pieces then gives the next launch those that
+        // start before its window and keeps the others for later ones; the
+        // last launch hands nothing on
         a.pieces_in = nullptr;
         a.n_pieces = 0;
         a.hand_off = 0;
         a.n_out = cnt + 5;
         a.out_cap = 0;
         a.pieces_out = nullptr;
+        a.window = INFINITY;
         if (a.prune) {
             const int ho = c.tune.ccd_hand_off >= 0 ? c.tune.ccd_hand_off : kHandOff;
-            if (ho > 0) {
-                RIGC_TRY(c.ccd_pieces[0].reserve(kPiecesCap * sizeof(Piece)));
-                RIGC_TRY(c.ccd_pieces[1].reserve(kPiecesCap * sizeof(Piece)));
-                a.hand_off = (unsigned long long)ho;
-                a.out_cap = kPiecesCap;
+            const int wl = mode == 0                     ? 0
+                           : c.tune.ccd_window_log2 >= 0 ? c.tune.ccd_window_log2
+                           : n >= kWindowMinCandidates   ? kWindowLog2
+                                                         : 0;
+            unsigned long long cap = ho > 0 ? kPiecesCap : 0;
+            if (wl > 0) {
+                // deferred boxes: a few per candidate whose search goes deeper
+                // than its root box
+                if (!cap) cap = kPiecesCap;
+                while (cap < kWindowCap && cap < (unsigned long long)(n << a.seeds_log2) * 2) cap *= 2;
+                a.window = std::ldexp(1.0, -wl);
+            }
+            if (cap > 0) {
+                for (int b = 0; b < 4; b++) RIGC_TRY(c.ccd_pieces[b].reserve(cap * sizeof(Piece)));
+                a.hand_off = (unsigned long long)std::max(ho, 0);
+                a.out_cap = cap;
                 a.pieces_out = c.ccd_pieces[0].as<Piece>();
             }
         }
+        // pieces: [0] a launch's output, [1] the next launch's input, [2] / [3]
+        // those after its window (ping-pong)
+        unsigned long long* split_n = cnt + 6;
+        unsigned long long n_later = 0;
+        int later = 2;
+        int dev_sms = kNumSMs;
+        {
+            int dv = 0;
+            RIGC_CUDA(cudaGetDevice(&dv));
+            RIGC_CUDA(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, dv));
+        }
         int64_t want = ((n << a.seeds_log2) + per_block - 1) / per_block;
+        c.stats.ccd_launches = 0;
+        c.stats.ccd_pieces = 0;
         for (int launch = 0;; launch++) {
             RIGC_COUNT_LAUNCH();
             const unsigned grid = (unsigned)std::min(want, full);
@@ -1596,20 +1722,42 @@ int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flag
             default: k_ccd<<<grid, kCCDThreads, 0, st>>>(a);
             }
             RIGC_CUDA(cudaGetLastError());
-            if (!a.hand_off) break;
-            unsigned long long np = 0;
-            RIGC_CUDA(cudaMemcpyAsync(&np, a.n_out, sizeof(np), cudaMemcpyDeviceToHost, st));
-            RIGC_CUDA(cudaStreamSynchronize(st));
-            np = std::min(np, a.out_cap);
-            if (np == 0) break;
-            // the pieces just written become the next launch's work
+            c.stats.ccd_launches++;
+            if (!a.out_cap) break;
+            // the next launch's pieces: those that start before its window,
+            // among this launch's and the later windows' (none after the
+            // running minimum of a single scene); empty windows are skipped
+            const bool last_launch = launch + 1 >= kMaxLaunches - 1;
+            unsigned long long n_now = 0;
+            bool from_out = true;
+            for (;;) {
+                const double next_window = last_launch || !(a.window < 0.5) ? INFINITY : 2 * a.window;
+                RIGC_CUDA(cudaMemsetAsync(split_n, 0, 2 * sizeof(unsigned long long), st));
+                RIGC_COUNT_LAUNCH();
+                k_split_pieces<<<4 * dev_sms, 256, 0, st>>>(
+                    c.ccd_pieces[0].as<Piece>(), from_out ? a.n_out : nullptr, a.out_cap,
+                    c.ccd_pieces[later].as<Piece>(), n_later, next_window,
+                    c.s.nscenes > 1 ? nullptr : a.gmin, c.ccd_pieces[1].as<Piece>(),
+                    c.ccd_pieces[5 - later].as<Piece>(), split_n);
+                RIGC_CUDA(cudaGetLastError());
+                unsigned long long h[2];
+                RIGC_CUDA(cudaMemcpyAsync(h, split_n, sizeof(h), cudaMemcpyDeviceToHost, st));
+                RIGC_CUDA(cudaStreamSynchronize(st));
+                n_now = std::min(h[0], a.out_cap);
+                n_later = std::min(h[1], a.out_cap);
+                later = 5 - later;
+                a.window = next_window;
+                from_out = false;
+                if (n_now > 0 || n_later == 0) break;
+            }
+            if (n_now == 0) break;
             const unsigned long long zero[2] = { 0, 0 };
             RIGC_CUDA(cudaMemcpyAsync(a.next, zero, sizeof(zero), cudaMemcpyHostToDevice, st));
-            a.pieces_in = a.pieces_out;
-            a.n_pieces = (long long)np;
-            a.pieces_out = c.ccd_pieces[(launch + 1) & 1].as<Piece>();
-            if (launch + 1 >= kMaxLaunches - 1) a.hand_off = 0;
-            want = ((int64_t)np + per_block - 1) / per_block;
+            a.pieces_in = c.ccd_pieces[1].as<Piece>();
+            a.n_pieces = (long long)n_now;
+            c.stats.ccd_pieces += (int64_t)n_now;
+            if (last_launch) a.hand_off = 0;
+            want = ((int64_t)n_now + per_block - 1) / per_block;
         }
     }
     c.bp_table.valid = false;

@@ -185,7 +185,7 @@ struct Ctx {
     DevBuf cand_tol;  // CCD: per-candidate tolerances
     DevBuf frame_keys, frame_vals;  // CCD frame cache (hash table)
     DevBuf pl_table;  // piecewise-linear CCD: per-body piece frames and point rotations
-    DevBuf ccd_pieces[2];           // CCD search pieces handed between launches
+    DevBuf ccd_pieces[4];           // CCD search pieces: a launch's input and output, the later windows' (two)
     Friction fric;
     int64_t ccd_max_boxes = int64_t(1) << 22;  // per-candidate CCD box budget
     // launch shapes chosen by rigc_autotune (0: the built-in choice)
@@ -195,6 +195,7 @@ struct Ctx {
         int barrier_per_warp = 0;      // constraints per warp of k_barrier_local (0: by count)
         int ccd_seeds_log2 = -1;       // CCD searches per candidate, log2 (-1: by count)
         int ccd_hand_off = -1;         // CCD boxes per search piece before a hand-off (-1: default, 0: never)
+        int ccd_window_log2 = -1;      // CCD first time window 2^-k (-1: built-in, 0: no windows)
         int ccd_warp = -1;             // CCD search per lane (0) or per warp (1); -1: by candidate count
         int pl_per_lane = -1;          // piecewise-linear CCD: a candidate per lane (1) or per warp (0, -1)
     } tune;

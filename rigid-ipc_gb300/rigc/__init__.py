@@ -230,6 +230,13 @@ class Context:
         -1: the default)."""
         L.check(self.lib.rigc_set_pl_search(self.h, int(per_lane)), "rigc_set_pl_search")
 
+    def set_ccd_window(self, window_log2=-1):
+        """Time windows of the rigid CCD's pruned searches: first window
+        2^-window_log2, doubled each launch (-1: the built-in 2^-6 from
+        65,536 candidates on, 0: no windows).  The earliest time of impact
+        does not depend on it."""
+        L.check(self.lib.rigc_set_ccd_window(self.h, int(window_log2)), "rigc_set_ccd_window")
+
     def compute_earliest_toi_piecewise_linear(self, x0, x1, dmin=0.0):
         """DistanceBarrierConstraint::compute_earliest_toi with trajectory
         PIECEWISE_LINEAR (broad phase with inflation dmin / 2, then the narrow

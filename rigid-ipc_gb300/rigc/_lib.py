@@ -38,7 +38,7 @@ EXPORTS = [
     "rigc_scene_barrier_energies", "rigc_sim_rollout", "rigc_sim_backward",
     "rigc_sim_scene_params", "rigc_autotune", "rigc_set_tune", "rigc_fp64_throughput",
     "rigc_min_distance", "rigc_detect_intersections", "rigc_earliest_toi_piecewise_linear",
-    "rigc_compute_earliest_toi_piecewise_linear", "rigc_set_pl_search",
+    "rigc_compute_earliest_toi_piecewise_linear", "rigc_set_pl_search", "rigc_set_ccd_window",
 ]
 RIGC_ERR_TOO_LARGE = 7
 RIGC_ERR_SOLVE = 8
@@ -108,7 +108,8 @@ class TuneReport(C.Structure):
                 ("barrier_per_warp", C.c_int32), ("ccd_ms_default", C.c_double),
                 ("ccd_ms", C.c_double), ("barrier_ms_default", C.c_double),
                 ("barrier_ms", C.c_double), ("ccd_seeds_log2", C.c_int32),
-                ("ccd_hand_off", C.c_int32), ("ccd_warp", C.c_int32)]
+                ("ccd_hand_off", C.c_int32), ("ccd_warp", C.c_int32),
+                ("ccd_window_log2", C.c_int32)]
 
 
 class StepStats(C.Structure):
@@ -122,7 +123,8 @@ class Stats(C.Structure):
                 ("ccd_collisions", C.c_int64), ("grid_items", C.c_int64),
                 ("large_elements", C.c_int64), ("cand_ee", C.c_int64),
                 ("cand_fv", C.c_int64), ("kernel_launches", C.c_int64),
-                ("last_status", C.c_int32)]
+                ("last_status", C.c_int32), ("ccd_launches", C.c_int32),
+                ("ccd_pieces", C.c_int64)]
 
 
 _lib = None
@@ -151,6 +153,7 @@ def load():
     L.rigc_earliest_toi_piecewise_linear.argtypes = [_vp, _vp, _vp, C.c_double, _d, _vp]
     L.rigc_compute_earliest_toi_piecewise_linear.argtypes = [_vp, _vp, _vp, C.c_double, _d]
     L.rigc_set_pl_search.argtypes = [_vp, C.c_int32]
+    L.rigc_set_ccd_window.argtypes = [_vp, C.c_int32]
     L.rigc_construct_constraint_set.argtypes = [_vp, _vp, C.c_double, C.c_double,
                                                 C.POINTER(ConstraintsView)]
     L.rigc_set_constraints.argtypes = [_vp, C.c_int64, _vp, _vp, _vp, _vp, _vp, _vp]

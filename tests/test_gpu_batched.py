@@ -176,6 +176,12 @@ def test_batched_hull_scenes_match_oracle(oracle):
     ee_b, fv_b = cb.detect_collision_candidates_rigid(X0, X1, True, 0.0)
     cb.compute_earliest_toi(X0, X1)
     tois_b = cb.scene_tois()
+    # the CCD's time windows (per-scene running minima) change no bit
+    for k in (0, 3, 12):
+        cb.set_ccd_window(k)
+        cb.compute_earliest_toi(X0, X1)
+        assert np.array_equal(cb.scene_tois(), tois_b), k
+    cb.set_ccd_window(-1)
     eed_b, fvd_b = cb.detect_collision_candidates_rigid(X0, X0, False, DHAT / 2)
     cs_b = cb.construct_constraint_set(X0, DHAT)
     e_b, g_b, _ = cb.compute_barrier_term(X0, DHAT)

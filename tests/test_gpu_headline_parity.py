@@ -112,3 +112,24 @@ def test_constraint_set_and_barrier(pile):
         blk_g = val_g[rp_o[row]:rp_o[row + 1]]
         if blk_o.size:
             assert np.linalg.norm(blk_g - blk_o) <= HESS_RTOL * np.linalg.norm(blk_o)
+
+
+@pytest.mark.parametrize("warp", [1, 2, 5])
+def test_earliest_toi_time_windows(pile, warp):
+    """The pruned earliest time of impact with the CCD's time windows (first
+    window 2^-k, doubled each launch; k = 0: none) is the oracle's bit for
+    bit whatever the window, and the windows search fewer boxes than one
+    launch under the running minimum alone."""
+    sc, x0, x1, r, ctx = pile
+    ctx.detect_collision_candidates_rigid(x0, x1, True, 0.0)
+    ctx.set_tune(ccd_warp=warp)
+    boxes = {}
+    try:
+        for k in (0, 2, 7, 12):
+            ctx.set_ccd_window(k)
+            assert ctx.earliest_toi(x0, x1, prune=True) == r["toi"], k
+            boxes[k] = ctx.stats()["ccd_boxes"]
+    finally:
+        ctx.set_ccd_window(-1)
+        ctx.set_tune()
+    assert boxes[7] < boxes[0]
