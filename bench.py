@@ -805,16 +805,24 @@ def main():
             best.append(a.elapsed_time(b) / 1e3)
         return statistics.median(best)
 
-    ctx.detect_collision_candidates_rigid(x0d, x1d, True, 0.0)
-    # one untimed CCD call in the NVTX range "ccd_call": its k_ccd launches
-    # (ncu --nvtx-include ccd_call/) give the DRAM traffic of one call
+    # one untimed compute_earliest_toi in the NVTX range "ccd_call": its
+    # CCD launches (ncu --nvtx-include ccd_call/ -k regex:k_ccd) give the
+    # DRAM traffic of one CCD call as the step makes it
     torch.cuda.nvtx.range_push("ccd_call")
-    ctx.earliest_toi(x0d, x1d)
+    ctx.compute_earliest_toi(x0d, x1d)
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_pop()
-    t_ccd = timed(lambda: ctx.earliest_toi(x0d, x1d))
     st = ctx.stats()
-    t_bp = timed(lambda: ctx.detect_collision_candidates_rigid(x0d, x1d, True, 0.0))
+    # one untimed continuous broad phase in the NVTX range "bp_call"
+    torch.cuda.nvtx.range_push("bp_call")
+    ctx.count_collision_candidates_rigid(x0d, x1d, True, 0.0)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
+    # the broad phase with the candidates left on the device, and the CCD as
+    # the step runs it: compute_earliest_toi (broad phase, then the CCD taking
+    # over its frames) less the broad phase
+    t_bp = timed(lambda: ctx.count_collision_candidates_rigid(x0d, x1d, True, 0.0))
+    t_ccd = timed(lambda: ctx.compute_earliest_toi(x0d, x1d)) - t_bp
     ctx.construct_constraint_set(x0d, dhat)
     t_bar = timed(lambda: ctx.compute_barrier_term(x0d, dhat))
 

@@ -329,20 +329,24 @@ k_vertex_boxes_cont(const double* __restrict__ x0, const double* __restrict__ x1
 // the CCD's frames for the same poses (PoseI::interpolate through the same
 // interval operations; a product with a non-negative time interval gives
 // the same bits in either form), so the CCD that follows on these poses
-// takes them over.  One thread per (included body, node).
+// takes them over, with slot 127: [0, toi_tol], the interval of the
+// tolerance test every candidate's search starts with.  One thread per
+// (included body, slot).
 constexpr int kBPTableNodes = 127;  // slots 0 .. 126: depths 0 .. 6
 
 __global__ void k_bp_frames(const double* __restrict__ x0, const double* __restrict__ x1,
-                            const int* __restrict__ body_in, int nb, double* __restrict__ table)
+                            const int* __restrict__ body_in, int nb, double toi_tol,
+                            double* __restrict__ table)
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= (int64_t)nb * kBPTableNodes) return;
-    const int b = (int)(i / kBPTableNodes), slot = (int)(i % kBPTableNodes);
+    if (i >= (int64_t)nb * kRotTableSlots) return;
+    const int b = (int)(i / kRotTableSlots), slot = (int)(i % kRotTableSlots);
     if (!body_in[b]) return;
     const int d = 31 - __clz(slot + 1);
     const int k = slot + 1 - (1 << d);
-    body_time_frame(x0, x1, b, ldexp((double)k, -d), ldexp((double)(k + 1), -d),
-                    table + ((size_t)b * kRotTableSlots + slot) * kRotTableEntry);
+    double* out = table + ((size_t)b * kRotTableSlots + slot) * kRotTableEntry;
+    if (slot == kBPTableNodes) body_time_frame(x0, x1, b, 0.0, toi_tol, out);
+    else body_time_frame(x0, x1, b, ldexp((double)k, -d), ldexp((double)(k + 1), -d), out);
 }
 
 // One thread per vertex: its interval positions over the two forced halves,
@@ -852,10 +856,10 @@ __device__ __forceinline__ bool pair_types(int kind, int ta, int tb)
 // an EE (edges) or FV (face, vertex in either order) pair of elements whose
 // groups differ, or an EF pair (edge, face in either order; output in the FV
 // stream, key face * ne + edge): the overlap tests and the output key
-__device__ __forceinline__ void test_pair(const Elems& E, const float* __restrict__ f32, int ta, int ia,
-                                          int tb, int ib, const PairOut& o)
+// (after the float boxes overlap) the double boxes and the output key
+__device__ __forceinline__ void exact_pair(const Elems& E, int ta, int ia, int tb, int ib,
+                                           const PairOut& o)
 {
-    if (fboxes_disjoint(f32 + 6 * E.index(ta, ia), f32 + 6 * E.index(tb, ib))) return;
     if (!boxes_overlap(E.box(ta, ia), E.box(tb, ib))) return;
     if (ta + tb == 3) {
         const int f = ta == 2 ? ia : ib, e = ta == 2 ? ib : ia;
@@ -869,6 +873,13 @@ __device__ __forceinline__ void test_pair(const Elems& E, const float* __restric
     }
 }
 
+__device__ __forceinline__ void test_pair(const Elems& E, const float* __restrict__ f32, int ta, int ia,
+                                          int tb, int ib, const PairOut& o)
+{
+    if (fboxes_disjoint(f32 + 6 * E.index(ta, ia), f32 + 6 * E.index(tb, ib))) return;
+    exact_pair(E, ta, ia, tb, ib, o);
+}
+
 // One thread per sorted item: pairs with the items of later groups in its
 // cell (the earlier groups' items pair with it), reported in the first cell
 // both elements cover.
@@ -877,36 +888,73 @@ __global__ void k_cell_pairs(const uint64_t* __restrict__ keys, const uint32_t* 
                              const float* __restrict__ f32, PairOut o)
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    // the end of each item's run (same scene, cell and group): the warp's 32
-    // consecutive items mark where a run ends, and an item takes the first
-    // mark at or after it; a run that goes on past the warp's items is
-    // followed in memory
+    // the ends of each item's run (same scene, cell and group) and cell
+    // (same scene and cell): the warp's 32 consecutive items mark where runs
+    // and cells end, and an item takes the first mark at or after it; a run
+    // or cell that goes on past the warp's items is followed in memory
     const int lane = threadIdx.x & 31;
     const bool valid = i < m;
+    const int cs = 3 + group_bits;
     const uint64_t ki = valid ? keys[i] : 0;
-    const bool last = !valid || i + 1 >= m || (keys[i + 1] >> 3) != (ki >> 3);
-    const unsigned ends = __ballot_sync(0xffffffffu, last) & (0xffffffffu << lane);
+    const uint64_t kn = valid && i + 1 < m ? keys[i + 1] : 0;
+    const bool next = valid && i + 1 < m;
+    const bool run_last = !next || (kn >> 3) != (ki >> 3);
+    const bool cell_last = !next || (kn >> cs) != (ki >> cs);
+    const unsigned above = 0xffffffffu << lane;
+    const unsigned run_ends = __ballot_sync(0xffffffffu, run_last) & above;
+    const unsigned cell_ends = __ballot_sync(0xffffffffu, cell_last) & above;
     if (!valid) return;
-    const uint64_t run = ki >> 3;                 // (scene, cell, group)
-    const uint64_t cellk = ki >> (3 + group_bits);  // (scene, cell)
+    const uint64_t run = ki >> 3;     // (scene, cell, group)
+    const uint64_t cellk = ki >> cs;  // (scene, cell)
     const unsigned fa = (unsigned)(ki & 7);
-    int64_t j;
-    if (ends) {
-        j = i - lane + (__ffs(ends) - 1) + 1;
+    int64_t j0, j1;
+    if (run_ends) {
+        j0 = i - lane + __ffs(run_ends);
     } else {
-        j = i - lane + 32;
-        while (j < m && (keys[j] >> 3) == run) j++;
+        j0 = i - lane + 32;
+        while (j0 < m && (keys[j0] >> 3) == run) j0++;
     }
+    if (cell_ends) {
+        j1 = i - lane + __ffs(cell_ends);
+    } else {
+        j1 = j0 > i - lane + 32 ? j0 : i - lane + 32;
+        while (j1 < m && (keys[j1] >> cs) == cellk) j1++;
+    }
+    if (j0 >= j1) return;
     const uint32_t a = vals[i];
     const int ta = a >> 30, ia = a & 0x3fffffff;
-    for (; j < m; j++) {
-        const uint64_t kj = keys[j];
-        if ((kj >> (3 + group_bits)) != cellk) break;
-        if ((fa | (unsigned)(kj & 7)) != 7) continue;
-        const uint32_t b = vals[j];
-        const int tb = b >> 30;
-        if (!pair_types(kind, ta, tb)) continue;
-        test_pair(E, f32, ta, ia, tb, b & 0x3fffffff, o);
+    float fa_box[6];
+    {
+        const float* p = f32 + 6 * E.index(ta, ia);
+#pragma unroll
+        for (int k = 0; k < 6; k++) fa_box[k] = p[k];
+    }
+    // the later groups' items of the cell, four at a time: their keys and
+    // values, then the float boxes of those that pair, then the tests
+    constexpr int kU = 4;
+    for (int64_t j = j0; j < j1; j += kU) {
+        uint64_t kk[kU];
+        uint32_t bb[kU];
+        bool want[kU];
+#pragma unroll
+        for (int u = 0; u < kU; u++) {
+            const bool in = j + u < j1;
+            kk[u] = in ? keys[j + u] : 0;
+            bb[u] = in ? vals[j + u] : 0;
+            want[u] = in && (fa | (unsigned)(kk[u] & 7)) == 7 && pair_types(kind, ta, (int)(bb[u] >> 30));
+        }
+        float fb[kU][6];
+#pragma unroll
+        for (int u = 0; u < kU; u++) {
+            if (!want[u]) continue;
+            const float* p = f32 + 6 * E.index((int)(bb[u] >> 30), (int)(bb[u] & 0x3fffffff));
+#pragma unroll
+            for (int k = 0; k < 6; k++) fb[u][k] = p[k];
+        }
+#pragma unroll
+        for (int u = 0; u < kU; u++)
+            if (want[u] && !fboxes_disjoint(fa_box, fb[u]))
+                exact_pair(E, ta, ia, (int)(bb[u] >> 30), (int)(bb[u] & 0x3fffffff), o);
     }
 }
 
@@ -1045,8 +1093,8 @@ int detect_pairs(Ctx& c, const double* x0, const double* x1, bool continuous, do
         RIGC_COUNT_LAUNCH();
         k_scene_box<<<1, 256, 0, st>>>(c.body_box.as<double>(), c.body_in.as<int>(), s.nb, d_domain);
         RIGC_COUNT_LAUNCH();
-        k_bp_frames<<<grid_for((int64_t)s.nb * kBPTableNodes, 128), 128, 0, st>>>(
-            x0, x1, c.body_in.as<int>(), s.nb, table);
+        k_bp_frames<<<grid_for((int64_t)s.nb * kRotTableSlots, 128), 128, 0, st>>>(
+            x0, x1, c.body_in.as<int>(), s.nb, kDefaultToiTol, table);
         RIGC_CUDA(cudaMemsetAsync(c.bp_deeper.ptr, 0, (size_t)s.nb * sizeof(int), st));
         RIGC_COUNT_LAUNCH();
         k_vertex_boxes_half<<<grid_for(s.nv, 128), 128, 0, st>>>(
@@ -1202,6 +1250,7 @@ int detect_pairs(Ctx& c, const double* x0, const double* x1, bool continuous, do
     if (continuous && kind == kPairsEEFV) {
         c.bp_table.x0 = x0;
         c.bp_table.x1 = x1;
+        c.bp_table.toi_tol = kDefaultToiTol;
         c.bp_table.valid = true;
     }
     return RIGC_OK;

@@ -253,6 +253,21 @@ constexpr int kTableSlots = kTableNodes + 1;            // + [0, toi_tol]
 constexpr int kTableEntry = 24;                         // R (9 intervals) + p (3)
 static_assert(kTableSlots == kRotTableSlots && kTableEntry == kRotTableEntry, "table layout");
 
+// a body's trajectory (x0, I(x1) - I(x0)) and fixed flag
+__device__ __forceinline__ void store_traj(const BodyTraj& T, int b, double* __restrict__ traj,
+                                           int* __restrict__ bfixed)
+{
+    double* e = traj + (size_t)b * kTrajDoubles;
+    bool fixed = true;
+    for (int k = 0; k < 6; k++) {
+        e[k] = T.x0[k];
+        e[6 + 2 * k] = T.dx[k].lo;
+        e[7 + 2 * k] = T.dx[k].hi;
+        fixed = fixed && is_zero(T.dx[k].lo) && is_zero(T.dx[k].hi);
+    }
+    bfixed[b] = fixed ? 1 : 0;
+}
+
 // tree_ready: the slots of the tree nodes already hold these poses' frames
 // for every body a candidate can have (the continuous broad phase computed
 // them); only [0, toi_tol], the trajectories and the fixed flags are left
@@ -274,17 +289,19 @@ __global__ void k_rot_table(const double* __restrict__ x0, const double* __restr
         body_at(T, t, R, p);
         frame_store(table + (size_t)i * kTableEntry, R, p);
     }
-    if (node == 0) {
-        double* e = traj + (size_t)b * kTrajDoubles;
-        bool fixed = true;
-        for (int k = 0; k < 6; k++) {
-            e[k] = T.x0[k];
-            e[6 + 2 * k] = T.dx[k].lo;
-            e[7 + 2 * k] = T.dx[k].hi;
-            fixed = fixed && is_zero(T.dx[k].lo) && is_zero(T.dx[k].hi);
-        }
-        bfixed[b] = fixed ? 1 : 0;
-    }
+    if (node == 0) store_traj(T, b, traj, bfixed);
+}
+
+// every slot, [0, toi_tol] included, already holds these poses' frames:
+// the trajectories and fixed flags alone, one thread per body
+__global__ void k_traj_table(const double* __restrict__ x0, const double* __restrict__ x1, int nb,
+                             double* __restrict__ traj, int* __restrict__ bfixed)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    BodyTraj T;
+    load_traj(x0, x1, b, T);
+    store_traj(T, b, traj, bfixed);
 }
 
 
@@ -1622,9 +1639,13 @@ int run_ccd(Ctx& c, const double* x0, const double* x1, double toi_tol, int flag
         // every body a candidate can have, for these poses
         const int tree_ready = c.bp_table.valid && c.bp_table.x0 == x0 && c.bp_table.x1 == x1;
         RIGC_COUNT_LAUNCH();
-        k_rot_table<<<grid_for((int64_t)c.s.nb * kTableSlots, 128), 128, 0, st>>>(
-            x0, x1, c.s.nb, toi_tol, const_cast<double*>(a.table), const_cast<double*>(a.traj),
-            const_cast<int*>(a.bfixed), tree_ready);
+        if (tree_ready && c.bp_table.toi_tol == toi_tol)
+            k_traj_table<<<grid_for(c.s.nb, 128), 128, 0, st>>>(
+                x0, x1, c.s.nb, const_cast<double*>(a.traj), const_cast<int*>(a.bfixed));
+        else
+            k_rot_table<<<grid_for((int64_t)c.s.nb * kTableSlots, 128), 128, 0, st>>>(
+                x0, x1, c.s.nb, toi_tol, const_cast<double*>(a.table), const_cast<double*>(a.traj),
+                const_cast<int*>(a.bfixed), tree_ready);
         // frame cache: 1024 slots per body (or the tuned count), at least
         // 2^16, at most 2^22
         const size_t per_body = c.tune.cache_slots_per_body > 0 ? c.tune.cache_slots_per_body : 1024;

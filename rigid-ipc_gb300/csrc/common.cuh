@@ -19,6 +19,8 @@ constexpr int kNumSMs = 152;  // GB300: 2 dies x 76 SMs
 // the dyadic time nodes [k 2^-d, (k + 1) 2^-d] of depth d < 7 (slot
 // 2^d - 1 + k) and over [0, toi_tol] (slot 127)
 constexpr int kRotTableSlots = 128;
+// the rigid CCD's time tolerance of the line searches (the reference's 1e-4)
+constexpr double kDefaultToiTol = 1e-4;
 constexpr int kRotTableEntry = 24;
 
 // ---------------------------------------------------------------------------
@@ -167,11 +169,13 @@ struct Ctx {
     DevBuf bp_misc, bp_deeper, bp_sig, bp_ec0, bp_eext, bp_f32, bp_cnt;
     int64_t bp_pair_hint[2] = { 0, 0 };  // largest EE / FV pair counts seen
     // The continuous broad phase leaves the interval frames of the included
-    // bodies over the dyadic time nodes of depth < 7 in rot_table (the CCD's
-    // layout); the CCD right after it on the same poses reuses them.
+    // bodies over the dyadic time nodes of depth < 7 and over [0, toi_tol]
+    // in rot_table (the CCD's layout); the CCD right after it on the same
+    // poses reuses them.
     struct {
         const double* x0 = nullptr;
         const double* x1 = nullptr;
+        double toi_tol = 0;
         bool valid = false;
     } bp_table;
     // rigc_min_distance / rigc_detect_intersections: world vertices, their

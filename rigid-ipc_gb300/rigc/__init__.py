@@ -153,6 +153,19 @@ class Context:
         fv = self.copy_out(out.fv, (out.num_fv, 2), np.int32)
         return ee, fv
 
+    def count_collision_candidates_rigid(self, x0, x1=None, continuous=True, inflation=0.0):
+        """The hash-grid broad phase with the candidates left on the device
+        (the next CCD or constraint set takes them); returns (num_ee, num_fv)."""
+        x0d = self.device(x0)
+        x1d = self.device(x0 if x1 is None else x1)
+        out = L.Candidates()
+        L.check(self.lib.rigc_detect_candidates(self.h, C.c_void_p(x0d.data_ptr()),
+                                                C.c_void_p(x1d.data_ptr()), int(continuous),
+                                                inflation, C.byref(out)),
+                "rigc_detect_candidates")
+        self._last_counts = (out.num_ee, out.num_fv)
+        return out.num_ee, out.num_fv
+
     def scene_tois(self):
         """Per-scene earliest time of impact of the last CCD call."""
         out = np.empty(self.num_scenes)
