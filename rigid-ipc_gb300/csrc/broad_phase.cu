@@ -127,6 +127,8 @@ __global__ void k_close_bodies(const double* __restrict__ box, const int* __rest
 __global__ void k_scene_box(const double* __restrict__ box, const int* __restrict__ body_in, int nb,
                             double* __restrict__ out)
 {
+    // per thread over a stride of bodies, then a tree over the block (the
+    // minimum and maximum are exact, so the order does not matter)
     __shared__ double sh[6][256];
     double lo[3] = { INFINITY, INFINITY, INFINITY }, hi[3] = { -INFINITY, -INFINITY, -INFINITY };
     for (int b = threadIdx.x; b < nb; b += blockDim.x)
@@ -140,12 +142,19 @@ __global__ void k_scene_box(const double* __restrict__ box, const int* __restric
         sh[3 + j][threadIdx.x] = hi[j];
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int t = 1; t < blockDim.x; t++)
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w)
             for (int j = 0; j < 3; j++) {
-                lo[j] = smin(lo[j], sh[j][t]);
-                hi[j] = smax(hi[j], sh[3 + j][t]);
+                sh[j][threadIdx.x] = smin(sh[j][threadIdx.x], sh[j][threadIdx.x + w]);
+                sh[3 + j][threadIdx.x] = smax(sh[3 + j][threadIdx.x], sh[3 + j][threadIdx.x + w]);
             }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        for (int j = 0; j < 3; j++) {
+            lo[j] = sh[j][0];
+            hi[j] = sh[3 + j][0];
+        }
         double d0 = RSUB(hi[0], lo[0]), d1 = RSUB(hi[1], lo[1]), d2 = RSUB(hi[2], lo[2]);
         double diag = __dsqrt_rn(RADD(RADD(RMUL(d0, d0), RMUL(d1, d1)), RMUL(d2, d2)));
         for (int j = 0; j < 3; j++) {
@@ -832,13 +841,21 @@ struct PairOut {
     unsigned long long* n_fv;
 };
 
+// one slot per pair; the lanes that push together take their slots of a
+// stream with one atomic
 __device__ __forceinline__ void push_pair(const PairOut& o, bool is_ee, unsigned long long key)
 {
+    const unsigned act = __activemask();
+    const unsigned peers = __match_any_sync(act, is_ee ? 1u : 0u);
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(peers) - 1;
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(is_ee ? o.n_ee : o.n_fv, (unsigned long long)__popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    const unsigned long long k = base + (unsigned long long)__popc(peers & ((1u << lane) - 1u));
     if (is_ee) {
-        unsigned long long k = atomicAdd(o.n_ee, 1ull);
         if (k < o.cap_ee) o.ee[k] = key;
     } else {
-        unsigned long long k = atomicAdd(o.n_fv, 1ull);
         if (k < o.cap_fv) o.fv[k] = key;
     }
 }
@@ -1013,6 +1030,152 @@ __global__ void k_decode_pairs(const unsigned long long* __restrict__ keys, int6
     const unsigned long long k = keys[i] & ((1ull << tbit) - 1);
     if (i < nee) out_ee[i] = make_int2((int)(k / ee_stride), (int)(k % ee_stride));
     else out_fv[i - nee] = make_int2((int)(k / fv_stride), (int)(k % fv_stride));
+}
+
+// Canonical order of the two pair streams by buckets: a pair's bucket is its
+// first element (EE: the lower edge, bucket e; FV / EF: the face, bucket
+// ne + f), the buckets in order hold the pairs in the order of their keys
+// once each bucket is sorted by the second element.  k_bucket_count counts,
+// k_bucket_fill places the second elements at the scanned bucket offsets
+// (in any order within a bucket), k_bucket_pairs sorts each bucket (a few
+// pairs: insertion) and writes the (first, second) pairs, EE then FV.
+__device__ __forceinline__ void pair_bucket(unsigned long long key, bool ee, unsigned long long ee_stride,
+                                            unsigned long long fv_stride, int ne, int& bucket, int& second)
+{
+    const unsigned long long stride = ee ? ee_stride : fv_stride;
+    const unsigned long long first = key / stride;
+    second = (int)(key - first * stride);
+    bucket = ee ? (int)first : ne + (int)first;
+}
+
+__global__ void k_bucket_count(const unsigned long long* __restrict__ kee, int64_t nee,
+                               const unsigned long long* __restrict__ kfv, int64_t nfv,
+                               unsigned long long ee_stride, unsigned long long fv_stride, int ne,
+                               int32_t* __restrict__ count)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nee + nfv) return;
+    const bool ee = i < nee;
+    int b, sec;
+    pair_bucket(ee ? kee[i] : kfv[i - nee], ee, ee_stride, fv_stride, ne, b, sec);
+    atomicAdd(count + b, 1);
+}
+
+__global__ void k_bucket_fill(const unsigned long long* __restrict__ kee, int64_t nee,
+                              const unsigned long long* __restrict__ kfv, int64_t nfv,
+                              unsigned long long ee_stride, unsigned long long fv_stride, int ne,
+                              const int32_t* __restrict__ offset, int32_t* __restrict__ fill,
+                              int32_t* __restrict__ second)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nee + nfv) return;
+    const bool ee = i < nee;
+    int b, sec;
+    pair_bucket(ee ? kee[i] : kfv[i - nee], ee, ee_stride, fv_stride, ne, b, sec);
+    second[offset[b] + atomicAdd(fill + b, 1)] = sec;
+}
+
+// buckets of up to kSmallBucket pairs: sorted here; larger ones (a large
+// element's bucket: the floor's faces) are listed for k_bucket_large
+constexpr int kSmallBucket = 32;
+
+__device__ __forceinline__ void write_pair(int b, int ne, int64_t nee, int64_t pos, int sec,
+                                           int2* __restrict__ out_ee, int2* __restrict__ out_fv)
+{
+    if (b < ne) out_ee[pos] = make_int2(b, sec);
+    else out_fv[pos - nee] = make_int2(b - ne, sec);
+}
+
+__global__ void k_bucket_pairs(const int32_t* __restrict__ count, const int32_t* __restrict__ offset,
+                               int nbuckets, int ne, int64_t nee, int32_t* __restrict__ second,
+                               int2* __restrict__ out_ee, int2* __restrict__ out_fv,
+                               int32_t* __restrict__ large, int32_t* __restrict__ nlarge)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nbuckets) return;
+    const int n = count[b];
+    if (n == 0) return;
+    if (n > kSmallBucket) {
+        large[atomicAdd(nlarge, 1)] = b;
+        return;
+    }
+    int32_t* v = second + offset[b];
+    for (int k = 1; k < n; k++) {
+        const int x = v[k];
+        int j = k - 1;
+        while (j >= 0 && v[j] > x) {
+            v[j + 1] = v[j];
+            j--;
+        }
+        v[j + 1] = x;
+    }
+    const int64_t o = offset[b];
+    for (int k = 0; k < n; k++) write_pair(b, ne, nee, o + k, v[k], out_ee, out_fv);
+}
+
+// One block per listed bucket (grid-stride over the list): its second
+// elements (distinct: each pair is found once) as bits of a bitmap over
+// their range (EE: edges; FV: vertices; EF: edges), then written in the
+// order of the bits.  bitmap: words_per_block words per block.
+__global__ void __launch_bounds__(1024) k_bucket_large(
+    const int32_t* __restrict__ large, const int32_t* __restrict__ nlarge,
+    const int32_t* __restrict__ count, const int32_t* __restrict__ offset,
+    const int32_t* __restrict__ second, int ne, int64_t nee, int fv_range,
+    unsigned* __restrict__ bitmap_all, int64_t words_per_block,
+    int2* __restrict__ out_ee, int2* __restrict__ out_fv)
+{
+    __shared__ int32_t warp_sum[32];
+    __shared__ int32_t carry;
+    unsigned* bitmap = bitmap_all + (int64_t)blockIdx.x * words_per_block;
+    const int nl = *nlarge;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (int li = blockIdx.x; li < nl; li += gridDim.x) {
+        const int b = large[li];
+        const int n = count[b];
+        const int64_t o = offset[b];
+        const int range = b < ne ? ne : fv_range;
+        const int64_t words = ((int64_t)range + 31) / 32;
+        for (int64_t w = threadIdx.x; w < words; w += blockDim.x) bitmap[w] = 0u;
+        __syncthreads();
+        for (int k = threadIdx.x; k < n; k += blockDim.x) {
+            const int x = second[o + k];
+            atomicOr(bitmap + (x >> 5), 1u << (x & 31));
+        }
+        if (threadIdx.x == 0) carry = 0;
+        __syncthreads();
+        // the set bits in order: a block scan of the words' bit counts per
+        // chunk of blockDim words
+        for (int64_t w0 = 0; w0 < words; w0 += blockDim.x) {
+            const int64_t w = w0 + threadIdx.x;
+            const unsigned bits = w < words ? bitmap[w] : 0u;
+            const int c = __popc(bits);
+            int incl = c;
+            for (int d = 1; d < 32; d <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, incl, d);
+                if (lane >= d) incl += y;
+            }
+            if (lane == 31) warp_sum[warp] = incl;
+            __syncthreads();
+            if (warp == 0) {
+                int t = lane < nwarps ? warp_sum[lane] : 0;
+                for (int d = 1; d < 32; d <<= 1) {
+                    const int y = __shfl_up_sync(0xffffffffu, t, d);
+                    if (lane >= d) t += y;
+                }
+                if (lane < nwarps) warp_sum[lane] = t;
+            }
+            __syncthreads();
+            int pos = carry + (warp ? warp_sum[warp - 1] : 0) + incl - c;
+            for (unsigned r = bits; r; r &= r - 1) {
+                const int x = (int)(w * 32) + __ffs(r) - 1;
+                write_pair(b, ne, nee, o + pos, x, out_ee, out_fv);
+                pos++;
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) carry += warp_sum[nwarps - 1];
+            __syncthreads();
+        }
+    }
 }
 
 __global__ void k_iota(uint32_t* __restrict__ v, int64_t n)
@@ -1231,10 +1394,44 @@ int detect_pairs(Ctx& c, const double* x0, const double* x1, bool continuous, do
     const int tbit = std::max(bits_for((uint64_t)s.ne * (uint64_t)s.ne),
                               bits_for((uint64_t)s.nf * fv_stride));
     const int64_t np = nee + nfv;
-    RIGC_TRY(c.pair_key.reserve((size_t)np * 8 + 8));
-    RIGC_TRY(S[0].reserve((size_t)np * 4 + 8));
-    RIGC_TRY(S[1].reserve((size_t)np * 4 + 8));
-    if (np > 0) {
+    const int64_t nbuckets = (int64_t)s.ne + s.nf;
+    if (np > 0 && np < (int64_t)INT32_MAX && nbuckets < (int64_t)INT32_MAX) {
+        // by buckets of the first element
+        RIGC_TRY(S[0].reserve((size_t)2 * nbuckets * sizeof(int32_t)));
+        RIGC_TRY(S[1].reserve((size_t)(nbuckets + np) * sizeof(int32_t)));
+        int32_t* count = S[0].as<int32_t>();
+        int32_t* fill = count + nbuckets;
+        int32_t* offset = S[1].as<int32_t>();
+        int32_t* second = offset + nbuckets;
+        RIGC_CUDA(cudaMemsetAsync(count, 0, (size_t)2 * nbuckets * sizeof(int32_t), st));
+        RIGC_COUNT_LAUNCH();
+        k_bucket_count<<<grid_for(np, 256), 256, 0, st>>>(kee, nee, kfv, nfv, (unsigned long long)s.ne,
+                                                           fv_stride, s.ne, count);
+        RIGC_TRY(exclusive_scan_i32(count, offset, nbuckets, d_count + 2, S[7], st));
+        RIGC_COUNT_LAUNCH();
+        k_bucket_fill<<<grid_for(np, 256), 256, 0, st>>>(kee, nee, kfv, nfv, (unsigned long long)s.ne,
+                                                          fv_stride, s.ne, offset, fill, second);
+        RIGC_TRY(S[2].reserve((size_t)nbuckets * sizeof(int32_t)));
+        int32_t* nlarge = d_count + 3;
+        RIGC_CUDA(cudaMemsetAsync(nlarge, 0, sizeof(int32_t), st));
+        RIGC_COUNT_LAUNCH();
+        k_bucket_pairs<<<grid_for(nbuckets, 256), 256, 0, st>>>(count, offset, (int)nbuckets, s.ne, nee,
+                                                                 second, out.ee.as<int2>(),
+                                                                 out.fv.as<int2>(), S[2].as<int32_t>(),
+                                                                 nlarge);
+        // the large buckets, a block each (at most kLargeBlocks at a time)
+        constexpr int kLargeBlocks = 32;
+        const int fv_range = kind == kPairsEF ? s.ne : s.nv;
+        const int64_t words = ((int64_t)std::max(s.ne, fv_range) + 31) / 32;
+        RIGC_TRY(S[3].reserve((size_t)kLargeBlocks * words * sizeof(unsigned)));
+        RIGC_COUNT_LAUNCH();
+        k_bucket_large<<<kLargeBlocks, 1024, 0, st>>>(S[2].as<int32_t>(), nlarge, count, offset, second, s.ne,
+                                                     nee, fv_range, S[3].as<unsigned>(), words,
+                                                     out.ee.as<int2>(), out.fv.as<int2>());
+    } else if (np > 0) {
+        RIGC_TRY(c.pair_key.reserve((size_t)np * 8 + 8));
+        RIGC_TRY(S[0].reserve((size_t)np * 4 + 8));
+        RIGC_TRY(S[1].reserve((size_t)np * 4 + 8));
         RIGC_COUNT_LAUNCH();
         k_pack_pairs<<<grid_for(np, 256), 256, 0, st>>>(kee, nee, kfv, nfv, tbit, c.pair_key.as<unsigned long long>(),
                                                         S[0].as<uint32_t>());
