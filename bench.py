@@ -39,19 +39,24 @@ METRIC = "candidate pairs/s (CCD+barrier grad/Hess)"
 UNIT = "pairs/s"
 CCD_BYTES_PER_PAIR = 304        # ids + 4 rest vertices + 4 poses + toi
 # DRAM bytes (read + write) per continuous candidate of one CCD call (all its
-# launches), from ncu captures of the 200-icosphere pile (132,242
-# candidates): k_ccd 56.95 MB read + 311.51 MB written over two launches
-# (per-lane candidate state spilling from L1, the frame cache);
-# k_ccd_group<32, 4> (one search per warp fitted to 4 blocks per SM: 128
-# registers, one interval bound per lane) 27.94 MB + 45.73 MB over three,
-# most of the writes its spills.  The traffic of a full call is this times
-# its candidates.  FP64 figures of the same captures: pipe active (fraction
-# of peak) and lane-level GFLOP/s (dadd + dmul + 2 dfma over the launch).
+# search launches and the splits of their deferred pieces), from ncu captures
+# of the 200-icosphere pile (132,242 candidates): k_ccd 56.95 MB read +
+# 311.51 MB written over two launches (per-lane candidate state spilling
+# from L1, the frame cache; it searches without time windows);
+# k_ccd_group<32, 4> (one search per warp fitted to 4 blocks per SM)
+# 119.20 MB + 40.87 MB and k_ccd_group<16, 4> (one search per half-warp, the
+# same fit) 134.27 MB + 32.55 MB over three launches with time windows from
+# 2^-6, most of it the deferred pieces written and read back and the spills.
+# The traffic of a full call is this times its candidates.  FP64 figures of
+# the first launch of the same calls: pipe active (fraction of peak) and
+# lane-level GFLOP/s (dadd + dmul + 2 dfma over the launch).
 K_CCD_DRAM_BYTES_PER_CANDIDATE = {
     "k_ccd": (42209536 + 14743808 + 310226176 + 1279232) / 132242,
-    "k_ccd_group<32, 4>": (23012864 + 3960320 + 968448 + 45619968 + 103680 + 5632) / 132242}
+    "k_ccd_group<32, 4>": (119197184 + 40870912) / 132242,
+    "k_ccd_group<16, 4>": (134271488 + 32547072) / 132242}
 K_CCD_FP64 = {"k_ccd": {"pipe_active": 0.233, "lane_gflops": 53.0},
-              "k_ccd_group<32, 4>": {"pipe_active": 0.384, "lane_gflops": 99.5}}
+              "k_ccd_group<32, 4>": {"pipe_active": 0.416, "lane_gflops": 108.6},
+              "k_ccd_group<16, 4>": {"pipe_active": 0.343, "lane_gflops": 73.5}}
 BARRIER_BYTES_PER_CONSTRAINT = 1456
 # the CCD kernel of each search mode (rigc_set_tune's ccd_warp)
 CCD_KERNELS = {0: "k_ccd", 1: "k_ccd_group<32, 1>", 2: "k_ccd_group<32, 4>",

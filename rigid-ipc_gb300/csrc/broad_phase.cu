@@ -1099,9 +1099,11 @@ __global__ void k_bucket_pairs(const int32_t* __restrict__ count, const int32_t*
         large[atomicAdd(nlarge, 1)] = b;
         return;
     }
-    int32_t* v = second + offset[b];
-    for (int k = 1; k < n; k++) {
-        const int x = v[k];
+    // sorted in a thread-local copy (L1-resident), then written
+    const int64_t o = offset[b];
+    int v[kSmallBucket];
+    for (int k = 0; k < n; k++) {
+        const int x = second[o + k];
         int j = k - 1;
         while (j >= 0 && v[j] > x) {
             v[j + 1] = v[j];
@@ -1109,7 +1111,6 @@ __global__ void k_bucket_pairs(const int32_t* __restrict__ count, const int32_t*
         }
         v[j + 1] = x;
     }
-    const int64_t o = offset[b];
     for (int k = 0; k < n; k++) write_pair(b, ne, nee, o + k, v[k], out_ee, out_fv);
 }
 
