@@ -471,7 +471,7 @@ struct Grid {
     int key_bits;               // bits of the largest (scene, cell) key
 };
 
-constexpr int kStatBlocks = 256;
+constexpr int kStatBlocks = 1024;
 constexpr int kStatThreads = 256;
 constexpr long long kMaxAxisCells = 1ll << 21;
 // cell-filter slot states; a group rank (>= 0) otherwise

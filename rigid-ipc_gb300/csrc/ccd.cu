@@ -707,6 +707,93 @@ __device__ __forceinline__ Node seed_node(int d, int64_t j, const double* tol, u
     return c;
 }
 
+// The rare paths of the search loops (k_ccd, k_ccd_group), kept out of
+// their bodies so that the loop run box after box stays short.
+// Hand-off: the pending boxes of the group's search (and its current box)
+// become pieces of the next launch; without room for all of them the slots
+// taken are voided and the search goes on (no further hand-offs).
+template <int W>
+static __device__ __noinline__ void hand_off_pending(const CCDArgs& a, const Node& cn, u128 mt, u128 ma,
+                                                     u128& pend_hi, bool& has_cn, bool& hand_ok,
+                                                     long long cur, double earliest,
+                                                     unsigned long long boxes, int gl, unsigned gmask)
+{
+    const int k = popc128(pend_hi) + (has_cn ? 1 : 0);
+    unsigned long long s = 0;
+    if (gl == 0) s = atomicAdd(a.n_out, (unsigned long long)k);
+    s = __shfl_sync(gmask, s, 0, W);
+    if (s + k <= a.out_cap) {
+        if (gl == 0) {
+            Piece pc;
+            pc.cand = cur;
+            pc.earliest = earliest;
+            pc.boxes = boxes;
+            unsigned long long o = s;
+            for (u128 r = pend_hi; r != 0; r &= r - 1) {
+                const Node g = pending_node(cn, mt, ma, lsb128(r));
+                for (int d = 0; d < 3; d++) {
+                    pc.ix[d] = g.ix[d];
+                    pc.lv[d] = g.lv[d];
+                }
+                pc.depth = g.depth;
+                a.pieces_out[o++] = pc;
+            }
+            if (has_cn) {
+                for (int d = 0; d < 3; d++) {
+                    pc.ix[d] = cn.ix[d];
+                    pc.lv[d] = cn.lv[d];
+                }
+                pc.depth = cn.depth;
+                a.pieces_out[o++] = pc;
+            }
+        }
+        pend_hi = 0;
+        has_cn = false;
+    } else {
+        if (gl == 0)
+            for (unsigned long long t = s; t < s + k && t < a.out_cap; t++) a.pieces_out[t].cand = -1;
+        hand_ok = false;
+    }
+}
+
+// A box after the launch's time window becomes a piece of the next launch;
+// false when there is no room for it (it is searched now).
+template <int W>
+static __device__ __noinline__ bool defer_node(const CCDArgs& a, const Node& cn, long long cur,
+                                               double earliest, unsigned long long boxes, int gl,
+                                               unsigned gmask)
+{
+    unsigned long long s = 0;
+    if (gl == 0) s = atomicAdd(a.n_out, 1ull);
+    s = __shfl_sync(gmask, s, 0, W);
+    if (s >= a.out_cap) return false;
+    if (gl == 0) {
+        Piece pc;
+        pc.cand = cur;
+        pc.earliest = earliest;
+        pc.boxes = boxes;
+        for (int d = 0; d < 3; d++) {
+            pc.ix[d] = cn.ix[d];
+            pc.lv[d] = cn.lv[d];
+        }
+        pc.depth = cn.depth;
+        a.pieces_out[s] = pc;
+    }
+    return true;
+}
+
+// the smallest t.lo of the current box and the pending boxes
+static __device__ __noinline__ double earliest_unexplored(const Node& cn, u128 mt, u128 ma, u128 pend_hi,
+                                                          double t0)
+{
+    double m = t0;
+    for (u128 r = pend_hi; r != 0; r &= r - 1) {
+        const Node g = pending_node(cn, mt, ma, lsb128(r));
+        m = smin(m, dyadic(g.ix[0], g.lv[0]));
+    }
+    return m;
+}
+
 // Persistent kernel: each lane takes the next unprocessed candidate from a
 // global counter whenever its search runs out of boxes.  Every iteration each
 // lane pops boxes until one survives the cheap tests (or takes a new
@@ -938,12 +1025,7 @@ k_ccd(CCDArgs a)
         if (!have) continue;
         if (cbase + cboxes >= (unsigned long long)a.max_boxes) {
             // budget exhausted: the earliest unexplored t.lo is conservative
-            double m = x.t0;
-            for (u128 r = pend_hi; r != 0; r &= r - 1) {
-                const Node g = pending_node(cn, mt, ma, lsb128(r));
-                m = smin(m, dyadic(g.ix[0], g.lv[0]));
-            }
-            earliest = smin(earliest, m);
+            earliest = smin(earliest, earliest_unexplored(cn, mt, ma, pend_hi, x.t0));
             found = true;
             status = RIGC_ERR_ITER_LIMIT;
             pend_hi = 0;
@@ -1148,44 +1230,9 @@ k_ccd_group(CCDArgs a)
     while (true) {
         // hand the pending boxes of a long piece to the next launch once
         // the work list has run dry
-        if (tail && hand_ok && cboxes >= a.hand_off && (pend_hi != 0 || has_cn)) {
-            const int k = popc128(pend_hi) + (has_cn ? 1 : 0);
-            unsigned long long s = 0;
-            if (gl == 0) s = atomicAdd(a.n_out, (unsigned long long)k);
-            s = __shfl_sync(gmask, s, 0, W);
-            if (s + k <= a.out_cap) {
-                if (gl == 0) {
-                    Piece pc;
-                    pc.cand = cur;
-                    pc.earliest = earliest;
-                    pc.boxes = cbase + cboxes;
-                    unsigned long long o = s;
-                    for (u128 r = pend_hi; r != 0; r &= r - 1) {
-                        const Node g = pending_node(cn, mt, ma, lsb128(r));
-                        for (int d = 0; d < 3; d++) {
-                            pc.ix[d] = g.ix[d];
-                            pc.lv[d] = g.lv[d];
-                        }
-                        pc.depth = g.depth;
-                        a.pieces_out[o++] = pc;
-                    }
-                    if (has_cn) {
-                        for (int d = 0; d < 3; d++) {
-                            pc.ix[d] = cn.ix[d];
-                            pc.lv[d] = cn.lv[d];
-                        }
-                        pc.depth = cn.depth;
-                        a.pieces_out[o++] = pc;
-                    }
-                }
-                pend_hi = 0;
-                has_cn = false;
-            } else {
-                if (gl == 0)
-                    for (unsigned long long t = s; t < s + k && t < a.out_cap; t++) a.pieces_out[t].cand = -1;
-                hand_ok = false;
-            }
-        }
+        if (tail && hand_ok && cboxes >= a.hand_off && (pend_hi != 0 || has_cn))
+            hand_off_pending<W>(a, cn, mt, ma, pend_hi, has_cn, hand_ok, cur, earliest, cbase + cboxes, gl,
+                                gmask);
         bool have = false;
         Box x;
         while (has_cn || pend_hi != 0) {
@@ -1213,28 +1260,9 @@ k_ccd_group(CCDArgs a)
                 double sl = add_dn(x.a0, x.b0), sh = add_up(x.a1, x.b1);
                 if (!(le_nn(sl, 1.0) && !is_neg(sh))) continue;
             }
-            if (x.t0 >= a.window) {
-                // after the window: a piece of the next launch (searched
-                // now when there is no room for it)
-                unsigned long long s = 0;
-                if (gl == 0) s = atomicAdd(a.n_out, 1ull);
-                s = __shfl_sync(gmask, s, 0, W);
-                if (s < a.out_cap) {
-                    if (gl == 0) {
-                        Piece pc;
-                        pc.cand = cur;
-                        pc.earliest = earliest;
-                        pc.boxes = cbase + cboxes;
-                        for (int d = 0; d < 3; d++) {
-                            pc.ix[d] = cn.ix[d];
-                            pc.lv[d] = cn.lv[d];
-                        }
-                        pc.depth = cn.depth;
-                        a.pieces_out[s] = pc;
-                    }
-                    continue;
-                }
-            }
+            // after the window: a piece of the next launch (searched now
+            // when there is no room for it)
+            if (x.t0 >= a.window && defer_node<W>(a, cn, cur, earliest, cbase + cboxes, gl, gmask)) continue;
             have = true;
             break;
         }
@@ -1312,12 +1340,7 @@ k_ccd_group(CCDArgs a)
         }
         if (cbase + cboxes >= (unsigned long long)a.max_boxes) {
             // budget exhausted: the earliest unexplored t.lo is conservative
-            double m = x.t0;
-            for (u128 r = pend_hi; r != 0; r &= r - 1) {
-                const Node g = pending_node(cn, mt, ma, lsb128(r));
-                m = smin(m, dyadic(g.ix[0], g.lv[0]));
-            }
-            earliest = smin(earliest, m);
+            earliest = smin(earliest, earliest_unexplored(cn, mt, ma, pend_hi, x.t0));
             found = true;
             status = RIGC_ERR_ITER_LIMIT;
             pend_hi = 0;
