@@ -451,6 +451,19 @@ int rigc_sim_get_state(rigc_ctx* ctx, double* poses, double* velocities,
 int rigc_sim_scene_params(rigc_ctx* ctx, const double* average_mass,
                           const double* bbox_diagonal);
 
+/* A kinematic body's schedule (RigidBody::kinematic_max_time and
+ * kinematic_poses, src/physics/rigid_body.hpp:260-261, read by
+ * src/io/read_rb_scene.cpp:94-101,233-245), set after rigc_sim_init: each
+ * time step drives the body to the next of the num_poses poses (host,
+ * num_poses x 6: position, rotation vector; init_augmented_lagrangian,
+ * src/problems/distance_barrier_rb_problem.cpp:204-226), then to x0 + h v
+ * once they are used up; once max_time has run out (a negative max_time is
+ * no limit) the body becomes static: every dof fixed, its velocity zero
+ * (step_kinematic_bodies, :237-251).  Plain contexts; RIGC_ERR_ARG for a
+ * body that is not kinematic. */
+int rigc_sim_set_kinematic(rigc_ctx* ctx, int32_t body, double max_time, int64_t num_poses,
+                           const double* poses);
+
 /* ---- autotuner (new).  Times the narrow phase's launch shapes on the
  * context's own workload -- k_ccd's resident blocks per SM, the CCD frame
  * cache's slots per body, the CCD searches per candidate,

@@ -3,6 +3,7 @@
 #include "interval.hpp"
 #include "oracle.hpp"
 
+#include <cmath>
 #include <cstring>
 #include <memory>
 
@@ -594,10 +595,18 @@ static SimParams unpack_params(const double* params)
 void orc_simulation_step_rec(
     void* p, const double* mass, const double* moment, double* pose, double* vel,
     double* Qdot, const int* fixed, const int* type, const double* params, double* kappa,
-    long long* stats, double* x_out, double* rec_out)
+    long long* stats, double* x_out, double* rec_out, const double* kin_target)
 {
     const Scene& s = static_cast<OwnedScene*>(p)->s;
     std::vector<BodyState> bodies = unpack_bodies(s.nb, mass, moment, pose, vel, Qdot, fixed, type);
+    // kin_target (optional, 6 per body): a kinematic body's target pose, NaN
+    // in its first component for none
+    if (kin_target)
+        for (int b = 0; b < s.nb; b++)
+            if (!std::isnan(kin_target[6 * b])) {
+                bodies[b].has_target = true;
+                for (int i = 0; i < 6; i++) bodies[b].kin_target[i] = kin_target[6 * b + i];
+            }
     SimParams sp = unpack_params(params);
     SimStats st;
     StepRecord rec;
@@ -628,7 +637,7 @@ void orc_simulation_step(
     long long* stats)
 {
     orc_simulation_step_rec(p, mass, moment, pose, vel, Qdot, fixed, type, params, kappa, stats,
-                            nullptr, nullptr);
+                            nullptr, nullptr, nullptr);
 }
 
 // adjoint of one step: the start-of-step state (pose, vel, Qdot), the step's

@@ -263,6 +263,11 @@ struct BodyState {
     double Qdot[9];        // row-major
     bool fixed[6];
     int type;
+    // kinematic bodies: the pose the step drives the body to (the front of
+    // its kinematic pose list, init_augmented_lagrangian); without one,
+    // x0 + h v
+    bool has_target = false;
+    double kin_target[6] = { 0, 0, 0, 0, 0, 0 };
 };
 double body_energy(
     const BodyState& b, const double* x6, const double gravity[3], double h,

@@ -70,7 +70,7 @@ def lib():
                                         _i, _d, C.c_longlong, _ll]
         L.orc_simulation_step.argtypes = [C.c_void_p, _d, _d, _d, _d, _d, _i, _i, _d, _d, _ll]
         L.orc_simulation_step_rec.argtypes = [C.c_void_p, _d, _d, _d, _d, _d, _i, _i, _d, _d, _ll,
-                                              _d, _d]
+                                              _d, _d, _d]
         L.orc_adjoint_step.argtypes = [C.c_void_p] + [_d] * 5 + [_i, _i] + [_d] * 9
         L.orc_adjoint_step.restype = C.c_int
         L.orc_barrier_term.argtypes = [C.c_void_p, _d, C.c_longlong, _i, _i, _i, _i, _d, _d,
@@ -467,6 +467,57 @@ class OracleSim:
         self.kappa = C.c_double(1.0)
         self.stats = np.zeros(4, np.int64)
         self.tape = []
+        # kinematic schedules (rigid_body.hpp:260-261): the time a kinematic
+        # body keeps moving (+inf: always) and the poses it is driven to, one
+        # per step
+        nb = len(self.mass)
+        self.kin_max_time = np.full(nb, np.inf)
+        self.kin_poses = [[] for _ in range(nb)]
+        for b, body in enumerate(sc.bodies):
+            if self.type[b] == 1:
+                self.set_kinematic(b, getattr(body, "kinematic_max_time", np.inf),
+                                   getattr(body, "kinematic_poses", ()))
+
+    def set_kinematic(self, body, max_time=np.inf, poses=()):
+        """A kinematic body's schedule: it becomes static once max_time has
+        run out (a negative max_time reads as +inf, as read_rb_scene does), and
+        each step drives it to the next pose of the list (x0 + h v once the
+        list is empty)."""
+        assert self.type[body] == 1, "only kinematic bodies have a schedule"
+        self.kin_max_time[body] = np.inf if max_time < 0 else float(max_time)
+        self.kin_poses[body] = [np.asarray(q, np.float64).reshape(6).copy() for q in poses]
+
+    def _kinematic_targets(self):
+        """init_augmented_lagrangian (distance_barrier_rb_problem.cpp:190-234):
+        kinematic bodies whose time has run out become static
+        (RigidBody::convert_to_static, rigid_body.hpp:186-193: every dof
+        fixed, velocity zero); the others' targets, NaN for none."""
+        nb = len(self.mass)
+        tgt = np.full(6 * nb, np.nan)
+        for b in range(nb):
+            if self.type[b] != 1:
+                continue
+            if self.kin_max_time[b] < 0:
+                self.type[b] = 0
+                self.fixed[6 * b:6 * b + 6] = 1
+                self.vel[6 * b:6 * b + 6] = 0.0
+            elif self.kin_poses[b]:
+                tgt[6 * b:6 * b + 6] = self.kin_poses[b][0]
+        return tgt
+
+    def _advance_kinematic(self):
+        """step_kinematic_bodies (distance_barrier_rb_problem.cpp:237-251)."""
+        for b in range(len(self.mass)):
+            if self.type[b] != 1:
+                continue
+            if self.kin_max_time[b] < 0:
+                self.type[b] = 0
+                self.fixed[6 * b:6 * b + 6] = 1
+                self.vel[6 * b:6 * b + 6] = 0.0
+            else:
+                self.kin_max_time[b] -= self.h
+                if self.kin_poses[b]:
+                    self.kin_poses[b].pop(0)
 
     def params(self):
         p = self.p
@@ -488,12 +539,14 @@ class OracleSim:
             rec = np.empty(2)
         else:
             x = rec = None
+        tgt = self._kinematic_targets()
         lib().orc_simulation_step_rec(self.o.h, _p(self.mass, _d), _p(self.moment, _d),
                                       _p(self.pose, _d), _p(self.vel, _d), _p(self.Qdot, _d),
                                       _p(self.fixed, _i), _p(self.type, _i), _p(prm, _d),
                                       C.byref(self.kappa), st.ctypes.data_as(_ll),
                                       None if x is None else _p(x, _d),
-                                      None if rec is None else _p(rec, _d))
+                                      None if rec is None else _p(rec, _d), _p(tgt, _d))
+        self._advance_kinematic()
         if record:
             self.tape.append((pre, x, rec))
         self.stats += st

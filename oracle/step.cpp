@@ -356,14 +356,17 @@ void simulation_step(const Scene& s, std::vector<BodyState>& bodies, const SimPa
     for (int b = 0; b < nb; b++)
         for (int k = 0; k < 6; k++) pr.x0[6 * b + k] = bodies[b].pose_t0[k];
     const double* x0 = pr.x0.data();
-    // init_augmented_lagrangian: kinematic targets x0 + h v
+    // init_augmented_lagrangian (distance_barrier_rb_problem.cpp:190-234):
+    // kinematic targets, the front of the body's pose list or x0 + h v
     pr.x_pred = pr.x0;
     pr.lam.assign(3 * (size_t)nb, 0.0);
     pr.Lam.assign(9 * (size_t)nb, 0.0);
     for (int b = 0; b < nb; b++)
         if (bodies[b].type == 1) {
             pr.has_kinematic = true;
-            for (int k = 0; k < 6; k++) pr.x_pred[6 * b + k] += p.h * bodies[b].vel_t0[k];
+            for (int k = 0; k < 6; k++)
+                pr.x_pred[6 * b + k] = bodies[b].has_target ? bodies[b].kin_target[k]
+                                                            : pr.x0[6 * b + k] + p.h * bodies[b].vel_t0[k];
         }
 
     // update_constraints: lagged friction at x0 with the current stiffness

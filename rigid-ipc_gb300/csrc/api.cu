@@ -32,6 +32,7 @@ int sim_step(Ctx& c, rigc_step_stats* stats);
 int sim_get_state(Ctx& c, double* poses, double* velocities, double* Qdot, double* kappa);
 int sim_rollout(Ctx& c, int steps, int every, rigc_step_stats* stats);
 int sim_scene_params(Ctx& c, const double* average_mass, const double* bbox_diagonal);
+int sim_set_kinematic(Ctx& c, int body, double max_time, int64_t num_poses, const double* poses);
 int autotune(Ctx& c, const double* x0, const double* x1, double dhat, double dmin,
              rigc_tune_report* rep);
 int sim_backward(Ctx& c, const double* dp, const double* dv, const double* dq, double* gp,
@@ -678,6 +679,13 @@ int rigc_sim_scene_params(rigc_ctx* ctx, const double* average_mass, const doubl
 {
     if (!ctx) return RIGC_ERR_ARG;
     return sim_scene_params(*ctx_of(ctx), average_mass, bbox_diagonal);
+}
+
+int rigc_sim_set_kinematic(rigc_ctx* ctx, int32_t body, double max_time, int64_t num_poses,
+                           const double* poses)
+{
+    if (!ctx) return RIGC_ERR_ARG;
+    return sim_set_kinematic(*ctx_of(ctx), body, max_time, num_poses, poses);
 }
 
 int rigc_sim_rollout(rigc_ctx* ctx, int32_t num_steps, int32_t checkpoint_every,

@@ -33,6 +33,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <array>
+#include <deque>
 #include <vector>
 
 #include "common.cuh"
@@ -614,12 +616,16 @@ __device__ __forceinline__ void al_J(const double* I, double J[3], double Js[3])
 }
 
 __global__ void k_al_init(int nb, const int* __restrict__ type, const double* __restrict__ x0,
-                          const double* __restrict__ v, double h, double* __restrict__ xpred,
-                          double* __restrict__ lam, double* __restrict__ Lam)
+                          const double* __restrict__ v, double h, const double* __restrict__ target,
+                          double* __restrict__ xpred, double* __restrict__ lam, double* __restrict__ Lam)
 {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= nb) return;
-    for (int k = 0; k < 6; k++) xpred[6 * b + k] = x0[6 * b + k] + (type[b] == RIGC_BODY_KINEMATIC ? h * v[6 * b + k] : 0.0);
+    // a kinematic body's target: its scheduled pose, else x0 + h v
+    const bool to_pose = type[b] == RIGC_BODY_KINEMATIC && target && !isnan(target[6 * b]);
+    for (int k = 0; k < 6; k++)
+        xpred[6 * b + k] = to_pose ? target[6 * b + k]
+                                   : x0[6 * b + k] + (type[b] == RIGC_BODY_KINEMATIC ? h * v[6 * b + k] : 0.0);
     for (int k = 0; k < 3; k++) lam[3 * b + k] = 0;
     for (int k = 0; k < 9; k++) Lam[9 * b + k] = 0;
 }
@@ -1121,6 +1127,12 @@ struct Sim {
     bool has_kinematic = false, al_sat_q = false, al_sat_Q = false;
     double al_kq = 1e3, al_kQ = 1e3;
     DevBuf al_xpred, al_lam, al_Lam, al_e;
+    // kinematic schedules (rigid_body.hpp:260-261): per body the time it
+    // keeps moving and the poses each step drives it to; the step's targets
+    // (6 per body, NaN first for none)
+    std::vector<double> kin_max_time;
+    std::vector<std::deque<std::array<double, 6>>> kin_poses;
+    DevBuf kin_target;
     // CUDA graphs of the CG solvers' iteration loops (single problem, per
     // scene): one while node whose body is one CG iteration ending in its
     // continuation test.  Rebuilt when an argument (a buffer address or a
@@ -1780,6 +1792,101 @@ int max_vertex_move_scenes(Ctx& c, Sim& S, const double* x, const double* x1, st
 // step bound, line search, convergence and stiffness updates; the kernels
 // run over all scenes at once.  Friction and the polish are not supported
 // here (RIGC_ERR_ARG).  Per-scene linear solves by block-Jacobi PCG.
+// The free dofs' compact indices from the bodies' fixed flags (the
+// reference's free_dof slicing) and the dense solver's buffers for them.
+int set_free_dofs(Ctx& c, Sim& S)
+{
+    const int nb = S.nb;
+    std::vector<int> fidx(6 * (size_t)nb, -1);
+    int nf = 0;
+    for (int b = 0; b < nb; b++)
+        for (int k = 0; k < 6; k++)
+            if (!((S.h_fixed[b] >> k) & 1)) fidx[6 * b + k] = nf++;
+    S.nfree = nf;
+    RIGC_TRY(S.free_idx.reserve(fidx.size() * sizeof(int) + 8));
+    RIGC_CUDA(cudaMemcpyAsync(S.free_idx.ptr, fidx.data(), fidx.size() * sizeof(int),
+                              cudaMemcpyHostToDevice, c.stream));
+    if (nf <= kDenseMax) {
+        RIGC_TRY(S.dense.reserve((size_t)nf * nf * sizeof(double) + 8));
+        RIGC_TRY(S.dense_b.reserve((size_t)nf * sizeof(double) + 8));
+        RIGC_TRY(S.dense_x.reserve((size_t)nf * sizeof(double) + 8));
+        RIGC_TRY(S.dense_d.reserve((size_t)nf * sizeof(double) + 8));
+    }
+    RIGC_CUDA(cudaStreamSynchronize(c.stream));
+    return RIGC_OK;
+}
+
+// RigidBody::convert_to_static (rigid_body.hpp:186-193): the body static,
+// every dof fixed, its velocity zero
+int convert_to_static(Ctx& c, Sim& S, int b)
+{
+    const int stat = RIGC_BODY_STATIC, all = 0x3f;
+    c.s.h_type[b] = stat;
+    S.h_fixed[b] = all;
+    RIGC_CUDA(cudaMemcpyAsync(c.s.type + b, &stat, sizeof(int), cudaMemcpyHostToDevice, c.stream));
+    RIGC_CUDA(cudaMemcpyAsync(S.fixed.as<int>() + b, &all, sizeof(int), cudaMemcpyHostToDevice, c.stream));
+    RIGC_CUDA(cudaMemsetAsync(S.vel.as<double>() + 6 * (size_t)b, 0, 6 * sizeof(double), c.stream));
+    RIGC_CUDA(cudaStreamSynchronize(c.stream));
+    return RIGC_OK;
+}
+
+// init_augmented_lagrangian's part of the schedules
+// (distance_barrier_rb_problem.cpp:204-226): *target the step's targets, or
+// null without any scheduled pose
+int kinematic_targets(Ctx& c, Sim& S, const double** target)
+{
+    *target = nullptr;
+    if (S.kin_max_time.empty()) return RIGC_OK;
+    const int nb = S.nb;
+    bool changed = false, any = false;
+    std::vector<double> t(6 * (size_t)nb, NAN);
+    for (int b = 0; b < nb; b++) {
+        if (c.s.h_type[b] != RIGC_BODY_KINEMATIC) continue;
+        if (S.kin_max_time[b] < 0) {
+            RIGC_TRY(convert_to_static(c, S, b));
+            changed = true;
+        } else if (!S.kin_poses[b].empty()) {
+            for (int k = 0; k < 6; k++) t[6 * (size_t)b + k] = S.kin_poses[b].front()[k];
+            any = true;
+        }
+    }
+    if (changed) {
+        RIGC_TRY(set_free_dofs(c, S));
+        S.has_kinematic = false;
+        for (int b = 0; b < nb; b++) S.has_kinematic |= c.s.h_type[b] == RIGC_BODY_KINEMATIC;
+    }
+    if (!any) return RIGC_OK;
+    RIGC_TRY(S.kin_target.reserve(t.size() * sizeof(double)));
+    RIGC_CUDA(cudaMemcpyAsync(S.kin_target.ptr, t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice,
+                              c.stream));
+    RIGC_CUDA(cudaStreamSynchronize(c.stream));
+    *target = S.kin_target.as<double>();
+    return RIGC_OK;
+}
+
+// step_kinematic_bodies (distance_barrier_rb_problem.cpp:237-251)
+int advance_kinematic(Ctx& c, Sim& S)
+{
+    if (S.kin_max_time.empty()) return RIGC_OK;
+    bool changed = false;
+    for (int b = 0; b < S.nb; b++) {
+        if (c.s.h_type[b] != RIGC_BODY_KINEMATIC) continue;
+        if (S.kin_max_time[b] < 0) {
+            RIGC_TRY(convert_to_static(c, S, b));
+            changed = true;
+        } else {
+            S.kin_max_time[b] -= S.p.timestep;
+            if (!S.kin_poses[b].empty()) S.kin_poses[b].pop_front();
+        }
+    }
+    if (changed) {
+        RIGC_TRY(set_free_dofs(c, S));
+        S.has_kinematic = false;
+        for (int b = 0; b < S.nb; b++) S.has_kinematic |= c.s.h_type[b] == RIGC_BODY_KINEMATIC;
+    }
+    return RIGC_OK;
+}
+
 int sim_step_scenes(Ctx& c, rigc_step_stats* stats)
 {
     Sim& S = *c.sim;
@@ -2054,23 +2161,9 @@ int sim_init(Ctx& c, const rigc_sim_params& p, const rigc_sim_state& s)
     RIGC_CUDA(cudaMemcpyAsync(S.Qdot.ptr, s.Qdot, (size_t)nb * 72, cudaMemcpyHostToDevice, st));
     RIGC_CUDA(cudaStreamSynchronize(st));
     S.h_fixed.assign(s.dof_fixed, s.dof_fixed + nb);
-    // compact indices of the free dofs (the reference's free_dof slicing)
-    std::vector<int> fidx(6 * (size_t)nb, -1);
-    int nf = 0;
-    for (int b = 0; b < nb; b++)
-        for (int k = 0; k < 6; k++)
-            if (!((s.dof_fixed[b] >> k) & 1)) fidx[6 * b + k] = nf++;
-    S.nfree = nf;
-    RIGC_TRY(S.free_idx.reserve(fidx.size() * sizeof(int) + 8));
-    RIGC_CUDA(cudaMemcpyAsync(S.free_idx.ptr, fidx.data(), fidx.size() * sizeof(int),
-                              cudaMemcpyHostToDevice, st));
-    if (nf <= kDenseMax) {
-        RIGC_TRY(S.dense.reserve((size_t)nf * nf * sizeof(double) + 8));
-        RIGC_TRY(S.dense_b.reserve((size_t)nf * sizeof(double) + 8));
-        RIGC_TRY(S.dense_x.reserve((size_t)nf * sizeof(double) + 8));
-        RIGC_TRY(S.dense_d.reserve((size_t)nf * sizeof(double) + 8));
-    }
-    RIGC_CUDA(cudaStreamSynchronize(st));
+    RIGC_TRY(set_free_dofs(c, S));
+    S.kin_max_time.clear();
+    S.kin_poses.clear();
     // per-scene set-up of batched contexts (average mass and bounding-box
     // diagonal default to the global ones; rigc_sim_scene_params sets them)
     const int ns = c.s.nscenes;
@@ -2118,14 +2211,18 @@ int sim_step(Ctx& c, rigc_step_stats* stats)
         RIGC_TRY(build_constraints(c, x0, p.dhat, p.dmin));
         RIGC_TRY(friction_setup(c, x0, p.dhat, S.kappa, p.coefficient_friction, 0.0));
     }
-    // init_augmented_lagrangian: kinematic targets x0 + h v
+    // init_augmented_lagrangian: kinematic bodies whose time has run out
+    // become static, the others' targets are their scheduled poses or
+    // x0 + h v
     S.al_kq = S.al_kQ = 1e3;
     S.al_sat_q = S.al_sat_Q = false;
+    const double* kin_target = nullptr;
+    RIGC_TRY(kinematic_targets(c, S, &kin_target));
     if (S.has_kinematic) {
         RIGC_COUNT_LAUNCH();
         k_al_init<<<grid_for(nb, 128), 128, 0, st>>>(nb, c.s.type, x0, S.vel.as<double>(), p.timestep,
-                                                     S.al_xpred.as<double>(), S.al_lam.as<double>(),
-                                                     S.al_Lam.as<double>());
+                                                     kin_target, S.al_xpred.as<double>(),
+                                                     S.al_lam.as<double>(), S.al_Lam.as<double>());
     }
 
     // IPCSolver::init_solve
@@ -2298,6 +2395,7 @@ int sim_step(Ctx& c, rigc_step_stats* stats)
                                                    p.timestep);
     RIGC_CUDA(cudaGetLastError());
     RIGC_CUDA(cudaStreamSynchronize(st));
+    RIGC_TRY(advance_kinematic(c, S));
     local.barrier_stiffness = S.kappa;
     if (stats) {
         stats->newton_iterations += local.newton_iterations;
@@ -2306,6 +2404,27 @@ int sim_step(Ctx& c, rigc_step_stats* stats)
         stats->ccd_calls += local.ccd_calls;
         stats->cg_iterations += local.cg_iterations;
         stats->barrier_stiffness = local.barrier_stiffness;
+    }
+    return RIGC_OK;
+}
+
+int sim_set_kinematic(Ctx& c, int body, double max_time, int64_t num_poses, const double* poses)
+{
+    if (!c.sim || c.s.nscenes > 1 || body < 0 || body >= c.s.nb || num_poses < 0 || (num_poses && !poses))
+        return RIGC_ERR_ARG;
+    if (c.s.h_type[body] != RIGC_BODY_KINEMATIC) return RIGC_ERR_ARG;
+    Sim& S = *c.sim;
+    if (S.kin_max_time.empty()) {
+        S.kin_max_time.assign(S.nb, INFINITY);
+        S.kin_poses.assign(S.nb, {});
+    }
+    // read_rb_scene.cpp:99-101: a negative time is no limit
+    S.kin_max_time[body] = max_time < 0 ? INFINITY : max_time;
+    S.kin_poses[body].clear();
+    for (int64_t i = 0; i < num_poses; i++) {
+        std::array<double, 6> q;
+        for (int k = 0; k < 6; k++) q[k] = poses[6 * i + k];
+        S.kin_poses[body].push_back(q);
     }
     return RIGC_OK;
 }

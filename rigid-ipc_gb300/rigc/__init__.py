@@ -14,7 +14,7 @@ import math
 import numpy as np
 
 from . import _lib as L
-from .scene import Scene  # noqa: F401
+from .scene import BODY_KINEMATIC, Scene  # noqa: F401
 
 __all__ = ["Context", "Scene", "L", "fp64_throughput"]
 
@@ -459,6 +459,11 @@ class Context:
         s = L.SimState(*[k.ctypes.data for k in keep])
         L.check(self.lib.rigc_sim_init(self.h, C.byref(p), C.byref(s)), "rigc_sim_init")
         self.sim_params = p
+        # the kinematic bodies' schedules read from the scene
+        if self.num_scenes == 1:
+            for i, b in enumerate(sc.bodies):
+                if b.type == BODY_KINEMATIC and (b.kinematic_poses or np.isfinite(b.kinematic_max_time)):
+                    self.sim_set_kinematic(i, b.kinematic_max_time, b.kinematic_poses)
         if self.num_scenes > 1:
             # each scene's average mass (RigidBodyAssembler::average_mass over
             # its free dofs) and initial bounding-box diagonal
@@ -499,6 +504,16 @@ class Context:
         L.check(self.lib.rigc_set_tune(self.h, ccd_blocks_per_sm, cache_slots_per_body,
                                        barrier_per_warp, ccd_seeds_log2, ccd_hand_off, ccd_warp),
                 "rigc_set_tune")
+
+    def sim_set_kinematic(self, body, max_time=-1.0, poses=()):
+        """A kinematic body's schedule: the poses (n x 6) the next steps drive
+        it to, then x0 + h v; static once max_time has run out (negative: no
+        limit)."""
+        q = np.ascontiguousarray(np.asarray(poses, np.float64).reshape(-1, 6))
+        mt = -1.0 if not np.isfinite(max_time) else float(max_time)
+        L.check(self.lib.rigc_sim_set_kinematic(self.h, int(body), mt, len(q),
+                                                q.ctypes.data if len(q) else None),
+                "rigc_sim_set_kinematic")
 
     def sim_rollout(self, num_steps, checkpoint_every=10):
         """Advance num_steps steps, keeping checkpoints for sim_backward."""

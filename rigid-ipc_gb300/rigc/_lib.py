@@ -39,6 +39,7 @@ EXPORTS = [
     "rigc_sim_scene_params", "rigc_autotune", "rigc_set_tune", "rigc_fp64_throughput",
     "rigc_min_distance", "rigc_detect_intersections", "rigc_earliest_toi_piecewise_linear",
     "rigc_compute_earliest_toi_piecewise_linear", "rigc_set_pl_search", "rigc_set_ccd_window",
+    "rigc_sim_set_kinematic",
 ]
 RIGC_ERR_TOO_LARGE = 7
 RIGC_ERR_SOLVE = 8
@@ -154,6 +155,7 @@ def load():
     L.rigc_compute_earliest_toi_piecewise_linear.argtypes = [_vp, _vp, _vp, C.c_double, _d]
     L.rigc_set_pl_search.argtypes = [_vp, C.c_int32]
     L.rigc_set_ccd_window.argtypes = [_vp, C.c_int32]
+    L.rigc_sim_set_kinematic.argtypes = [_vp, C.c_int32, C.c_double, C.c_int64, _vp]
     L.rigc_construct_constraint_set.argtypes = [_vp, _vp, C.c_double, C.c_double,
                                                 C.POINTER(ConstraintsView)]
     L.rigc_set_constraints.argtypes = [_vp, C.c_int64, _vp, _vp, _vp, _vp, _vp, _vp]

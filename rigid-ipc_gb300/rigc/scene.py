@@ -217,6 +217,11 @@ class RigidBody:
     r_max: float = 0.0
     average_edge_length: float = 0.0
     Qdot: np.ndarray = field(default_factory=lambda: np.zeros((3, 3)))
+    # kinematic bodies (rigid_body.hpp:260-261): the time the body keeps
+    # moving (+inf: always) and the poses (p, theta) it is driven to, one per
+    # time step, before its velocity takes over
+    kinematic_max_time: float = float("inf")
+    kinematic_poses: list = field(default_factory=list)
 
 
 def make_body(vertices, faces, *, position=(0, 0, 0), rotation_deg=(0, 0, 0),
@@ -483,6 +488,15 @@ def scene_from_json(spec) -> Scene:
             body_type=jb.get("type", "dynamic"),
             group_id=jb.get("group_id", -1),
             name=mesh or "RigidBody"))
+        # read_rb_scene.cpp:94-101,233-245: a negative max time is +inf; a
+        # kinematic pose's position and rotation are taken as given (missing
+        # parts zero)
+        kmt = float(jb.get("kinematic_max_time", -1))
+        bodies[-1].kinematic_max_time = float("inf") if kmt < 0 else kmt
+        bodies[-1].kinematic_poses = [
+            np.concatenate([np.asarray(q.get("position", [0, 0, 0]), dtype=np.float64),
+                            np.asarray(q.get("rotation", [0, 0, 0]), dtype=np.float64)])
+            for q in jb.get("kinematic_poses", [])]
     assign_group_ids(bodies)
     dbc = spec.get("distance_barrier_constraint", {})
     return Scene(

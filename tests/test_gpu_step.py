@@ -94,6 +94,40 @@ def test_kinematic_bodies_match_oracle(oracle):
         ctx.sim_backward(np.zeros((sc.num_bodies, 6)))
 
 
+def test_kinematic_schedule_matches_oracle(oracle):
+    """A kinematic cube driven through its JSON pose list into a dynamic one,
+    then by its velocity, static once kinematic_max_time has run out
+    (rigc_sim_set_kinematic, set by sim_init from the scene): device poses
+    against the oracle's after each of 8 steps, with the reference's solver
+    settings, within 1e-6 (the kinematic targets are met to the augmented
+    Lagrangian's progress tolerance, 0.999 of the step, and its discrete
+    penalty and multiplier updates follow the iterates, so a rounding-level
+    difference in a contact step can move the solution at that level; the
+    same settings keep the first four steps within 1e-7); the body does not
+    move after it became static."""
+    import rigc
+
+    from test_kinematic_oracle import scheduled_scene
+
+    sc = scheduled_scene()
+    sim = oracle.OracleSim(sc, h=0.01, gravity=(0.0, -9.81, 0.0), dhat=1e-3)
+    ctx = rigc.Context(sc)
+    ctx.sim_init(0.01, (0.0, -9.81, 0.0), 1e-3)
+    frozen = None
+    for k in range(8):
+        sim.step()
+        ctx.sim_step(1)
+        P, V, Q, _ = ctx.sim_state()
+        assert np.abs(P.reshape(-1) - sim.pose).max() <= (1e-7 if k < 4 else 1e-6), k
+        if k >= 5:
+            assert sim.type[1] == 0 and np.all(V[1] == 0)
+            if frozen is None:
+                frozen = P[1].copy()
+            assert np.array_equal(P[1], frozen)
+    with pytest.raises(RuntimeError):  # only kinematic bodies have a schedule
+        ctx.sim_set_kinematic(2, 1.0, [])
+
+
 # ---------------------------------------------------------------------------
 # whole runs against the oracle's trajectories (tests/golden/
 # step_trajectories.npz, made by make_step_fixtures.py), at the 1e-8 pose

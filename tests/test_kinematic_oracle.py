@@ -59,3 +59,62 @@ def test_kinematic_body_pushes_dynamic_one(oracle):
             assert np.all(np.isfinite(e))
     # the dynamic cube was pushed along +x
     assert P[1, 0] - x0[1, 0] > 1e-3
+
+
+def scheduled_scene(max_time=0.05, n_poses=3):
+    """A kinematic cube with a pose list (JSON kinematic_poses) and a
+    kinematic_max_time, a dynamic cube in its way, a static plane."""
+    from rigc import scene as S
+
+    poses = [{"position": [0.2 + 0.1 * (k + 1), 0.6, 0.0], "rotation": [0.0, 0.05 * (k + 1), 0.0]}
+             for k in range(n_poses)]
+    spec = {"timestep": H, "rigid_body_problem": {"gravity": list(G), "rigid_bodies": [
+        {"mesh": "plane", "type": "static", "scale": 20.0},
+        {"mesh": "cube", "type": "kinematic", "position": [0.2, 0.6, 0.0],
+         "linear_velocity": [0.5, 0.0, 0.0], "kinematic_max_time": max_time,
+         "kinematic_poses": poses},
+        {"mesh": "cube", "position": [1.27, 0.5008, 0.0]}]}}
+    return S.scene_from_json(spec)
+
+
+def test_scene_reads_kinematic_schedule():
+    """read_rb_scene.cpp:94-101,233-245: the pose list as given, a negative
+    max time as no limit."""
+    from rigc import scene as S
+
+    sc = scheduled_scene()
+    b = sc.bodies[1]
+    assert b.kinematic_max_time == 0.05 and len(b.kinematic_poses) == 3
+    assert np.array_equal(b.kinematic_poses[1], [0.4, 0.6, 0.0, 0.0, 0.1, 0.0])
+    spec = {"rigid_body_problem": {"rigid_bodies": [
+        {"mesh": "cube", "type": "kinematic", "kinematic_max_time": -1}]}}
+    assert S.scene_from_json(spec).bodies[0].kinematic_max_time == np.inf
+
+
+def test_kinematic_schedule(oracle):
+    """The body is driven to each listed pose in turn (positions to the
+    augmented Lagrangian's progress tolerance), then by its velocity; once
+    kinematic_max_time has run out it is static: type 0, every dof fixed,
+    velocity zero, pose unchanged from then on (init_augmented_lagrangian and
+    step_kinematic_bodies, distance_barrier_rb_problem.cpp:190-251)."""
+    sc = scheduled_scene()
+    sim = oracle.OracleSim(sc, h=H, gravity=G, dhat=1e-3)
+    targets = [np.asarray(q) for q in sc.bodies[1].kinematic_poses]
+    for k in range(3):
+        prev = sim.pose[6:12].copy()
+        sim.step()
+        P = sim.pose[6:12]
+        step = np.linalg.norm(targets[k][:3] - prev[:3])
+        assert np.linalg.norm(P[:3] - targets[k][:3]) <= 1e-3 * step + 1e-12
+        assert sim.type[1] == 1
+    # the list used up: x0 + h v (v the initial 0.5 m/s along x)
+    prev = sim.pose[6:12].copy()
+    sim.step()
+    assert abs(sim.pose[6] - (prev[0] + H * 0.5)) <= 1e-3 * H * 0.5 + 1e-12
+    # 0.05 s run out after five steps: static from the sixth step's start
+    sim.step()
+    sim.step()
+    assert sim.type[1] == 0 and np.all(sim.fixed[6:12] == 1) and np.all(sim.vel[6:12] == 0)
+    frozen = sim.pose[6:12].copy()
+    sim.step()
+    assert np.array_equal(sim.pose[6:12], frozen)
