@@ -459,11 +459,11 @@ __global__ void k_dense_fill(HessView H, const int* __restrict__ free_idx, int n
 constexpr int kPanel = 32;
 constexpr int kPanelStride = kPanel + 1;  // shared-memory row stride (no bank conflicts down a column)
 
-__global__ void __launch_bounds__(512) k_ldlt_panel(double* __restrict__ A, int n, int j0,
+__global__ void __launch_bounds__(512) k_ldlt_panel(double* __restrict__ A, int n, int j0, int rows,
                                                     double* __restrict__ D, int* __restrict__ flags)
 {
-    extern __shared__ double P[];  // (n - j0) x kPanel, row stride kPanelStride
-    const int m = n - j0, w = min(kPanel, m);
+    extern __shared__ double P[];  // rows x kPanel, row stride kPanelStride
+    const int m = min(rows, n - j0), w = min(kPanel, n - j0);
     if (flags[0]) return;
     for (int e = threadIdx.x; e < m * w; e += blockDim.x) {
         const int r = e / w, c = e % w;
@@ -496,6 +496,41 @@ __global__ void __launch_bounds__(512) k_ldlt_panel(double* __restrict__ A, int 
         if (r > c) A[(size_t)(j0 + r) * n + j0 + c] = P[r * kPanelStride + c];
         else if (r == c) D[j0 + c] = P[r * kPanelStride + c];
     }
+}
+
+// Systems too large for a panel in shared memory: after k_ldlt_panel has
+// factorised the panel's w x w diagonal block, each row r below it takes its
+// panel entries through the same column-by-column elimination as
+// k_ldlt_panel's (divide by the pivot, then subtract l_rc d_c l_c'c from the
+// later columns), one thread per row
+__global__ void __launch_bounds__(128) k_ldlt_trsm(double* __restrict__ A, int n, int j0, int w,
+                                                   const double* __restrict__ D,
+                                                   const int* __restrict__ flags)
+{
+    if (flags[0]) return;
+    __shared__ double L[kPanel][kPanel + 1], d[kPanel];
+    for (int e = threadIdx.x; e < kPanel * kPanel; e += blockDim.x) {
+        const int r = e / kPanel, c = e % kPanel;
+        L[r][c] = (r < w && c < r) ? A[(size_t)(j0 + r) * n + j0 + c] : 0.0;
+    }
+    if (threadIdx.x < kPanel) d[threadIdx.x] = threadIdx.x < w ? D[j0 + threadIdx.x] : 1.0;
+    __syncthreads();
+    const int r = j0 + w + blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    double x[kPanel];
+#pragma unroll
+    for (int c = 0; c < kPanel; c++) x[c] = c < w ? A[(size_t)r * n + j0 + c] : 0.0;
+#pragma unroll
+    for (int c = 0; c < kPanel; c++) {
+        if (c >= w) break;
+        x[c] /= d[c];
+#pragma unroll
+        for (int cc = c + 1; cc < kPanel; cc++)
+            if (cc < w) x[cc] -= x[c] * d[c] * L[cc][c];
+    }
+#pragma unroll
+    for (int c = 0; c < kPanel; c++)
+        if (c < w) A[(size_t)r * n + j0 + c] = x[c];
 }
 
 // A[i][k] -= sum_c L[i][c] D[c] L[k][c] over the panel columns c, for the
@@ -1099,6 +1134,10 @@ double barrier_hessian_d(double d, double s)
 
 // systems with at most this many free dofs are factorised densely
 constexpr int kDenseMax = 768;
+// above kDenseMax free dofs: PCG for at most kCGTry iterations, then (up to
+// kDenseLimit free dofs, n^2 doubles) the dense LDL^T for the rest of the step
+constexpr int kDenseLimit = 8192;
+constexpr long long kCGTry = 300;
 
 struct Sim {
     rigc_sim_params p {};
@@ -1111,6 +1150,7 @@ struct Sim {
     double kappa = 1, kappa_max = 0;
     double dk = 0;  // d kappa / d kappa0 of the current step (0 when kappa0 is clamped)
     std::vector<int> h_fixed;
+    bool dense_step = false;  // this step's PCG did not converge: dense LDL^T from then on
     // rollout tape: checkpoints (21 nb doubles each: poses, velocities, Qdot),
     // the state after the rollout, and one recomputed segment
     int tape_steps = 0, tape_every = 0;
@@ -1304,7 +1344,7 @@ HessView hess_view(Sim& S, const Objective& O, double reg)
 
 // PCG for (H + reg I) d = -g on the free dofs; false when it breaks down
 // or does not reach the tolerance
-int pcg(Ctx& c, Sim& S, const HessView& H, bool& ok, int64_t& iters)
+int pcg(Ctx& c, Sim& S, const HessView& H, bool& ok, int64_t& iters, long long cap = 0)
 {
     const int64_t n = 6 * (int64_t)S.nb;
     cudaStream_t st = c.stream;
@@ -1336,7 +1376,7 @@ int pcg(Ctx& c, Sim& S, const HessView& H, bool& ok, int64_t& iters)
     iters = 0;
     if (bnorm2 == 0) return RIGC_OK;
     const double tol2 = 1e-24 * bnorm2;  // relative residual 1e-12
-    const long long max_it = std::max<long long>(1000, 4 * n);
+    const long long max_it = cap > 0 ? cap : std::max<long long>(1000, 4 * n);
     // the iteration loop runs on the device as one graph launch: its
     // arguments are fixed, so the view, the tolerance and the iteration
     // count live in device memory (sc[7] tolerance, sc[20] iterations)
@@ -1392,12 +1432,20 @@ int dense_ldlt(Ctx& c, double* A, int n, double* D, int* flags)
                                        (int)smem));
         attr = true;
     }
+    // up to kDenseMax unknowns the whole panel column is factorised in shared
+    // memory; above, its diagonal block there and the rows below by k_ldlt_trsm
+    const bool big = n > kDenseMax;
     for (int j0 = 0; j0 < n; j0 += kPanel) {
         const int w = std::min(kPanel, n - j0);
+        const int rows = big ? w : n - j0;
         RIGC_COUNT_LAUNCH();
-        k_ldlt_panel<<<1, 512, (size_t)(n - j0) * kPanelStride * sizeof(double), c.stream>>>(
-            A, n, j0, D, flags);
+        k_ldlt_panel<<<1, 512, (size_t)rows * kPanelStride * sizeof(double), c.stream>>>(
+            A, n, j0, rows, D, flags);
         const int rest = n - j0 - w;
+        if (big && rest > 0) {
+            RIGC_COUNT_LAUNCH();
+            k_ldlt_trsm<<<grid_for(rest, 128), 128, 0, c.stream>>>(A, n, j0, w, D, flags);
+        }
         if (rest > 0) {
             const int tiles = (rest + 31) / 32;
             RIGC_COUNT_LAUNCH();
@@ -1414,6 +1462,12 @@ int dense_solve(Ctx& c, Sim& S, const HessView& H, bool& ok)
     const int n = S.nfree;
     const int n6 = 6 * S.nb;
     cudaStream_t st = c.stream;
+    if (n > kDenseMax) {
+        RIGC_TRY(S.dense.reserve((size_t)n * n * sizeof(double) + 8));
+        RIGC_TRY(S.dense_b.reserve((size_t)n * sizeof(double) + 8));
+        RIGC_TRY(S.dense_x.reserve((size_t)n * sizeof(double) + 8));
+        RIGC_TRY(S.dense_d.reserve((size_t)n * sizeof(double) + 8));
+    }
     int* flags = reinterpret_cast<int*>(S.scal.as<double>() + 8);
     RIGC_CUDA(cudaMemsetAsync(flags, 0, 2 * sizeof(int), st));
     RIGC_CUDA(cudaMemsetAsync(S.dense.ptr, 0, (size_t)n * n * sizeof(double), st));
@@ -1434,6 +1488,23 @@ int dense_solve(Ctx& c, Sim& S, const HessView& H, bool& ok)
     RIGC_CUDA(cudaMemcpyAsync(&fl, flags, sizeof(int), cudaMemcpyDeviceToHost, st));
     RIGC_CUDA(cudaStreamSynchronize(st));
     ok = fl == 0;
+    return RIGC_OK;
+}
+
+// The Newton system on the free dofs: the dense LDL^T up to kDenseMax
+// unknowns; above, PCG, and when it does not converge within kCGTry
+// iterations (the stiff couplings of a contact pile) the dense LDL^T up to
+// kDenseLimit unknowns, for the rest of the time step
+int newton_solve(Ctx& c, Sim& S, const HessView& H, bool& solved, int64_t& cgit)
+{
+    cgit = 0;
+    if (S.nfree <= kDenseMax || S.dense_step) return dense_solve(c, S, H, solved);
+    const bool can_dense = S.nfree <= kDenseLimit;
+    RIGC_TRY(pcg(c, S, H, solved, cgit, can_dense ? kCGTry : 0));
+    if (!solved && can_dense) {
+        S.dense_step = true;
+        RIGC_TRY(dense_solve(c, S, H, solved));
+    }
     return RIGC_OK;
 }
 
@@ -2205,6 +2276,7 @@ int sim_step(Ctx& c, rigc_step_stats* stats)
     double* xt = S.xt.as<double>();
     double* dir = S.dir.as<double>();
     rigc_step_stats local {};
+    S.dense_step = false;
 
     // update_constraints: lagged friction at x0 with the current stiffness
     if (p.coefficient_friction > 0) {
@@ -2266,12 +2338,7 @@ int sim_step(Ctx& c, rigc_step_stats* stats)
             bool solved;
             int64_t cgit;
             HessView H = hess_view(S, O, coeff);
-            if (S.nfree <= kDenseMax) {
-                cgit = 0;
-                RIGC_TRY(dense_solve(c, S, H, solved));
-            } else {
-                RIGC_TRY(pcg(c, S, H, solved, cgit));
-            }
+            RIGC_TRY(newton_solve(c, S, H, solved, cgit));
             local.cg_iterations += cgit;
             double gd = solved ? host_dot(c, S, S.g.as<double>(), S.sol.as<double>()) : 0;
             ok = solved && gd <= 0;
@@ -2367,8 +2434,7 @@ int sim_step(Ctx& c, rigc_step_stats* stats)
         bool solved;
         int64_t cgit = 0;
         HessView H = hess_view(S, O, 0.0);
-        if (S.nfree <= kDenseMax) RIGC_TRY(dense_solve(c, S, H, solved));
-        else RIGC_TRY(pcg(c, S, H, solved, cgit));
+        RIGC_TRY(newton_solve(c, S, H, solved, cgit));
         local.cg_iterations += cgit;
         if (!solved) break;
         const double gd = host_dot(c, S, S.g.as<double>(), S.sol.as<double>());
