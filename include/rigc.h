@@ -371,10 +371,14 @@ int rigc_friction_local_terms(rigc_ctx* ctx, const double* x,
  * (src/problems/distance_barrier_rb_problem.cpp:118-143) with the IPC Newton
  * solver (src/solvers/ipc_solver.cpp, src/solvers/newton_solver.cpp) for the
  * default settings: implicit Euler, velocity convergence, one friction
- * lagging iteration, no kinematic bodies.  Every term, the CCD line-search
- * filter and the Newton linear solve (a dense LDL^T for at most 768 free
- * dofs, else block-Jacobi preconditioned conjugate gradients on the
- * block-sparse Hessian, relative residual 1e-12) run on the device; the solver's scalar decisions run on the host.  Field names follow
+ * lagging iteration, kinematic bodies through the augmented Lagrangian
+ * (their schedules: rigc_sim_set_kinematic).  Every term, the CCD
+ * line-search filter and the Newton linear solve (a dense LDL^T for at most
+ * 768 free dofs, else block-Jacobi preconditioned conjugate gradients on the
+ * block-sparse Hessian, relative residual 1e-12, and when those do not
+ * converge within 300 iterations the dense LDL^T for the rest of the step,
+ * up to 8192 free dofs) run on the device; the solver's scalar decisions run
+ * on the host.  Field names follow
  * the reference's JSON settings; average_mass and world_bbox_diagonal are the
  * values the problem computes at start-up (RigidBodyAssembler::average_mass,
  * rigid_body_assembler.cpp:104-118; the world bounding-box diagonal,
