@@ -15,12 +15,38 @@
 #include "oracle.hpp"
 
 #include <algorithm>
+#include <atomic>
+#include <thread>
+
+#include <algorithm>
 #include <unordered_map>
 
 namespace orc {
 
 void irotation(const I r[3], I R[9]);
 void iworld_vertex(const I R[9], const I p[3], const double* v, I out[3]);
+
+// fn(i) for i in [0, n) over the host's threads (items taken one chunk at
+// a time); the result of each i may not depend on the others'
+template <class F> static void parallel_for(long long n, long long chunk, F fn)
+{
+    const int nt = std::max(1, (int)std::thread::hardware_concurrency());
+    if (nt == 1 || n <= chunk) {
+        for (long long i = 0; i < n; i++) fn(i);
+        return;
+    }
+    std::atomic<long long> next(0);
+    auto work = [&]() {
+        for (;;) {
+            const long long i0 = next.fetch_add(chunk);
+            if (i0 >= n) break;
+            for (long long i = i0; i < std::min(n, i0 + chunk); i++) fn(i);
+        }
+    };
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; t++) th.emplace_back(work);
+    for (auto& t : th) t.join();
+}
 
 static AABB make_box(const double lo[3], const double hi[3])
 {
@@ -188,8 +214,10 @@ void element_aabbs(
     if (continuous) {
         double dlo[3], dhi[3];
         scene_box(s, x0, x1, body_in, dlo, dhi);
-        for (int b = 0; b < s.nb; b++) {
-            if (!body_in[b]) continue;
+        // the bodies over the host's threads (each writes its own vertices)
+        parallel_for(s.nb, 1, [&](long long bl) {
+            const int b = (int)bl;
+            if (!body_in[b]) return;
             std::vector<I> iv;
             body_vertex_intervals(s, b, x0, x1, I(0.0, 1.0), 1, 0, dlo, dhi, inflation, iv);
             for (int v = 0; v < s.bvs[b + 1] - s.bvs[b]; v++) {
@@ -207,7 +235,7 @@ void element_aabbs(
                     vin[gv] = 1;
                 }
             }
-        }
+        });
     } else {
         std::vector<double> V;
         world_vertices(s, x0, V);
@@ -279,7 +307,7 @@ void detect_candidates(
         return;
     }
 
-    // sequential hash grid over the boxes of the included elements
+    // hash grid over the boxes of the included elements
     double lo[3] = { INFINITY, INFINITY, INFINITY }, hi[3] = { -INFINITY, -INFINITY, -INFINITY };
     double len = 0;
     long nl = 0;
@@ -317,44 +345,92 @@ void detect_candidates(
                 for (long long z = c0[2]; z <= c1[2]; z++)
                     items.push_back({ (z * dims[1] + y) * dims[0] + x, id });
     };
-    std::vector<Item> vitems, eitems, fitems;
-    for (int v = 0; v < s.nv; v++)
-        if (vi[v]) add(vb[v], v, vitems);
-    for (int e = 0; e < s.ne; e++)
-        if (ei[e]) add(eb[e], e, eitems);
-    for (int f = 0; f < s.nf; f++)
-        if (fi[f]) add(fb[f], f, fitems);
-    std::sort(vitems.begin(), vitems.end());
-    std::sort(eitems.begin(), eitems.end());
-    std::sort(fitems.begin(), fitems.end());
+    // the items of each kind (chunks of elements over the host's threads,
+    // concatenated in chunk order), sorted by (cell, element): the same
+    // sorted lists as one sequential pass
+    const int nt = std::max(1, (int)std::thread::hardware_concurrency());
+    auto items_of = [&](int n, const std::vector<AABB>& box, const std::vector<char>& in) {
+        std::vector<std::vector<Item>> part(nt);
+        const long long per = (n + nt - 1) / nt;
+        parallel_for(nt, 1, [&](long long t) {
+            for (long long k = t * per; k < std::min<long long>(n, (t + 1) * per); k++)
+                if (in[k]) add(box[k], (int)k, part[t]);
+        });
+        std::vector<Item> all;
+        for (auto& q : part) all.insert(all.end(), q.begin(), q.end());
+        // sorted chunks, then merged pairwise
+        std::vector<size_t> cut(nt + 1);
+        for (int t = 0; t <= nt; t++) cut[t] = all.size() * t / nt;
+        parallel_for(nt, 1, [&](long long t) { std::sort(all.begin() + cut[t], all.begin() + cut[t + 1]); });
+        for (int w = 1; w < nt; w *= 2) {
+            std::vector<long long> lefts;
+            for (int t = 0; t + w < nt; t += 2 * w) lefts.push_back(t);
+            parallel_for((long long)lefts.size(), 1, [&](long long k) {
+                const int t = (int)lefts[k];
+                std::inplace_merge(all.begin() + cut[t], all.begin() + cut[t + w],
+                                   all.begin() + cut[std::min(nt, t + 2 * w)]);
+            });
+        }
+        return all;
+    };
+    std::vector<Item> vitems = items_of(s.nv, vb, vi), eitems = items_of(s.ne, eb, ei),
+                      fitems = items_of(s.nf, fb, fi);
+    // cell runs of a sorted list split over the threads at cell boundaries
+    auto runs = [&](const std::vector<Item>& it) {
+        std::vector<size_t> cut(nt + 1, it.size());
+        cut[0] = 0;
+        for (int t = 1; t < nt; t++) {
+            size_t c = std::max(cut[t - 1], it.size() * t / nt);
+            while (c > 0 && c < it.size() && it[c].key == it[c - 1].key) c++;
+            cut[t] = std::min(c, it.size());
+        }
+        return cut;
+    };
+    std::vector<std::vector<std::array<int, 2>>> pee(nt), pfv(nt);
     // edge-edge within cells
-    for (size_t i = 0; i < eitems.size();) {
-        size_t j = i;
-        while (j < eitems.size() && eitems[j].key == eitems[i].key) j++;
-        for (size_t a = i; a < j; a++)
-            for (size_t b = a + 1; b < j; b++) {
-                int ea = eitems[a].id, ebb = eitems[b].id;
-                if (egrp(ea) != egrp(ebb) && aabb_overlap(eb[ea], eb[ebb]))
-                    out.ee.push_back({ std::min(ea, ebb), std::max(ea, ebb) });
+    {
+        const std::vector<size_t> cut = runs(eitems);
+        parallel_for(nt, 1, [&](long long t) {
+            for (size_t i = cut[t]; i < cut[t + 1];) {
+                size_t j = i;
+                while (j < eitems.size() && eitems[j].key == eitems[i].key) j++;
+                for (size_t a = i; a < j; a++)
+                    for (size_t b = a + 1; b < j; b++) {
+                        int ea = eitems[a].id, ebb = eitems[b].id;
+                        if (egrp(ea) != egrp(ebb) && aabb_overlap(eb[ea], eb[ebb]))
+                            pee[t].push_back({ std::min(ea, ebb), std::max(ea, ebb) });
+                    }
+                i = j;
             }
-        i = j;
+        });
     }
     // face-vertex within cells (merge of the two sorted lists)
-    size_t vpos = 0;
-    for (size_t i = 0; i < fitems.size();) {
-        size_t j = i;
-        while (j < fitems.size() && fitems[j].key == fitems[i].key) j++;
-        long long key = fitems[i].key;
-        while (vpos < vitems.size() && vitems[vpos].key < key) vpos++;
-        size_t vend = vpos;
-        while (vend < vitems.size() && vitems[vend].key == key) vend++;
-        for (size_t a = i; a < j; a++)
-            for (size_t b = vpos; b < vend; b++) {
-                int f = fitems[a].id, v = vitems[b].id;
-                if (fgrp(f) != vgrp(v) && aabb_overlap(fb[f], vb[v]))
-                    out.fv.push_back({ f, v });
+    {
+        const std::vector<size_t> cut = runs(fitems);
+        parallel_for(nt, 1, [&](long long t) {
+            if (cut[t] >= cut[t + 1]) return;
+            size_t vpos = std::lower_bound(vitems.begin(), vitems.end(), Item { fitems[cut[t]].key, -1 })
+                          - vitems.begin();
+            for (size_t i = cut[t]; i < cut[t + 1];) {
+                size_t j = i;
+                while (j < fitems.size() && fitems[j].key == fitems[i].key) j++;
+                long long key = fitems[i].key;
+                while (vpos < vitems.size() && vitems[vpos].key < key) vpos++;
+                size_t vend = vpos;
+                while (vend < vitems.size() && vitems[vend].key == key) vend++;
+                for (size_t a = i; a < j; a++)
+                    for (size_t b = vpos; b < vend; b++) {
+                        int f = fitems[a].id, v = vitems[b].id;
+                        if (fgrp(f) != vgrp(v) && aabb_overlap(fb[f], vb[v]))
+                            pfv[t].push_back({ f, v });
+                    }
+                i = j;
             }
-        i = j;
+        });
+    }
+    for (int t = 0; t < nt; t++) {
+        out.ee.insert(out.ee.end(), pee[t].begin(), pee[t].end());
+        out.fv.insert(out.fv.end(), pfv[t].begin(), pfv[t].end());
     }
     std::sort(out.ee.begin(), out.ee.end());
     out.ee.erase(std::unique(out.ee.begin(), out.ee.end()), out.ee.end());
