@@ -284,6 +284,20 @@ def test_hash_grid_equals_brute_force(oracle, cube_scene):
         assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
 
 
+def test_hash_grid_equals_brute_force_on_a_pile(oracle):
+    """The same on an icosphere contact pile (thousands of grid items, so
+    the threads' chunks of items, sorts and cell runs all meet boundaries)."""
+    import bench
+
+    sc, x0, x1 = bench.make_workload(8, 0)
+    o = oracle.OracleScene(sc)
+    for cont, infl in ((True, 0.0), (False, 5e-4)):
+        a = o.detect_candidates(x0, x1, cont, infl)
+        b = o.detect_candidates(x0, x1, cont, infl, brute=True)
+        assert len(a[0]) + len(a[1]) > 0
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
 def parallel_edges(offset, direction=(1.0, 2e-5, 1e-5)):
     """Two single-edge bodies whose edges are nearly parallel (mollified) and
     whose closest features are endpoints for the given offset of the second."""
