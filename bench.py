@@ -255,8 +255,8 @@ def cpu_pass(o, x0, x1, dhat, nthreads):
     return time.perf_counter() - t
 
 
-CPU_SAMPLE = ("one whole narrow-phase pass per step: both hash-grid broad phases and the CCD over "
-              "every candidate on {n} threads, the constraint set and barrier terms on 1 thread")
+CPU_SAMPLE = ("one whole narrow-phase pass per step: both hash-grid broad phases, the CCD over "
+              "every candidate and the barrier terms on {n} threads, the constraint set on 1 thread")
 
 
 def cpu_baseline(sc, x0, x1, dhat, passes=2):

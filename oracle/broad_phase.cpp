@@ -26,28 +26,6 @@ namespace orc {
 void irotation(const I r[3], I R[9]);
 void iworld_vertex(const I R[9], const I p[3], const double* v, I out[3]);
 
-// fn(i) for i in [0, n) over the host's threads (items taken one chunk at
-// a time); the result of each i may not depend on the others'
-template <class F> static void parallel_for(long long n, long long chunk, F fn)
-{
-    const int nt = std::max(1, (int)std::thread::hardware_concurrency());
-    if (nt == 1 || n <= chunk) {
-        for (long long i = 0; i < n; i++) fn(i);
-        return;
-    }
-    std::atomic<long long> next(0);
-    auto work = [&]() {
-        for (;;) {
-            const long long i0 = next.fetch_add(chunk);
-            if (i0 >= n) break;
-            for (long long i = i0; i < std::min(n, i0 + chunk); i++) fn(i);
-        }
-    };
-    std::vector<std::thread> th;
-    for (int t = 0; t < nt; t++) th.emplace_back(work);
-    for (auto& t : th) t.join();
-}
-
 static AABB make_box(const double lo[3], const double hi[3])
 {
     AABB b;
@@ -214,8 +192,10 @@ void element_aabbs(
     if (continuous) {
         double dlo[3], dhi[3];
         scene_box(s, x0, x1, body_in, dlo, dhi);
-        // the bodies over the host's threads (each writes its own vertices)
-        parallel_for(s.nb, 1, [&](long long bl) {
+        // the bodies over the host's threads (each writes its own vertices;
+        // threads for large scenes only, the time step calls this often)
+        const bool big = (long long)s.nv + s.ne + s.nf >= 100000;
+        parallel_for(s.nb, big ? 1 : s.nb, [&](long long bl) {
             const int b = (int)bl;
             if (!body_in[b]) return;
             std::vector<I> iv;
@@ -348,7 +328,9 @@ void detect_candidates(
     // the items of each kind (chunks of elements over the host's threads,
     // concatenated in chunk order), sorted by (cell, element): the same
     // sorted lists as one sequential pass
-    const int nt = std::max(1, (int)std::thread::hardware_concurrency());
+    const int nt = (long long)s.nv + s.ne + s.nf >= 100000
+                       ? std::max(1, (int)std::thread::hardware_concurrency())
+                       : 1;
     auto items_of = [&](int n, const std::vector<AABB>& box, const std::vector<char>& in) {
         std::vector<std::vector<Item>> part(nt);
         const long long per = (n + nt - 1) / nt;

@@ -161,7 +161,10 @@ void world_vertices_diff(
     world_vertices(s, x, V);
     dV.assign(9 * s.nv, 0.0);
     d2V.assign(27 * s.nv, 0.0);
-    for (int b = 0; b < s.nb; b++) {
+    // each body writes its own vertices (threads for large scenes only: the
+    // time step calls this for every objective evaluation)
+    parallel_for(s.nb, s.nv >= 200000 ? 4 : s.nb, [&](long long bl) {
+        const int b = (int)bl;
         D2<3> t[3];
         for (int k = 0; k < 3; k++) t[k] = D2<3>::var(x[6 * b + 3 + k], k);
         D2<3> R[9];
@@ -176,7 +179,7 @@ void world_vertices_diff(
                         d2V[27 * i + 9 * j + 3 * k + l] = vj.h[k][l];
             }
         }
-    }
+    });
 }
 
 // ---------------------------------------------------------------------------
@@ -780,9 +783,15 @@ double barrier_term(
     grad.assign(6 * s.nb, 0.0);
     std::map<std::pair<int, int>, std::array<double, 36>> blocks;
     double energy = 0;
-    for (const auto& c : cs) {
-        LocalTerm t;
-        constraint_local_term(s, c, V, dV, d2V, dhat, dmin, project, t);
+    // the constraints' local terms over the host's threads, then summed in
+    // constraint order
+    std::vector<LocalTerm> terms(cs.size());
+    parallel_for((long long)cs.size(), cs.size() >= 512 ? 16 : (long long)cs.size(), [&](long long i) {
+        constraint_local_term(s, cs[i], V, dV, d2V, dhat, dmin, project, terms[i]);
+    });
+    for (size_t ci = 0; ci < cs.size(); ci++) {
+        const Constraint& c = cs[ci];
+        const LocalTerm& t = terms[ci];
         energy += t.energy;
         for (int lb = 0; lb < 2; lb++)
             for (int k = 0; k < 6; k++) grad[6 * c.body[lb] + k] += t.grad[6 * lb + k];

@@ -18,9 +18,34 @@
 #include <atomic>
 #include <cmath>
 #include <cstdint>
+#include <thread>
 #include <vector>
 
 namespace orc {
+
+// fn(i) for i in [0, n) over the host's threads, chunk items at a time; the
+// work of each i may not depend on another's (results that are summed are
+// summed afterwards, in index order, by the caller)
+template <class F> void parallel_for(long long n, long long chunk, F fn)
+{
+    const int nt = std::max(1, (int)std::thread::hardware_concurrency());
+    if (nt == 1 || n <= chunk) {
+        for (long long i = 0; i < n; i++) fn(i);
+        return;
+    }
+    std::atomic<long long> next(0);
+    auto work = [&]() {
+        for (;;) {
+            const long long i0 = next.fetch_add(chunk);
+            if (i0 >= n) break;
+            for (long long i = i0; i < std::min(n, i0 + chunk); i++) fn(i);
+        }
+    };
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; t++) th.emplace_back(work);
+    for (auto& t : th) t.join();
+}
+
 
 // ---------------------------------------------------------------------------
 // Second-order forward-mode autodiff scalar with N variables (value, gradient,
